@@ -1,0 +1,371 @@
+"""GB300 CCD + (T) engine for infinite nuclear matter: Python binding of the C ABI.
+
+The engine itself is libccx.so (CUDA, sm_103a) built from csrc/ by build.py; this
+module binds include/ccx.h with ctypes.  Nothing here computes on the CPU: when the
+library or a GPU is missing every call raises CcxError.
+
+Names follow the reference solver (deltafull-CCMkspace): t2_intermediate,
+diis_t1t2, ccd_energy (ccd_energy_save), ccd_iter, pert_triples, and the T2 blocks
+t2_ccm(ch)%val as (n_pp, n_hh) column-major complex arrays.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "build", "libccx.so")
+
+CH_HHHH, CH_HHHP, CH_HHPP, CH_HPHP, CH_HPPP = 1, 2, 3, 4, 5
+CH_PH_PHHP, CH_PH_HPHP, CH_PH_HPPH = 11, 12, 13
+V_PPPP = 6
+POT_MINNESOTA, POT_CHIRAL_LIKE = 0, 1
+MODE_REFERENCE, MODE_STANDARD = 0, 1
+PREC_FP64, PREC_MIXED = 0, 1
+SCALAR_COMPLEX, SCALAR_REAL = 0, 1
+
+
+class CcxError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"ccx error {code}: {msg}")
+        self.code = code
+
+
+class _Deck(C.Structure):
+    _fields_ = [
+        ("chiral_order", C.c_int32), ("lam", C.c_double), ("cE", C.c_double), ("cD", C.c_double),
+        ("A", C.c_int32), ("snm", C.c_int32), ("input_is_kfermi", C.c_int32), ("bc", C.c_char * 16),
+        ("dens_or_kf", C.c_double), ("ntwist", C.c_int32), ("nmax", C.c_int32), ("my_twists", C.c_int32),
+        ("cc_approx", C.c_char * 16), ("tnf_switch", C.c_int32), ("tnf_approx", C.c_int32),
+        ("cutoff_3nf", C.c_double), ("nexp_3nf", C.c_int32),
+        ("potential", C.c_int32), ("lec_seed", C.c_uint64), ("mode", C.c_int32), ("diis_dim", C.c_int32),
+        ("tol", C.c_double), ("max_iter", C.c_int32), ("precision", C.c_int32), ("theta", C.c_double * 3),
+    ]
+
+
+class _BasisParams(C.Structure):
+    _fields_ = [("nmax", C.c_int32), ("A", C.c_int32), ("snm", C.c_int32), ("density", C.c_double),
+                ("theta", C.c_double * 3)]
+
+
+class _Orbits(C.Structure):
+    _fields_ = [("n_states", C.c_int32), ("n_holes", C.c_int32),
+                ("nx", C.POINTER(C.c_int32)), ("ny", C.POINTER(C.c_int32)), ("nz", C.POINTER(C.c_int32)),
+                ("sz", C.POINTER(C.c_int32)), ("tz", C.POINTER(C.c_int32)),
+                ("kx", C.POINTER(C.c_double)), ("ky", C.POINTER(C.c_double)), ("kz", C.POINTER(C.c_double)),
+                ("e", C.POINTER(C.c_double)), ("box_length", C.c_double)]
+
+
+class _EngineOptions(C.Structure):
+    _fields_ = [("device", C.c_int32), ("scalar", C.c_int32)]
+
+
+class _Potential(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("lec_seed", C.c_uint64), ("f32_literals", C.c_int32)]
+
+
+class _IterOpts(C.Structure):
+    _fields_ = [("mode", C.c_int32), ("precision", C.c_int32), ("max_iter", C.c_int32), ("tol", C.c_double),
+                ("diis_dim", C.c_int32), ("defect_period", C.c_int32), ("verbose", C.c_int32)]
+
+
+class _IterResult(C.Structure):
+    _fields_ = [("iterations", C.c_int32), ("converged", C.c_int32), ("e_mbpt2", C.c_double * 2),
+                ("e_ccd", C.c_double * 2), ("res_norm", C.c_double), ("seconds", C.c_double)]
+
+
+_lib = None
+vp = C.c_void_p
+
+
+def lib():
+    """Load libccx.so (raises CcxError if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise CcxError(-1, f"{LIB_PATH} not built; run build.py (or __graft_entry__.build())")
+    L = C.CDLL(LIB_PATH)
+    i32, i64, dbl = C.c_int32, C.c_int64, C.c_double
+    sig = {
+        "ccx_last_error": ([], C.c_char_p),
+        "ccx_deck_parse": ([C.c_char_p, C.POINTER(_Deck)], C.c_int),
+        "ccx_layout_from_basis": ([C.POINTER(_BasisParams), C.POINTER(vp)], C.c_int),
+        "ccx_layout_from_orbits": ([C.POINTER(_Orbits), C.POINTER(vp)], C.c_int),
+        "ccx_layout_destroy": ([vp], C.c_int),
+        "ccx_layout_orbits": ([vp, C.POINTER(_Orbits)], C.c_int),
+        "ccx_layout_counts": ([vp, vp], C.c_int),
+        "ccx_layout_channel": ([vp, i32, i32, vp, C.POINTER(i32), C.POINTER(i32)], C.c_int),
+        "ccx_layout_pairs": ([vp, i32, i32, vp, vp], C.c_int),
+        "ccx_layout_hash": ([vp, C.POINTER(C.c_uint64)], C.c_int),
+        "ccx_engine_create": ([vp, C.POINTER(_EngineOptions), C.POINTER(vp)], C.c_int),
+        "ccx_engine_destroy": ([vp], C.c_int),
+        "ccx_engine_memory": ([vp, C.POINTER(i64)], C.c_int),
+        "ccx_engine_launches": ([vp, C.POINTER(i64)], C.c_int),
+        "ccx_engine_timers": ([vp, vp], C.c_int),
+        "ccx_set_fock": ([vp, vp, vp], C.c_int),
+        "ccx_set_vblock": ([vp, i32, i32, vp], C.c_int),
+        "ccx_generate_interaction": ([vp, C.POINTER(_Potential)], C.c_int),
+        "ccx_get_e0": ([vp, vp], C.c_int),
+        "ccx_setup_t_amplitudes": ([vp], C.c_int),
+        "ccx_set_t2": ([vp, i32, vp], C.c_int),
+        "ccx_get_t2": ([vp, i32, vp], C.c_int),
+        "ccx_get_t2_eqn": ([vp, i32, vp], C.c_int),
+        "ccx_set_t2_all": ([vp, vp], C.c_int),
+        "ccx_get_t2_all": ([vp, vp], C.c_int),
+        "ccx_get_denominators": ([vp, vp, vp], C.c_int),
+        "ccx_t2_intermediate": ([vp], C.c_int),
+        "ccx_diis_setup": ([vp, i32, i32], C.c_int),
+        "ccx_diis_t1t2": ([vp, C.POINTER(i32)], C.c_int),
+        "ccx_ccd_energy": ([vp, vp], C.c_int),
+        "ccx_residual_norm": ([vp, C.POINTER(dbl)], C.c_int),
+        "ccx_ccd_iter": ([vp, C.POINTER(_IterOpts), C.POINTER(_IterResult)], C.c_int),
+        "ccx_pert_triples": ([vp, vp], C.c_int),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = res
+    _lib = L
+    return L
+
+
+def _check(rc: int):
+    if rc != 0:
+        raise CcxError(rc, lib().ccx_last_error().decode(errors="replace"))
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(vp)
+
+
+def _cplx_fortran(a: np.ndarray) -> np.ndarray:
+    """Complex block -> contiguous interleaved doubles in column-major order."""
+    z = np.asarray(a, dtype=np.complex128)
+    return np.ascontiguousarray(z.reshape(-1, order="F")).view(np.float64)
+
+
+def deck_parse(text: str) -> dict:
+    d = _Deck()
+    _check(lib().ccx_deck_parse(text.encode(), C.byref(d)))
+    out = {k: getattr(d, k) for k, _ in _Deck._fields_}
+    out["bc"] = d.bc.decode()
+    out["cc_approx"] = d.cc_approx.decode()
+    out["theta"] = tuple(d.theta)
+    out["lambda"] = out.pop("lam")
+    return out
+
+
+class Layout:
+    """Basis and channel tables with the reference's ordering (host only)."""
+
+    def __init__(self, handle):
+        self._h = handle
+
+    @classmethod
+    def from_basis(cls, nmax: int, A: int, density: float, snm: bool = False, theta=(0.0, 0.0, 0.0)) -> "Layout":
+        p = _BasisParams(nmax, A, int(snm), density, (C.c_double * 3)(*theta))
+        h = vp()
+        _check(lib().ccx_layout_from_basis(C.byref(p), C.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def from_orbits(cls, orb: dict, n_holes: int, box_length: float) -> "Layout":
+        keep = {k: np.ascontiguousarray(orb[k], dtype=np.int32) for k in ("nx", "ny", "nz", "sz", "tz")}
+        keep.update({k: np.ascontiguousarray(orb[k], dtype=np.float64) for k in ("kx", "ky", "kz", "e")})
+        o = _Orbits()
+        o.n_states = len(keep["nx"])
+        o.n_holes = n_holes
+        for k in ("nx", "ny", "nz", "sz", "tz"):
+            setattr(o, k, keep[k].ctypes.data_as(C.POINTER(C.c_int32)))
+        for k in ("kx", "ky", "kz", "e"):
+            setattr(o, k, keep[k].ctypes.data_as(C.POINTER(C.c_double)))
+        o.box_length = box_length
+        h = vp()
+        _check(lib().ccx_layout_from_orbits(C.byref(o), C.byref(h)))
+        return cls(h)
+
+    def close(self):
+        if self._h:
+            lib().ccx_layout_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def orbits(self) -> dict:
+        o = _Orbits()
+        _check(lib().ccx_layout_orbits(self._h, C.byref(o)))
+        n = o.n_states
+        out = {k: np.ctypeslib.as_array(getattr(o, k), shape=(n,)).copy() for k in ("nx", "ny", "nz", "sz", "tz", "kx", "ky", "kz", "e")}
+        out["n_holes"] = o.n_holes
+        out["box_length"] = o.box_length
+        return out
+
+    def counts(self) -> dict:
+        c = np.zeros(8, np.int64)
+        _check(lib().ccx_layout_counts(self._h, _ptr(c)))
+        keys = ("hhpp", "hhhh", "hhhp", "hphp", "ph_phhp", "ph_hphp", "ph_hpph", "amps")
+        return dict(zip(keys, (int(x) for x in c)))
+
+    def channel(self, kind: int, ch: int):
+        q = np.zeros(4, np.int32)
+        n1, n2 = C.c_int32(), C.c_int32()
+        _check(lib().ccx_layout_channel(self._h, kind, ch, _ptr(q), C.byref(n1), C.byref(n2)))
+        return q, n1.value, n2.value
+
+    def pairs(self, kind: int, ch: int):
+        _, n1, n2 = self.channel(kind, ch)
+        a = np.zeros((max(n1, 1), 2), np.int32)
+        b = np.zeros((max(n2, 1), 2), np.int32)
+        _check(lib().ccx_layout_pairs(self._h, kind, ch, _ptr(a), _ptr(b)))
+        return a[:n1], b[:n2]
+
+    def hash(self) -> int:
+        h = C.c_uint64()
+        _check(lib().ccx_layout_hash(self._h, C.byref(h)))
+        return h.value
+
+    def hhpp_dims(self):
+        c = self.counts()["hhpp"]
+        return [self.channel(CH_HHPP, i)[1:] for i in range(c)]
+
+
+class Engine:
+    """One CCD problem resident on one GPU."""
+
+    def __init__(self, layout: Layout, device: int = 0, real: bool = True):
+        self.layout = layout
+        self.real = real
+        o = _EngineOptions(device, SCALAR_REAL if real else SCALAR_COMPLEX)
+        h = vp()
+        _check(lib().ccx_engine_create(layout._h, C.byref(o), C.byref(h)))
+        self._h = h
+        self._dims = layout.hhpp_dims()  # (n_hh, n_pp) per hhpp channel
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().ccx_engine_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---- interaction ------------------------------------------------------
+    def generate(self, potential: int = POT_MINNESOTA, lec_seed: int = 20261203, f32_literals: bool = True):
+        p = _Potential(potential, lec_seed, int(f32_literals))
+        _check(lib().ccx_generate_interaction(self._h, C.byref(p)))
+
+    def set_fock(self, fock: np.ndarray, e0: complex = 0.0):
+        f = _cplx_fortran(fock)
+        z = np.array([complex(e0).real, complex(e0).imag])
+        _check(lib().ccx_set_fock(self._h, _ptr(f), _ptr(z)))
+
+    def set_vblock(self, kind: int, ch: int, block: np.ndarray):
+        b = _cplx_fortran(block)
+        _check(lib().ccx_set_vblock(self._h, kind, ch, _ptr(b)))
+
+    def e0(self) -> complex:
+        z = np.zeros(2)
+        _check(lib().ccx_get_e0(self._h, _ptr(z)))
+        return complex(z[0], z[1])
+
+    # ---- amplitudes ---------------------------------------------------------
+    def setup_t_amplitudes(self):
+        _check(lib().ccx_setup_t_amplitudes(self._h))
+
+    def _get(self, fn, ch):
+        nh, npp = self._dims[ch]
+        z = np.zeros(2 * nh * npp)
+        _check(fn(self._h, ch, _ptr(z)))
+        return z.view(np.complex128).reshape(npp, nh, order="F")
+
+    def t2(self, ch: int) -> np.ndarray:
+        return self._get(lib().ccx_get_t2, ch)
+
+    def t2_eqn(self, ch: int) -> np.ndarray:
+        return self._get(lib().ccx_get_t2_eqn, ch)
+
+    def set_t2(self, ch: int, t: np.ndarray):
+        z = _cplx_fortran(t)
+        _check(lib().ccx_set_t2(self._h, ch, _ptr(z)))
+
+    def t2_all(self) -> np.ndarray:
+        n = self.layout.counts()["amps"]
+        z = np.zeros(2 * n)
+        _check(lib().ccx_get_t2_all(self._h, _ptr(z)))
+        return z.view(np.complex128)
+
+    def set_t2_all(self, flat: np.ndarray):
+        z = np.ascontiguousarray(np.asarray(flat, np.complex128)).view(np.float64)
+        _check(lib().ccx_set_t2_all(self._h, _ptr(z)))
+
+    def denominators(self):
+        orb = self.layout.orbits()
+        A = orb["n_holes"]
+        n = len(orb["nx"])
+        a = np.zeros(2 * A)
+        b = np.zeros(2 * (n - A))
+        _check(lib().ccx_get_denominators(self._h, _ptr(a), _ptr(b)))
+        return a.view(np.complex128), b.view(np.complex128)
+
+    # ---- hot path -------------------------------------------------------------
+    def t2_intermediate(self):
+        _check(lib().ccx_t2_intermediate(self._h))
+
+    def diis_setup(self, subspace: int = 6, step: int = 6):
+        _check(lib().ccx_diis_setup(self._h, subspace, step))
+
+    def diis_t1t2(self, count: int) -> int:
+        c = C.c_int32(count)
+        _check(lib().ccx_diis_t1t2(self._h, C.byref(c)))
+        return c.value
+
+    def ccd_energy(self) -> complex:
+        z = np.zeros(2)
+        _check(lib().ccx_ccd_energy(self._h, _ptr(z)))
+        return complex(z[0], z[1])
+
+    def residual_norm(self) -> float:
+        x = C.c_double()
+        _check(lib().ccx_residual_norm(self._h, C.byref(x)))
+        return x.value
+
+    def ccd_iter(self, mode=MODE_REFERENCE, precision=PREC_FP64, max_iter=100, tol=1e-6, diis_dim=8,
+                 defect_period=4, verbose=False) -> dict:
+        o = _IterOpts(mode, precision, max_iter, tol, diis_dim, defect_period, int(verbose))
+        r = _IterResult()
+        _check(lib().ccx_ccd_iter(self._h, C.byref(o), C.byref(r)))
+        return {"iterations": r.iterations, "converged": bool(r.converged),
+                "e_mbpt2": complex(r.e_mbpt2[0], r.e_mbpt2[1]), "e_ccd": complex(r.e_ccd[0], r.e_ccd[1]),
+                "res_norm": r.res_norm, "seconds": r.seconds}
+
+    def pert_triples(self) -> complex:
+        z = np.zeros(2)
+        _check(lib().ccx_pert_triples(self._h, _ptr(z)))
+        return complex(z[0], z[1])
+
+    # ---- diagnostics ----------------------------------------------------------
+    def memory(self) -> int:
+        x = C.c_int64()
+        _check(lib().ccx_engine_memory(self._h, C.byref(x)))
+        return x.value
+
+    def launches(self) -> int:
+        x = C.c_int64()
+        _check(lib().ccx_engine_launches(self._h, C.byref(x)))
+        return x.value
+
+    def timers(self) -> dict:
+        z = np.zeros(10)
+        _check(lib().ccx_engine_timers(self._h, _ptr(z)))
+        keys = ("tph_gather", "i9_i7", "i6", "i4", "ring", "r_init", "ladders", "update", "diis", "total")
+        return dict(zip(keys, z.tolist()))

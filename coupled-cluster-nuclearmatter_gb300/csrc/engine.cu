@@ -1,0 +1,934 @@
+// CCD engine: device image of the layout and the iteration driver
+// (ccd_iter, ccm_iter.f90:1-133, with t2_intermediate, diis_t1t2 and
+// ccd_energy_save as its per-iteration steps).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "common.cuh"
+#include "devlayout.hpp"
+#include "engine.hpp"
+#include "kernels.hpp"
+#include "triples.hpp"
+
+namespace ccx {
+
+namespace {
+
+void ck(cudaError_t e, const char *what) {
+  if (e != cudaSuccess) throw EngineError(2, std::string(what) + ": " + cudaGetErrorString(e));
+}
+#define CK(x) ck((x), #x)
+
+// RAII device buffer
+struct DBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+  DBuf() = default;
+  DBuf(const DBuf &) = delete;
+  DBuf &operator=(const DBuf &) = delete;
+  ~DBuf() { if (p) cudaFree(p); }
+  void alloc(size_t b, int64_t *counter) {
+    if (p) { cudaFree(p); if (counter) *counter -= (int64_t)bytes; p = nullptr; }
+    bytes = b;
+    if (b == 0) return;
+    cudaError_t e = cudaMalloc(&p, b);
+    if (e != cudaSuccess) {
+      p = nullptr;
+      throw EngineError(3, std::string("cudaMalloc of ") + std::to_string(b) + " bytes: " + cudaGetErrorString(e));
+    }
+    if (counter) *counter += (int64_t)b;
+  }
+  template <typename T> T *as() const { return (T *)p; }
+};
+
+template <typename T>
+void upload(DBuf &d, const std::vector<T> &h, int64_t *counter) {
+  d.alloc(std::max<size_t>(h.size(), 1) * sizeof(T), counter);
+  if (!h.empty()) CK(cudaMemcpy(d.p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice));
+}
+
+uint64_t splitmix(uint64_t &st) {
+  uint64_t z = (st += 0x9e3779b97f4a7c15ULL);
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
+  return z ^ (z >> 31);
+}
+
+// complex LU solve with partial pivoting on |re|+|im| (the pivot rule of ZGESV)
+bool zsolve(int n, std::vector<std::complex<double>> &a, std::vector<std::complex<double>> &b) {
+  std::vector<int> piv(n);
+  for (int k = 0; k < n; ++k) {
+    int p = k;
+    double best = -1.0;
+    for (int i = k; i < n; ++i) {
+      const auto v = a[i + n * k];
+      const double m = std::fabs(v.real()) + std::fabs(v.imag());
+      if (m > best) { best = m; p = i; }
+    }
+    piv[k] = p;
+    if (best == 0.0) return false;
+    if (p != k)
+      for (int j = 0; j < n; ++j) std::swap(a[k + n * j], a[p + n * j]);
+    for (int i = k + 1; i < n; ++i) {
+      a[i + n * k] /= a[k + n * k];
+      for (int j = k + 1; j < n; ++j) a[i + n * j] -= a[i + n * k] * a[k + n * j];
+    }
+  }
+  for (int k = 0; k < n; ++k)
+    if (piv[k] != k) std::swap(b[k], b[piv[k]]);
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < i; ++j) b[i] -= a[i + n * j] * b[j];
+  for (int i = n - 1; i >= 0; --i) {
+    for (int j = i + 1; j < n; ++j) b[i] -= a[i + n * j] * b[j];
+    b[i] /= a[i + n * i];
+  }
+  return true;
+}
+
+bool dsolve(int n, std::vector<double> a, std::vector<double> &b) {
+  for (int k = 0; k < n; ++k) {
+    int p = k;
+    for (int i = k + 1; i < n; ++i)
+      if (std::fabs(a[i + n * k]) > std::fabs(a[p + n * k])) p = i;
+    if (a[p + n * k] == 0.0) return false;
+    if (p != k) {
+      for (int j = 0; j < n; ++j) std::swap(a[k + n * j], a[p + n * j]);
+      std::swap(b[k], b[p]);
+    }
+    for (int i = k + 1; i < n; ++i) {
+      const double f = a[i + n * k] / a[k + n * k];
+      for (int j = k; j < n; ++j) a[i + n * j] -= f * a[k + n * j];
+      b[i] -= f * b[k];
+    }
+  }
+  for (int i = n - 1; i >= 0; --i) {
+    for (int j = i + 1; j < n; ++j) b[i] -= a[i + n * j] * b[j];
+    b[i] /= a[i + n * i];
+  }
+  return true;
+}
+
+}  // namespace
+
+void draw_lecs(uint64_t seed, double out[9]) {
+  // centres: CS, CT in 10^4 GeV^-2, C1..C7 in 10^4 GeV^-4, each drawn uniformly in +/-50%
+  // from a splitmix64 stream; units converted to MeV (x1e-2, x1e-8) as the reference does
+  // (chiral_module_andreas_with_delta.f90:586-596) and divided by 16 pi, the normalisation
+  // of its operator LECs (CS = (c1s0+3 c3s1)/16/pi, :599-600; cnlo, :604-614)
+  const double centre[9] = {-0.1, 0.01, 0.1, 0.1, 0.1, 0.1, 0.1, 0.1, 0.1};
+  const double pi = 3.14159265358979;
+  uint64_t st = seed;
+  for (int i = 0; i < 9; ++i) {
+    const double u = (double)(splitmix(st) >> 11) * 0x1.0p-53;
+    out[i] = centre[i] * (0.5 + u) * (i < 2 ? 1.0e-2 : 1.0e-8) / (16.0 * pi);
+  }
+}
+
+template <typename S>
+class Engine final : public IEngine {
+ public:
+  Engine(std::shared_ptr<const Layout> L, int device) : L_(std::move(L)) {
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) throw EngineError(6, "no CUDA device available");
+    if (device < 0 || device >= ndev) throw EngineError(1, "device ordinal out of range");
+    device_ = device;
+    CK(cudaSetDevice(device_));
+    CK(cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking));
+    for (auto &e : ev_) CK(cudaEventCreate(&e));
+    build_tables();
+    alloc_state();
+  }
+  ~Engine() override {
+    cudaSetDevice(device_);
+    if (st_) cudaStreamSynchronize(st_);
+    for (auto &e : ev_) if (e) cudaEventDestroy(e);
+    if (st_) cudaStreamDestroy(st_);
+    if (host_res_) cudaFreeHost(host_res_);
+  }
+
+  bool is_complex() const override { return ScalarOf<S>::complex; }
+  int64_t device_bytes() const override { return bytes_; }
+  int64_t launches() const override { return launches_; }
+  void timers(double ms[10]) const override { for (int i = 0; i < 10; ++i) ms[i] = timers_[i]; }
+
+  // ---------------------------------------------------------------- interaction
+  void set_fock(const double *fock, const double e0[2]) override {
+    const Layout &L = *L_;
+    const int ns = L.b.ns, A = L.b.A;
+    std::vector<S> fd(ns), f6(std::max(ns - A, 1)), f7(std::max(A, 1));
+    auto F = [&](int p, int q) {
+      const size_t o = 2 * ((size_t)p + (size_t)ns * q);
+      return check_real(fock[o], fock[o + 1]);
+    };
+    for (int p = 0; p < ns; ++p) {
+      fd[p] = F(p, p);
+      const int pb = partner_[p];
+      if (p >= A) f6[p - A] = (pb >= A) ? F(p, pb) : S(0.0);
+      else f7[p] = (pb >= 0 && pb < A) ? F(pb, p) : S(0.0);
+    }
+    CK(cudaMemcpy(fdiag_.p, fd.data(), ns * sizeof(S), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(f6_.p, f6.data(), f6.size() * sizeof(S), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(f7_.p, f7.data(), f7.size() * sizeof(S), cudaMemcpyHostToDevice));
+    e0_[0] = e0 ? e0[0] : 0.0;
+    e0_[1] = e0 ? e0[1] : 0.0;
+    have_fock_ = true;
+  }
+
+  void set_vblock(int kind, int ch, const double *v) override {
+    const Layout &L = *L_;
+    if (!v) throw EngineError(1, "null V block");
+    int rows = 0;
+    int64_t elems = 0;
+    int target = -1;
+    switch (kind) {
+      case 3:
+        check_ch(ch, L.fam[3].count());
+        rows = L.pk[ch].n_hh;
+        elems = (int64_t)rows * L.pk[ch].n_pp;
+        target = ch;
+        break;
+      case 6:
+        check_ch(ch, L.fam[3].count());
+        rows = L.pk[ch].n_pp;
+        elems = (int64_t)rows * rows;
+        target = ch;
+        break;
+      case 1: {
+        check_ch(ch, L.fam[1].count());
+        rows = L.fam[1].side1[ch].size();
+        elems = (int64_t)rows * rows;
+        target = hhhh_to_hhpp_[ch];
+        break;
+      }
+      case 4: {
+        check_ch(ch, L.fam[4].count());
+        const int n = L.fam[4].side1[ch].size();
+        CK(cudaMemcpyAsync(v4_.as<double>() + 2 * v4_off_h_[ch], v, (size_t)n * n * 2 * sizeof(double),
+                           cudaMemcpyHostToDevice, st_));
+        dirty_ = true;
+        return;
+      }
+      case 2:
+        check_ch(ch, L.fam[2].count());
+        if (!tr_) tr_ = make_triples<S>(*L_, D_, O_, device_);
+        tr_->set_hhhp(ch, v, st_);
+        return;
+      case 5:
+        check_ch(ch, L.fam[5].count());
+        if (!tr_) tr_ = make_triples<S>(*L_, D_, O_, device_);
+        tr_->set_hppp(ch, v, st_);
+        return;
+      default:
+        throw EngineError(1, "unknown V block kind");
+    }
+    if (target < 0) return;  // an hhhh channel without an hhpp partner is not used by CCD
+    CK(cudaMemcpyAsync(stage_.p, v, (size_t)elems * 2 * sizeof(double), cudaMemcpyHostToDevice, st_));
+    S *dst = kind == 3 ? Vhp_.as<S>() : kind == 6 ? Vpp_.as<S>() : Vhh_.as<S>();
+    launch_pack_vblock<S>(D_, kind, target, rows, stage_.as<double>(), dst, flag_.as<int>(), st_);
+    ++launches_;
+    check_flag("V block has a non-zero imaginary part but the engine is real");
+    dirty_ = true;
+  }
+
+  void generate(const PotentialSpec &p) override {
+    if (!ScalarOf<S>::complex && p.kind != 0) throw EngineError(1, "the chiral-like potential needs a complex engine");
+    DevPotential pot{};
+    pot.kind = p.kind;
+    pot.f32_literals = p.f32_literals;
+    draw_lecs(p.lec_seed, pot.lec);
+    launch_generate<S>(D_, O_, pot, Vhp_.as<S>(), Vpp_.as<S>(), Vhh_.as<S>(), W_.as<S>(), fdiag_.as<S>(), f6_.as<S>(),
+                       f7_.as<S>(), res_.as<double>(), st_);
+    launches_ += 6;
+    CK(cudaMemcpyAsync(host_res_, res_.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, st_));
+    CK(cudaStreamSynchronize(st_));
+    e0_[0] = host_res_[0];
+    e0_[1] = host_res_[1];
+    have_fock_ = true;
+    generated_ = true;
+    pot_ = pot;
+    dirty_ = true;
+    vph_ready_ = false;
+    commit();
+  }
+  void get_e0(double e0[2]) override { e0[0] = e0_[0]; e0[1] = e0_[1]; }
+
+  // ---------------------------------------------------------------- amplitudes
+  void mp2() override {
+    commit();
+    launch_mp2<S>(D_, Vhp_.as<S>(), fdiag_.as<S>(), T_.as<S>(), st_);
+    ++launches_;
+    have_t_ = true;
+    CK(cudaStreamSynchronize(st_));
+  }
+  void set_t2(int ch, const double *t) override {
+    const Layout &L = *L_;
+    check_ch(ch, L.fam[3].count());
+    const auto &P = L.pk[ch];
+    CK(cudaMemcpyAsync(stage_.p, t, (size_t)P.n_pp * P.n_hh * 2 * sizeof(double), cudaMemcpyHostToDevice, st_));
+    launch_pack_t<S>(D_, ch, P.n_pp, stage_.as<double>(), T_.as<S>(), flag_.as<int>(), st_);
+    ++launches_;
+    check_flag("T2 has a non-zero imaginary part but the engine is real");
+    have_t_ = true;
+  }
+  void get_block(int ch, const S *src, double *out) {
+    const Layout &L = *L_;
+    check_ch(ch, L.fam[3].count());
+    const auto &P = L.pk[ch];
+    launch_unpack_t<S>(D_, ch, P.n_pp, pp_sgn_.as<int>() + ppsgn_off_[ch], hh_sgn_.as<int>() + hhsgn_off_[ch], P.n_hh,
+                       src, stage_.as<double>(), st_);
+    ++launches_;
+    CK(cudaMemcpyAsync(out, stage_.p, (size_t)P.n_pp * P.n_hh * 2 * sizeof(double), cudaMemcpyDeviceToHost, st_));
+    CK(cudaStreamSynchronize(st_));
+  }
+  void get_t2(int ch, double *t) override { get_block(ch, T_.as<S>(), t); }
+  void get_r2(int ch, double *r) override { get_block(ch, R_.as<S>(), r); }
+  void set_t2_all(const double *t) override {
+    const Layout &L = *L_;
+    for (int c = 0; c < L.fam[3].count(); ++c) set_t2(c, t + 2 * L.pk[c].amp_off);
+  }
+  void get_t2_all(double *t) override {
+    const Layout &L = *L_;
+    for (int c = 0; c < L.fam[3].count(); ++c) get_t2(c, t + 2 * L.pk[c].amp_off);
+  }
+  void get_denominators(double *d2ij, double *d2ab) override {
+    const Layout &L = *L_;
+    const int A = L.b.A, NP = L.b.ns - A;
+    std::vector<S> a(A), b(NP);
+    CK(cudaStreamSynchronize(st_));
+    CK(cudaMemcpy(a.data(), d2ij_.p, A * sizeof(S), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(b.data(), d2ab_.p, NP * sizeof(S), cudaMemcpyDeviceToHost));
+    for (int i = 0; i < A; ++i) { d2ij[2 * i] = real_(a[i]); d2ij[2 * i + 1] = imag_(a[i]); }
+    for (int i = 0; i < NP; ++i) { d2ab[2 * i] = real_(b[i]); d2ab[2 * i + 1] = imag_(b[i]); }
+  }
+
+  // ---------------------------------------------------------------- hot path
+  void t2_intermediate() override {
+    require_ready();
+    residual(false);
+    CK(cudaStreamSynchronize(st_));
+  }
+  void diis_setup(int subspace, int step) override {
+    if (subspace < 2 || subspace > 6 || step < 1) throw EngineError(1, "diis subspace must be 2..6, step >= 1");
+    subspace_ = subspace;
+    diis_step_ = step;
+    nstep_ = 0;
+    hist_.alloc((size_t)(subspace + 1) * n_t_ * sizeof(S), &bytes_);
+    phys_.resize(subspace + 1);
+    for (int i = 0; i <= subspace; ++i) phys_[i] = i;
+  }
+  void diis_t1t2(int *count) override {
+    if (subspace_ == 0) diis_setup(6, 6);
+    ++nstep_;
+    reference_update(*count);
+    if (*count == diis_step_) *count = 0;
+    CK(cudaStreamSynchronize(st_));
+  }
+  void energy(double e[2]) override {
+    require_ready();
+    launch_update<S>(D_, 2, T_.as<S>(), R_.as<S>(), Vhp_.as<S>(), d2ij_.as<S>(), d2ab_.as<S>(), nullptr, nullptr,
+                     partial_.as<double>(), res_.as<double>(), st_);
+    launches_ += 2;
+    fetch_res(3);
+    e[0] = host_res_[0];
+    e[1] = host_res_[1];
+  }
+  double residual_norm() override {
+    launch_update<S>(D_, 3, T_.as<S>(), R_.as<S>(), Vhp_.as<S>(), d2ij_.as<S>(), d2ab_.as<S>(), nullptr, nullptr,
+                     partial_.as<double>(), res_.as<double>(), st_);
+    launches_ += 2;
+    fetch_res(3);
+    return 2.0 * std::sqrt(host_res_[2]);
+  }
+
+  void ccd_iter(const IterOpts &o, IterResult &r) override {
+    require_ready();
+    if (o.precision != 0) throw EngineError(1, "mixed precision is not available in this build of the engine");
+    r = IterResult();
+    double e[2];
+    energy(e);
+    r.e_mbpt2[0] = e[0];
+    r.e_mbpt2[1] = e[1];
+    for (double &t : timers_) t = 0.0;
+    timing_ = true;
+    CK(cudaEventRecord(ev_[10], st_));
+    if (o.mode == 0) iterate_reference(o, r);
+    else iterate_standard(o, r);
+    CK(cudaEventRecord(ev_[11], st_));
+    CK(cudaEventSynchronize(ev_[11]));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, ev_[10], ev_[11]));
+    r.seconds = ms * 1e-3;
+    timers_[9] = ms;
+    timing_ = false;
+  }
+
+  void triples(double et[2]) override {
+    require_ready();
+    if (!tr_) tr_ = make_triples<S>(*L_, D_, O_, device_);
+    if (!tr_->has_v()) {
+      if (!generated_) throw EngineError(4, "(T) needs V_hhhp and V_hppp: set every HHHP and HPPP block, or generate the interaction");
+      tr_->generate_v(pot_, st_);
+    }
+    tr_->energy(T_.as<S>(), fdiag_.as<S>(), et, st_);
+    launches_ += tr_->launches();
+  }
+
+ private:
+  // ================================================================== setup
+  void check_ch(int ch, int n) const {
+    if (ch < 0 || ch >= n) throw EngineError(1, "channel index out of range");
+  }
+  S check_real(double re, double im) {
+    if (!ScalarOf<S>::complex && im != 0.0) throw EngineError(1, "complex input given to a real engine");
+    return make_scalar<S>(re, im);
+  }
+  void check_flag(const char *msg) {
+    int f = 0;
+    CK(cudaMemcpyAsync(&host_flag_, flag_.p, sizeof(int), cudaMemcpyDeviceToHost, st_));
+    CK(cudaStreamSynchronize(st_));
+    f = host_flag_;
+    if (f) {
+      CK(cudaMemsetAsync(flag_.p, 0, sizeof(int), st_));
+      throw EngineError(1, msg);
+    }
+  }
+  void require_ready() {
+    if (!have_fock_) throw EngineError(4, "no Fock matrix / interaction set");
+    if (!have_t_) throw EngineError(4, "no T2 amplitudes (call setup_t_amplitudes or set_t2)");
+    commit();
+  }
+  void commit() {
+    if (!dirty_ && vph_ready_) return;
+    launch_build_vph<S>(D_, Vhp_.as<S>(), Vph_.as<S>(), st_);
+    ++launches_;
+    if (!generated_) {
+      launch_build_w<S>(D_, hp4_slot_.as<int2>(), v4_off_.as<int64_t>(), n4_.as<int>(), v4_.as<double>(), W_.as<S>(),
+                        flag_.as<int>(), st_);
+      ++launches_;
+      check_flag("V_hphp has a non-zero imaginary part but the engine is real");
+    }
+    dirty_ = false;
+    vph_ready_ = true;
+  }
+
+  void build_tables() {
+    const Layout &L = *L_;
+    const int ns = L.b.ns, A = L.b.A, NP = ns - A;
+    const int nc = L.fam[3].count();
+    std::vector<int> P(nc), H(nc), pp_off(nc), hh_off(nc);
+    std::vector<int64_t> t_off(nc), vpp_off(nc), hh2_off(nc);
+    std::vector<int2> pp_orb, hh_orb, ttile, vtile;
+    std::vector<int> pp_row, hh_row, pp_sgn, hh_sgn;
+    int64_t vacc = 0, hacc = 0;
+    hhhh_to_hhpp_.assign(L.fam[1].count(), -1);
+    for (int c = 0; c < nc; ++c) {
+      const PackedChannel &pk = L.pk[c];
+      P[c] = pk.P;
+      H[c] = pk.H;
+      t_off[c] = pk.t_off;
+      vpp_off[c] = vacc;
+      hh2_off[c] = hacc;
+      vacc += (int64_t)pk.P * pk.P;
+      hacc += (int64_t)pk.H * pk.H;
+      pp_off[c] = (int)pp_orb.size();
+      hh_off[c] = (int)hh_orb.size();
+      const PairList &pl = L.fam[3].side2[c], &hl = L.fam[3].side1[c];
+      for (int r : pk.pp_of_packed) { pp_orb.push_back(make_int2(pl.p[r], pl.q[r])); pp_row.push_back(r); }
+      for (int r : pk.hh_of_packed) { hh_orb.push_back(make_int2(hl.p[r], hl.q[r])); hh_row.push_back(r); }
+      ppsgn_off_.push_back((int64_t)pp_sgn.size());
+      hhsgn_off_.push_back((int64_t)hh_sgn.size());
+      pp_sgn.insert(pp_sgn.end(), pk.pp_packed.begin(), pk.pp_packed.end());
+      hh_sgn.insert(hh_sgn.end(), pk.hh_packed.begin(), pk.hh_packed.end());
+      for (int64_t s = 0; s < (int64_t)pk.P * pk.H; s += kTileElems) ttile.push_back(make_int2(c, (int)s));
+      for (int64_t s = 0; s < (int64_t)pk.P * pk.P; s += kTileElems) vtile.push_back(make_int2(c, (int)s));
+      if (pk.hhhh >= 0) hhhh_to_hhpp_[pk.hhhh] = c;
+      max_stage_ = std::max<int64_t>(max_stage_, (int64_t)pk.n_pp * std::max(pk.n_pp, pk.n_hh));
+    }
+    n_t_ = L.n_tpacked;
+    n_vpp_ = vacc;
+    n_hh2_ = hacc;
+    // slots
+    std::vector<int2> pp_slot((size_t)NP * NP, make_int2(-1, 0)), hh_slot((size_t)A * A, make_int2(-1, 0));
+    for (int a = A; a < ns; ++a)
+      for (int b = A; b < ns; ++b) {
+        const int pos = L.pp_hhpp[(size_t)a * ns + b];
+        if (!pos) continue;
+        const int c = L.chan3_of_pair(a, b);
+        pp_slot[(size_t)(a - A) * NP + (b - A)] = make_int2(c, L.pk[c].pp_packed[pos - 1]);
+      }
+    for (int i = 0; i < A; ++i)
+      for (int j = 0; j < A; ++j) {
+        const int pos = L.hh_hhpp[(size_t)i * ns + j];
+        if (!pos) continue;
+        const int c = L.chan3_of_pair(i, j);
+        hh_slot[(size_t)i * A + j] = make_int2(c, L.pk[c].hh_packed[pos - 1]);
+      }
+    partner_.assign(ns, -1);
+    for (int p = 0; p < ns; ++p) partner_[p] = L.b.orbitof(L.b.nx[p], L.b.ny[p], L.b.nz[p], -L.b.sz[p], L.b.tz[p]);
+    // ring channels
+    const int nq = L.ph[1].count();
+    std::vector<int> nph(nq), nhp(nq), ph_off(nq), hp_off(nq);
+    std::vector<int64_t> tph_off(nq), i4_off(nq), vph_off(nq);
+    std::vector<int2> ph_orb, hp_orb, phtile;
+    int64_t tacc = 0, iacc = 0;
+    for (int q = 0; q < nq; ++q) {
+      const PairList &s1 = L.ph[1].side1[q], &s2 = L.ph[1].side2[q];
+      nph[q] = s1.size();
+      nhp[q] = s2.size();
+      tph_off[q] = tacc;
+      vph_off[q] = tacc;
+      i4_off[q] = iacc;
+      tacc += (int64_t)nph[q] * nhp[q];
+      iacc += (int64_t)nhp[q] * nhp[q];
+      ph_off[q] = (int)ph_orb.size();
+      hp_off[q] = (int)hp_orb.size();
+      for (int r = 0; r < s1.size(); ++r) ph_orb.push_back(make_int2(s1.p[r], s1.q[r]));
+      for (int r = 0; r < s2.size(); ++r) hp_orb.push_back(make_int2(s2.p[r], s2.q[r]));
+      for (int64_t s = 0; s < (int64_t)nph[q] * nhp[q]; s += kTileElems) phtile.push_back(make_int2(q, (int)s));
+    }
+    n_ph_ = tacc;
+    n_i4_ = iacc;
+    std::vector<int2> ph_slot((size_t)NP * A, make_int2(-1, 0)), hp_slot((size_t)A * NP, make_int2(-1, 0));
+    for (int a = A; a < ns; ++a)
+      for (int i = 0; i < A; ++i) {
+        const int pos = L.ph_ph_phhp[(size_t)a * ns + i];
+        if (!pos) continue;
+        const int q = L.phgrid[1].get((L.b.tz[a] - L.b.tz[i]) / 2, L.b.nx[a] - L.b.nx[i], L.b.ny[a] - L.b.ny[i],
+                                      L.b.nz[a] - L.b.nz[i]) - 1;
+        ph_slot[(size_t)(a - A) * A + i] = make_int2(q, pos - 1);
+      }
+    for (int j = 0; j < A; ++j)
+      for (int b = A; b < ns; ++b) {
+        const int pos = L.hp_ph_phhp[(size_t)j * ns + b];
+        if (!pos) continue;
+        const int q = L.phgrid[1].get((L.b.tz[j] - L.b.tz[b]) / 2, L.b.nx[j] - L.b.nx[b], L.b.ny[j] - L.b.ny[b],
+                                      L.b.nz[j] - L.b.nz[b]) - 1;
+        hp_slot[(size_t)j * NP + (b - A)] = make_int2(q, pos - 1);
+      }
+    // kind-4 (hphp pair-sum) blocks for W
+    const int n4c = L.fam[4].count();
+    std::vector<int> n4(std::max(n4c, 1));
+    std::vector<int2> hp4_slot((size_t)A * NP, make_int2(-1, 0));
+    int64_t v4acc = 0;
+    v4_off_h_.resize(std::max(n4c, 1));
+    for (int c = 0; c < n4c; ++c) {
+      n4[c] = L.fam[4].side1[c].size();
+      v4_off_h_[c] = v4acc;
+      v4acc += (int64_t)n4[c] * n4[c];
+      const PairList &pl = L.fam[4].side1[c];
+      for (int r = 0; r < pl.size(); ++r) hp4_slot[(size_t)pl.p[r] * NP + (pl.q[r] - A)] = make_int2(c, r);
+    }
+    // uploads
+    upload(dP_, P, &bytes_); upload(dH_, H, &bytes_);
+    upload(dt_off_, t_off, &bytes_); upload(dvpp_off_, vpp_off, &bytes_); upload(dhh2_off_, hh2_off, &bytes_);
+    upload(dpp_off_, pp_off, &bytes_); upload(dhh_off_, hh_off, &bytes_);
+    upload(dpp_orb_, pp_orb, &bytes_); upload(dhh_orb_, hh_orb, &bytes_);
+    upload(dpp_row_, pp_row, &bytes_); upload(dhh_row_, hh_row, &bytes_);
+    upload(dpp_slot_, pp_slot, &bytes_); upload(dhh_slot_, hh_slot, &bytes_);
+    upload(dpartner_, partner_, &bytes_);
+    upload(dn_ph_, nph, &bytes_); upload(dn_hp_, nhp, &bytes_);
+    upload(dtph_off_, tph_off, &bytes_); upload(di4_off_, i4_off, &bytes_); upload(dvph_off_, vph_off, &bytes_);
+    upload(dph_off_, ph_off, &bytes_); upload(dhp_off_, hp_off, &bytes_);
+    upload(dph_orb_, ph_orb, &bytes_); upload(dhp_orb_, hp_orb, &bytes_);
+    upload(dph_slot_, ph_slot, &bytes_); upload(dhp_slot_, hp_slot, &bytes_);
+    upload(dttile_, ttile, &bytes_); upload(dphtile_, phtile, &bytes_); upload(dvtile_, vtile, &bytes_);
+    upload(pp_sgn_, pp_sgn, &bytes_); upload(hh_sgn_, hh_sgn, &bytes_);
+    upload(n4_, n4, &bytes_); upload(hp4_slot_, hp4_slot, &bytes_);
+    std::vector<int64_t> v4off(v4_off_h_.begin(), v4_off_h_.end());
+    upload(v4_off_, v4off, &bytes_);
+    v4_.alloc((size_t)std::max<int64_t>(v4acc, 1) * 2 * sizeof(double), &bytes_);
+    CK(cudaMemset(v4_.p, 0, v4_.bytes));
+    // orbits
+    upload(onx_, L.b.nx, &bytes_); upload(ony_, L.b.ny, &bytes_); upload(onz_, L.b.nz, &bytes_);
+    upload(osz_, L.b.sz, &bytes_); upload(otz_, L.b.tz, &bytes_);
+    upload(okx_, L.b.kx, &bytes_); upload(oky_, L.b.ky, &bytes_); upload(okz_, L.b.kz, &bytes_);
+    upload(oe_, L.b.e, &bytes_);
+    O_.ns = ns;
+    O_.nx = onx_.as<int>(); O_.ny = ony_.as<int>(); O_.nz = onz_.as<int>();
+    O_.sz = osz_.as<int>(); O_.tz = otz_.as<int>();
+    O_.kx = okx_.as<double>(); O_.ky = oky_.as<double>(); O_.kz = okz_.as<double>(); O_.e = oe_.as<double>();
+    O_.volume = L.b.L * L.b.L * L.b.L;
+
+    DevLayout &D = D_;
+    D.ns = ns; D.A = A; D.NP = NP; D.nch = nc;
+    D.P = dP_.as<int>(); D.H = dH_.as<int>();
+    D.t_off = dt_off_.as<int64_t>(); D.vpp_off = dvpp_off_.as<int64_t>(); D.hh2_off = dhh2_off_.as<int64_t>();
+    D.pp_off = dpp_off_.as<int>(); D.hh_off = dhh_off_.as<int>();
+    D.pp_orb = dpp_orb_.as<int2>(); D.hh_orb = dhh_orb_.as<int2>();
+    D.pp_row = dpp_row_.as<int>(); D.hh_row = dhh_row_.as<int>();
+    D.pp_slot = dpp_slot_.as<int2>(); D.hh_slot = dhh_slot_.as<int2>();
+    D.partner = dpartner_.as<int>();
+    D.nph = nq;
+    D.n_ph = dn_ph_.as<int>(); D.n_hp = dn_hp_.as<int>();
+    D.tph_off = dtph_off_.as<int64_t>(); D.i4_off = di4_off_.as<int64_t>(); D.vph_off = dvph_off_.as<int64_t>();
+    D.ph_off = dph_off_.as<int>(); D.hp_off = dhp_off_.as<int>();
+    D.ph_orb = dph_orb_.as<int2>(); D.hp_orb = dhp_orb_.as<int2>();
+    D.ph_slot = dph_slot_.as<int2>(); D.hp_slot = dhp_slot_.as<int2>();
+    D.ttile = dttile_.as<int2>(); D.nttile = (int)ttile.size();
+    D.phtile = dphtile_.as<int2>(); D.nphtile = (int)phtile.size();
+    D.vtile = dvtile_.as<int2>(); D.nvtile = (int)vtile.size();
+    n_ttile_ = D.nttile;
+  }
+
+  void alloc_state() {
+    const Layout &L = *L_;
+    const int ns = L.b.ns, A = L.b.A, NP = ns - A;
+    const size_t s = sizeof(S);
+    T_.alloc(std::max<int64_t>(n_t_, 1) * s, &bytes_);
+    R_.alloc(std::max<int64_t>(n_t_, 1) * s, &bytes_);
+    Vhp_.alloc(std::max<int64_t>(n_t_, 1) * s, &bytes_);
+    Vpp_.alloc(std::max<int64_t>(n_vpp_, 1) * s, &bytes_);
+    Vhh_.alloc(std::max<int64_t>(n_hh2_, 1) * s, &bytes_);
+    X_.alloc(std::max<int64_t>(n_hh2_, 1) * s, &bytes_);
+    I9_.alloc(std::max<int64_t>(n_hh2_, 1) * s, &bytes_);
+    Tph_.alloc(std::max<int64_t>(n_ph_, 1) * s, &bytes_);
+    Rph_.alloc(std::max<int64_t>(n_ph_, 1) * s, &bytes_);
+    Vph_.alloc(std::max<int64_t>(n_ph_, 1) * s, &bytes_);
+    W_.alloc(std::max<int64_t>(n_i4_, 1) * s, &bytes_);
+    I4_.alloc(std::max<int64_t>(n_i4_, 1) * s, &bytes_);
+    fdiag_.alloc(ns * s, &bytes_);
+    f6_.alloc(std::max(NP, 1) * s, &bytes_);
+    f7_.alloc(std::max(A, 1) * s, &bytes_);
+    d2ij_.alloc(std::max(A, 1) * s, &bytes_);
+    d2ab_.alloc(std::max(NP, 1) * s, &bytes_);
+    i6off_.alloc(std::max(NP, 1) * s, &bytes_);
+    i7off_.alloc(std::max(A, 1) * s, &bytes_);
+    for (DBuf *b : {&T_, &R_, &Vhp_, &Vpp_, &Vhh_, &X_, &I9_, &Tph_, &Rph_, &Vph_, &W_, &I4_, &fdiag_, &f6_, &f7_, &d2ij_,
+                    &d2ab_, &i6off_, &i7off_})
+      CK(cudaMemset(b->p, 0, b->bytes));
+    const size_t npart = std::max<size_t>({(size_t)n_ttile_ * 3, (size_t)608 * 32, 64});
+    partial_.alloc(npart * sizeof(double), &bytes_);
+    res_.alloc(64 * sizeof(double), &bytes_);
+    flag_.alloc(sizeof(int), &bytes_);
+    CK(cudaMemset(flag_.p, 0, sizeof(int)));
+    stage_.alloc((size_t)std::max<int64_t>(max_stage_, 1) * 2 * sizeof(double), &bytes_);
+    CK(cudaMallocHost(&host_res_, 64 * sizeof(double)));
+    build_gemm_plans();
+  }
+
+  void add_tiles(std::vector<GemmTile> &tiles, int prob, int M, int N) {
+    for (int m0 = 0; m0 < M; m0 += kGemmBM)
+      for (int n0 = 0; n0 < N; n0 += kGemmBN) tiles.push_back(GemmTile{prob, m0, n0, 0});
+  }
+  struct Plan {
+    DBuf probs, tiles;
+    int ntiles = 0;
+  };
+  void finalize_plan(Plan &pl, std::vector<GemmProb<S>> &probs, std::vector<GemmTile> &tiles, const std::vector<int64_t> &work) {
+    // largest problems first for load balance across the SMs
+    std::stable_sort(tiles.begin(), tiles.end(), [&](const GemmTile &a, const GemmTile &b) { return work[a.prob] > work[b.prob]; });
+    upload(pl.probs, probs, &bytes_);
+    upload(pl.tiles, tiles, &bytes_);
+    pl.ntiles = (int)tiles.size();
+  }
+  void build_gemm_plans() {
+    const Layout &L = *L_;
+    const int nc = L.fam[3].count();
+    {  // X = V_hhpp' T'  (H x H, K = P)
+      std::vector<GemmProb<S>> probs;
+      std::vector<GemmTile> tiles;
+      std::vector<int64_t> work;
+      int64_t hoff = 0;
+      for (int c = 0; c < nc; ++c) {
+        const auto &pk = L.pk[c];
+        if (pk.H > 0 && pk.P > 0) {
+          GemmProb<S> p{};
+          p.nseg = 1;
+          p.M = pk.H; p.N = pk.H;
+          p.seg[0] = GemmSeg<S>{Vhp_.as<S>() + pk.t_off, T_.as<S>() + pk.t_off, pk.P, 1, 1, pk.P, pk.P, 1.0};
+          p.C = X_.as<S>() + hoff; p.C0 = nullptr; p.sCm = 1; p.sCn = pk.H; p.accumulate = 0;
+          add_tiles(tiles, (int)probs.size(), p.M, p.N);
+          work.push_back((int64_t)pk.H * pk.H * pk.P);
+          probs.push_back(p);
+        }
+        hoff += (int64_t)pk.H * pk.H;
+      }
+      finalize_plan(planX_, probs, tiles, work);
+    }
+    {  // R' += V_pppp' T' + T' I9'
+      std::vector<GemmProb<S>> probs;
+      std::vector<GemmTile> tiles;
+      std::vector<int64_t> work;
+      int64_t hoff = 0, voff = 0;
+      for (int c = 0; c < nc; ++c) {
+        const auto &pk = L.pk[c];
+        if (pk.H > 0 && pk.P > 0) {
+          GemmProb<S> p{};
+          p.nseg = 2;
+          p.M = pk.P; p.N = pk.H;
+          p.seg[0] = GemmSeg<S>{Vpp_.as<S>() + voff, T_.as<S>() + pk.t_off, pk.P, 1, 1, pk.P, pk.P, 1.0};
+          p.seg[1] = GemmSeg<S>{T_.as<S>() + pk.t_off, I9_.as<S>() + hoff, 1, pk.P, 1, pk.H, pk.H, 1.0};
+          p.C = R_.as<S>() + pk.t_off; p.C0 = nullptr; p.sCm = 1; p.sCn = pk.P; p.accumulate = 1;
+          add_tiles(tiles, (int)probs.size(), p.M, p.N);
+          work.push_back((int64_t)pk.P * pk.H * (pk.P + pk.H));
+          probs.push_back(p);
+        }
+        hoff += (int64_t)pk.H * pk.H;
+        voff += (int64_t)pk.P * pk.P;
+      }
+      finalize_plan(planLadder_, probs, tiles, work);
+    }
+    {  // I4 = W + 1/2 V_ph T_ph ; R_ph = T_ph I4
+      std::vector<GemmProb<S>> p4, pr;
+      std::vector<GemmTile> t4, tr;
+      std::vector<int64_t> w4, wr;
+      int64_t toff = 0, ioff = 0;
+      for (int q = 0; q < L.ph[1].count(); ++q) {
+        const int nph = L.ph[1].side1[q].size(), nhp = L.ph[1].side2[q].size();
+        if (nph > 0 && nhp > 0) {
+          GemmProb<S> a{};
+          a.nseg = 1;
+          a.M = nhp; a.N = nhp;
+          a.seg[0] = GemmSeg<S>{Vph_.as<S>() + toff, Tph_.as<S>() + toff, 1, nhp, 1, nph, nph, 0.5};
+          a.C = I4_.as<S>() + ioff; a.C0 = W_.as<S>() + ioff; a.sCm = 1; a.sCn = nhp; a.accumulate = 0;
+          add_tiles(t4, (int)p4.size(), a.M, a.N);
+          w4.push_back((int64_t)nhp * nhp * nph);
+          p4.push_back(a);
+          GemmProb<S> b{};
+          b.nseg = 1;
+          b.M = nph; b.N = nhp;
+          b.seg[0] = GemmSeg<S>{Tph_.as<S>() + toff, I4_.as<S>() + ioff, 1, nph, 1, nhp, nhp, 1.0};
+          b.C = Rph_.as<S>() + toff; b.C0 = nullptr; b.sCm = 1; b.sCn = nph; b.accumulate = 0;
+          add_tiles(tr, (int)pr.size(), b.M, b.N);
+          wr.push_back((int64_t)nph * nhp * nhp);
+          pr.push_back(b);
+        }
+        toff += (int64_t)nph * nhp;
+        ioff += (int64_t)nhp * nhp;
+      }
+      finalize_plan(planI4_, p4, t4, w4);
+      finalize_plan(planRing_, pr, tr, wr);
+    }
+  }
+
+  // ================================================================== iteration
+  void mark(int i) {
+    if (timing_) CK(cudaEventRecord(ev_[i], st_));
+  }
+  void residual(bool /*unused*/) {
+    mark(0);
+    launch_gather_tph<S>(D_, T_.as<S>(), Tph_.as<S>(), st_);
+    mark(1);
+    launch_gemm<S>((const GemmProb<S> *)planX_.probs.p, (const GemmTile *)planX_.tiles.p, planX_.ntiles, st_);
+    launch_i7<S>(D_, X_.as<S>(), fdiag_.as<S>(), f7_.as<S>(), d2ij_.as<S>(), i7off_.as<S>(), st_);
+    launch_i9<S>(D_, n_hh2_, Vhh_.as<S>(), X_.as<S>(), I9_.as<S>(), st_);
+    mark(2);
+    launch_i6<S>(D_, T_.as<S>(), Vhp_.as<S>(), fdiag_.as<S>(), f6_.as<S>(), d2ab_.as<S>(), i6off_.as<S>(), st_);
+    mark(3);
+    launch_gemm<S>((const GemmProb<S> *)planI4_.probs.p, (const GemmTile *)planI4_.tiles.p, planI4_.ntiles, st_);
+    mark(4);
+    launch_gemm<S>((const GemmProb<S> *)planRing_.probs.p, (const GemmTile *)planRing_.tiles.p, planRing_.ntiles, st_);
+    mark(5);
+    launch_rinit<S>(D_, T_.as<S>(), Vhp_.as<S>(), Rph_.as<S>(), i6off_.as<S>(), i7off_.as<S>(), R_.as<S>(), st_);
+    mark(6);
+    launch_gemm<S>((const GemmProb<S> *)planLadder_.probs.p, (const GemmTile *)planLadder_.tiles.p, planLadder_.ntiles, st_);
+    mark(7);
+    launches_ += 9;
+    if (timing_) accumulate_timers(0, 7);
+  }
+  void accumulate_timers(int first, int last) {
+    CK(cudaEventSynchronize(ev_[last]));
+    for (int i = first; i < last; ++i) {
+      float ms = 0.f;
+      CK(cudaEventElapsedTime(&ms, ev_[i], ev_[i + 1]));
+      timers_[i] += ms;
+    }
+  }
+  void fetch_res(int n) {
+    CK(cudaMemcpyAsync(host_res_, res_.p, n * sizeof(double), cudaMemcpyDeviceToHost, st_));
+    CK(cudaStreamSynchronize(st_));
+    if (!std::isfinite(host_res_[0]) || !std::isfinite(host_res_[1]))
+      throw EngineError(5, "non-finite energy: the iteration diverged or the input holds NaN/Inf");
+  }
+
+  // diis_t1t2 (ccm_diis.f90:74-249) on the packed vectors; the reference's column
+  // shift of t2_diis is a rotation of the physical column ids here.
+  void reference_update(int count) {
+    if (nstep_ > subspace_) {
+      nstep_ = subspace_;
+      const int first = phys_[0];
+      for (int i = 0; i < subspace_ - 1; ++i) phys_[i] = phys_[i + 1];
+      phys_[subspace_ - 1] = first;
+    }
+    S *col = hist_.as<S>() + (int64_t)phys_[nstep_ - 1] * n_t_;
+    mark(7);
+    launch_update<S>(D_, 0, T_.as<S>(), R_.as<S>(), Vhp_.as<S>(), d2ij_.as<S>(), d2ab_.as<S>(), col, nullptr,
+                     partial_.as<double>(), res_.as<double>(), st_);
+    launches_ += 2;
+    fetch_res(3);
+    last_rn_ = 2.0 * std::sqrt(host_res_[2]);
+    mark(8);
+    if (timing_) accumulate_timers(7, 8);
+    if (count != diis_step_) return;
+    const int ns = nstep_;
+    if (ns < 2) return;
+    std::vector<const S *> cols(ns);
+    for (int i = 0; i < ns; ++i) cols[i] = hist_.as<S>() + (int64_t)phys_[i] * n_t_;
+    launch_diis_gram<S>(n_t_, cols.data(), ns, partial_.as<double>(), res_.as<double>(), st_);
+    launches_ += 2;
+    fetch_res(30);
+    std::vector<std::complex<double>> B((size_t)ns * ns, 0.0), sol(ns, 0.0);
+    const int nd = ns - 1;
+    int k = 0;
+    for (int i = 0; i < 5; ++i)
+      for (int j = i; j < 5; ++j) {
+        if (i < nd && j < nd) {
+          // x4: the ordered vectors hold each packed amplitude four times
+          const std::complex<double> v(4.0 * host_res_[2 * k], 4.0 * host_res_[2 * k + 1]);
+          B[i + (size_t)ns * j] = v;
+          B[j + (size_t)ns * i] = v;
+        }
+        ++k;
+      }
+    for (int i = 0; i < nd; ++i) { B[i + (size_t)ns * nd] = -1.0; B[nd + (size_t)ns * i] = -1.0; }
+    B[nd + (size_t)ns * nd] = 0.0;
+    sol[nd] = -1.0;
+    if (!zsolve(ns, B, sol)) throw EngineError(5, "singular DIIS matrix");
+    std::vector<double> coef(2 * nd);
+    for (int i = 0; i < nd; ++i) { coef[2 * i] = sol[i].real(); coef[2 * i + 1] = ScalarOf<S>::complex ? sol[i].imag() : 0.0; }
+    launch_combine<S>(n_t_, cols.data(), coef.data(), nd, T_.as<S>(), st_);
+    ++launches_;
+    mark(9);
+    if (timing_) accumulate_timers(8, 9);
+  }
+
+  void iterate_reference(const IterOpts &o, IterResult &r) {
+    diis_setup(6, 6);
+    int count = 0;
+    std::complex<double> e1(r.e_mbpt2[0], r.e_mbpt2[1]), e2(0.0, 0.0), de(4.0, 0.0);
+    int it = 0;
+    for (it = 1; it <= o.max_iter; ++it) {
+      if (!(std::abs(de) > o.tol)) break;
+      residual(true);
+      ++count;
+      ++nstep_;
+      reference_update(count);
+      if (count == diis_step_) count = 0;
+      r.res_norm = last_rn_;
+      // energy of the updated (or extrapolated) amplitudes
+      double e[2];
+      energy(e);
+      e2 = std::complex<double>(e[0], e[1]);
+      de = e2 - e1;
+      e1 = e2;
+      r.iterations = it;
+      if (o.verbose) std::printf("ccx it %3d dE %.3e E %.12f |R| %.3e\n", it, de.real(), e2.real(), r.res_norm);
+    }
+    r.converged = !(std::abs(de) > o.tol);
+    r.e_ccd[0] = e2.real();
+    r.e_ccd[1] = e2.imag();
+  }
+
+  void iterate_standard(const IterOpts &o, IterResult &r) {
+    const int m = std::max(2, std::min(o.diis_dim, 15));
+    hist_t_.alloc((size_t)m * n_t_ * sizeof(S), &bytes_);
+    hist_e_.alloc((size_t)m * n_t_ * sizeof(S), &bytes_);
+    std::vector<double> B((size_t)m * m, 0.0);
+    int nh = 0, head = 0;
+    double e[2] = {r.e_mbpt2[0], r.e_mbpt2[1]};
+    for (int it = 1; it <= o.max_iter; ++it) {
+      residual(true);
+      S *ht = hist_t_.as<S>() + (int64_t)head * n_t_;
+      S *he = hist_e_.as<S>() + (int64_t)head * n_t_;
+      mark(7);
+      launch_update<S>(D_, 1, T_.as<S>(), R_.as<S>(), Vhp_.as<S>(), d2ij_.as<S>(), d2ab_.as<S>(), ht, he,
+                       partial_.as<double>(), res_.as<double>(), st_);
+      launches_ += 2;
+      fetch_res(3);
+      mark(8);
+      if (timing_) accumulate_timers(7, 8);
+      e[0] = host_res_[0];
+      e[1] = host_res_[1];
+      r.res_norm = 2.0 * std::sqrt(host_res_[2]);
+      r.iterations = it - 1;
+      if (o.verbose) std::printf("ccx it %3d |R| %.3e E %.12f\n", it, r.res_norm, e[0]);
+      if (r.res_norm < o.tol) { r.converged = 1; break; }
+      // Gram row of the new step against every stored step, with conjugation
+      const int slot = head;
+      if (nh < m) ++nh;
+      std::vector<const S *> es(nh);
+      for (int j = 0; j < nh; ++j) es[j] = hist_e_.as<S>() + (int64_t)j * n_t_;
+      launch_dots<S>(n_t_, he, es.data(), nh, 1, partial_.as<double>(), res_.as<double>(), st_);
+      launches_ += 2;
+      CK(cudaMemcpyAsync(host_res_, res_.p, 2 * nh * sizeof(double), cudaMemcpyDeviceToHost, st_));
+      CK(cudaStreamSynchronize(st_));
+      for (int j = 0; j < nh; ++j) { B[slot + (size_t)m * j] = host_res_[2 * j]; B[j + (size_t)m * slot] = host_res_[2 * j]; }
+      head = (head + 1) % m;
+      std::vector<double> coef;
+      bool ok = false;
+      if (nh >= 2) {
+        const int n1 = nh + 1;
+        std::vector<double> Bm((size_t)n1 * n1, 0.0), rhs(n1, 0.0);
+        for (int i = 0; i < nh; ++i)
+          for (int j = 0; j < nh; ++j) Bm[i + (size_t)n1 * j] = B[i + (size_t)m * j];
+        for (int i = 0; i < nh; ++i) { Bm[i + (size_t)n1 * nh] = -1.0; Bm[nh + (size_t)n1 * i] = -1.0; }
+        rhs[nh] = -1.0;
+        ok = dsolve(n1, Bm, rhs);
+        if (ok) {
+          coef.resize(2 * nh);
+          for (int i = 0; i < nh; ++i) { coef[2 * i] = rhs[i]; coef[2 * i + 1] = 0.0; }
+        }
+      }
+      mark(8);
+      if (ok) {
+        std::vector<const S *> ts(nh);
+        for (int j = 0; j < nh; ++j) ts[j] = hist_t_.as<S>() + (int64_t)j * n_t_;
+        launch_combine<S>(n_t_, ts.data(), coef.data(), nh, T_.as<S>(), st_);
+      } else {
+        CK(cudaMemcpyAsync(T_.p, ht, n_t_ * sizeof(S), cudaMemcpyDeviceToDevice, st_));
+      }
+      ++launches_;
+      mark(9);
+      if (timing_) accumulate_timers(8, 9);
+      r.iterations = it;
+    }
+    r.e_ccd[0] = e[0];
+    r.e_ccd[1] = e[1];
+  }
+
+  // ================================================================== state
+  std::shared_ptr<const Layout> L_;
+  int device_ = 0;
+  cudaStream_t st_ = nullptr;
+  cudaEvent_t ev_[12] = {};
+  double timers_[10] = {};
+  bool timing_ = false;
+  int64_t bytes_ = 0, launches_ = 0;
+  DevLayout D_{};
+  DevOrbits O_{};
+  DevPotential pot_{};
+  std::vector<int> partner_, hhhh_to_hhpp_;
+  std::vector<int64_t> ppsgn_off_, hhsgn_off_, v4_off_h_;
+  int64_t n_t_ = 0, n_vpp_ = 0, n_hh2_ = 0, n_ph_ = 0, n_i4_ = 0, max_stage_ = 0;
+  int n_ttile_ = 0;
+  // device tables
+  DBuf dP_, dH_, dt_off_, dvpp_off_, dhh2_off_, dpp_off_, dhh_off_, dpp_orb_, dhh_orb_, dpp_row_, dhh_row_, dpp_slot_,
+      dhh_slot_, dpartner_, dn_ph_, dn_hp_, dtph_off_, di4_off_, dvph_off_, dph_off_, dhp_off_, dph_orb_, dhp_orb_,
+      dph_slot_, dhp_slot_, dttile_, dphtile_, dvtile_, pp_sgn_, hh_sgn_, n4_, hp4_slot_, v4_off_, v4_;
+  DBuf onx_, ony_, onz_, osz_, otz_, okx_, oky_, okz_, oe_;
+  // state
+  DBuf T_, R_, Vhp_, Vpp_, Vhh_, X_, I9_, Tph_, Rph_, Vph_, W_, I4_, fdiag_, f6_, f7_, d2ij_, d2ab_, i6off_, i7off_;
+  DBuf partial_, res_, flag_, stage_, hist_, hist_t_, hist_e_;
+  Plan planX_, planLadder_, planI4_, planRing_;
+  double *host_res_ = nullptr;
+  int host_flag_ = 0;
+  double e0_[2] = {0, 0};
+  double last_rn_ = 0.0;
+  bool have_fock_ = false, have_t_ = false, dirty_ = true, vph_ready_ = false, generated_ = false;
+  int subspace_ = 0, diis_step_ = 6, nstep_ = 0;
+  std::vector<int> phys_;
+  std::unique_ptr<ITriples<S>> tr_;
+};
+
+std::unique_ptr<IEngine> make_engine(std::shared_ptr<const Layout> L, int device, bool complex_scalars) {
+  if (complex_scalars) return std::unique_ptr<IEngine>(new Engine<cplx>(std::move(L), device));
+  return std::unique_ptr<IEngine>(new Engine<double>(std::move(L), device));
+}
+
+}  // namespace ccx

@@ -1,0 +1,70 @@
+// CCD engine: device image of a layout plus the iteration driver.
+#pragma once
+
+#include <cstdint>
+#include <memory>
+#include <stdexcept>
+#include <string>
+
+#include "layout.hpp"
+
+namespace ccx {
+
+struct EngineError : std::runtime_error {
+  int code;
+  EngineError(int c, const std::string &m) : std::runtime_error(m), code(c) {}
+};
+
+struct IterOpts {
+  int mode = 0;          // 0 reference, 1 standard
+  int precision = 0;     // 0 FP64, 1 mixed
+  int max_iter = 100;
+  double tol = 1e-6;
+  int diis_dim = 8;
+  int defect_period = 4;
+  int verbose = 0;
+};
+struct IterResult {
+  int iterations = 0, converged = 0;
+  double e_mbpt2[2] = {0, 0}, e_ccd[2] = {0, 0};
+  double res_norm = 0.0, seconds = 0.0;
+};
+struct PotentialSpec {
+  int kind = 0;
+  uint64_t lec_seed = 20261203ULL;
+  int f32_literals = 1;
+};
+
+class IEngine {
+ public:
+  virtual ~IEngine() = default;
+  virtual bool is_complex() const = 0;
+  virtual int64_t device_bytes() const = 0;
+  virtual int64_t launches() const = 0;
+  virtual void timers(double ms[10]) const = 0;
+  virtual void set_fock(const double *fock, const double e0[2]) = 0;
+  virtual void set_vblock(int kind, int ch, const double *v) = 0;
+  virtual void generate(const PotentialSpec &p) = 0;
+  virtual void get_e0(double e0[2]) = 0;
+  virtual void mp2() = 0;
+  virtual void set_t2(int ch, const double *t) = 0;
+  virtual void get_t2(int ch, double *t) = 0;
+  virtual void get_r2(int ch, double *r) = 0;
+  virtual void set_t2_all(const double *t) = 0;
+  virtual void get_t2_all(double *t) = 0;
+  virtual void get_denominators(double *d2ij, double *d2ab) = 0;
+  virtual void t2_intermediate() = 0;
+  virtual void diis_setup(int subspace, int step) = 0;
+  virtual void diis_t1t2(int *count) = 0;
+  virtual void energy(double e[2]) = 0;
+  virtual double residual_norm() = 0;
+  virtual void ccd_iter(const IterOpts &o, IterResult &r) = 0;
+  virtual void triples(double et[2]) = 0;
+};
+
+std::unique_ptr<IEngine> make_engine(std::shared_ptr<const Layout> L, int device, bool complex_scalars);
+
+// contact LECs of the chiral-like synthetic potential drawn from a seed
+void draw_lecs(uint64_t seed, double out[9]);
+
+}  // namespace ccx

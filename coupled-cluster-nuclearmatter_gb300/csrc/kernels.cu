@@ -1,0 +1,745 @@
+// CCD kernels of the FP64 path (real or complex scalars).
+//
+// The engine stores T2 packed: one block per hhpp channel over pairs a<b and i<j
+// (column-major, P x H).  Every term of the reference residual
+// (ccm_t2_eqn.f90:4-1304) is restated on that representation:
+//   ordered sums 1/2 sum_cd over (c,d) become sums over c<d with weight 1, and
+//   the reference's antisymmetrising scatters become gathers with signs.
+#include <algorithm>
+#include <cstdio>
+
+#include "common.cuh"
+#include "devlayout.hpp"
+#include "kernels.hpp"
+#include "potential.cuh"
+
+namespace ccx {
+
+namespace {
+
+__device__ inline double2 warp_sum2(double2 v) {
+  for (int o = 16; o > 0; o >>= 1) {
+    v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+    v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+  }
+  return v;
+}
+__device__ inline double2 to2(double x) { return make_double2(x, 0.0); }
+__device__ inline double2 to2(cplx x) { return make_double2(x.re, x.im); }
+template <typename S> __device__ inline S from2(double2 v);
+template <> __device__ inline double from2<double>(double2 v) { return v.x; }
+template <> __device__ inline cplx from2<cplx>(double2 v) { return cplx(v.x, v.y); }
+
+// Block-wide sum of NV doubles per thread into partial[blockIdx.x*NV + k].
+template <int NV>
+__device__ void block_partial(double (&v)[NV], double *partial) {
+  __shared__ double red[NV][32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    double x = warp_sum(v[k]);
+    if (lane == 0) red[k][wid] = x;
+  }
+  __syncthreads();
+  if (wid == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      double x = lane < nw ? red[k][lane] : 0.0;
+      x = warp_sum(x);
+      if (lane == 0) partial[(int64_t)blockIdx.x * NV + k] = x;
+    }
+  }
+}
+
+// Fixed-order finish of nb partial rows of nv values: out[k] = sum_b partial[b*nv+k].
+__global__ void k_finish(const double *partial, int nb, int nv, double *out) {
+  const int k = blockIdx.x;
+  double s = 0.0;
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) s += partial[(int64_t)b * nv + k];
+  __shared__ double red[32];
+  s = warp_sum(s);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double x = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+    x = warp_sum(x);
+    if (threadIdx.x == 0) out[k] = x;
+  }
+}
+
+void finish(const double *partial, int nb, int nv, double *out, cudaStream_t st) {
+  k_finish<<<nv, 256, 0, st>>>(partial, nb, nv, out);
+}
+
+template <typename S> __device__ inline S cvt_in(const double *p, int *flag);
+template <> __device__ inline double cvt_in<double>(const double *p, int *flag) {
+  if (p[1] != 0.0) atomicExch(flag, 1);
+  return p[0];
+}
+template <> __device__ inline cplx cvt_in<cplx>(const double *p, int *) { return cplx(p[0], p[1]); }
+
+}  // namespace
+
+// ============================================================================
+// grouped GEMM, FP64 FMA.  One CTA per 64x64 output tile of one problem; up to two
+// K segments share the accumulator (the pp-ladder and hh-ladder both add into R).
+// ============================================================================
+template <typename S>
+__global__ void __launch_bounds__(256) k_gemm(const GemmProb<S> *__restrict__ probs, const GemmTile *__restrict__ tiles) {
+  constexpr int BM = kGemmBM, BN = kGemmBN, BK = kGemmBK, TM = 4, TN = 4;
+  __shared__ S As[BK][BM + 1];
+  __shared__ S Bs[BK][BN + 1];
+  const GemmTile tl = tiles[blockIdx.x];
+  const GemmProb<S> pr = probs[tl.prob];
+  const int tid = threadIdx.x;
+  const int tm = tid & 15, tn = tid >> 4;
+  const bool active = (tl.m0 + tm * TM < pr.M) && (tl.n0 + tn * TN < pr.N);
+  S acc[TM][TN];
+#pragma unroll
+  for (int i = 0; i < TM; ++i)
+#pragma unroll
+    for (int j = 0; j < TN; ++j) acc[i][j] = S(0.0);
+  for (int s = 0; s < pr.nseg; ++s) {
+    const GemmSeg<S> sg = pr.seg[s];
+    for (int k0 = 0; k0 < sg.K; k0 += BK) {
+      for (int x = tid; x < BM * BK; x += 256) {
+        int m, k;
+        if (sg.sAm == 1) { m = x % BM; k = x / BM; } else { k = x % BK; m = x / BK; }
+        const int gm = tl.m0 + m, gk = k0 + k;
+        S v = S(0.0);
+        if (gm < pr.M && gk < sg.K) v = sg.alpha * sg.A[(int64_t)gm * sg.sAm + (int64_t)gk * sg.sAk];
+        As[k][m] = v;
+      }
+      for (int x = tid; x < BK * BN; x += 256) {
+        int k, n;
+        if (sg.sBk == 1) { k = x % BK; n = x / BK; } else { n = x % BN; k = x / BN; }
+        const int gk = k0 + k, gn = tl.n0 + n;
+        S v = S(0.0);
+        if (gk < sg.K && gn < pr.N) v = sg.B[(int64_t)gk * sg.sBk + (int64_t)gn * sg.sBn];
+        Bs[k][n] = v;
+      }
+      __syncthreads();
+      if (active) {
+#pragma unroll
+        for (int k = 0; k < BK; ++k) {
+          S a[TM], b[TN];
+#pragma unroll
+          for (int i = 0; i < TM; ++i) a[i] = As[k][tm * TM + i];
+#pragma unroll
+          for (int j = 0; j < TN; ++j) b[j] = Bs[k][tn * TN + j];
+#pragma unroll
+          for (int i = 0; i < TM; ++i)
+#pragma unroll
+            for (int j = 0; j < TN; ++j) acc[i][j] += a[i] * b[j];
+        }
+      }
+      __syncthreads();
+    }
+  }
+  if (!active) return;
+#pragma unroll
+  for (int i = 0; i < TM; ++i) {
+    const int m = tl.m0 + tm * TM + i;
+    if (m >= pr.M) continue;
+#pragma unroll
+    for (int j = 0; j < TN; ++j) {
+      const int n = tl.n0 + tn * TN + j;
+      if (n >= pr.N) continue;
+      const int64_t o = (int64_t)m * pr.sCm + (int64_t)n * pr.sCn;
+      if (pr.accumulate) pr.C[o] += acc[i][j];
+      else pr.C[o] = (pr.C0 ? pr.C0[o] : S(0.0)) + acc[i][j];
+    }
+  }
+}
+
+template <typename S>
+void launch_gemm(const GemmProb<S> *probs, const GemmTile *tiles, int ntiles, cudaStream_t st) {
+  if (ntiles > 0) k_gemm<S><<<ntiles, 256, 0, st>>>(probs, tiles);
+}
+
+// ============================================================================
+// T_ph(ai, jb) = T(ab, ij): gather of ccm_t2_eqn.f90:37-62
+// ============================================================================
+template <typename S>
+__global__ void k_gather_tph(DevLayout L, const S *__restrict__ T, S *__restrict__ Tph) {
+  const int2 tl = L.phtile[blockIdx.x];
+  const int q = tl.x;
+  const int nph = L.n_ph[q], nhp = L.n_hp[q];
+  const int64_t n = (int64_t)nph * nhp;
+  const int64_t end = min((int64_t)tl.y + kTileElems, n);
+  for (int64_t e = tl.y + threadIdx.x; e < end; e += blockDim.x) {
+    const int r = (int)(e % nph), c = (int)(e / nph);
+    const int2 ai = L.ph_orb[L.ph_off[q] + r];
+    const int2 jb = L.hp_orb[L.hp_off[q] + c];
+    const int2 sab = L.pp_slot[(int64_t)(ai.x - L.A) * L.NP + (jb.y - L.A)];
+    const int2 sij = L.hh_slot[ai.y * L.A + jb.x];
+    S v = S(0.0);
+    if (sab.y != 0 && sij.y != 0) {
+      const int ch = sab.x;
+      v = (ssign(sab.y) * ssign(sij.y)) * T[L.t_off[ch] + sidx(sab.y) + (int64_t)L.P[ch] * sidx(sij.y)];
+    }
+    Tph[L.tph_off[q] + e] = v;
+  }
+}
+template <typename S> void launch_gather_tph(const DevLayout &L, const S *T, S *Tph, cudaStream_t st) {
+  if (L.nphtile) k_gather_tph<S><<<L.nphtile, 256, 0, st>>>(L, T, Tph);
+}
+
+// ============================================================================
+// I7(k,i) = f(k,i) + 1/2 sum V(kl,cd) T(cd,il), ccm_t2_eqn.f90:1352-1392, from the
+// packed X = V_hhpp' T'; only k in {i, partner(i)} is non-zero.  The diagonal
+// becomes d2ij (ccm_t2_eqn.f90:81-84).
+// ============================================================================
+template <typename S>
+__global__ void k_i7(DevLayout L, const S *__restrict__ X, const S *__restrict__ fdiag, const S *__restrict__ f7,
+                     S *d2ij, S *i7off) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= 2 * L.A) return;
+  const int y = t >> 1, which = t & 1;
+  const int c = which ? L.partner[y] : y;
+  if (which && (c < 0 || c >= L.A)) { i7off[y] = S(0.0); return; }
+  S acc = which ? f7[y] : fdiag[y];
+  for (int l = 0; l < L.A; ++l) {
+    const int2 s1 = L.hh_slot[c * L.A + l], s2 = L.hh_slot[y * L.A + l];
+    if (s1.y == 0 || s2.y == 0) continue;
+    const int ch = s1.x;
+    acc += (ssign(s1.y) * ssign(s2.y)) * X[L.hh2_off[ch] + sidx(s1.y) + (int64_t)L.H[ch] * sidx(s2.y)];
+  }
+  if (which) i7off[y] = acc;
+  else d2ij[y] = acc;
+}
+template <typename S>
+void launch_i7(const DevLayout &L, const S *X, const S *fdiag, const S *f7, S *d2ij, S *i7off, cudaStream_t st) {
+  const int n = 2 * L.A;
+  k_i7<S><<<(n + 127) / 128, 128, 0, st>>>(L, X, fdiag, f7, d2ij, i7off);
+}
+
+template <typename S>
+__global__ void k_i9(int64_t n, const S *__restrict__ Vhh, const S *__restrict__ X, S *I9) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    I9[i] = Vhh[i] + X[i];
+}
+template <typename S> void launch_i9(const DevLayout &, int64_t n, const S *Vhh, const S *X, S *I9, cudaStream_t st) {
+  if (n > 0) k_i9<S><<<(int)std::min<int64_t>((n + 255) / 256, 4096), 256, 0, st>>>(n, Vhh, X, I9);
+}
+
+// ============================================================================
+// I6(a,c) = f(a,c) - 1/2 sum V(kl,dc) T(da,kl), ccm_t2_eqn.f90:1399-1441, for
+// c in {a, partner(a)}; one warp per (a, c).  The diagonal becomes d2ab (:86-89).
+// ============================================================================
+template <typename S>
+__global__ void k_i6(DevLayout L, const S *__restrict__ T, const S *__restrict__ Vhp, const S *__restrict__ fdiag,
+                     const S *__restrict__ f6, S *d2ab, S *i6off) {
+  const int w = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (w >= 2 * L.NP) return;
+  const int u = w >> 1, which = w & 1;
+  const int x = L.A + u;
+  const int c = which ? L.partner[x] : x;
+  if (which && c < L.A) {
+    if (lane == 0) i6off[u] = S(0.0);
+    return;
+  }
+  const int v = c - L.A;
+  S acc = S(0.0);
+  for (int d = lane; d < L.NP; d += 32) {
+    const int2 s1 = L.pp_slot[(int64_t)d * L.NP + u];
+    const int2 s2 = L.pp_slot[(int64_t)d * L.NP + v];
+    if (s1.y == 0 || s2.y == 0) continue;
+    const int ch = s1.x;
+    const int64_t P = L.P[ch];
+    const int H = L.H[ch];
+    const S *tc = T + L.t_off[ch] + sidx(s1.y);
+    const S *vc = Vhp + L.t_off[ch] + sidx(s2.y);
+    S dot = S(0.0);
+    for (int k = 0; k < H; ++k) dot += tc[P * k] * vc[P * k];
+    acc += (ssign(s1.y) * ssign(s2.y)) * dot;
+  }
+  const S tot = from2<S>(warp_sum2(to2(acc)));
+  if (lane == 0) {
+    const S val = (which ? f6[u] : fdiag[x]) - tot;
+    if (which) i6off[u] = val;
+    else d2ab[u] = val;
+  }
+}
+template <typename S>
+void launch_i6(const DevLayout &L, const S *T, const S *Vhp, const S *fdiag, const S *f6, S *d2ab, S *i6off, cudaStream_t st) {
+  const int64_t threads = (int64_t)2 * L.NP * 32;
+  k_i6<S><<<(int)((threads + 255) / 256), 256, 0, st>>>(L, T, Vhp, fdiag, f6, d2ab, i6off);
+}
+
+// ============================================================================
+// R' = conj(V(ij,ab)) (:106-138) + one-body I6/I7 terms (:144-211) + the P(ab)P(ij)
+// ring scatter (:840-892) written as a gather of four R_ph entries.
+// ============================================================================
+template <typename S>
+__device__ inline S ring_at(const DevLayout &L, const S *__restrict__ Rph, int a, int i, int j, int b) {
+  const int2 s1 = L.ph_slot[(int64_t)(a - L.A) * L.A + i];
+  const int2 s2 = L.hp_slot[(int64_t)j * L.NP + (b - L.A)];
+  if (s1.x < 0 || s2.x < 0) return S(0.0);
+  const int q = s1.x;
+  return Rph[L.tph_off[q] + s1.y + (int64_t)L.n_ph[q] * s2.y];
+}
+
+template <typename S>
+__global__ void k_rinit(DevLayout L, const S *__restrict__ T, const S *__restrict__ Vhp, const S *__restrict__ Rph,
+                        const S *__restrict__ i6off, const S *__restrict__ i7off, S *__restrict__ R) {
+  const int2 tl = L.ttile[blockIdx.x];
+  const int ch = tl.x;
+  const int P = L.P[ch], H = L.H[ch];
+  const int64_t n = (int64_t)P * H;
+  const int64_t end = min((int64_t)tl.y + kTileElems, n);
+  const S *tc = T + L.t_off[ch];
+  const int A = L.A, NP = L.NP;
+  for (int64_t e = tl.y + threadIdx.x; e < end; e += blockDim.x) {
+    const int ab = (int)(e % P), ij = (int)(e / P);
+    const int2 po = L.pp_orb[L.pp_off[ch] + ab];
+    const int2 ho = L.hh_orb[L.hh_off[ch] + ij];
+    const int a = po.x, b = po.y, i = ho.x, j = ho.y;
+    S r = conj_(Vhp[L.t_off[ch] + e]);
+    const int bb = L.partner[b];
+    if (bb >= A) {
+      const int2 s = L.pp_slot[(int64_t)(a - A) * NP + (bb - A)];
+      if (s.y) r += i6off[b - A] * (ssign(s.y) * tc[sidx(s.y) + (int64_t)P * ij]);
+    }
+    const int aa = L.partner[a];
+    if (aa >= A) {
+      const int2 s = L.pp_slot[(int64_t)(b - A) * NP + (aa - A)];
+      if (s.y) r -= i6off[a - A] * (ssign(s.y) * tc[sidx(s.y) + (int64_t)P * ij]);
+    }
+    const int jj = L.partner[j];
+    if (jj >= 0 && jj < A) {
+      const int2 s = L.hh_slot[i * A + jj];
+      if (s.y) r -= i7off[j] * (ssign(s.y) * tc[ab + (int64_t)P * sidx(s.y)]);
+    }
+    const int ii = L.partner[i];
+    if (ii >= 0 && ii < A) {
+      const int2 s = L.hh_slot[j * A + ii];
+      if (s.y) r += i7off[i] * (ssign(s.y) * tc[ab + (int64_t)P * sidx(s.y)]);
+    }
+    r += ring_at<S>(L, Rph, a, i, j, b) - ring_at<S>(L, Rph, b, i, j, a) - ring_at<S>(L, Rph, a, j, i, b) +
+         ring_at<S>(L, Rph, b, j, i, a);
+    R[L.t_off[ch] + e] = r;
+  }
+}
+template <typename S>
+void launch_rinit(const DevLayout &L, const S *T, const S *Vhp, const S *Rph, const S *i6off, const S *i7off, S *R, cudaStream_t st) {
+  if (L.nttile) k_rinit<S><<<L.nttile, 256, 0, st>>>(L, T, Vhp, Rph, i6off, i7off, R);
+}
+
+// ============================================================================
+// Update / energy / residual norm (diis_t1t2 :93-126, ccd_energy_save, and
+// ||R - D T||).  Partials: [E.re, E.im, |R-DT|^2] per block.  Dressed denominator
+// d2ij(i)+d2ij(j)-d2ab(a)-d2ab(b) in the reference's evaluation order.
+// ============================================================================
+template <typename S>
+__global__ void k_update(DevLayout L, int mode, S *__restrict__ T, const S *__restrict__ R, const S *__restrict__ Vhp,
+                         const S *__restrict__ d2ij, const S *__restrict__ d2ab, S *__restrict__ hist_t,
+                         S *__restrict__ hist_e, double *partial) {
+  const int2 tl = L.ttile[blockIdx.x];
+  const int ch = tl.x;
+  const int P = L.P[ch], H = L.H[ch];
+  const int64_t n = (int64_t)P * H;
+  const int64_t end = min((int64_t)tl.y + kTileElems, n);
+  double v[3] = {0.0, 0.0, 0.0};
+  const int A = L.A;
+  for (int64_t e = tl.y + threadIdx.x; e < end; e += blockDim.x) {
+    const int64_t g = L.t_off[ch] + e;
+    const S t = T[g];
+    const S vij = Vhp[g];
+    if (mode == 2) {
+      const S pr = t * vij;
+      v[0] += real_(pr);
+      v[1] += imag_(pr);
+      continue;
+    }
+    const int ab = (int)(e % P), ij = (int)(e / P);
+    const int2 po = L.pp_orb[L.pp_off[ch] + ab];
+    const int2 ho = L.hh_orb[L.hh_off[ch] + ij];
+    const S D = ((d2ij[ho.x] + d2ij[ho.y]) - d2ab[po.x - A]) - d2ab[po.y - A];
+    const S r = R[g];
+    v[2] += abs2(r - D * t);
+    S tn = t;
+    if (mode == 0) {
+      tn = 0.75 * t + 0.25 * (r / D);
+      T[g] = tn;
+      hist_t[g] = tn;
+    } else if (mode == 1) {
+      const S tj = r / D;
+      hist_t[g] = tj;
+      hist_e[g] = tj - t;
+    }
+    const S pr = tn * vij;
+    v[0] += real_(pr);
+    v[1] += imag_(pr);
+  }
+  block_partial<3>(v, partial);
+}
+template <typename S>
+void launch_update(const DevLayout &L, int mode, S *T, const S *R, const S *Vhp, const S *d2ij, const S *d2ab, S *hist_t,
+                   S *hist_e, double *partial, double *out4, cudaStream_t st) {
+  if (!L.nttile) return;
+  k_update<S><<<L.nttile, 256, 0, st>>>(L, mode, T, R, Vhp, d2ij, d2ab, hist_t, hist_e, partial);
+  finish(partial, L.nttile, 3, out4, st);
+}
+
+// ============================================================================
+// dot products and DIIS helpers
+// ============================================================================
+constexpr int kMaxDots = 16;
+template <typename S>
+struct PtrPack {
+  const S *p[kMaxDots];
+};
+
+template <typename S>
+__global__ void k_dots(int64_t n, const S *__restrict__ a, PtrPack<S> bs, int nb, int conj_a, double *partial) {
+  double v[2 * kMaxDots];
+#pragma unroll
+  for (int k = 0; k < 2 * kMaxDots; ++k) v[k] = 0.0;
+  for (int64_t x = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; x < n; x += (int64_t)gridDim.x * blockDim.x) {
+    const S av = conj_a ? conj_(a[x]) : a[x];
+#pragma unroll
+    for (int k = 0; k < kMaxDots; ++k) {
+      if (k < nb) {
+        const S pr = av * bs.p[k][x];
+        v[2 * k] += real_(pr);
+        v[2 * k + 1] += imag_(pr);
+      }
+    }
+  }
+  block_partial<2 * kMaxDots>(v, partial);
+}
+template <typename S>
+void launch_dots(int64_t n, const S *a, const S *const *bs, int nb, int conj_a, double *partial, double *out, cudaStream_t st) {
+  PtrPack<S> pk{};
+  for (int k = 0; k < nb && k < kMaxDots; ++k) pk.p[k] = bs[k];
+  const int blocks = 608;
+  k_dots<S><<<blocks, 256, 0, st>>>(n, a, pk, nb, conj_a, partial);
+  finish(partial, blocks, 2 * kMaxDots, out, st);
+}
+
+// Gram matrix of consecutive differences d_i = t_{i+1} - t_i, B_ij = sum d_i d_j
+// without conjugation (ccm_diis.f90:134-150).  Upper triangle, 2 doubles per entry.
+template <typename S>
+__global__ void k_diis_gram(int64_t n, PtrPack<S> cols, int nstep, double *partial) {
+  constexpr int MAXD = 5;
+  double v[2 * 15];
+#pragma unroll
+  for (int k = 0; k < 30; ++k) v[k] = 0.0;
+  const int nd = nstep - 1;
+  for (int64_t x = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; x < n; x += (int64_t)gridDim.x * blockDim.x) {
+    S d[MAXD];
+#pragma unroll
+    for (int i = 0; i < MAXD; ++i) d[i] = (i < nd) ? cols.p[i + 1][x] - cols.p[i][x] : S(0.0);
+    int k = 0;
+#pragma unroll
+    for (int i = 0; i < MAXD; ++i)
+#pragma unroll
+      for (int j = i; j < MAXD; ++j) {
+        const S pr = d[i] * d[j];
+        v[2 * k] += real_(pr);
+        v[2 * k + 1] += imag_(pr);
+        ++k;
+      }
+  }
+  block_partial<30>(v, partial);
+}
+template <typename S>
+void launch_diis_gram(int64_t n, const S *const *cols, int nstep, double *partial, double *out, cudaStream_t st) {
+  PtrPack<S> pk{};
+  for (int k = 0; k < nstep && k < kMaxDots; ++k) pk.p[k] = cols[k];
+  const int blocks = 608;
+  k_diis_gram<S><<<blocks, 256, 0, st>>>(n, pk, nstep, partial);
+  finish(partial, blocks, 30, out, st);
+}
+
+template <typename S>
+struct CoefPack {
+  double re[kMaxDots], im[kMaxDots];
+};
+template <typename S>
+__global__ void k_combine(int64_t n, PtrPack<S> xs, CoefPack<S> c, int m, S *y) {
+  for (int64_t x = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; x < n; x += (int64_t)gridDim.x * blockDim.x) {
+    S acc = S(0.0);
+    for (int i = 0; i < m; ++i) acc += make_scalar<S>(c.re[i], c.im[i]) * xs.p[i][x];
+    y[x] = acc;
+  }
+}
+template <typename S>
+void launch_combine(int64_t n, const S *const *xs, const double *coef, int m, S *y, cudaStream_t st) {
+  PtrPack<S> pk{};
+  CoefPack<S> c{};
+  for (int k = 0; k < m && k < kMaxDots; ++k) {
+    pk.p[k] = xs[k];
+    c.re[k] = coef[2 * k];
+    c.im[k] = coef[2 * k + 1];
+  }
+  k_combine<S><<<1216, 256, 0, st>>>(n, pk, c, m, y);
+}
+
+// ============================================================================
+// Interaction blocks handed over in the reference's ordered layout
+// ============================================================================
+// kind 3: V_hhpp(n_hh, n_pp) -> Vhp'(ij', ab') at [ij'*P + ab']
+// kind 6: V_pppp(n_pp, n_pp) -> Vpp'(ab', cd') at [ab'*P + cd']
+// kind 1: V_hhhh(n_hh, n_hh) of the matching hhhh channel -> Vhh'(kl', ij') col-major
+template <typename S>
+__global__ void k_pack_vblock(DevLayout L, int kind, int ch, int n_rows, const double *__restrict__ stage,
+                              S *__restrict__ dst, int *flag) {
+  const int P = L.P[ch], H = L.H[ch];
+  int64_t n;
+  if (kind == 3) n = (int64_t)H * P;
+  else if (kind == 6) n = (int64_t)P * P;
+  else n = (int64_t)H * H;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+    int64_t src, o;
+    if (kind == 3) {
+      const int ij = (int)(e / P), ab = (int)(e % P);
+      src = L.hh_row[L.hh_off[ch] + ij] + (int64_t)n_rows * L.pp_row[L.pp_off[ch] + ab];
+      o = L.t_off[ch] + e;
+    } else if (kind == 6) {
+      const int r = (int)(e / P), c = (int)(e % P);
+      src = L.pp_row[L.pp_off[ch] + r] + (int64_t)n_rows * L.pp_row[L.pp_off[ch] + c];
+      o = L.vpp_off[ch] + e;
+    } else {
+      const int r = (int)(e % H), c = (int)(e / H);
+      src = L.hh_row[L.hh_off[ch] + r] + (int64_t)n_rows * L.hh_row[L.hh_off[ch] + c];
+      o = L.hh2_off[ch] + e;
+    }
+    dst[o] = cvt_in<S>(stage + 2 * src, flag);
+  }
+}
+template <typename S>
+void launch_pack_vblock(const DevLayout &L, int kind, int ch, int n_rows, const double *stage, S *dst, int *flag, cudaStream_t st) {
+  k_pack_vblock<S><<<1216, 256, 0, st>>>(L, kind, ch, n_rows, stage, dst, flag);
+}
+
+// W(ia, jb) = -V_hphp(ib, ja), the constant part of I4 (ccm_t2_eqn.f90:740-780)
+template <typename S>
+__global__ void k_build_w(DevLayout L, const int2 *__restrict__ hp4_slot, const int64_t *__restrict__ v4_off,
+                          const int *__restrict__ n4, const double *__restrict__ v4, S *__restrict__ W, int *flag) {
+  for (int q = blockIdx.x; q < L.nph; q += gridDim.x) {
+    const int nhp = L.n_hp[q];
+    const int64_t n = (int64_t)nhp * nhp;
+    for (int64_t e = threadIdx.x; e < n; e += blockDim.x) {
+      const int r = (int)(e % nhp), c = (int)(e / nhp);
+      const int2 ia = L.hp_orb[L.hp_off[q] + r];
+      const int2 jb = L.hp_orb[L.hp_off[q] + c];
+      const int2 sib = hp4_slot[(int64_t)ia.x * L.NP + (jb.y - L.A)];
+      const int2 sja = hp4_slot[(int64_t)jb.x * L.NP + (ia.y - L.A)];
+      S w = S(0.0);
+      if (sib.x >= 0 && sja.x >= 0) {
+        const int c4 = sib.x;
+        const S v = cvt_in<S>(v4 + 2 * (v4_off[c4] + sib.y + (int64_t)n4[c4] * sja.y), flag);
+        w = S(0.0) - v;
+      }
+      W[L.i4_off[q] + e] = w;
+    }
+  }
+}
+template <typename S>
+void launch_build_w(const DevLayout &L, const int2 *hp4_slot, const int64_t *v4_off, const int *n4, const double *v4, S *W,
+                    int *flag, cudaStream_t st) {
+  if (L.nph) k_build_w<S><<<min(L.nph, 4096), 256, 0, st>>>(L, hp4_slot, v4_off, n4, v4, W, flag);
+}
+
+// V_ph(ia, bj) = V(ij, ab): the `amat` gather of ccm_t2_eqn.f90:694-716, done once
+template <typename S>
+__global__ void k_build_vph(DevLayout L, const S *__restrict__ Vhp, S *__restrict__ Vph) {
+  for (int q = blockIdx.x; q < L.nph; q += gridDim.x) {
+    const int nhp = L.n_hp[q], nph = L.n_ph[q];
+    const int64_t n = (int64_t)nhp * nph;
+    for (int64_t e = threadIdx.x; e < n; e += blockDim.x) {
+      const int r = (int)(e % nhp), c = (int)(e / nhp);
+      const int2 ia = L.hp_orb[L.hp_off[q] + r];
+      const int2 bj = L.ph_orb[L.ph_off[q] + c];
+      const int2 sij = L.hh_slot[ia.x * L.A + bj.y];
+      const int2 sab = L.pp_slot[(int64_t)(ia.y - L.A) * L.NP + (bj.x - L.A)];
+      S v = S(0.0);
+      if (sij.y && sab.y) {
+        const int ch = sij.x;
+        v = (ssign(sij.y) * ssign(sab.y)) * Vhp[L.t_off[ch] + (int64_t)sidx(sij.y) * L.P[ch] + sidx(sab.y)];
+      }
+      Vph[L.vph_off[q] + e] = v;
+    }
+  }
+}
+template <typename S> void launch_build_vph(const DevLayout &L, const S *Vhp, S *Vph, cudaStream_t st) {
+  if (L.nph) k_build_vph<S><<<min(L.nph, 4096), 256, 0, st>>>(L, Vhp, Vph);
+}
+
+// ============================================================================
+// Device potentials (generation of every block on the GPU)
+// ============================================================================
+
+
+template <typename S>
+__global__ void k_gen_tblocks(DevLayout L, DevOrbits O, DevPotential P, S *Vhp) {
+  const int2 tl = L.ttile[blockIdx.x];
+  const int ch = tl.x, Pc = L.P[ch], H = L.H[ch];
+  const int64_t n = (int64_t)Pc * H, end = min((int64_t)tl.y + kTileElems, n);
+  for (int64_t e = tl.y + threadIdx.x; e < end; e += blockDim.x) {
+    const int ij = (int)(e / Pc), ab = (int)(e % Pc);  // Vhp'(ij', ab') at ij'*P + ab'
+    const int2 h = L.hh_orb[L.hh_off[ch] + ij], p = L.pp_orb[L.pp_off[ch] + ab];
+    Vhp[L.t_off[ch] + e] = pot::vanti<S>(O, P, h.x, h.y, p.x, p.y);
+  }
+}
+template <typename S>
+__global__ void k_gen_vpp(DevLayout L, DevOrbits O, DevPotential P, S *Vpp) {
+  const int2 tl = L.vtile[blockIdx.x];
+  const int ch = tl.x, Pc = L.P[ch];
+  const int64_t n = (int64_t)Pc * Pc, end = min((int64_t)tl.y + kTileElems, n);
+  for (int64_t e = tl.y + threadIdx.x; e < end; e += blockDim.x) {
+    const int r = (int)(e / Pc), c = (int)(e % Pc);
+    const int2 x = L.pp_orb[L.pp_off[ch] + r], y = L.pp_orb[L.pp_off[ch] + c];
+    Vpp[L.vpp_off[ch] + e] = pot::vanti<S>(O, P, x.x, x.y, y.x, y.y);
+  }
+}
+template <typename S>
+__global__ void k_gen_vhh(DevLayout L, DevOrbits O, DevPotential P, S *Vhh) {
+  for (int ch = blockIdx.x; ch < L.nch; ch += gridDim.x) {
+    const int H = L.H[ch];
+    for (int e = threadIdx.x; e < H * H; e += blockDim.x) {
+      const int r = e % H, c = e / H;
+      const int2 x = L.hh_orb[L.hh_off[ch] + r], y = L.hh_orb[L.hh_off[ch] + c];
+      Vhh[L.hh2_off[ch] + e] = pot::vanti<S>(O, P, x.x, x.y, y.x, y.y);
+    }
+  }
+}
+template <typename S>
+__global__ void k_gen_w(DevLayout L, DevOrbits O, DevPotential P, S *W) {
+  for (int q = blockIdx.x; q < L.nph; q += gridDim.x) {
+    const int nhp = L.n_hp[q];
+    for (int64_t e = threadIdx.x; e < (int64_t)nhp * nhp; e += blockDim.x) {
+      const int r = (int)(e % nhp), c = (int)(e / nhp);
+      const int2 ia = L.hp_orb[L.hp_off[q] + r], jb = L.hp_orb[L.hp_off[q] + c];
+      W[L.i4_off[q] + e] = S(0.0) - pot::vanti<S>(O, P, ia.x, jb.y, jb.x, ia.y);
+    }
+  }
+}
+// Fock pieces: f(p,p), f(x, partner) for particles, f(partner, y) for holes;
+// normal_ordered_hamiltonian, ccm_main.f90:1586-1657.  E0 :1661-1684.
+template <typename S>
+__global__ void k_gen_fock(DevLayout L, DevOrbits O, DevPotential P, S *fdiag, S *f6, S *f7) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= L.ns) return;
+  S d = S(O.e[p]);
+  for (int h = 0; h < L.A; ++h) d += pot::vanti<S>(O, P, h, p, h, p);
+  fdiag[p] = d;
+  const int pb = L.partner[p];
+  if (p >= L.A) {
+    S o = S(0.0);
+    if (pb >= L.A)
+      for (int h = 0; h < L.A; ++h) o += pot::vanti<S>(O, P, h, p, h, pb);
+    f6[p - L.A] = o;
+  } else {
+    S o = S(0.0);
+    if (pb >= 0 && pb < L.A)
+      for (int h = 0; h < L.A; ++h) o += pot::vanti<S>(O, P, h, pb, h, p);
+    f7[p] = o;
+  }
+}
+template <typename S>
+__global__ void k_gen_e0(DevLayout L, DevOrbits O, DevPotential P, double *e0) {
+  double v[2] = {0.0, 0.0};
+  for (int x = threadIdx.x; x < L.A * L.A; x += blockDim.x) {
+    const int i = x / L.A, j = x % L.A;
+    const S w = pot::vanti<S>(O, P, i, j, i, j);
+    v[0] += 0.5 * real_(w);
+    v[1] += 0.5 * imag_(w);
+  }
+  for (int i = threadIdx.x; i < L.A; i += blockDim.x) v[0] += O.e[i];
+  block_partial<2>(v, e0);
+}
+
+template <typename S>
+void launch_generate(const DevLayout &L, const DevOrbits &O, const DevPotential &pot, S *Vhp, S *Vpp, S *Vhh, S *W,
+                     S *fdiag, S *f6, S *f7, double *e0, cudaStream_t st) {
+  if (L.nttile) k_gen_tblocks<S><<<L.nttile, 256, 0, st>>>(L, O, pot, Vhp);
+  if (L.nvtile) k_gen_vpp<S><<<L.nvtile, 256, 0, st>>>(L, O, pot, Vpp);
+  if (L.nch) k_gen_vhh<S><<<min(L.nch, 4096), 128, 0, st>>>(L, O, pot, Vhh);
+  if (L.nph) k_gen_w<S><<<min(L.nph, 4096), 128, 0, st>>>(L, O, pot, W);
+  k_gen_fock<S><<<(L.ns + 127) / 128, 128, 0, st>>>(L, O, pot, fdiag, f6, f7);
+  k_gen_e0<S><<<1, 256, 0, st>>>(L, O, pot, e0);
+}
+
+// MP2, setup_t_amplitudes (ccm_iter.f90:2355-2368): T = conj(V(ij,ab)) / (f_ii+f_jj-f_aa-f_bb)
+template <typename S>
+__global__ void k_mp2(DevLayout L, const S *__restrict__ Vhp, const S *__restrict__ fd, S *__restrict__ T) {
+  const int2 tl = L.ttile[blockIdx.x];
+  const int ch = tl.x, P = L.P[ch], H = L.H[ch];
+  const int64_t n = (int64_t)P * H, end = min((int64_t)tl.y + kTileElems, n);
+  for (int64_t e = tl.y + threadIdx.x; e < end; e += blockDim.x) {
+    const int ab = (int)(e % P), ij = (int)(e / P);
+    const int2 po = L.pp_orb[L.pp_off[ch] + ab], ho = L.hh_orb[L.hh_off[ch] + ij];
+    const S den = ((S(0.0) - fd[po.x]) - fd[po.y] + fd[ho.x]) + fd[ho.y];
+    const int64_t g = L.t_off[ch] + e;
+    T[g] = (abs2(den) == 0.0) ? S(0.0) : conj_(Vhp[g]) / den;
+  }
+}
+template <typename S> void launch_mp2(const DevLayout &L, const S *Vhp, const S *fdiag, S *T, cudaStream_t st) {
+  if (L.nttile) k_mp2<S><<<L.nttile, 256, 0, st>>>(L, Vhp, fdiag, T);
+}
+
+// ordered (n_pp x n_hh) block <-> packed block
+template <typename S>
+__global__ void k_pack_t(DevLayout L, int ch, int n_pp, const double *__restrict__ stage, S *T, int *flag) {
+  const int P = L.P[ch], H = L.H[ch];
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < (int64_t)P * H; e += (int64_t)gridDim.x * blockDim.x) {
+    const int ab = (int)(e % P), ij = (int)(e / P);
+    const int64_t src = L.pp_row[L.pp_off[ch] + ab] + (int64_t)n_pp * L.hh_row[L.hh_off[ch] + ij];
+    T[L.t_off[ch] + e] = cvt_in<S>(stage + 2 * src, flag);
+  }
+}
+template <typename S> void launch_pack_t(const DevLayout &L, int ch, int n_pp, const double *stage, S *T, int *flag, cudaStream_t st) {
+  k_pack_t<S><<<608, 256, 0, st>>>(L, ch, n_pp, stage, T, flag);
+}
+template <typename S>
+__global__ void k_unpack_t(DevLayout L, int ch, int n_pp, const int *__restrict__ pp_signed, const int *__restrict__ hh_signed,
+                            int n_hh, const S *__restrict__ T, double *stage) {
+  const int P = L.P[ch];
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < (int64_t)n_pp * n_hh; e += (int64_t)gridDim.x * blockDim.x) {
+    const int r = (int)(e % n_pp), c = (int)(e / n_pp);
+    const int sp = pp_signed[r], sh = hh_signed[c];
+    S v = S(0.0);
+    if (sp && sh) v = (ssign(sp) * ssign(sh)) * T[L.t_off[ch] + sidx(sp) + (int64_t)P * sidx(sh)];
+    stage[2 * e] = real_(v);
+    stage[2 * e + 1] = imag_(v);
+  }
+}
+template <typename S>
+void launch_unpack_t(const DevLayout &L, int ch, int n_pp, const int *pp_signed, const int *hh_signed, int n_hh, const S *T,
+                     double *stage, cudaStream_t st) {
+  k_unpack_t<S><<<608, 256, 0, st>>>(L, ch, n_pp, pp_signed, hh_signed, n_hh, T, stage);
+}
+
+// ---- explicit instantiations -------------------------------------------------
+#define CCX_INST(S)                                                                                                    \
+  template void launch_gemm<S>(const GemmProb<S> *, const GemmTile *, int, cudaStream_t);                              \
+  template void launch_gather_tph<S>(const DevLayout &, const S *, S *, cudaStream_t);                                 \
+  template void launch_i7<S>(const DevLayout &, const S *, const S *, const S *, S *, S *, cudaStream_t);             \
+  template void launch_i9<S>(const DevLayout &, int64_t, const S *, const S *, S *, cudaStream_t);                     \
+  template void launch_i6<S>(const DevLayout &, const S *, const S *, const S *, const S *, S *, S *, cudaStream_t);  \
+  template void launch_rinit<S>(const DevLayout &, const S *, const S *, const S *, const S *, const S *, S *,         \
+                                cudaStream_t);                                                                         \
+  template void launch_update<S>(const DevLayout &, int, S *, const S *, const S *, const S *, const S *, S *, S *,    \
+                                 double *, double *, cudaStream_t);                                                    \
+  template void launch_dots<S>(int64_t, const S *, const S *const *, int, int, double *, double *, cudaStream_t);     \
+  template void launch_diis_gram<S>(int64_t, const S *const *, int, double *, double *, cudaStream_t);                \
+  template void launch_combine<S>(int64_t, const S *const *, const double *, int, S *, cudaStream_t);                 \
+  template void launch_pack_vblock<S>(const DevLayout &, int, int, int, const double *, S *, int *, cudaStream_t);    \
+  template void launch_build_w<S>(const DevLayout &, const int2 *, const int64_t *, const int *, const double *, S *,  \
+                                  int *, cudaStream_t);                                                                \
+  template void launch_build_vph<S>(const DevLayout &, const S *, S *, cudaStream_t);                                 \
+  template void launch_generate<S>(const DevLayout &, const DevOrbits &, const DevPotential &, S *, S *, S *, S *,    \
+                                   S *, S *, S *, double *, cudaStream_t);                                             \
+  template void launch_mp2<S>(const DevLayout &, const S *, const S *, S *, cudaStream_t);                            \
+  template void launch_pack_t<S>(const DevLayout &, int, int, const double *, S *, int *, cudaStream_t);          \
+  template void launch_unpack_t<S>(const DevLayout &, int, int, const int *, const int *, int, const S *, double *,   \
+                                   cudaStream_t);
+
+CCX_INST(double)
+CCX_INST(cplx)
+
+}  // namespace ccx

@@ -1,0 +1,87 @@
+// Host-callable launchers of the CCD kernels (implemented in kernels.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "common.cuh"
+#include "devlayout.hpp"
+
+namespace ccx {
+
+// ---- grouped GEMM (FP64 / complex FP64) ------------------------------------
+// C(m,n) [+]= sum_s alpha_s * sum_k A_s(m,k) B_s(k,n), element strides per operand.
+template <typename S>
+struct GemmSeg {
+  const S *A, *B;
+  int64_t sAm, sAk, sBk, sBn;
+  int K;
+  double alpha;
+};
+template <typename S>
+struct GemmProb {
+  GemmSeg<S> seg[2];
+  int nseg;
+  int M, N;
+  S *C;
+  const S *C0;  // initial value when accumulate == 0 (nullptr: zero)
+  int64_t sCm, sCn;
+  int accumulate;
+};
+struct GemmTile {
+  int prob, m0, n0, pad;
+};
+constexpr int kGemmBM = 64, kGemmBN = 64, kGemmBK = 16;
+
+template <typename S>
+void launch_gemm(const GemmProb<S> *probs, const GemmTile *tiles, int ntiles, cudaStream_t st);
+
+// ---- potentials -----------------------------------------------------------
+struct DevPotential {
+  int kind;            // 0 Minnesota, 1 chiral-like
+  int f32_literals;
+  double lec[9];       // CS, CT, C1..C7 (MeV units)
+};
+
+// ---- residual pieces --------------------------------------------------------
+template <typename S> void launch_gather_tph(const DevLayout &L, const S *T, S *Tph, cudaStream_t st);
+template <typename S> void launch_i7(const DevLayout &L, const S *X, const S *fdiag, const S *f7, S *d2ij, S *i7off, cudaStream_t st);
+template <typename S> void launch_i9(const DevLayout &L, int64_t n, const S *Vhh, const S *X, S *I9, cudaStream_t st);
+template <typename S> void launch_i6(const DevLayout &L, const S *T, const S *Vhp, const S *fdiag, const S *f6, S *d2ab, S *i6off, cudaStream_t st);
+template <typename S> void launch_rinit(const DevLayout &L, const S *T, const S *Vhp, const S *Rph, const S *i6off, const S *i7off, S *R, cudaStream_t st);
+
+// ---- update / energy / norms (per-block partial sums, then a fixed-order finish) --
+// mode 0: reference update T <- 0.75 T + 0.25 R/D, history column written
+// mode 1: Jacobi T_jac = R/D into hist_t, step into hist_e, T untouched
+// mode 2: energy only (no update); mode 3: residual norm + energy, no update
+template <typename S>
+void launch_update(const DevLayout &L, int mode, S *T, const S *R, const S *Vhp, const S *d2ij, const S *d2ab,
+                   S *hist_t, S *hist_e, double *partial, double *out4, cudaStream_t st);
+// dot products: out[j] = sum_x w(a[x]) * b_j[x] for j < nb; conj on a when conj_a
+template <typename S>
+void launch_dots(int64_t n, const S *a, const S *const *bs, int nb, int conj_a, double *partial, double *out, cudaStream_t st);
+// reference DIIS Gram matrix of differences of nstep history columns (no conjugation)
+template <typename S>
+void launch_diis_gram(int64_t n, const S *const *cols, int nstep, double *partial, double *out, cudaStream_t st);
+// y = sum_i c_i x_i
+template <typename S>
+void launch_combine(int64_t n, const S *const *xs, const double *coef /* host, 2 per term */, int m, S *y, cudaStream_t st);
+
+// ---- interaction -----------------------------------------------------------
+template <typename S>
+void launch_pack_vblock(const DevLayout &L, int kind, int ch, int n_rows, const double *stage, S *dst, int *flag, cudaStream_t st);
+template <typename S>
+void launch_build_w(const DevLayout &L, const int2 *hp4_slot, const int64_t *v4_off, const int *n4, const double *v4,
+                    S *W, int *flag, cudaStream_t st);
+template <typename S> void launch_build_vph(const DevLayout &L, const S *Vhp, S *Vph, cudaStream_t st);
+template <typename S>
+void launch_generate(const DevLayout &L, const DevOrbits &O, const DevPotential &pot, S *Vhp, S *Vpp, S *Vhh, S *W,
+                     S *fdiag, S *f6, S *f7, double *e0, cudaStream_t st);
+template <typename S> void launch_mp2(const DevLayout &L, const S *Vhp, const S *fdiag, S *T, cudaStream_t st);
+template <typename S> void launch_pack_t(const DevLayout &L, int ch, int n_pp, const double *stage, S *T, int *flag, cudaStream_t st);
+template <typename S>
+void launch_unpack_t(const DevLayout &L, int ch, int n_pp, const int *pp_signed, const int *hh_signed, int n_hh, const S *T,
+                     double *stage, cudaStream_t st);
+
+}  // namespace ccx

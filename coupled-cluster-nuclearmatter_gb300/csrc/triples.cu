@@ -1,0 +1,415 @@
+// Perturbative triples (T): pert_triples2 (ccm_triples.f90:528-735) with its two
+// helpers three_body_oneparticle_1 (:174-232) and three_body_onehole_1 (:238-294),
+// over the triple channels of setup_t3_channel_structures
+// (ccm_t3full_channels.f90:4-284).  One thread per (abc, ijk) pair; the FP64 sum of
+// conj(W) W / D is reduced per block and finished in a fixed order.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <stdexcept>
+#include <vector>
+
+#include "common.cuh"
+#include "engine.hpp"
+#include "potential.cuh"
+#include "triples.hpp"
+
+namespace ccx {
+
+namespace {
+
+void tck(cudaError_t e, const char *what) {
+  if (e != cudaSuccess) throw EngineError(2, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+struct TriplesDev {
+  int ns, A, NP, nk0, nk1, nk2, tzmin, tzmax;
+  const int *orbit_of;                 // (nx, ny, nz, spin, isospin) -> orbital or -1
+  const int *nx, *ny, *nz, *tz;
+  const int2 *hp5_slot, *pp5_slot;     // hppp blocks: (channel, row) / (channel, column)
+  const int64_t *v5_off;
+  const int *n5;                       // rows of each hppp block
+  const int2 *hh2_slot, *hp2_slot;     // hhhp blocks: (channel, row) / (channel, column)
+  const int64_t *v2_off;
+  const int *n2;
+  int nt3;
+  const int64_t *elem_off;             // prefix of n_hhh * n_ppp over triple channels
+  const int *nbra;                     // n_hhh per channel
+  const int64_t *hhh_off, *ppp_off;
+  const int3 *hhh, *ppp;
+};
+
+__device__ inline int t_orbitof(const TriplesDev &D, int x, int y, int z, int s, int t) {
+  if (x < -D.nk0 || x > D.nk0 || y < -D.nk1 || y > D.nk1 || z < -D.nk2 || z > D.nk2) return -1;
+  if (t < D.tzmin || t > D.tzmax) return -1;
+  const int ey = 2 * D.nk1 + 1, ez = 2 * D.nk2 + 1;
+  const size_t idx = ((((size_t)(x + D.nk0) * ey + (y + D.nk1)) * ez + (z + D.nk2)) * 2 + (s > 0)) * 2 + (t > 0);
+  return D.orbit_of[idx];
+}
+
+template <typename S>
+__device__ inline S t2_at(const DevLayout &L, const S *T, int a, int b, int i, int j) {
+  const int2 sab = L.pp_slot[(int64_t)(a - L.A) * L.NP + (b - L.A)];
+  const int2 sij = L.hh_slot[i * L.A + j];
+  if (sab.y == 0 || sij.y == 0) return S(0.0);
+  const int ch = sab.x;
+  return (ssign(sab.y) * ssign(sij.y)) * T[L.t_off[ch] + sidx(sab.y) + (int64_t)L.P[ch] * sidx(sij.y)];
+}
+
+// sum_d conj(<cb|V|kd>) T(ad, ij)
+template <typename S>
+__device__ S one_particle(const TriplesDev &D, const DevLayout &L, const S *T, const S *V5, int a, int b, int c, int i,
+                          int j, int k) {
+  const int nxd = D.nx[i] + D.nx[j] - D.nx[a], nyd = D.ny[i] + D.ny[j] - D.ny[a];
+  const int nzd = D.nz[i] + D.nz[j] - D.nz[a], tzd = D.tz[i] + D.tz[j] - D.tz[a];
+  S sum = S(0.0);
+  if (abs(nxd) > D.nk0 || abs(nyd) > D.nk1 || abs(nzd) > D.nk2 || abs(tzd) > 1) return sum;
+  for (int sd = -1; sd <= 1; sd += 2) {
+    const int d = t_orbitof(D, nxd, nyd, nzd, sd, tzd);
+    if (d < D.A) continue;
+    const S t = t2_at<S>(L, T, a, d, i, j);
+    const int2 r = D.hp5_slot[(int64_t)k * D.NP + (d - D.A)];
+    const int2 cl = D.pp5_slot[(int64_t)(c - D.A) * D.NP + (b - D.A)];
+    if (r.x < 0 || cl.x < 0) continue;
+    const S v = V5[D.v5_off[r.x] + r.y + (int64_t)D.n5[r.x] * cl.y];
+    sum += conj_(v) * t;
+  }
+  return sum;
+}
+
+// sum_l conj(<jk|V|lc>) T(ab, il)
+template <typename S>
+__device__ S one_hole(const TriplesDev &D, const DevLayout &L, const S *T, const S *V2, int a, int b, int c, int i, int j,
+                      int k) {
+  const int nxl = D.nx[k] + D.nx[j] - D.nx[c], nyl = D.ny[k] + D.ny[j] - D.ny[c];
+  const int nzl = D.nz[k] + D.nz[j] - D.nz[c], tzl = D.tz[k] + D.tz[j] - D.tz[c];
+  S sum = S(0.0);
+  if (abs(nxl) > D.nk0 || abs(nyl) > D.nk1 || abs(nzl) > D.nk2 || abs(tzl) > 1) return sum;
+  for (int sl = -1; sl <= 1; sl += 2) {
+    const int l = t_orbitof(D, nxl, nyl, nzl, sl, tzl);
+    if (l < 0 || l >= D.A) continue;
+    const S t = t2_at<S>(L, T, a, b, i, l);
+    const int2 r = D.hh2_slot[j * D.A + k];
+    const int2 cl = D.hp2_slot[(int64_t)l * D.NP + (c - D.A)];
+    if (r.x < 0 || cl.x < 0) continue;
+    const S v = V2[D.v2_off[r.x] + r.y + (int64_t)D.n2[r.x] * cl.y];
+    sum += conj_(v) * t;
+  }
+  return sum;
+}
+
+template <int NV>
+__device__ void block_sum(double (&v)[NV], double *partial) {
+  __shared__ double red[NV][32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int k = 0; k < NV; ++k) {
+    double x = warp_sum(v[k]);
+    if (lane == 0) red[k][wid] = x;
+  }
+  __syncthreads();
+  if (wid == 0)
+    for (int k = 0; k < NV; ++k) {
+      double x = lane < nw ? red[k][lane] : 0.0;
+      x = warp_sum(x);
+      if (lane == 0) partial[(int64_t)blockIdx.x * NV + k] = x;
+    }
+}
+
+template <typename S>
+__global__ void __launch_bounds__(256) k_triples(TriplesDev D, DevLayout L, const S *__restrict__ T,
+                                                 const S *__restrict__ V5, const S *__restrict__ V2,
+                                                 const S *__restrict__ fd, int64_t total, double *partial) {
+  double acc[2] = {0.0, 0.0};
+  int ch = 0;
+  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < total; g += (int64_t)gridDim.x * blockDim.x) {
+    while (g >= D.elem_off[ch + 1]) ++ch;
+    const int64_t loc = g - D.elem_off[ch];
+    const int nb = D.nbra[ch];
+    const int ket = (int)(loc / nb), bra = (int)(loc % nb);
+    const int3 abc = D.ppp[D.ppp_off[ch] + ket];
+    const int3 ijk = D.hhh[D.hhh_off[ch] + bra];
+    const int a = abc.x, b = abc.y, c = abc.z, i = ijk.x, j = ijk.y, k = ijk.z;
+    const S spen = fd[i] + fd[j] + fd[k] - fd[a] - fd[b] - fd[c];
+    S tc = one_particle<S>(D, L, T, V5, a, b, c, i, j, k) - one_particle<S>(D, L, T, V5, b, a, c, i, j, k) -
+           one_particle<S>(D, L, T, V5, c, b, a, i, j, k) - one_particle<S>(D, L, T, V5, a, b, c, k, j, i) -
+           one_particle<S>(D, L, T, V5, a, b, c, i, k, j) + one_particle<S>(D, L, T, V5, c, b, a, i, k, j) +
+           one_particle<S>(D, L, T, V5, c, b, a, k, j, i) + one_particle<S>(D, L, T, V5, b, a, c, i, k, j) +
+           one_particle<S>(D, L, T, V5, b, a, c, k, j, i);
+    const S th = one_hole<S>(D, L, T, V2, a, b, c, i, j, k) - one_hole<S>(D, L, T, V2, a, c, b, i, j, k) -
+                 one_hole<S>(D, L, T, V2, c, b, a, i, j, k) - one_hole<S>(D, L, T, V2, a, b, c, k, j, i) -
+                 one_hole<S>(D, L, T, V2, a, b, c, j, i, k) + one_hole<S>(D, L, T, V2, c, b, a, j, i, k) +
+                 one_hole<S>(D, L, T, V2, c, b, a, k, j, i) + one_hole<S>(D, L, T, V2, a, c, b, j, i, k) +
+                 one_hole<S>(D, L, T, V2, a, c, b, k, j, i);
+    tc = tc - th;
+    const S term = (conj_(tc) * tc) / spen;
+    acc[0] += real_(term);
+    acc[1] += imag_(term);
+  }
+  block_sum<2>(acc, partial);
+}
+
+__global__ void k_finish2(const double *partial, int nb, double *out) {
+  const int k = blockIdx.x;
+  double s = 0.0;
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) s += partial[(int64_t)b * 2 + k];
+  __shared__ double red[32];
+  s = warp_sum(s);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double x = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+    x = warp_sum(x);
+    if (threadIdx.x == 0) out[k] = x;
+  }
+}
+
+// generation of the V_hppp / V_hhhp blocks (setup_vnn_hppp_block NN part, ccm_iter.f90:1720-1760;
+// V_hhhp as ccm_iter.f90:885-930): vnn_hppp(kl, ij) = <ij|V|kl>, vnn_hhhp(ij, kd) = <ij|V|kd>
+template <typename S>
+__global__ void k_gen_block(DevOrbits O, DevPotential P, const int2 *__restrict__ rows, const int2 *__restrict__ cols,
+                            const int64_t *__restrict__ off, const int *__restrict__ nr, const int *__restrict__ nc,
+                            const int *__restrict__ roff, const int *__restrict__ coff, int nchan, int rows_are_ket,
+                            S *__restrict__ V) {
+  for (int ch = blockIdx.x; ch < nchan; ch += gridDim.x) {
+    const int r = nr[ch], c = nc[ch];
+    for (int64_t e = threadIdx.x; e < (int64_t)r * c; e += blockDim.x) {
+      const int ri = (int)(e % r), ci = (int)(e / r);
+      const int2 x = rows[roff[ch] + ri], y = cols[coff[ch] + ci];
+      V[off[ch] + e] = rows_are_ket ? pot::vanti<S>(O, P, y.x, y.y, x.x, x.y) : pot::vanti<S>(O, P, x.x, x.y, y.x, y.y);
+    }
+  }
+}
+
+template <typename S> __device__ inline S in_cvt(const double *p);
+template <> __device__ inline double in_cvt<double>(const double *p) { return p[0]; }
+template <> __device__ inline cplx in_cvt<cplx>(const double *p) { return cplx(p[0], p[1]); }
+template <typename S>
+__global__ void k_copy_in(const double *__restrict__ src, int64_t n, S *__restrict__ dst) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
+    dst[e] = in_cvt<S>(src + 2 * e);
+}
+
+struct DB {
+  void *p = nullptr;
+  size_t n = 0;
+  ~DB() { if (p) cudaFree(p); }
+  template <typename T> void put(const std::vector<T> &h) {
+    n = std::max<size_t>(h.size(), 1) * sizeof(T);
+    tck(cudaMalloc(&p, n), "cudaMalloc (T)");
+    if (!h.empty()) tck(cudaMemcpy(p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice), "upload (T)");
+  }
+  void zeros(size_t bytes) {
+    n = std::max<size_t>(bytes, 1);
+    tck(cudaMalloc(&p, n), "cudaMalloc (T)");
+    tck(cudaMemset(p, 0, n), "memset (T)");
+  }
+  template <typename T> T *as() const { return (T *)p; }
+};
+
+}  // namespace
+
+template <typename S>
+class Triples final : public ITriples<S> {
+ public:
+  Triples(const Layout &L, const DevLayout &D, const DevOrbits &O, int device) : D_(D), O_(O) {
+    tck(cudaSetDevice(device), "cudaSetDevice");
+    const Basis &B = L.b;
+    const int ns = B.ns, A = B.A, NP = ns - A;
+    TD_.ns = ns; TD_.A = A; TD_.NP = NP;
+    TD_.nk0 = B.nkmax[0]; TD_.nk1 = B.nkmax[1]; TD_.nk2 = B.nkmax[2];
+    TD_.tzmin = B.tzmin; TD_.tzmax = B.tzmax;
+    orbit_of_.put(B.orbit_of);
+    TD_.orbit_of = orbit_of_.as<int>();
+    TD_.nx = O.nx; TD_.ny = O.ny; TD_.nz = O.nz; TD_.tz = O.tz;
+    // hppp (kind 5) and hhhp (kind 2) blocks in the reference's ordered layout
+    auto blocks = [&](int kind, std::vector<int2> &s1slot, std::vector<int2> &s2slot, bool s1_is_hh, DB &off, DB &nrow,
+                      std::vector<int64_t> &offh, std::vector<int2> &rows, std::vector<int2> &cols, std::vector<int> &nr,
+                      std::vector<int> &nc, std::vector<int> &roff, std::vector<int> &coff) {
+      const ChannelFamily &F = L.fam[kind];
+      int64_t acc = 0;
+      for (int c = 0; c < F.count(); ++c) {
+        const PairList &a = F.side1[c], &b = F.side2[c];
+        offh.push_back(acc);
+        nr.push_back(a.size());
+        nc.push_back(b.size());
+        roff.push_back((int)rows.size());
+        coff.push_back((int)cols.size());
+        acc += (int64_t)a.size() * b.size();
+        for (int r = 0; r < a.size(); ++r) {
+          rows.push_back(make_int2(a.p[r], a.q[r]));
+          if (s1_is_hh) s1slot[(size_t)a.p[r] * A + a.q[r]] = make_int2(c, r);
+          else s1slot[(size_t)a.p[r] * NP + (a.q[r] - A)] = make_int2(c, r);
+        }
+        for (int r = 0; r < b.size(); ++r) {
+          cols.push_back(make_int2(b.p[r], b.q[r]));
+          if (kind == 5) s2slot[(size_t)(b.p[r] - A) * NP + (b.q[r] - A)] = make_int2(c, r);
+          else s2slot[(size_t)b.p[r] * NP + (b.q[r] - A)] = make_int2(c, r);
+        }
+      }
+      off.put(offh);
+      nrow.put(nr);
+      return acc;
+    };
+    std::vector<int2> hp5((size_t)A * NP, make_int2(-1, 0)), pp5((size_t)NP * NP, make_int2(-1, 0));
+    std::vector<int2> hh2((size_t)A * A, make_int2(-1, 0)), hp2((size_t)A * NP, make_int2(-1, 0));
+    std::vector<int64_t> o5, o2;
+    std::vector<int2> r5, c5, r2, c2;
+    std::vector<int> nr5, nc5, ro5, co5, nr2, nc2, ro2, co2;
+    n_v5_ = blocks(5, hp5, pp5, false, v5_off_, n5_, o5, r5, c5, nr5, nc5, ro5, co5);
+    n_v2_ = blocks(2, hh2, hp2, true, v2_off_, n2_, o2, r2, c2, nr2, nc2, ro2, co2);
+    off5_h_ = o5; off2_h_ = o2; nr5_h_ = nr5; nc5_h_ = nc5; nr2_h_ = nr2; nc2_h_ = nc2;
+    hp5_slot_.put(hp5); pp5_slot_.put(pp5); hh2_slot_.put(hh2); hp2_slot_.put(hp2);
+    rows5_.put(r5); cols5_.put(c5); rows2_.put(r2); cols2_.put(c2);
+    nc5_.put(nc5); ro5_.put(ro5); co5_.put(co5); nc2_.put(nc2); ro2_.put(ro2); co2_.put(co2);
+    TD_.hp5_slot = hp5_slot_.as<int2>(); TD_.pp5_slot = pp5_slot_.as<int2>();
+    TD_.v5_off = v5_off_.as<int64_t>(); TD_.n5 = n5_.as<int>();
+    TD_.hh2_slot = hh2_slot_.as<int2>(); TD_.hp2_slot = hp2_slot_.as<int2>();
+    TD_.v2_off = v2_off_.as<int64_t>(); TD_.n2 = n2_.as<int>();
+    V5_.zeros((size_t)n_v5_ * sizeof(S));
+    V2_.zeros((size_t)n_v2_ * sizeof(S));
+    build_t3(L);
+    partial_.zeros(kBlocks * 2 * sizeof(double));
+    res_.zeros(4 * sizeof(double));
+  }
+
+  bool has_v() const override { return have5_ && have2_; }
+  int64_t launches() const override { return launches_; }
+  int64_t count() const override { return total_; }
+
+  void set_hhhp(int ch, const double *v, cudaStream_t st) override {
+    if (ch < 0 || ch >= (int)off2_h_.size()) throw EngineError(1, "hhhp channel out of range");
+    stage(v, (int64_t)nr2_h_[ch] * nc2_h_[ch], V2_.as<S>() + off2_h_[ch], st);
+    have2_ = true;
+  }
+  void set_hppp(int ch, const double *v, cudaStream_t st) override {
+    if (ch < 0 || ch >= (int)off5_h_.size()) throw EngineError(1, "hppp channel out of range");
+    stage(v, (int64_t)nr5_h_[ch] * nc5_h_[ch], V5_.as<S>() + off5_h_[ch], st);
+    have5_ = true;
+  }
+  void generate_v(const DevPotential &pot, cudaStream_t st) override {
+    const int n5 = (int)off5_h_.size(), n2 = (int)off2_h_.size();
+    if (n5) k_gen_block<S><<<std::min(n5, 8192), 256, 0, st>>>(O_, pot, rows5_.as<int2>(), cols5_.as<int2>(), v5_off_.as<int64_t>(),
+                                                    n5_.as<int>(), nc5_.as<int>(), ro5_.as<int>(), co5_.as<int>(), n5, 1,
+                                                    V5_.as<S>());
+    if (n2) k_gen_block<S><<<std::min(n2, 8192), 256, 0, st>>>(O_, pot, rows2_.as<int2>(), cols2_.as<int2>(), v2_off_.as<int64_t>(),
+                                                    n2_.as<int>(), nc2_.as<int>(), ro2_.as<int>(), co2_.as<int>(), n2, 0,
+                                                    V2_.as<S>());
+    launches_ += 2;
+    tck(cudaGetLastError(), "V_hppp/V_hhhp generation");
+    have5_ = have2_ = true;
+  }
+  void energy(const S *T, const S *fdiag, double et[2], cudaStream_t st) override {
+    if (!has_v()) throw EngineError(4, "(T): V_hppp and V_hhhp blocks are not set");
+    if (total_ > 0) {
+      k_triples<S><<<kBlocks, 256, 0, st>>>(TD_, D_, T, V5_.as<S>(), V2_.as<S>(), fdiag, total_, partial_.as<double>());
+      k_finish2<<<2, 256, 0, st>>>(partial_.as<double>(), kBlocks, res_.as<double>());
+      launches_ += 2;
+      tck(cudaGetLastError(), "(T) kernel");
+      double h[2];
+      tck(cudaMemcpyAsync(h, res_.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, st), "(T) result");
+      tck(cudaStreamSynchronize(st), "(T) sync");
+      et[0] = h[0];
+      et[1] = h[1];
+    } else {
+      et[0] = et[1] = 0.0;
+    }
+  }
+
+ private:
+  static constexpr int kBlocks = 152 * 8;
+
+  void stage(const double *v, int64_t n, S *dst, cudaStream_t st) {
+    if (!v) throw EngineError(1, "null V block");
+    DB tmp;
+    tmp.zeros((size_t)n * 2 * sizeof(double));
+    tck(cudaMemcpyAsync(tmp.p, v, (size_t)n * 2 * sizeof(double), cudaMemcpyHostToDevice, st), "V block upload");
+    k_copy_in<S><<<608, 256, 0, st>>>(tmp.as<double>(), n, dst);
+    ++launches_;
+    tck(cudaStreamSynchronize(st), "V block sync");
+    if (!ScalarOf<S>::complex) {
+      std::vector<double> h((size_t)n * 2);
+      std::copy(v, v + 2 * n, h.begin());
+      for (int64_t e = 0; e < n; ++e)
+        if (h[2 * e + 1] != 0.0) throw EngineError(1, "complex V block given to a real engine");
+    }
+  }
+
+  // triple channels keyed by (Tz, N), hhh (i<j<k) bras and ppp (a<b<c) kets, in the
+  // enumeration order of setup_t3_channel_structures; only keys with both kinds.
+  void build_t3(const Layout &L) {
+    const Basis &B = L.b;
+    const int ns = B.ns, A = B.A;
+    int mn[3] = {1 << 30, 1 << 30, 1 << 30}, mx[3] = {-(1 << 30), -(1 << 30), -(1 << 30)};
+    for (int p = 0; p < ns; ++p) {
+      const int v[3] = {B.nx[p], B.ny[p], B.nz[p]};
+      for (int d = 0; d < 3; ++d) { mn[d] = std::min(mn[d], v[d]); mx[d] = std::max(mx[d], v[d]); }
+    }
+    const int lo[3] = {3 * mn[0], 3 * mn[1], 3 * mn[2]}, hi[3] = {3 * mx[0], 3 * mx[1], 3 * mx[2]};
+    const int tlo = 3 * B.tzmin, thi = 3 * B.tzmax;
+    const int ex[3] = {hi[0] - lo[0] + 1, hi[1] - lo[1] + 1, hi[2] - lo[2] + 1};
+    const int et = thi - tlo + 1;
+    auto key = [&](int t, int x, int y, int z) {
+      return (((size_t)(t - tlo) * ex[0] + (x - lo[0])) * ex[1] + (y - lo[1])) * ex[2] + (z - lo[2]);
+    };
+    const size_t nkeys = (size_t)et * ex[0] * ex[1] * ex[2];
+    std::vector<std::vector<int3>> hhh(nkeys);
+    for (int a = 0; a < A; ++a)
+      for (int b = a + 1; b < A; ++b)
+        for (int c = b + 1; c < A; ++c)
+          hhh[key(B.tz[a] + B.tz[b] + B.tz[c], B.nx[a] + B.nx[b] + B.nx[c], B.ny[a] + B.ny[b] + B.ny[c],
+                  B.nz[a] + B.nz[b] + B.nz[c])].push_back(make_int3(a, b, c));
+    std::vector<std::vector<int3>> ppp(nkeys);
+    for (int a = A; a < ns; ++a)
+      for (int b = a + 1; b < ns; ++b) {
+        const int t2 = B.tz[a] + B.tz[b], x2 = B.nx[a] + B.nx[b], y2 = B.ny[a] + B.ny[b], z2 = B.nz[a] + B.nz[b];
+        for (int c = b + 1; c < ns; ++c) {
+          const size_t k = key(t2 + B.tz[c], x2 + B.nx[c], y2 + B.ny[c], z2 + B.nz[c]);
+          if (!hhh[k].empty()) ppp[k].push_back(make_int3(a, b, c));
+        }
+      }
+    std::vector<int64_t> eoff(1, 0), hoff, poff;
+    std::vector<int> nbra;
+    std::vector<int3> hl, pl;
+    for (int t = tlo; t <= thi; t += 2)
+      for (int x = lo[0]; x <= hi[0]; ++x)
+        for (int y = lo[1]; y <= hi[1]; ++y)
+          for (int z = lo[2]; z <= hi[2]; ++z) {
+            const size_t k = key(t, x, y, z);
+            if (hhh[k].empty() || ppp[k].empty()) continue;
+            hoff.push_back((int64_t)hl.size());
+            poff.push_back((int64_t)pl.size());
+            nbra.push_back((int)hhh[k].size());
+            hl.insert(hl.end(), hhh[k].begin(), hhh[k].end());
+            pl.insert(pl.end(), ppp[k].begin(), ppp[k].end());
+            eoff.push_back(eoff.back() + (int64_t)hhh[k].size() * ppp[k].size());
+          }
+    TD_.nt3 = (int)nbra.size();
+    total_ = eoff.back();
+    eoff.push_back(eoff.back());  // sentinel so the channel walk never reads past the end
+    elem_off_.put(eoff); nbra_.put(nbra); hhh_off_.put(hoff); ppp_off_.put(poff); hhh_.put(hl); ppp_.put(pl);
+    TD_.elem_off = elem_off_.as<int64_t>(); TD_.nbra = nbra_.as<int>();
+    TD_.hhh_off = hhh_off_.as<int64_t>(); TD_.ppp_off = ppp_off_.as<int64_t>();
+    TD_.hhh = hhh_.as<int3>(); TD_.ppp = ppp_.as<int3>();
+  }
+
+  DevLayout D_;
+  DevOrbits O_;
+  TriplesDev TD_{};
+  DB orbit_of_, hp5_slot_, pp5_slot_, hh2_slot_, hp2_slot_, v5_off_, n5_, v2_off_, n2_;
+  DB rows5_, cols5_, rows2_, cols2_, nc5_, ro5_, co5_, nc2_, ro2_, co2_;
+  DB V5_, V2_, elem_off_, nbra_, hhh_off_, ppp_off_, hhh_, ppp_, partial_, res_;
+  std::vector<int64_t> off5_h_, off2_h_;
+  std::vector<int> nr5_h_, nc5_h_, nr2_h_, nc2_h_;
+  int64_t n_v5_ = 0, n_v2_ = 0, total_ = 0, launches_ = 0;
+  bool have5_ = false, have2_ = false;
+};
+
+template <typename S>
+std::unique_ptr<ITriples<S>> make_triples(const Layout &L, const DevLayout &D, const DevOrbits &O, int device) {
+  return std::unique_ptr<ITriples<S>>(new Triples<S>(L, D, O, device));
+}
+
+template std::unique_ptr<ITriples<double>> make_triples<double>(const Layout &, const DevLayout &, const DevOrbits &, int);
+template std::unique_ptr<ITriples<cplx>> make_triples<cplx>(const Layout &, const DevLayout &, const DevOrbits &, int);
+
+}  // namespace ccx

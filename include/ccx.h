@@ -1,0 +1,260 @@
+/*
+ * ccx.h -- C ABI of the GB300 CCD + (T) engine.
+ *
+ * Drop-in boundary for the CCD solver of paolofinelli/Coupled-Cluster-NuclearMatter
+ * (directory deltafull-CCMkspace).  The reference has no plugin API: its solver is
+ * the set of Fortran subroutines that ccd_iter (ccm_iter.f90:1-170) calls, and they
+ * talk through module globals.  Each entry point below names the subroutine or
+ * global it replaces.  A Fortran caller binds them with ISO_C_BINDING; complex*16
+ * arrays are passed as interleaved (re, im) double pairs, which is the memory
+ * layout of complex(c_double_complex).
+ *
+ * Conventions
+ *  - Every function returns 0 on success and a nonzero CCX_E* code on failure; the
+ *    message of the last failure on the calling thread is ccx_last_error().  No
+ *    entry point exits or stops the process.
+ *  - Orbitals are 0-based in pair lists (the Fortran shim adds 1).  Channels are
+ *    0-based and numbered in the reference's enumeration order.
+ *  - Per-channel blocks use the reference's column-major layout, e.g. the T2 block
+ *    of hhpp channel ch is t2_ccm(ch)%val(n_pp, n_hh) with ab fastest.
+ *  - One engine drives one GPU through one CUDA stream; calls on one engine are
+ *    not thread safe.
+ */
+#ifndef CCX_H
+#define CCX_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CCX_OK 0
+#define CCX_EINVAL 1      /* bad argument or malformed input */
+#define CCX_ECUDA 2       /* CUDA runtime failure (message holds the CUDA error) */
+#define CCX_ENOMEM 3      /* device or host allocation failed / plan too large */
+#define CCX_ESTATE 4      /* call out of order (e.g. iterate before amplitudes) */
+#define CCX_ENUMERIC 5    /* NaN/Inf detected, or singular DIIS system */
+#define CCX_ENOGPU 6      /* no CUDA device available */
+
+typedef struct ccx_layout ccx_layout;
+typedef struct ccx_engine ccx_engine;
+
+/* ------------------------------------------------------------------ */
+/* Input deck                                                           */
+/* ------------------------------------------------------------------ */
+
+/* The nine value lines of ccm_in, read by ccm_main.f90:31-32 and allocate_sp_data
+ * (ccm_main.f90:893-900), plus an optional extension block that the reference
+ * parser never reads (lines after the ninth value line of the form "key = value"). */
+typedef struct {
+  int32_t chiral_order;      /* line 1 */
+  double lambda;             /* line 1 */
+  double cE, cD;             /* line 2 */
+  int32_t A;                 /* line 3: number of particles (below_ef) */
+  int32_t snm;               /* line 4: 0 pnm, 1 snm */
+  int32_t input_is_kfermi;   /* line 4: 0 density, 1 kfermi */
+  char bc[16];               /* line 5: PBC / TABC / TABCsp */
+  double dens_or_kf;         /* line 6 */
+  int32_t ntwist, nmax, my_twists; /* line 6 */
+  char cc_approx[16];        /* line 7: CCD / CCD(T) / CCDT1 / mbpt2 */
+  int32_t tnf_switch, tnf_approx;  /* line 8 */
+  double cutoff_3nf;         /* line 9 */
+  int32_t nexp_3nf;          /* line 9 */
+  /* extension block (defaults reproduce the reference) */
+  int32_t potential;         /* CCX_POT_*; default CCX_POT_MINNESOTA */
+  uint64_t lec_seed;         /* default 20261203 */
+  int32_t mode;              /* CCX_MODE_*; default CCX_MODE_REFERENCE */
+  int32_t diis_dim;          /* standard mode history; default 8 */
+  double tol;                /* default 1e-6 (|dE|, reference mode) */
+  int32_t max_iter;          /* default 100 */
+  int32_t precision;         /* CCX_PREC_*; default CCX_PREC_FP64 */
+  double theta[3];           /* twist per axis for PBC runs; default 0 */
+} ccx_deck;
+
+/* Parse ccm_in text.  Replaces the read(5,*) sequence of ccm_main.f90:31-32 and
+ * allocate_sp_data (ccm_main.f90:893-900). */
+int ccx_deck_parse(const char *text, ccx_deck *out);
+
+/* ------------------------------------------------------------------ */
+/* Basis and channel layout (host only, no GPU needed)                  */
+/* ------------------------------------------------------------------ */
+
+/* Momentum-lattice single-particle basis in the reference's order.  Replaces
+ * setup_sp_data (ccm_main.f90:1003-1197): k-mesh order, |k|^2 index sort
+ * (ccm_main.f90:2654-2732), spin/isospin inner order, holes = first A states. */
+typedef struct {
+  int32_t nmax;
+  int32_t A;
+  int32_t snm;
+  double density;            /* fm^-3 */
+  double theta[3];           /* twist angles */
+} ccx_basis_params;
+
+typedef struct {
+  int32_t n_states;          /* all_orbit%total_orbits */
+  int32_t n_holes;           /* below_ef */
+  const int32_t *nx, *ny, *nz, *sz, *tz;  /* all_orbit%nx ... %itzp */
+  const double *kx, *ky, *kz;             /* all_orbit%kx ... (fm^-1) */
+  const double *e;           /* all_orbit%e, kinetic energy (MeV) */
+  double box_length;         /* lx (fm); volume = lx^3 */
+} ccx_orbits;
+
+/* Build the basis; the arrays of *orbits stay owned by the layout. */
+int ccx_layout_from_basis(const ccx_basis_params *p, ccx_layout **out);
+/* Wrap a caller's basis (e.g. the Fortran all_orbit arrays); arrays are copied.
+ * Channel tables are then enumerated exactly as setup_channel_structures
+ * (ccm_iter.f90:175-812) and setup_ph_channel_structures (ccm_iter.f90:1816-2105)
+ * enumerate them. */
+int ccx_layout_from_orbits(const ccx_orbits *orbits, ccx_layout **out);
+int ccx_layout_destroy(ccx_layout *l);
+int ccx_layout_orbits(const ccx_layout *l, ccx_orbits *out);
+
+/* counts[0..7]: #hhpp (= #pppp), #hhhh, #hhhp, #hphp, #phhp ph channels, #hphp ph
+ * channels, #hpph ph channels, #T2 amplitudes (ordered, as t2_ccm stores them) */
+int ccx_layout_counts(const ccx_layout *l, int64_t counts[8]);
+
+/* Channel tables.  kind: CCX_CH_* below.  qn = (tz, Nx, Ny, Nz) as in
+ * channels%hhpp_quantum_numbers(4*ch-3 .. 4*ch); side 1 is the bra list
+ * (lookup_*_configs(1,ch)), side 2 the ket list (lookup_*_configs(2,ch)). */
+#define CCX_CH_HHHH 1
+#define CCX_CH_HHHP 2
+#define CCX_CH_HHPP 3
+#define CCX_CH_HPHP 4
+#define CCX_CH_HPPP 5   /* setup_vnn_hppp_block channels (ccm_iter.f90:1407-1534), used by (T) */
+#define CCX_CH_PH_PHHP 11
+#define CCX_CH_PH_HPHP 12
+#define CCX_CH_PH_HPPH 13
+int ccx_layout_channel(const ccx_layout *l, int32_t kind, int32_t ch, int32_t qn[4],
+                       int32_t *n_side1, int32_t *n_side2);
+/* pairs written as (p0, q0, p1, q1, ...), 0-based orbitals; NULL to skip a side */
+int ccx_layout_pairs(const ccx_layout *l, int32_t kind, int32_t ch, int32_t *side1,
+                     int32_t *side2);
+/* 64-bit FNV-1a hash over the orbit table and every channel table */
+int ccx_layout_hash(const ccx_layout *l, uint64_t *hash);
+
+/* ------------------------------------------------------------------ */
+/* Engine                                                               */
+/* ------------------------------------------------------------------ */
+#define CCX_SCALAR_COMPLEX 0   /* complex*16 arithmetic, as the reference */
+#define CCX_SCALAR_REAL 1      /* real arithmetic; V and Fock must be real */
+
+#define CCX_PREC_FP64 0        /* every term in FP64 */
+#define CCX_PREC_MIXED 1       /* ladder/ring GEMMs on the tensor cores (split products), FP64 defect correction */
+
+#define CCX_MODE_REFERENCE 0   /* 0.75/0.25 mixing + DIIS every 6 (ccm_diis.f90:74-249), |dE| stop */
+#define CCX_MODE_STANDARD 1    /* Jacobi step + Pulay DIIS on steps, ||R - D T|| stop */
+
+typedef struct {
+  int32_t device;            /* CUDA device ordinal */
+  int32_t scalar;            /* CCX_SCALAR_* */
+} ccx_engine_options;
+
+/* Allocate the device image of the layout (T2, R, intermediates, maps). */
+int ccx_engine_create(const ccx_layout *l, const ccx_engine_options *opt, ccx_engine **out);
+int ccx_engine_destroy(ccx_engine *e);
+/* device bytes held by the engine */
+int ccx_engine_memory(const ccx_engine *e, int64_t *bytes);
+
+/* ---- interaction input ---------------------------------------------- */
+/* Full Fock matrix (n_states x n_states, column-major, complex interleaved);
+ * replaces one_body_operators%fock_mtx built by normal_ordered_hamiltonian
+ * (ccm_main.f90:1523-1684).  e0 is the reference energy E0. */
+int ccx_set_fock(ccx_engine *e, const double *fock, const double e0[2]);
+
+/* One antisymmetrised V block, exactly the array the reference holds:
+ *   CCX_CH_HHPP  vnn_hhpp(ch)%val(n_hh, n_pp)      ccm_iter.f90:935-1030
+ *   CCX_V_PPPP   vnn_pppp(ch)%val(n_pp, n_pp)      ccm_iter.f90:1203-1305
+ *   CCX_CH_HHHH  vnn_hhhh(ch)%val(n_hh, n_hh)      ccm_iter.f90:835-878
+ *   CCX_CH_HPHP  vnn_hphp(ch)%val(n_hp, n_hp)      ccm_iter.f90:1070-1150
+ *   CCX_CH_HHHP  vnn_hhhp(ch)%val(n_hh, n_hp)      ccm_iter.f90:885-930 (used by (T))
+ *   CCX_CH_HPPP  vnn_hppp(ch)%val(n_hp, n_pp)      ccm_iter.f90:1680-1760 (used by (T))
+ * col-major, complex interleaved, leading dimension = rows.  The host buffer is
+ * only read during the call. */
+#define CCX_V_PPPP 6
+int ccx_set_vblock(ccx_engine *e, int32_t kind, int32_t ch, const double *v);
+
+/* Generate Fock, E0 and every V block on the device from a synthetic potential
+ * (replaces the potential loops of setup_channel_structures, ccm_iter.f90:819-1311,
+ * and normal_ordered_hamiltonian, ccm_main.f90:1586-1684). */
+#define CCX_POT_MINNESOTA 0    /* vmom_minnesota, chiral_module_andreas_with_delta.f90:8980-9111 */
+#define CCX_POT_CHIRAL_LIKE 1  /* OPE + LO/NLO contacts in the operator form of chiral_pot */
+typedef struct {
+  int32_t kind;              /* CCX_POT_* */
+  uint64_t lec_seed;         /* chiral-like contact LEC draw */
+  int32_t f32_literals;      /* 1: Minnesota constants rounded to 4-byte reals like the reference */
+} ccx_potential;
+int ccx_generate_interaction(ccx_engine *e, const ccx_potential *pot);
+/* E0 = sum_i t_ii + 1/2 sum_ij <ij|V|ij> (ccm_main.f90:1661-1684) of the interaction
+ * generated on the device, or the value passed to ccx_set_fock */
+int ccx_get_e0(ccx_engine *e, double e0[2]);
+
+/* ---- amplitudes ----------------------------------------------------- */
+/* MP2 start: setup_t_amplitudes (ccm_iter.f90:2329-2368) */
+int ccx_setup_t_amplitudes(ccx_engine *e);
+/* t2_ccm(ch)%val in / out, (n_pp x n_hh) col-major complex interleaved */
+int ccx_set_t2(ccx_engine *e, int32_t ch, const double *t);
+int ccx_get_t2(ccx_engine *e, int32_t ch, double *t);
+/* t2_ccm_eqn(ch)%val after ccx_t2_intermediate */
+int ccx_get_t2_eqn(ccx_engine *e, int32_t ch, double *r);
+/* all channels concatenated in channel order (n_amps complex values) */
+int ccx_set_t2_all(ccx_engine *e, const double *t);
+int ccx_get_t2_all(ccx_engine *e, double *t);
+/* d2ij(1:A), d2ab(A+1:n) of the last residual, complex interleaved */
+int ccx_get_denominators(ccx_engine *e, double *d2ij, double *d2ab);
+
+/* ---- hot path --------------------------------------------------------- */
+/* t2_intermediate(0), ccm_t2_eqn.f90:4-1304 (with setup_I6I7_intermediate
+ * :1312-1518): the CCD right-hand side R and the dressed denominators from the
+ * current T2. */
+int ccx_t2_intermediate(ccx_engine *e);
+/* diis_t1t2(count), ccm_diis.f90:74-249: T <- 0.75 T + 0.25 R/D, DIIS every
+ * diis_step calls; *count is reset to 0 when DIIS runs, as in the reference.
+ * The subspace is set by ccx_diis_setup (diis_setup, ccm_diis.f90:257-293). */
+int ccx_diis_setup(ccx_engine *e, int32_t subspace, int32_t diis_step);
+int ccx_diis_t1t2(ccx_engine *e, int32_t *count);
+/* ccd_energy_save(ener), ccm_energy.f90:4-71: 1/4 sum T(ab,ij) V(ij,ab) */
+int ccx_ccd_energy(ccx_engine *e, double ener[2]);
+/* ||R - D T|| over the stored (ordered) amplitudes of the last residual */
+int ccx_residual_norm(ccx_engine *e, double *norm);
+
+typedef struct {
+  int32_t mode;              /* CCX_MODE_* */
+  int32_t precision;         /* CCX_PREC_* */
+  int32_t max_iter;          /* reference: 100 (ccm_iter.f90:71) */
+  double tol;                /* reference: 1e-6 on |dE| (ccm_iter.f90:74) */
+  int32_t diis_dim;          /* standard mode history length */
+  int32_t defect_period;     /* mixed precision: FP64 residual every k iterations */
+  int32_t verbose;
+} ccx_iter_opts;
+
+typedef struct {
+  int32_t iterations;
+  int32_t converged;
+  double e_mbpt2[2];         /* correlation energy at the start amplitudes */
+  double e_ccd[2];           /* final correlation energy (eccsd - e0) */
+  double res_norm;           /* ||R - D T|| of the last FP64 residual */
+  double seconds;            /* device time of the loop */
+} ccx_iter_result;
+
+/* ccd_iter loop, ccm_iter.f90:67-133 */
+int ccx_ccd_iter(ccx_engine *e, const ccx_iter_opts *opt, ccx_iter_result *res);
+
+/* ---- (T) -------------------------------------------------------------- */
+/* pert_triples2, ccm_triples.f90:528-735 (NN part): E(T) from the current T2 with
+ * the V_hppp / V_hhhp blocks of setup_vnn_hppp_block (ccm_iter.f90:1361-1810). */
+int ccx_pert_triples(ccx_engine *e, double et[2]);
+
+/* ---- diagnostics -------------------------------------------------------- */
+const char *ccx_last_error(void);
+/* kernel launches issued by this engine since creation */
+int ccx_engine_launches(const ccx_engine *e, int64_t *launches);
+/* per-term device milliseconds of the last ccx_ccd_iter:
+ * [0] T_ph gather, [1] I9/I7, [2] I6, [3] I4, [4] ring, [5] R init, [6] ladders,
+ * [7] update/energy, [8] DIIS, [9] total */
+int ccx_engine_timers(const ccx_engine *e, double ms[10]);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

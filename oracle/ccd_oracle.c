@@ -430,13 +430,15 @@ static uint64_t sm64(uint64_t *st) {
 }
 static void draw_lecs(ocl_t *o) {
   /* centres in 10^4 GeV^-2 (CS, CT) and 10^4 GeV^-4 (C1..C7), converted to MeV units as
-   * at chiral_module_andreas_with_delta.f90:586-596 (x1e-2 MeV^-2, x1e-8 MeV^-4) */
+   * at chiral_module_andreas_with_delta.f90:586-596 (x1e-2 MeV^-2, x1e-8 MeV^-4), with the
+   * 1/(16 pi) normalisation the reference applies when it forms its operator LECs
+   * (CS = (c1s0+3 c3s1)/16/pi, :599-600; cnlo(i) = (...)/(16 pi), :604-614) */
   const double centre[9] = {-0.1, 0.01, 0.1, 0.1, 0.1, 0.1, 0.1, 0.1, 0.1};
   uint64_t st = o->prm.lec_seed;
   for (int i = 0; i < 9; i++) {
     double u = (double)(sm64(&st) >> 11) * 0x1.0p-53;
     double v = centre[i] * (0.5 + u);
-    o->lec[i] = v * (i < 2 ? 1.0e-2 : 1.0e-8);
+    o->lec[i] = v * (i < 2 ? 1.0e-2 : 1.0e-8) / (16.0 * PI);
   }
 }
 
@@ -1343,8 +1345,12 @@ static int zsolve(int n, zd *Am, zd *b) {
   return 0;
 }
 
+/* The reference increments nstep in ccd_iter right before each call
+ * (ccm_iter.f90:86); this entry point does that increment itself. */
 void ocl_diis_t1t2(ocl_t *o, int *count) {
   const double a1 = 0.75, b1 = 0.25;
+  if (!o->t2_diis) ocl_diis_setup(o, 6, 6);
+  o->nstep++;
   size_t nd = (size_t)o->n_diis;
   if (o->nstep > o->subspace) {
     o->nstep = o->subspace;
@@ -1449,7 +1455,6 @@ int ocl_ccd_iter(ocl_t *o, const ocl_iter_opts *opt, ocl_iter_result *res) {
       ocl_t2_intermediate(o);
       res->res_norm = ocl_residual_norm(o);
       count++;
-      o->nstep++;
       ocl_diis_t1t2(o, &count);
       ocl_ccd_energy(o, e);
       ener2 = e[0] + I * e[1];

@@ -93,7 +93,7 @@ void ocl_get_denoms(const ocl_t *o, double *d2ij, double *d2ab); /* complex inte
 
 /* ---- hot path -------------------------------------------------------- */
 void ocl_t2_intermediate(ocl_t *o);              /* t2_intermediate(0) */
-void ocl_diis_t1t2(ocl_t *o, int *count);        /* diis_t1t2(count); ocl_diis_setup first */
+void ocl_diis_t1t2(ocl_t *o, int *count);        /* nstep += 1, then diis_t1t2(count) */
 void ocl_diis_setup(ocl_t *o, int subspace, int diis_step);
 void ocl_ccd_energy(const ocl_t *o, double *re_im);  /* ccd_energy_save */
 double ocl_residual_norm(const ocl_t *o);        /* ||R - D T|| over ordered amplitudes */

@@ -1,0 +1,246 @@
+"""GPU engine against the CPU oracle, through the C ABI (libccx.so).
+
+Tolerances: FP64 path vs FP64 oracle.  The engine sums in a different order (packed
+a<b, i<j blocks, tiled GEMMs), so element-wise agreement is to ~1e-12 relative to the
+block's scale and energies to ~1e-10 relative.  The one exception is the reference's
+own DIIS step (see test_reference_iteration_step_by_step).  The spec bar (1e-6
+relative in E/A, 1e-5 in E(T)) is far looser.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+C1 = dict(nmax=2, A=14, rho=0.08, snm=False)
+
+
+def make(ccx, O, nmax, A, rho, snm=False, pot=0, real=True, theta=(0.0, 0.0, 0.0)):
+    o = O.Oracle(O.Config(nmax=nmax, A=A, rho=rho, snm=snm, theta=theta, potential=pot))
+    L = ccx.Layout.from_basis(nmax, A, rho, snm=snm, theta=theta)
+    e = ccx.Engine(L, real=real)
+    e.generate(potential=pot)
+    return o, L, e
+
+
+def rel(a, b):
+    return float(np.abs(np.asarray(a) - np.asarray(b)).max() / max(np.abs(np.asarray(b)).max(), 1e-300))
+
+
+def check_blocks(o, e, get_o, get_e, tol):
+    worst = 0.0
+    scale = max(np.abs(get_o(c)).max() for c in range(o.n_channels(3)))
+    for c in range(o.n_channels(3)):
+        d = np.abs(get_e(c) - get_o(c)).max() / scale
+        worst = max(worst, d)
+    assert worst < tol, worst
+    return worst
+
+
+def test_e0_and_mp2(ccx, O):
+    o, L, e = make(ccx, O, **C1)
+    assert abs(e.e0() - o.e0()) < 1e-12 * abs(o.e0())
+    o.mp2()
+    e.setup_t_amplitudes()
+    check_blocks(o, e, o.t2, e.t2, 1e-13)
+    assert abs(e.ccd_energy() - o.energy()) < 1e-12 * abs(o.energy())
+
+
+def test_residual_matches_oracle_at_mp2(ccx, O):
+    o, L, e = make(ccx, O, **C1)
+    o.mp2()
+    e.setup_t_amplitudes()
+    o.t2_intermediate()
+    e.t2_intermediate()
+    check_blocks(o, e, o.r2, e.t2_eqn, 1e-12)
+    d1o, d2o = o.denoms()
+    d1e, d2e = e.denominators()
+    assert rel(d1e, d1o) < 1e-13 and rel(d2e, d2o) < 1e-13
+    assert abs(e.residual_norm() - o.residual_norm()) < 1e-10 * o.residual_norm()
+
+
+def test_residual_matches_oracle_at_iterated_t(ccx, O):
+    """Residual of a non-MP2 amplitude: the oracle's T after 4 reference steps."""
+    o, L, e = make(ccx, O, **C1)
+    o.mp2()
+    o.diis_setup()
+    cnt = 0
+    for _ in range(4):
+        o.t2_intermediate()
+        cnt = o.diis_t1t2(cnt + 1)
+    e.setup_t_amplitudes()
+    for c in range(o.n_channels(3)):
+        e.set_t2(c, o.t2(c))
+    check_blocks(o, e, o.t2, e.t2, 1e-15)
+    o.t2_intermediate()
+    e.t2_intermediate()
+    check_blocks(o, e, o.r2, e.t2_eqn, 1e-12)
+
+
+def test_reference_iteration_step_by_step(ccx, O):
+    """t2_intermediate / diis_t1t2 / ccd_energy called one by one, as ccd_iter does.
+
+    The damped updates agree to rounding.  The reference's DIIS step (every 6th call)
+    solves a bordered system of unconjugated dot products of consecutive differences
+    (ccm_diis.f90:134-173) whose condition number is ~1e15 here, so a different
+    summation order alone moves the extrapolated energy by ~1e-7 relative; after the
+    first DIIS step the trajectories are compared at the spec bar (1e-6)."""
+    o, L, e = make(ccx, O, **C1)
+    o.mp2()
+    e.setup_t_amplitudes()
+    o.diis_setup(6, 6)
+    e.diis_setup(6, 6)
+    co = ce = 0
+    for it in range(14):
+        o.t2_intermediate()
+        e.t2_intermediate()
+        co = o.diis_t1t2(co + 1)
+        ce = e.diis_t1t2(ce + 1)
+        assert co == ce
+        eo, ee = o.energy(), e.ccd_energy()
+        tol = 1e-11 if it < 5 else 1e-6
+        assert abs(ee - eo) < tol * abs(eo), (it, ee, eo)
+
+
+def test_ccd_iter_reference_mode(ccx, O):
+    o, L, e = make(ccx, O, **C1)
+    o.mp2()
+    e.setup_t_amplitudes()
+    ro = o.ccd_iter(mode=O.MODE_REFERENCE)
+    re_ = e.ccd_iter(mode=ccx.MODE_REFERENCE)
+    assert re_["converged"] and abs(re_["iterations"] - ro["iterations"]) <= 2
+    # both stop at |dE| < 1e-6 MeV (ccm_iter.f90:74)
+    assert abs(re_["e_ccd"] - ro["e_ccd"]) < 5e-7 * abs(ro["e_ccd"])
+    assert abs(re_["e_mbpt2"] - ro["e_mbpt2"]) < 1e-12 * abs(ro["e_mbpt2"])
+
+
+def test_ccd_iter_standard_mode_converges_to_1e10(ccx, O):
+    o, L, e = make(ccx, O, **C1)
+    o.mp2()
+    e.setup_t_amplitudes()
+    ro = o.ccd_iter(mode=O.MODE_STANDARD, tol=1e-10)
+    re_ = e.ccd_iter(mode=ccx.MODE_STANDARD, tol=1e-10)
+    assert re_["converged"] and re_["res_norm"] < 1e-10
+    assert abs(re_["e_ccd"] - ro["e_ccd"]) < 1e-11 * abs(ro["e_ccd"])
+    # E/A within 1e-6 relative of the oracle (the spec bar), here ~1e-12
+    ea_o = (o.e0() + ro["e_ccd"]).real / 14
+    ea_e = (e.e0() + re_["e_ccd"]).real / 14
+    assert abs(ea_e - ea_o) < 1e-6 * abs(ea_o)
+
+
+def test_complex_engine_matches_real_engine(ccx, O):
+    _, L, er = make(ccx, O, **C1)
+    ec = ccx.Engine(L, real=False)
+    ec.generate()
+    er.setup_t_amplitudes()
+    ec.setup_t_amplitudes()
+    rr = er.ccd_iter(mode=ccx.MODE_STANDARD, tol=1e-10)
+    rc = ec.ccd_iter(mode=ccx.MODE_STANDARD, tol=1e-10)
+    assert rr["iterations"] == rc["iterations"]
+    assert abs(rr["e_ccd"] - rc["e_ccd"]) < 1e-12 * abs(rr["e_ccd"])
+
+
+@pytest.mark.parametrize("cfg", [dict(nmax=1, A=4, rho=0.16, snm=True), dict(nmax=2, A=28, rho=0.16, snm=True)],
+                         ids=["snm4", "snm28"])
+def test_chiral_like_snm_complex(ccx, O, cfg):
+    o, L, e = make(ccx, O, pot=1, real=False, **cfg)
+    assert abs(e.e0() - o.e0()) < 1e-11 * abs(o.e0())
+    o.mp2()
+    e.setup_t_amplitudes()
+    o.t2_intermediate()
+    e.t2_intermediate()
+    check_blocks(o, e, o.r2, e.t2_eqn, 1e-11)
+    ro = o.ccd_iter(mode=O.MODE_STANDARD, tol=1e-9, max_iter=80)
+    o.mp2()
+    re_ = e.ccd_iter(mode=ccx.MODE_STANDARD, tol=1e-9, max_iter=80)
+    assert ro["converged"] and re_["converged"]
+    assert abs(re_["e_ccd"] - ro["e_ccd"]) < 1e-9 * abs(ro["e_ccd"])
+
+
+def test_real_engine_rejects_complex_potential(ccx):
+    L = ccx.Layout.from_basis(1, 4, 0.16, snm=True)
+    e = ccx.Engine(L, real=True)
+    with pytest.raises(ccx.CcxError) as ex:
+        e.generate(potential=ccx.POT_CHIRAL_LIKE)
+    assert ex.value.code == 1
+
+
+def test_iterate_before_amplitudes_is_a_state_error(ccx):
+    L = ccx.Layout.from_basis(1, 2, 0.08)
+    e = ccx.Engine(L, real=True)
+    with pytest.raises(ccx.CcxError) as ex:
+        e.ccd_iter()
+    assert ex.value.code == 4
+    e.generate()
+    with pytest.raises(ccx.CcxError) as ex:
+        e.t2_intermediate()
+    assert ex.value.code == 4
+
+
+def test_triples_matches_oracle(ccx, O):
+    o, L, e = make(ccx, O, **C1)
+    o.mp2()
+    e.setup_t_amplitudes()
+    o.ccd_iter(mode=O.MODE_STANDARD, tol=1e-10)
+    e.ccd_iter(mode=ccx.MODE_STANDARD, tol=1e-10)
+    eo = o.triples()
+    ee = e.pert_triples()
+    assert abs(ee - eo) < 1e-10 * abs(eo)
+
+
+def test_triples_chiral_like_snm(ccx, O):
+    o, L, e = make(ccx, O, nmax=1, A=4, rho=0.16, snm=True, pot=1, real=False)
+    o.mp2()
+    e.setup_t_amplitudes()
+    o.ccd_iter(mode=O.MODE_STANDARD, tol=1e-10)
+    e.ccd_iter(mode=ccx.MODE_STANDARD, tol=1e-10)
+    eo, ee = o.triples(), e.pert_triples()
+    assert abs(ee - eo) < 1e-9 * abs(eo)
+
+
+def test_caller_supplied_blocks_match_generated(ccx, O):
+    """The drop-in path: the Fortran host hands over fock_mtx and the vnn_* blocks."""
+    o, L, eg = make(ccx, O, **C1)
+    e = ccx.Engine(L, real=True)
+    e.set_fock(o.fock(), o.e0())
+    for c in range(o.n_channels(3)):
+        e.set_vblock(ccx.CH_HHPP, c, o.v_hhpp(c))
+        e.set_vblock(ccx.V_PPPP, c, o.v_pppp(c))
+    for c in range(o.n_channels(1)):
+        e.set_vblock(ccx.CH_HHHH, c, o.v_hhhh(c))
+    for c in range(o.n_channels(4)):
+        e.set_vblock(ccx.CH_HPHP, c, o.v_hphp(c))
+    assert abs(e.e0() - o.e0()) == 0.0
+    e.setup_t_amplitudes()
+    eg.setup_t_amplitudes()
+    e.t2_intermediate()
+    eg.t2_intermediate()
+    for c in range(o.n_channels(3)):
+        assert rel(e.t2_eqn(c), eg.t2_eqn(c)) < 1e-12
+    e.setup_t_amplitudes()
+    eg.setup_t_amplitudes()
+    r1 = e.ccd_iter(mode=ccx.MODE_STANDARD, tol=1e-10)
+    r2 = eg.ccd_iter(mode=ccx.MODE_STANDARD, tol=1e-10)
+    o.mp2()
+    ro = o.ccd_iter(mode=O.MODE_STANDARD, tol=1e-10)
+    assert r1["converged"] and r2["converged"]
+    assert abs(r1["e_ccd"] - ro["e_ccd"]) < 1e-11 * abs(ro["e_ccd"])
+    assert abs(r1["e_ccd"] - r2["e_ccd"]) < 1e-11 * abs(ro["e_ccd"])
+
+
+def test_complex_block_into_real_engine_is_rejected(ccx, O):
+    o = O.Oracle(O.Config(nmax=1, A=2, rho=0.08))
+    L = ccx.Layout.from_basis(1, 2, 0.08)
+    e = ccx.Engine(L, real=True)
+    v = o.v_hhpp(0) + 1e-3j
+    with pytest.raises(ccx.CcxError) as ex:
+        e.set_vblock(ccx.CH_HHPP, 0, v)
+    assert ex.value.code == 1
+
+
+def test_twisted_lattice(ccx, O):
+    o, L, e = make(ccx, O, nmax=1, A=14, rho=0.10, theta=(0.3, -1.1, 2.0))
+    o.mp2()
+    e.setup_t_amplitudes()
+    ro = o.ccd_iter(mode=O.MODE_STANDARD, tol=1e-10)
+    re_ = e.ccd_iter(mode=ccx.MODE_STANDARD, tol=1e-10)
+    assert abs(re_["e_ccd"] - ro["e_ccd"]) < 1e-10 * abs(ro["e_ccd"])
