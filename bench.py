@@ -1,0 +1,352 @@
+"""Benchmark: time to a converged CCD E/A on one lattice per GPU.
+
+Workload (default): pure neutron matter, A=66 at rho=0.16 fm^-3 on the nmax=4
+lattice (9^3 momenta x 2 spins = 1458 states), synthetic Minnesota interaction,
+single twist, MP2 start.  A step is one full solve: MP2 amplitudes, then CCD
+iterations (Jacobi + DIIS(8)) until ||R - D T|| < 1e-10, with the interaction
+resident in HBM.  value = seconds per solve (lower is better), device time from CUDA
+events on the engine's stream.  e2e = the same solve driven through the C ABI from
+pinned host buffers holding the reference-layout V blocks and Fock matrix, with the
+host->device copies and the T2 readback inside the timed region.
+
+--impl reference times the CPU path (the oracle restatement of the reference's
+complex<double> solver, all host cores) on a bounded sample: single CCD iterations
+of the same lattice, scaled by the reference algorithm's iteration count.
+
+Multi-GPU: the lattice is one twist; N GPUs solve N independent twists (replicas,
+no collective); value is the slowest rank's time, scaling "weak".
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import importlib.util
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG_DIR = os.path.join(ROOT, "coupled-cluster-nuclearmatter_gb300")
+ORACLE_DIR = os.path.join(ROOT, "oracle")
+
+METRIC = "time-to-converged E/A (<1 keV vs FP64) mixed+batched+learned vs plain GPU"
+WORKLOADS = {
+    "pnm66": dict(nmax=4, A=66, rho=0.16, snm=False, potential=0,
+                  desc="PNM A=66, rho=0.16 fm^-3, nmax=4 (1458 states), Minnesota, theta=0"),
+    "pnm14": dict(nmax=2, A=14, rho=0.08, snm=False, potential=0,
+                  desc="PNM A=14, rho=0.08 fm^-3, nmax=2 (250 states), Minnesota, theta=0"),
+}
+# Iterations the reference algorithm (0.75/0.25 mixing + DIIS every 6, |dE| < 1e-6 MeV,
+# ccm_iter.f90:67-96) takes on each lattice, as run by the engine's reference mode.
+REFERENCE_ITERATIONS = {"pnm66": None, "pnm14": 13}
+
+
+def load_pkg():
+    if "ccnm_gb300" in sys.modules:
+        return sys.modules["ccnm_gb300"]
+    spec = importlib.util.spec_from_file_location("ccnm_gb300", os.path.join(PKG_DIR, "__init__.py"),
+                                                  submodule_search_locations=[PKG_DIR])
+    m = importlib.util.module_from_spec(spec)
+    sys.modules["ccnm_gb300"] = m
+    spec.loader.exec_module(m)
+    return m
+
+
+def packed_sizes(L, ccx):
+    """Packed (a<b, i<j) sizes per hhpp channel and ring-channel sizes."""
+    c = L.counts()
+    P, H = [], []
+    for ch in range(c["hhpp"]):
+        hh, pp = L.pairs(ccx.CH_HHPP, ch)
+        H.append(int((hh[:, 0] < hh[:, 1]).sum()))
+        P.append(int((pp[:, 0] < pp[:, 1]).sum()))
+    ring = []
+    for q in range(c["ph_phhp"]):
+        _, nph, nhp = L.channel(ccx.CH_PH_PHHP, q)
+        ring.append((nph, nhp))
+    return P, H, ring
+
+
+def flop_model(P, H, ring, real=True):
+    """Algorithmic FLOPs per CCD iteration on unique pairs (a<b, i<j); 2 per real MAC."""
+    m = 2.0 if real else 8.0
+    pp = sum(m * p * p * h for p, h in zip(P, H))
+    hh = sum(m * p * h * h for p, h in zip(P, H))
+    x = sum(m * h * h * p for p, h in zip(P, H))
+    i4 = sum(m * nhp * nhp * nph for nph, nhp in ring)
+    rg = sum(m * nph * nhp * nhp for nph, nhp in ring)
+    return {"pp_ladder": pp, "hh_ladder": hh, "i9": x, "i4": i4, "ring": rg, "ladders": pp + hh,
+            "total": pp + hh + x + i4 + rg}
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    def __init__(self, index: int):
+        self.f = tempfile.NamedTemporaryFile(prefix="clocks", suffix=".csv", delete=False)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(index), f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                       "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self) -> dict:
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        self.p.wait()
+        self.f.close()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.f.name):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.f.name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def oracle_sample(wl: dict, iters: int, warm: int):
+    """Seconds per CCD iteration of the CPU oracle on the full lattice (reference mode)."""
+    sys.path.insert(0, ORACLE_DIR)
+    import oracle as O
+    O.build()
+    o = O.Oracle(O.Config(nmax=wl["nmax"], A=wl["A"], rho=wl["rho"], snm=wl["snm"], potential=wl["potential"]))
+    o.mp2()
+    o.diis_setup()
+    cnt = 0
+    times = []
+    for k in range(warm + iters):
+        t = time.perf_counter()
+        o.t2_intermediate()
+        cnt = o.diis_t1t2(cnt + 1)
+        o.energy()
+        dt = time.perf_counter() - t
+        if k >= warm:
+            times.append(dt)
+    return statistics.mean(times), O.num_threads(), o
+
+
+def run_reference(args, wl):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    n_ref = REFERENCE_ITERATIONS[args.workload]
+    per_it, cores, _ = oracle_sample(wl, args.steps, args.warmup)
+    value = per_it * n_ref
+    sample = (f"{args.steps} timed CCD iterations (after {args.warmup} warm-up) of the oracle restatement "
+              f"(complex<double> ordered blocks, as the reference), x {n_ref} reference-mode iterations")
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_it * 1e3, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
+            "config": {"workload": wl["desc"], "algorithm": "reference (0.75/0.25 mixing, DIIS every 6, |dE|<1e-6)",
+                       "sample_unit": "one CCD iteration"},
+            "cpu_baseline": {"value": value, "unit": "s", "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args, wl):
+    import torch
+    ccx = load_pkg()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    # each rank solves its own twist of the lattice (replicas, no data exchange)
+    theta = (0.0, 0.0, 0.0) if rank == 0 else (0.1 * rank, -0.07 * rank, 0.05 * rank)
+    L = ccx.Layout.from_basis(wl["nmax"], wl["A"], wl["rho"], snm=wl["snm"], theta=theta)
+    real = wl["potential"] == ccx.POT_MINNESOTA
+    e = ccx.Engine(L, device=local, real=real)
+    e.generate(potential=wl["potential"])
+    stream = torch.cuda.ExternalStream(e.stream(), device=local)
+    P, H, ring = packed_sizes(L, ccx)
+    flops = flop_model(P, H, ring, real=real)
+
+    def solve(eng):
+        eng.setup_t_amplitudes()
+        return eng.ccd_iter(mode=ccx.MODE_STANDARD, tol=args.tol, max_iter=200, diis_dim=8)
+
+    for _ in range(args.warmup):
+        r = solve(e)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    launches0 = e.launches()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    results = []
+    timers = {}
+    for _ in range(args.steps):
+        results.append(solve(e))
+        t = e.timers()
+        for k, v in t.items():
+            timers[k] = timers.get(k, 0.0) + v
+    ev1.record(stream)
+    ev1.synchronize()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    launches = e.launches() - launches0
+    ms = ev0.elapsed_time(ev1) / args.steps
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    r = results[-1]
+    iters = sum(x["iterations"] for x in results) / len(results)
+    ea = (e.e0() + r["e_ccd"]).real / wl["A"]
+
+    # ---- roofline of the dominant kernel (the fused pp+hh ladder GEMM, FP64 FMA) ----
+    n_it = sum(x["iterations"] + 1 for x in results)  # residual evaluations in the timed steps
+    ladder_ms = timers["ladders"] / n_it
+    ring_ms = timers["ring"] / n_it
+    i4_ms = timers["i4"] / n_it
+    peak64 = ccx.device_fp64_peak(local)
+    achieved = flops["ladders"] / (ladder_ms * 1e-3) / 1e12
+    roofline = {"bound": "fp64", "kernel": "k_gemm (pp-ladder + hh-ladder, packed a<b, i<j)",
+                "achieved": achieved, "peak": peak64, "unit": "TFLOP/s", "frac": achieved / peak64,
+                "peak_source": "measured FP64 FMA probe (ccx_device_fp64_peak); FP64 is not in MEASURED_PEAKS.json",
+                "traffic": None, "ms_per_launch": ladder_ms,
+                "flops_per_launch": flops["ladders"]}
+    terms = {k: v / n_it for k, v in timers.items() if k != "total"}
+
+    # ---- end to end through the C ABI from pinned host buffers ----
+    e2e = None
+    if not args.no_e2e:
+        e2e = run_e2e(args, ccx, torch, L, e, local, real, solve)
+
+    line = {"metric": METRIC, "value": ms * 1e-3, "unit": "s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64" if real else "c128", "data": "synthetic",
+            "form": "plain FP64 GPU (packed unique pairs, real arithmetic)",
+            "config": {"workload": wl["desc"], "solver": f"Jacobi + DIIS(8) to ||R-DT||<{args.tol:g}",
+                       "l2": "inputs larger than L2 (V_pppp packed, %.2f GB)" % (sum(p * p for p in P) * 8 / 1e9),
+                       "replicas": world},
+            "iterations": iters, "ccd_iterations_per_s": iters / (ms * 1e-3), "E_per_A_MeV": ea,
+            "res_norm": r["res_norm"], "term_ms_per_iteration": terms,
+            "gflop_per_iteration": flops["total"] / 1e9,
+            "roofline": roofline, "clocks": clk, "gpu_launches": launches, "e2e": e2e}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        n_ref = REFERENCE_ITERATIONS[args.workload] or reference_iterations(e, ccx)
+        per_it, cores, _ = oracle_sample(wl, 1, 0)
+        line["cpu_baseline"] = {"value": per_it * n_ref, "unit": "s", "cores": cores, "kind": "port",
+                                "sample": f"1 CCD iteration of the oracle (complex<double>, as the reference) on the "
+                                          f"full lattice, x {n_ref} reference-mode iterations"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def reference_iterations(e, ccx):
+    e.setup_t_amplitudes()
+    return e.ccd_iter(mode=ccx.MODE_REFERENCE)["iterations"]
+
+
+def run_e2e(args, ccx, torch, L, e, local, real, solve):
+    lib = ccx.lib()
+    c = L.counts()
+    dims = L.hhpp_dims()
+    n = len(L.orbits()["nx"])
+    # reference-layout host blocks (pinned), exported once from the resident interaction
+    blocks = []
+
+    def pinned(nd):
+        return torch.empty(nd, dtype=torch.float64, pin_memory=True)
+
+    def export(kind, ch, rows, cols):
+        buf = pinned(2 * rows * cols)
+        ccx._check(lib.ccx_get_vblock(e._h, kind, ch, C.c_void_p(buf.data_ptr())))
+        blocks.append((kind, ch, buf))
+
+    for ch in range(c["hhpp"]):
+        nh, npp = dims[ch]
+        export(ccx.CH_HHPP, ch, nh, npp)
+        export(ccx.V_PPPP, ch, npp, npp)
+    for ch in range(c["hhhh"]):
+        _, nh, _ = L.channel(ccx.CH_HHHH, ch)
+        export(ccx.CH_HHHH, ch, nh, nh)
+    for ch in range(c["hphp"]):
+        _, nhp, _ = L.channel(ccx.CH_HPHP, ch)
+        export(ccx.CH_HPHP, ch, nhp, nhp)
+    fock = pinned(2 * n * n)
+    ccx._check(lib.ccx_get_fock(e._h, C.c_void_p(fock.data_ptr())))
+    e0 = e.e0()
+    e0buf = (C.c_double * 2)(e0.real, e0.imag)
+    t_out = pinned(2 * c["amps"])
+    h2d = sum(b.numel() * 8 for _, _, b in blocks) + fock.numel() * 8
+    d2h = t_out.numel() * 8 + 16
+    eb = ccx.Engine(L, device=local, real=real)
+    stream = torch.cuda.ExternalStream(eb.stream(), device=local)
+
+    def step():
+        ccx._check(lib.ccx_set_fock(eb._h, C.c_void_p(fock.data_ptr()), e0buf))
+        for kind, ch, buf in blocks:
+            ccx._check(lib.ccx_set_vblock(eb._h, kind, ch, C.c_void_p(buf.data_ptr())))
+        r = solve(eb)
+        ccx._check(lib.ccx_get_t2_all(eb._h, C.c_void_p(t_out.data_ptr())))
+        return r
+
+    for _ in range(max(1, args.warmup // 2)):
+        step()
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    t0 = time.perf_counter()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        r = step()
+    ev1.record(stream)
+    ev1.synchronize()
+    wall = (time.perf_counter() - t0) / args.steps
+    ms = ev0.elapsed_time(ev1) / args.steps
+    eb.close()
+    return {"value": ms * 1e-3, "unit": "s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+            "host_wall_s": wall, "iterations": r["iterations"],
+            "path": "ccx_set_fock + ccx_set_vblock (all HHPP/PPPP/HHHH/HPHP blocks) + ccx_setup_t_amplitudes + "
+                    "ccx_ccd_iter + ccx_get_t2_all"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="pnm66", choices=sorted(WORKLOADS))
+    ap.add_argument("--tol", type=float, default=1e-10)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    wl = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        return run_reference(args, wl)
+    return run_ours(args, wl)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -123,6 +123,10 @@ def lib():
         "ccx_residual_norm": ([vp, C.POINTER(dbl)], C.c_int),
         "ccx_ccd_iter": ([vp, C.POINTER(_IterOpts), C.POINTER(_IterResult)], C.c_int),
         "ccx_pert_triples": ([vp, vp], C.c_int),
+        "ccx_get_vblock": ([vp, i32, i32, vp], C.c_int),
+        "ccx_get_fock": ([vp, vp], C.c_int),
+        "ccx_engine_stream": ([vp, C.POINTER(vp)], C.c_int),
+        "ccx_device_fp64_peak": ([i32, C.POINTER(dbl)], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -145,6 +149,13 @@ def _cplx_fortran(a: np.ndarray) -> np.ndarray:
     """Complex block -> contiguous interleaved doubles in column-major order."""
     z = np.asarray(a, dtype=np.complex128)
     return np.ascontiguousarray(z.reshape(-1, order="F")).view(np.float64)
+
+
+def device_fp64_peak(device: int = 0) -> float:
+    """Measured FP64 FMA throughput of the device in TFLOP/s."""
+    x = C.c_double()
+    _check(lib().ccx_device_fp64_peak(device, C.byref(x)))
+    return x.value
 
 
 def deck_parse(text: str) -> dict:
@@ -272,6 +283,33 @@ class Engine:
     def set_vblock(self, kind: int, ch: int, block: np.ndarray):
         b = _cplx_fortran(block)
         _check(lib().ccx_set_vblock(self._h, kind, ch, _ptr(b)))
+
+    def vblock(self, kind: int, ch: int) -> np.ndarray:
+        """One V block in the reference's ordered layout (see ccx_get_vblock)."""
+        shape = self._vshape(kind, ch)
+        z = np.zeros(2 * shape[0] * shape[1])
+        _check(lib().ccx_get_vblock(self._h, kind, ch, _ptr(z)))
+        return z.view(np.complex128).reshape(shape, order="F")
+
+    def _vshape(self, kind, ch):
+        if kind == V_PPPP:
+            n = self._dims[ch][1]
+            return (n, n)
+        _, n1, n2 = self.layout.channel(kind, ch)
+        if kind in (CH_HHHH, CH_HPHP):
+            return (n1, n1)
+        return (n1, n2)
+
+    def fock(self) -> np.ndarray:
+        n = len(self.layout.orbits()["nx"])
+        z = np.zeros(2 * n * n)
+        _check(lib().ccx_get_fock(self._h, _ptr(z)))
+        return z.view(np.complex128).reshape(n, n, order="F")
+
+    def stream(self) -> int:
+        s = vp()
+        _check(lib().ccx_engine_stream(self._h, C.byref(s)))
+        return s.value or 0
 
     def e0(self) -> complex:
         z = np.zeros(2)

@@ -371,6 +371,23 @@ int ccx_get_e0(ccx_engine *e, double e0[2]) {
   if (!e0) return fail(CCX_EINVAL, "null argument");
   ENGINE_CALL(e, e->E->get_e0(e0));
 }
+int ccx_get_vblock(ccx_engine *e, int32_t kind, int32_t ch, double *v) { ENGINE_CALL(e, e->E->get_vblock(kind, ch, v)); }
+int ccx_get_fock(ccx_engine *e, double *f) {
+  if (!f) return fail(CCX_EINVAL, "null argument");
+  ENGINE_CALL(e, e->E->get_fock(f));
+}
+int ccx_engine_stream(const ccx_engine *e, void **stream) {
+  if (!stream) return fail(CCX_EINVAL, "null argument");
+  ENGINE_CALL(e, *stream = e->E->stream());
+}
+int ccx_device_fp64_peak(int32_t device, double *tflops) {
+  if (!tflops) return fail(CCX_EINVAL, "null argument");
+  return guard([&] {
+    const double v = ccx::fp64_peak(device);
+    if (v <= 0) throw ccx::EngineError(CCX_ECUDA, "FP64 probe failed (no GPU?)");
+    *tflops = v;
+  });
+}
 int ccx_setup_t_amplitudes(ccx_engine *e) { ENGINE_CALL(e, e->E->mp2()); }
 int ccx_set_t2(ccx_engine *e, int32_t ch, const double *t) {
   if (!t) return fail(CCX_EINVAL, "null T2 block");

@@ -257,6 +257,79 @@ class Engine final : public IEngine {
     commit();
   }
   void get_e0(double e0[2]) override { e0[0] = e0_[0]; e0[1] = e0_[1]; }
+  void *stream() const override { return (void *)st_; }
+
+  void get_vblock(int kind, int ch, double *v) override {
+    const Layout &L = *L_;
+    if (!v) throw EngineError(1, "null output block");
+    const ChannelFamily *F = nullptr;
+    switch (kind) {
+      case 1: F = &L.fam[1]; break;
+      case 2: F = &L.fam[2]; break;
+      case 3: F = &L.fam[3]; break;
+      case 4: F = &L.fam[4]; break;
+      case 5: F = &L.fam[5]; break;
+      case 6: F = &L.fam[3]; break;
+      default: throw EngineError(1, "unknown V block kind");
+    }
+    check_ch(ch, F->count());
+    const PairList &rows = kind == 6 ? F->side2[ch] : F->side1[ch];
+    const PairList &cols = (kind == 1 || kind == 4) ? F->side1[ch] : F->side2[ch];
+    const int nr = rows.size(), nc = cols.size();
+    const size_t bytes = (size_t)nr * nc * 2 * sizeof(double);
+    if (bytes > stage_.bytes) stage_.alloc(bytes, &bytes_);
+    if (generated_) {
+      std::vector<int2> r(nr), c(nc);
+      for (int i = 0; i < nr; ++i) r[i] = make_int2(rows.p[i], rows.q[i]);
+      for (int i = 0; i < nc; ++i) c[i] = make_int2(cols.p[i], cols.q[i]);
+      DBuf dr, dc;
+      upload(dr, r, nullptr);
+      upload(dc, c, nullptr);
+      launch_gen_ordered<S>(O_, pot_, dr.as<int2>(), dc.as<int2>(), nr, nc, kind == 5 ? 1 : 0, stage_.as<double>(), st_);
+      ++launches_;
+      CK(cudaMemcpyAsync(v, stage_.p, bytes, cudaMemcpyDeviceToHost, st_));
+      CK(cudaStreamSynchronize(st_));
+      return;
+    }
+    int target = ch;
+    if (kind == 1) target = hhhh_to_hhpp_[ch];
+    if (!(kind == 3 || kind == 6 || (kind == 1 && target >= 0)))
+      throw EngineError(4, "this V block is not stored by the engine (it was not generated on the device)");
+    const int *rs = (kind == 3 || kind == 1) ? hh_sgn_.as<int>() + hhsgn_off_[target] : pp_sgn_.as<int>() + ppsgn_off_[target];
+    const int *cs = (kind == 1) ? hh_sgn_.as<int>() + hhsgn_off_[target] : pp_sgn_.as<int>() + ppsgn_off_[target];
+    const S *src = kind == 3 ? Vhp_.as<S>() : kind == 6 ? Vpp_.as<S>() : Vhh_.as<S>();
+    launch_unpack_vblock<S>(D_, kind, target, nr, nc, rs, cs, src, stage_.as<double>(), st_);
+    ++launches_;
+    CK(cudaMemcpyAsync(v, stage_.p, bytes, cudaMemcpyDeviceToHost, st_));
+    CK(cudaStreamSynchronize(st_));
+  }
+
+  void get_fock(double *f) override {
+    const Layout &L = *L_;
+    const int ns = L.b.ns, A = L.b.A;
+    std::vector<S> fd(ns), f6(std::max(ns - A, 1)), f7(std::max(A, 1));
+    CK(cudaStreamSynchronize(st_));
+    CK(cudaMemcpy(fd.data(), fdiag_.p, ns * sizeof(S), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(f6.data(), f6_.p, f6.size() * sizeof(S), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(f7.data(), f7_.p, f7.size() * sizeof(S), cudaMemcpyDeviceToHost));
+    std::fill(f, f + 2 * (size_t)ns * ns, 0.0);
+    auto put = [&](int p, int q, S v, bool conj) {
+      const size_t o = 2 * ((size_t)p + (size_t)ns * q);
+      f[o] = real_(v);
+      f[o + 1] = conj ? -imag_(v) : imag_(v);
+    };
+    for (int p = 0; p < ns; ++p) {
+      put(p, p, fd[p], false);
+      const int pb = partner_[p];
+      if (p >= A && pb >= A) {
+        put(p, pb, f6[p - A], false);
+        put(pb, p, f6[p - A], true);
+      } else if (p < A && pb >= 0 && pb < A) {
+        put(pb, p, f7[p], false);
+        put(p, pb, f7[p], true);
+      }
+    }
+  }
 
   // ---------------------------------------------------------------- amplitudes
   void mp2() override {
@@ -925,6 +998,8 @@ class Engine final : public IEngine {
   std::vector<int> phys_;
   std::unique_ptr<ITriples<S>> tr_;
 };
+
+double fp64_peak(int device) { return measure_fp64_peak(device); }
 
 std::unique_ptr<IEngine> make_engine(std::shared_ptr<const Layout> L, int device, bool complex_scalars) {
   if (complex_scalars) return std::unique_ptr<IEngine>(new Engine<cplx>(std::move(L), device));

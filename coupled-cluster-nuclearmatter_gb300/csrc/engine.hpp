@@ -46,6 +46,9 @@ class IEngine {
   virtual void set_vblock(int kind, int ch, const double *v) = 0;
   virtual void generate(const PotentialSpec &p) = 0;
   virtual void get_e0(double e0[2]) = 0;
+  virtual void get_vblock(int kind, int ch, double *v) = 0;
+  virtual void get_fock(double *f) = 0;
+  virtual void *stream() const = 0;
   virtual void mp2() = 0;
   virtual void set_t2(int ch, const double *t) = 0;
   virtual void get_t2(int ch, double *t) = 0;
@@ -66,5 +69,7 @@ std::unique_ptr<IEngine> make_engine(std::shared_ptr<const Layout> L, int device
 
 // contact LECs of the chiral-like synthetic potential drawn from a seed
 void draw_lecs(uint64_t seed, double out[9]);
+// FP64 FMA throughput probe (TFLOP/s)
+double fp64_peak(int device);
 
 }  // namespace ccx

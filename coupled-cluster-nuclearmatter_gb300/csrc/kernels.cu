@@ -664,6 +664,83 @@ void launch_generate(const DevLayout &L, const DevOrbits &O, const DevPotential 
   k_gen_e0<S><<<1, 256, 0, st>>>(L, O, pot, e0);
 }
 
+template <typename S>
+__global__ void k_gen_ordered(DevOrbits O, DevPotential P, const int2 *__restrict__ rows, const int2 *__restrict__ cols,
+                              int nr, int nc, int swap, double *__restrict__ out) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < (int64_t)nr * nc; e += (int64_t)gridDim.x * blockDim.x) {
+    const int2 x = rows[e % nr], y = cols[e / nr];
+    const S v = swap ? pot::vanti<S>(O, P, y.x, y.y, x.x, x.y) : pot::vanti<S>(O, P, x.x, x.y, y.x, y.y);
+    out[2 * e] = real_(v);
+    out[2 * e + 1] = imag_(v);
+  }
+}
+template <typename S>
+void launch_gen_ordered(const DevOrbits &O, const DevPotential &pot, const int2 *rows, const int2 *cols, int nr, int nc,
+                        int swap, double *out, cudaStream_t st) {
+  if ((int64_t)nr * nc > 0) k_gen_ordered<S><<<1216, 256, 0, st>>>(O, pot, rows, cols, nr, nc, swap, out);
+}
+
+template <typename S>
+__global__ void k_unpack_vblock(DevLayout L, int kind, int ch, int nr, int nc, const int *__restrict__ rs,
+                                const int *__restrict__ cs, const S *__restrict__ src, double *__restrict__ out) {
+  const int P = L.P[ch], H = L.H[ch];
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < (int64_t)nr * nc; e += (int64_t)gridDim.x * blockDim.x) {
+    const int r = rs[e % nr], c = cs[e / nr];
+    S v = S(0.0);
+    if (r && c) {
+      const double sg = ssign(r) * ssign(c);
+      if (kind == 3) v = sg * src[L.t_off[ch] + (int64_t)sidx(r) * P + sidx(c)];
+      else if (kind == 6) v = sg * src[L.vpp_off[ch] + (int64_t)sidx(r) * P + sidx(c)];
+      else v = sg * src[L.hh2_off[ch] + sidx(r) + (int64_t)H * sidx(c)];
+    }
+    out[2 * e] = real_(v);
+    out[2 * e + 1] = imag_(v);
+  }
+}
+template <typename S>
+void launch_unpack_vblock(const DevLayout &L, int kind, int ch, int n_rows, int n_cols, const int *row_sgn,
+                          const int *col_sgn, const S *src, double *out, cudaStream_t st) {
+  if ((int64_t)n_rows * n_cols > 0)
+    k_unpack_vblock<S><<<1216, 256, 0, st>>>(L, kind, ch, n_rows, n_cols, row_sgn, col_sgn, src, out);
+}
+
+// register-only FMA chains; one store per thread
+__global__ void k_fp64_probe(double *out, int iters) {
+  double x[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) x[k] = threadIdx.x * 1e-3 + k;
+  for (int i = 0; i < iters; ++i)
+#pragma unroll
+    for (int k = 0; k < 8; ++k) x[k] = fma(x[k], 0.999, 1e-3);
+  double s = 0.0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) s += x[k];
+  out[(int64_t)blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+double measure_fp64_peak(int device) {
+  int sm = 0;
+  if (cudaSetDevice(device) != cudaSuccess || cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, device) != cudaSuccess)
+    return -1.0;
+  const int blocks = sm * 8, threads = 256, iters = 2048;
+  double *out = nullptr;
+  if (cudaMalloc(&out, (size_t)blocks * threads * sizeof(double)) != cudaSuccess) return -1.0;
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  k_fp64_probe<<<blocks, threads>>>(out, iters);
+  cudaEventRecord(a);
+  k_fp64_probe<<<blocks, threads>>>(out, iters);
+  cudaEventRecord(b);
+  cudaEventSynchronize(b);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, a, b);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaFree(out);
+  if (cudaGetLastError() != cudaSuccess || ms <= 0.f) return -1.0;
+  return 2.0 * 8.0 * iters * (double)blocks * threads / (ms * 1e-3) / 1e12;
+}
+
 // MP2, setup_t_amplitudes (ccm_iter.f90:2355-2368): T = conj(V(ij,ab)) / (f_ii+f_jj-f_aa-f_bb)
 template <typename S>
 __global__ void k_mp2(DevLayout L, const S *__restrict__ Vhp, const S *__restrict__ fd, S *__restrict__ T) {
@@ -736,6 +813,10 @@ void launch_unpack_t(const DevLayout &L, int ch, int n_pp, const int *pp_signed,
                                    S *, S *, S *, double *, cudaStream_t);                                             \
   template void launch_mp2<S>(const DevLayout &, const S *, const S *, S *, cudaStream_t);                            \
   template void launch_pack_t<S>(const DevLayout &, int, int, const double *, S *, int *, cudaStream_t);          \
+  template void launch_gen_ordered<S>(const DevOrbits &, const DevPotential &, const int2 *, const int2 *, int, int,  \
+                                      int, double *, cudaStream_t);                                                    \
+  template void launch_unpack_vblock<S>(const DevLayout &, int, int, int, int, const int *, const int *, const S *,  \
+                                        double *, cudaStream_t);                                                       \
   template void launch_unpack_t<S>(const DevLayout &, int, int, const int *, const int *, int, const S *, double *,   \
                                    cudaStream_t);
 

@@ -78,6 +78,15 @@ template <typename S> void launch_build_vph(const DevLayout &L, const S *Vhp, S 
 template <typename S>
 void launch_generate(const DevLayout &L, const DevOrbits &O, const DevPotential &pot, S *Vhp, S *Vpp, S *Vhh, S *W,
                      S *fdiag, S *f6, S *f7, double *e0, cudaStream_t st);
+// ordered block of <row|V|col> (or <col|V|row> when swap) into interleaved doubles
+template <typename S>
+void launch_gen_ordered(const DevOrbits &O, const DevPotential &pot, const int2 *rows, const int2 *cols, int nr, int nc,
+                        int swap, double *out, cudaStream_t st);
+// packed V' -> ordered reference block (kind 3 V_hhpp, 6 V_pppp, 1 V_hhhh of hhpp channel ch)
+template <typename S>
+void launch_unpack_vblock(const DevLayout &L, int kind, int ch, int n_rows, int n_cols, const int *row_sgn,
+                          const int *col_sgn, const S *src, double *out, cudaStream_t st);
+double measure_fp64_peak(int device);
 template <typename S> void launch_mp2(const DevLayout &L, const S *Vhp, const S *fdiag, S *T, cudaStream_t st);
 template <typename S> void launch_pack_t(const DevLayout &L, int ch, int n_pp, const double *stage, S *T, int *flag, cudaStream_t st);
 template <typename S>

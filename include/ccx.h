@@ -189,6 +189,15 @@ int ccx_generate_interaction(ccx_engine *e, const ccx_potential *pot);
  * generated on the device, or the value passed to ccx_set_fock */
 int ccx_get_e0(ccx_engine *e, double e0[2]);
 
+/* Export of the interaction in the reference's ordered layout (the inverse of
+ * ccx_set_vblock / ccx_set_fock).  For a generated interaction every kind is
+ * available (blocks are re-evaluated on the device); for a caller-supplied one, the
+ * kinds the engine stores (HHPP, PPPP, HHHH of channels with pp pairs).  The Fock
+ * export holds the momentum-diagonal entries the CCD path uses (f(p,p) and the
+ * same-momentum spin partners), zeros elsewhere. */
+int ccx_get_vblock(ccx_engine *e, int32_t kind, int32_t ch, double *v);
+int ccx_get_fock(ccx_engine *e, double *fock);
+
 /* ---- amplitudes ----------------------------------------------------- */
 /* MP2 start: setup_t_amplitudes (ccm_iter.f90:2329-2368) */
 int ccx_setup_t_amplitudes(ccx_engine *e);
@@ -247,6 +256,11 @@ int ccx_pert_triples(ccx_engine *e, double et[2]);
 
 /* ---- diagnostics -------------------------------------------------------- */
 const char *ccx_last_error(void);
+/* the engine's CUDA stream (cudaStream_t), for callers that order their own work
+ * or time with events on it */
+int ccx_engine_stream(const ccx_engine *e, void **stream);
+/* measured FP64 FMA throughput of the device (TFLOP/s), from a register-only probe */
+int ccx_device_fp64_peak(int32_t device, double *tflops);
 /* kernel launches issued by this engine since creation */
 int ccx_engine_launches(const ccx_engine *e, int64_t *launches);
 /* per-term device milliseconds of the last ccx_ccd_iter:
