@@ -127,6 +127,7 @@ def lib():
         "ccx_get_fock": ([vp, vp], C.c_int),
         "ccx_engine_stream": ([vp, C.POINTER(vp)], C.c_int),
         "ccx_device_fp64_peak": ([i32, C.POINTER(dbl)], C.c_int),
+        "ccx_selftest_tc_gemm": ([i32, i32, i32, vp, vp, vp, i32, C.c_uint64, C.POINTER(dbl), C.POINTER(dbl)], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -156,6 +157,18 @@ def device_fp64_peak(device: int = 0) -> float:
     x = C.c_double()
     _check(lib().ccx_device_fp64_peak(device, C.byref(x)))
     return x.value
+
+
+def selftest_tc_gemm(shapes, kind: int = 0, use_alo: bool = True, seed: int = 1, device: int = 0):
+    """Tensor-core split GEMM against FP64 on random problems [(M, N, K), ...].
+    Returns (max relative error, kernel ms)."""
+    M = np.array([s[0] for s in shapes], np.int32)
+    N = np.array([s[1] for s in shapes], np.int32)
+    K = np.array([s[2] for s in shapes], np.int32)
+    err, ms = C.c_double(), C.c_double()
+    _check(lib().ccx_selftest_tc_gemm(device, kind, len(shapes), _ptr(M), _ptr(N), _ptr(K), int(use_alo), seed,
+                                      C.byref(err), C.byref(ms)))
+    return err.value, ms.value
 
 
 def deck_parse(text: str) -> dict:

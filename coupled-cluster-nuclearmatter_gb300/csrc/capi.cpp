@@ -388,6 +388,12 @@ int ccx_device_fp64_peak(int32_t device, double *tflops) {
     *tflops = v;
   });
 }
+int ccx_selftest_tc_gemm(int32_t device, int32_t kind, int32_t nprob, const int32_t *M, const int32_t *N,
+                         const int32_t *K, int32_t use_alo, uint64_t seed, double *max_rel_err, double *ms) {
+  if (!M || !N || !K || !max_rel_err || !ms || nprob <= 0 || (kind != 0 && kind != 1))
+    return fail(CCX_EINVAL, "bad selftest arguments");
+  return guard([&] { ccx::tc_selftest(device, kind, nprob, M, N, K, use_alo, seed, max_rel_err, ms); });
+}
 int ccx_setup_t_amplitudes(ccx_engine *e) { ENGINE_CALL(e, e->E->mp2()); }
 int ccx_set_t2(ccx_engine *e, int32_t ch, const double *t) {
   if (!t) return fail(CCX_EINVAL, "null T2 block");

@@ -685,29 +685,66 @@ class Engine final : public IEngine {
     build_gemm_plans();
   }
 
-  void add_tiles(std::vector<GemmTile> &tiles, int prob, int M, int N) {
-    for (int m0 = 0; m0 < M; m0 += kGemmBM)
-      for (int n0 = 0; n0 < N; n0 += kGemmBN) tiles.push_back(GemmTile{prob, m0, n0, 0});
-  }
+  // A grouped GEMM launch plan: problems, tile lists per tile shape, split-K problems.
   struct Plan {
-    DBuf probs, tiles;
-    int ntiles = 0;
+    DBuf probs, tiles[2], splits;
+    int ntiles[2] = {0, 0}, nsplit = 0;
   };
-  void finalize_plan(Plan &pl, std::vector<GemmProb<S>> &probs, std::vector<GemmTile> &tiles, const std::vector<int64_t> &work) {
+  struct PlanBuilder {
+    std::vector<GemmProb<S>> probs;
+    std::vector<GemmTile> tiles[2];
+    std::vector<int> splits;
+    std::vector<int64_t> work;
+    void add(GemmProb<S> p, int64_t w) {
+      const int shape = p.N <= 32 ? kShape128x32 : kShape64x64;
+      const int bm = gemm_bm(shape), bn = gemm_bn(shape);
+      const int id = (int)probs.size();
+      const int nsl = p.kchunk > 0 ? (p.seg[0].K + p.kchunk - 1) / p.kchunk : 1;
+      for (int ks = 0; ks < nsl; ++ks)
+        for (int m0 = 0; m0 < p.M; m0 += bm)
+          for (int n0 = 0; n0 < p.N; n0 += bn) tiles[shape].push_back(GemmTile{id, m0, n0, ks});
+      if (p.kchunk > 0) splits.push_back(id);
+      probs.push_back(p);
+      work.push_back(p.kchunk > 0 ? w / nsl : w);
+    }
+  };
+  void finalize_plan(Plan &pl, PlanBuilder &b) {
     // largest problems first for load balance across the SMs
-    std::stable_sort(tiles.begin(), tiles.end(), [&](const GemmTile &a, const GemmTile &b) { return work[a.prob] > work[b.prob]; });
-    upload(pl.probs, probs, &bytes_);
-    upload(pl.tiles, tiles, &bytes_);
-    pl.ntiles = (int)tiles.size();
+    for (int sh = 0; sh < 2; ++sh) {
+      std::stable_sort(b.tiles[sh].begin(), b.tiles[sh].end(),
+                       [&](const GemmTile &x, const GemmTile &y) { return b.work[x.prob] > b.work[y.prob]; });
+      upload(pl.tiles[sh], b.tiles[sh], &bytes_);
+      pl.ntiles[sh] = (int)b.tiles[sh].size();
+    }
+    upload(pl.probs, b.probs, &bytes_);
+    upload(pl.splits, b.splits, &bytes_);
+    pl.nsplit = (int)b.splits.size();
+  }
+  void run_plan(const Plan &pl) {
+    const GemmProb<S> *pr = (const GemmProb<S> *)pl.probs.p;
+    for (int sh = 0; sh < 2; ++sh)
+      if (pl.ntiles[sh]) {
+        launch_gemm<S>(sh, pr, (const GemmTile *)pl.tiles[sh].p, pl.ntiles[sh], st_);
+        ++launches_;
+      }
+    if (pl.nsplit) {
+      launch_splitk_reduce<S>(pr, (const int *)pl.splits.p, pl.nsplit, st_);
+      ++launches_;
+    }
   }
   void build_gemm_plans() {
     const Layout &L = *L_;
     const int nc = L.fam[3].count();
-    {  // X = V_hhpp' T'  (H x H, K = P)
-      std::vector<GemmProb<S>> probs;
-      std::vector<GemmTile> tiles;
-      std::vector<int64_t> work;
-      int64_t hoff = 0;
+    constexpr int kXChunk = 128;  // split-K chunk of the X = V_hhpp' T' GEMM (K = P)
+    {  // X = V_hhpp' T'  (H x H, K = P), split along K; partials in the split-K scratch
+      int64_t need = 0;
+      for (int c = 0; c < nc; ++c) {
+        const auto &pk = L.pk[c];
+        if (pk.H > 0 && pk.P > 0) need += (int64_t)((pk.P + kXChunk - 1) / kXChunk) * pk.H * pk.H;
+      }
+      splitk_.alloc((size_t)std::max<int64_t>(need, 1) * sizeof(S), &bytes_);
+      PlanBuilder b;
+      int64_t hoff = 0, poff = 0;
       for (int c = 0; c < nc; ++c) {
         const auto &pk = L.pk[c];
         if (pk.H > 0 && pk.P > 0) {
@@ -716,18 +753,17 @@ class Engine final : public IEngine {
           p.M = pk.H; p.N = pk.H;
           p.seg[0] = GemmSeg<S>{Vhp_.as<S>() + pk.t_off, T_.as<S>() + pk.t_off, pk.P, 1, 1, pk.P, pk.P, 1.0};
           p.C = X_.as<S>() + hoff; p.C0 = nullptr; p.sCm = 1; p.sCn = pk.H; p.accumulate = 0;
-          add_tiles(tiles, (int)probs.size(), p.M, p.N);
-          work.push_back((int64_t)pk.H * pk.H * pk.P);
-          probs.push_back(p);
+          p.kchunk = kXChunk;
+          p.part = splitk_.as<S>() + poff;
+          poff += (int64_t)((pk.P + kXChunk - 1) / kXChunk) * pk.H * pk.H;
+          b.add(p, (int64_t)pk.H * pk.H * pk.P);
         }
         hoff += (int64_t)pk.H * pk.H;
       }
-      finalize_plan(planX_, probs, tiles, work);
+      finalize_plan(planX_, b);
     }
     {  // R' += V_pppp' T' + T' I9'
-      std::vector<GemmProb<S>> probs;
-      std::vector<GemmTile> tiles;
-      std::vector<int64_t> work;
+      PlanBuilder b;
       int64_t hoff = 0, voff = 0;
       for (int c = 0; c < nc; ++c) {
         const auto &pk = L.pk[c];
@@ -738,19 +774,15 @@ class Engine final : public IEngine {
           p.seg[0] = GemmSeg<S>{Vpp_.as<S>() + voff, T_.as<S>() + pk.t_off, pk.P, 1, 1, pk.P, pk.P, 1.0};
           p.seg[1] = GemmSeg<S>{T_.as<S>() + pk.t_off, I9_.as<S>() + hoff, 1, pk.P, 1, pk.H, pk.H, 1.0};
           p.C = R_.as<S>() + pk.t_off; p.C0 = nullptr; p.sCm = 1; p.sCn = pk.P; p.accumulate = 1;
-          add_tiles(tiles, (int)probs.size(), p.M, p.N);
-          work.push_back((int64_t)pk.P * pk.H * (pk.P + pk.H));
-          probs.push_back(p);
+          b.add(p, (int64_t)pk.P * pk.H * (pk.P + pk.H));
         }
         hoff += (int64_t)pk.H * pk.H;
         voff += (int64_t)pk.P * pk.P;
       }
-      finalize_plan(planLadder_, probs, tiles, work);
+      finalize_plan(planLadder_, b);
     }
     {  // I4 = W + 1/2 V_ph T_ph ; R_ph = T_ph I4
-      std::vector<GemmProb<S>> p4, pr;
-      std::vector<GemmTile> t4, tr;
-      std::vector<int64_t> w4, wr;
+      PlanBuilder b4, br;
       int64_t toff = 0, ioff = 0;
       for (int q = 0; q < L.ph[1].count(); ++q) {
         const int nph = L.ph[1].side1[q].size(), nhp = L.ph[1].side2[q].size();
@@ -760,23 +792,19 @@ class Engine final : public IEngine {
           a.M = nhp; a.N = nhp;
           a.seg[0] = GemmSeg<S>{Vph_.as<S>() + toff, Tph_.as<S>() + toff, 1, nhp, 1, nph, nph, 0.5};
           a.C = I4_.as<S>() + ioff; a.C0 = W_.as<S>() + ioff; a.sCm = 1; a.sCn = nhp; a.accumulate = 0;
-          add_tiles(t4, (int)p4.size(), a.M, a.N);
-          w4.push_back((int64_t)nhp * nhp * nph);
-          p4.push_back(a);
-          GemmProb<S> b{};
-          b.nseg = 1;
-          b.M = nph; b.N = nhp;
-          b.seg[0] = GemmSeg<S>{Tph_.as<S>() + toff, I4_.as<S>() + ioff, 1, nph, 1, nhp, nhp, 1.0};
-          b.C = Rph_.as<S>() + toff; b.C0 = nullptr; b.sCm = 1; b.sCn = nph; b.accumulate = 0;
-          add_tiles(tr, (int)pr.size(), b.M, b.N);
-          wr.push_back((int64_t)nph * nhp * nhp);
-          pr.push_back(b);
+          b4.add(a, (int64_t)nhp * nhp * nph);
+          GemmProb<S> r{};
+          r.nseg = 1;
+          r.M = nph; r.N = nhp;
+          r.seg[0] = GemmSeg<S>{Tph_.as<S>() + toff, I4_.as<S>() + ioff, 1, nph, 1, nhp, nhp, 1.0};
+          r.C = Rph_.as<S>() + toff; r.C0 = nullptr; r.sCm = 1; r.sCn = nph; r.accumulate = 0;
+          br.add(r, (int64_t)nph * nhp * nhp);
         }
         toff += (int64_t)nph * nhp;
         ioff += (int64_t)nhp * nhp;
       }
-      finalize_plan(planI4_, p4, t4, w4);
-      finalize_plan(planRing_, pr, tr, wr);
+      finalize_plan(planI4_, b4);
+      finalize_plan(planRing_, br);
     }
   }
 
@@ -788,21 +816,21 @@ class Engine final : public IEngine {
     mark(0);
     launch_gather_tph<S>(D_, T_.as<S>(), Tph_.as<S>(), st_);
     mark(1);
-    launch_gemm<S>((const GemmProb<S> *)planX_.probs.p, (const GemmTile *)planX_.tiles.p, planX_.ntiles, st_);
+    run_plan(planX_);
     launch_i7<S>(D_, X_.as<S>(), fdiag_.as<S>(), f7_.as<S>(), d2ij_.as<S>(), i7off_.as<S>(), st_);
     launch_i9<S>(D_, n_hh2_, Vhh_.as<S>(), X_.as<S>(), I9_.as<S>(), st_);
     mark(2);
     launch_i6<S>(D_, T_.as<S>(), Vhp_.as<S>(), fdiag_.as<S>(), f6_.as<S>(), d2ab_.as<S>(), i6off_.as<S>(), st_);
     mark(3);
-    launch_gemm<S>((const GemmProb<S> *)planI4_.probs.p, (const GemmTile *)planI4_.tiles.p, planI4_.ntiles, st_);
+    run_plan(planI4_);
     mark(4);
-    launch_gemm<S>((const GemmProb<S> *)planRing_.probs.p, (const GemmTile *)planRing_.tiles.p, planRing_.ntiles, st_);
+    run_plan(planRing_);
     mark(5);
     launch_rinit<S>(D_, T_.as<S>(), Vhp_.as<S>(), Rph_.as<S>(), i6off_.as<S>(), i7off_.as<S>(), R_.as<S>(), st_);
     mark(6);
-    launch_gemm<S>((const GemmProb<S> *)planLadder_.probs.p, (const GemmTile *)planLadder_.tiles.p, planLadder_.ntiles, st_);
+    run_plan(planLadder_);
     mark(7);
-    launches_ += 9;
+    launches_ += 5;
     if (timing_) accumulate_timers(0, 7);
   }
   void accumulate_timers(int first, int last) {
@@ -987,7 +1015,7 @@ class Engine final : public IEngine {
   DBuf onx_, ony_, onz_, osz_, otz_, okx_, oky_, okz_, oe_;
   // state
   DBuf T_, R_, Vhp_, Vpp_, Vhh_, X_, I9_, Tph_, Rph_, Vph_, W_, I4_, fdiag_, f6_, f7_, d2ij_, d2ab_, i6off_, i7off_;
-  DBuf partial_, res_, flag_, stage_, hist_, hist_t_, hist_e_;
+  DBuf partial_, res_, flag_, stage_, hist_, hist_t_, hist_e_, splitk_;
   Plan planX_, planLadder_, planI4_, planRing_;
   double *host_res_ = nullptr;
   int host_flag_ = 0;

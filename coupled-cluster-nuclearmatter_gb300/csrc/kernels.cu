@@ -81,41 +81,53 @@ template <> __device__ inline cplx cvt_in<cplx>(const double *p, int *) { return
 }  // namespace
 
 // ============================================================================
-// grouped GEMM, FP64 FMA.  One CTA per 64x64 output tile of one problem; up to two
+// grouped GEMM, FP64 FMA.  One CTA per BM x BN output tile of one problem; up to two
 // K segments share the accumulator (the pp-ladder and hh-ladder both add into R).
+// Thread (tm, tn) owns a TM x TN register tile, tm fastest; threads whose columns
+// lie beyond N skip the FMA loop, so narrow problems waste few FP64 lanes.
 // ============================================================================
-template <typename S>
+template <typename S, int BM, int BN, int TM, int TN>
 __global__ void __launch_bounds__(256) k_gemm(const GemmProb<S> *__restrict__ probs, const GemmTile *__restrict__ tiles) {
-  constexpr int BM = kGemmBM, BN = kGemmBN, BK = kGemmBK, TM = 4, TN = 4;
+  constexpr int BK = kGemmBK;
+  constexpr int NTM = BM / TM;  // threads along M
+  static_assert(NTM * (BN / TN) == 256, "256 threads");
   __shared__ S As[BK][BM + 1];
   __shared__ S Bs[BK][BN + 1];
   const GemmTile tl = tiles[blockIdx.x];
-  const GemmProb<S> pr = probs[tl.prob];
+  const GemmProb<S> &pr = probs[tl.prob];
+  const int M = pr.M, N = pr.N, nseg = pr.nseg, kchunk = pr.kchunk;
   const int tid = threadIdx.x;
-  const int tm = tid & 15, tn = tid >> 4;
-  const bool active = (tl.m0 + tm * TM < pr.M) && (tl.n0 + tn * TN < pr.N);
+  const int tm = tid % NTM, tn = tid / NTM;
+  const bool active = (tl.m0 + tm * TM < M) && (tl.n0 + tn * TN < N);
   S acc[TM][TN];
 #pragma unroll
   for (int i = 0; i < TM; ++i)
 #pragma unroll
     for (int j = 0; j < TN; ++j) acc[i][j] = S(0.0);
-  for (int s = 0; s < pr.nseg; ++s) {
-    const GemmSeg<S> sg = pr.seg[s];
-    for (int k0 = 0; k0 < sg.K; k0 += BK) {
+  for (int s = 0; s < nseg; ++s) {
+    const S *A = pr.seg[s].A, *B = pr.seg[s].B;
+    const int64_t sAm = pr.seg[s].sAm, sAk = pr.seg[s].sAk, sBk = pr.seg[s].sBk, sBn = pr.seg[s].sBn;
+    const double alpha = pr.seg[s].alpha;
+    int kbeg = 0, kend = pr.seg[s].K;
+    if (kchunk > 0) {
+      kbeg = tl.kslice * kchunk;
+      kend = min(kend, kbeg + kchunk);
+    }
+    for (int k0 = kbeg; k0 < kend; k0 += BK) {
       for (int x = tid; x < BM * BK; x += 256) {
         int m, k;
-        if (sg.sAm == 1) { m = x % BM; k = x / BM; } else { k = x % BK; m = x / BK; }
+        if (sAm == 1) { m = x % BM; k = x / BM; } else { k = x % BK; m = x / BK; }
         const int gm = tl.m0 + m, gk = k0 + k;
         S v = S(0.0);
-        if (gm < pr.M && gk < sg.K) v = sg.alpha * sg.A[(int64_t)gm * sg.sAm + (int64_t)gk * sg.sAk];
+        if (gm < M && gk < kend) v = alpha * A[(int64_t)gm * sAm + (int64_t)gk * sAk];
         As[k][m] = v;
       }
       for (int x = tid; x < BK * BN; x += 256) {
         int k, n;
-        if (sg.sBk == 1) { k = x % BK; n = x / BK; } else { n = x % BN; k = x / BN; }
+        if (sBk == 1) { k = x % BK; n = x / BK; } else { n = x % BN; k = x / BN; }
         const int gk = k0 + k, gn = tl.n0 + n;
         S v = S(0.0);
-        if (gk < sg.K && gn < pr.N) v = sg.B[(int64_t)gk * sg.sBk + (int64_t)gn * sg.sBn];
+        if (gk < kend && gn < N) v = B[(int64_t)gk * sBk + (int64_t)gn * sBn];
         Bs[k][n] = v;
       }
       __syncthreads();
@@ -140,11 +152,15 @@ __global__ void __launch_bounds__(256) k_gemm(const GemmProb<S> *__restrict__ pr
 #pragma unroll
   for (int i = 0; i < TM; ++i) {
     const int m = tl.m0 + tm * TM + i;
-    if (m >= pr.M) continue;
+    if (m >= M) continue;
 #pragma unroll
     for (int j = 0; j < TN; ++j) {
       const int n = tl.n0 + tn * TN + j;
-      if (n >= pr.N) continue;
+      if (n >= N) continue;
+      if (kchunk > 0) {
+        pr.part[(int64_t)tl.kslice * M * N + m + (int64_t)M * n] = acc[i][j];
+        continue;
+      }
       const int64_t o = (int64_t)m * pr.sCm + (int64_t)n * pr.sCn;
       if (pr.accumulate) pr.C[o] += acc[i][j];
       else pr.C[o] = (pr.C0 ? pr.C0[o] : S(0.0)) + acc[i][j];
@@ -153,8 +169,29 @@ __global__ void __launch_bounds__(256) k_gemm(const GemmProb<S> *__restrict__ pr
 }
 
 template <typename S>
-void launch_gemm(const GemmProb<S> *probs, const GemmTile *tiles, int ntiles, cudaStream_t st) {
-  if (ntiles > 0) k_gemm<S><<<ntiles, 256, 0, st>>>(probs, tiles);
+void launch_gemm(int shape, const GemmProb<S> *probs, const GemmTile *tiles, int ntiles, cudaStream_t st) {
+  if (ntiles <= 0) return;
+  if (shape == kShape64x64) k_gemm<S, 64, 64, 4, 4><<<ntiles, 256, 0, st>>>(probs, tiles);
+  else k_gemm<S, 128, 32, 8, 2><<<ntiles, 256, 0, st>>>(probs, tiles);
+}
+
+template <typename S>
+__global__ void k_splitk_reduce(const GemmProb<S> *__restrict__ probs, const int *__restrict__ plist) {
+  const GemmProb<S> &pr = probs[plist[blockIdx.x]];
+  const int M = pr.M, N = pr.N;
+  const int ns = (pr.seg[0].K + pr.kchunk - 1) / pr.kchunk;
+  for (int e = threadIdx.x; e < M * N; e += blockDim.x) {
+    S acc = S(0.0);
+    for (int s = 0; s < ns; ++s) acc += pr.part[(int64_t)s * M * N + e];
+    const int m = e % M, n = e / M;
+    const int64_t o = (int64_t)m * pr.sCm + (int64_t)n * pr.sCn;
+    if (pr.accumulate) pr.C[o] += acc;
+    else pr.C[o] = (pr.C0 ? pr.C0[o] : S(0.0)) + acc;
+  }
+}
+template <typename S>
+void launch_splitk_reduce(const GemmProb<S> *probs, const int *plist, int n, cudaStream_t st) {
+  if (n > 0) k_splitk_reduce<S><<<n, 256, 0, st>>>(probs, plist);
 }
 
 // ============================================================================
@@ -793,7 +830,8 @@ void launch_unpack_t(const DevLayout &L, int ch, int n_pp, const int *pp_signed,
 
 // ---- explicit instantiations -------------------------------------------------
 #define CCX_INST(S)                                                                                                    \
-  template void launch_gemm<S>(const GemmProb<S> *, const GemmTile *, int, cudaStream_t);                              \
+  template void launch_gemm<S>(int, const GemmProb<S> *, const GemmTile *, int, cudaStream_t);                         \
+  template void launch_splitk_reduce<S>(const GemmProb<S> *, const int *, int, cudaStream_t);                          \
   template void launch_gather_tph<S>(const DevLayout &, const S *, S *, cudaStream_t);                                 \
   template void launch_i7<S>(const DevLayout &, const S *, const S *, const S *, S *, S *, cudaStream_t);             \
   template void launch_i9<S>(const DevLayout &, int64_t, const S *, const S *, S *, cudaStream_t);                     \

@@ -28,14 +28,23 @@ struct GemmProb {
   const S *C0;  // initial value when accumulate == 0 (nullptr: zero)
   int64_t sCm, sCn;
   int accumulate;
+  int kchunk;   // > 0: split-K over one segment; tile.kslice picks the chunk
+  S *part;      // split-K partial products, kslice-major, each M x N column-major
 };
 struct GemmTile {
-  int prob, m0, n0, pad;
+  int prob, m0, n0, kslice;
 };
-constexpr int kGemmBM = 64, kGemmBN = 64, kGemmBK = 16;
+constexpr int kGemmBK = 16;
+// two tile shapes: 64x64 (4x4 per thread) and 128x32 (8x2 per thread, for N <= 32)
+enum GemmShape { kShape64x64 = 0, kShape128x32 = 1 };
+inline int gemm_bm(int shape) { return shape == kShape64x64 ? 64 : 128; }
+inline int gemm_bn(int shape) { return shape == kShape64x64 ? 64 : 32; }
 
 template <typename S>
-void launch_gemm(const GemmProb<S> *probs, const GemmTile *tiles, int ntiles, cudaStream_t st);
+void launch_gemm(int shape, const GemmProb<S> *probs, const GemmTile *tiles, int ntiles, cudaStream_t st);
+// C = (accumulate ? C : C0 or 0) + sum over the split-K partials, fixed order
+template <typename S>
+void launch_splitk_reduce(const GemmProb<S> *probs, const int *plist, int n, cudaStream_t st);
 
 // ---- potentials -----------------------------------------------------------
 struct DevPotential {

@@ -1,0 +1,145 @@
+// Self-test of the tensor-core split GEMM: grouped random problems against an FP64
+// host product.  Exposed through ccx_selftest_tc_gemm.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <random>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "engine.hpp"
+#include "tcgemm.cuh"
+
+namespace ccx {
+
+namespace {
+void sck(cudaError_t e, const char *w) {
+  if (e != cudaSuccess) throw EngineError(2, std::string(w) + ": " + cudaGetErrorString(e));
+}
+struct Dev {
+  void *p = nullptr;
+  explicit Dev(size_t b) { sck(cudaMalloc(&p, std::max<size_t>(b, 16)), "cudaMalloc"); }
+  ~Dev() { cudaFree(p); }
+};
+}  // namespace
+
+// problems: M_i, N_i, K_i for i < nprob.  Returns max |C - C_ref| / max |C_ref| over all
+// problems and the kernel time (ms).
+void tc_selftest(int device, int kind, int nprob, const int *Ms, const int *Ns, const int *Ks, int use_alo, uint64_t seed,
+                 double *max_rel, double *ms) {
+  sck(cudaSetDevice(device), "cudaSetDevice");
+  const int tk = kind == kTcBF16 ? 64 : 32;
+  const int es = kind == kTcBF16 ? 2 : 4;
+  std::mt19937_64 rng(seed);
+  std::uniform_real_distribution<double> U(-1.0, 1.0);
+  struct Host {
+    int M, N, K, nk, npad, mpad;
+    std::vector<double> A, B, C;
+    size_t a_el, b_el;
+  };
+  std::vector<Host> h(nprob);
+  size_t a_tot = 0, b_tot = 0, c_tot = 0;
+  int npad_max = 16;
+  for (int i = 0; i < nprob; ++i) {
+    Host &x = h[i];
+    x.M = Ms[i];
+    x.N = Ns[i];
+    x.K = Ks[i];
+    if (x.M <= 0 || x.N <= 0 || x.N > 256 || x.K <= 0) throw EngineError(1, "selftest: bad problem shape");
+    x.nk = (x.K + tk - 1) / tk;
+    x.npad = (x.N + 15) / 16 * 16;
+    x.mpad = (x.M + 127) / 128 * 128;
+    npad_max = std::max(npad_max, x.npad);
+    x.A.resize((size_t)x.M * x.K);
+    x.B.resize((size_t)x.K * x.N);
+    x.C.resize((size_t)x.M * x.N);
+    // entries spanning a few decades, as CCD operands do
+    for (double &v : x.A) v = U(rng) * std::pow(10.0, -3.0 * std::fabs(U(rng)));
+    for (double &v : x.B) v = U(rng) * std::pow(10.0, -3.0 * std::fabs(U(rng)));
+    for (double &v : x.C) v = U(rng);
+    x.a_el = (size_t)x.mpad * x.nk * tk;
+    x.b_el = (size_t)x.npad * x.nk * tk;
+    a_tot += x.a_el;
+    b_tot += x.b_el;
+    c_tot += x.C.size();
+  }
+  // FP64 device copies of the inputs (A row-major M x K, B column-major K x N, C col-major)
+  size_t fa = 0, fb = 0;
+  for (auto &x : h) { fa += x.A.size(); fb += x.B.size(); }
+  Dev dA(fa * 8), dB(fb * 8), dC(c_tot * 8), tAh(a_tot * es), tAl(a_tot * es), tBh(b_tot * es), tBl(b_tot * es);
+  std::vector<TcSplitJob> jobs;
+  std::vector<TcProb> probs;
+  std::vector<TcTile> tiles;
+  size_t oa = 0, ob = 0, oc = 0, ta = 0, tb = 0;
+  int64_t max_el = 0;
+  for (int i = 0; i < nprob; ++i) {
+    Host &x = h[i];
+    sck(cudaMemcpy((double *)dA.p + oa, x.A.data(), x.A.size() * 8, cudaMemcpyHostToDevice), "copy A");
+    sck(cudaMemcpy((double *)dB.p + ob, x.B.data(), x.B.size() * 8, cudaMemcpyHostToDevice), "copy B");
+    sck(cudaMemcpy((double *)dC.p + oc, x.C.data(), x.C.size() * 8, cudaMemcpyHostToDevice), "copy C");
+    TcSplitJob ja{};
+    ja.src = (double *)dA.p + oa; ja.sub = nullptr; ja.sr = x.K; ja.sk = 1;
+    ja.rows = x.M; ja.cols = x.K; ja.tile_rows = 128; ja.nk = x.nk; ja.rows_pad = x.mpad;
+    ja.hi = (char *)tAh.p + ta * es; ja.lo = (char *)tAl.p + ta * es; ja.scale = 1.0;
+    TcSplitJob jb{};
+    jb.src = (double *)dB.p + ob; jb.sub = nullptr; jb.sr = x.K; jb.sk = 1;  // B(n, k) = B_colmajor[k + K n]
+    jb.rows = x.N; jb.cols = x.K; jb.tile_rows = x.npad; jb.nk = x.nk; jb.rows_pad = x.npad;
+    jb.hi = (char *)tBh.p + tb * es; jb.lo = (char *)tBl.p + tb * es; jb.scale = 1.0;
+    jobs.push_back(ja);
+    jobs.push_back(jb);
+    max_el = std::max<int64_t>({max_el, (int64_t)x.a_el, (int64_t)x.b_el});
+    TcProb p{};
+    p.Ahi = ja.hi; p.Alo = use_alo ? ja.lo : nullptr; p.Bhi = jb.hi; p.Blo = jb.lo;
+    p.M = x.M; p.N = x.N; p.nk = x.nk; p.npad = x.npad;
+    p.C = (double *)dC.p + oc; p.sCm = 1; p.sCn = x.M; p.alpha = 0.5;
+    for (int mt = 0; mt < x.mpad / 128; ++mt) tiles.push_back(TcTile{i, mt});
+    probs.push_back(p);
+    oa += x.A.size(); ob += x.B.size(); oc += x.C.size(); ta += x.a_el; tb += x.b_el;
+  }
+  Dev dJ(jobs.size() * sizeof(TcSplitJob)), dP(probs.size() * sizeof(TcProb)), dT(tiles.size() * sizeof(TcTile)), dE(4);
+  sck(cudaMemcpy(dJ.p, jobs.data(), jobs.size() * sizeof(TcSplitJob), cudaMemcpyHostToDevice), "copy jobs");
+  sck(cudaMemcpy(dP.p, probs.data(), probs.size() * sizeof(TcProb), cudaMemcpyHostToDevice), "copy probs");
+  sck(cudaMemcpy(dT.p, tiles.data(), tiles.size() * sizeof(TcTile), cudaMemcpyHostToDevice), "copy tiles");
+  sck(cudaMemset(dE.p, 0, 4), "memset");
+  launch_tc_split(kind, (const TcSplitJob *)dJ.p, (int)jobs.size(), max_el, 0);
+  sck(cudaGetLastError(), "split launch");
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventRecord(e0);
+  launch_tc_gemm(kind, (const TcProb *)dP.p, (const TcTile *)dT.p, (int)tiles.size(), npad_max, (int *)dE.p, 0);
+  cudaEventRecord(e1);
+  sck(cudaGetLastError(), "tc gemm launch");
+  sck(cudaEventSynchronize(e1), "tc gemm");
+  float t = 0.f;
+  cudaEventElapsedTime(&t, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  *ms = t;
+  int err = 0;
+  sck(cudaMemcpy(&err, dE.p, 4, cudaMemcpyDeviceToHost), "copy err");
+  if (err) throw EngineError(2, "tensor-core GEMM reported error code " + std::to_string(err));
+  double worst = 0.0;
+  oc = 0;
+  for (auto &x : h) {
+    std::vector<double> c(x.C.size());
+    sck(cudaMemcpy(c.data(), (double *)dC.p + oc, c.size() * 8, cudaMemcpyDeviceToHost), "copy C back");
+    double scale = 0.0, diff = 0.0;
+    for (int n = 0; n < x.N; ++n)
+      for (int m = 0; m < x.M; ++m) {
+        double ref = 0.0;
+        for (int k = 0; k < x.K; ++k) ref += x.A[(size_t)m * x.K + k] * x.B[(size_t)k + (size_t)x.K * n];
+        const double prod = 0.5 * ref;
+        scale = std::max(scale, std::fabs(prod));
+        diff = std::max(diff, std::fabs(c[m + (size_t)x.M * n] - (x.C[m + (size_t)x.M * n] + prod)));
+      }
+    worst = std::max(worst, diff / std::max(scale, 1e-300));
+    oc += x.C.size();
+  }
+  *max_rel = worst;
+}
+
+}  // namespace ccx

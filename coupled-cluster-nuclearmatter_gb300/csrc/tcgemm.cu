@@ -1,0 +1,315 @@
+// Tensor-core split-precision GEMM on sm_103a (tcgen05 + TMEM + bulk async copies).
+//
+// C(fp64) += alpha * (A_hi B_hi + A_hi B_lo + A_lo B_hi), with the hi/lo pairs of BF16
+// (kind::f16) or TF32 (kind::tf32) operands, FP32 accumulation in tensor memory.
+// One CTA of 128 threads per 128-row tile of one problem, all N (<= 256) columns in one
+// accumulator.  Thread 0 streams the pre-tiled K tiles of A and B into a ring of
+// shared-memory stages with cp.async.bulk (one contiguous copy per operand tile,
+// completion on an mbarrier) and issues the MMAs; tcgen05.commit releases each stage.
+// The four warps then read their 32 TMEM lanes (rows) with tcgen05.ld and add into C.
+// Every mbarrier wait is bounded by a clock budget: on expiry the kernel records an
+// error code, lets its own copies land, frees its TMEM and returns.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+
+#include "tcgemm.cuh"
+
+namespace ccx {
+
+namespace {
+
+constexpr long long kWaitBudget = 4000000000LL;  // cycles (~2 s at 2 GHz)
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// bounded wait: true when the phase completed, false when the clock budget ran out
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+  const long long t0 = clock64();
+  while (!mbar_try_wait(bar, parity)) {
+    if (clock64() - t0 > kWaitBudget) return false;
+  }
+  return true;
+}
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+               "l"(src), "r"(bytes), "r"(bar)
+               : "memory");
+}
+__device__ __forceinline__ void tmem_alloc(uint32_t slot, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(slot), "r"(ncols) : "memory");
+}
+__device__ __forceinline__ void tmem_relinquish() {
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+template <int KIND>
+__device__ __forceinline__ void tc_mma(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+  if (KIND == kTcBF16)
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
+        "l"(a), "l"(b), "r"(idesc), "r"(acc)
+        : "memory");
+  else
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
+        "l"(a), "l"(b), "r"(idesc), "r"(acc)
+        : "memory");
+}
+__device__ __forceinline__ void tc_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t (&r)[8]) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr)
+               : "memory");
+}
+__device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+// shared-memory matrix descriptor: canonical K-major, no swizzle, LBO 128 B (next core
+// matrix along K), SBO 1024 B (next 8-row group), descriptor version 1
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
+  return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)(128u >> 4) << 16) | ((uint64_t)(1024u >> 4) << 32) |
+         (1ull << 46);
+}
+// instruction descriptor: D f32, A/B bf16 (kind::f16) or tf32 (kind::tf32), both K-major
+template <int KIND>
+__device__ __forceinline__ uint32_t instr_desc(int m, int n) {
+  const uint32_t fmt = KIND == kTcBF16 ? 1u : 2u;
+  return (1u << 4) | (fmt << 7) | (fmt << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+
+template <int KIND>
+__global__ void __launch_bounds__(128, 1) k_tc_gemm(const TcProb *__restrict__ probs, const TcTile *__restrict__ tiles,
+                                                   int stages, int npad_max, int *err) {
+  extern __shared__ __align__(1024) uint8_t smem[];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const TcTile tl = tiles[blockIdx.x];
+  const TcProb &P = probs[tl.prob];
+  const int npad = P.npad, nk = P.nk;
+  if (npad < 16 || npad > 256 || (npad & 15) || npad > npad_max) {
+    if (tid == 0) atomicExch(err, 4);
+    return;
+  }
+  constexpr uint32_t a_bytes = 128u * 128u;
+  const uint32_t b_bytes = (uint32_t)npad * 128u;
+  const uint32_t stage_bytes = 2u * a_bytes + 2u * (uint32_t)npad_max * 128u;
+  uint64_t *full = (uint64_t *)(smem + (size_t)stages * stage_bytes);
+  uint64_t *empty = full + stages;
+  uint64_t *done = empty + stages;
+  uint32_t *tmem_slot = (uint32_t *)(done + 1);
+  uint32_t ncols = 32;
+  while (ncols < (uint32_t)npad) ncols <<= 1;
+
+  if (warp == 0) {
+    tmem_alloc(smem_u32(tmem_slot), ncols);
+    tmem_relinquish();
+  }
+  if (tid == 0) {
+    for (int s = 0; s < stages; ++s) {
+      mbar_init(smem_u32(&full[s]), 1);
+      mbar_init(smem_u32(&empty[s]), 1);
+    }
+    mbar_init(smem_u32(done), 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+  const bool two_a = P.Alo != nullptr;
+
+  if (tid == 0) {
+    const uint8_t *Ahi = (const uint8_t *)P.Ahi + (size_t)tl.mt * nk * a_bytes;
+    const uint8_t *Alo = two_a ? (const uint8_t *)P.Alo + (size_t)tl.mt * nk * a_bytes : nullptr;
+    const uint8_t *Bhi = (const uint8_t *)P.Bhi;
+    const uint8_t *Blo = (const uint8_t *)P.Blo;
+    const uint32_t tx = (two_a ? 2u : 1u) * a_bytes + 2u * b_bytes;
+    int issued[8] = {0, 0, 0, 0, 0, 0, 0, 0}, landed[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    auto load = [&](int kt, int s) {
+      uint8_t *st = smem + (size_t)s * stage_bytes;
+      const uint32_t fb = smem_u32(&full[s]);
+      mbar_expect_tx(fb, tx);
+      bulk_g2s(smem_u32(st), Ahi + (size_t)kt * a_bytes, a_bytes, fb);
+      if (two_a) bulk_g2s(smem_u32(st + a_bytes), Alo + (size_t)kt * a_bytes, a_bytes, fb);
+      bulk_g2s(smem_u32(st + 2 * a_bytes), Bhi + (size_t)kt * b_bytes, b_bytes, fb);
+      bulk_g2s(smem_u32(st + 2 * a_bytes + (size_t)npad_max * 128), Blo + (size_t)kt * b_bytes, b_bytes, fb);
+      ++issued[s];
+    };
+    const uint32_t idesc = instr_desc<KIND>(128, npad);
+    const int pre = min(stages, nk);
+    for (int s = 0; s < pre; ++s) load(s, s);
+    int code = 0;
+    for (int kt = 0; kt < nk; ++kt) {
+      const int s = kt % stages;
+      const uint32_t ph = (uint32_t)(kt / stages) & 1u;
+      if (!mbar_wait(smem_u32(&full[s]), ph)) {
+        code = 1;
+        break;
+      }
+      ++landed[s];
+      tc_fence_after();
+      const uint32_t sa = smem_u32(smem + (size_t)s * stage_bytes);
+      const uint32_t sal = sa + a_bytes;
+      const uint32_t sb = sa + 2 * a_bytes;
+      const uint32_t sbl = sb + (uint32_t)npad_max * 128u;
+#pragma unroll
+      for (int ks = 0; ks < 4; ++ks) {
+        const uint32_t o = (uint32_t)ks * 256u;
+        const uint32_t acc0 = (kt > 0 || ks > 0) ? 1u : 0u;
+        tc_mma<KIND>(tmem, smem_desc(sa + o), smem_desc(sb + o), idesc, acc0);
+        tc_mma<KIND>(tmem, smem_desc(sa + o), smem_desc(sbl + o), idesc, 1u);
+        if (two_a) tc_mma<KIND>(tmem, smem_desc(sal + o), smem_desc(sb + o), idesc, 1u);
+      }
+      tc_commit(smem_u32(&empty[s]));
+      if (kt + stages < nk) {
+        if (!mbar_wait(smem_u32(&empty[s]), ph)) {
+          code = 2;
+          break;
+        }
+        load(kt + stages, s);
+      }
+    }
+    tc_commit(smem_u32(done));
+    if (code) {
+      atomicExch(err, code);
+      // let this CTA's own copies land before the shared memory goes away
+      for (int s = 0; s < stages; ++s)
+        while (landed[s] < issued[s]) {
+          if (!mbar_wait(smem_u32(&full[s]), (uint32_t)landed[s] & 1u)) break;
+          ++landed[s];
+        }
+    }
+  }
+  __syncwarp();
+  const bool fin = mbar_wait(smem_u32(done), 0);
+  if (!fin && lane == 0) atomicExch(err, 3);
+  tc_fence_after();
+  const int row = warp * 32 + lane;
+  const int m = tl.mt * 128 + row;
+  const uint32_t tl_addr = tmem + ((uint32_t)(warp * 32) << 16);
+  for (int c0 = 0; c0 < npad; c0 += 8) {
+    uint32_t r[8];
+    tmem_ld8(tl_addr + (uint32_t)c0, r);
+    tmem_ld_wait();
+    if (fin && m < P.M) {
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const int n = c0 + j;
+        if (n < P.N) P.C[(int64_t)m * P.sCm + (int64_t)n * P.sCn] += P.alpha * (double)__uint_as_float(r[j]);
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    tmem_dealloc(tmem, ncols);
+  }
+}
+
+// ---- operand preparation ---------------------------------------------------------
+template <int KIND> struct Half;
+template <> struct Half<kTcBF16> {
+  using T = __nv_bfloat16;
+  static constexpr int per16 = 8;  // elements per 16 bytes
+  __device__ static void split(double x, T &hi, T &lo) {
+    hi = __float2bfloat16_rn((float)x);
+    lo = __float2bfloat16_rn((float)(x - (double)__bfloat162float(hi)));
+  }
+};
+__device__ __forceinline__ float to_tf32(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return __uint_as_float(r);
+}
+template <> struct Half<kTcTF32> {
+  using T = float;
+  static constexpr int per16 = 4;
+  __device__ static void split(double x, T &hi, T &lo) {
+    hi = to_tf32((float)x);
+    lo = to_tf32((float)(x - (double)hi));
+  }
+};
+
+template <int KIND>
+__global__ void k_tc_split(const TcSplitJob *__restrict__ jobs) {
+  using H = Half<KIND>;
+  using T = typename H::T;
+  const TcSplitJob J = jobs[blockIdx.y];
+  constexpr int cme = H::per16;      // elements per core-matrix row
+  constexpr int tk = 8 * cme;        // elements per 128-byte tile row
+  const int64_t tile_elems = (int64_t)J.tile_rows * tk;
+  const int64_t total = (int64_t)(J.rows_pad / J.tile_rows) * J.nk * tile_elems;
+  T *hi = (T *)J.hi, *lo = (T *)J.lo;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t t = e / tile_elems;
+    const int w = (int)(e % tile_elems);
+    const int rt = (int)(t / J.nk), kt = (int)(t % J.nk);
+    const int cm = w / (8 * cme), in = w % (8 * cme);
+    const int row = rt * J.tile_rows + (cm / 8) * 8 + in / cme;
+    const int k = kt * tk + (cm % 8) * cme + in % cme;
+    double x = 0.0;
+    if (row < J.rows && k < J.cols) {
+      const int64_t o = (int64_t)row * J.sr + (int64_t)k * J.sk;
+      x = J.src[o];
+      if (J.sub) x -= J.sub[o];
+      x *= J.scale;
+    }
+    T h, l;
+    H::split(x, h, l);
+    hi[e] = h;
+    if (lo) lo[e] = l;
+  }
+}
+
+}  // namespace
+
+void launch_tc_gemm(int kind, const TcProb *probs, const TcTile *tiles, int ntiles, int npad_max, int *err,
+                    cudaStream_t st) {
+  if (ntiles <= 0) return;
+  const size_t stage_bytes = 2 * 128 * 128 + 2 * (size_t)npad_max * 128;
+  const size_t budget = 227 * 1024 - 256;
+  int stages = (int)std::min<size_t>(4, budget / stage_bytes);
+  if (stages < 1) stages = 1;
+  const size_t smem = (size_t)stages * stage_bytes + (2 * stages + 1) * 8 + 16;
+  if (kind == kTcBF16) {
+    cudaFuncSetAttribute(k_tc_gemm<kTcBF16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_tc_gemm<kTcBF16><<<ntiles, 128, smem, st>>>(probs, tiles, stages, npad_max, err);
+  } else {
+    cudaFuncSetAttribute(k_tc_gemm<kTcTF32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_tc_gemm<kTcTF32><<<ntiles, 128, smem, st>>>(probs, tiles, stages, npad_max, err);
+  }
+}
+
+void launch_tc_split(int kind, const TcSplitJob *jobs, int njobs, int64_t max_elems, cudaStream_t st) {
+  if (njobs <= 0) return;
+  const int bx = (int)std::min<int64_t>((max_elems + 255) / 256, 2048);
+  dim3 grid(std::max(bx, 1), njobs);
+  if (kind == kTcBF16) k_tc_split<kTcBF16><<<grid, 256, 0, st>>>(jobs);
+  else k_tc_split<kTcTF32><<<grid, 256, 0, st>>>(jobs);
+}
+
+}  // namespace ccx

@@ -1,0 +1,52 @@
+// Tensor-core (tcgen05) split-precision GEMM: C(fp64) += alpha * A B with A, B given
+// as hi/lo pairs of BF16 (or TF32) in a pre-tiled K-major layout.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace ccx {
+
+// Pre-tiled operand layout (both operands K-major, 128-byte K tiles):
+//   A (M x K): tile (mt, kt) of 128 rows x 128 bytes of K at element offset
+//              (mt * nk + kt) * 128 * kTileK, rows padded to a multiple of 128;
+//   B (N x K): tile kt of npad rows x 128 bytes at element offset kt * npad * kTileK.
+// Inside a tile the rows form 8-row groups of eight 8x16-byte core matrices along K:
+//   byte offset of (row, kbyte) = ((row/8)*8 + kbyte/16)*128 + (row%8)*16 + kbyte%16,
+// i.e. the canonical SWIZZLE_NONE K-major layout with LBO = 128 B, SBO = 1024 B.
+enum TcKind { kTcBF16 = 0, kTcTF32 = 1 };
+
+struct TcProb {
+  const void *Ahi, *Alo;  // pre-tiled A (this problem), nullptr Alo: A taken as hi only
+  const void *Bhi, *Blo;  // pre-tiled B
+  int M, N, nk, npad;     // rows, columns, K tiles, padded columns (multiple of 16, <= 256)
+  double *C;              // C(m, n) at C[m * sCm + n * sCn]
+  int64_t sCm, sCn;
+  double alpha;
+};
+struct TcTile {
+  int prob, mt;
+};
+
+// elements of one 128-byte K tile row
+inline int tc_tile_k(int kind) { return kind == kTcBF16 ? 64 : 32; }
+
+// error codes written to *err (0 = ok): 1 load wait timed out, 2 MMA wait timed out,
+// 3 final wait timed out, 4 bad problem (npad > 256 or not a multiple of 16)
+void launch_tc_gemm(int kind, const TcProb *probs, const TcTile *tiles, int ntiles, int npad_max, int *err,
+                    cudaStream_t st);
+
+// FP64 matrix (rows x cols, element (r, k) at src[r*sr + k*sk], optionally minus sub at
+// the same strides) -> pre-tiled hi/lo pair, zero padded.  tile_rows = 128 for an A
+// operand, npad for a B operand; nk = ceil(cols / tile_k).
+struct TcSplitJob {
+  const double *src, *sub;
+  int64_t sr, sk;
+  int rows, cols, tile_rows, nk, rows_pad;
+  void *hi, *lo;
+  double scale;
+};
+void launch_tc_split(int kind, const TcSplitJob *jobs, int njobs, int64_t max_elems, cudaStream_t st);
+
+}  // namespace ccx

@@ -261,6 +261,13 @@ const char *ccx_last_error(void);
 int ccx_engine_stream(const ccx_engine *e, void **stream);
 /* measured FP64 FMA throughput of the device (TFLOP/s), from a register-only probe */
 int ccx_device_fp64_peak(int32_t device, double *tflops);
+/* Self-test of the tensor-core split GEMM used by CCX_PREC_MIXED: nprob random
+ * problems C += 1/2 A B (M_i x K_i times K_i x N_i, N_i <= 256) through the same
+ * operand tiling and tcgen05 kernel, against an FP64 host product.
+ * kind 0: BF16 hi/lo split, kind 1: TF32 hi/lo split; use_alo 0 drops the A_lo term.
+ * *max_rel_err = max |C - C_ref| / max |1/2 A B| over the problems; *ms kernel time. */
+int ccx_selftest_tc_gemm(int32_t device, int32_t kind, int32_t nprob, const int32_t *M, const int32_t *N,
+                         const int32_t *K, int32_t use_alo, uint64_t seed, double *max_rel_err, double *ms);
 /* kernel launches issued by this engine since creation */
 int ccx_engine_launches(const ccx_engine *e, int64_t *launches);
 /* per-term device milliseconds of the last ccx_ccd_iter:
