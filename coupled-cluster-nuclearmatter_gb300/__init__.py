@@ -23,7 +23,7 @@ CH_PH_PHHP, CH_PH_HPHP, CH_PH_HPPH = 11, 12, 13
 V_PPPP = 6
 POT_MINNESOTA, POT_CHIRAL_LIKE = 0, 1
 MODE_REFERENCE, MODE_STANDARD = 0, 1
-PREC_FP64, PREC_MIXED = 0, 1
+PREC_FP64, PREC_MIXED, PREC_MIXED_TF32 = 0, 1, 2
 SCALAR_COMPLEX, SCALAR_REAL = 0, 1
 
 
@@ -73,7 +73,8 @@ class _IterOpts(C.Structure):
 
 class _IterResult(C.Structure):
     _fields_ = [("iterations", C.c_int32), ("converged", C.c_int32), ("e_mbpt2", C.c_double * 2),
-                ("e_ccd", C.c_double * 2), ("res_norm", C.c_double), ("seconds", C.c_double)]
+                ("e_ccd", C.c_double * 2), ("res_norm", C.c_double), ("seconds", C.c_double),
+                ("fp64_sweeps", C.c_int32), ("mixed_iterations", C.c_int32)]
 
 
 _lib = None
@@ -391,13 +392,14 @@ class Engine:
         return x.value
 
     def ccd_iter(self, mode=MODE_REFERENCE, precision=PREC_FP64, max_iter=100, tol=1e-6, diis_dim=8,
-                 defect_period=4, verbose=False) -> dict:
+                 defect_period=0, verbose=False) -> dict:
         o = _IterOpts(mode, precision, max_iter, tol, diis_dim, defect_period, int(verbose))
         r = _IterResult()
         _check(lib().ccx_ccd_iter(self._h, C.byref(o), C.byref(r)))
         return {"iterations": r.iterations, "converged": bool(r.converged),
                 "e_mbpt2": complex(r.e_mbpt2[0], r.e_mbpt2[1]), "e_ccd": complex(r.e_ccd[0], r.e_ccd[1]),
-                "res_norm": r.res_norm, "seconds": r.seconds}
+                "res_norm": r.res_norm, "seconds": r.seconds, "fp64_sweeps": r.fp64_sweeps,
+                "mixed_iterations": r.mixed_iterations}
 
     def pert_triples(self) -> complex:
         z = np.zeros(2)

@@ -460,6 +460,8 @@ int ccx_ccd_iter(ccx_engine *e, const ccx_iter_opts *opt, ccx_iter_result *res) 
     res->e_ccd[1] = r.e_ccd[1];
     res->res_norm = r.res_norm;
     res->seconds = r.seconds;
+    res->fp64_sweeps = r.fp64_sweeps;
+    res->mixed_iterations = r.mixed_iterations;
   });
 }
 int ccx_pert_triples(ccx_engine *e, double et[2]) {

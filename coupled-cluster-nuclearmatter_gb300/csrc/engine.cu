@@ -14,6 +14,7 @@
 #include "devlayout.hpp"
 #include "engine.hpp"
 #include "kernels.hpp"
+#include "tcgemm.cuh"
 #include "triples.hpp"
 
 namespace ccx {
@@ -212,6 +213,7 @@ class Engine final : public IEngine {
         CK(cudaMemcpyAsync(v4_.as<double>() + 2 * v4_off_h_[ch], v, (size_t)n * n * 2 * sizeof(double),
                            cudaMemcpyHostToDevice, st_));
         dirty_ = true;
+        ++v_version_;
         return;
       }
       case 2:
@@ -234,6 +236,7 @@ class Engine final : public IEngine {
     ++launches_;
     check_flag("V block has a non-zero imaginary part but the engine is real");
     dirty_ = true;
+    ++v_version_;
   }
 
   void generate(const PotentialSpec &p) override {
@@ -253,6 +256,7 @@ class Engine final : public IEngine {
     generated_ = true;
     pot_ = pot;
     dirty_ = true;
+    ++v_version_;
     vph_ready_ = false;
     commit();
   }
@@ -421,7 +425,10 @@ class Engine final : public IEngine {
 
   void ccd_iter(const IterOpts &o, IterResult &r) override {
     require_ready();
-    if (o.precision != 0) throw EngineError(1, "mixed precision is not available in this build of the engine");
+    if (o.precision < 0 || o.precision > 2) throw EngineError(1, "unknown precision");
+    if (o.precision != 0 && o.mode != 1) throw EngineError(1, "mixed precision runs with the standard (DIIS) mode");
+    if (o.precision != 0 && ScalarOf<S>::complex)
+      throw EngineError(1, "mixed precision is implemented for real interactions (real engine)");
     r = IterResult();
     double e[2];
     energy(e);
@@ -926,15 +933,37 @@ class Engine final : public IEngine {
     r.e_ccd[1] = e2.imag();
   }
 
+  // Standard mode: Jacobi step + Pulay DIIS on the steps.  With mixed precision the
+  // residual is evaluated as R(T_b) [cached, FP64] + tensor-core corrections in
+  // T - T_b (defect correction); an FP64 residual re-bases T_b when the mixed residual
+  // has dropped by kRebaseDrop since the last FP64 one, stalls, reaches the tolerance,
+  // or every defect_period iterations, and only an FP64 residual can end the solve.
   void iterate_standard(const IterOpts &o, IterResult &r) {
+    const bool mixed = o.precision != 0;
+    constexpr double kRebaseDrop = 1e-4;
+    if (mixed) {
+      prepare_mixed(o.precision == 2 ? kTcTF32 : kTcBF16);
+      set_base_zero();
+    }
     const int m = std::max(2, std::min(o.diis_dim, 15));
     hist_t_.alloc((size_t)m * n_t_ * sizeof(S), &bytes_);
     hist_e_.alloc((size_t)m * n_t_ * sizeof(S), &bytes_);
     std::vector<double> B((size_t)m * m, 0.0);
     int nh = 0, head = 0;
     double e[2] = {r.e_mbpt2[0], r.e_mbpt2[1]};
+    bool need_fp64 = false;
+    double phase_r0 = -1.0, best = 1e300;
+    int stall = 0, since = 0;
     for (int it = 1; it <= o.max_iter; ++it) {
-      residual(true);
+      const bool exact = !mixed || need_fp64;
+      if (!mixed) residual(true);
+      else if (exact) {
+        residual_fp64_rebase();
+        ++r.fp64_sweeps;
+      } else {
+        residual_mixed();
+        ++r.mixed_iterations;
+      }
       S *ht = hist_t_.as<S>() + (int64_t)head * n_t_;
       S *he = hist_e_.as<S>() + (int64_t)head * n_t_;
       mark(7);
@@ -946,10 +975,28 @@ class Engine final : public IEngine {
       if (timing_) accumulate_timers(7, 8);
       e[0] = host_res_[0];
       e[1] = host_res_[1];
-      r.res_norm = 2.0 * std::sqrt(host_res_[2]);
+      const double rn = 2.0 * std::sqrt(host_res_[2]);
+      if (mixed) check_tc_error();
+      if (exact) r.res_norm = rn;
       r.iterations = it - 1;
-      if (o.verbose) std::printf("ccx it %3d |R| %.3e E %.12f\n", it, r.res_norm, e[0]);
-      if (r.res_norm < o.tol) { r.converged = 1; break; }
+      if (o.verbose) std::printf("ccx it %3d %s |R| %.3e E %.12f\n", it, exact ? "fp64 " : "mixed", rn, e[0]);
+      if (exact && rn < o.tol) { r.converged = 1; break; }
+      if (mixed) {
+        if (exact) {
+          need_fp64 = false;
+          phase_r0 = rn;
+          best = rn;
+          stall = 0;
+          since = 0;
+        } else {
+          ++since;
+          if (phase_r0 < 0) phase_r0 = rn;
+          if (rn < 0.9 * best) { best = rn; stall = 0; } else ++stall;
+          const bool periodic = o.defect_period > 0 && since >= o.defect_period;
+          const bool dropped = o.defect_period <= 0 && rn < kRebaseDrop * phase_r0;
+          if (rn < o.tol || stall >= 2 || periodic || dropped) need_fp64 = true;
+        }
+      }
       // Gram row of the new step against every stored step, with conjugation
       const int slot = head;
       if (nh < m) ++nh;
@@ -993,6 +1040,290 @@ class Engine final : public IEngine {
     r.e_ccd[1] = e[1];
   }
 
+  // ================================================================== mixed precision
+  struct TcPlan {
+    DBuf probs, tiles;
+    int ntiles = 0, npad_max = 16;
+  };
+  struct SplitPlan {
+    DBuf jobs;
+    int njobs = 0;
+    int64_t max_el = 0;
+  };
+  struct TileBuf {
+    DBuf hi, lo;
+    int64_t n = 0;  // elements
+  };
+  void finalize_tc(TcPlan &pl, const std::vector<TcProb> &probs, const std::vector<TcTile> &tiles, int npad_max) {
+    upload(pl.probs, probs, &bytes_);
+    upload(pl.tiles, tiles, &bytes_);
+    pl.ntiles = (int)tiles.size();
+    pl.npad_max = npad_max;
+  }
+  void finalize_split(SplitPlan &pl, const std::vector<TcSplitJob> &jobs) {
+    upload(pl.jobs, jobs, &bytes_);
+    pl.njobs = (int)jobs.size();
+    pl.max_el = 0;
+    for (const auto &j : jobs) pl.max_el = std::max<int64_t>(pl.max_el, (int64_t)(j.rows_pad / j.tile_rows) * j.nk * j.tile_rows * tc_tile_k(tc_kind_));
+  }
+  void run_tc(const TcPlan &pl) {
+    if (!pl.ntiles) return;
+    launch_tc_gemm(tc_kind_, (const TcProb *)pl.probs.p, (const TcTile *)pl.tiles.p, pl.ntiles, pl.npad_max,
+                   tcerr_.as<int>(), st_);
+    ++launches_;
+  }
+  void run_split(const SplitPlan &pl) {
+    if (!pl.njobs) return;
+    launch_tc_split(tc_kind_, (const TcSplitJob *)pl.jobs.p, pl.njobs, pl.max_el, st_);
+    ++launches_;
+  }
+  void check_tc_error() {
+    int err = 0;
+    CK(cudaMemcpyAsync(&host_flag_, tcerr_.p, sizeof(int), cudaMemcpyDeviceToHost, st_));
+    CK(cudaStreamSynchronize(st_));
+    err = host_flag_;
+    if (err) {
+      CK(cudaMemsetAsync(tcerr_.p, 0, sizeof(int), st_));
+      throw EngineError(2, "tensor-core GEMM reported error code " + std::to_string(err));
+    }
+  }
+
+  // Tile buffers, split jobs and tensor-core problem lists of the mixed residual.
+  void prepare_mixed(int kind) {
+    if (mixed_ready_ && tc_kind_ == kind && mixed_v_version_ == v_version_) return;
+    const Layout &L = *L_;
+    tc_kind_ = kind;
+    const int tk = tc_tile_k(kind);
+    const size_t es = kind == kTcBF16 ? 2 : 4;
+    auto mpad = [](int x) { return (x + 127) / 128 * 128; };
+    auto npadf = [](int x) { return (x + 15) / 16 * 16; };
+    auto nkf = [&](int x) { return (x + tk - 1) / tk; };
+    const int nc = L.fam[3].count(), nq = L.ph[1].count();
+    // sizes
+    TileBuf *bufs[8] = {&tVpp_, &tD_, &tVph_, &tDphB_, &tTphbA_, &tDphA_, &tdI4B_, &tI4B_};
+    for (TileBuf *b : bufs) b->n = 0;
+    for (int c = 0; c < nc; ++c) {
+      const auto &pk = L.pk[c];
+      if (pk.P <= 0 || pk.H <= 0) continue;
+      if (pk.H > 256) throw EngineError(1, "mixed precision: an hhpp channel has more than 256 packed hole pairs");
+      tVpp_.n += (int64_t)mpad(pk.P) * nkf(pk.P) * tk;
+      tD_.n += (int64_t)npadf(pk.H) * nkf(pk.P) * tk;
+    }
+    for (int q = 0; q < nq; ++q) {
+      const int nph = L.ph[1].side1[q].size(), nhp = L.ph[1].side2[q].size();
+      if (nph <= 0 || nhp <= 0) continue;
+      if (nhp > 256) throw EngineError(1, "mixed precision: a ring channel has more than 256 hole-particle pairs");
+      tVph_.n += (int64_t)mpad(nhp) * nkf(nph) * tk;
+      tDphB_.n += (int64_t)npadf(nhp) * nkf(nph) * tk;
+      tTphbA_.n += (int64_t)mpad(nph) * nkf(nhp) * tk;
+      tDphA_.n += (int64_t)mpad(nph) * nkf(nhp) * tk;
+      tdI4B_.n += (int64_t)npadf(nhp) * nkf(nhp) * tk;
+      tI4B_.n += (int64_t)npadf(nhp) * nkf(nhp) * tk;
+    }
+    for (TileBuf *b : bufs) {
+      b->hi.alloc((size_t)std::max<int64_t>(b->n, 16) * es, &bytes_);
+      b->lo.alloc((size_t)std::max<int64_t>(b->n, 16) * es, &bytes_);
+    }
+    const size_t sz = sizeof(S);
+    Tb_.alloc(std::max<int64_t>(n_t_, 1) * sz, &bytes_);
+    PPb_.alloc(std::max<int64_t>(n_t_, 1) * sz, &bytes_);
+    Tphb_.alloc(std::max<int64_t>(n_ph_, 1) * sz, &bytes_);
+    Rphb_.alloc(std::max<int64_t>(n_ph_, 1) * sz, &bytes_);
+    I4b_.alloc(std::max<int64_t>(n_i4_, 1) * sz, &bytes_);
+    dI4_.alloc(std::max<int64_t>(n_i4_, 1) * sz, &bytes_);
+    tcerr_.alloc(sizeof(int), &bytes_);
+    CK(cudaMemset(tcerr_.p, 0, sizeof(int)));
+    auto at = [&](TileBuf &b, int64_t off, bool hi) { return (void *)((char *)(hi ? b.hi.p : b.lo.p) + off * es); };
+    auto job = [&](const S *src, const S *sub, int64_t sr, int64_t sk, int rows, int cols, int tile_rows, int rows_pad,
+                   TileBuf &b, int64_t off) {
+      TcSplitJob j{};
+      j.src = (const double *)src;
+      j.sub = (const double *)sub;
+      j.sr = sr; j.sk = sk; j.rows = rows; j.cols = cols; j.tile_rows = tile_rows;
+      j.nk = nkf(cols); j.rows_pad = rows_pad;
+      j.hi = at(b, off, true); j.lo = at(b, off, false); j.scale = 1.0;
+      return j;
+    };
+    auto prob = [&](TileBuf &a, int64_t ao, TileBuf &b, int64_t bo, int M, int N, int K, S *C, int64_t sCm, int64_t sCn,
+                    double alpha) {
+      TcProb p{};
+      p.Ahi = at(a, ao, true); p.Alo = at(a, ao, false); p.Bhi = at(b, bo, true); p.Blo = at(b, bo, false);
+      p.M = M; p.N = N; p.nk = nkf(K); p.npad = npadf(N);
+      p.C = (double *)C; p.sCm = sCm; p.sCn = sCn; p.alpha = alpha;
+      return p;
+    };
+    std::vector<TcSplitJob> js_static, js_tphb, js_it1, js_it2;
+    std::vector<TcProb> pp, p4, pr1, pr2;
+    std::vector<TcTile> tp, t4, tr1, tr2;
+    int np_pp = 16, np_4 = 16, np_r = 16;
+    {
+      int64_t oa = 0, ob = 0, voff = 0;
+      for (int c = 0; c < nc; ++c) {
+        const auto &pk = L.pk[c];
+        if (pk.P > 0 && pk.H > 0) {
+          js_static.push_back(job(Vpp_.as<S>() + voff, nullptr, pk.P, 1, pk.P, pk.P, 128, mpad(pk.P), tVpp_, oa));
+          js_it1.push_back(job(T_.as<S>() + pk.t_off, Tb_.as<S>() + pk.t_off, pk.P, 1, pk.H, pk.P, npadf(pk.H),
+                               npadf(pk.H), tD_, ob));
+          for (int mt = 0; mt < mpad(pk.P) / 128; ++mt) tp.push_back(TcTile{(int)pp.size(), mt});
+          pp.push_back(prob(tVpp_, oa, tD_, ob, pk.P, pk.H, pk.P, R_.as<S>() + pk.t_off, 1, pk.P, 1.0));
+          np_pp = std::max(np_pp, npadf(pk.H));
+          oa += (int64_t)mpad(pk.P) * nkf(pk.P) * tk;
+          ob += (int64_t)npadf(pk.H) * nkf(pk.P) * tk;
+        }
+        voff += (int64_t)pk.P * pk.P;
+      }
+    }
+    {
+      int64_t ov = 0, odb = 0, ota = 0, oda = 0, oi = 0, oib = 0, toff = 0, ioff = 0;
+      for (int q = 0; q < nq; ++q) {
+        const int nph = L.ph[1].side1[q].size(), nhp = L.ph[1].side2[q].size();
+        if (nph > 0 && nhp > 0) {
+          S *tph = Tph_.as<S>() + toff, *tphb = Tphb_.as<S>() + toff;
+          // static A = V_ph (n_hp x n_ph, column-major)
+          js_static.push_back(job(Vph_.as<S>() + toff, nullptr, 1, nhp, nhp, nph, 128, mpad(nhp), tVph_, ov));
+          // per iteration: B = dTph (rows n_hp, K = n_ph), A = dTph (rows n_ph, K = n_hp)
+          js_it1.push_back(job(tph, tphb, nph, 1, nhp, nph, npadf(nhp), npadf(nhp), tDphB_, odb));
+          js_it1.push_back(job(tph, tphb, 1, nph, nph, nhp, 128, mpad(nph), tDphA_, oda));
+          // at re-base: A = Tph_b
+          js_tphb.push_back(job(tphb, nullptr, 1, nph, nph, nhp, 128, mpad(nph), tTphbA_, ota));
+          // after dI4: B = dI4 and B = I4 (rows n_hp, K = n_hp)
+          js_it2.push_back(job(dI4_.as<S>() + ioff, nullptr, nhp, 1, nhp, nhp, npadf(nhp), npadf(nhp), tdI4B_, oi));
+          js_it2.push_back(job(I4_.as<S>() + ioff, nullptr, nhp, 1, nhp, nhp, npadf(nhp), npadf(nhp), tI4B_, oib));
+          for (int mt = 0; mt < mpad(nhp) / 128; ++mt) t4.push_back(TcTile{(int)p4.size(), mt});
+          p4.push_back(prob(tVph_, ov, tDphB_, odb, nhp, nhp, nph, dI4_.as<S>() + ioff, 1, nhp, 0.5));
+          for (int mt = 0; mt < mpad(nph) / 128; ++mt) {
+            tr1.push_back(TcTile{(int)pr1.size(), mt});
+            tr2.push_back(TcTile{(int)pr2.size(), mt});
+          }
+          pr1.push_back(prob(tTphbA_, ota, tdI4B_, oi, nph, nhp, nhp, Rph_.as<S>() + toff, 1, nph, 1.0));
+          pr2.push_back(prob(tDphA_, oda, tI4B_, oib, nph, nhp, nhp, Rph_.as<S>() + toff, 1, nph, 1.0));
+          np_4 = std::max(np_4, npadf(nhp));
+          np_r = std::max(np_r, npadf(nhp));
+          ov += (int64_t)mpad(nhp) * nkf(nph) * tk;
+          odb += (int64_t)npadf(nhp) * nkf(nph) * tk;
+          ota += (int64_t)mpad(nph) * nkf(nhp) * tk;
+          oda += (int64_t)mpad(nph) * nkf(nhp) * tk;
+          oi += (int64_t)npadf(nhp) * nkf(nhp) * tk;
+          oib += (int64_t)npadf(nhp) * nkf(nhp) * tk;
+        }
+        toff += (int64_t)nph * nhp;
+        ioff += (int64_t)nhp * nhp;
+      }
+    }
+    finalize_split(spStatic_, js_static);
+    finalize_split(spTphb_, js_tphb);
+    finalize_split(spIter1_, js_it1);
+    finalize_split(spIter2_, js_it2);
+    finalize_tc(tcPP_, pp, tp, np_pp);
+    finalize_tc(tcI4_, p4, t4, np_4);
+    finalize_tc(tcR1_, pr1, tr1, np_r);
+    finalize_tc(tcR2_, pr2, tr2, np_r);
+    // FP64 plans of the re-base: PP_b = V_pppp' T, and R' += T I9
+    {
+      PlanBuilder bp, bh;
+      int64_t hoff = 0, voff = 0;
+      for (int c = 0; c < nc; ++c) {
+        const auto &pk = L.pk[c];
+        if (pk.H > 0 && pk.P > 0) {
+          GemmProb<S> a{};
+          a.nseg = 1;
+          a.M = pk.P; a.N = pk.H;
+          a.seg[0] = GemmSeg<S>{Vpp_.as<S>() + voff, T_.as<S>() + pk.t_off, pk.P, 1, 1, pk.P, pk.P, 1.0};
+          a.C = PPb_.as<S>() + pk.t_off; a.sCm = 1; a.sCn = pk.P; a.accumulate = 0;
+          bp.add(a, (int64_t)pk.P * pk.P * pk.H);
+          GemmProb<S> h{};
+          h.nseg = 1;
+          h.M = pk.P; h.N = pk.H;
+          h.seg[0] = GemmSeg<S>{T_.as<S>() + pk.t_off, I9_.as<S>() + hoff, 1, pk.P, 1, pk.H, pk.H, 1.0};
+          h.C = R_.as<S>() + pk.t_off; h.sCm = 1; h.sCn = pk.P; h.accumulate = 1;
+          bh.add(h, (int64_t)pk.P * pk.H * pk.H);
+        }
+        hoff += (int64_t)pk.H * pk.H;
+        voff += (int64_t)pk.P * pk.P;
+      }
+      finalize_plan(planPP_, bp);
+      finalize_plan(planHH_, bh);
+    }
+    commit();
+    run_split(spStatic_);
+    CK(cudaStreamSynchronize(st_));
+    mixed_ready_ = true;
+    mixed_v_version_ = v_version_;
+  }
+
+  // base T_b = 0: every cached product vanishes except I4_b = W
+  void set_base_zero() {
+    CK(cudaMemsetAsync(Tb_.p, 0, Tb_.bytes, st_));
+    CK(cudaMemsetAsync(PPb_.p, 0, PPb_.bytes, st_));
+    CK(cudaMemsetAsync(Tphb_.p, 0, Tphb_.bytes, st_));
+    CK(cudaMemsetAsync(Rphb_.p, 0, Rphb_.bytes, st_));
+    CK(cudaMemcpyAsync(I4b_.p, W_.p, std::max<int64_t>(n_i4_, 1) * sizeof(S), cudaMemcpyDeviceToDevice, st_));
+    run_split(spTphb_);
+  }
+
+  // FP64 residual at T that also becomes the new base of the defect correction
+  void residual_fp64_rebase() {
+    mark(0);
+    launch_gather_tph<S>(D_, T_.as<S>(), Tph_.as<S>(), st_);
+    mark(1);
+    run_plan(planX_);
+    launch_i7<S>(D_, X_.as<S>(), fdiag_.as<S>(), f7_.as<S>(), d2ij_.as<S>(), i7off_.as<S>(), st_);
+    launch_i9<S>(D_, n_hh2_, Vhh_.as<S>(), X_.as<S>(), I9_.as<S>(), st_);
+    mark(2);
+    launch_i6<S>(D_, T_.as<S>(), Vhp_.as<S>(), fdiag_.as<S>(), f6_.as<S>(), d2ab_.as<S>(), i6off_.as<S>(), st_);
+    mark(3);
+    run_plan(planI4_);
+    mark(4);
+    run_plan(planRing_);
+    mark(5);
+    launch_rinit<S>(D_, T_.as<S>(), Vhp_.as<S>(), Rph_.as<S>(), i6off_.as<S>(), i7off_.as<S>(), R_.as<S>(), st_);
+    mark(6);
+    run_plan(planPP_);
+    launch_axpy<S>(n_t_, PPb_.as<S>(), R_.as<S>(), st_);
+    run_plan(planHH_);
+    // the new base
+    CK(cudaMemcpyAsync(Tb_.p, T_.p, n_t_ * sizeof(S), cudaMemcpyDeviceToDevice, st_));
+    CK(cudaMemcpyAsync(Tphb_.p, Tph_.p, std::max<int64_t>(n_ph_, 1) * sizeof(S), cudaMemcpyDeviceToDevice, st_));
+    CK(cudaMemcpyAsync(Rphb_.p, Rph_.p, std::max<int64_t>(n_ph_, 1) * sizeof(S), cudaMemcpyDeviceToDevice, st_));
+    CK(cudaMemcpyAsync(I4b_.p, I4_.p, std::max<int64_t>(n_i4_, 1) * sizeof(S), cudaMemcpyDeviceToDevice, st_));
+    run_split(spTphb_);
+    mark(7);
+    launches_ += 6;
+    if (timing_) accumulate_timers(0, 7);
+  }
+
+  // mixed residual: the one-body, I9/I7 and I6 pieces in FP64, the ladder and ring
+  // contractions as cached FP64 products at T_b plus tensor-core corrections
+  void residual_mixed() {
+    mark(0);
+    launch_gather_tph<S>(D_, T_.as<S>(), Tph_.as<S>(), st_);
+    mark(1);
+    run_plan(planX_);
+    launch_i7<S>(D_, X_.as<S>(), fdiag_.as<S>(), f7_.as<S>(), d2ij_.as<S>(), i7off_.as<S>(), st_);
+    launch_i9<S>(D_, n_hh2_, Vhh_.as<S>(), X_.as<S>(), I9_.as<S>(), st_);
+    mark(2);
+    launch_i6<S>(D_, T_.as<S>(), Vhp_.as<S>(), fdiag_.as<S>(), f6_.as<S>(), d2ab_.as<S>(), i6off_.as<S>(), st_);
+    mark(3);
+    run_split(spIter1_);  // dT (B), dT_ph (B and A)
+    CK(cudaMemsetAsync(dI4_.p, 0, std::max<int64_t>(n_i4_, 1) * sizeof(S), st_));
+    run_tc(tcI4_);  // dI4 = 1/2 V_ph dT_ph
+    launch_add<S>(n_i4_, I4b_.as<S>(), dI4_.as<S>(), I4_.as<S>(), st_);
+    run_split(spIter2_);  // dI4 (B), I4 (B)
+    mark(4);
+    CK(cudaMemcpyAsync(Rph_.p, Rphb_.p, std::max<int64_t>(n_ph_, 1) * sizeof(S), cudaMemcpyDeviceToDevice, st_));
+    run_tc(tcR1_);  // R_ph += T_ph,b dI4
+    run_tc(tcR2_);  // R_ph += dT_ph I4
+    mark(5);
+    launch_rinit<S>(D_, T_.as<S>(), Vhp_.as<S>(), Rph_.as<S>(), i6off_.as<S>(), i7off_.as<S>(), R_.as<S>(), st_);
+    mark(6);
+    launch_axpy<S>(n_t_, PPb_.as<S>(), R_.as<S>(), st_);
+    run_tc(tcPP_);  // R' += V_pppp' dT
+    run_plan(planHH_);
+    mark(7);
+    launches_ += 7;
+    if (timing_) accumulate_timers(0, 7);
+  }
+
   // ================================================================== state
   std::shared_ptr<const Layout> L_;
   int device_ = 0;
@@ -1016,7 +1347,15 @@ class Engine final : public IEngine {
   // state
   DBuf T_, R_, Vhp_, Vpp_, Vhh_, X_, I9_, Tph_, Rph_, Vph_, W_, I4_, fdiag_, f6_, f7_, d2ij_, d2ab_, i6off_, i7off_;
   DBuf partial_, res_, flag_, stage_, hist_, hist_t_, hist_e_, splitk_;
-  Plan planX_, planLadder_, planI4_, planRing_;
+  Plan planX_, planLadder_, planI4_, planRing_, planPP_, planHH_;
+  // mixed precision
+  bool mixed_ready_ = false;
+  int tc_kind_ = 0;
+  int64_t v_version_ = 0, mixed_v_version_ = -1;
+  DBuf Tb_, PPb_, Tphb_, Rphb_, I4b_, dI4_, tcerr_;
+  TileBuf tVpp_, tD_, tVph_, tDphB_, tTphbA_, tDphA_, tdI4B_, tI4B_;
+  TcPlan tcPP_, tcI4_, tcR1_, tcR2_;
+  SplitPlan spStatic_, spTphb_, spIter1_, spIter2_;
   double *host_res_ = nullptr;
   int host_flag_ = 0;
   double e0_[2] = {0, 0};

@@ -17,15 +17,16 @@ struct EngineError : std::runtime_error {
 
 struct IterOpts {
   int mode = 0;          // 0 reference, 1 standard
-  int precision = 0;     // 0 FP64, 1 mixed
+  int precision = 0;     // 0 FP64, 1 mixed BF16x3, 2 mixed TF32x3
   int max_iter = 100;
   double tol = 1e-6;
   int diis_dim = 8;
-  int defect_period = 4;
+  int defect_period = 0;  // mixed: FP64 re-base every k iterations; 0 adaptive
   int verbose = 0;
 };
 struct IterResult {
   int iterations = 0, converged = 0;
+  int fp64_sweeps = 0, mixed_iterations = 0;
   double e_mbpt2[2] = {0, 0}, e_ccd[2] = {0, 0};
   double res_norm = 0.0, seconds = 0.0;
 };

@@ -741,6 +741,21 @@ void launch_unpack_vblock(const DevLayout &L, int kind, int ch, int n_rows, int 
     k_unpack_vblock<S><<<1216, 256, 0, st>>>(L, kind, ch, n_rows, n_cols, row_sgn, col_sgn, src, out);
 }
 
+template <typename S>
+__global__ void k_axpy(int64_t n, const S *__restrict__ x, S *__restrict__ y) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) y[i] += x[i];
+}
+template <typename S> void launch_axpy(int64_t n, const S *x, S *y, cudaStream_t st) {
+  if (n > 0) k_axpy<S><<<(int)std::min<int64_t>((n + 255) / 256, 2432), 256, 0, st>>>(n, x, y);
+}
+template <typename S>
+__global__ void k_add(int64_t n, const S *__restrict__ x, const S *__restrict__ y, S *__restrict__ z) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) z[i] = x[i] + y[i];
+}
+template <typename S> void launch_add(int64_t n, const S *x, const S *y, S *z, cudaStream_t st) {
+  if (n > 0) k_add<S><<<(int)std::min<int64_t>((n + 255) / 256, 2432), 256, 0, st>>>(n, x, y, z);
+}
+
 // register-only FMA chains; one store per thread
 __global__ void k_fp64_probe(double *out, int iters) {
   double x[8];
@@ -851,6 +866,8 @@ void launch_unpack_t(const DevLayout &L, int ch, int n_pp, const int *pp_signed,
                                    S *, S *, S *, double *, cudaStream_t);                                             \
   template void launch_mp2<S>(const DevLayout &, const S *, const S *, S *, cudaStream_t);                            \
   template void launch_pack_t<S>(const DevLayout &, int, int, const double *, S *, int *, cudaStream_t);          \
+  template void launch_axpy<S>(int64_t, const S *, S *, cudaStream_t);                                                 \
+  template void launch_add<S>(int64_t, const S *, const S *, S *, cudaStream_t);                                       \
   template void launch_gen_ordered<S>(const DevOrbits &, const DevPotential &, const int2 *, const int2 *, int, int,  \
                                       int, double *, cudaStream_t);                                                    \
   template void launch_unpack_vblock<S>(const DevLayout &, int, int, int, int, const int *, const int *, const S *,  \

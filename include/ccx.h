@@ -140,7 +140,9 @@ int ccx_layout_hash(const ccx_layout *l, uint64_t *hash);
 #define CCX_SCALAR_REAL 1      /* real arithmetic; V and Fock must be real */
 
 #define CCX_PREC_FP64 0        /* every term in FP64 */
-#define CCX_PREC_MIXED 1       /* ladder/ring GEMMs on the tensor cores (split products), FP64 defect correction */
+#define CCX_PREC_MIXED 1       /* ladder/ring contractions as BF16 hi/lo split products on the tensor
+                                  cores (FP32 accumulate), FP64 defect correction; standard mode, real engine */
+#define CCX_PREC_MIXED_TF32 2  /* as CCX_PREC_MIXED with TF32 hi/lo split products */
 
 #define CCX_MODE_REFERENCE 0   /* 0.75/0.25 mixing + DIIS every 6 (ccm_diis.f90:74-249), |dE| stop */
 #define CCX_MODE_STANDARD 1    /* Jacobi step + Pulay DIIS on steps, ||R - D T|| stop */
@@ -233,7 +235,8 @@ typedef struct {
   int32_t max_iter;          /* reference: 100 (ccm_iter.f90:71) */
   double tol;                /* reference: 1e-6 on |dE| (ccm_iter.f90:74) */
   int32_t diis_dim;          /* standard mode history length */
-  int32_t defect_period;     /* mixed precision: FP64 residual every k iterations */
+  int32_t defect_period;     /* mixed precision: FP64 re-base every k iterations; 0 = adaptive
+                                (when the mixed residual has dropped 1e4x, stalls or meets tol) */
   int32_t verbose;
 } ccx_iter_opts;
 
@@ -244,6 +247,8 @@ typedef struct {
   double e_ccd[2];           /* final correlation energy (eccsd - e0) */
   double res_norm;           /* ||R - D T|| of the last FP64 residual */
   double seconds;            /* device time of the loop */
+  int32_t fp64_sweeps;       /* mixed precision: FP64 residual evaluations (re-bases) */
+  int32_t mixed_iterations;  /* mixed precision: tensor-core residual evaluations */
 } ccx_iter_result;
 
 /* ccd_iter loop, ccm_iter.f90:67-133 */

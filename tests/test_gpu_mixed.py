@@ -1,0 +1,68 @@
+"""Mixed-precision CCD (tensor-core BF16x3 / TF32x3 contractions with FP64 defect
+correction) against the FP64 solve of the same engine and the oracle.
+
+Only an FP64 residual can end a mixed solve, so at the same tolerance the converged
+E/A agrees with the FP64 one to rounding; the spec bar is 1 keV/nucleon."""
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def solve(ccx, nmax, A, rho, precision, tol=1e-10, defect_period=0, snm=False):
+    L = ccx.Layout.from_basis(nmax, A, rho, snm=snm)
+    e = ccx.Engine(L, real=True)
+    e.generate()
+    e.setup_t_amplitudes()
+    r = e.ccd_iter(mode=ccx.MODE_STANDARD, precision=precision, tol=tol, max_iter=200, defect_period=defect_period)
+    return e, r
+
+
+@pytest.mark.parametrize("prec", ["bf16", "tf32"])
+def test_mixed_matches_fp64_pnm14(ccx, O, prec):
+    p = ccx.PREC_MIXED if prec == "bf16" else ccx.PREC_MIXED_TF32
+    e64, r64 = solve(ccx, 2, 14, 0.08, ccx.PREC_FP64)
+    em, rm = solve(ccx, 2, 14, 0.08, p)
+    assert r64["converged"] and rm["converged"]
+    assert rm["res_norm"] < 1e-10
+    assert rm["fp64_sweeps"] >= 1 and rm["mixed_iterations"] >= 1
+    assert abs(rm["e_ccd"] - r64["e_ccd"]) < 1e-10 * abs(r64["e_ccd"])
+    o = O.Oracle(O.Config(nmax=2, A=14, rho=0.08))
+    o.mp2()
+    ro = o.ccd_iter(mode=O.MODE_STANDARD, tol=1e-10)
+    assert abs(rm["e_ccd"] - ro["e_ccd"]) < 1e-10 * abs(ro["e_ccd"])
+
+
+def test_mixed_fixed_defect_period(ccx):
+    _, r64 = solve(ccx, 2, 14, 0.08, ccx.PREC_FP64)
+    _, rm = solve(ccx, 2, 14, 0.08, ccx.PREC_MIXED, defect_period=3)
+    assert rm["converged"] and abs(rm["e_ccd"] - r64["e_ccd"]) < 1e-10 * abs(r64["e_ccd"])
+
+
+def test_mixed_snm_minnesota(ccx):
+    _, r64 = solve(ccx, 2, 28, 0.16, ccx.PREC_FP64, snm=True)
+    _, rm = solve(ccx, 2, 28, 0.16, ccx.PREC_MIXED, snm=True)
+    assert rm["converged"] and abs(rm["e_ccd"] - r64["e_ccd"]) < 1e-10 * abs(r64["e_ccd"])
+
+
+def test_mixed_pnm66_full_size(ccx):
+    """PNM 66 at nmax=4 (1458 states): E/A of the mixed solve vs FP64, in keV."""
+    e64, r64 = solve(ccx, 4, 66, 0.16, ccx.PREC_FP64)
+    em, rm = solve(ccx, 4, 66, 0.16, ccx.PREC_MIXED)
+    assert rm["converged"] and rm["res_norm"] < 1e-10
+    dea_kev = abs((rm["e_ccd"] - r64["e_ccd"]).real) / 66 * 1e3
+    assert dea_kev < 1e-6  # well inside the 1 keV bar
+    assert rm["seconds"] < r64["seconds"]
+
+
+def test_mixed_rejects_unsupported(ccx):
+    L = ccx.Layout.from_basis(1, 2, 0.08)
+    ec = ccx.Engine(L, real=False)
+    ec.generate()
+    ec.setup_t_amplitudes()
+    with pytest.raises(ccx.CcxError):
+        ec.ccd_iter(mode=ccx.MODE_STANDARD, precision=ccx.PREC_MIXED)
+    er = ccx.Engine(L, real=True)
+    er.generate()
+    er.setup_t_amplitudes()
+    with pytest.raises(ccx.CcxError):
+        er.ccd_iter(mode=ccx.MODE_REFERENCE, precision=ccx.PREC_MIXED)
