@@ -129,6 +129,7 @@ def lib():
         "ccx_engine_stream": ([vp, C.POINTER(vp)], C.c_int),
         "ccx_device_fp64_peak": ([i32, C.POINTER(dbl)], C.c_int),
         "ccx_selftest_tc_gemm": ([i32, i32, i32, vp, vp, vp, i32, C.c_uint64, C.POINTER(dbl), C.POINTER(dbl)], C.c_int),
+        "ccx_ccd_energy_noalloc": ([i32, vp, vp, vp, vp, vp], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -170,6 +171,12 @@ def selftest_tc_gemm(shapes, kind: int = 0, use_alo: bool = True, seed: int = 1,
     _check(lib().ccx_selftest_tc_gemm(device, kind, len(shapes), _ptr(M), _ptr(N), _ptr(K), int(use_alo), seed,
                                       C.byref(err), C.byref(ms)))
     return err.value, ms.value
+
+
+def ccd_energy_noalloc(nch: int, dims_ptr: int, t2_ptr: int, vhhpp_ptr: int, energy_ptr: int, stream: int = 0):
+    """ccx_ccd_energy_noalloc on caller-owned device buffers (raw device pointers)."""
+    _check(lib().ccx_ccd_energy_noalloc(nch, vp(dims_ptr), vp(t2_ptr), vp(vhhpp_ptr), vp(energy_ptr),
+                                        vp(stream) if stream else None))
 
 
 def deck_parse(text: str) -> dict:

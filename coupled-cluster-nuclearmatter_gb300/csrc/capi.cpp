@@ -112,6 +112,10 @@ std::string lower(std::string s) {
 
 }  // namespace
 
+namespace ccx {
+void set_last_error(const std::string &msg) { g_err = msg; }
+}  // namespace ccx
+
 extern "C" {
 
 const char *ccx_last_error(void) { return g_err.c_str(); }

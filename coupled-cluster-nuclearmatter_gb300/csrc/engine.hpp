@@ -72,6 +72,8 @@ std::unique_ptr<IEngine> make_engine(std::shared_ptr<const Layout> L, int device
 void draw_lecs(uint64_t seed, double out[9]);
 // FP64 FMA throughput probe (TFLOP/s)
 double fp64_peak(int device);
+// message returned by ccx_last_error() on the calling thread
+void set_last_error(const std::string &msg);
 // tensor-core split GEMM self-test (tc_selftest.cu)
 void tc_selftest(int device, int kind, int nprob, const int *Ms, const int *Ns, const int *Ks, int use_alo, uint64_t seed,
                  double *max_rel, double *ms);

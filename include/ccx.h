@@ -226,6 +226,19 @@ int ccx_diis_setup(ccx_engine *e, int32_t subspace, int32_t diis_step);
 int ccx_diis_t1t2(ccx_engine *e, int32_t *count);
 /* ccd_energy_save(ener), ccm_energy.f90:4-71: 1/4 sum T(ab,ij) V(ij,ab) */
 int ccx_ccd_energy(ccx_engine *e, double ener[2]);
+/* The same correlation energy on caller-owned device buffers, allocating nothing.
+ * No counterpart in the reference.  For callers that cannot allocate device memory:
+ * a host that owns every device buffer through its own pool, or code running where
+ * an allocation is not allowed.  dims: device array of nch (n_hh, n_pp) pairs;
+ * t2 / vhhpp: device, the t2_ccm(ch)%val (n_pp x n_hh) and vnn_hhpp(ch)%val
+ * (n_hh x n_pp) blocks concatenated in channel order, complex interleaved; energy:
+ * device, 2 doubles.  Asynchronous on stream (NULL: the legacy default stream).
+ * Scratch is a static device array of 16384 channel slots (512 KiB) held by each
+ * GPU that loads the library until exit; nch > 16384 is rejected.  The first call
+ * on a device looks up that array's address -- make it before any stream capture.
+ * All calls share the array: calls that overlap on the GPU race. */
+int ccx_ccd_energy_noalloc(int32_t nch, const int32_t *dims, const double *t2, const double *vhhpp, double *energy,
+                           void *stream);
 /* ||R - D T|| over the stored (ordered) amplitudes of the last residual */
 int ccx_residual_norm(ccx_engine *e, double *norm);
 
