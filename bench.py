@@ -3,11 +3,14 @@
 Workload (default): pure neutron matter, A=66 at rho=0.16 fm^-3 on the nmax=4
 lattice (9^3 momenta x 2 spins = 1458 states), synthetic Minnesota interaction,
 single twist, MP2 start.  A step is one full solve: MP2 amplitudes, then CCD
-iterations (Jacobi + DIIS(8)) until ||R - D T|| < 1e-10, with the interaction
-resident in HBM.  value = seconds per solve (lower is better), device time from CUDA
-events on the engine's stream.  e2e = the same solve driven through the C ABI from
-pinned host buffers holding the reference-layout V blocks and Fock matrix, with the
-host->device copies and the T2 readback inside the timed region.
+iterations (Jacobi + DIIS(8)) until the FP64 residual ||R - D T|| < 1e-10, with the
+interaction resident in HBM.  value = seconds per solve of the mixed-precision form
+(--precision bf16x3, default; tf32x3; or fp64 for the plain form), device time from
+CUDA events on the engine's stream.  The plain FP64 solve of the same lattice is timed
+beside it (plain_fp64, speedup_vs_plain_fp64), and the E/A difference between the two
+is reported in keV.  e2e = the same solve driven through the C ABI from pinned host
+buffers holding the reference-layout V blocks and Fock matrix, with the host->device
+copies and the T2 readback inside the timed region.
 
 --impl reference times the CPU path (the oracle restatement of the reference's
 complex<double> solver, all host cores) on a bounded sample: single CCD iterations
@@ -42,7 +45,7 @@ WORKLOADS = {
 }
 # Iterations the reference algorithm (0.75/0.25 mixing + DIIS every 6, |dE| < 1e-6 MeV,
 # ccm_iter.f90:67-96) takes on each lattice, as run by the engine's reference mode.
-REFERENCE_ITERATIONS = {"pnm66": None, "pnm14": 13}
+REFERENCE_ITERATIONS = {"pnm66": 13, "pnm14": 13}
 
 
 def load_pkg():
@@ -163,6 +166,46 @@ def run_reference(args, wl):
     return 0
 
 
+PRECISIONS = {"fp64": 0, "bf16x3": 1, "tf32x3": 2}
+FALLBACK_HBM_GBS = 6800.0
+
+
+def hbm_peak():
+    """Measured copy bandwidth (GB/s) of this GPU model, else the fallback figure."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "MEASURED_PEAKS.json hbm_gbs (of measured)"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback 6.8 TB/s (of fallback)"
+
+
+def kernel_work(P, H, ring, precision):
+    """Algorithmic work of one timed bracket per kernel slot: ('flop', F) or ('byte', B).
+
+    FP64 GEMMs count 2 flops per multiply-add on unique pairs.  Tensor-core launches are
+    HBM-bound (arithmetic intensity far below the BF16 ridge): their bytes are the split
+    operands read once (hi + lo, es bytes each), C read and written in FP64."""
+    es = 2 if precision == 1 else 4
+    pp = sum(2.0 * p * p * h for p, h in zip(P, H))
+    hh = sum(2.0 * p * h * h for p, h in zip(P, H))
+    x = sum(2.0 * h * h * p for p, h in zip(P, H))
+    i4 = sum(2.0 * nhp * nhp * nph for nph, nhp in ring)
+    rg = sum(2.0 * nph * nhp * nhp for nph, nhp in ring)
+    b_pp = sum(2 * es * (p * p + p * h) + 16.0 * p * h for p, h in zip(P, H))
+    b_i4 = sum(2 * es * (2.0 * nhp * nph) + 16.0 * nhp * nhp for nph, nhp in ring)
+    b_ring = sum(2 * es * (nph * nhp + nhp * nhp) + 16.0 * nph * nhp for nph, nhp in ring)
+    return {"x_fp64": ("flop", x), "i4_fp64": ("flop", i4), "ring_fp64": ("flop", rg),
+            "ladder_fp64": ("flop", pp + hh), "pp_rebase_fp64": ("flop", pp), "hh_fp64": ("flop", hh),
+            "pp_tc": ("byte", b_pp), "i4_tc": ("byte", b_i4), "ring_tc": ("byte", b_ring)}
+
+
+KERNEL_NAMES = {"x_fp64": "k_gemm<double> X = V_hhpp' T' (split-K)", "i4_fp64": "k_gemm<double> I4",
+                "ring_fp64": "k_gemm<double> ring", "ladder_fp64": "k_gemm<double> fused pp+hh ladder",
+                "pp_rebase_fp64": "k_gemm<double> pp-ladder at a re-base", "hh_fp64": "k_gemm<double> hh-ladder",
+                "pp_tc": "k_tc_gemm pp-ladder correction", "i4_tc": "k_tc_gemm dI4 correction",
+                "ring_tc": "k_tc_gemm ring corrections", "split": "k_tc_split"}
+
+
 def run_ours(args, wl):
     import torch
     ccx = load_pkg()
@@ -178,76 +221,109 @@ def run_ours(args, wl):
     theta = (0.0, 0.0, 0.0) if rank == 0 else (0.1 * rank, -0.07 * rank, 0.05 * rank)
     L = ccx.Layout.from_basis(wl["nmax"], wl["A"], wl["rho"], snm=wl["snm"], theta=theta)
     real = wl["potential"] == ccx.POT_MINNESOTA
+    prec = PRECISIONS[args.precision] if real else 0
     e = ccx.Engine(L, device=local, real=real)
     e.generate(potential=wl["potential"])
     stream = torch.cuda.ExternalStream(e.stream(), device=local)
     P, H, ring = packed_sizes(L, ccx)
     flops = flop_model(P, H, ring, real=real)
 
-    def solve(eng):
+    def solve(eng, precision):
         eng.setup_t_amplitudes()
-        return eng.ccd_iter(mode=ccx.MODE_STANDARD, tol=args.tol, max_iter=200, diis_dim=8)
+        return eng.ccd_iter(mode=ccx.MODE_STANDARD, precision=precision, tol=args.tol, max_iter=200, diis_dim=8,
+                            defect_period=args.defect_period)
 
+    def timed(precision, steps, sample_clocks):
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        clocks = ClockSampler(local) if sample_clocks else None
+        launches0 = e.launches()
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        results, timers, ktimers = [], {}, {}
+        for _ in range(steps):
+            results.append(solve(e, precision))
+            for k, v in e.timers().items():
+                timers[k] = timers.get(k, 0.0) + v
+            for k, (ms_k, n_k) in e.kernel_timers().items():
+                a, b = ktimers.get(k, (0.0, 0))
+                ktimers[k] = (a + ms_k, b + n_k)
+        ev1.record(stream)
+        ev1.synchronize()
+        torch.cuda.synchronize()
+        clk = clocks.stop() if clocks else None
+        ms = ev0.elapsed_time(ev1) / steps
+        if dist:
+            t = torch.tensor([ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms, results, timers, ktimers, e.launches() - launches0, clk
+
+    # warm-up: both forms (tensor-core tiles are prepared by the first mixed solve)
     for _ in range(args.warmup):
-        r = solve(e)
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize()
-    clocks = ClockSampler(local)
-    launches0 = e.launches()
-    ev0 = torch.cuda.Event(enable_timing=True)
-    ev1 = torch.cuda.Event(enable_timing=True)
-    ev0.record(stream)
-    results = []
-    timers = {}
-    for _ in range(args.steps):
-        results.append(solve(e))
-        t = e.timers()
-        for k, v in t.items():
-            timers[k] = timers.get(k, 0.0) + v
-    ev1.record(stream)
-    ev1.synchronize()
-    torch.cuda.synchronize()
-    clk = clocks.stop()
-    launches = e.launches() - launches0
-    ms = ev0.elapsed_time(ev1) / args.steps
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+        solve(e, prec)
+        if prec:
+            solve(e, 0)
+    ms, results, timers, ktimers, launches, clk = timed(prec, args.steps, True)
     r = results[-1]
     iters = sum(x["iterations"] for x in results) / len(results)
     ea = (e.e0() + r["e_ccd"]).real / wl["A"]
+    if prec:
+        ms64, res64, _, _, _, _ = timed(0, args.steps, False)
+        ea64 = (e.e0() + res64[-1]["e_ccd"]).real / wl["A"]
+        plain = {"s": ms64 * 1e-3, "iterations": res64[-1]["iterations"], "E_per_A_MeV": ea64,
+                 "res_norm": res64[-1]["res_norm"]}
+    else:
+        ms64, ea64, plain = ms, ea, None
 
-    # ---- roofline of the dominant kernel (the fused pp+hh ladder GEMM, FP64 FMA) ----
-    n_it = sum(x["iterations"] + 1 for x in results)  # residual evaluations in the timed steps
-    ladder_ms = timers["ladders"] / n_it
-    ring_ms = timers["ring"] / n_it
-    i4_ms = timers["i4"] / n_it
-    peak64 = ccx.device_fp64_peak(local)
-    achieved = flops["ladders"] / (ladder_ms * 1e-3) / 1e12
-    roofline = {"bound": "fp64", "kernel": "k_gemm (pp-ladder + hh-ladder, packed a<b, i<j)",
-                "achieved": achieved, "peak": peak64, "unit": "TFLOP/s", "frac": achieved / peak64,
-                "peak_source": "measured FP64 FMA probe (ccx_device_fp64_peak); FP64 is not in MEASURED_PEAKS.json",
-                "traffic": None, "ms_per_launch": ladder_ms,
-                "flops_per_launch": flops["ladders"]}
-    terms = {k: v / n_it for k, v in timers.items() if k != "total"}
+    # ---- roofline of the dominant kernel (largest device time in the timed solves) ----
+    work = kernel_work(P, H, ring, prec)
+    dom = max((k for k in ktimers if k in work and ktimers[k][1] > 0), key=lambda k: ktimers[k][0])
+    kms, kn = ktimers[dom]
+    per_launch_ms = kms / kn
+    kind, amount = work[dom]
+    if kind == "flop":
+        peak = ccx.device_fp64_peak(local)
+        achieved = amount / (per_launch_ms * 1e-3) / 1e12
+        roofline = {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                    "peak_source": "measured FP64 FMA probe on this GPU (ccx_device_fp64_peak); "
+                                   "MEASURED_PEAKS.json holds no FP64 figure",
+                    "flop_per_launch": amount}
+    else:
+        peak, src = hbm_peak()
+        achieved = amount / (per_launch_ms * 1e-3) / 1e9
+        roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                    "peak_source": src, "bytes_per_launch": amount}
+    roofline.update({"kernel": KERNEL_NAMES[dom], "ms_per_launch": per_launch_ms, "launches_timed": kn,
+                     "traffic": PROFILED_TRAFFIC.get((args.workload, args.precision, dom))})
+    kernel_ms = {k: {"ms": v[0] / args.steps, "brackets": v[1] // args.steps} for k, v in ktimers.items() if v[1]}
 
     # ---- end to end through the C ABI from pinned host buffers ----
     e2e = None
     if not args.no_e2e:
-        e2e = run_e2e(args, ccx, torch, L, e, local, real, solve)
+        e2e = run_e2e(args, ccx, torch, L, e, local, real, lambda eng: solve(eng, prec))
 
+    form = {0: "plain FP64", 1: "mixed BF16x3 + FP64 defect correction",
+            2: "mixed TF32x3 + FP64 defect correction"}[prec]
     line = {"metric": METRIC, "value": ms * 1e-3, "unit": "s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64" if real else "c128", "data": "synthetic",
-            "form": "plain FP64 GPU (packed unique pairs, real arithmetic)",
-            "config": {"workload": wl["desc"], "solver": f"Jacobi + DIIS(8) to ||R-DT||<{args.tol:g}",
-                       "l2": "inputs larger than L2 (V_pppp packed, %.2f GB)" % (sum(p * p for p in P) * 8 / 1e9),
+            "form": form + " (packed unique pairs, real arithmetic)" if real else form,
+            "config": {"workload": wl["desc"], "solver": f"Jacobi + DIIS(8) to ||R-DT||<{args.tol:g} (FP64 residual)",
+                       "precision": args.precision if prec else "fp64",
+                       "defect_period": args.defect_period or "adaptive",
+                       "l2": "inputs larger than L2 (V_pppp packed, %.2f GB, read every iteration)"
+                             % (sum(p * p for p in P) * 8 / 1e9),
                        "replicas": world},
-            "iterations": iters, "ccd_iterations_per_s": iters / (ms * 1e-3), "E_per_A_MeV": ea,
-            "res_norm": r["res_norm"], "term_ms_per_iteration": terms,
+            "iterations": iters, "fp64_sweeps": r["fp64_sweeps"], "mixed_iterations": r["mixed_iterations"],
+            "ccd_iterations_per_s": iters / (ms * 1e-3), "E_per_A_MeV": ea, "res_norm": r["res_norm"],
+            "plain_fp64": plain, "speedup_vs_plain_fp64": (ms64 / ms) if prec else None,
+            "dE_per_A_keV_vs_fp64": abs(ea - ea64) * 1e3 if prec else 0.0,
             "gflop_per_iteration": flops["total"] / 1e9,
+            "term_ms_per_solve": {k: v / args.steps for k, v in timers.items()},
+            "kernel_ms_per_solve": kernel_ms,
             "roofline": roofline, "clocks": clk, "gpu_launches": launches, "e2e": e2e}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         n_ref = REFERENCE_ITERATIONS[args.workload] or reference_iterations(e, ccx)
@@ -260,6 +336,10 @@ def run_ours(args, wl):
     if dist:
         dist.destroy_process_group()
     return 0
+
+
+# DRAM bytes per launch of the dominant kernel from an ncu capture (workload, precision, slot)
+PROFILED_TRAFFIC = {}
 
 
 def reference_iterations(e, ccx):
@@ -339,6 +419,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="pnm66", choices=sorted(WORKLOADS))
     ap.add_argument("--tol", type=float, default=1e-10)
+    ap.add_argument("--precision", default="bf16x3", choices=sorted(PRECISIONS))
+    ap.add_argument("--defect-period", type=int, default=0, help="FP64 re-base every k iterations (0: adaptive)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()

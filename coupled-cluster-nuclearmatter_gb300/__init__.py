@@ -130,6 +130,7 @@ def lib():
         "ccx_device_fp64_peak": ([i32, C.POINTER(dbl)], C.c_int),
         "ccx_selftest_tc_gemm": ([i32, i32, i32, vp, vp, vp, i32, C.c_uint64, C.POINTER(dbl), C.POINTER(dbl)], C.c_int),
         "ccx_ccd_energy_noalloc": ([i32, vp, vp, vp, vp, vp], C.c_int),
+        "ccx_engine_kernel_timers": ([vp, vp, vp], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -423,6 +424,16 @@ class Engine:
         x = C.c_int64()
         _check(lib().ccx_engine_launches(self._h, C.byref(x)))
         return x.value
+
+    KERNEL_SLOTS = ("x_fp64", "i4_fp64", "ring_fp64", "ladder_fp64", "pp_rebase_fp64", "hh_fp64",
+                    "pp_tc", "i4_tc", "ring_tc", "split")
+
+    def kernel_timers(self) -> dict:
+        """{slot: (total ms, timed brackets)} of individual launches in the last ccd_iter."""
+        ms = np.zeros(12)
+        n = np.zeros(12, np.int64)
+        _check(lib().ccx_engine_kernel_timers(self._h, _ptr(ms), _ptr(n)))
+        return {k: (float(ms[i]), int(n[i])) for i, k in enumerate(self.KERNEL_SLOTS)}
 
     def timers(self) -> dict:
         z = np.zeros(10)

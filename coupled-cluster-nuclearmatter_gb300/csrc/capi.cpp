@@ -353,6 +353,10 @@ int ccx_engine_timers(const ccx_engine *e, double ms[10]) {
   if (!ms) return fail(CCX_EINVAL, "null argument");
   ENGINE_CALL(e, e->E->timers(ms));
 }
+int ccx_engine_kernel_timers(const ccx_engine *e, double ms[12], int64_t launches[12]) {
+  if (!ms || !launches) return fail(CCX_EINVAL, "null argument");
+  ENGINE_CALL(e, e->E->kernel_timers(ms, launches));
+}
 int ccx_set_fock(ccx_engine *e, const double *fock, const double e0[2]) {
   if (!fock) return fail(CCX_EINVAL, "null Fock matrix");
   ENGINE_CALL(e, e->E->set_fock(fock, e0));

@@ -142,6 +142,7 @@ class Engine final : public IEngine {
     CK(cudaSetDevice(device_));
     CK(cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking));
     for (auto &e : ev_) CK(cudaEventCreate(&e));
+    for (auto &e : kev_) CK(cudaEventCreate(&e));
     build_tables();
     alloc_state();
   }
@@ -149,6 +150,7 @@ class Engine final : public IEngine {
     cudaSetDevice(device_);
     if (st_) cudaStreamSynchronize(st_);
     for (auto &e : ev_) if (e) cudaEventDestroy(e);
+    for (auto &e : kev_) if (e) cudaEventDestroy(e);
     if (st_) cudaStreamDestroy(st_);
     if (host_res_) cudaFreeHost(host_res_);
   }
@@ -157,6 +159,9 @@ class Engine final : public IEngine {
   int64_t device_bytes() const override { return bytes_; }
   int64_t launches() const override { return launches_; }
   void timers(double ms[10]) const override { for (int i = 0; i < 10; ++i) ms[i] = timers_[i]; }
+  void kernel_timers(double ms[kKernelSlots], int64_t n[kKernelSlots]) const override {
+    for (int i = 0; i < kKernelSlots; ++i) { ms[i] = ktimers_[i]; n[i] = kcount_[i]; }
+  }
 
   // ---------------------------------------------------------------- interaction
   void set_fock(const double *fock, const double e0[2]) override {
@@ -435,6 +440,9 @@ class Engine final : public IEngine {
     r.e_mbpt2[0] = e[0];
     r.e_mbpt2[1] = e[1];
     for (double &t : timers_) t = 0.0;
+    for (double &t : ktimers_) t = 0.0;
+    for (int64_t &c : kcount_) c = 0;
+    kn_ = 0;
     timing_ = true;
     CK(cudaEventRecord(ev_[10], st_));
     if (o.mode == 0) iterate_reference(o, r);
@@ -823,24 +831,56 @@ class Engine final : public IEngine {
     mark(0);
     launch_gather_tph<S>(D_, T_.as<S>(), Tph_.as<S>(), st_);
     mark(1);
+    kbegin(kKX);
     run_plan(planX_);
+    kend();
     launch_i7<S>(D_, X_.as<S>(), fdiag_.as<S>(), f7_.as<S>(), d2ij_.as<S>(), i7off_.as<S>(), st_);
     launch_i9<S>(D_, n_hh2_, Vhh_.as<S>(), X_.as<S>(), I9_.as<S>(), st_);
     mark(2);
     launch_i6<S>(D_, T_.as<S>(), Vhp_.as<S>(), fdiag_.as<S>(), f6_.as<S>(), d2ab_.as<S>(), i6off_.as<S>(), st_);
     mark(3);
+    kbegin(kKI4);
     run_plan(planI4_);
+    kend();
     mark(4);
+    kbegin(kKRing);
     run_plan(planRing_);
+    kend();
     mark(5);
     launch_rinit<S>(D_, T_.as<S>(), Vhp_.as<S>(), Rph_.as<S>(), i6off_.as<S>(), i7off_.as<S>(), R_.as<S>(), st_);
     mark(6);
+    kbegin(kKLadder);
     run_plan(planLadder_);
+    kend();
     mark(7);
     launches_ += 5;
     if (timing_) accumulate_timers(0, 7);
   }
+  // Event pairs around individual launches (slots kK*), read back with the phase timers.
+  void kbegin(int slot) {
+    kcur_ = -1;
+    if (!timing_ || kn_ >= kKernelEvents) return;
+    CK(cudaEventRecord(kev_[2 * kn_], st_));
+    kcur_ = slot;
+  }
+  void kend() {
+    if (kcur_ < 0) return;
+    CK(cudaEventRecord(kev_[2 * kn_ + 1], st_));
+    kslot_[kn_++] = kcur_;
+    kcur_ = -1;
+  }
+  void kflush() {
+    for (int i = 0; i < kn_; ++i) {
+      CK(cudaEventSynchronize(kev_[2 * i + 1]));
+      float ms = 0.f;
+      CK(cudaEventElapsedTime(&ms, kev_[2 * i], kev_[2 * i + 1]));
+      ktimers_[kslot_[i]] += ms;
+      ++kcount_[kslot_[i]];
+    }
+    kn_ = 0;
+  }
   void accumulate_timers(int first, int last) {
+    kflush();
     CK(cudaEventSynchronize(ev_[last]));
     for (int i = first; i < last; ++i) {
       float ms = 0.f;
@@ -1266,21 +1306,31 @@ class Engine final : public IEngine {
     mark(0);
     launch_gather_tph<S>(D_, T_.as<S>(), Tph_.as<S>(), st_);
     mark(1);
+    kbegin(kKX);
     run_plan(planX_);
+    kend();
     launch_i7<S>(D_, X_.as<S>(), fdiag_.as<S>(), f7_.as<S>(), d2ij_.as<S>(), i7off_.as<S>(), st_);
     launch_i9<S>(D_, n_hh2_, Vhh_.as<S>(), X_.as<S>(), I9_.as<S>(), st_);
     mark(2);
     launch_i6<S>(D_, T_.as<S>(), Vhp_.as<S>(), fdiag_.as<S>(), f6_.as<S>(), d2ab_.as<S>(), i6off_.as<S>(), st_);
     mark(3);
+    kbegin(kKI4);
     run_plan(planI4_);
+    kend();
     mark(4);
+    kbegin(kKRing);
     run_plan(planRing_);
+    kend();
     mark(5);
     launch_rinit<S>(D_, T_.as<S>(), Vhp_.as<S>(), Rph_.as<S>(), i6off_.as<S>(), i7off_.as<S>(), R_.as<S>(), st_);
     mark(6);
+    kbegin(kKPP64);
     run_plan(planPP_);
+    kend();
     launch_axpy<S>(n_t_, PPb_.as<S>(), R_.as<S>(), st_);
+    kbegin(kKHH64);
     run_plan(planHH_);
+    kend();
     // the new base
     CK(cudaMemcpyAsync(Tb_.p, T_.p, n_t_ * sizeof(S), cudaMemcpyDeviceToDevice, st_));
     CK(cudaMemcpyAsync(Tphb_.p, Tph_.p, std::max<int64_t>(n_ph_, 1) * sizeof(S), cudaMemcpyDeviceToDevice, st_));
@@ -1298,27 +1348,43 @@ class Engine final : public IEngine {
     mark(0);
     launch_gather_tph<S>(D_, T_.as<S>(), Tph_.as<S>(), st_);
     mark(1);
+    kbegin(kKX);
     run_plan(planX_);
+    kend();
     launch_i7<S>(D_, X_.as<S>(), fdiag_.as<S>(), f7_.as<S>(), d2ij_.as<S>(), i7off_.as<S>(), st_);
     launch_i9<S>(D_, n_hh2_, Vhh_.as<S>(), X_.as<S>(), I9_.as<S>(), st_);
     mark(2);
     launch_i6<S>(D_, T_.as<S>(), Vhp_.as<S>(), fdiag_.as<S>(), f6_.as<S>(), d2ab_.as<S>(), i6off_.as<S>(), st_);
     mark(3);
+    kbegin(kKSplit);
     run_split(spIter1_);  // dT (B), dT_ph (B and A)
+    kend();
     CK(cudaMemsetAsync(dI4_.p, 0, std::max<int64_t>(n_i4_, 1) * sizeof(S), st_));
+    kbegin(kKTcI4);
     run_tc(tcI4_);  // dI4 = 1/2 V_ph dT_ph
+    kend();
     launch_add<S>(n_i4_, I4b_.as<S>(), dI4_.as<S>(), I4_.as<S>(), st_);
+    kbegin(kKSplit);
     run_split(spIter2_);  // dI4 (B), I4 (B)
+    kend();
     mark(4);
     CK(cudaMemcpyAsync(Rph_.p, Rphb_.p, std::max<int64_t>(n_ph_, 1) * sizeof(S), cudaMemcpyDeviceToDevice, st_));
+    kbegin(kKTcRing);
     run_tc(tcR1_);  // R_ph += T_ph,b dI4
+    kend();
+    kbegin(kKTcRing);
     run_tc(tcR2_);  // R_ph += dT_ph I4
+    kend();
     mark(5);
     launch_rinit<S>(D_, T_.as<S>(), Vhp_.as<S>(), Rph_.as<S>(), i6off_.as<S>(), i7off_.as<S>(), R_.as<S>(), st_);
     mark(6);
     launch_axpy<S>(n_t_, PPb_.as<S>(), R_.as<S>(), st_);
+    kbegin(kKTcPP);
     run_tc(tcPP_);  // R' += V_pppp' dT
+    kend();
+    kbegin(kKHH64);
     run_plan(planHH_);
+    kend();
     mark(7);
     launches_ += 7;
     if (timing_) accumulate_timers(0, 7);
@@ -1331,6 +1397,12 @@ class Engine final : public IEngine {
   cudaEvent_t ev_[12] = {};
   double timers_[10] = {};
   bool timing_ = false;
+  static constexpr int kKernelEvents = 32;
+  cudaEvent_t kev_[2 * kKernelEvents] = {};
+  int kslot_[kKernelEvents] = {};
+  int kn_ = 0, kcur_ = -1;
+  double ktimers_[kKernelSlots] = {};
+  int64_t kcount_[kKernelSlots] = {};
   int64_t bytes_ = 0, launches_ = 0;
   DevLayout D_{};
   DevOrbits O_{};

@@ -36,6 +36,21 @@ struct PotentialSpec {
   int f32_literals = 1;
 };
 
+// Per-kernel timer slots: device time of individual launches inside ccx_ccd_iter.
+enum KernelSlot {
+  kKX = 0,      // k_gemm: X = V_hhpp' T' (split-K + reduce)
+  kKI4 = 1,     // k_gemm: I4 = W + 1/2 V_ph T_ph (FP64)
+  kKRing = 2,   // k_gemm: R_ph = T_ph I4 (FP64)
+  kKLadder = 3, // k_gemm: fused pp+hh ladder (FP64 solve)
+  kKPP64 = 4,   // k_gemm: V_pppp' T' at a mixed-precision re-base (FP64)
+  kKHH64 = 5,   // k_gemm: T' I9' hh-ladder of the mixed-precision residual (FP64)
+  kKTcPP = 6,   // k_tc_gemm: pp-ladder correction V_pppp' dT
+  kKTcI4 = 7,   // k_tc_gemm: dI4 = 1/2 V_ph dT_ph
+  kKTcRing = 8, // k_tc_gemm: ring corrections (two launches per residual)
+  kKSplit = 9,  // k_tc_split: per-iteration operand splits
+  kKernelSlots = 12
+};
+
 class IEngine {
  public:
   virtual ~IEngine() = default;
@@ -43,6 +58,7 @@ class IEngine {
   virtual int64_t device_bytes() const = 0;
   virtual int64_t launches() const = 0;
   virtual void timers(double ms[10]) const = 0;
+  virtual void kernel_timers(double ms[kKernelSlots], int64_t n[kKernelSlots]) const = 0;
   virtual void set_fock(const double *fock, const double e0[2]) = 0;
   virtual void set_vblock(int kind, int ch, const double *v) = 0;
   virtual void generate(const PotentialSpec &p) = 0;

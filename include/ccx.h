@@ -292,6 +292,14 @@ int ccx_engine_launches(const ccx_engine *e, int64_t *launches);
  * [0] T_ph gather, [1] I9/I7, [2] I6, [3] I4, [4] ring, [5] R init, [6] ladders,
  * [7] update/energy, [8] DIIS, [9] total */
 int ccx_engine_timers(const ccx_engine *e, double ms[10]);
+/* device milliseconds and timed brackets of individual kernel launches in the last
+ * ccx_ccd_iter (CUDA events on the engine stream around each launch or launch group):
+ * [0] X = V_hhpp' T' (FP64 split-K GEMM + reduce), [1] I4 (FP64), [2] ring (FP64),
+ * [3] fused pp+hh ladder (FP64), [4] V_pppp' T' at a mixed-precision re-base (FP64),
+ * [5] hh-ladder of the mixed residual (FP64), [6] pp-ladder correction (tensor cores),
+ * [7] dI4 correction (tensor cores), [8] ring corrections (tensor cores),
+ * [9] operand splits, [10..11] unused */
+int ccx_engine_kernel_timers(const ccx_engine *e, double ms[12], int64_t launches[12]);
 
 #ifdef __cplusplus
 }
