@@ -747,35 +747,32 @@ class Engine final : public IEngine {
       ++launches_;
     }
   }
+  void run_x() {
+    launch_xdot<S>(D_, (const int4 *)xwork_.p, nxwork_, Vhp_.as<S>(), T_.as<S>(), X_.as<S>(), st_);
+    ++launches_;
+  }
   void build_gemm_plans() {
     const Layout &L = *L_;
     const int nc = L.fam[3].count();
-    constexpr int kXChunk = 128;  // split-K chunk of the X = V_hhpp' T' GEMM (K = P)
-    {  // X = V_hhpp' T'  (H x H, K = P), split along K; partials in the split-K scratch
-      int64_t need = 0;
+    {  // I6 row tiles and the per-row dot buffer
+      std::vector<int2> rt;
+      for (int c = 0; c < nc; ++c)
+        for (int r0 = 0; r0 < L.pk[c].P; r0 += kI6Rows)
+          if (L.pk[c].H > 0) rt.push_back(make_int2(c, r0));
+      upload(i6rows_, rt, &bytes_);
+      ni6rows_ = (int)rt.size();
+      i6dots_.alloc((size_t)std::max<int64_t>(3 * n_t_, 1) * sizeof(S), &bytes_);
+    }
+    {  // X = V_hhpp' T'  (H x H, K = P): column-dot work items
+      std::vector<int4> w;
       for (int c = 0; c < nc; ++c) {
         const auto &pk = L.pk[c];
-        if (pk.H > 0 && pk.P > 0) need += (int64_t)((pk.P + kXChunk - 1) / kXChunk) * pk.H * pk.H;
+        if (pk.H <= 0 || pk.P <= 0) continue;
+        for (int m0 = 0; m0 < pk.H; m0 += kXM)
+          for (int j0 = 0; j0 < pk.H; j0 += kXJ) w.push_back(make_int4(c, m0, j0, 0));
       }
-      splitk_.alloc((size_t)std::max<int64_t>(need, 1) * sizeof(S), &bytes_);
-      PlanBuilder b;
-      int64_t hoff = 0, poff = 0;
-      for (int c = 0; c < nc; ++c) {
-        const auto &pk = L.pk[c];
-        if (pk.H > 0 && pk.P > 0) {
-          GemmProb<S> p{};
-          p.nseg = 1;
-          p.M = pk.H; p.N = pk.H;
-          p.seg[0] = GemmSeg<S>{Vhp_.as<S>() + pk.t_off, T_.as<S>() + pk.t_off, pk.P, 1, 1, pk.P, pk.P, 1.0};
-          p.C = X_.as<S>() + hoff; p.C0 = nullptr; p.sCm = 1; p.sCn = pk.H; p.accumulate = 0;
-          p.kchunk = kXChunk;
-          p.part = splitk_.as<S>() + poff;
-          poff += (int64_t)((pk.P + kXChunk - 1) / kXChunk) * pk.H * pk.H;
-          b.add(p, (int64_t)pk.H * pk.H * pk.P);
-        }
-        hoff += (int64_t)pk.H * pk.H;
-      }
-      finalize_plan(planX_, b);
+      upload(xwork_, w, &bytes_);
+      nxwork_ = (int)w.size();
     }
     {  // R' += V_pppp' T' + T' I9'
       PlanBuilder b;
@@ -832,12 +829,13 @@ class Engine final : public IEngine {
     launch_gather_tph<S>(D_, T_.as<S>(), Tph_.as<S>(), st_);
     mark(1);
     kbegin(kKX);
-    run_plan(planX_);
+    run_x();
     kend();
     launch_i7<S>(D_, X_.as<S>(), fdiag_.as<S>(), f7_.as<S>(), d2ij_.as<S>(), i7off_.as<S>(), st_);
     launch_i9<S>(D_, n_hh2_, Vhh_.as<S>(), X_.as<S>(), I9_.as<S>(), st_);
     mark(2);
-    launch_i6<S>(D_, T_.as<S>(), Vhp_.as<S>(), fdiag_.as<S>(), f6_.as<S>(), d2ab_.as<S>(), i6off_.as<S>(), st_);
+    launch_i6<S>(D_, (const int2 *)i6rows_.p, ni6rows_, i6dots_.as<S>(), T_.as<S>(), Vhp_.as<S>(), fdiag_.as<S>(),
+                 f6_.as<S>(), d2ab_.as<S>(), i6off_.as<S>(), st_);
     mark(3);
     kbegin(kKI4);
     run_plan(planI4_);
@@ -1081,40 +1079,55 @@ class Engine final : public IEngine {
   }
 
   // ================================================================== mixed precision
+  // Tiles bucketed by padded N, so that small problems run with small shared-memory
+  // stages (and more CTAs per SM) instead of the largest problem's footprint.
+  static constexpr int kTcBuckets = 4;
   struct TcPlan {
-    DBuf probs, tiles;
-    int ntiles = 0, npad_max = 16;
+    DBuf probs;
+    DBuf tiles[kTcBuckets];
+    int ntiles[kTcBuckets] = {}, npad_max[kTcBuckets] = {}, max_nk[kTcBuckets] = {};
   };
   struct SplitPlan {
-    DBuf jobs;
-    int njobs = 0;
-    int64_t max_el = 0;
+    DBuf jobs, chunks;
+    int nchunks = 0;
   };
   struct TileBuf {
     DBuf hi, lo;
     int64_t n = 0;  // elements
   };
-  void finalize_tc(TcPlan &pl, const std::vector<TcProb> &probs, const std::vector<TcTile> &tiles, int npad_max) {
+  void finalize_tc(TcPlan &pl, const std::vector<TcProb> &probs, const std::vector<TcTile> &tiles, int /*npad_max*/) {
     upload(pl.probs, probs, &bytes_);
-    upload(pl.tiles, tiles, &bytes_);
-    pl.ntiles = (int)tiles.size();
-    pl.npad_max = npad_max;
+    std::vector<TcTile> b[kTcBuckets];
+    for (int k = 0; k < kTcBuckets; ++k) { pl.npad_max[k] = 16; pl.max_nk[k] = 1; }
+    for (const TcTile &t : tiles) {
+      const TcProb &p = probs[t.prob];
+      const int k = p.npad <= 32 ? 0 : p.npad <= 64 ? 1 : p.npad <= 128 ? 2 : 3;
+      b[k].push_back(t);
+      pl.npad_max[k] = std::max(pl.npad_max[k], p.npad);
+      pl.max_nk[k] = std::max(pl.max_nk[k], p.nk);
+    }
+    for (int k = 0; k < kTcBuckets; ++k) {
+      upload(pl.tiles[k], b[k], &bytes_);
+      pl.ntiles[k] = (int)b[k].size();
+    }
   }
   void finalize_split(SplitPlan &pl, const std::vector<TcSplitJob> &jobs) {
     upload(pl.jobs, jobs, &bytes_);
-    pl.njobs = (int)jobs.size();
-    pl.max_el = 0;
-    for (const auto &j : jobs) pl.max_el = std::max<int64_t>(pl.max_el, (int64_t)(j.rows_pad / j.tile_rows) * j.nk * j.tile_rows * tc_tile_k(tc_kind_));
+    const std::vector<int2> ch = tc_split_chunks(jobs);
+    upload(pl.chunks, ch, &bytes_);
+    pl.nchunks = (int)ch.size();
   }
   void run_tc(const TcPlan &pl) {
-    if (!pl.ntiles) return;
-    launch_tc_gemm(tc_kind_, (const TcProb *)pl.probs.p, (const TcTile *)pl.tiles.p, pl.ntiles, pl.npad_max,
-                   tcerr_.as<int>(), st_);
-    ++launches_;
+    for (int k = 0; k < kTcBuckets; ++k) {
+      if (!pl.ntiles[k]) continue;
+      launch_tc_gemm(tc_kind_, (const TcProb *)pl.probs.p, (const TcTile *)pl.tiles[k].p, pl.ntiles[k],
+                     pl.npad_max[k], pl.max_nk[k], tcerr_.as<int>(), st_);
+      ++launches_;
+    }
   }
   void run_split(const SplitPlan &pl) {
-    if (!pl.njobs) return;
-    launch_tc_split(tc_kind_, (const TcSplitJob *)pl.jobs.p, pl.njobs, pl.max_el, st_);
+    if (!pl.nchunks) return;
+    launch_tc_split(tc_kind_, (const TcSplitJob *)pl.jobs.p, (const int2 *)pl.chunks.p, pl.nchunks, st_);
     ++launches_;
   }
   void check_tc_error() {
@@ -1307,12 +1320,13 @@ class Engine final : public IEngine {
     launch_gather_tph<S>(D_, T_.as<S>(), Tph_.as<S>(), st_);
     mark(1);
     kbegin(kKX);
-    run_plan(planX_);
+    run_x();
     kend();
     launch_i7<S>(D_, X_.as<S>(), fdiag_.as<S>(), f7_.as<S>(), d2ij_.as<S>(), i7off_.as<S>(), st_);
     launch_i9<S>(D_, n_hh2_, Vhh_.as<S>(), X_.as<S>(), I9_.as<S>(), st_);
     mark(2);
-    launch_i6<S>(D_, T_.as<S>(), Vhp_.as<S>(), fdiag_.as<S>(), f6_.as<S>(), d2ab_.as<S>(), i6off_.as<S>(), st_);
+    launch_i6<S>(D_, (const int2 *)i6rows_.p, ni6rows_, i6dots_.as<S>(), T_.as<S>(), Vhp_.as<S>(), fdiag_.as<S>(),
+                 f6_.as<S>(), d2ab_.as<S>(), i6off_.as<S>(), st_);
     mark(3);
     kbegin(kKI4);
     run_plan(planI4_);
@@ -1349,12 +1363,13 @@ class Engine final : public IEngine {
     launch_gather_tph<S>(D_, T_.as<S>(), Tph_.as<S>(), st_);
     mark(1);
     kbegin(kKX);
-    run_plan(planX_);
+    run_x();
     kend();
     launch_i7<S>(D_, X_.as<S>(), fdiag_.as<S>(), f7_.as<S>(), d2ij_.as<S>(), i7off_.as<S>(), st_);
     launch_i9<S>(D_, n_hh2_, Vhh_.as<S>(), X_.as<S>(), I9_.as<S>(), st_);
     mark(2);
-    launch_i6<S>(D_, T_.as<S>(), Vhp_.as<S>(), fdiag_.as<S>(), f6_.as<S>(), d2ab_.as<S>(), i6off_.as<S>(), st_);
+    launch_i6<S>(D_, (const int2 *)i6rows_.p, ni6rows_, i6dots_.as<S>(), T_.as<S>(), Vhp_.as<S>(), fdiag_.as<S>(),
+                 f6_.as<S>(), d2ab_.as<S>(), i6off_.as<S>(), st_);
     mark(3);
     kbegin(kKSplit);
     run_split(spIter1_);  // dT (B), dT_ph (B and A)
@@ -1418,8 +1433,9 @@ class Engine final : public IEngine {
   DBuf onx_, ony_, onz_, osz_, otz_, okx_, oky_, okz_, oe_;
   // state
   DBuf T_, R_, Vhp_, Vpp_, Vhh_, X_, I9_, Tph_, Rph_, Vph_, W_, I4_, fdiag_, f6_, f7_, d2ij_, d2ab_, i6off_, i7off_;
-  DBuf partial_, res_, flag_, stage_, hist_, hist_t_, hist_e_, splitk_;
-  Plan planX_, planLadder_, planI4_, planRing_, planPP_, planHH_;
+  DBuf partial_, res_, flag_, stage_, hist_, hist_t_, hist_e_, xwork_, i6rows_, i6dots_;
+  int nxwork_ = 0, ni6rows_ = 0;
+  Plan planLadder_, planI4_, planRing_, planPP_, planHH_;
   // mixed precision
   bool mixed_ready_ = false;
   int tc_kind_ = 0;

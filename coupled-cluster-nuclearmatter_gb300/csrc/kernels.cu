@@ -202,10 +202,10 @@ __global__ void k_gather_tph(DevLayout L, const S *__restrict__ T, S *__restrict
   const int2 tl = L.phtile[blockIdx.x];
   const int q = tl.x;
   const int nph = L.n_ph[q], nhp = L.n_hp[q];
-  const int64_t n = (int64_t)nph * nhp;
-  const int64_t end = min((int64_t)tl.y + kTileElems, n);
-  for (int64_t e = tl.y + threadIdx.x; e < end; e += blockDim.x) {
-    const int r = (int)(e % nph), c = (int)(e / nph);
+  const int n = nph * nhp;  // < 2^31 per channel
+  const int end = min(tl.y + kTileElems, n);
+  for (int e = tl.y + threadIdx.x; e < end; e += blockDim.x) {
+    const int c = e / nph, r = e - c * nph;
     const int2 ai = L.ph_orb[L.ph_off[q] + r];
     const int2 jb = L.hp_orb[L.hp_off[q] + c];
     const int2 sab = L.pp_slot[(int64_t)(ai.x - L.A) * L.NP + (jb.y - L.A)];
@@ -220,6 +220,68 @@ __global__ void k_gather_tph(DevLayout L, const S *__restrict__ T, S *__restrict
 }
 template <typename S> void launch_gather_tph(const DevLayout &L, const S *T, S *Tph, cudaStream_t st) {
   if (L.nphtile) k_gather_tph<S><<<L.nphtile, 256, 0, st>>>(L, T, Tph);
+}
+
+// ============================================================================
+// X'(m, j) = sum_k V'(k, m) T'(k, j) per hhpp channel (the V_hhpp T product of the I9
+// ZGEMM, ccm_t2_eqn.f90:459, on packed pairs).  V_hhpp' and T' are P x H column-major,
+// so X(m, j) is the dot product of two contiguous columns of length P.  One CTA per
+// (channel, kXM rows, kXJ columns): the kXJ columns of T' are staged in shared memory
+// in K chunks, each warp owns rows m (lanes stride over k), and the lane partials are
+// reduced with shuffles at the end, in a fixed order.
+// ============================================================================
+template <typename S>
+__global__ void __launch_bounds__(256) k_xdot(DevLayout L, const int4 *__restrict__ work, const S *__restrict__ V,
+                                              const S *__restrict__ T, S *__restrict__ X) {
+  constexpr int RPW = kXM / 8;  // rows per warp
+  __shared__ S Ts[kXJ][kXK];
+  const int4 w = work[blockIdx.x];
+  const int ch = w.x, m0 = w.y, j0 = w.z;
+  const int P = L.P[ch], H = L.H[ch];
+  const int64_t off = L.t_off[ch];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nj = min(kXJ, H - j0);
+  S acc[RPW][kXJ];
+#pragma unroll
+  for (int r = 0; r < RPW; ++r)
+#pragma unroll
+    for (int j = 0; j < kXJ; ++j) acc[r][j] = S(0.0);
+  for (int k0 = 0; k0 < P; k0 += kXK) {
+    const int kn = min(kXK, P - k0);
+    for (int x = threadIdx.x; x < kXJ * kXK; x += blockDim.x) {
+      const int j = x / kXK, k = x % kXK;
+      Ts[j][k] = (j < nj && k < kn) ? T[off + (int64_t)P * (j0 + j) + k0 + k] : S(0.0);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < RPW; ++r) {
+      const int m = m0 + warp + 8 * r;
+      if (m < H) {
+        const S *vc = V + off + (int64_t)P * m + k0;
+        for (int k = lane; k < kn; k += 32) {
+          const S v = vc[k];
+#pragma unroll
+          for (int j = 0; j < kXJ; ++j) acc[r][j] += v * Ts[j][k];
+        }
+      }
+    }
+    __syncthreads();
+  }
+  S *xc = X + L.hh2_off[ch];
+#pragma unroll
+  for (int r = 0; r < RPW; ++r) {
+    const int m = m0 + warp + 8 * r;
+    if (m >= H) continue;
+#pragma unroll
+    for (int j = 0; j < kXJ; ++j) {
+      const S tot = from2<S>(warp_sum2(to2(acc[r][j])));
+      if (lane == 0 && j < nj) xc[m + (int64_t)H * (j0 + j)] = tot;
+    }
+  }
+}
+template <typename S>
+void launch_xdot(const DevLayout &L, const int4 *work, int nwork, const S *V, const S *T, S *X, cudaStream_t st) {
+  if (nwork > 0) k_xdot<S><<<nwork, 256, 0, st>>>(L, work, V, T, X);
 }
 
 // ============================================================================
@@ -262,11 +324,57 @@ template <typename S> void launch_i9(const DevLayout &, int64_t n, const S *Vhh,
 
 // ============================================================================
 // I6(a,c) = f(a,c) - 1/2 sum V(kl,dc) T(da,kl), ccm_t2_eqn.f90:1399-1441, for
-// c in {a, partner(a)}; one warp per (a, c).  The diagonal becomes d2ab (:86-89).
+// c in {a, partner(a)}; the diagonal becomes d2ab (:86-89).  Two passes:
+//  1. k_i6_rows, one thread per packed pp row rho = (p, q), p < q: the three column
+//     dots over the packed hole pairs that row feeds, D0 = T_rho . V_rho (into
+//     I6(p,p) and I6(q,q)), D1 = T_rho . V_(q,p') (into I6(p,p')) and
+//     D2 = T_rho . V_(p,q') (into I6(q,q')), with the antisymmetry signs of the
+//     pair slots.  Rows of one channel are adjacent, so the T and V_rho reads are
+//     coalesced; they are stored at the row's first element of the T layout.
+//  2. k_i6_sum, one warp per (a, c): the sum over d of the dots of the rows (a, d).
 // ============================================================================
 template <typename S>
-__global__ void k_i6(DevLayout L, const S *__restrict__ T, const S *__restrict__ Vhp, const S *__restrict__ fdiag,
-                     const S *__restrict__ f6, S *d2ab, S *i6off) {
+__global__ void k_i6_rows(DevLayout L, const int2 *__restrict__ rowtile, const S *__restrict__ T,
+                          const S *__restrict__ Vhp, S *__restrict__ D) {
+  const int2 rt = rowtile[blockIdx.x];
+  const int ch = rt.x, rho = rt.y + threadIdx.x;
+  const int P = L.P[ch];
+  if (rho >= P) return;
+  const int H = L.H[ch], A = L.A, NP = L.NP;
+  const int64_t off = L.t_off[ch];
+  const int2 po = L.pp_orb[L.pp_off[ch] + rho];
+  const int p = po.x, q = po.y;
+  // I6(p, p'): d = q, pairs (q, p) and (q, p')
+  int i1 = -1, i2 = -1;
+  double sg1 = 0.0, sg2 = 0.0;
+  const int pp = L.partner[p], qq = L.partner[q];
+  if (pp >= A) {
+    const int2 s1 = L.pp_slot[(int64_t)(q - A) * NP + (p - A)], s2 = L.pp_slot[(int64_t)(q - A) * NP + (pp - A)];
+    if (s1.y != 0 && s2.y != 0) { i1 = sidx(s2.y); sg1 = ssign(s1.y) * ssign(s2.y); }
+  }
+  // I6(q, q'): d = p, pairs (p, q) and (p, q')
+  if (qq >= A) {
+    const int2 s1 = L.pp_slot[(int64_t)(p - A) * NP + (q - A)], s2 = L.pp_slot[(int64_t)(p - A) * NP + (qq - A)];
+    if (s1.y != 0 && s2.y != 0) { i2 = sidx(s2.y); sg2 = ssign(s1.y) * ssign(s2.y); }
+  }
+  S d0 = S(0.0), d1 = S(0.0), d2 = S(0.0);
+  const S *tc = T + off, *vc = Vhp + off;
+  for (int k = 0; k < H; ++k) {
+    const int64_t o = (int64_t)P * k;
+    const S t = tc[o + rho];
+    d0 += t * vc[o + rho];
+    if (i1 >= 0) d1 += t * vc[o + i1];
+    if (i2 >= 0) d2 += t * vc[o + i2];
+  }
+  S *dr = D + 3 * (off + rho);
+  dr[0] = d0;
+  dr[1] = sg1 * d1;
+  dr[2] = sg2 * d2;
+}
+
+template <typename S>
+__global__ void k_i6_sum(DevLayout L, const S *__restrict__ D, const S *__restrict__ fdiag, const S *__restrict__ f6,
+                         S *d2ab, S *i6off) {
   const int w = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
   const int lane = threadIdx.x & 31;
   if (w >= 2 * L.NP) return;
@@ -277,20 +385,14 @@ __global__ void k_i6(DevLayout L, const S *__restrict__ T, const S *__restrict__
     if (lane == 0) i6off[u] = S(0.0);
     return;
   }
-  const int v = c - L.A;
   S acc = S(0.0);
   for (int d = lane; d < L.NP; d += 32) {
-    const int2 s1 = L.pp_slot[(int64_t)d * L.NP + u];
-    const int2 s2 = L.pp_slot[(int64_t)d * L.NP + v];
-    if (s1.y == 0 || s2.y == 0) continue;
-    const int ch = s1.x;
-    const int64_t P = L.P[ch];
-    const int H = L.H[ch];
-    const S *tc = T + L.t_off[ch] + sidx(s1.y);
-    const S *vc = Vhp + L.t_off[ch] + sidx(s2.y);
-    S dot = S(0.0);
-    for (int k = 0; k < H; ++k) dot += tc[P * k] * vc[P * k];
-    acc += (ssign(s1.y) * ssign(s2.y)) * dot;
+    const int2 s = L.pp_slot[(int64_t)u * L.NP + d];
+    if (s.y == 0) continue;
+    const int ch = s.x, rho = sidx(s.y);
+    const S *dr = D + 3 * (L.t_off[ch] + rho);
+    if (!which) acc += dr[0];
+    else acc += (L.pp_orb[L.pp_off[ch] + rho].x == x) ? dr[1] : dr[2];
   }
   const S tot = from2<S>(warp_sum2(to2(acc)));
   if (lane == 0) {
@@ -300,9 +402,11 @@ __global__ void k_i6(DevLayout L, const S *__restrict__ T, const S *__restrict__
   }
 }
 template <typename S>
-void launch_i6(const DevLayout &L, const S *T, const S *Vhp, const S *fdiag, const S *f6, S *d2ab, S *i6off, cudaStream_t st) {
+void launch_i6(const DevLayout &L, const int2 *rowtile, int nrowtile, S *D, const S *T, const S *Vhp, const S *fdiag,
+               const S *f6, S *d2ab, S *i6off, cudaStream_t st) {
+  if (nrowtile > 0) k_i6_rows<S><<<nrowtile, kI6Rows, 0, st>>>(L, rowtile, T, Vhp, D);
   const int64_t threads = (int64_t)2 * L.NP * 32;
-  k_i6<S><<<(int)((threads + 255) / 256), 256, 0, st>>>(L, T, Vhp, fdiag, f6, d2ab, i6off);
+  k_i6_sum<S><<<(int)((threads + 255) / 256), 256, 0, st>>>(L, D, fdiag, f6, d2ab, i6off);
 }
 
 // ============================================================================
@@ -324,12 +428,12 @@ __global__ void k_rinit(DevLayout L, const S *__restrict__ T, const S *__restric
   const int2 tl = L.ttile[blockIdx.x];
   const int ch = tl.x;
   const int P = L.P[ch], H = L.H[ch];
-  const int64_t n = (int64_t)P * H;
-  const int64_t end = min((int64_t)tl.y + kTileElems, n);
+  const int n = P * H;  // < 2^31 per channel
+  const int end = min(tl.y + kTileElems, n);
   const S *tc = T + L.t_off[ch];
   const int A = L.A, NP = L.NP;
-  for (int64_t e = tl.y + threadIdx.x; e < end; e += blockDim.x) {
-    const int ab = (int)(e % P), ij = (int)(e / P);
+  for (int e = tl.y + threadIdx.x; e < end; e += blockDim.x) {
+    const int ij = e / P, ab = e - ij * P;
     const int2 po = L.pp_orb[L.pp_off[ch] + ab];
     const int2 ho = L.hh_orb[L.hh_off[ch] + ij];
     const int a = po.x, b = po.y, i = ho.x, j = ho.y;
@@ -376,11 +480,11 @@ __global__ void k_update(DevLayout L, int mode, S *__restrict__ T, const S *__re
   const int2 tl = L.ttile[blockIdx.x];
   const int ch = tl.x;
   const int P = L.P[ch], H = L.H[ch];
-  const int64_t n = (int64_t)P * H;
-  const int64_t end = min((int64_t)tl.y + kTileElems, n);
+  const int n = P * H;  // < 2^31 per channel
+  const int end = min(tl.y + kTileElems, n);
   double v[3] = {0.0, 0.0, 0.0};
   const int A = L.A;
-  for (int64_t e = tl.y + threadIdx.x; e < end; e += blockDim.x) {
+  for (int e = tl.y + threadIdx.x; e < end; e += blockDim.x) {
     const int64_t g = L.t_off[ch] + e;
     const S t = T[g];
     const S vij = Vhp[g];
@@ -390,7 +494,7 @@ __global__ void k_update(DevLayout L, int mode, S *__restrict__ T, const S *__re
       v[1] += imag_(pr);
       continue;
     }
-    const int ab = (int)(e % P), ij = (int)(e / P);
+    const int ij = e / P, ab = e - ij * P;
     const int2 po = L.pp_orb[L.pp_off[ch] + ab];
     const int2 ho = L.hh_orb[L.hh_off[ch] + ij];
     const S D = ((d2ij[ho.x] + d2ij[ho.y]) - d2ab[po.x - A]) - d2ab[po.y - A];
@@ -799,8 +903,8 @@ __global__ void k_mp2(DevLayout L, const S *__restrict__ Vhp, const S *__restric
   const int2 tl = L.ttile[blockIdx.x];
   const int ch = tl.x, P = L.P[ch], H = L.H[ch];
   const int64_t n = (int64_t)P * H, end = min((int64_t)tl.y + kTileElems, n);
-  for (int64_t e = tl.y + threadIdx.x; e < end; e += blockDim.x) {
-    const int ab = (int)(e % P), ij = (int)(e / P);
+  for (int e = tl.y + threadIdx.x; e < end; e += blockDim.x) {
+    const int ij = e / P, ab = e - ij * P;
     const int2 po = L.pp_orb[L.pp_off[ch] + ab], ho = L.hh_orb[L.hh_off[ch] + ij];
     const S den = ((S(0.0) - fd[po.x]) - fd[po.y] + fd[ho.x]) + fd[ho.y];
     const int64_t g = L.t_off[ch] + e;
@@ -850,7 +954,9 @@ void launch_unpack_t(const DevLayout &L, int ch, int n_pp, const int *pp_signed,
   template void launch_gather_tph<S>(const DevLayout &, const S *, S *, cudaStream_t);                                 \
   template void launch_i7<S>(const DevLayout &, const S *, const S *, const S *, S *, S *, cudaStream_t);             \
   template void launch_i9<S>(const DevLayout &, int64_t, const S *, const S *, S *, cudaStream_t);                     \
-  template void launch_i6<S>(const DevLayout &, const S *, const S *, const S *, const S *, S *, S *, cudaStream_t);  \
+  template void launch_xdot<S>(const DevLayout &, const int4 *, int, const S *, const S *, S *, cudaStream_t);        \
+  template void launch_i6<S>(const DevLayout &, const int2 *, int, S *, const S *, const S *, const S *, const S *,   \
+                             S *, S *, cudaStream_t);                                                                  \
   template void launch_rinit<S>(const DevLayout &, const S *, const S *, const S *, const S *, const S *, S *,         \
                                 cudaStream_t);                                                                         \
   template void launch_update<S>(const DevLayout &, int, S *, const S *, const S *, const S *, const S *, S *, S *,    \

@@ -55,9 +55,16 @@ struct DevPotential {
 
 // ---- residual pieces --------------------------------------------------------
 template <typename S> void launch_gather_tph(const DevLayout &L, const S *T, S *Tph, cudaStream_t st);
+// X' = V_hhpp'^T T' per channel; work items (channel, first row, first column, 0)
+constexpr int kXM = 32, kXJ = 8, kXK = 256;
+template <typename S> void launch_xdot(const DevLayout &L, const int4 *work, int nwork, const S *V, const S *T, S *X, cudaStream_t st);
 template <typename S> void launch_i7(const DevLayout &L, const S *X, const S *fdiag, const S *f7, S *d2ij, S *i7off, cudaStream_t st);
 template <typename S> void launch_i9(const DevLayout &L, int64_t n, const S *Vhh, const S *X, S *I9, cudaStream_t st);
-template <typename S> void launch_i6(const DevLayout &L, const S *T, const S *Vhp, const S *fdiag, const S *f6, S *d2ab, S *i6off, cudaStream_t st);
+// I6 in two passes; rowtile: (channel, first packed pp row) per block of kI6Rows rows;
+// D: 3 values per packed row, at 3 * (t_off[ch] + row)
+constexpr int kI6Rows = 128;
+template <typename S> void launch_i6(const DevLayout &L, const int2 *rowtile, int nrowtile, S *D, const S *T, const S *Vhp,
+                                     const S *fdiag, const S *f6, S *d2ab, S *i6off, cudaStream_t st);
 template <typename S> void launch_rinit(const DevLayout &L, const S *T, const S *Vhp, const S *Rph, const S *i6off, const S *i7off, S *R, cudaStream_t st);
 
 // ---- update / energy / norms (per-block partial sums, then a fixed-order finish) --

@@ -74,7 +74,6 @@ void tc_selftest(int device, int kind, int nprob, const int *Ms, const int *Ns, 
   std::vector<TcProb> probs;
   std::vector<TcTile> tiles;
   size_t oa = 0, ob = 0, oc = 0, ta = 0, tb = 0;
-  int64_t max_el = 0;
   for (int i = 0; i < nprob; ++i) {
     Host &x = h[i];
     sck(cudaMemcpy((double *)dA.p + oa, x.A.data(), x.A.size() * 8, cudaMemcpyHostToDevice), "copy A");
@@ -90,7 +89,6 @@ void tc_selftest(int device, int kind, int nprob, const int *Ms, const int *Ns, 
     jb.hi = (char *)tBh.p + tb * es; jb.lo = (char *)tBl.p + tb * es; jb.scale = 1.0;
     jobs.push_back(ja);
     jobs.push_back(jb);
-    max_el = std::max<int64_t>({max_el, (int64_t)x.a_el, (int64_t)x.b_el});
     TcProb p{};
     p.Ahi = ja.hi; p.Alo = use_alo ? ja.lo : nullptr; p.Bhi = jb.hi; p.Blo = jb.lo;
     p.M = x.M; p.N = x.N; p.nk = x.nk; p.npad = x.npad;
@@ -104,13 +102,18 @@ void tc_selftest(int device, int kind, int nprob, const int *Ms, const int *Ns, 
   sck(cudaMemcpy(dP.p, probs.data(), probs.size() * sizeof(TcProb), cudaMemcpyHostToDevice), "copy probs");
   sck(cudaMemcpy(dT.p, tiles.data(), tiles.size() * sizeof(TcTile), cudaMemcpyHostToDevice), "copy tiles");
   sck(cudaMemset(dE.p, 0, 4), "memset");
-  launch_tc_split(kind, (const TcSplitJob *)dJ.p, (int)jobs.size(), max_el, 0);
+  const std::vector<int2> chunks = tc_split_chunks(jobs);
+  Dev dK(chunks.size() * sizeof(int2));
+  sck(cudaMemcpy(dK.p, chunks.data(), chunks.size() * sizeof(int2), cudaMemcpyHostToDevice), "copy chunks");
+  launch_tc_split(kind, (const TcSplitJob *)dJ.p, (const int2 *)dK.p, (int)chunks.size(), 0);
   sck(cudaGetLastError(), "split launch");
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   cudaEventRecord(e0);
-  launch_tc_gemm(kind, (const TcProb *)dP.p, (const TcTile *)dT.p, (int)tiles.size(), npad_max, (int *)dE.p, 0);
+  int max_nk = 1;
+  for (const auto &x : h) max_nk = std::max(max_nk, x.nk);
+  launch_tc_gemm(kind, (const TcProb *)dP.p, (const TcTile *)dT.p, (int)tiles.size(), npad_max, max_nk, (int *)dE.p, 0);
   cudaEventRecord(e1);
   sck(cudaGetLastError(), "tc gemm launch");
   sck(cudaEventSynchronize(e1), "tc gemm");

@@ -80,11 +80,16 @@ __device__ __forceinline__ void tc_mma(uint32_t d, uint64_t a, uint64_t b, uint3
 __device__ __forceinline__ void tc_commit(uint32_t bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
 }
-__device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t (&r)[8]) {
-  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
-               : "r"(taddr)
-               : "memory");
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,"
+      "%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr)
+      : "memory");
 }
 __device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
@@ -102,12 +107,13 @@ __device__ __forceinline__ uint32_t instr_desc(int m, int n) {
 }
 
 template <int KIND>
-__global__ void __launch_bounds__(128, 1) k_tc_gemm(const TcProb *__restrict__ probs, const TcTile *__restrict__ tiles,
-                                                   int stages, int npad_max, int *err) {
+__global__ void __launch_bounds__(128) k_tc_gemm(const TcProb *__restrict__ probs, const TcTile *__restrict__ tiles,
+                                                int stages, int npad_max, int *err) {
   extern __shared__ __align__(1024) uint8_t smem[];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const TcTile tl = tiles[blockIdx.x];
-  const TcProb &P = probs[tl.prob];
+  // by value: the epilogue's stores to C must not force re-reads of the descriptor
+  const TcProb P = probs[tl.prob];
   const int npad = P.npad, nk = P.nk;
   if (npad < 16 || npad > 256 || (npad & 15) || npad > npad_max) {
     if (tid == 0) atomicExch(err, 4);
@@ -210,16 +216,22 @@ __global__ void __launch_bounds__(128, 1) k_tc_gemm(const TcProb *__restrict__ p
   const int row = warp * 32 + lane;
   const int m = tl.mt * 128 + row;
   const uint32_t tl_addr = tmem + ((uint32_t)(warp * 32) << 16);
-  for (int c0 = 0; c0 < npad; c0 += 8) {
-    uint32_t r[8];
-    tmem_ld8(tl_addr + (uint32_t)c0, r);
+  double *__restrict__ crow = P.C + (int64_t)m * P.sCm;
+  const int64_t sCn = P.sCn;
+  const double alpha = P.alpha;
+  const int nvalid = P.N;
+  // 32 columns per TMEM read (npad rounded up to 32 stays inside the allocated columns)
+  for (int c0 = 0; c0 < npad; c0 += 32) {
+    uint32_t r[32];
+    tmem_ld32(tl_addr + (uint32_t)c0, r);
     tmem_ld_wait();
     if (fin && m < P.M) {
+      double old[32];
 #pragma unroll
-      for (int j = 0; j < 8; ++j) {
-        const int n = c0 + j;
-        if (n < P.N) P.C[(int64_t)m * P.sCm + (int64_t)n * P.sCn] += P.alpha * (double)__uint_as_float(r[j]);
-      }
+      for (int j = 0; j < 32; ++j) old[j] = (c0 + j < nvalid) ? crow[(int64_t)(c0 + j) * sCn] : 0.0;
+#pragma unroll
+      for (int j = 0; j < 32; ++j)
+        if (c0 + j < nvalid) crow[(int64_t)(c0 + j) * sCn] = old[j] + alpha * (double)__uint_as_float(r[j]);
     }
   }
   tc_fence_before();
@@ -231,68 +243,143 @@ __global__ void __launch_bounds__(128, 1) k_tc_gemm(const TcProb *__restrict__ p
 }
 
 // ---- operand preparation ---------------------------------------------------------
+// x = hi + lo split of an FP64 value into two narrow floats (BF16: 8 significant bits
+// each; TF32: 11), computed on the bit pattern with integer operations: the FP64 pipe
+// of this GPU is narrow, and a float conversion of a double runs on it.  hi is x
+// rounded to NB significant bits (half away from zero), lo the exact remainder rounded
+// the same way, so |x - hi - lo| <= 2^(-2 NB) |x|.  Values below the float range
+// (2^-126) become zero.
+template <int NB>
+struct BitSplit {
+  // float bit pattern of sign * sig * 2^(e2 - (NB - 1)), sig in [2^(NB-1), 2^NB)
+  __device__ static uint32_t pack(uint32_t sign, int e2, uint32_t sig) {
+    const int biased = e2 + 127;
+    if (biased <= 0) return sign << 31;
+    return (sign << 31) | ((uint32_t)biased << 23) | ((sig & ((1u << (NB - 1)) - 1)) << (24 - NB));
+  }
+  __device__ static void split(double x, uint32_t &hi, uint32_t &lo) {
+    const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+    const uint32_t sign = (uint32_t)(u >> 63);
+    const int e = (int)((u >> 52) & 0x7ff);
+    if (e == 0) {  // zero (and FP64 subnormals, far below the float range)
+      hi = lo = sign << 31;
+      return;
+    }
+    const long long full = (long long)((u & 0xFFFFFFFFFFFFFull) | (1ull << 52));  // 53-bit significand
+    constexpr int drop = 53 - NB;
+    uint32_t h = (uint32_t)((full + (1ll << (drop - 1))) >> drop);
+    const long long rem = full - ((long long)h << drop);  // |rem| <= 2^(drop-1)
+    int eh = e - 1023;
+    if (h == (1u << NB)) { h >>= 1; ++eh; }
+    hi = pack(sign, eh, h);
+    if (rem == 0) {
+      lo = 0;
+      return;
+    }
+    const unsigned long long a = (unsigned long long)(rem < 0 ? -rem : rem);
+    const int pos = 63 - __clzll((long long)a);  // leading bit of the remainder
+    uint32_t l;
+    int el = e - 1075 + pos;
+    if (pos >= NB) {
+      const int sh = pos - (NB - 1);
+      l = (uint32_t)((a + (1ull << (sh - 1))) >> sh);
+      if (l == (1u << NB)) { l >>= 1; ++el; }
+    } else {
+      l = (uint32_t)(a << ((NB - 1) - pos));
+    }
+    lo = pack(sign ^ (rem < 0 ? 1u : 0u), el, l);
+  }
+};
 template <int KIND> struct Half;
 template <> struct Half<kTcBF16> {
-  using T = __nv_bfloat16;
   static constexpr int per16 = 8;  // elements per 16 bytes
-  __device__ static void split(double x, T &hi, T &lo) {
-    hi = __float2bfloat16_rn((float)x);
-    lo = __float2bfloat16_rn((float)(x - (double)__bfloat162float(hi)));
+  // one 16-byte unit of hi and of lo from 8 values
+  __device__ static void split8(const double (&x)[8], uint4 &hi, uint4 &lo) {
+    uint32_t h[8], l[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) BitSplit<8>::split(x[j], h[j], l[j]);
+    hi = make_uint4((h[0] >> 16) | (h[1] & 0xFFFF0000u), (h[2] >> 16) | (h[3] & 0xFFFF0000u),
+                    (h[4] >> 16) | (h[5] & 0xFFFF0000u), (h[6] >> 16) | (h[7] & 0xFFFF0000u));
+    lo = make_uint4((l[0] >> 16) | (l[1] & 0xFFFF0000u), (l[2] >> 16) | (l[3] & 0xFFFF0000u),
+                    (l[4] >> 16) | (l[5] & 0xFFFF0000u), (l[6] >> 16) | (l[7] & 0xFFFF0000u));
   }
 };
-__device__ __forceinline__ float to_tf32(float x) {
-  uint32_t r;
-  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
-  return __uint_as_float(r);
-}
 template <> struct Half<kTcTF32> {
-  using T = float;
   static constexpr int per16 = 4;
-  __device__ static void split(double x, T &hi, T &lo) {
-    hi = to_tf32((float)x);
-    lo = to_tf32((float)(x - (double)hi));
+  __device__ static void split4(const double (&x)[4], uint4 &hi, uint4 &lo) {
+    uint32_t h[4], l[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) BitSplit<11>::split(x[j], h[j], l[j]);
+    hi = make_uint4(h[0], h[1], h[2], h[3]);
+    lo = make_uint4(l[0], l[1], l[2], l[3]);
   }
 };
+template <int KIND, int N> __device__ inline void split_unit(const double (&x)[N], uint4 &hi, uint4 &lo);
+template <> __device__ inline void split_unit<kTcBF16, 8>(const double (&x)[8], uint4 &hi, uint4 &lo) {
+  Half<kTcBF16>::split8(x, hi, lo);
+}
+template <> __device__ inline void split_unit<kTcTF32, 4>(const double (&x)[4], uint4 &hi, uint4 &lo) {
+  Half<kTcTF32>::split4(x, hi, lo);
+}
 
+// One thread per 16-byte unit of the tiled output (one core-matrix row: 8 BF16 or 4
+// TF32 values of one operand row).  Inside a tile the units are ordered
+// (row group, K chunk, row in group), so a warp reads 8 rows x 4 consecutive K chunks
+// and writes 512 contiguous bytes.  Blocks cover kSplitChunk units of one job.
 template <int KIND>
-__global__ void k_tc_split(const TcSplitJob *__restrict__ jobs) {
+__global__ void __launch_bounds__(256) k_tc_split(const TcSplitJob *__restrict__ jobs, const int2 *__restrict__ chunks) {
   using H = Half<KIND>;
-  using T = typename H::T;
-  const TcSplitJob J = jobs[blockIdx.y];
-  constexpr int cme = H::per16;      // elements per core-matrix row
-  constexpr int tk = 8 * cme;        // elements per 128-byte tile row
-  const int64_t tile_elems = (int64_t)J.tile_rows * tk;
-  const int64_t total = (int64_t)(J.rows_pad / J.tile_rows) * J.nk * tile_elems;
-  T *hi = (T *)J.hi, *lo = (T *)J.lo;
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t t = e / tile_elems;
-    const int w = (int)(e % tile_elems);
-    const int rt = (int)(t / J.nk), kt = (int)(t % J.nk);
-    const int cm = w / (8 * cme), in = w % (8 * cme);
-    const int row = rt * J.tile_rows + (cm / 8) * 8 + in / cme;
-    const int k = kt * tk + (cm % 8) * cme + in % cme;
-    double x = 0.0;
-    if (row < J.rows && k < J.cols) {
-      const int64_t o = (int64_t)row * J.sr + (int64_t)k * J.sk;
-      x = J.src[o];
-      if (J.sub) x -= J.sub[o];
-      x *= J.scale;
+  constexpr int cme = H::per16;  // elements per unit
+  constexpr int tk = 8 * cme;    // elements per 128-byte tile row
+  const int2 ck = chunks[blockIdx.x];
+  const TcSplitJob J = jobs[ck.x];
+  const int tile_units = J.tile_rows * 8;
+  const int total = (J.rows_pad / J.tile_rows) * J.nk * tile_units;
+  const int end = min(total, ck.y + kSplitChunk);
+  const bool scaled = J.scale != 1.0;
+  uint4 *hi = (uint4 *)J.hi, *lo = (uint4 *)J.lo;
+  for (int u = ck.y + threadIdx.x; u < end; u += blockDim.x) {
+    const int t = u / tile_units, w = u - t * tile_units;
+    const int rt = t / J.nk, kt = t - rt * J.nk;
+    const int g = w >> 6, kc = (w >> 3) & 7, r8 = w & 7;
+    const int row = rt * J.tile_rows + g * 8 + r8;
+    const int k0 = kt * tk + kc * cme;
+    double x[cme];
+    const bool live = row < J.rows && k0 < J.cols;
+    if (live) {
+      const double *src = J.src + (int64_t)row * J.sr;
+      const double *sub = J.sub ? J.sub + (int64_t)row * J.sr : nullptr;
+#pragma unroll
+      for (int j = 0; j < cme; ++j) {
+        const int k = k0 + j;
+        double v = 0.0;
+        if (k < J.cols) {
+          v = src[(int64_t)k * J.sk];
+          if (sub) v -= sub[(int64_t)k * J.sk];
+          if (scaled) v *= J.scale;
+        }
+        x[j] = v;
+      }
+      uint4 h, l;
+      split_unit<KIND, cme>(x, h, l);
+      hi[u] = h;
+      if (lo) lo[u] = l;
+    } else {
+      hi[u] = make_uint4(0, 0, 0, 0);
+      if (lo) lo[u] = make_uint4(0, 0, 0, 0);
     }
-    T h, l;
-    H::split(x, h, l);
-    hi[e] = h;
-    if (lo) lo[e] = l;
   }
 }
 
 }  // namespace
 
-void launch_tc_gemm(int kind, const TcProb *probs, const TcTile *tiles, int ntiles, int npad_max, int *err,
+void launch_tc_gemm(int kind, const TcProb *probs, const TcTile *tiles, int ntiles, int npad_max, int max_nk, int *err,
                     cudaStream_t st) {
   if (ntiles <= 0) return;
   const size_t stage_bytes = 2 * 128 * 128 + 2 * (size_t)npad_max * 128;
   const size_t budget = 227 * 1024 - 256;
   int stages = (int)std::min<size_t>(4, budget / stage_bytes);
+  stages = std::min(stages, std::max(max_nk, 1));
   if (stages < 1) stages = 1;
   const size_t smem = (size_t)stages * stage_bytes + (2 * stages + 1) * 8 + 16;
   if (kind == kTcBF16) {
@@ -304,12 +391,20 @@ void launch_tc_gemm(int kind, const TcProb *probs, const TcTile *tiles, int ntil
   }
 }
 
-void launch_tc_split(int kind, const TcSplitJob *jobs, int njobs, int64_t max_elems, cudaStream_t st) {
-  if (njobs <= 0) return;
-  const int bx = (int)std::min<int64_t>((max_elems + 255) / 256, 2048);
-  dim3 grid(std::max(bx, 1), njobs);
-  if (kind == kTcBF16) k_tc_split<kTcBF16><<<grid, 256, 0, st>>>(jobs);
-  else k_tc_split<kTcTF32><<<grid, 256, 0, st>>>(jobs);
+std::vector<int2> tc_split_chunks(const std::vector<TcSplitJob> &jobs) {
+  std::vector<int2> out;
+  for (size_t j = 0; j < jobs.size(); ++j) {
+    const TcSplitJob &J = jobs[j];
+    const int64_t units = (int64_t)(J.rows_pad / J.tile_rows) * J.nk * J.tile_rows * 8;
+    for (int64_t u = 0; u < units; u += kSplitChunk) out.push_back(make_int2((int)j, (int)u));
+  }
+  return out;
+}
+
+void launch_tc_split(int kind, const TcSplitJob *jobs, const int2 *chunks, int nchunks, cudaStream_t st) {
+  if (nchunks <= 0) return;
+  if (kind == kTcBF16) k_tc_split<kTcBF16><<<nchunks, 256, 0, st>>>(jobs, chunks);
+  else k_tc_split<kTcTF32><<<nchunks, 256, 0, st>>>(jobs, chunks);
 }
 
 }  // namespace ccx

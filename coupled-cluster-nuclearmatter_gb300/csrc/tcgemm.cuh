@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <vector>
 
 namespace ccx {
 
@@ -34,7 +35,8 @@ inline int tc_tile_k(int kind) { return kind == kTcBF16 ? 64 : 32; }
 
 // error codes written to *err (0 = ok): 1 load wait timed out, 2 MMA wait timed out,
 // 3 final wait timed out, 4 bad problem (npad > 256 or not a multiple of 16)
-void launch_tc_gemm(int kind, const TcProb *probs, const TcTile *tiles, int ntiles, int npad_max, int *err,
+// max_nk: largest K-tile count among the tiles (caps the shared-memory stages)
+void launch_tc_gemm(int kind, const TcProb *probs, const TcTile *tiles, int ntiles, int npad_max, int max_nk, int *err,
                     cudaStream_t st);
 
 // FP64 matrix (rows x cols, element (r, k) at src[r*sr + k*sk], optionally minus sub at
@@ -47,6 +49,9 @@ struct TcSplitJob {
   void *hi, *lo;
   double scale;
 };
-void launch_tc_split(int kind, const TcSplitJob *jobs, int njobs, int64_t max_elems, cudaStream_t st);
+// Work list of the split kernel: (job, first 16-byte unit) per block of kSplitChunk units.
+constexpr int kSplitChunk = 1024;
+std::vector<int2> tc_split_chunks(const std::vector<TcSplitJob> &jobs);
+void launch_tc_split(int kind, const TcSplitJob *jobs, const int2 *chunks, int nchunks, cudaStream_t st);
 
 }  // namespace ccx
