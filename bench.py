@@ -194,16 +194,20 @@ def kernel_work(P, H, ring, precision):
     b_pp = sum(2 * es * (p * p + p * h) + 16.0 * p * h for p, h in zip(P, H))
     b_i4 = sum(2 * es * (2.0 * nhp * nph) + 16.0 * nhp * nhp for nph, nhp in ring)
     b_ring = sum(2 * es * (nph * nhp + nhp * nhp) + 16.0 * nph * nhp for nph, nhp in ring)
+    # digit-product GEMM: 9 BF16 digit planes of V_pppp' and of T_b read once, C written
+    b_oz = sum(9 * 2.0 * (p * p + p * h) + 16.0 * p * h for p, h in zip(P, H))
     return {"x_fp64": ("flop", x), "i4_fp64": ("flop", i4), "ring_fp64": ("flop", rg),
             "ladder_fp64": ("flop", pp + hh), "pp_rebase_fp64": ("flop", pp), "hh_fp64": ("flop", hh),
-            "pp_tc": ("byte", b_pp), "i4_tc": ("byte", b_i4), "ring_tc": ("byte", b_ring)}
+            "pp_tc": ("byte", b_pp), "i4_tc": ("byte", b_i4), "ring_tc": ("byte", b_ring),
+            "pp_rebase_digits": ("byte", b_oz)}
 
 
 KERNEL_NAMES = {"x_fp64": "k_gemm<double> X = V_hhpp' T' (split-K)", "i4_fp64": "k_gemm<double> I4",
                 "ring_fp64": "k_gemm<double> ring", "ladder_fp64": "k_gemm<double> fused pp+hh ladder",
                 "pp_rebase_fp64": "k_gemm<double> pp-ladder at a re-base", "hh_fp64": "k_gemm<double> hh-ladder",
                 "pp_tc": "k_tc_gemm pp-ladder correction", "i4_tc": "k_tc_gemm dI4 correction",
-                "ring_tc": "k_tc_gemm ring corrections", "split": "k_tc_split"}
+                "ring_tc": "k_tc_gemm ring corrections", "split": "k_tc_split",
+                "pp_rebase_digits": "k_oz_gemm pp-ladder at a re-base (exact digit products)"}
 
 
 def run_ours(args, wl):
@@ -231,7 +235,8 @@ def run_ours(args, wl):
     def solve(eng, precision):
         eng.setup_t_amplitudes()
         return eng.ccd_iter(mode=ccx.MODE_STANDARD, precision=precision, tol=args.tol, max_iter=200, diis_dim=8,
-                            defect_period=args.defect_period)
+                            defect_period=args.defect_period,
+                            rebase=ccx.REBASE_DIGITS if (precision and args.rebase == "digits") else ccx.REBASE_FP64)
 
     def timed(precision, steps, sample_clocks):
         if dist:
@@ -307,6 +312,8 @@ def run_ours(args, wl):
 
     form = {0: "plain FP64", 1: "mixed BF16x3 + FP64 defect correction",
             2: "mixed TF32x3 + FP64 defect correction"}[prec]
+    if prec and args.rebase == "digits":
+        form += " (re-base pp-ladder as exact digit products on the tensor cores)"
     line = {"metric": METRIC, "value": ms * 1e-3, "unit": "s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64" if real else "c128", "data": "synthetic",
@@ -314,6 +321,7 @@ def run_ours(args, wl):
             "config": {"workload": wl["desc"], "solver": f"Jacobi + DIIS(8) to ||R-DT||<{args.tol:g} (FP64 residual)",
                        "precision": args.precision if prec else "fp64",
                        "defect_period": args.defect_period or "adaptive",
+                       "rebase": args.rebase if prec else None,
                        "l2": "inputs larger than L2 (V_pppp packed, %.2f GB, read every iteration)"
                              % (sum(p * p for p in P) * 8 / 1e9),
                        "replicas": world},
@@ -421,6 +429,8 @@ def main():
     ap.add_argument("--tol", type=float, default=1e-10)
     ap.add_argument("--precision", default="bf16x3", choices=sorted(PRECISIONS))
     ap.add_argument("--defect-period", type=int, default=0, help="FP64 re-base every k iterations (0: adaptive)")
+    ap.add_argument("--rebase", default="digits", choices=["fp64", "digits"],
+                    help="pp-ladder product of a re-base: FP64 FMA GEMM or exact digit products on the tensor cores")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()

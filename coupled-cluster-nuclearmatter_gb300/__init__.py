@@ -24,6 +24,7 @@ V_PPPP = 6
 POT_MINNESOTA, POT_CHIRAL_LIKE = 0, 1
 MODE_REFERENCE, MODE_STANDARD = 0, 1
 PREC_FP64, PREC_MIXED, PREC_MIXED_TF32 = 0, 1, 2
+REBASE_FP64, REBASE_DIGITS = 0, 1
 SCALAR_COMPLEX, SCALAR_REAL = 0, 1
 
 
@@ -68,7 +69,7 @@ class _Potential(C.Structure):
 
 class _IterOpts(C.Structure):
     _fields_ = [("mode", C.c_int32), ("precision", C.c_int32), ("max_iter", C.c_int32), ("tol", C.c_double),
-                ("diis_dim", C.c_int32), ("defect_period", C.c_int32), ("verbose", C.c_int32)]
+                ("diis_dim", C.c_int32), ("defect_period", C.c_int32), ("verbose", C.c_int32), ("rebase", C.c_int32)]
 
 
 class _IterResult(C.Structure):
@@ -400,8 +401,8 @@ class Engine:
         return x.value
 
     def ccd_iter(self, mode=MODE_REFERENCE, precision=PREC_FP64, max_iter=100, tol=1e-6, diis_dim=8,
-                 defect_period=0, verbose=False) -> dict:
-        o = _IterOpts(mode, precision, max_iter, tol, diis_dim, defect_period, int(verbose))
+                 defect_period=0, verbose=False, rebase=REBASE_FP64) -> dict:
+        o = _IterOpts(mode, precision, max_iter, tol, diis_dim, defect_period, int(verbose), rebase)
         r = _IterResult()
         _check(lib().ccx_ccd_iter(self._h, C.byref(o), C.byref(r)))
         return {"iterations": r.iterations, "converged": bool(r.converged),
@@ -426,7 +427,7 @@ class Engine:
         return x.value
 
     KERNEL_SLOTS = ("x_fp64", "i4_fp64", "ring_fp64", "ladder_fp64", "pp_rebase_fp64", "hh_fp64",
-                    "pp_tc", "i4_tc", "ring_tc", "split")
+                    "pp_tc", "i4_tc", "ring_tc", "split", "pp_rebase_digits")
 
     def kernel_timers(self) -> dict:
         """{slot: (total ms, timed brackets)} of individual launches in the last ccd_iter."""

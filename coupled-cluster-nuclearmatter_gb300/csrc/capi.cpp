@@ -398,7 +398,7 @@ int ccx_device_fp64_peak(int32_t device, double *tflops) {
 }
 int ccx_selftest_tc_gemm(int32_t device, int32_t kind, int32_t nprob, const int32_t *M, const int32_t *N,
                          const int32_t *K, int32_t use_alo, uint64_t seed, double *max_rel_err, double *ms) {
-  if (!M || !N || !K || !max_rel_err || !ms || nprob <= 0 || (kind != 0 && kind != 1))
+  if (!M || !N || !K || !max_rel_err || !ms || nprob <= 0 || kind < 0 || kind > 2)
     return fail(CCX_EINVAL, "bad selftest arguments");
   return guard([&] { ccx::tc_selftest(device, kind, nprob, M, N, K, use_alo, seed, max_rel_err, ms); });
 }
@@ -457,6 +457,7 @@ int ccx_ccd_iter(ccx_engine *e, const ccx_iter_opts *opt, ccx_iter_result *res) 
     o.tol = opt->tol;
     o.diis_dim = opt->diis_dim;
     o.defect_period = opt->defect_period;
+    o.rebase = opt->rebase;
     o.verbose = opt->verbose;
     ccx::IterResult r;
     e->E->ccd_iter(o, r);

@@ -14,6 +14,7 @@
 #include "devlayout.hpp"
 #include "engine.hpp"
 #include "kernels.hpp"
+#include "ozaki.cuh"
 #include "tcgemm.cuh"
 #include "triples.hpp"
 
@@ -431,6 +432,7 @@ class Engine final : public IEngine {
   void ccd_iter(const IterOpts &o, IterResult &r) override {
     require_ready();
     if (o.precision < 0 || o.precision > 2) throw EngineError(1, "unknown precision");
+    if (o.rebase < 0 || o.rebase > 1) throw EngineError(1, "unknown re-base product kind");
     if (o.precision != 0 && o.mode != 1) throw EngineError(1, "mixed precision runs with the standard (DIIS) mode");
     if (o.precision != 0 && ScalarOf<S>::complex)
       throw EngineError(1, "mixed precision is implemented for real interactions (real engine)");
@@ -981,6 +983,7 @@ class Engine final : public IEngine {
     constexpr double kRebaseDrop = 1e-4;
     if (mixed) {
       prepare_mixed(o.precision == 2 ? kTcTF32 : kTcBF16);
+      if (o.rebase == 1) prepare_oz();
       set_base_zero();
     }
     const int m = std::max(2, std::min(o.diis_dim, 15));
@@ -996,7 +999,7 @@ class Engine final : public IEngine {
       const bool exact = !mixed || need_fp64;
       if (!mixed) residual(true);
       else if (exact) {
-        residual_fp64_rebase();
+        residual_fp64_rebase(o.rebase == 1);
         ++r.fp64_sweeps;
       } else {
         residual_mixed();
@@ -1130,6 +1133,101 @@ class Engine final : public IEngine {
     launch_tc_split(tc_kind_, (const TcSplitJob *)pl.jobs.p, (const int2 *)pl.chunks.p, pl.nchunks, st_);
     ++launches_;
   }
+  // ---- FP64-accurate re-base products as exact digit products (Ozaki scheme) ----
+  struct OzSplitPlan {
+    DBuf jobs, rows, chunks;
+    int nrows = 0, nchunks = 0;
+  };
+  struct OzPlan {
+    DBuf probs, tiles;
+    int ntiles = 0;
+  };
+  void finalize_oz_split(OzSplitPlan &pl, const std::vector<OzSplitJob> &jobs) {
+    upload(pl.jobs, jobs, &bytes_);
+    const std::vector<int2> rows = oz_row_table(jobs), ch = oz_split_chunks(jobs);
+    upload(pl.rows, rows, &bytes_);
+    upload(pl.chunks, ch, &bytes_);
+    pl.nrows = (int)rows.size();
+    pl.nchunks = (int)ch.size();
+  }
+  void run_oz_split(const OzSplitPlan &pl) {
+    launch_oz_split((const OzSplitJob *)pl.jobs.p, (const int2 *)pl.rows.p, pl.nrows, (const int2 *)pl.chunks.p,
+                    pl.nchunks, st_);
+    launches_ += 2;
+  }
+  void run_oz(const OzPlan &pl) {
+    launch_oz_gemm((const OzProb *)pl.probs.p, (const OzTile *)pl.tiles.p, pl.ntiles, tcerr_.as<int>(), st_);
+    ++launches_;
+  }
+  // digit planes of V_pppp' (static), of the base amplitudes (per re-base) and the
+  // problem list of PP_b = V_pppp' T_b
+  void prepare_oz() {
+    if (oz_ready_ && oz_v_version_ == v_version_) return;
+    const Layout &L = *L_;
+    const int nc = L.fam[3].count();
+    auto mpad = [](int x) { return (x + 127) / 128 * 128; };
+    auto npadf = [](int x) { return (x + 15) / 16 * 16; };
+    auto nkf = [](int x) { return (x + 63) / 64; };
+    int64_t pa = 0, pb = 0, ra = 0, rb = 0;
+    for (int c = 0; c < nc; ++c) {
+      const auto &pk = L.pk[c];
+      if (pk.P <= 0 || pk.H <= 0) continue;
+      if (pk.H > 256) throw EngineError(1, "digit-product re-base: an hhpp channel has more than 256 packed hole pairs");
+      pa += (int64_t)mpad(pk.P) * nkf(pk.P) * 64;
+      pb += (int64_t)npadf(pk.H) * nkf(pk.P) * 64;
+      ra += pk.P;
+      rb += npadf(pk.H);
+    }
+    ozVpp_.alloc((size_t)std::max<int64_t>(pa, 8) * kOzSlices * 2, &bytes_);
+    ozVppE_.alloc((size_t)std::max<int64_t>(ra, 1) * 4, &bytes_);
+    ozTb_.alloc((size_t)std::max<int64_t>(pb, 8) * kOzSlices * 2, &bytes_);
+    ozTbE_.alloc((size_t)std::max<int64_t>(rb, 1) * 4, &bytes_);
+    if (!tcerr_.p) {
+      tcerr_.alloc(sizeof(int), &bytes_);
+      CK(cudaMemset(tcerr_.p, 0, sizeof(int)));
+    }
+    std::vector<OzSplitJob> ja, jb;
+    std::vector<OzProb> probs;
+    std::vector<OzTile> tiles;
+    int64_t qa = 0, qb = 0, xa = 0, xb = 0, voff = 0;
+    for (int c = 0; c < nc; ++c) {
+      const auto &pk = L.pk[c];
+      if (pk.P > 0 && pk.H > 0) {
+        OzSplitJob a{};
+        a.src = (const double *)(Vpp_.as<S>() + voff); a.sr = pk.P; a.sk = 1;
+        a.rows = pk.P; a.cols = pk.P; a.tile_rows = 128; a.nk = nkf(pk.P); a.rows_pad = mpad(pk.P);
+        a.planes = ozVpp_.as<uint16_t>() + qa; a.plane_elems = pa; a.exps = ozVppE_.as<int>() + xa;
+        OzSplitJob b{};
+        b.src = (const double *)(T_.as<S>() + pk.t_off); b.sr = pk.P; b.sk = 1;
+        b.rows = pk.H; b.cols = pk.P; b.tile_rows = npadf(pk.H); b.nk = nkf(pk.P); b.rows_pad = npadf(pk.H);
+        b.planes = ozTb_.as<uint16_t>() + qb; b.plane_elems = pb; b.exps = ozTbE_.as<int>() + xb;
+        OzProb p{};
+        p.A = a.planes; p.eA = a.exps; p.B = b.planes; p.eB = b.exps; p.a_plane = pa; p.b_plane = pb;
+        p.M = pk.P; p.N = pk.H; p.nk = nkf(pk.P); p.npad = npadf(pk.H);
+        p.C = (double *)(PPb_.as<S>() + pk.t_off); p.sCm = 1; p.sCn = pk.P; p.alpha = 1.0;
+        for (int mt = 0; mt < mpad(pk.P) / 128; ++mt)
+          for (int n0 = 0; n0 < p.npad; n0 += kOzN) tiles.push_back(OzTile{(int)probs.size(), mt, n0});
+        probs.push_back(p);
+        ja.push_back(a);
+        jb.push_back(b);
+        qa += (int64_t)mpad(pk.P) * nkf(pk.P) * 64;
+        qb += (int64_t)npadf(pk.H) * nkf(pk.P) * 64;
+        xa += pk.P;
+        xb += npadf(pk.H);
+      }
+      voff += (int64_t)pk.P * pk.P;
+    }
+    finalize_oz_split(ozsVpp_, ja);
+    finalize_oz_split(ozsTb_, jb);
+    upload(ozPP_.probs, probs, &bytes_);
+    upload(ozPP_.tiles, tiles, &bytes_);
+    ozPP_.ntiles = (int)tiles.size();
+    run_oz_split(ozsVpp_);
+    CK(cudaStreamSynchronize(st_));
+    oz_ready_ = true;
+    oz_v_version_ = v_version_;
+  }
+
   void check_tc_error() {
     int err = 0;
     CK(cudaMemcpyAsync(&host_flag_, tcerr_.p, sizeof(int), cudaMemcpyDeviceToHost, st_));
@@ -1144,6 +1242,7 @@ class Engine final : public IEngine {
   // Tile buffers, split jobs and tensor-core problem lists of the mixed residual.
   void prepare_mixed(int kind) {
     if (mixed_ready_ && tc_kind_ == kind && mixed_v_version_ == v_version_) return;
+    oz_ready_ = false;  // the re-base problem list points into buffers allocated here
     const Layout &L = *L_;
     tc_kind_ = kind;
     const int tk = tc_tile_k(kind);
@@ -1314,8 +1413,9 @@ class Engine final : public IEngine {
     run_split(spTphb_);
   }
 
-  // FP64 residual at T that also becomes the new base of the defect correction
-  void residual_fp64_rebase() {
+  // FP64 residual at T that also becomes the new base of the defect correction; with
+  // digits, PP_b = V_pppp' T comes from the exact digit-product GEMM
+  void residual_fp64_rebase(bool digits) {
     mark(0);
     launch_gather_tph<S>(D_, T_.as<S>(), Tph_.as<S>(), st_);
     mark(1);
@@ -1338,9 +1438,19 @@ class Engine final : public IEngine {
     mark(5);
     launch_rinit<S>(D_, T_.as<S>(), Vhp_.as<S>(), Rph_.as<S>(), i6off_.as<S>(), i7off_.as<S>(), R_.as<S>(), st_);
     mark(6);
-    kbegin(kKPP64);
-    run_plan(planPP_);
-    kend();
+    if (digits) {
+      kbegin(kKSplit);
+      run_oz_split(ozsTb_);
+      kend();
+      CK(cudaMemsetAsync(PPb_.p, 0, n_t_ * sizeof(S), st_));
+      kbegin(kKPPOz);
+      run_oz(ozPP_);
+      kend();
+    } else {
+      kbegin(kKPP64);
+      run_plan(planPP_);
+      kend();
+    }
     launch_axpy<S>(n_t_, PPb_.as<S>(), R_.as<S>(), st_);
     kbegin(kKHH64);
     run_plan(planHH_);
@@ -1441,6 +1551,11 @@ class Engine final : public IEngine {
   int tc_kind_ = 0;
   int64_t v_version_ = 0, mixed_v_version_ = -1;
   DBuf Tb_, PPb_, Tphb_, Rphb_, I4b_, dI4_, tcerr_;
+  DBuf ozVpp_, ozVppE_, ozTb_, ozTbE_;
+  OzSplitPlan ozsVpp_, ozsTb_;
+  OzPlan ozPP_;
+  bool oz_ready_ = false;
+  int64_t oz_v_version_ = -1;
   TileBuf tVpp_, tD_, tVph_, tDphB_, tTphbA_, tDphA_, tdI4B_, tI4B_;
   TcPlan tcPP_, tcI4_, tcR1_, tcR2_;
   SplitPlan spStatic_, spTphb_, spIter1_, spIter2_;

@@ -23,6 +23,7 @@ struct IterOpts {
   int diis_dim = 8;
   int defect_period = 0;  // mixed: FP64 re-base every k iterations; 0 adaptive
   int verbose = 0;
+  int rebase = 0;        // mixed: products of a re-base as 0 FP64 FMA GEMMs, 1 exact digit products (tensor cores)
 };
 struct IterResult {
   int iterations = 0, converged = 0;
@@ -48,6 +49,7 @@ enum KernelSlot {
   kKTcI4 = 7,   // k_tc_gemm: dI4 = 1/2 V_ph dT_ph
   kKTcRing = 8, // k_tc_gemm: ring corrections (two launches per residual)
   kKSplit = 9,  // k_tc_split: per-iteration operand splits
+  kKPPOz = 10,  // k_oz_gemm: V_pppp' T' at a re-base as exact digit products
   kKernelSlots = 12
 };
 

@@ -11,6 +11,7 @@
 #include <vector>
 
 #include "engine.hpp"
+#include "ozaki.cuh"
 #include "tcgemm.cuh"
 
 namespace ccx {
@@ -26,11 +27,125 @@ struct Dev {
 };
 }  // namespace
 
+// Ozaki digit-product GEMM on the same kind of problems; reference in long double.
+static void oz_selftest(int nprob, const int *Ms, const int *Ns, const int *Ks, uint64_t seed, double *max_rel, double *ms) {
+  std::mt19937_64 rng(seed);
+  std::uniform_real_distribution<double> U(-1.0, 1.0);
+  struct Host {
+    int M, N, K, nk, npad, mpad;
+    std::vector<double> A, B, C;
+  };
+  std::vector<Host> h(nprob);
+  size_t fa = 0, fb = 0, fc = 0, pa = 0, pb = 0;
+  for (int i = 0; i < nprob; ++i) {
+    Host &x = h[i];
+    x.M = Ms[i]; x.N = Ns[i]; x.K = Ks[i];
+    if (x.M <= 0 || x.N <= 0 || x.N > 256 || x.K <= 0) throw EngineError(1, "selftest: bad problem shape");
+    x.nk = (x.K + 63) / 64;
+    x.npad = (x.N + 15) / 16 * 16;
+    x.mpad = (x.M + 127) / 128 * 128;
+    x.A.resize((size_t)x.M * x.K);
+    x.B.resize((size_t)x.K * x.N);
+    x.C.resize((size_t)x.M * x.N);
+    for (double &v : x.A) v = U(rng) * std::pow(10.0, -3.0 * std::fabs(U(rng)));
+    for (double &v : x.B) v = U(rng) * std::pow(10.0, -3.0 * std::fabs(U(rng)));
+    for (double &v : x.C) v = U(rng);
+    fa += x.A.size(); fb += x.B.size(); fc += x.C.size();
+    pa += (size_t)x.mpad * x.nk * 64;
+    pb += (size_t)x.npad * x.nk * 64;
+  }
+  Dev dA(fa * 8), dB(fb * 8), dC(fc * 8), plA(pa * kOzSlices * 2), plB(pb * kOzSlices * 2);
+  size_t ra = 0, rb = 0;
+  for (auto &x : h) { ra += x.M; rb += x.npad; }
+  Dev eA(ra * 4), eB(rb * 4), dE(4);
+  std::vector<OzSplitJob> jobs;
+  std::vector<OzProb> probs;
+  std::vector<OzTile> tiles;
+  size_t oa = 0, ob = 0, oc = 0, qa = 0, qb = 0, xa = 0, xb = 0;
+  for (int i = 0; i < nprob; ++i) {
+    Host &x = h[i];
+    sck(cudaMemcpy((double *)dA.p + oa, x.A.data(), x.A.size() * 8, cudaMemcpyHostToDevice), "copy A");
+    sck(cudaMemcpy((double *)dB.p + ob, x.B.data(), x.B.size() * 8, cudaMemcpyHostToDevice), "copy B");
+    sck(cudaMemcpy((double *)dC.p + oc, x.C.data(), x.C.size() * 8, cudaMemcpyHostToDevice), "copy C");
+    OzSplitJob ja{};
+    ja.src = (double *)dA.p + oa; ja.sr = x.K; ja.sk = 1; ja.rows = x.M; ja.cols = x.K; ja.tile_rows = 128;
+    ja.nk = x.nk; ja.rows_pad = x.mpad; ja.planes = (uint16_t *)plA.p + qa; ja.plane_elems = (int64_t)pa;
+    ja.exps = (int *)eA.p + xa;
+    OzSplitJob jb{};
+    jb.src = (double *)dB.p + ob; jb.sr = x.K; jb.sk = 1; jb.rows = x.N; jb.cols = x.K; jb.tile_rows = x.npad;
+    jb.nk = x.nk; jb.rows_pad = x.npad; jb.planes = (uint16_t *)plB.p + qb; jb.plane_elems = (int64_t)pb;
+    jb.exps = (int *)eB.p + xb;
+    jobs.push_back(ja);
+    jobs.push_back(jb);
+    OzProb p{};
+    p.A = ja.planes; p.eA = ja.exps; p.B = jb.planes; p.eB = jb.exps; p.a_plane = (int64_t)pa; p.b_plane = (int64_t)pb;
+    p.M = x.M; p.N = x.N; p.nk = x.nk; p.npad = x.npad;
+    p.C = (double *)dC.p + oc; p.sCm = 1; p.sCn = x.M; p.alpha = 0.5;
+    for (int mt = 0; mt < x.mpad / 128; ++mt)
+      for (int n0 = 0; n0 < x.npad; n0 += kOzN) tiles.push_back(OzTile{i, mt, n0});
+    probs.push_back(p);
+    oa += x.A.size(); ob += x.B.size(); oc += x.C.size();
+    qa += (size_t)x.mpad * x.nk * 64; qb += (size_t)x.npad * x.nk * 64;
+    xa += x.M; xb += x.npad;
+  }
+  const std::vector<int2> rows = oz_row_table(jobs), chunks = oz_split_chunks(jobs);
+  Dev dJ(jobs.size() * sizeof(OzSplitJob)), dR(rows.size() * sizeof(int2)), dK(chunks.size() * sizeof(int2));
+  Dev dP(probs.size() * sizeof(OzProb)), dT(tiles.size() * sizeof(OzTile));
+  sck(cudaMemcpy(dJ.p, jobs.data(), jobs.size() * sizeof(OzSplitJob), cudaMemcpyHostToDevice), "copy jobs");
+  sck(cudaMemcpy(dR.p, rows.data(), rows.size() * sizeof(int2), cudaMemcpyHostToDevice), "copy rows");
+  sck(cudaMemcpy(dK.p, chunks.data(), chunks.size() * sizeof(int2), cudaMemcpyHostToDevice), "copy chunks");
+  sck(cudaMemcpy(dP.p, probs.data(), probs.size() * sizeof(OzProb), cudaMemcpyHostToDevice), "copy probs");
+  sck(cudaMemcpy(dT.p, tiles.data(), tiles.size() * sizeof(OzTile), cudaMemcpyHostToDevice), "copy tiles");
+  sck(cudaMemset(dE.p, 0, 4), "memset");
+  launch_oz_split((const OzSplitJob *)dJ.p, (const int2 *)dR.p, (int)rows.size(), (const int2 *)dK.p,
+                  (int)chunks.size(), 0);
+  sck(cudaGetLastError(), "oz split launch");
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventRecord(e0);
+  launch_oz_gemm((const OzProb *)dP.p, (const OzTile *)dT.p, (int)tiles.size(), (int *)dE.p, 0);
+  cudaEventRecord(e1);
+  sck(cudaGetLastError(), "oz gemm launch");
+  sck(cudaEventSynchronize(e1), "oz gemm");
+  float t = 0.f;
+  cudaEventElapsedTime(&t, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  *ms = t;
+  int err = 0;
+  sck(cudaMemcpy(&err, dE.p, 4, cudaMemcpyDeviceToHost), "copy err");
+  if (err) throw EngineError(2, "Ozaki GEMM reported error code " + std::to_string(err));
+  double worst = 0.0;
+  oc = 0;
+  for (auto &x : h) {
+    std::vector<double> c(x.C.size());
+    sck(cudaMemcpy(c.data(), (double *)dC.p + oc, c.size() * 8, cudaMemcpyDeviceToHost), "copy C back");
+    long double scale = 0.0L, diff = 0.0L;
+    for (int n = 0; n < x.N; ++n)
+      for (int m = 0; m < x.M; ++m) {
+        long double ref = 0.0L;
+        for (int k = 0; k < x.K; ++k) ref += (long double)x.A[(size_t)m * x.K + k] * x.B[(size_t)k + (size_t)x.K * n];
+        const long double prod = 0.5L * ref;
+        scale = std::max(scale, std::fabs(prod));
+        const long double exact = (long double)x.C[m + (size_t)x.M * n] + prod;
+        diff = std::max(diff, std::fabs((long double)c[m + (size_t)x.M * n] - exact));
+      }
+    worst = std::max(worst, (double)(diff / std::max(scale, 1e-300L)));
+    oc += x.C.size();
+  }
+  *max_rel = worst;
+}
+
 // problems: M_i, N_i, K_i for i < nprob.  Returns max |C - C_ref| / max |C_ref| over all
-// problems and the kernel time (ms).
+// problems and the kernel time (ms).  kind 2: the Ozaki digit-product GEMM.
 void tc_selftest(int device, int kind, int nprob, const int *Ms, const int *Ns, const int *Ks, int use_alo, uint64_t seed,
                  double *max_rel, double *ms) {
   sck(cudaSetDevice(device), "cudaSetDevice");
+  if (kind == 2) {
+    oz_selftest(nprob, Ms, Ns, Ks, seed, max_rel, ms);
+    return;
+  }
   const int tk = kind == kTcBF16 ? 64 : 32;
   const int es = kind == kTcBF16 ? 2 : 4;
   std::mt19937_64 rng(seed);

@@ -251,7 +251,11 @@ typedef struct {
   int32_t defect_period;     /* mixed precision: FP64 re-base every k iterations; 0 = adaptive
                                 (when the mixed residual has dropped 1e4x, stalls or meets tol) */
   int32_t verbose;
+  int32_t rebase;            /* mixed precision: CCX_REBASE_* */
 } ccx_iter_opts;
+#define CCX_REBASE_FP64 0      /* products of a re-base on the FP64 FMA pipe */
+#define CCX_REBASE_DIGITS 1    /* the pp-ladder product of a re-base as exact 6-bit digit products on the
+                                  BF16 tensor cores (Ozaki scheme), FP64-accurate */
 
 typedef struct {
   int32_t iterations;
@@ -282,7 +286,8 @@ int ccx_device_fp64_peak(int32_t device, double *tflops);
 /* Self-test of the tensor-core split GEMM used by CCX_PREC_MIXED: nprob random
  * problems C += 1/2 A B (M_i x K_i times K_i x N_i, N_i <= 256) through the same
  * operand tiling and tcgen05 kernel, against an FP64 host product.
- * kind 0: BF16 hi/lo split, kind 1: TF32 hi/lo split; use_alo 0 drops the A_lo term.
+ * kind 0: BF16 hi/lo split, kind 1: TF32 hi/lo split; use_alo 0 drops the A_lo term;
+ * kind 2: the FP64-accurate digit-product (Ozaki) GEMM, checked against long double.
  * *max_rel_err = max |C - C_ref| / max |1/2 A B| over the problems; *ms kernel time. */
 int ccx_selftest_tc_gemm(int32_t device, int32_t kind, int32_t nprob, const int32_t *M, const int32_t *N,
                          const int32_t *K, int32_t use_alo, uint64_t seed, double *max_rel_err, double *ms);
@@ -298,7 +303,7 @@ int ccx_engine_timers(const ccx_engine *e, double ms[10]);
  * [3] fused pp+hh ladder (FP64), [4] V_pppp' T' at a mixed-precision re-base (FP64),
  * [5] hh-ladder of the mixed residual (FP64), [6] pp-ladder correction (tensor cores),
  * [7] dI4 correction (tensor cores), [8] ring corrections (tensor cores),
- * [9] operand splits, [10..11] unused */
+ * [9] operand splits, [10] pp-ladder at a re-base as digit products (tensor cores), [11] unused */
 int ccx_engine_kernel_timers(const ccx_engine *e, double ms[12], int64_t launches[12]);
 
 #ifdef __cplusplus

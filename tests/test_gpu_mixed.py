@@ -8,12 +8,13 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def solve(ccx, nmax, A, rho, precision, tol=1e-10, defect_period=0, snm=False):
+def solve(ccx, nmax, A, rho, precision, tol=1e-10, defect_period=0, snm=False, rebase=0):
     L = ccx.Layout.from_basis(nmax, A, rho, snm=snm)
     e = ccx.Engine(L, real=True)
     e.generate()
     e.setup_t_amplitudes()
-    r = e.ccd_iter(mode=ccx.MODE_STANDARD, precision=precision, tol=tol, max_iter=200, defect_period=defect_period)
+    r = e.ccd_iter(mode=ccx.MODE_STANDARD, precision=precision, tol=tol, max_iter=200, defect_period=defect_period,
+                   rebase=rebase)
     return e, r
 
 
@@ -54,6 +55,27 @@ def test_mixed_pnm66_full_size(ccx):
     assert rm["seconds"] < r64["seconds"]
 
 
+@pytest.mark.parametrize("prec", ["bf16", "tf32"])
+def test_digit_rebase_matches_fp64_pnm14(ccx, prec):
+    """Re-base products as exact digit products on the tensor cores: same fixed point."""
+    p = ccx.PREC_MIXED if prec == "bf16" else ccx.PREC_MIXED_TF32
+    _, r64 = solve(ccx, 2, 14, 0.08, ccx.PREC_FP64)
+    _, rd = solve(ccx, 2, 14, 0.08, p, rebase=ccx.REBASE_DIGITS)
+    assert rd["converged"] and rd["res_norm"] < 1e-10
+    assert abs(rd["e_ccd"] - r64["e_ccd"]) < 1e-10 * abs(r64["e_ccd"])
+
+
+def test_digit_rebase_pnm66_full_size(ccx):
+    e64, r64 = solve(ccx, 4, 66, 0.16, ccx.PREC_FP64)
+    ed, rd = solve(ccx, 4, 66, 0.16, ccx.PREC_MIXED, rebase=ccx.REBASE_DIGITS)
+    assert rd["converged"] and rd["res_norm"] < 1e-10
+    assert abs((rd["e_ccd"] - r64["e_ccd"]).real) / 66 * 1e3 < 1e-6
+    # the re-base's pp-ladder agrees with the FP64 GEMM: the FP64 and digit re-base
+    # solves stop at the same residual level
+    _, rf = solve(ccx, 4, 66, 0.16, ccx.PREC_MIXED)
+    assert rd["fp64_sweeps"] <= rf["fp64_sweeps"] + 1
+
+
 def test_mixed_rejects_unsupported(ccx):
     L = ccx.Layout.from_basis(1, 2, 0.08)
     ec = ccx.Engine(L, real=False)
@@ -66,3 +88,5 @@ def test_mixed_rejects_unsupported(ccx):
     er.setup_t_amplitudes()
     with pytest.raises(ccx.CcxError):
         er.ccd_iter(mode=ccx.MODE_REFERENCE, precision=ccx.PREC_MIXED)
+    with pytest.raises(ccx.CcxError):
+        er.ccd_iter(mode=ccx.MODE_STANDARD, precision=ccx.PREC_MIXED, rebase=7)

@@ -1,4 +1,4 @@
-"""Tensor-core split GEMM (tcgen05, used by the mixed-precision CCD) against FP64.
+"""Tensor-core GEMMs (tcgen05, used by the mixed-precision CCD) against FP64.
 
 Error scale of a hi/lo split product: BF16 pairs carry ~16 significant bits, TF32
 pairs ~22, but both accumulate in FP32 tensor memory, which bounds the relative error
@@ -29,3 +29,12 @@ def test_dropping_a_lo_is_less_accurate(ccx):
     full, _ = ccx.selftest_tc_gemm(RAGGED, kind=0, use_alo=True)
     two, _ = ccx.selftest_tc_gemm(RAGGED, kind=0, use_alo=False)
     assert two > 10 * full and two < 2e-2
+
+
+@pytest.mark.parametrize("shapes", [SMALL, RAGGED], ids=["single_tile", "ragged_grouped"])
+def test_ozaki_digit_gemm_is_fp64_accurate(ccx, shapes):
+    """kind 2: 9 six-bit digits per operand, exact FP32 level sums; against a long
+    double reference the error stays at the FP64 rounding level (FP64 GEMM itself is
+    ~sqrt(K) 2^-53 relative to sum |a||b|, here ~1e-14 of max |AB|)."""
+    err, ms = ccx.selftest_tc_gemm(shapes, kind=2)
+    assert err < 1e-13, err
