@@ -196,10 +196,13 @@ def kernel_work(P, H, ring, precision):
     b_ring = sum(2 * es * (nph * nhp + nhp * nhp) + 16.0 * nph * nhp for nph, nhp in ring)
     # digit-product GEMM: 9 BF16 digit planes of V_pppp' and of T_b read once, C written
     b_oz = sum(9 * 2.0 * (p * p + p * h) + 16.0 * p * h for p, h in zip(P, H))
+    b_i4_oz = sum(9 * 2.0 * (2.0 * nhp * nph) + 16.0 * nhp * nhp for nph, nhp in ring)
+    b_ring_oz = sum(9 * 2.0 * (nph * nhp + nhp * nhp) + 16.0 * nph * nhp for nph, nhp in ring)
     return {"x_fp64": ("flop", x), "i4_fp64": ("flop", i4), "ring_fp64": ("flop", rg),
             "ladder_fp64": ("flop", pp + hh), "pp_rebase_fp64": ("flop", pp), "hh_fp64": ("flop", hh),
             "pp_tc": ("byte", b_pp), "i4_tc": ("byte", b_i4), "ring_tc": ("byte", b_ring),
-            "pp_rebase_digits": ("byte", b_oz)}
+            "pp_rebase_digits": ("byte", b_oz), "i4_rebase_digits": ("byte", b_i4_oz),
+            "ring_rebase_digits": ("byte", b_ring_oz)}
 
 
 KERNEL_NAMES = {"x_fp64": "k_gemm<double> X = V_hhpp' T' (split-K)", "i4_fp64": "k_gemm<double> I4",
@@ -207,7 +210,9 @@ KERNEL_NAMES = {"x_fp64": "k_gemm<double> X = V_hhpp' T' (split-K)", "i4_fp64": 
                 "pp_rebase_fp64": "k_gemm<double> pp-ladder at a re-base", "hh_fp64": "k_gemm<double> hh-ladder",
                 "pp_tc": "k_tc_gemm pp-ladder correction", "i4_tc": "k_tc_gemm dI4 correction",
                 "ring_tc": "k_tc_gemm ring corrections", "split": "k_tc_split",
-                "pp_rebase_digits": "k_oz_gemm pp-ladder at a re-base (exact digit products)"}
+                "pp_rebase_digits": "k_oz_gemm pp-ladder at a re-base (exact digit products)",
+                "i4_rebase_digits": "k_oz_gemm I4 at a re-base (exact digit products)",
+                "ring_rebase_digits": "k_oz_gemm ring at a re-base (exact digit products)"}
 
 
 def run_ours(args, wl):
@@ -313,7 +318,7 @@ def run_ours(args, wl):
     form = {0: "plain FP64", 1: "mixed BF16x3 + FP64 defect correction",
             2: "mixed TF32x3 + FP64 defect correction"}[prec]
     if prec and args.rebase == "digits":
-        form += " (re-base pp-ladder as exact digit products on the tensor cores)"
+        form += " (re-base products as exact digit products on the tensor cores)"
     line = {"metric": METRIC, "value": ms * 1e-3, "unit": "s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64" if real else "c128", "data": "synthetic",

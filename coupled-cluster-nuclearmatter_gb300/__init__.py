@@ -427,12 +427,13 @@ class Engine:
         return x.value
 
     KERNEL_SLOTS = ("x_fp64", "i4_fp64", "ring_fp64", "ladder_fp64", "pp_rebase_fp64", "hh_fp64",
-                    "pp_tc", "i4_tc", "ring_tc", "split", "pp_rebase_digits")
+                    "pp_tc", "i4_tc", "ring_tc", "split", "pp_rebase_digits", "i4_rebase_digits",
+                    "ring_rebase_digits")
 
     def kernel_timers(self) -> dict:
         """{slot: (total ms, timed brackets)} of individual launches in the last ccd_iter."""
-        ms = np.zeros(12)
-        n = np.zeros(12, np.int64)
+        ms = np.zeros(16)
+        n = np.zeros(16, np.int64)
         _check(lib().ccx_engine_kernel_timers(self._h, _ptr(ms), _ptr(n)))
         return {k: (float(ms[i]), int(n[i])) for i, k in enumerate(self.KERNEL_SLOTS)}
 

@@ -353,7 +353,7 @@ int ccx_engine_timers(const ccx_engine *e, double ms[10]) {
   if (!ms) return fail(CCX_EINVAL, "null argument");
   ENGINE_CALL(e, e->E->timers(ms));
 }
-int ccx_engine_kernel_timers(const ccx_engine *e, double ms[12], int64_t launches[12]) {
+int ccx_engine_kernel_timers(const ccx_engine *e, double ms[16], int64_t launches[16]) {
   if (!ms || !launches) return fail(CCX_EINVAL, "null argument");
   ENGINE_CALL(e, e->E->kernel_timers(ms, launches));
 }

@@ -1011,13 +1011,20 @@ class Engine final : public IEngine {
       launch_update<S>(D_, 1, T_.as<S>(), R_.as<S>(), Vhp_.as<S>(), d2ij_.as<S>(), d2ab_.as<S>(), ht, he,
                        partial_.as<double>(), res_.as<double>(), st_);
       launches_ += 2;
+      // the tensor-core error word rides on the same synchronisation as the energy
+      int *tc_word = (int *)(host_res_ + 63);
+      if (mixed) CK(cudaMemcpyAsync(tc_word, tcerr_.p, sizeof(int), cudaMemcpyDeviceToHost, st_));
       fetch_res(3);
       mark(8);
       if (timing_) accumulate_timers(7, 8);
       e[0] = host_res_[0];
       e[1] = host_res_[1];
       const double rn = 2.0 * std::sqrt(host_res_[2]);
-      if (mixed) check_tc_error();
+      if (mixed && *tc_word) {
+        const int err = *tc_word;
+        CK(cudaMemsetAsync(tcerr_.p, 0, sizeof(int), st_));
+        throw EngineError(2, "tensor-core GEMM reported error code " + std::to_string(err));
+      }
       if (exact) r.res_norm = rn;
       r.iterations = it - 1;
       if (o.verbose) std::printf("ccx it %3d %s |R| %.3e E %.12f\n", it, exact ? "fp64 " : "mixed", rn, e[0]);
@@ -1116,7 +1123,7 @@ class Engine final : public IEngine {
   }
   void finalize_split(SplitPlan &pl, const std::vector<TcSplitJob> &jobs) {
     upload(pl.jobs, jobs, &bytes_);
-    const std::vector<int2> ch = tc_split_chunks(jobs);
+    const std::vector<int4> ch = tc_split_chunks(jobs);
     upload(pl.chunks, ch, &bytes_);
     pl.nchunks = (int)ch.size();
   }
@@ -1130,7 +1137,7 @@ class Engine final : public IEngine {
   }
   void run_split(const SplitPlan &pl) {
     if (!pl.nchunks) return;
-    launch_tc_split(tc_kind_, (const TcSplitJob *)pl.jobs.p, (const int2 *)pl.chunks.p, pl.nchunks, st_);
+    launch_tc_split(tc_kind_, (const TcSplitJob *)pl.jobs.p, (const int4 *)pl.chunks.p, pl.nchunks, st_);
     ++launches_;
   }
   // ---- FP64-accurate re-base products as exact digit products (Ozaki scheme) ----
@@ -1144,14 +1151,15 @@ class Engine final : public IEngine {
   };
   void finalize_oz_split(OzSplitPlan &pl, const std::vector<OzSplitJob> &jobs) {
     upload(pl.jobs, jobs, &bytes_);
-    const std::vector<int2> rows = oz_row_table(jobs), ch = oz_split_chunks(jobs);
+    const std::vector<int2> rows = oz_row_table(jobs);
+    const std::vector<int4> ch = oz_split_chunks(jobs);
     upload(pl.rows, rows, &bytes_);
     upload(pl.chunks, ch, &bytes_);
     pl.nrows = (int)rows.size();
     pl.nchunks = (int)ch.size();
   }
   void run_oz_split(const OzSplitPlan &pl) {
-    launch_oz_split((const OzSplitJob *)pl.jobs.p, (const int2 *)pl.rows.p, pl.nrows, (const int2 *)pl.chunks.p,
+    launch_oz_split((const OzSplitJob *)pl.jobs.p, (const int2 *)pl.rows.p, pl.nrows, (const int4 *)pl.chunks.p,
                     pl.nchunks, st_);
     launches_ += 2;
   }
@@ -1182,6 +1190,8 @@ class Engine final : public IEngine {
     ozVppE_.alloc((size_t)std::max<int64_t>(ra, 1) * 4, &bytes_);
     ozTb_.alloc((size_t)std::max<int64_t>(pb, 8) * kOzSlices * 2, &bytes_);
     ozTbE_.alloc((size_t)std::max<int64_t>(rb, 1) * 4, &bytes_);
+    CK(cudaMemset(ozVpp_.p, 0, ozVpp_.bytes));
+    CK(cudaMemset(ozTb_.p, 0, ozTb_.bytes));
     if (!tcerr_.p) {
       tcerr_.alloc(sizeof(int), &bytes_);
       CK(cudaMemset(tcerr_.p, 0, sizeof(int)));
@@ -1222,21 +1232,100 @@ class Engine final : public IEngine {
     upload(ozPP_.probs, probs, &bytes_);
     upload(ozPP_.tiles, tiles, &bytes_);
     ozPP_.ntiles = (int)tiles.size();
+    prepare_oz_ring();
     run_oz_split(ozsVpp_);
+    run_oz_split(ozsVph_);
     CK(cudaStreamSynchronize(st_));
     oz_ready_ = true;
     oz_v_version_ = v_version_;
   }
 
-  void check_tc_error() {
-    int err = 0;
-    CK(cudaMemcpyAsync(&host_flag_, tcerr_.p, sizeof(int), cudaMemcpyDeviceToHost, st_));
-    CK(cudaStreamSynchronize(st_));
-    err = host_flag_;
-    if (err) {
-      CK(cudaMemsetAsync(tcerr_.p, 0, sizeof(int), st_));
-      throw EngineError(2, "tensor-core GEMM reported error code " + std::to_string(err));
+  // ring channels: I4 = W + 1/2 V_ph T_ph (A = V_ph, static; B = T_ph) and
+  // R_ph = T_ph I4 (A = T_ph, B = I4), all n_hp, n_ph <= 256
+  void prepare_oz_ring() {
+    const Layout &L = *L_;
+    const int nq = L.ph[1].count();
+    auto mpad = [](int x) { return (x + 127) / 128 * 128; };
+    auto npadf = [](int x) { return (x + 15) / 16 * 16; };
+    auto nkf = [](int x) { return (x + 63) / 64; };
+    int64_t pv = 0, pt = 0, pa = 0, pi = 0, rv = 0, rt = 0, ra = 0, ri = 0;
+    for (int q = 0; q < nq; ++q) {
+      const int nph = L.ph[1].side1[q].size(), nhp = L.ph[1].side2[q].size();
+      if (nph <= 0 || nhp <= 0) continue;
+      if (nhp > 256) throw EngineError(1, "digit-product re-base: a ring channel has more than 256 hole-particle pairs");
+      pv += (int64_t)mpad(nhp) * nkf(nph) * 64;   // A = V_ph (n_hp x n_ph)
+      pt += (int64_t)npadf(nhp) * nkf(nph) * 64;  // B = T_ph (K n_ph, N n_hp)
+      pa += (int64_t)mpad(nph) * nkf(nhp) * 64;   // A = T_ph (n_ph x n_hp)
+      pi += (int64_t)npadf(nhp) * nkf(nhp) * 64;  // B = I4 (K n_hp, N n_hp)
+      rv += nhp; rt += npadf(nhp); ra += nph; ri += npadf(nhp);
     }
+    auto planes = [&](DBuf &b, DBuf &e, int64_t el, int64_t rows) {
+      b.alloc((size_t)std::max<int64_t>(el, 8) * kOzSlices * 2, &bytes_);
+      e.alloc((size_t)std::max<int64_t>(rows, 1) * 4, &bytes_);
+      CK(cudaMemset(b.p, 0, b.bytes));
+    };
+    planes(ozVph_, ozVphE_, pv, rv);
+    planes(ozTphB_, ozTphBE_, pt, rt);
+    planes(ozTphA_, ozTphAE_, pa, ra);
+    planes(ozI4B_, ozI4BE_, pi, ri);
+    auto job = [](const S *src, int64_t sr, int64_t sk, int rows, int cols, int tile_rows, int rows_pad,
+                  uint16_t *pl, int64_t plane, int *ex) {
+      OzSplitJob j{};
+      j.src = (const double *)src; j.sr = sr; j.sk = sk; j.rows = rows; j.cols = cols; j.tile_rows = tile_rows;
+      j.nk = (cols + 63) / 64; j.rows_pad = rows_pad; j.planes = pl; j.plane_elems = plane; j.exps = ex;
+      return j;
+    };
+    std::vector<OzSplitJob> jv, jt, ji;
+    std::vector<OzProb> p4, pr;
+    std::vector<OzTile> t4, tr;
+    int64_t qv = 0, qt = 0, qa = 0, qi = 0, xv = 0, xt = 0, xa = 0, xi = 0, toff = 0, ioff = 0;
+    for (int q = 0; q < nq; ++q) {
+      const int nph = L.ph[1].side1[q].size(), nhp = L.ph[1].side2[q].size();
+      if (nph > 0 && nhp > 0) {
+        const OzSplitJob a4 = job(Vph_.as<S>() + toff, 1, nhp, nhp, nph, 128, mpad(nhp), ozVph_.as<uint16_t>() + qv, pv,
+                                  ozVphE_.as<int>() + xv);
+        const OzSplitJob b4 = job(Tph_.as<S>() + toff, nph, 1, nhp, nph, npadf(nhp), npadf(nhp),
+                                  ozTphB_.as<uint16_t>() + qt, pt, ozTphBE_.as<int>() + xt);
+        const OzSplitJob ar = job(Tph_.as<S>() + toff, 1, nph, nph, nhp, 128, mpad(nph), ozTphA_.as<uint16_t>() + qa, pa,
+                                  ozTphAE_.as<int>() + xa);
+        const OzSplitJob br = job(I4_.as<S>() + ioff, nhp, 1, nhp, nhp, npadf(nhp), npadf(nhp),
+                                  ozI4B_.as<uint16_t>() + qi, pi, ozI4BE_.as<int>() + xi);
+        jv.push_back(a4);
+        jt.push_back(b4);
+        jt.push_back(ar);
+        ji.push_back(br);
+        OzProb x{};
+        x.A = a4.planes; x.eA = a4.exps; x.B = b4.planes; x.eB = b4.exps; x.a_plane = pv; x.b_plane = pt;
+        x.M = nhp; x.N = nhp; x.nk = nkf(nph); x.npad = npadf(nhp);
+        x.C = (double *)(I4_.as<S>() + ioff); x.sCm = 1; x.sCn = nhp; x.alpha = 0.5;
+        for (int n0 = 0; n0 < x.npad; n0 += kOzN) t4.push_back(OzTile{(int)p4.size(), 0, n0});
+        if (mpad(nhp) > 128) for (int n0 = 0; n0 < x.npad; n0 += kOzN) t4.push_back(OzTile{(int)p4.size(), 1, n0});
+        p4.push_back(x);
+        OzProb y{};
+        y.A = ar.planes; y.eA = ar.exps; y.B = br.planes; y.eB = br.exps; y.a_plane = pa; y.b_plane = pi;
+        y.M = nph; y.N = nhp; y.nk = nkf(nhp); y.npad = npadf(nhp);
+        y.C = (double *)(Rph_.as<S>() + toff); y.sCm = 1; y.sCn = nph; y.alpha = 1.0;
+        for (int mt = 0; mt < mpad(nph) / 128; ++mt)
+          for (int n0 = 0; n0 < y.npad; n0 += kOzN) tr.push_back(OzTile{(int)pr.size(), mt, n0});
+        pr.push_back(y);
+        qv += (int64_t)mpad(nhp) * nkf(nph) * 64;
+        qt += (int64_t)npadf(nhp) * nkf(nph) * 64;
+        qa += (int64_t)mpad(nph) * nkf(nhp) * 64;
+        qi += (int64_t)npadf(nhp) * nkf(nhp) * 64;
+        xv += nhp; xt += npadf(nhp); xa += nph; xi += npadf(nhp);
+      }
+      toff += (int64_t)nph * nhp;
+      ioff += (int64_t)nhp * nhp;
+    }
+    finalize_oz_split(ozsVph_, jv);
+    finalize_oz_split(ozsTph_, jt);
+    finalize_oz_split(ozsI4_, ji);
+    upload(ozI4_.probs, p4, &bytes_);
+    upload(ozI4_.tiles, t4, &bytes_);
+    ozI4_.ntiles = (int)t4.size();
+    upload(ozRing_.probs, pr, &bytes_);
+    upload(ozRing_.tiles, tr, &bytes_);
+    ozRing_.ntiles = (int)tr.size();
   }
 
   // Tile buffers, split jobs and tensor-core problem lists of the mixed residual.
@@ -1272,9 +1361,11 @@ class Engine final : public IEngine {
       tdI4B_.n += (int64_t)npadf(nhp) * nkf(nhp) * tk;
       tI4B_.n += (int64_t)npadf(nhp) * nkf(nhp) * tk;
     }
-    for (TileBuf *b : bufs) {
+    for (TileBuf *b : bufs) {  // zeroed once: the splits never write all-padding row groups
       b->hi.alloc((size_t)std::max<int64_t>(b->n, 16) * es, &bytes_);
       b->lo.alloc((size_t)std::max<int64_t>(b->n, 16) * es, &bytes_);
+      CK(cudaMemset(b->hi.p, 0, b->hi.bytes));
+      CK(cudaMemset(b->lo.p, 0, b->lo.bytes));
     }
     const size_t sz = sizeof(S);
     Tb_.alloc(std::max<int64_t>(n_t_, 1) * sz, &bytes_);
@@ -1428,13 +1519,31 @@ class Engine final : public IEngine {
     launch_i6<S>(D_, (const int2 *)i6rows_.p, ni6rows_, i6dots_.as<S>(), T_.as<S>(), Vhp_.as<S>(), fdiag_.as<S>(),
                  f6_.as<S>(), d2ab_.as<S>(), i6off_.as<S>(), st_);
     mark(3);
-    kbegin(kKI4);
-    run_plan(planI4_);
-    kend();
-    mark(4);
-    kbegin(kKRing);
-    run_plan(planRing_);
-    kend();
+    if (digits) {  // I4 = W + 1/2 V_ph T_ph and R_ph = T_ph I4 as digit products
+      kbegin(kKSplit);
+      run_oz_split(ozsTph_);
+      kend();
+      CK(cudaMemcpyAsync(I4_.p, W_.p, std::max<int64_t>(n_i4_, 1) * sizeof(S), cudaMemcpyDeviceToDevice, st_));
+      kbegin(kKI4Oz);
+      run_oz(ozI4_);
+      kend();
+      kbegin(kKSplit);
+      run_oz_split(ozsI4_);
+      kend();
+      mark(4);
+      CK(cudaMemsetAsync(Rph_.p, 0, std::max<int64_t>(n_ph_, 1) * sizeof(S), st_));
+      kbegin(kKRingOz);
+      run_oz(ozRing_);
+      kend();
+    } else {
+      kbegin(kKI4);
+      run_plan(planI4_);
+      kend();
+      mark(4);
+      kbegin(kKRing);
+      run_plan(planRing_);
+      kend();
+    }
     mark(5);
     launch_rinit<S>(D_, T_.as<S>(), Vhp_.as<S>(), Rph_.as<S>(), i6off_.as<S>(), i7off_.as<S>(), R_.as<S>(), st_);
     mark(6);
@@ -1552,8 +1661,9 @@ class Engine final : public IEngine {
   int64_t v_version_ = 0, mixed_v_version_ = -1;
   DBuf Tb_, PPb_, Tphb_, Rphb_, I4b_, dI4_, tcerr_;
   DBuf ozVpp_, ozVppE_, ozTb_, ozTbE_;
-  OzSplitPlan ozsVpp_, ozsTb_;
-  OzPlan ozPP_;
+  DBuf ozVph_, ozVphE_, ozTphB_, ozTphBE_, ozTphA_, ozTphAE_, ozI4B_, ozI4BE_;
+  OzSplitPlan ozsVpp_, ozsTb_, ozsVph_, ozsTph_, ozsI4_;
+  OzPlan ozPP_, ozI4_, ozRing_;
   bool oz_ready_ = false;
   int64_t oz_v_version_ = -1;
   TileBuf tVpp_, tD_, tVph_, tDphB_, tTphbA_, tDphA_, tdI4B_, tI4B_;

@@ -50,7 +50,9 @@ enum KernelSlot {
   kKTcRing = 8, // k_tc_gemm: ring corrections (two launches per residual)
   kKSplit = 9,  // k_tc_split: per-iteration operand splits
   kKPPOz = 10,  // k_oz_gemm: V_pppp' T' at a re-base as exact digit products
-  kKernelSlots = 12
+  kKI4Oz = 11,  // k_oz_gemm: I4 at a re-base as exact digit products
+  kKRingOz = 12,  // k_oz_gemm: ring at a re-base as exact digit products
+  kKernelSlots = 16
 };
 
 class IEngine {

@@ -261,12 +261,11 @@ __device__ __forceinline__ void oz_digits(double x, int e, uint32_t (&d)[kOzSlic
   }
 }
 
-__global__ void __launch_bounds__(256) k_oz_digits(const OzSplitJob *__restrict__ jobs, const int2 *__restrict__ chunks) {
-  const int2 ck = chunks[blockIdx.x];
+__global__ void __launch_bounds__(256) k_oz_digits(const OzSplitJob *__restrict__ jobs, const int4 *__restrict__ chunks) {
+  const int4 ck = chunks[blockIdx.x];
   const OzSplitJob J = jobs[ck.x];
   const int tile_units = J.tile_rows * 8;
-  const int total = (J.rows_pad / J.tile_rows) * J.nk * tile_units;
-  const int end = min(total, ck.y + kSplitChunk);
+  const int end = ck.z;
   uint4 *planes = (uint4 *)J.planes;
   const int64_t pstride = J.plane_elems / 8;  // uint4 units between planes
   for (int u = ck.y + threadIdx.x; u < end; u += blockDim.x) {
@@ -305,13 +304,10 @@ void launch_oz_gemm(const OzProb *probs, const OzTile *tiles, int ntiles, int *e
   k_oz_gemm<<<ntiles, kOzThreads, kOzSmem, st>>>(probs, tiles, err);
 }
 
-std::vector<int2> oz_split_chunks(const std::vector<OzSplitJob> &jobs) {
-  std::vector<int2> out;
-  for (size_t j = 0; j < jobs.size(); ++j) {
-    const OzSplitJob &J = jobs[j];
-    const int64_t units = (int64_t)(J.rows_pad / J.tile_rows) * J.nk * J.tile_rows * 8;
-    for (int64_t u = 0; u < units; u += kSplitChunk) out.push_back(make_int2((int)j, (int)u));
-  }
+std::vector<int4> oz_split_chunks(const std::vector<OzSplitJob> &jobs) {
+  std::vector<int4> out;
+  for (size_t j = 0; j < jobs.size(); ++j)
+    split_ranges((int)j, jobs[j].rows, jobs[j].rows_pad, jobs[j].tile_rows, jobs[j].nk, out);
   return out;
 }
 
@@ -322,7 +318,7 @@ std::vector<int2> oz_row_table(const std::vector<OzSplitJob> &jobs) {
   return out;
 }
 
-void launch_oz_split(const OzSplitJob *jobs, const int2 *rowtab, int nrows, const int2 *chunks, int nchunks,
+void launch_oz_split(const OzSplitJob *jobs, const int2 *rowtab, int nrows, const int4 *chunks, int nchunks,
                      cudaStream_t st) {
   if (nrows > 0) k_oz_exps<<<(nrows * 32 + 255) / 256, 256, 0, st>>>(jobs, rowtab, nrows);
   if (nchunks > 0) k_oz_digits<<<nchunks, 256, 0, st>>>(jobs, chunks);

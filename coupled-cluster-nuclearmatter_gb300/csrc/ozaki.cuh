@@ -56,9 +56,10 @@ struct OzSplitJob {
   int64_t plane_elems;
   int *exps;           // rows exponents (written by the exponent pass, read by the digit pass)
 };
-std::vector<int2> oz_split_chunks(const std::vector<OzSplitJob> &jobs);
-// exps: one warp per row; rowtab: (job, row) pairs
-void launch_oz_split(const OzSplitJob *jobs, const int2 *rowtab, int nrows, const int2 *chunks, int nchunks,
+std::vector<int4> oz_split_chunks(const std::vector<OzSplitJob> &jobs);
+// exps: one warp per row; rowtab: (job, row) pairs; chunks as the split kernel's (the
+// digit planes are zeroed once when allocated)
+void launch_oz_split(const OzSplitJob *jobs, const int2 *rowtab, int nrows, const int4 *chunks, int nchunks,
                      cudaStream_t st);
 std::vector<int2> oz_row_table(const std::vector<OzSplitJob> &jobs);
 

@@ -22,7 +22,8 @@ void sck(cudaError_t e, const char *w) {
 }
 struct Dev {
   void *p = nullptr;
-  explicit Dev(size_t b) { sck(cudaMalloc(&p, std::max<size_t>(b, 16)), "cudaMalloc"); }
+  size_t bytes = 0;
+  explicit Dev(size_t b) : bytes(std::max<size_t>(b, 16)) { sck(cudaMalloc(&p, bytes), "cudaMalloc"); }
   ~Dev() { cudaFree(p); }
 };
 }  // namespace
@@ -88,16 +89,19 @@ static void oz_selftest(int nprob, const int *Ms, const int *Ns, const int *Ks, 
     qa += (size_t)x.mpad * x.nk * 64; qb += (size_t)x.npad * x.nk * 64;
     xa += x.M; xb += x.npad;
   }
-  const std::vector<int2> rows = oz_row_table(jobs), chunks = oz_split_chunks(jobs);
-  Dev dJ(jobs.size() * sizeof(OzSplitJob)), dR(rows.size() * sizeof(int2)), dK(chunks.size() * sizeof(int2));
+  const std::vector<int2> rows = oz_row_table(jobs);
+  const std::vector<int4> chunks = oz_split_chunks(jobs);
+  Dev dJ(jobs.size() * sizeof(OzSplitJob)), dR(rows.size() * sizeof(int2)), dK(chunks.size() * sizeof(int4));
   Dev dP(probs.size() * sizeof(OzProb)), dT(tiles.size() * sizeof(OzTile));
   sck(cudaMemcpy(dJ.p, jobs.data(), jobs.size() * sizeof(OzSplitJob), cudaMemcpyHostToDevice), "copy jobs");
   sck(cudaMemcpy(dR.p, rows.data(), rows.size() * sizeof(int2), cudaMemcpyHostToDevice), "copy rows");
-  sck(cudaMemcpy(dK.p, chunks.data(), chunks.size() * sizeof(int2), cudaMemcpyHostToDevice), "copy chunks");
+  sck(cudaMemcpy(dK.p, chunks.data(), chunks.size() * sizeof(int4), cudaMemcpyHostToDevice), "copy chunks");
   sck(cudaMemcpy(dP.p, probs.data(), probs.size() * sizeof(OzProb), cudaMemcpyHostToDevice), "copy probs");
+  sck(cudaMemset(plA.p, 0, pa * kOzSlices * 2), "memset planes");
+  sck(cudaMemset(plB.p, 0, pb * kOzSlices * 2), "memset planes");
   sck(cudaMemcpy(dT.p, tiles.data(), tiles.size() * sizeof(OzTile), cudaMemcpyHostToDevice), "copy tiles");
   sck(cudaMemset(dE.p, 0, 4), "memset");
-  launch_oz_split((const OzSplitJob *)dJ.p, (const int2 *)dR.p, (int)rows.size(), (const int2 *)dK.p,
+  launch_oz_split((const OzSplitJob *)dJ.p, (const int2 *)dR.p, (int)rows.size(), (const int4 *)dK.p,
                   (int)chunks.size(), 0);
   sck(cudaGetLastError(), "oz split launch");
   cudaEvent_t e0, e1;
@@ -217,10 +221,11 @@ void tc_selftest(int device, int kind, int nprob, const int *Ms, const int *Ns, 
   sck(cudaMemcpy(dP.p, probs.data(), probs.size() * sizeof(TcProb), cudaMemcpyHostToDevice), "copy probs");
   sck(cudaMemcpy(dT.p, tiles.data(), tiles.size() * sizeof(TcTile), cudaMemcpyHostToDevice), "copy tiles");
   sck(cudaMemset(dE.p, 0, 4), "memset");
-  const std::vector<int2> chunks = tc_split_chunks(jobs);
-  Dev dK(chunks.size() * sizeof(int2));
-  sck(cudaMemcpy(dK.p, chunks.data(), chunks.size() * sizeof(int2), cudaMemcpyHostToDevice), "copy chunks");
-  launch_tc_split(kind, (const TcSplitJob *)dJ.p, (const int2 *)dK.p, (int)chunks.size(), 0);
+  const std::vector<int4> chunks = tc_split_chunks(jobs);
+  Dev dK(chunks.size() * sizeof(int4));
+  sck(cudaMemcpy(dK.p, chunks.data(), chunks.size() * sizeof(int4), cudaMemcpyHostToDevice), "copy chunks");
+  for (Dev *b : {&tAh, &tAl, &tBh, &tBl}) sck(cudaMemset(b->p, 0, b->bytes), "memset tiles");
+  launch_tc_split(kind, (const TcSplitJob *)dJ.p, (const int4 *)dK.p, (int)chunks.size(), 0);
   sck(cudaGetLastError(), "split launch");
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);

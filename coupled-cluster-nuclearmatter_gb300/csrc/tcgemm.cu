@@ -245,15 +245,14 @@ template <> __device__ inline void split_unit<kTcTF32, 4>(const double (&x)[4], 
 // (row group, K chunk, row in group), so a warp reads 8 rows x 4 consecutive K chunks
 // and writes 512 contiguous bytes.  Blocks cover kSplitChunk units of one job.
 template <int KIND>
-__global__ void __launch_bounds__(256) k_tc_split(const TcSplitJob *__restrict__ jobs, const int2 *__restrict__ chunks) {
+__global__ void __launch_bounds__(256) k_tc_split(const TcSplitJob *__restrict__ jobs, const int4 *__restrict__ chunks) {
   using H = Half<KIND>;
   constexpr int cme = H::per16;  // elements per unit
   constexpr int tk = 8 * cme;    // elements per 128-byte tile row
-  const int2 ck = chunks[blockIdx.x];
+  const int4 ck = chunks[blockIdx.x];
   const TcSplitJob J = jobs[ck.x];
   const int tile_units = J.tile_rows * 8;
-  const int total = (J.rows_pad / J.tile_rows) * J.nk * tile_units;
-  const int end = min(total, ck.y + kSplitChunk);
+  const int end = ck.z;
   const bool scaled = J.scale != 1.0;
   uint4 *hi = (uint4 *)J.hi, *lo = (uint4 *)J.lo;
   for (int u = ck.y + threadIdx.x; u < end; u += blockDim.x) {
@@ -309,17 +308,28 @@ void launch_tc_gemm(int kind, const TcProb *probs, const TcTile *tiles, int ntil
   }
 }
 
-std::vector<int2> tc_split_chunks(const std::vector<TcSplitJob> &jobs) {
-  std::vector<int2> out;
-  for (size_t j = 0; j < jobs.size(); ++j) {
-    const TcSplitJob &J = jobs[j];
-    const int64_t units = (int64_t)(J.rows_pad / J.tile_rows) * J.nk * J.tile_rows * 8;
-    for (int64_t u = 0; u < units; u += kSplitChunk) out.push_back(make_int2((int)j, (int)u));
+void split_ranges(int job, int rows, int rows_pad, int tile_rows, int nk, std::vector<int4> &out) {
+  const int tile_units = tile_rows * 8;
+  for (int rt = 0; rt < rows_pad / tile_rows; ++rt) {
+    const int live_rows = std::min(tile_rows, rows - rt * tile_rows);
+    if (live_rows <= 0) continue;
+    const int live_units = (live_rows + 7) / 8 * 64;
+    for (int kt = 0; kt < nk; ++kt) {
+      const int base = (rt * nk + kt) * tile_units;
+      for (int u = 0; u < live_units; u += kSplitChunk)
+        out.push_back(make_int4(job, base + u, base + std::min(live_units, u + kSplitChunk), 0));
+    }
   }
+}
+
+std::vector<int4> tc_split_chunks(const std::vector<TcSplitJob> &jobs) {
+  std::vector<int4> out;
+  for (size_t j = 0; j < jobs.size(); ++j)
+    split_ranges((int)j, jobs[j].rows, jobs[j].rows_pad, jobs[j].tile_rows, jobs[j].nk, out);
   return out;
 }
 
-void launch_tc_split(int kind, const TcSplitJob *jobs, const int2 *chunks, int nchunks, cudaStream_t st) {
+void launch_tc_split(int kind, const TcSplitJob *jobs, const int4 *chunks, int nchunks, cudaStream_t st) {
   if (nchunks <= 0) return;
   if (kind == kTcBF16) k_tc_split<kTcBF16><<<nchunks, 256, 0, st>>>(jobs, chunks);
   else k_tc_split<kTcTF32><<<nchunks, 256, 0, st>>>(jobs, chunks);

@@ -49,9 +49,13 @@ struct TcSplitJob {
   void *hi, *lo;
   double scale;
 };
-// Work list of the split kernel: (job, first 16-byte unit) per block of kSplitChunk units.
+// Work list of the split kernels: (job, first unit, end unit) per block, at most
+// kSplitChunk 16-byte units, covering only the row groups of each tile that hold rows of
+// the matrix.  Units of all-padding row groups are never written: the tile buffers are
+// zeroed once when they are allocated.
 constexpr int kSplitChunk = 1024;
-std::vector<int2> tc_split_chunks(const std::vector<TcSplitJob> &jobs);
-void launch_tc_split(int kind, const TcSplitJob *jobs, const int2 *chunks, int nchunks, cudaStream_t st);
+void split_ranges(int job, int rows, int rows_pad, int tile_rows, int nk, std::vector<int4> &out);
+std::vector<int4> tc_split_chunks(const std::vector<TcSplitJob> &jobs);
+void launch_tc_split(int kind, const TcSplitJob *jobs, const int4 *chunks, int nchunks, cudaStream_t st);
 
 }  // namespace ccx

@@ -254,8 +254,8 @@ typedef struct {
   int32_t rebase;            /* mixed precision: CCX_REBASE_* */
 } ccx_iter_opts;
 #define CCX_REBASE_FP64 0      /* products of a re-base on the FP64 FMA pipe */
-#define CCX_REBASE_DIGITS 1    /* the pp-ladder product of a re-base as exact 6-bit digit products on the
-                                  BF16 tensor cores (Ozaki scheme), FP64-accurate */
+#define CCX_REBASE_DIGITS 1    /* the pp-ladder, I4 and ring products of a re-base as exact 6-bit digit
+                                  products on the BF16 tensor cores (Ozaki scheme), FP64-accurate */
 
 typedef struct {
   int32_t iterations;
@@ -303,8 +303,9 @@ int ccx_engine_timers(const ccx_engine *e, double ms[10]);
  * [3] fused pp+hh ladder (FP64), [4] V_pppp' T' at a mixed-precision re-base (FP64),
  * [5] hh-ladder of the mixed residual (FP64), [6] pp-ladder correction (tensor cores),
  * [7] dI4 correction (tensor cores), [8] ring corrections (tensor cores),
- * [9] operand splits, [10] pp-ladder at a re-base as digit products (tensor cores), [11] unused */
-int ccx_engine_kernel_timers(const ccx_engine *e, double ms[12], int64_t launches[12]);
+ * [9] operand splits, [10] pp-ladder, [11] I4 and [12] ring at a re-base as digit products
+ * (tensor cores), [13..15] unused */
+int ccx_engine_kernel_timers(const ccx_engine *e, double ms[16], int64_t launches[16]);
 
 #ifdef __cplusplus
 }
