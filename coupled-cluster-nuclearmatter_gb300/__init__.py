@@ -132,6 +132,17 @@ def lib():
         "ccx_selftest_tc_gemm": ([i32, i32, i32, vp, vp, vp, i32, C.c_uint64, C.POINTER(dbl), C.POINTER(dbl)], C.c_int),
         "ccx_ccd_energy_noalloc": ([i32, vp, vp, vp, vp, vp], C.c_int),
         "ccx_engine_kernel_timers": ([vp, vp, vp], C.c_int),
+        "ccx_learner_create": ([i32, C.c_uint64, C.POINTER(vp)], C.c_int),
+        "ccx_learner_destroy": ([vp], C.c_int),
+        "ccx_learner_add_solution": ([vp, vp], C.c_int),
+        "ccx_learner_clear": ([vp], C.c_int),
+        "ccx_learner_samples": ([vp, vp], C.c_int),
+        "ccx_learner_train": ([vp, i32, i32, C.c_double, C.c_uint64, C.POINTER(C.c_double)], C.c_int),
+        "ccx_init_learned": ([vp, vp], C.c_int),
+        "ccx_learner_get_params": ([vp, vp], C.c_int),
+        "ccx_learner_set_params": ([vp, vp], C.c_int),
+        "ccx_learner_loss_grad": ([vp, vp, vp, i32, C.POINTER(C.c_double), vp], C.c_int),
+        "ccx_learner_infer": ([vp, vp, i32, vp, i32], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -179,6 +190,72 @@ def ccd_energy_noalloc(nch: int, dims_ptr: int, t2_ptr: int, vhhpp_ptr: int, ene
     """ccx_ccd_energy_noalloc on caller-owned device buffers (raw device pointers)."""
     _check(lib().ccx_ccd_energy_noalloc(nch, vp(dims_ptr), vp(t2_ptr), vp(vhhpp_ptr), vp(energy_ptr),
                                         vp(stream) if stream else None))
+
+
+ML_FEATURES, ML_PARAMS = 16, 35329
+
+
+class Learner:
+    """Learned warm start: MLP predicting converged-minus-MP2 T2 amplitudes."""
+
+    def __init__(self, device: int = 0, seed: int = 20261203):
+        h = vp()
+        _check(lib().ccx_learner_create(device, seed, C.byref(h)))
+        self._h = h
+
+    def close(self):
+        if self._h:
+            lib().ccx_learner_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add_solution(self, engine: "Engine"):
+        _check(lib().ccx_learner_add_solution(self._h, engine._h))
+
+    def clear(self):
+        _check(lib().ccx_learner_clear(self._h))
+
+    def samples(self) -> int:
+        n = C.c_int64()
+        _check(lib().ccx_learner_samples(self._h, C.byref(n)))
+        return n.value
+
+    def train(self, steps: int = 2000, batch: int = 8192, lr: float = 1e-3, seed: int = 1) -> float:
+        loss = C.c_double()
+        _check(lib().ccx_learner_train(self._h, steps, batch, lr, seed, C.byref(loss)))
+        return loss.value
+
+    def warm_start(self, engine: "Engine"):
+        _check(lib().ccx_init_learned(engine._h, self._h))
+
+    def params(self) -> np.ndarray:
+        p = np.zeros(ML_PARAMS, np.float32)
+        _check(lib().ccx_learner_get_params(self._h, _ptr(p)))
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, np.float32)
+        assert p.size == ML_PARAMS
+        _check(lib().ccx_learner_set_params(self._h, _ptr(p)))
+
+    def loss_grad(self, X, y):
+        X = np.ascontiguousarray(X, np.float32)
+        y = np.ascontiguousarray(y, np.float32)
+        loss = C.c_double()
+        g = np.zeros(ML_PARAMS, np.float32)
+        _check(lib().ccx_learner_loss_grad(self._h, _ptr(X), _ptr(y), len(y), C.byref(loss), _ptr(g)))
+        return loss.value, g
+
+    def infer(self, X, tensor_cores: bool = True) -> np.ndarray:
+        X = np.ascontiguousarray(X, np.float32)
+        out = np.zeros(len(X), np.float32)
+        _check(lib().ccx_learner_infer(self._h, _ptr(X), len(X), _ptr(out), int(tensor_cores)))
+        return out
 
 
 def deck_parse(text: str) -> dict:

@@ -20,6 +20,9 @@ struct ccx_engine {
   std::shared_ptr<const ccx::Layout> L;
   std::unique_ptr<ccx::IEngine> E;
 };
+struct ccx_learner {
+  std::unique_ptr<ccx::ILearner> M;
+};
 
 namespace {
 
@@ -352,6 +355,72 @@ int ccx_engine_launches(const ccx_engine *e, int64_t *n) {
 int ccx_engine_timers(const ccx_engine *e, double ms[10]) {
   if (!ms) return fail(CCX_EINVAL, "null argument");
   ENGINE_CALL(e, e->E->timers(ms));
+}
+int ccx_learner_create(int32_t device, uint64_t seed, ccx_learner **out) {
+  if (!out) return fail(CCX_EINVAL, "null argument");
+  *out = nullptr;
+  return guard([&] {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n <= 0) throw ccx::EngineError(CCX_ENOGPU, "no CUDA device");
+    auto *l = new ccx_learner;
+    try {
+      l->M = ccx::make_learner(device, seed);
+    } catch (...) {
+      delete l;
+      throw;
+    }
+    *out = l;
+  });
+}
+int ccx_learner_destroy(ccx_learner *l) {
+  delete l;
+  return CCX_OK;
+}
+#define LEARNER_CALL(l, body)                                  \
+  if (!(l)) return fail(CCX_EINVAL, "null learner");           \
+  return guard([&] { body; })
+static ccx::MLView ml_view_of(ccx_engine *e, bool need_t) {
+  ccx::MLView v;
+  if (!e->E->ml_view(v, need_t)) throw ccx::EngineError(CCX_EINVAL, "the learned warm start needs a real engine");
+  return v;
+}
+int ccx_learner_add_solution(ccx_learner *l, ccx_engine *e) {
+  if (!e) return fail(CCX_EINVAL, "null engine");
+  LEARNER_CALL(l, l->M->add_solution(ml_view_of(e, true)));
+}
+int ccx_learner_clear(ccx_learner *l) { LEARNER_CALL(l, l->M->clear()); }
+int ccx_learner_samples(const ccx_learner *l, int64_t *n) {
+  if (!n) return fail(CCX_EINVAL, "null argument");
+  LEARNER_CALL(l, *n = l->M->samples());
+}
+int ccx_learner_train(ccx_learner *l, int32_t steps, int32_t batch, double lr, uint64_t seed, double *loss) {
+  LEARNER_CALL(l, {
+    const double v = l->M->train(steps, batch, lr, seed);
+    if (loss) *loss = v;
+  });
+}
+int ccx_init_learned(ccx_engine *e, ccx_learner *l) {
+  if (!e) return fail(CCX_EINVAL, "null engine");
+  LEARNER_CALL(l, {
+    l->M->warm_start(ml_view_of(e, false));
+    e->E->mark_t_set();
+  });
+}
+int ccx_learner_get_params(const ccx_learner *l, float *p) {
+  if (!p) return fail(CCX_EINVAL, "null argument");
+  LEARNER_CALL(l, l->M->get_params(p));
+}
+int ccx_learner_set_params(ccx_learner *l, const float *p) {
+  if (!p) return fail(CCX_EINVAL, "null argument");
+  LEARNER_CALL(l, l->M->set_params(p));
+}
+int ccx_learner_loss_grad(ccx_learner *l, const float *X, const float *y, int32_t n, double *loss, float *grad) {
+  if (!X || !y || !loss || !grad || n <= 0) return fail(CCX_EINVAL, "bad arguments");
+  LEARNER_CALL(l, l->M->loss_grad(X, y, n, loss, grad));
+}
+int ccx_learner_infer(ccx_learner *l, const float *X, int32_t n, float *out, int32_t tensor_cores) {
+  if (!X || !out || n <= 0) return fail(CCX_EINVAL, "bad arguments");
+  LEARNER_CALL(l, l->M->infer(X, n, out, tensor_cores));
 }
 int ccx_engine_kernel_timers(const ccx_engine *e, double ms[16], int64_t launches[16]) {
   if (!ms || !launches) return fail(CCX_EINVAL, "null argument");

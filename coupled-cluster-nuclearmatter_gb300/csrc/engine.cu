@@ -8,6 +8,7 @@
 #include <complex>
 #include <cstdio>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "common.cuh"
@@ -488,6 +489,37 @@ class Engine final : public IEngine {
       throw EngineError(1, msg);
     }
   }
+  bool ml_view(MLView &v, bool need_t) override {
+    if constexpr (!std::is_same<S, double>::value) {
+      return false;
+    } else {
+      if (!have_fock_) throw EngineError(4, "no Fock matrix / interaction set");
+      if (need_t && !have_t_) throw EngineError(4, "no T2 amplitudes");
+      commit();
+      const Basis &b = L_->b;
+      v.L = D_;
+      v.O = O_;
+      v.fdiag = fdiag_.as<double>();
+      v.Vhp = Vhp_.as<double>();
+      v.T = T_.as<double>();
+      v.n_t = n_t_;
+      v.vol = b.L * b.L * b.L;
+      v.rho = b.A / v.vol;
+      const bool snm = b.tzmin != b.tzmax;
+      const double pi = 3.14159265358979323846;
+      v.kF = std::cbrt(3.0 * pi * pi * v.rho / (snm ? 2.0 : 1.0));
+      v.eF = (197.3269788 * v.kF) * (197.3269788 * v.kF) / (2.0 * 939.565);
+      if (b.ns > 0) {
+        v.theta[0] = b.kx[0] * b.L - 2.0 * pi * b.nx[0];
+        v.theta[1] = b.ky[0] * b.L - 2.0 * pi * b.ny[0];
+        v.theta[2] = b.kz[0] * b.L - 2.0 * pi * b.nz[0];
+      }
+      v.st = st_;
+      return true;
+    }
+  }
+  void mark_t_set() override { have_t_ = true; }
+
   void require_ready() {
     if (!have_fock_) throw EngineError(4, "no Fock matrix / interaction set");
     if (!have_t_) throw EngineError(4, "no T2 amplitudes (call setup_t_amplitudes or set_t2)");

@@ -7,6 +7,7 @@
 #include <string>
 
 #include "layout.hpp"
+#include "learner.hpp"
 
 namespace ccx {
 
@@ -84,6 +85,9 @@ class IEngine {
   virtual double residual_norm() = 0;
   virtual void ccd_iter(const IterOpts &o, IterResult &r) = 0;
   virtual void triples(double et[2]) = 0;
+  // device view for the learned warm start (real engines only; false for complex)
+  virtual bool ml_view(MLView &v, bool need_t) = 0;
+  virtual void mark_t_set() = 0;
 };
 
 std::unique_ptr<IEngine> make_engine(std::shared_ptr<const Layout> L, int device, bool complex_scalars);

@@ -276,6 +276,36 @@ int ccx_ccd_iter(ccx_engine *e, const ccx_iter_opts *opt, ccx_iter_result *res);
  * the V_hppp / V_hhhp blocks of setup_vnn_hppp_block (ccm_iter.f90:1361-1810). */
 int ccx_pert_triples(ccx_engine *e, double et[2]);
 
+/* ---- learned warm start ------------------------------------------------------
+ * No counterpart in the reference (which always starts from MP2, ccm_iter.f90:2329-2368).
+ * A 4-layer MLP (16 features -> 128 -> 128 -> 128 -> 1, SiLU) predicts per packed T2
+ * amplitude the difference between the converged CCD amplitude and its MP2 value, from
+ * features that transfer across lattices: density, twist, bare denominator / e_F, bare
+ * <ij|V|ab> and MP2 amplitude scaled by the volume, momentum transfers and pair momenta
+ * / k_F, spin and isospin products.  Training (FP32, Adam) uses amplitudes the solver
+ * converged on other lattices; inference runs in BF16 on the tensor cores.  Real
+ * engines only.  The CCD iteration from the warm start is unchanged, so the converged
+ * energy is the same as from MP2. */
+typedef struct ccx_learner ccx_learner;
+#define CCX_ML_FEATURES 16
+#define CCX_ML_PARAMS 35329    /* W1[128][16] b1 W2[128][128] b2 W3[128][128] b3 w4[128] b4, FP32 */
+int ccx_learner_create(int32_t device, uint64_t seed, ccx_learner **out);
+int ccx_learner_destroy(ccx_learner *l);
+/* training samples (features, converged - MP2) from the engine's current T2 */
+int ccx_learner_add_solution(ccx_learner *l, ccx_engine *e);
+int ccx_learner_clear(ccx_learner *l);
+int ccx_learner_samples(const ccx_learner *l, int64_t *n);
+/* Adam on shuffled minibatches; *loss = mean loss of the last 10 steps */
+int ccx_learner_train(ccx_learner *l, int32_t steps, int32_t batch, double lr, uint64_t seed, double *loss);
+/* T2 <- MP2 + predicted correction (needs the interaction; replaces ccx_setup_t_amplitudes) */
+int ccx_init_learned(ccx_engine *e, ccx_learner *l);
+int ccx_learner_get_params(const ccx_learner *l, float *params);
+int ccx_learner_set_params(ccx_learner *l, const float *params);
+/* loss and gradient on a host batch (X: n x CCX_ML_FEATURES, y: n) with the training kernels */
+int ccx_learner_loss_grad(ccx_learner *l, const float *X, const float *y, int32_t n, double *loss, float *grad);
+/* network output on host features: tensor_cores 0 = FP32 training forward, 1 = BF16 kernel */
+int ccx_learner_infer(ccx_learner *l, const float *X, int32_t n, float *out, int32_t tensor_cores);
+
 /* ---- diagnostics -------------------------------------------------------- */
 const char *ccx_last_error(void);
 /* the engine's CUDA stream (cudaStream_t), for callers that order their own work
