@@ -132,6 +132,7 @@ def lib():
         "ccx_selftest_tc_gemm": ([i32, i32, i32, vp, vp, vp, i32, C.c_uint64, C.POINTER(dbl), C.POINTER(dbl)], C.c_int),
         "ccx_ccd_energy_noalloc": ([i32, vp, vp, vp, vp, vp], C.c_int),
         "ccx_engine_kernel_timers": ([vp, vp, vp], C.c_int),
+        "ccx_set_vblocks": ([vp, i32, i32, vp, vp], C.c_int),
         "ccx_learner_create": ([i32, C.c_uint64, C.POINTER(vp)], C.c_int),
         "ccx_learner_destroy": ([vp], C.c_int),
         "ccx_learner_add_solution": ([vp, vp], C.c_int),
@@ -383,6 +384,13 @@ class Engine:
     def set_vblock(self, kind: int, ch: int, block: np.ndarray):
         b = _cplx_fortran(block)
         _check(lib().ccx_set_vblock(self._h, kind, ch, _ptr(b)))
+
+    def set_vblocks(self, kind: int, blocks: dict):
+        """Many blocks of one kind in one call: {channel: block}."""
+        bs = [_cplx_fortran(b) for b in blocks.values()]
+        chs = (C.c_int32 * len(bs))(*blocks.keys())
+        ptrs = (vp * len(bs))(*[b.ctypes.data for b in bs])
+        _check(lib().ccx_set_vblocks(self._h, kind, len(bs), chs, ptrs))
 
     def vblock(self, kind: int, ch: int) -> np.ndarray:
         """One V block in the reference's ordered layout (see ccx_get_vblock)."""

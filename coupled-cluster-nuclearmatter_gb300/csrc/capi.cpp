@@ -430,6 +430,12 @@ int ccx_set_fock(ccx_engine *e, const double *fock, const double e0[2]) {
   if (!fock) return fail(CCX_EINVAL, "null Fock matrix");
   ENGINE_CALL(e, e->E->set_fock(fock, e0));
 }
+int ccx_set_vblocks(ccx_engine *e, int32_t kind, int32_t n, const int32_t *chs, const double *const *v) {
+  if (n < 0 || (n > 0 && (!chs || !v))) return fail(CCX_EINVAL, "null block list");
+  for (int32_t i = 0; i < n; ++i)
+    if (!v[i]) return fail(CCX_EINVAL, "null V block in the list");
+  ENGINE_CALL(e, e->E->set_vblocks(kind, n, chs, v));
+}
 int ccx_set_vblock(ccx_engine *e, int32_t kind, int32_t ch, const double *v) {
   ENGINE_CALL(e, e->E->set_vblock(kind, ch, v));
 }

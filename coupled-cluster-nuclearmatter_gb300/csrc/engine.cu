@@ -31,20 +31,27 @@ void ck(cudaError_t e, const char *what) {
 // RAII device buffer
 struct DBuf {
   void *p = nullptr;
-  size_t bytes = 0;
+  size_t bytes = 0;  // requested size
+  size_t cap = 0;    // allocated size: a later request that fits reuses the allocation
   DBuf() = default;
   DBuf(const DBuf &) = delete;
   DBuf &operator=(const DBuf &) = delete;
   ~DBuf() { if (p) cudaFree(p); }
   void alloc(size_t b, int64_t *counter) {
-    if (p) { cudaFree(p); if (counter) *counter -= (int64_t)bytes; p = nullptr; }
+    if (p && b <= cap) {
+      bytes = b;
+      return;
+    }
+    if (p) { cudaFree(p); if (counter) *counter -= (int64_t)cap; p = nullptr; }
     bytes = b;
+    cap = 0;
     if (b == 0) return;
     cudaError_t e = cudaMalloc(&p, b);
     if (e != cudaSuccess) {
       p = nullptr;
       throw EngineError(3, std::string("cudaMalloc of ") + std::to_string(b) + " bytes: " + cudaGetErrorString(e));
     }
+    cap = b;
     if (counter) *counter += (int64_t)b;
   }
   template <typename T> T *as() const { return (T *)p; }
@@ -154,6 +161,8 @@ class Engine final : public IEngine {
     for (auto &e : ev_) if (e) cudaEventDestroy(e);
     for (auto &e : kev_) if (e) cudaEventDestroy(e);
     if (st_) cudaStreamDestroy(st_);
+    if (cs_) cudaStreamDestroy(cs_);
+    for (auto &e : sev_) if (e) cudaEventDestroy(e);
     if (host_res_) cudaFreeHost(host_res_);
   }
 
@@ -188,7 +197,39 @@ class Engine final : public IEngine {
     have_fock_ = true;
   }
 
+  // one block; the host buffer is read before the call returns
   void set_vblock(int kind, int ch, const double *v) override {
+    set_vblock_async(kind, ch, v, 0);
+    finish_vblocks();
+  }
+  // Many blocks of one kind with one synchronisation at the end.  Staged blocks
+  // alternate between two staging buffers: the host-to-device copies run back to back
+  // on a copy stream while the compute stream packs the previous block.
+  void set_vblocks(int kind, int n, const int *chs, const double *const *vs) override {
+    const bool staged = kind == 1 || kind == 3 || kind == 6;
+    if (staged && n > 1) {
+      if (!cs_) {
+        CK(cudaStreamCreateWithFlags(&cs_, cudaStreamNonBlocking));
+        for (auto &e : sev_) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+      }
+      if (stage2_.bytes < stage_.bytes) stage2_.alloc(stage_.bytes, &bytes_);
+      // earlier work on the compute stream may still read the staging buffers
+      CK(cudaEventRecord(sev_[4], st_));
+      CK(cudaStreamWaitEvent(cs_, sev_[4], 0));
+    }
+    for (int i = 0; i < n; ++i) set_vblock_async(kind, chs[i], vs[i], staged && n > 1 ? 1 + (i & 1) : 0, i >= 2);
+    if (staged && n > 1) CK(cudaStreamSynchronize(cs_));
+    finish_vblocks();
+  }
+  // the copies have been read once this returns; a real engine also reports here
+  // whether any block it packed had a non-zero imaginary part
+  void finish_vblocks() {
+    if (!ScalarOf<S>::complex) check_flag("V block has a non-zero imaginary part but the engine is real");
+    else CK(cudaStreamSynchronize(st_));
+  }
+  // slot 0: stage through stage_ on the compute stream; slots 1, 2: stage_ / stage2_
+  // with the copy on the copy stream (reuse waits for the slot's previous pack)
+  void set_vblock_async(int kind, int ch, const double *v, int slot, bool reuse = false) {
     const Layout &L = *L_;
     if (!v) throw EngineError(1, "null V block");
     int rows = 0;
@@ -237,11 +278,22 @@ class Engine final : public IEngine {
         throw EngineError(1, "unknown V block kind");
     }
     if (target < 0) return;  // an hhhh channel without an hhpp partner is not used by CCD
-    CK(cudaMemcpyAsync(stage_.p, v, (size_t)elems * 2 * sizeof(double), cudaMemcpyHostToDevice, st_));
     S *dst = kind == 3 ? Vhp_.as<S>() : kind == 6 ? Vpp_.as<S>() : Vhh_.as<S>();
-    launch_pack_vblock<S>(D_, kind, target, rows, stage_.as<double>(), dst, flag_.as<int>(), st_);
+    const size_t bytes = (size_t)elems * 2 * sizeof(double);
+    if (slot == 0) {
+      CK(cudaMemcpyAsync(stage_.p, v, bytes, cudaMemcpyHostToDevice, st_));
+      launch_pack_vblock<S>(D_, kind, target, rows, stage_.as<double>(), dst, flag_.as<int>(), st_);
+    } else {
+      const int b = slot - 1;
+      double *buf = (b ? stage2_ : stage_).as<double>();
+      if (reuse) CK(cudaStreamWaitEvent(cs_, sev_[2 + b], 0));  // the slot's previous pack is done
+      CK(cudaMemcpyAsync(buf, v, bytes, cudaMemcpyHostToDevice, cs_));
+      CK(cudaEventRecord(sev_[b], cs_));
+      CK(cudaStreamWaitEvent(st_, sev_[b], 0));
+      launch_pack_vblock<S>(D_, kind, target, rows, buf, dst, flag_.as<int>(), st_);
+      CK(cudaEventRecord(sev_[2 + b], st_));
+    }
     ++launches_;
-    check_flag("V block has a non-zero imaginary part but the engine is real");
     dirty_ = true;
     ++v_version_;
   }
@@ -1203,6 +1255,13 @@ class Engine final : public IEngine {
   // problem list of PP_b = V_pppp' T_b
   void prepare_oz() {
     if (oz_ready_ && oz_v_version_ == v_version_) return;
+    if (oz_ready_) {  // plans unchanged: digits of the new V only
+      run_oz_split(ozsVpp_);
+      run_oz_split(ozsVph_);
+      CK(cudaStreamSynchronize(st_));
+      oz_v_version_ = v_version_;
+      return;
+    }
     const Layout &L = *L_;
     const int nc = L.fam[3].count();
     auto mpad = [](int x) { return (x + 127) / 128 * 128; };
@@ -1363,6 +1422,14 @@ class Engine final : public IEngine {
   // Tile buffers, split jobs and tensor-core problem lists of the mixed residual.
   void prepare_mixed(int kind) {
     if (mixed_ready_ && tc_kind_ == kind && mixed_v_version_ == v_version_) return;
+    if (mixed_ready_ && tc_kind_ == kind) {
+      // same layout and operand kind: only the split of the new V is redone
+      commit();
+      run_split(spStatic_);
+      CK(cudaStreamSynchronize(st_));
+      mixed_v_version_ = v_version_;
+      return;
+    }
     oz_ready_ = false;  // the re-base problem list points into buffers allocated here
     const Layout &L = *L_;
     tc_kind_ = kind;
@@ -1703,6 +1770,9 @@ class Engine final : public IEngine {
   SplitPlan spStatic_, spTphb_, spIter1_, spIter2_;
   double *host_res_ = nullptr;
   int host_flag_ = 0;
+  cudaStream_t cs_ = nullptr;       // copy stream of ccx_set_vblocks
+  cudaEvent_t sev_[5] = {};         // copied[2], packed[2], compute-stream mark
+  DBuf stage2_;
   double e0_[2] = {0, 0};
   double last_rn_ = 0.0;
   bool have_fock_ = false, have_t_ = false, dirty_ = true, vph_ready_ = false, generated_ = false;

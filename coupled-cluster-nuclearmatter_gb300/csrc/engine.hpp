@@ -66,6 +66,7 @@ class IEngine {
   virtual void kernel_timers(double ms[kKernelSlots], int64_t n[kKernelSlots]) const = 0;
   virtual void set_fock(const double *fock, const double e0[2]) = 0;
   virtual void set_vblock(int kind, int ch, const double *v) = 0;
+  virtual void set_vblocks(int kind, int n, const int *chs, const double *const *vs) = 0;
   virtual void generate(const PotentialSpec &p) = 0;
   virtual void get_e0(double e0[2]) = 0;
   virtual void get_vblock(int kind, int ch, double *v) = 0;

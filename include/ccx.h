@@ -175,6 +175,11 @@ int ccx_set_fock(ccx_engine *e, const double *fock, const double e0[2]);
  * only read during the call. */
 #define CCX_V_PPPP 6
 int ccx_set_vblock(ccx_engine *e, int32_t kind, int32_t ch, const double *v);
+/* The same for n blocks of one kind (channels chs[i], buffers v[i]) in one call: the
+ * copies are queued back to back and the call returns once all have been read, so a
+ * host that hands over every channel of a family pays one synchronisation.  Same
+ * reference arrays as ccx_set_vblock. */
+int ccx_set_vblocks(ccx_engine *e, int32_t kind, int32_t n, const int32_t *chs, const double *const *v);
 
 /* Generate Fock, E0 and every V block on the device from a synthetic potential
  * (replaces the potential loops of setup_channel_structures, ccm_iter.f90:819-1311,

@@ -227,6 +227,34 @@ def test_caller_supplied_blocks_match_generated(ccx, O):
     assert abs(r1["e_ccd"] - r2["e_ccd"]) < 1e-11 * abs(ro["e_ccd"])
 
 
+def test_set_vblocks_matches_single_blocks(ccx, O):
+    """ccx_set_vblocks (one call per block family) gives the same engine as one call per block."""
+    o, L, eg = make(ccx, O, **C1)
+    e1 = ccx.Engine(L, real=True)
+    e2 = ccx.Engine(L, real=True)
+    for e in (e1, e2):
+        e.set_fock(o.fock(), o.e0())
+    for c in range(o.n_channels(3)):
+        e1.set_vblock(ccx.CH_HHPP, c, o.v_hhpp(c))
+        e1.set_vblock(ccx.V_PPPP, c, o.v_pppp(c))
+    for c in range(o.n_channels(1)):
+        e1.set_vblock(ccx.CH_HHHH, c, o.v_hhhh(c))
+    for c in range(o.n_channels(4)):
+        e1.set_vblock(ccx.CH_HPHP, c, o.v_hphp(c))
+    e2.set_vblocks(ccx.CH_HHPP, {c: o.v_hhpp(c) for c in range(o.n_channels(3))})
+    e2.set_vblocks(ccx.V_PPPP, {c: o.v_pppp(c) for c in range(o.n_channels(3))})
+    e2.set_vblocks(ccx.CH_HHHH, {c: o.v_hhhh(c) for c in range(o.n_channels(1))})
+    e2.set_vblocks(ccx.CH_HPHP, {c: o.v_hphp(c) for c in range(o.n_channels(4))})
+    for e in (e1, e2):
+        e.setup_t_amplitudes()
+        e.t2_intermediate()
+    for c in range(o.n_channels(3)):
+        assert np.array_equal(e1.t2_eqn(c), e2.t2_eqn(c))
+    with pytest.raises(ccx.CcxError) as ex:
+        e2.set_vblocks(ccx.CH_HHPP, {0: o.v_hhpp(0), 1: o.v_hhpp(1) + 1e-3j})
+    assert ex.value.code == 1
+
+
 def test_complex_block_into_real_engine_is_rejected(ccx, O):
     o = O.Oracle(O.Config(nmax=1, A=2, rho=0.08))
     L = ccx.Layout.from_basis(1, 2, 0.08)
