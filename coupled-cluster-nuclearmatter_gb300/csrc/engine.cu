@@ -487,8 +487,6 @@ class Engine final : public IEngine {
     if (o.precision < 0 || o.precision > 2) throw EngineError(1, "unknown precision");
     if (o.rebase < 0 || o.rebase > 1) throw EngineError(1, "unknown re-base product kind");
     if (o.precision != 0 && o.mode != 1) throw EngineError(1, "mixed precision runs with the standard (DIIS) mode");
-    if (o.precision != 0 && ScalarOf<S>::complex)
-      throw EngineError(1, "mixed precision is implemented for real interactions (real engine)");
     r = IterResult();
     double e[2];
     energy(e);
@@ -1173,13 +1171,19 @@ class Engine final : public IEngine {
   }
 
   // ================================================================== mixed precision
+  // Tensor-core products on FP64 data of either scalar kind.  A real product is one
+  // problem.  A complex product C += a A B becomes four real ones on the re / im parts
+  // of the interleaved operands, in two launch phases so that no two CTAs update the
+  // same C entries at once: phase 0 C_re += a Are Bre, C_im += a Are Bim; phase 1
+  // C_re -= a Aim Bim, C_im += a Aim Bre.
+  static constexpr int kNComp = ScalarOf<S>::complex ? 2 : 1;
   // Tiles bucketed by padded N, so that small problems run with small shared-memory
   // stages (and more CTAs per SM) instead of the largest problem's footprint.
   static constexpr int kTcBuckets = 4;
   struct TcPlan {
     DBuf probs;
-    DBuf tiles[kTcBuckets];
-    int ntiles[kTcBuckets] = {}, npad_max[kTcBuckets] = {}, max_nk[kTcBuckets] = {};
+    DBuf tiles[2][kTcBuckets];
+    int ntiles[2][kTcBuckets] = {}, npad_max[2][kTcBuckets] = {}, max_nk[2][kTcBuckets] = {};
   };
   struct SplitPlan {
     DBuf jobs, chunks;
@@ -1187,23 +1191,32 @@ class Engine final : public IEngine {
   };
   struct TileBuf {
     DBuf hi, lo;
-    int64_t n = 0;  // elements
+    int64_t n = 0;  // elements of one scalar component; the buffer holds kNComp of them
   };
-  void finalize_tc(TcPlan &pl, const std::vector<TcProb> &probs, const std::vector<TcTile> &tiles, int /*npad_max*/) {
-    upload(pl.probs, probs, &bytes_);
-    std::vector<TcTile> b[kTcBuckets];
-    for (int k = 0; k < kTcBuckets; ++k) { pl.npad_max[k] = 16; pl.max_nk[k] = 1; }
-    for (const TcTile &t : tiles) {
-      const TcProb &p = probs[t.prob];
+  // problems, their launch phase and their row tiles, built on the host
+  struct TcList {
+    std::vector<TcProb> probs;
+    std::vector<int> phase;
+    std::vector<TcTile> tiles;
+  };
+  void finalize_tc(TcPlan &pl, const TcList &l) {
+    upload(pl.probs, l.probs, &bytes_);
+    std::vector<TcTile> b[2][kTcBuckets];
+    for (int ph = 0; ph < 2; ++ph)
+      for (int k = 0; k < kTcBuckets; ++k) { pl.npad_max[ph][k] = 16; pl.max_nk[ph][k] = 1; }
+    for (const TcTile &t : l.tiles) {
+      const TcProb &p = l.probs[t.prob];
+      const int ph = l.phase[t.prob];
       const int k = p.npad <= 32 ? 0 : p.npad <= 64 ? 1 : p.npad <= 128 ? 2 : 3;
-      b[k].push_back(t);
-      pl.npad_max[k] = std::max(pl.npad_max[k], p.npad);
-      pl.max_nk[k] = std::max(pl.max_nk[k], p.nk);
+      b[ph][k].push_back(t);
+      pl.npad_max[ph][k] = std::max(pl.npad_max[ph][k], p.npad);
+      pl.max_nk[ph][k] = std::max(pl.max_nk[ph][k], p.nk);
     }
-    for (int k = 0; k < kTcBuckets; ++k) {
-      upload(pl.tiles[k], b[k], &bytes_);
-      pl.ntiles[k] = (int)b[k].size();
-    }
+    for (int ph = 0; ph < 2; ++ph)
+      for (int k = 0; k < kTcBuckets; ++k) {
+        upload(pl.tiles[ph][k], b[ph][k], &bytes_);
+        pl.ntiles[ph][k] = (int)b[ph][k].size();
+      }
   }
   void finalize_split(SplitPlan &pl, const std::vector<TcSplitJob> &jobs) {
     upload(pl.jobs, jobs, &bytes_);
@@ -1212,27 +1225,93 @@ class Engine final : public IEngine {
     pl.nchunks = (int)ch.size();
   }
   void run_tc(const TcPlan &pl) {
-    for (int k = 0; k < kTcBuckets; ++k) {
-      if (!pl.ntiles[k]) continue;
-      launch_tc_gemm(tc_kind_, (const TcProb *)pl.probs.p, (const TcTile *)pl.tiles[k].p, pl.ntiles[k],
-                     pl.npad_max[k], pl.max_nk[k], tcerr_.as<int>(), st_);
-      ++launches_;
-    }
+    for (int ph = 0; ph < 2; ++ph)
+      for (int k = 0; k < kTcBuckets; ++k) {
+        if (!pl.ntiles[ph][k]) continue;
+        launch_tc_gemm(tc_kind_, (const TcProb *)pl.probs.p, (const TcTile *)pl.tiles[ph][k].p, pl.ntiles[ph][k],
+                       pl.npad_max[ph][k], pl.max_nk[ph][k], tcerr_.as<int>(), st_);
+        ++launches_;
+      }
   }
   void run_split(const SplitPlan &pl) {
     if (!pl.nchunks) return;
     launch_tc_split(tc_kind_, (const TcSplitJob *)pl.jobs.p, (const int4 *)pl.chunks.p, pl.nchunks, st_);
     ++launches_;
   }
+  // split jobs of one matrix operand (element (r, k) at src[r sr + k sk] in S units,
+  // minus sub when given), one per scalar component, into tile buffer b at offset off
+  void add_split(std::vector<TcSplitJob> &js, const S *src, const S *sub, int64_t sr, int64_t sk, int rows, int cols,
+                 int tile_rows, int rows_pad, TileBuf &b, int64_t off) {
+    const size_t es = tc_kind_ == kTcBF16 ? 2 : 4;
+    const int tk = tc_tile_k(tc_kind_);
+    for (int c = 0; c < kNComp; ++c) {
+      TcSplitJob j{};
+      j.src = (const double *)src + c;
+      j.sub = sub ? (const double *)sub + c : nullptr;
+      j.sr = sr * kNComp;
+      j.sk = sk * kNComp;
+      j.rows = rows; j.cols = cols; j.tile_rows = tile_rows; j.nk = (cols + tk - 1) / tk; j.rows_pad = rows_pad;
+      j.hi = (char *)b.hi.p + (off + c * b.n) * es;
+      j.lo = (char *)b.lo.p + (off + c * b.n) * es;
+      j.scale = 1.0;
+      js.push_back(j);
+    }
+  }
+  // C (S units, strides sCm, sCn) += alpha A B with A (M x K) in tile buffer a at ao and
+  // B (N x K) in b at bo
+  void add_tc(TcList &l, TileBuf &a, int64_t ao, TileBuf &b, int64_t bo, int M, int N, int K, S *C, int64_t sCm,
+              int64_t sCn, double alpha) {
+    const size_t es = tc_kind_ == kTcBF16 ? 2 : 4;
+    const int tk = tc_tile_k(tc_kind_);
+    auto one = [&](int ca, int cb, int cc, double al, int ph) {
+      TcProb p{};
+      p.Ahi = (char *)a.hi.p + (ao + ca * a.n) * es;
+      p.Alo = (char *)a.lo.p + (ao + ca * a.n) * es;
+      p.Bhi = (char *)b.hi.p + (bo + cb * b.n) * es;
+      p.Blo = (char *)b.lo.p + (bo + cb * b.n) * es;
+      p.M = M; p.N = N; p.nk = (K + tk - 1) / tk; p.npad = (N + 15) / 16 * 16;
+      p.C = (double *)C + cc; p.sCm = sCm * kNComp; p.sCn = sCn * kNComp; p.alpha = al;
+      for (int mt = 0; mt < (M + 127) / 128; ++mt) l.tiles.push_back(TcTile{(int)l.probs.size(), mt});
+      l.probs.push_back(p);
+      l.phase.push_back(ph);
+    };
+    if (kNComp == 1) {
+      one(0, 0, 0, alpha, 0);
+    } else {
+      one(0, 0, 0, alpha, 0);
+      one(0, 1, 1, alpha, 0);
+      one(1, 1, 0, -alpha, 1);
+      one(1, 0, 1, alpha, 1);
+    }
+  }
+
   // ---- FP64-accurate re-base products as exact digit products (Ozaki scheme) ----
   struct OzSplitPlan {
     DBuf jobs, rows, chunks;
     int nrows = 0, nchunks = 0;
   };
   struct OzPlan {
-    DBuf probs, tiles;
-    int ntiles = 0;
+    DBuf probs, tiles[2];
+    int ntiles[2] = {0, 0};
   };
+  // digit planes of one operand kind: kNComp x (kOzSlices planes of n elements), and
+  // kNComp x rows exponents
+  struct OzBuf {
+    DBuf planes, exps;
+    int64_t n = 0, rows = 0;
+  };
+  struct OzList {
+    std::vector<OzProb> probs;
+    std::vector<int> phase;
+    std::vector<OzTile> tiles;
+  };
+  void alloc_oz(OzBuf &b, int64_t n, int64_t rows) {
+    b.n = std::max<int64_t>(n, 8);
+    b.rows = std::max<int64_t>(rows, 1);
+    b.planes.alloc((size_t)b.n * kOzSlices * kNComp * 2, &bytes_);
+    b.exps.alloc((size_t)b.rows * kNComp * 4, &bytes_);
+    CK(cudaMemset(b.planes.p, 0, b.planes.bytes));  // padding row groups stay zero
+  }
   void finalize_oz_split(OzSplitPlan &pl, const std::vector<OzSplitJob> &jobs) {
     upload(pl.jobs, jobs, &bytes_);
     const std::vector<int2> rows = oz_row_table(jobs);
@@ -1242,28 +1321,82 @@ class Engine final : public IEngine {
     pl.nrows = (int)rows.size();
     pl.nchunks = (int)ch.size();
   }
+  void finalize_oz(OzPlan &pl, const OzList &l) {
+    upload(pl.probs, l.probs, &bytes_);
+    std::vector<OzTile> t[2];
+    for (const OzTile &x : l.tiles) t[l.phase[x.prob]].push_back(x);
+    for (int ph = 0; ph < 2; ++ph) {
+      upload(pl.tiles[ph], t[ph], &bytes_);
+      pl.ntiles[ph] = (int)t[ph].size();
+    }
+  }
   void run_oz_split(const OzSplitPlan &pl) {
     launch_oz_split((const OzSplitJob *)pl.jobs.p, (const int2 *)pl.rows.p, pl.nrows, (const int4 *)pl.chunks.p,
                     pl.nchunks, st_);
     launches_ += 2;
   }
   void run_oz(const OzPlan &pl) {
-    launch_oz_gemm((const OzProb *)pl.probs.p, (const OzTile *)pl.tiles.p, pl.ntiles, tcerr_.as<int>(), st_);
-    ++launches_;
+    for (int ph = 0; ph < 2; ++ph) {
+      if (!pl.ntiles[ph]) continue;
+      launch_oz_gemm((const OzProb *)pl.probs.p, (const OzTile *)pl.tiles[ph].p, pl.ntiles[ph], tcerr_.as<int>(), st_);
+      ++launches_;
+    }
   }
-  // digit planes of V_pppp' (static), of the base amplitudes (per re-base) and the
-  // problem list of PP_b = V_pppp' T_b
+  // digit jobs of one operand (element (r, k) at src[r sr + k sk], S units), one per
+  // scalar component, into b at element offset off and exponent offset xoff
+  void add_oz_split(std::vector<OzSplitJob> &js, const S *src, int64_t sr, int64_t sk, int rows, int cols,
+                    int tile_rows, int rows_pad, OzBuf &b, int64_t off, int64_t xoff) {
+    for (int c = 0; c < kNComp; ++c) {
+      OzSplitJob j{};
+      j.src = (const double *)src + c;
+      j.sr = sr * kNComp;
+      j.sk = sk * kNComp;
+      j.rows = rows; j.cols = cols; j.tile_rows = tile_rows; j.nk = (cols + 63) / 64; j.rows_pad = rows_pad;
+      j.planes = ((uint16_t *)b.planes.p) + (int64_t)c * b.n * kOzSlices + off;
+      j.plane_elems = b.n;
+      j.exps = ((int *)b.exps.p) + (int64_t)c * b.rows + xoff;
+      js.push_back(j);
+    }
+  }
+  void add_oz(OzList &l, OzBuf &a, int64_t ao, int64_t axo, OzBuf &b, int64_t bo, int64_t bxo, int M, int N, int K,
+              S *C, int64_t sCm, int64_t sCn, double alpha) {
+    auto one = [&](int ca, int cb, int cc, double al, int ph) {
+      OzProb p{};
+      p.A = ((uint16_t *)a.planes.p) + (int64_t)ca * a.n * kOzSlices + ao;
+      p.eA = ((int *)a.exps.p) + (int64_t)ca * a.rows + axo;
+      p.B = ((uint16_t *)b.planes.p) + (int64_t)cb * b.n * kOzSlices + bo;
+      p.eB = ((int *)b.exps.p) + (int64_t)cb * b.rows + bxo;
+      p.a_plane = a.n;
+      p.b_plane = b.n;
+      p.M = M; p.N = N; p.nk = (K + 63) / 64; p.npad = (N + 15) / 16 * 16;
+      p.C = (double *)C + cc; p.sCm = sCm * kNComp; p.sCn = sCn * kNComp; p.alpha = al;
+      for (int mt = 0; mt < (M + 127) / 128; ++mt)
+        for (int n0 = 0; n0 < p.npad; n0 += kOzN) l.tiles.push_back(OzTile{(int)l.probs.size(), mt, n0});
+      l.probs.push_back(p);
+      l.phase.push_back(ph);
+    };
+    if (kNComp == 1) {
+      one(0, 0, 0, alpha, 0);
+    } else {
+      one(0, 0, 0, alpha, 0);
+      one(0, 1, 1, alpha, 0);
+      one(1, 1, 0, -alpha, 1);
+      one(1, 0, 1, alpha, 1);
+    }
+  }
+
+  // Digit planes of V_pppp' and V_ph (static), of T_b', T_ph and I4 (per re-base), and
+  // the problem lists of PP_b = V_pppp' T_b, I4 = W + 1/2 V_ph T_ph and R_ph = T_ph I4.
   void prepare_oz() {
     if (oz_ready_ && oz_v_version_ == v_version_) return;
     if (oz_ready_) {  // plans unchanged: digits of the new V only
-      run_oz_split(ozsVpp_);
-      run_oz_split(ozsVph_);
+      run_oz_split(ozsV_);
       CK(cudaStreamSynchronize(st_));
       oz_v_version_ = v_version_;
       return;
     }
     const Layout &L = *L_;
-    const int nc = L.fam[3].count();
+    const int nc = L.fam[3].count(), nq = L.ph[1].count();
     auto mpad = [](int x) { return (x + 127) / 128 * 128; };
     auto npadf = [](int x) { return (x + 15) / 16 * 16; };
     auto nkf = [](int x) { return (x + 63) / 64; };
@@ -1277,146 +1410,77 @@ class Engine final : public IEngine {
       ra += pk.P;
       rb += npadf(pk.H);
     }
-    ozVpp_.alloc((size_t)std::max<int64_t>(pa, 8) * kOzSlices * 2, &bytes_);
-    ozVppE_.alloc((size_t)std::max<int64_t>(ra, 1) * 4, &bytes_);
-    ozTb_.alloc((size_t)std::max<int64_t>(pb, 8) * kOzSlices * 2, &bytes_);
-    ozTbE_.alloc((size_t)std::max<int64_t>(rb, 1) * 4, &bytes_);
-    CK(cudaMemset(ozVpp_.p, 0, ozVpp_.bytes));
-    CK(cudaMemset(ozTb_.p, 0, ozTb_.bytes));
-    if (!tcerr_.p) {
-      tcerr_.alloc(sizeof(int), &bytes_);
-      CK(cudaMemset(tcerr_.p, 0, sizeof(int)));
-    }
-    std::vector<OzSplitJob> ja, jb;
-    std::vector<OzProb> probs;
-    std::vector<OzTile> tiles;
-    int64_t qa = 0, qb = 0, xa = 0, xb = 0, voff = 0;
-    for (int c = 0; c < nc; ++c) {
-      const auto &pk = L.pk[c];
-      if (pk.P > 0 && pk.H > 0) {
-        OzSplitJob a{};
-        a.src = (const double *)(Vpp_.as<S>() + voff); a.sr = pk.P; a.sk = 1;
-        a.rows = pk.P; a.cols = pk.P; a.tile_rows = 128; a.nk = nkf(pk.P); a.rows_pad = mpad(pk.P);
-        a.planes = ozVpp_.as<uint16_t>() + qa; a.plane_elems = pa; a.exps = ozVppE_.as<int>() + xa;
-        OzSplitJob b{};
-        b.src = (const double *)(T_.as<S>() + pk.t_off); b.sr = pk.P; b.sk = 1;
-        b.rows = pk.H; b.cols = pk.P; b.tile_rows = npadf(pk.H); b.nk = nkf(pk.P); b.rows_pad = npadf(pk.H);
-        b.planes = ozTb_.as<uint16_t>() + qb; b.plane_elems = pb; b.exps = ozTbE_.as<int>() + xb;
-        OzProb p{};
-        p.A = a.planes; p.eA = a.exps; p.B = b.planes; p.eB = b.exps; p.a_plane = pa; p.b_plane = pb;
-        p.M = pk.P; p.N = pk.H; p.nk = nkf(pk.P); p.npad = npadf(pk.H);
-        p.C = (double *)(PPb_.as<S>() + pk.t_off); p.sCm = 1; p.sCn = pk.P; p.alpha = 1.0;
-        for (int mt = 0; mt < mpad(pk.P) / 128; ++mt)
-          for (int n0 = 0; n0 < p.npad; n0 += kOzN) tiles.push_back(OzTile{(int)probs.size(), mt, n0});
-        probs.push_back(p);
-        ja.push_back(a);
-        jb.push_back(b);
-        qa += (int64_t)mpad(pk.P) * nkf(pk.P) * 64;
-        qb += (int64_t)npadf(pk.H) * nkf(pk.P) * 64;
-        xa += pk.P;
-        xb += npadf(pk.H);
-      }
-      voff += (int64_t)pk.P * pk.P;
-    }
-    finalize_oz_split(ozsVpp_, ja);
-    finalize_oz_split(ozsTb_, jb);
-    upload(ozPP_.probs, probs, &bytes_);
-    upload(ozPP_.tiles, tiles, &bytes_);
-    ozPP_.ntiles = (int)tiles.size();
-    prepare_oz_ring();
-    run_oz_split(ozsVpp_);
-    run_oz_split(ozsVph_);
-    CK(cudaStreamSynchronize(st_));
-    oz_ready_ = true;
-    oz_v_version_ = v_version_;
-  }
-
-  // ring channels: I4 = W + 1/2 V_ph T_ph (A = V_ph, static; B = T_ph) and
-  // R_ph = T_ph I4 (A = T_ph, B = I4), all n_hp, n_ph <= 256
-  void prepare_oz_ring() {
-    const Layout &L = *L_;
-    const int nq = L.ph[1].count();
-    auto mpad = [](int x) { return (x + 127) / 128 * 128; };
-    auto npadf = [](int x) { return (x + 15) / 16 * 16; };
-    auto nkf = [](int x) { return (x + 63) / 64; };
-    int64_t pv = 0, pt = 0, pa = 0, pi = 0, rv = 0, rt = 0, ra = 0, ri = 0;
+    int64_t pv = 0, pt = 0, pr = 0, pi = 0, rv = 0, rt = 0, rr = 0, ri = 0;
     for (int q = 0; q < nq; ++q) {
       const int nph = L.ph[1].side1[q].size(), nhp = L.ph[1].side2[q].size();
       if (nph <= 0 || nhp <= 0) continue;
       if (nhp > 256) throw EngineError(1, "digit-product re-base: a ring channel has more than 256 hole-particle pairs");
       pv += (int64_t)mpad(nhp) * nkf(nph) * 64;   // A = V_ph (n_hp x n_ph)
       pt += (int64_t)npadf(nhp) * nkf(nph) * 64;  // B = T_ph (K n_ph, N n_hp)
-      pa += (int64_t)mpad(nph) * nkf(nhp) * 64;   // A = T_ph (n_ph x n_hp)
+      pr += (int64_t)mpad(nph) * nkf(nhp) * 64;   // A = T_ph (n_ph x n_hp)
       pi += (int64_t)npadf(nhp) * nkf(nhp) * 64;  // B = I4 (K n_hp, N n_hp)
-      rv += nhp; rt += npadf(nhp); ra += nph; ri += npadf(nhp);
+      rv += nhp; rt += npadf(nhp); rr += nph; ri += npadf(nhp);
     }
-    auto planes = [&](DBuf &b, DBuf &e, int64_t el, int64_t rows) {
-      b.alloc((size_t)std::max<int64_t>(el, 8) * kOzSlices * 2, &bytes_);
-      e.alloc((size_t)std::max<int64_t>(rows, 1) * 4, &bytes_);
-      CK(cudaMemset(b.p, 0, b.bytes));
-    };
-    planes(ozVph_, ozVphE_, pv, rv);
-    planes(ozTphB_, ozTphBE_, pt, rt);
-    planes(ozTphA_, ozTphAE_, pa, ra);
-    planes(ozI4B_, ozI4BE_, pi, ri);
-    auto job = [](const S *src, int64_t sr, int64_t sk, int rows, int cols, int tile_rows, int rows_pad,
-                  uint16_t *pl, int64_t plane, int *ex) {
-      OzSplitJob j{};
-      j.src = (const double *)src; j.sr = sr; j.sk = sk; j.rows = rows; j.cols = cols; j.tile_rows = tile_rows;
-      j.nk = (cols + 63) / 64; j.rows_pad = rows_pad; j.planes = pl; j.plane_elems = plane; j.exps = ex;
-      return j;
-    };
-    std::vector<OzSplitJob> jv, jt, ji;
-    std::vector<OzProb> p4, pr;
-    std::vector<OzTile> t4, tr;
-    int64_t qv = 0, qt = 0, qa = 0, qi = 0, xv = 0, xt = 0, xa = 0, xi = 0, toff = 0, ioff = 0;
-    for (int q = 0; q < nq; ++q) {
-      const int nph = L.ph[1].side1[q].size(), nhp = L.ph[1].side2[q].size();
-      if (nph > 0 && nhp > 0) {
-        const OzSplitJob a4 = job(Vph_.as<S>() + toff, 1, nhp, nhp, nph, 128, mpad(nhp), ozVph_.as<uint16_t>() + qv, pv,
-                                  ozVphE_.as<int>() + xv);
-        const OzSplitJob b4 = job(Tph_.as<S>() + toff, nph, 1, nhp, nph, npadf(nhp), npadf(nhp),
-                                  ozTphB_.as<uint16_t>() + qt, pt, ozTphBE_.as<int>() + xt);
-        const OzSplitJob ar = job(Tph_.as<S>() + toff, 1, nph, nph, nhp, 128, mpad(nph), ozTphA_.as<uint16_t>() + qa, pa,
-                                  ozTphAE_.as<int>() + xa);
-        const OzSplitJob br = job(I4_.as<S>() + ioff, nhp, 1, nhp, nhp, npadf(nhp), npadf(nhp),
-                                  ozI4B_.as<uint16_t>() + qi, pi, ozI4BE_.as<int>() + xi);
-        jv.push_back(a4);
-        jt.push_back(b4);
-        jt.push_back(ar);
-        ji.push_back(br);
-        OzProb x{};
-        x.A = a4.planes; x.eA = a4.exps; x.B = b4.planes; x.eB = b4.exps; x.a_plane = pv; x.b_plane = pt;
-        x.M = nhp; x.N = nhp; x.nk = nkf(nph); x.npad = npadf(nhp);
-        x.C = (double *)(I4_.as<S>() + ioff); x.sCm = 1; x.sCn = nhp; x.alpha = 0.5;
-        for (int n0 = 0; n0 < x.npad; n0 += kOzN) t4.push_back(OzTile{(int)p4.size(), 0, n0});
-        if (mpad(nhp) > 128) for (int n0 = 0; n0 < x.npad; n0 += kOzN) t4.push_back(OzTile{(int)p4.size(), 1, n0});
-        p4.push_back(x);
-        OzProb y{};
-        y.A = ar.planes; y.eA = ar.exps; y.B = br.planes; y.eB = br.exps; y.a_plane = pa; y.b_plane = pi;
-        y.M = nph; y.N = nhp; y.nk = nkf(nhp); y.npad = npadf(nhp);
-        y.C = (double *)(Rph_.as<S>() + toff); y.sCm = 1; y.sCn = nph; y.alpha = 1.0;
-        for (int mt = 0; mt < mpad(nph) / 128; ++mt)
-          for (int n0 = 0; n0 < y.npad; n0 += kOzN) tr.push_back(OzTile{(int)pr.size(), mt, n0});
-        pr.push_back(y);
-        qv += (int64_t)mpad(nhp) * nkf(nph) * 64;
-        qt += (int64_t)npadf(nhp) * nkf(nph) * 64;
-        qa += (int64_t)mpad(nph) * nkf(nhp) * 64;
-        qi += (int64_t)npadf(nhp) * nkf(nhp) * 64;
-        xv += nhp; xt += npadf(nhp); xa += nph; xi += npadf(nhp);
+    alloc_oz(ozVpp_, pa, ra);
+    alloc_oz(ozTb_, pb, rb);
+    alloc_oz(ozVph_, pv, rv);
+    alloc_oz(ozTphB_, pt, rt);
+    alloc_oz(ozTphA_, pr, rr);
+    alloc_oz(ozI4B_, pi, ri);
+    if (!tcerr_.p) {
+      tcerr_.alloc(sizeof(int), &bytes_);
+      CK(cudaMemset(tcerr_.p, 0, sizeof(int)));
+    }
+    std::vector<OzSplitJob> jv, jb, jt, ji;
+    OzList lpp, l4, lr;
+    {
+      int64_t qa = 0, qb = 0, xa = 0, xb = 0, voff = 0;
+      for (int c = 0; c < nc; ++c) {
+        const auto &pk = L.pk[c];
+        if (pk.P > 0 && pk.H > 0) {
+          add_oz_split(jv, Vpp_.as<S>() + voff, pk.P, 1, pk.P, pk.P, 128, mpad(pk.P), ozVpp_, qa, xa);
+          add_oz_split(jb, T_.as<S>() + pk.t_off, pk.P, 1, pk.H, pk.P, npadf(pk.H), npadf(pk.H), ozTb_, qb, xb);
+          add_oz(lpp, ozVpp_, qa, xa, ozTb_, qb, xb, pk.P, pk.H, pk.P, PPb_.as<S>() + pk.t_off, 1, pk.P, 1.0);
+          qa += (int64_t)mpad(pk.P) * nkf(pk.P) * 64;
+          qb += (int64_t)npadf(pk.H) * nkf(pk.P) * 64;
+          xa += pk.P;
+          xb += npadf(pk.H);
+        }
+        voff += (int64_t)pk.P * pk.P;
       }
-      toff += (int64_t)nph * nhp;
-      ioff += (int64_t)nhp * nhp;
     }
-    finalize_oz_split(ozsVph_, jv);
+    {
+      int64_t qv = 0, qt = 0, qr = 0, qi = 0, xv = 0, xt = 0, xr = 0, xi = 0, toff = 0, ioff = 0;
+      for (int q = 0; q < nq; ++q) {
+        const int nph = L.ph[1].side1[q].size(), nhp = L.ph[1].side2[q].size();
+        if (nph > 0 && nhp > 0) {
+          add_oz_split(jv, Vph_.as<S>() + toff, 1, nhp, nhp, nph, 128, mpad(nhp), ozVph_, qv, xv);
+          add_oz_split(jt, Tph_.as<S>() + toff, nph, 1, nhp, nph, npadf(nhp), npadf(nhp), ozTphB_, qt, xt);
+          add_oz_split(jt, Tph_.as<S>() + toff, 1, nph, nph, nhp, 128, mpad(nph), ozTphA_, qr, xr);
+          add_oz_split(ji, I4_.as<S>() + ioff, nhp, 1, nhp, nhp, npadf(nhp), npadf(nhp), ozI4B_, qi, xi);
+          add_oz(l4, ozVph_, qv, xv, ozTphB_, qt, xt, nhp, nhp, nph, I4_.as<S>() + ioff, 1, nhp, 0.5);
+          add_oz(lr, ozTphA_, qr, xr, ozI4B_, qi, xi, nph, nhp, nhp, Rph_.as<S>() + toff, 1, nph, 1.0);
+          qv += (int64_t)mpad(nhp) * nkf(nph) * 64;
+          qt += (int64_t)npadf(nhp) * nkf(nph) * 64;
+          qr += (int64_t)mpad(nph) * nkf(nhp) * 64;
+          qi += (int64_t)npadf(nhp) * nkf(nhp) * 64;
+          xv += nhp; xt += npadf(nhp); xr += nph; xi += npadf(nhp);
+        }
+        toff += (int64_t)nph * nhp;
+        ioff += (int64_t)nhp * nhp;
+      }
+    }
+    finalize_oz_split(ozsV_, jv);
+    finalize_oz_split(ozsTb_, jb);
     finalize_oz_split(ozsTph_, jt);
     finalize_oz_split(ozsI4_, ji);
-    upload(ozI4_.probs, p4, &bytes_);
-    upload(ozI4_.tiles, t4, &bytes_);
-    ozI4_.ntiles = (int)t4.size();
-    upload(ozRing_.probs, pr, &bytes_);
-    upload(ozRing_.tiles, tr, &bytes_);
-    ozRing_.ntiles = (int)tr.size();
+    finalize_oz(ozPP_, lpp);
+    finalize_oz(ozI4_, l4);
+    finalize_oz(ozRing_, lr);
+    run_oz_split(ozsV_);
+    CK(cudaStreamSynchronize(st_));
+    oz_ready_ = true;
+    oz_v_version_ = v_version_;
   }
 
   // Tile buffers, split jobs and tensor-core problem lists of the mixed residual.
@@ -1461,8 +1525,9 @@ class Engine final : public IEngine {
       tI4B_.n += (int64_t)npadf(nhp) * nkf(nhp) * tk;
     }
     for (TileBuf *b : bufs) {  // zeroed once: the splits never write all-padding row groups
-      b->hi.alloc((size_t)std::max<int64_t>(b->n, 16) * es, &bytes_);
-      b->lo.alloc((size_t)std::max<int64_t>(b->n, 16) * es, &bytes_);
+      b->n = std::max<int64_t>(b->n, 16);
+      b->hi.alloc((size_t)b->n * kNComp * es, &bytes_);
+      b->lo.alloc((size_t)b->n * kNComp * es, &bytes_);
       CK(cudaMemset(b->hi.p, 0, b->hi.bytes));
       CK(cudaMemset(b->lo.p, 0, b->lo.bytes));
     }
@@ -1475,40 +1540,17 @@ class Engine final : public IEngine {
     dI4_.alloc(std::max<int64_t>(n_i4_, 1) * sz, &bytes_);
     tcerr_.alloc(sizeof(int), &bytes_);
     CK(cudaMemset(tcerr_.p, 0, sizeof(int)));
-    auto at = [&](TileBuf &b, int64_t off, bool hi) { return (void *)((char *)(hi ? b.hi.p : b.lo.p) + off * es); };
-    auto job = [&](const S *src, const S *sub, int64_t sr, int64_t sk, int rows, int cols, int tile_rows, int rows_pad,
-                   TileBuf &b, int64_t off) {
-      TcSplitJob j{};
-      j.src = (const double *)src;
-      j.sub = (const double *)sub;
-      j.sr = sr; j.sk = sk; j.rows = rows; j.cols = cols; j.tile_rows = tile_rows;
-      j.nk = nkf(cols); j.rows_pad = rows_pad;
-      j.hi = at(b, off, true); j.lo = at(b, off, false); j.scale = 1.0;
-      return j;
-    };
-    auto prob = [&](TileBuf &a, int64_t ao, TileBuf &b, int64_t bo, int M, int N, int K, S *C, int64_t sCm, int64_t sCn,
-                    double alpha) {
-      TcProb p{};
-      p.Ahi = at(a, ao, true); p.Alo = at(a, ao, false); p.Bhi = at(b, bo, true); p.Blo = at(b, bo, false);
-      p.M = M; p.N = N; p.nk = nkf(K); p.npad = npadf(N);
-      p.C = (double *)C; p.sCm = sCm; p.sCn = sCn; p.alpha = alpha;
-      return p;
-    };
     std::vector<TcSplitJob> js_static, js_tphb, js_it1, js_it2;
-    std::vector<TcProb> pp, p4, pr1, pr2;
-    std::vector<TcTile> tp, t4, tr1, tr2;
-    int np_pp = 16, np_4 = 16, np_r = 16;
+    TcList pp, p4, pr1, pr2;
     {
       int64_t oa = 0, ob = 0, voff = 0;
       for (int c = 0; c < nc; ++c) {
         const auto &pk = L.pk[c];
         if (pk.P > 0 && pk.H > 0) {
-          js_static.push_back(job(Vpp_.as<S>() + voff, nullptr, pk.P, 1, pk.P, pk.P, 128, mpad(pk.P), tVpp_, oa));
-          js_it1.push_back(job(T_.as<S>() + pk.t_off, Tb_.as<S>() + pk.t_off, pk.P, 1, pk.H, pk.P, npadf(pk.H),
-                               npadf(pk.H), tD_, ob));
-          for (int mt = 0; mt < mpad(pk.P) / 128; ++mt) tp.push_back(TcTile{(int)pp.size(), mt});
-          pp.push_back(prob(tVpp_, oa, tD_, ob, pk.P, pk.H, pk.P, R_.as<S>() + pk.t_off, 1, pk.P, 1.0));
-          np_pp = std::max(np_pp, npadf(pk.H));
+          add_split(js_static, Vpp_.as<S>() + voff, nullptr, pk.P, 1, pk.P, pk.P, 128, mpad(pk.P), tVpp_, oa);
+          add_split(js_it1, T_.as<S>() + pk.t_off, Tb_.as<S>() + pk.t_off, pk.P, 1, pk.H, pk.P, npadf(pk.H),
+                    npadf(pk.H), tD_, ob);
+          add_tc(pp, tVpp_, oa, tD_, ob, pk.P, pk.H, pk.P, R_.as<S>() + pk.t_off, 1, pk.P, 1.0);
           oa += (int64_t)mpad(pk.P) * nkf(pk.P) * tk;
           ob += (int64_t)npadf(pk.H) * nkf(pk.P) * tk;
         }
@@ -1522,25 +1564,18 @@ class Engine final : public IEngine {
         if (nph > 0 && nhp > 0) {
           S *tph = Tph_.as<S>() + toff, *tphb = Tphb_.as<S>() + toff;
           // static A = V_ph (n_hp x n_ph, column-major)
-          js_static.push_back(job(Vph_.as<S>() + toff, nullptr, 1, nhp, nhp, nph, 128, mpad(nhp), tVph_, ov));
+          add_split(js_static, Vph_.as<S>() + toff, nullptr, 1, nhp, nhp, nph, 128, mpad(nhp), tVph_, ov);
           // per iteration: B = dTph (rows n_hp, K = n_ph), A = dTph (rows n_ph, K = n_hp)
-          js_it1.push_back(job(tph, tphb, nph, 1, nhp, nph, npadf(nhp), npadf(nhp), tDphB_, odb));
-          js_it1.push_back(job(tph, tphb, 1, nph, nph, nhp, 128, mpad(nph), tDphA_, oda));
+          add_split(js_it1, tph, tphb, nph, 1, nhp, nph, npadf(nhp), npadf(nhp), tDphB_, odb);
+          add_split(js_it1, tph, tphb, 1, nph, nph, nhp, 128, mpad(nph), tDphA_, oda);
           // at re-base: A = Tph_b
-          js_tphb.push_back(job(tphb, nullptr, 1, nph, nph, nhp, 128, mpad(nph), tTphbA_, ota));
+          add_split(js_tphb, tphb, nullptr, 1, nph, nph, nhp, 128, mpad(nph), tTphbA_, ota);
           // after dI4: B = dI4 and B = I4 (rows n_hp, K = n_hp)
-          js_it2.push_back(job(dI4_.as<S>() + ioff, nullptr, nhp, 1, nhp, nhp, npadf(nhp), npadf(nhp), tdI4B_, oi));
-          js_it2.push_back(job(I4_.as<S>() + ioff, nullptr, nhp, 1, nhp, nhp, npadf(nhp), npadf(nhp), tI4B_, oib));
-          for (int mt = 0; mt < mpad(nhp) / 128; ++mt) t4.push_back(TcTile{(int)p4.size(), mt});
-          p4.push_back(prob(tVph_, ov, tDphB_, odb, nhp, nhp, nph, dI4_.as<S>() + ioff, 1, nhp, 0.5));
-          for (int mt = 0; mt < mpad(nph) / 128; ++mt) {
-            tr1.push_back(TcTile{(int)pr1.size(), mt});
-            tr2.push_back(TcTile{(int)pr2.size(), mt});
-          }
-          pr1.push_back(prob(tTphbA_, ota, tdI4B_, oi, nph, nhp, nhp, Rph_.as<S>() + toff, 1, nph, 1.0));
-          pr2.push_back(prob(tDphA_, oda, tI4B_, oib, nph, nhp, nhp, Rph_.as<S>() + toff, 1, nph, 1.0));
-          np_4 = std::max(np_4, npadf(nhp));
-          np_r = std::max(np_r, npadf(nhp));
+          add_split(js_it2, dI4_.as<S>() + ioff, nullptr, nhp, 1, nhp, nhp, npadf(nhp), npadf(nhp), tdI4B_, oi);
+          add_split(js_it2, I4_.as<S>() + ioff, nullptr, nhp, 1, nhp, nhp, npadf(nhp), npadf(nhp), tI4B_, oib);
+          add_tc(p4, tVph_, ov, tDphB_, odb, nhp, nhp, nph, dI4_.as<S>() + ioff, 1, nhp, 0.5);
+          add_tc(pr1, tTphbA_, ota, tdI4B_, oi, nph, nhp, nhp, Rph_.as<S>() + toff, 1, nph, 1.0);
+          add_tc(pr2, tDphA_, oda, tI4B_, oib, nph, nhp, nhp, Rph_.as<S>() + toff, 1, nph, 1.0);
           ov += (int64_t)mpad(nhp) * nkf(nph) * tk;
           odb += (int64_t)npadf(nhp) * nkf(nph) * tk;
           ota += (int64_t)mpad(nph) * nkf(nhp) * tk;
@@ -1556,10 +1591,10 @@ class Engine final : public IEngine {
     finalize_split(spTphb_, js_tphb);
     finalize_split(spIter1_, js_it1);
     finalize_split(spIter2_, js_it2);
-    finalize_tc(tcPP_, pp, tp, np_pp);
-    finalize_tc(tcI4_, p4, t4, np_4);
-    finalize_tc(tcR1_, pr1, tr1, np_r);
-    finalize_tc(tcR2_, pr2, tr2, np_r);
+    finalize_tc(tcPP_, pp);
+    finalize_tc(tcI4_, p4);
+    finalize_tc(tcR1_, pr1);
+    finalize_tc(tcR2_, pr2);
     // FP64 plans of the re-base: PP_b = V_pppp' T, and R' += T I9
     {
       PlanBuilder bp, bh;
@@ -1759,9 +1794,8 @@ class Engine final : public IEngine {
   int tc_kind_ = 0;
   int64_t v_version_ = 0, mixed_v_version_ = -1;
   DBuf Tb_, PPb_, Tphb_, Rphb_, I4b_, dI4_, tcerr_;
-  DBuf ozVpp_, ozVppE_, ozTb_, ozTbE_;
-  DBuf ozVph_, ozVphE_, ozTphB_, ozTphBE_, ozTphA_, ozTphAE_, ozI4B_, ozI4BE_;
-  OzSplitPlan ozsVpp_, ozsTb_, ozsVph_, ozsTph_, ozsI4_;
+  OzBuf ozVpp_, ozTb_, ozVph_, ozTphB_, ozTphA_, ozI4B_;
+  OzSplitPlan ozsV_, ozsTb_, ozsTph_, ozsI4_;
   OzPlan ozPP_, ozI4_, ozRing_;
   bool oz_ready_ = false;
   int64_t oz_v_version_ = -1;

@@ -141,7 +141,8 @@ int ccx_layout_hash(const ccx_layout *l, uint64_t *hash);
 
 #define CCX_PREC_FP64 0        /* every term in FP64 */
 #define CCX_PREC_MIXED 1       /* ladder/ring contractions as BF16 hi/lo split products on the tensor
-                                  cores (FP32 accumulate), FP64 defect correction; standard mode, real engine */
+                                  cores (FP32 accumulate), FP64 defect correction; standard mode; a complex
+                                  engine runs each complex product as four real ones */
 #define CCX_PREC_MIXED_TF32 2  /* as CCX_PREC_MIXED with TF32 hi/lo split products */
 
 #define CCX_MODE_REFERENCE 0   /* 0.75/0.25 mixing + DIIS every 6 (ccm_diis.f90:74-249), |dE| stop */

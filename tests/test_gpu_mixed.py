@@ -76,13 +76,47 @@ def test_digit_rebase_pnm66_full_size(ccx):
     assert rd["fp64_sweeps"] <= rf["fp64_sweeps"] + 1
 
 
+@pytest.mark.parametrize("rebase", [0, 1], ids=["fp64_rebase", "digit_rebase"])
+def test_mixed_complex_chiral_like_snm(ccx, O, rebase):
+    """Complex engine (chiral-like SNM, complex V): each complex product runs as four
+    real tensor-core products; the converged energy matches the complex FP64 solve
+    and the oracle."""
+    L = ccx.Layout.from_basis(1, 4, 0.16, snm=True)
+    e64 = ccx.Engine(L, real=False)
+    e64.generate(potential=ccx.POT_CHIRAL_LIKE)
+    e64.setup_t_amplitudes()
+    r64 = e64.ccd_iter(mode=ccx.MODE_STANDARD, tol=1e-10, max_iter=200)
+    em = ccx.Engine(L, real=False)
+    em.generate(potential=ccx.POT_CHIRAL_LIKE)
+    em.setup_t_amplitudes()
+    rm = em.ccd_iter(mode=ccx.MODE_STANDARD, precision=ccx.PREC_MIXED, tol=1e-10, max_iter=200, rebase=rebase)
+    assert r64["converged"] and rm["converged"] and rm["res_norm"] < 1e-10
+    assert rm["mixed_iterations"] >= 1
+    assert abs(rm["e_ccd"] - r64["e_ccd"]) < 1e-10 * abs(r64["e_ccd"])
+    o = O.Oracle(O.Config(nmax=1, A=4, rho=0.16, snm=True, potential=O.POT_CHIRAL_LIKE))
+    o.mp2()
+    ro = o.ccd_iter(mode=O.MODE_STANDARD, tol=1e-10)
+    assert abs(rm["e_ccd"] - ro["e_ccd"]) < 1e-9 * abs(ro["e_ccd"])
+
+
+def test_mixed_complex_matches_real_engine(ccx):
+    """The same real problem through a complex engine: identical energies to rounding."""
+    L = ccx.Layout.from_basis(2, 14, 0.08)
+    er = ccx.Engine(L, real=True)
+    ec = ccx.Engine(L, real=False)
+    for e in (er, ec):
+        e.generate()
+        e.setup_t_amplitudes()
+    rr = er.ccd_iter(mode=ccx.MODE_STANDARD, precision=ccx.PREC_MIXED, tol=1e-10, max_iter=200,
+                     rebase=ccx.REBASE_DIGITS)
+    rc = ec.ccd_iter(mode=ccx.MODE_STANDARD, precision=ccx.PREC_MIXED, tol=1e-10, max_iter=200,
+                     rebase=ccx.REBASE_DIGITS)
+    assert rr["converged"] and rc["converged"]
+    assert abs(rc["e_ccd"] - rr["e_ccd"]) < 1e-10 * abs(rr["e_ccd"])
+
+
 def test_mixed_rejects_unsupported(ccx):
     L = ccx.Layout.from_basis(1, 2, 0.08)
-    ec = ccx.Engine(L, real=False)
-    ec.generate()
-    ec.setup_t_amplitudes()
-    with pytest.raises(ccx.CcxError):
-        ec.ccd_iter(mode=ccx.MODE_STANDARD, precision=ccx.PREC_MIXED)
     er = ccx.Engine(L, real=True)
     er.generate()
     er.setup_t_amplitudes()
