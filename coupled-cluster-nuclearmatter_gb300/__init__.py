@@ -133,6 +133,7 @@ def lib():
         "ccx_ccd_energy_noalloc": ([i32, vp, vp, vp, vp, vp], C.c_int),
         "ccx_engine_kernel_timers": ([vp, vp, vp], C.c_int),
         "ccx_set_vblocks": ([vp, i32, i32, vp, vp], C.c_int),
+        "ccx_ccd_iter_batch": ([vp, i32, vp, vp, C.POINTER(C.c_double)], C.c_int),
         "ccx_learner_create": ([i32, C.c_uint64, C.POINTER(vp)], C.c_int),
         "ccx_learner_destroy": ([vp], C.c_int),
         "ccx_learner_add_solution": ([vp, vp], C.c_int),
@@ -191,6 +192,24 @@ def ccd_energy_noalloc(nch: int, dims_ptr: int, t2_ptr: int, vhhpp_ptr: int, ene
     """ccx_ccd_energy_noalloc on caller-owned device buffers (raw device pointers)."""
     _check(lib().ccx_ccd_energy_noalloc(nch, vp(dims_ptr), vp(t2_ptr), vp(vhhpp_ptr), vp(energy_ptr),
                                         vp(stream) if stream else None))
+
+
+def ccd_iter_batch(engines, mode=MODE_STANDARD, precision=PREC_FP64, max_iter=200, tol=1e-10, diis_dim=8,
+                   defect_period=0, verbose=False, rebase=REBASE_FP64):
+    """Solve several engines (e.g. twists) together in lockstep; returns (results, seconds)."""
+    n = len(engines)
+    hs = (vp * n)(*[e._h for e in engines])
+    o = _IterOpts(mode, precision, max_iter, tol, diis_dim, defect_period, int(verbose), rebase)
+    rs = (_IterResult * n)()
+    sec = C.c_double()
+    _check(lib().ccx_ccd_iter_batch(hs, n, C.byref(o), rs, C.byref(sec)))
+    out = []
+    for r in rs:
+        out.append({"iterations": r.iterations, "converged": bool(r.converged),
+                    "e_mbpt2": complex(r.e_mbpt2[0], r.e_mbpt2[1]), "e_ccd": complex(r.e_ccd[0], r.e_ccd[1]),
+                    "res_norm": r.res_norm, "seconds": r.seconds, "fp64_sweeps": r.fp64_sweeps,
+                    "mixed_iterations": r.mixed_iterations})
+    return out, sec.value
 
 
 ML_FEATURES, ML_PARAMS = 16, 35329

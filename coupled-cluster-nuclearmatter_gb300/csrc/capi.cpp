@@ -3,6 +3,7 @@
 #include <cctype>
 #include <cstdio>
 #include <cstdlib>
+#include <chrono>
 #include <cstring>
 #include <memory>
 #include <sstream>
@@ -355,6 +356,65 @@ int ccx_engine_launches(const ccx_engine *e, int64_t *n) {
 int ccx_engine_timers(const ccx_engine *e, double ms[10]) {
   if (!ms) return fail(CCX_EINVAL, "null argument");
   ENGINE_CALL(e, e->E->timers(ms));
+}
+int ccx_ccd_iter_batch(ccx_engine *const *engines, int32_t n, const ccx_iter_opts *opt, ccx_iter_result *res,
+                       double *seconds) {
+  if (!engines || !opt || !res || n < 1) return fail(CCX_EINVAL, "bad batch arguments");
+  for (int32_t i = 0; i < n; ++i)
+    if (!engines[i]) return fail(CCX_EINVAL, "null engine in the batch");
+  return guard([&] {
+    ccx::IterOpts o;
+    o.mode = opt->mode;
+    o.precision = opt->precision;
+    o.max_iter = opt->max_iter;
+    o.tol = opt->tol;
+    o.diis_dim = opt->diis_dim;
+    o.defect_period = opt->defect_period;
+    o.verbose = opt->verbose;
+    o.rebase = opt->rebase;
+    std::vector<ccx::IterResult> rr(n);
+    std::vector<ccx::IEngine *> act;
+    for (int32_t i = 0; i < n; ++i) {
+      engines[i]->E->set_timing(false);
+      engines[i]->E->std_begin(o, rr[i]);
+      if (!engines[i]->E->std_done()) act.push_back(engines[i]->E.get());
+    }
+    const auto t0 = std::chrono::steady_clock::now();
+    // lockstep: every engine's launches go to its own stream, so the GPU overlaps the
+    // engines; one host synchronisation per step for the whole batch
+    while (!act.empty()) {
+      for (auto *e : act) {
+        e->std_launch_residual();
+        e->std_launch_update();
+      }
+      std::vector<ccx::IEngine *> next;
+      for (auto *e : act) e->sync();
+      for (auto *e : act)
+        if (!e->std_after_update()) next.push_back(e);
+      for (auto *e : next) e->std_launch_dots();
+      for (auto *e : next) e->sync();
+      act.clear();
+      for (auto *e : next) {
+        e->std_after_dots();
+        if (!e->std_done()) act.push_back(e);
+      }
+    }
+    const double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    for (int32_t i = 0; i < n; ++i) {
+      ccx_iter_result &x = res[i];
+      x.iterations = rr[i].iterations;
+      x.converged = rr[i].converged;
+      x.e_mbpt2[0] = rr[i].e_mbpt2[0];
+      x.e_mbpt2[1] = rr[i].e_mbpt2[1];
+      x.e_ccd[0] = rr[i].e_ccd[0];
+      x.e_ccd[1] = rr[i].e_ccd[1];
+      x.res_norm = rr[i].res_norm;
+      x.seconds = dt;
+      x.fp64_sweeps = rr[i].fp64_sweeps;
+      x.mixed_iterations = rr[i].mixed_iterations;
+    }
+    if (seconds) *seconds = dt;
+  });
 }
 int ccx_learner_create(int32_t device, uint64_t seed, ccx_learner **out) {
   if (!out) return fail(CCX_EINVAL, "null argument");

@@ -488,10 +488,12 @@ class Engine final : public IEngine {
     if (o.rebase < 0 || o.rebase > 1) throw EngineError(1, "unknown re-base product kind");
     if (o.precision != 0 && o.mode != 1) throw EngineError(1, "mixed precision runs with the standard (DIIS) mode");
     r = IterResult();
-    double e[2];
-    energy(e);
-    r.e_mbpt2[0] = e[0];
-    r.e_mbpt2[1] = e[1];
+    if (o.mode == 0) {
+      double e[2];
+      energy(e);
+      r.e_mbpt2[0] = e[0];
+      r.e_mbpt2[1] = e[1];
+    }
     for (double &t : timers_) t = 0.0;
     for (double &t : ktimers_) t = 0.0;
     for (int64_t &c : kcount_) c = 0;
@@ -1060,114 +1062,181 @@ class Engine final : public IEngine {
   // T - T_b (defect correction); an FP64 residual re-bases T_b when the mixed residual
   // has dropped by kRebaseDrop since the last FP64 one, stalls, reaches the tolerance,
   // or every defect_period iterations, and only an FP64 residual can end the solve.
-  void iterate_standard(const IterOpts &o, IterResult &r) {
-    const bool mixed = o.precision != 0;
-    constexpr double kRebaseDrop = 1e-4;
-    if (mixed) {
+  //
+  // The loop is a state machine so that a batch of engines can run it in lockstep:
+  //   std_begin; repeat { std_launch_residual; std_launch_update; [sync]
+  //   std_after_update (true: finished); std_launch_dots; [sync] std_after_dots }.
+  struct StdState {
+    IterOpts o;
+    IterResult *r = nullptr;
+    bool mixed = false, need_fp64 = false, exact = false, done = false;
+    int m = 8, nh = 0, head = 0, it = 0, stall = 0, since = 0;
+    double e[2] = {0, 0}, phase_r0 = -1.0, best = 1e300;
+    std::vector<double> B;
+    S *ht = nullptr, *he = nullptr;
+  };
+  StdState ss_;
+  static constexpr double kRebaseDrop = 1e-4;
+
+  void std_begin(const IterOpts &o, IterResult &r) override {
+    require_ready();
+    if (o.precision < 0 || o.precision > 2) throw EngineError(1, "unknown precision");
+    if (o.rebase < 0 || o.rebase > 1) throw EngineError(1, "unknown re-base product kind");
+    if (o.mode != 1) throw EngineError(1, "the batched iteration runs the standard (DIIS) mode");
+    r = IterResult();
+    double e0[2];
+    energy(e0);
+    r.e_mbpt2[0] = e0[0];
+    r.e_mbpt2[1] = e0[1];
+    StdState &s = ss_;
+    s = StdState();
+    s.o = o;
+    s.r = &r;
+    s.mixed = o.precision != 0;
+    if (s.mixed) {
       prepare_mixed(o.precision == 2 ? kTcTF32 : kTcBF16);
       if (o.rebase == 1) prepare_oz();
       set_base_zero();
     }
-    const int m = std::max(2, std::min(o.diis_dim, 15));
-    hist_t_.alloc((size_t)m * n_t_ * sizeof(S), &bytes_);
-    hist_e_.alloc((size_t)m * n_t_ * sizeof(S), &bytes_);
-    std::vector<double> B((size_t)m * m, 0.0);
-    int nh = 0, head = 0;
-    double e[2] = {r.e_mbpt2[0], r.e_mbpt2[1]};
-    bool need_fp64 = false;
-    double phase_r0 = -1.0, best = 1e300;
-    int stall = 0, since = 0;
-    for (int it = 1; it <= o.max_iter; ++it) {
-      const bool exact = !mixed || need_fp64;
-      if (!mixed) residual(true);
-      else if (exact) {
-        residual_fp64_rebase(o.rebase == 1);
-        ++r.fp64_sweeps;
-      } else {
-        residual_mixed();
-        ++r.mixed_iterations;
-      }
-      S *ht = hist_t_.as<S>() + (int64_t)head * n_t_;
-      S *he = hist_e_.as<S>() + (int64_t)head * n_t_;
-      mark(7);
-      launch_update<S>(D_, 1, T_.as<S>(), R_.as<S>(), Vhp_.as<S>(), d2ij_.as<S>(), d2ab_.as<S>(), ht, he,
-                       partial_.as<double>(), res_.as<double>(), st_);
-      launches_ += 2;
-      // the tensor-core error word rides on the same synchronisation as the energy
-      int *tc_word = (int *)(host_res_ + 63);
-      if (mixed) CK(cudaMemcpyAsync(tc_word, tcerr_.p, sizeof(int), cudaMemcpyDeviceToHost, st_));
-      fetch_res(3);
-      mark(8);
-      if (timing_) accumulate_timers(7, 8);
-      e[0] = host_res_[0];
-      e[1] = host_res_[1];
-      const double rn = 2.0 * std::sqrt(host_res_[2]);
-      if (mixed && *tc_word) {
-        const int err = *tc_word;
-        CK(cudaMemsetAsync(tcerr_.p, 0, sizeof(int), st_));
-        throw EngineError(2, "tensor-core GEMM reported error code " + std::to_string(err));
-      }
-      if (exact) r.res_norm = rn;
-      r.iterations = it - 1;
-      if (o.verbose) std::printf("ccx it %3d %s |R| %.3e E %.12f\n", it, exact ? "fp64 " : "mixed", rn, e[0]);
-      if (exact && rn < o.tol) { r.converged = 1; break; }
-      if (mixed) {
-        if (exact) {
-          need_fp64 = false;
-          phase_r0 = rn;
-          best = rn;
-          stall = 0;
-          since = 0;
-        } else {
-          ++since;
-          if (phase_r0 < 0) phase_r0 = rn;
-          if (rn < 0.9 * best) { best = rn; stall = 0; } else ++stall;
-          const bool periodic = o.defect_period > 0 && since >= o.defect_period;
-          const bool dropped = o.defect_period <= 0 && rn < kRebaseDrop * phase_r0;
-          if (rn < o.tol || stall >= 2 || periodic || dropped) need_fp64 = true;
-        }
-      }
-      // Gram row of the new step against every stored step, with conjugation
-      const int slot = head;
-      if (nh < m) ++nh;
-      std::vector<const S *> es(nh);
-      for (int j = 0; j < nh; ++j) es[j] = hist_e_.as<S>() + (int64_t)j * n_t_;
-      launch_dots<S>(n_t_, he, es.data(), nh, 1, partial_.as<double>(), res_.as<double>(), st_);
-      launches_ += 2;
-      CK(cudaMemcpyAsync(host_res_, res_.p, 2 * nh * sizeof(double), cudaMemcpyDeviceToHost, st_));
-      CK(cudaStreamSynchronize(st_));
-      for (int j = 0; j < nh; ++j) { B[slot + (size_t)m * j] = host_res_[2 * j]; B[j + (size_t)m * slot] = host_res_[2 * j]; }
-      head = (head + 1) % m;
-      std::vector<double> coef;
-      bool ok = false;
-      if (nh >= 2) {
-        const int n1 = nh + 1;
-        std::vector<double> Bm((size_t)n1 * n1, 0.0), rhs(n1, 0.0);
-        for (int i = 0; i < nh; ++i)
-          for (int j = 0; j < nh; ++j) Bm[i + (size_t)n1 * j] = B[i + (size_t)m * j];
-        for (int i = 0; i < nh; ++i) { Bm[i + (size_t)n1 * nh] = -1.0; Bm[nh + (size_t)n1 * i] = -1.0; }
-        rhs[nh] = -1.0;
-        ok = dsolve(n1, Bm, rhs);
-        if (ok) {
-          coef.resize(2 * nh);
-          for (int i = 0; i < nh; ++i) { coef[2 * i] = rhs[i]; coef[2 * i + 1] = 0.0; }
-        }
-      }
-      mark(8);
-      if (ok) {
-        std::vector<const S *> ts(nh);
-        for (int j = 0; j < nh; ++j) ts[j] = hist_t_.as<S>() + (int64_t)j * n_t_;
-        launch_combine<S>(n_t_, ts.data(), coef.data(), nh, T_.as<S>(), st_);
-      } else {
-        CK(cudaMemcpyAsync(T_.p, ht, n_t_ * sizeof(S), cudaMemcpyDeviceToDevice, st_));
-      }
-      ++launches_;
-      mark(9);
-      if (timing_) accumulate_timers(8, 9);
-      r.iterations = it;
+    s.m = std::max(2, std::min(o.diis_dim, 15));
+    hist_t_.alloc((size_t)s.m * n_t_ * sizeof(S), &bytes_);
+    hist_e_.alloc((size_t)s.m * n_t_ * sizeof(S), &bytes_);
+    s.B.assign((size_t)s.m * s.m, 0.0);
+    s.e[0] = r.e_mbpt2[0];
+    s.e[1] = r.e_mbpt2[1];
+    s.done = o.max_iter < 1;
+  }
+  bool std_done() const override { return ss_.done; }
+  void std_launch_residual() override {
+    StdState &s = ss_;
+    ++s.it;
+    s.exact = !s.mixed || s.need_fp64;
+    if (!s.mixed) residual(true);
+    else if (s.exact) {
+      residual_fp64_rebase(s.o.rebase == 1);
+      ++s.r->fp64_sweeps;
+    } else {
+      residual_mixed();
+      ++s.r->mixed_iterations;
     }
-    r.e_ccd[0] = e[0];
-    r.e_ccd[1] = e[1];
+  }
+  void std_launch_update() override {
+    StdState &s = ss_;
+    s.ht = hist_t_.as<S>() + (int64_t)s.head * n_t_;
+    s.he = hist_e_.as<S>() + (int64_t)s.head * n_t_;
+    mark(7);
+    launch_update<S>(D_, 1, T_.as<S>(), R_.as<S>(), Vhp_.as<S>(), d2ij_.as<S>(), d2ab_.as<S>(), s.ht, s.he,
+                     partial_.as<double>(), res_.as<double>(), st_);
+    launches_ += 2;
+    // the tensor-core error word rides on the same synchronisation as the energy
+    if (s.mixed) CK(cudaMemcpyAsync((int *)(host_res_ + 63), tcerr_.p, sizeof(int), cudaMemcpyDeviceToHost, st_));
+    CK(cudaMemcpyAsync(host_res_, res_.p, 3 * sizeof(double), cudaMemcpyDeviceToHost, st_));
+  }
+  bool std_after_update() override {
+    StdState &s = ss_;
+    IterResult &r = *s.r;
+    if (!std::isfinite(host_res_[0]) || !std::isfinite(host_res_[1]))
+      throw EngineError(5, "non-finite energy: the iteration diverged or the input holds NaN/Inf");
+    mark(8);
+    if (timing_) accumulate_timers(7, 8);
+    s.e[0] = host_res_[0];
+    s.e[1] = host_res_[1];
+    const double rn = 2.0 * std::sqrt(host_res_[2]);
+    const int *tc_word = (const int *)(host_res_ + 63);
+    if (s.mixed && *tc_word) {
+      const int err = *tc_word;
+      CK(cudaMemsetAsync(tcerr_.p, 0, sizeof(int), st_));
+      throw EngineError(2, "tensor-core GEMM reported error code " + std::to_string(err));
+    }
+    if (s.exact) r.res_norm = rn;
+    r.iterations = s.it - 1;
+    r.e_ccd[0] = s.e[0];
+    r.e_ccd[1] = s.e[1];
+    if (s.o.verbose) std::printf("ccx it %3d %s |R| %.3e E %.12f\n", s.it, s.exact ? "fp64 " : "mixed", rn, s.e[0]);
+    if (s.exact && rn < s.o.tol) {
+      r.converged = 1;
+      s.done = true;
+      return true;
+    }
+    if (s.mixed) {
+      if (s.exact) {
+        s.need_fp64 = false;
+        s.phase_r0 = rn;
+        s.best = rn;
+        s.stall = 0;
+        s.since = 0;
+      } else {
+        ++s.since;
+        if (s.phase_r0 < 0) s.phase_r0 = rn;
+        if (rn < 0.9 * s.best) { s.best = rn; s.stall = 0; } else ++s.stall;
+        const bool periodic = s.o.defect_period > 0 && s.since >= s.o.defect_period;
+        const bool dropped = s.o.defect_period <= 0 && rn < kRebaseDrop * s.phase_r0;
+        if (rn < s.o.tol || s.stall >= 2 || periodic || dropped) s.need_fp64 = true;
+      }
+    }
+    return false;
+  }
+  // Gram row of the new step against every stored step, with conjugation
+  void std_launch_dots() override {
+    StdState &s = ss_;
+    if (s.nh < s.m) ++s.nh;
+    std::vector<const S *> es(s.nh);
+    for (int j = 0; j < s.nh; ++j) es[j] = hist_e_.as<S>() + (int64_t)j * n_t_;
+    launch_dots<S>(n_t_, s.he, es.data(), s.nh, 1, partial_.as<double>(), res_.as<double>(), st_);
+    launches_ += 2;
+    CK(cudaMemcpyAsync(host_res_, res_.p, 2 * s.nh * sizeof(double), cudaMemcpyDeviceToHost, st_));
+  }
+  void std_after_dots() override {
+    StdState &s = ss_;
+    const int m = s.m, nh = s.nh, slot = s.head;
+    for (int j = 0; j < nh; ++j) {
+      s.B[slot + (size_t)m * j] = host_res_[2 * j];
+      s.B[j + (size_t)m * slot] = host_res_[2 * j];
+    }
+    s.head = (s.head + 1) % m;
+    std::vector<double> coef;
+    bool ok = false;
+    if (nh >= 2) {
+      const int n1 = nh + 1;
+      std::vector<double> Bm((size_t)n1 * n1, 0.0), rhs(n1, 0.0);
+      for (int i = 0; i < nh; ++i)
+        for (int j = 0; j < nh; ++j) Bm[i + (size_t)n1 * j] = s.B[i + (size_t)m * j];
+      for (int i = 0; i < nh; ++i) { Bm[i + (size_t)n1 * nh] = -1.0; Bm[nh + (size_t)n1 * i] = -1.0; }
+      rhs[nh] = -1.0;
+      ok = dsolve(n1, Bm, rhs);
+      if (ok) {
+        coef.resize(2 * nh);
+        for (int i = 0; i < nh; ++i) { coef[2 * i] = rhs[i]; coef[2 * i + 1] = 0.0; }
+      }
+    }
+    mark(8);
+    if (ok) {
+      std::vector<const S *> ts(nh);
+      for (int j = 0; j < nh; ++j) ts[j] = hist_t_.as<S>() + (int64_t)j * n_t_;
+      launch_combine<S>(n_t_, ts.data(), coef.data(), nh, T_.as<S>(), st_);
+    } else {
+      CK(cudaMemcpyAsync(T_.p, s.ht, n_t_ * sizeof(S), cudaMemcpyDeviceToDevice, st_));
+    }
+    ++launches_;
+    mark(9);
+    if (timing_) accumulate_timers(8, 9);
+    s.r->iterations = s.it;
+    if (s.it >= s.o.max_iter) s.done = true;
+  }
+  void sync() override { CK(cudaStreamSynchronize(st_)); }
+  void set_timing(bool on) override { timing_ = on; }
+
+  void iterate_standard(const IterOpts &o, IterResult &r) {
+    std_begin(o, r);
+    while (!ss_.done) {
+      std_launch_residual();
+      std_launch_update();
+      sync();
+      if (std_after_update()) break;
+      std_launch_dots();
+      sync();
+      std_after_dots();
+    }
   }
 
   // ================================================================== mixed precision

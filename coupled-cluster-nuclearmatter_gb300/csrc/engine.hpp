@@ -86,6 +86,17 @@ class IEngine {
   virtual double residual_norm() = 0;
   virtual void ccd_iter(const IterOpts &o, IterResult &r) = 0;
   virtual void triples(double et[2]) = 0;
+  // standard-mode iteration as a state machine (see Engine::iterate_standard), for
+  // solving several engines in lockstep
+  virtual void std_begin(const IterOpts &o, IterResult &r) = 0;
+  virtual bool std_done() const = 0;
+  virtual void std_launch_residual() = 0;
+  virtual void std_launch_update() = 0;
+  virtual bool std_after_update() = 0;
+  virtual void std_launch_dots() = 0;
+  virtual void std_after_dots() = 0;
+  virtual void sync() = 0;
+  virtual void set_timing(bool on) = 0;
   // device view for the learned warm start (real engines only; false for complex)
   virtual bool ml_view(MLView &v, bool need_t) = 0;
   virtual void mark_t_set() = 0;

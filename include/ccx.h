@@ -276,6 +276,14 @@ typedef struct {
 
 /* ccd_iter loop, ccm_iter.f90:67-133 */
 int ccx_ccd_iter(ccx_engine *e, const ccx_iter_opts *opt, ccx_iter_result *res);
+/* n engines on one device (for example the twists of a twist-averaged run,
+ * ccm_main.f90:163-279, which the reference solves one after the other) solved
+ * together in the standard mode: the iterations run in lockstep, each engine's kernels
+ * on its own stream so that the GPU overlaps the engines, with one host
+ * synchronisation per step for the whole batch.  res[i] is engine i's result; every
+ * res[i].seconds and *seconds hold the wall time of the whole batch. */
+int ccx_ccd_iter_batch(ccx_engine *const *engines, int32_t n, const ccx_iter_opts *opt, ccx_iter_result *res,
+                       double *seconds);
 
 /* ---- (T) -------------------------------------------------------------- */
 /* pert_triples2, ccm_triples.f90:528-735 (NN part): E(T) from the current T2 with
