@@ -215,6 +215,22 @@ KERNEL_NAMES = {"x_fp64": "k_gemm<double> X = V_hhpp' T' (split-K)", "i4_fp64": 
                 "ring_rebase_digits": "k_oz_gemm ring at a re-base (exact digit products)"}
 
 
+def replica_theta(rank: int):
+    """Twist of a replica: rank 0 solves the untwisted lattice, the others their own
+    twist (replicas, no data exchange between ranks)."""
+    return (0.0, 0.0, 0.0) if rank == 0 else (0.1 * rank, -0.07 * rank, 0.05 * rank)
+
+
+def max_over_ranks(value: float, dist, device) -> float:
+    """The slowest rank's time: all_reduce MAX (the only collective of the bench)."""
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def run_ours(args, wl):
     import torch
     ccx = load_pkg()
@@ -226,13 +242,14 @@ def run_ours(args, wl):
         import torch.distributed as dist
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
-    # each rank solves its own twist of the lattice (replicas, no data exchange)
-    theta = (0.0, 0.0, 0.0) if rank == 0 else (0.1 * rank, -0.07 * rank, 0.05 * rank)
+    theta = replica_theta(rank)
     L = ccx.Layout.from_basis(wl["nmax"], wl["A"], wl["rho"], snm=wl["snm"], theta=theta)
     real = wl["potential"] == ccx.POT_MINNESOTA
     prec = PRECISIONS[args.precision] if real else 0
     e = ccx.Engine(L, device=local, real=real)
     e.generate(potential=wl["potential"])
+    e.setup_t_amplitudes()
+    tuned_shapes, _ = e.autotune()  # FP64 GEMM tile shape per column-count bucket
     stream = torch.cuda.ExternalStream(e.stream(), device=local)
     P, H, ring = packed_sizes(L, ccx)
     flops = flop_model(P, H, ring, real=real)
@@ -265,10 +282,7 @@ def run_ours(args, wl):
         torch.cuda.synchronize()
         clk = clocks.stop() if clocks else None
         ms = ev0.elapsed_time(ev1) / steps
-        if dist:
-            t = torch.tensor([ms], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
+        ms = max_over_ranks(ms, dist, "cuda")
         return ms, results, timers, ktimers, e.launches() - launches0, clk
 
     # warm-up: both forms (tensor-core tiles are prepared by the first mixed solve)
@@ -327,6 +341,7 @@ def run_ours(args, wl):
                        "precision": args.precision if prec else "fp64",
                        "defect_period": args.defect_period or "adaptive",
                        "rebase": args.rebase if prec else None,
+                       "gemm_tile_shapes_by_N_bucket": tuned_shapes,
                        "l2": "inputs larger than L2 (V_pppp packed, %.2f GB, read every iteration)"
                              % (sum(p * p for p in P) * 8 / 1e9),
                        "replicas": world},
@@ -416,6 +431,8 @@ def run_e2e(args, ccx, torch, L, e, local, real, solve):
 
     for _ in range(max(1, args.warmup // 2)):
         step()
+    eb.autotune()  # once per engine, as a host would after handing over the interaction
+    step()
     torch.cuda.synchronize()
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
@@ -434,6 +451,76 @@ def run_e2e(args, ccx, torch, L, e, local, real, solve):
                     "ccx_setup_t_amplitudes + ccx_ccd_iter + ccx_get_t2_all"}
 
 
+TWIST_LATTICES = {
+    "pnm66": dict(nmax=4, A=66, rho=0.16, snm=False, desc="PNM A=66, rho=0.16 fm^-3, nmax=4 (1458 states), Minnesota"),
+    "snm132n3": dict(nmax=3, A=132, rho=0.16, snm=True, desc="SNM A=132, rho=0.16 fm^-3, nmax=3 (1372 states), Minnesota"),
+}
+
+
+def gauss_legendre_twists():
+    """4 x 4 x 4 Gauss-Legendre product grid on [-pi, pi]^3 with its weights (sum 1)."""
+    import itertools
+    import math
+    x = (-0.8611363115940526, -0.3399810435848563, 0.3399810435848563, 0.8611363115940526)
+    w = (0.3478548451374538, 0.6521451548625461, 0.6521451548625461, 0.3478548451374538)
+    out = []
+    for (xa, wa), (xb, wb), (xc, wc) in itertools.product(zip(x, w), repeat=3):
+        out.append(((math.pi * xa, math.pi * xb, math.pi * xc), wa * wb * wc / 8.0))
+    return out
+
+
+def run_twists(args):
+    """Twist batch: the same lattice at N twists, solved as one lockstep batch
+    (ccx_ccd_iter_batch) against a per-twist sequential loop (ccx_ccd_iter), both in the
+    mixed form with digit-product re-bases, MP2 start, ||R - D T|| < tol."""
+    import torch
+    ccx = load_pkg()
+    lat = TWIST_LATTICES[args.lattice]
+    grid = gauss_legendre_twists()
+    # a spread subset when fewer than 64 twists are asked for
+    step = max(1, len(grid) // args.twists)
+    grid = grid[::step][:args.twists]
+    prec = PRECISIONS[args.precision]
+    rb = ccx.REBASE_DIGITS if (prec and args.rebase == "digits") else ccx.REBASE_FP64
+    opts = dict(precision=prec, rebase=rb, tol=args.tol, max_iter=200, diis_dim=8)
+    engines = []
+    for th, _ in grid:
+        L = ccx.Layout.from_basis(lat["nmax"], lat["A"], lat["rho"], snm=lat["snm"], theta=th)
+        e = ccx.Engine(L, real=True)
+        e.generate()
+        e.setup_t_amplitudes()
+        e.ccd_iter(mode=ccx.MODE_STANDARD, **opts)  # warm-up: operand tiles and digit planes
+        engines.append(e)
+    seq, bat = [], []
+    for _ in range(args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        rs = []
+        for e in engines:
+            e.setup_t_amplitudes()
+            rs.append(e.ccd_iter(mode=ccx.MODE_STANDARD, **opts))
+        torch.cuda.synchronize()
+        seq.append(time.perf_counter() - t0)
+        t0 = time.perf_counter()
+        for e in engines:
+            e.setup_t_amplitudes()
+        rb_, _ = ccx.ccd_iter_batch(engines, **opts)
+        torch.cuda.synchronize()
+        bat.append(time.perf_counter() - t0)
+    wsum = sum(w for _, w in grid)
+    ea = sum(w * (e.e0() + r["e_ccd"]).real / lat["A"] for (_, w), e, r in zip(grid, engines, rb_)) / wsum
+    ea_seq = sum(w * (e.e0() + r["e_ccd"]).real / lat["A"] for (_, w), e, r in zip(grid, engines, rs)) / wsum
+    line = {"metric": "time to converged twist-averaged E/A", "impl": "ours", "workload": "twist batch",
+            "lattice": lat["desc"], "twists": len(grid), "form": args.precision + " + " + args.rebase + " re-base",
+            "batched_s": statistics.median(bat), "sequential_s": statistics.median(seq),
+            "speedup_batched_vs_sequential": statistics.median(seq) / statistics.median(bat),
+            "iterations": [r["iterations"] for r in rb_], "E_per_A_twist_averaged_MeV": ea,
+            "dE_per_A_keV_batched_vs_sequential": abs(ea - ea_seq) * 1e3, "steps": args.steps,
+            "device_GB_per_engine": engines[0].memory() / 1e9}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -444,12 +531,17 @@ def main():
     ap.add_argument("--tol", type=float, default=1e-10)
     ap.add_argument("--precision", default="bf16x3", choices=sorted(PRECISIONS))
     ap.add_argument("--defect-period", type=int, default=0, help="FP64 re-base every k iterations (0: adaptive)")
+    ap.add_argument("--twists", type=int, default=0,
+                    help="run the twist-batch comparison with this many twists instead of the headline")
+    ap.add_argument("--lattice", default="pnm66", choices=sorted(TWIST_LATTICES))
     ap.add_argument("--rebase", default="digits", choices=["fp64", "digits"],
                     help="pp-ladder product of a re-base: FP64 FMA GEMM or exact digit products on the tensor cores")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     wl = WORKLOADS[args.workload]
+    if args.twists > 0 and args.impl == "ours":
+        return run_twists(args)
     if args.impl == "reference":
         return run_reference(args, wl)
     return run_ours(args, wl)

@@ -134,6 +134,7 @@ def lib():
         "ccx_engine_kernel_timers": ([vp, vp, vp], C.c_int),
         "ccx_set_vblocks": ([vp, i32, i32, vp, vp], C.c_int),
         "ccx_ccd_iter_batch": ([vp, i32, vp, vp, C.POINTER(C.c_double)], C.c_int),
+        "ccx_engine_autotune": ([vp, vp, vp], C.c_int),
         "ccx_learner_create": ([i32, C.c_uint64, C.POINTER(vp)], C.c_int),
         "ccx_learner_destroy": ([vp], C.c_int),
         "ccx_learner_add_solution": ([vp, vp], C.c_int),
@@ -533,6 +534,13 @@ class Engine:
     KERNEL_SLOTS = ("x_fp64", "i4_fp64", "ring_fp64", "ladder_fp64", "pp_rebase_fp64", "hh_fp64",
                     "pp_tc", "i4_tc", "ring_tc", "split", "pp_rebase_digits", "i4_rebase_digits",
                     "ring_rebase_digits")
+
+    def autotune(self):
+        """Pick the FP64 GEMM tile shape per N bucket by timing; returns (shapes, ms)."""
+        s = np.zeros(4, np.int32)
+        ms = np.zeros(8)
+        _check(lib().ccx_engine_autotune(self._h, _ptr(s), _ptr(ms)))
+        return s.tolist(), ms.reshape(4, 2).tolist()
 
     def kernel_timers(self) -> dict:
         """{slot: (total ms, timed brackets)} of individual launches in the last ccd_iter."""

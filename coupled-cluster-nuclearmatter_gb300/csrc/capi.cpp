@@ -357,6 +357,14 @@ int ccx_engine_timers(const ccx_engine *e, double ms[10]) {
   if (!ms) return fail(CCX_EINVAL, "null argument");
   ENGINE_CALL(e, e->E->timers(ms));
 }
+int ccx_engine_autotune(ccx_engine *e, int32_t shapes[4], double ms[8]) {
+  if (!shapes || !ms) return fail(CCX_EINVAL, "null argument");
+  ENGINE_CALL(e, {
+    int s[4];
+    e->E->autotune(s, ms);
+    for (int k = 0; k < 4; ++k) shapes[k] = s[k];
+  });
+}
 int ccx_ccd_iter_batch(ccx_engine *const *engines, int32_t n, const ccx_iter_opts *opt, ccx_iter_result *res,
                        double *seconds) {
   if (!engines || !opt || !res || n < 1) return fail(CCX_EINVAL, "bad batch arguments");

@@ -791,13 +791,18 @@ class Engine final : public IEngine {
     DBuf probs, tiles[2], splits;
     int ntiles[2] = {0, 0}, nsplit = 0;
   };
+  // N buckets of the tile-shape choice: N <= 16, <= 32, <= 64, > 64
+  static int n_bucket(int N) { return N <= 16 ? 0 : N <= 32 ? 1 : N <= 64 ? 2 : 3; }
   struct PlanBuilder {
+    const int *shape_of = nullptr;  // tile shape per N bucket
+    int only_bucket = -1;           // >= 0: keep only the problems of this bucket
     std::vector<GemmProb<S>> probs;
     std::vector<GemmTile> tiles[2];
     std::vector<int> splits;
     std::vector<int64_t> work;
     void add(GemmProb<S> p, int64_t w) {
-      const int shape = p.N <= 32 ? kShape128x32 : kShape64x64;
+      if (only_bucket >= 0 && n_bucket(p.N) != only_bucket) return;
+      const int shape = shape_of ? shape_of[n_bucket(p.N)] : (p.N <= 32 ? kShape128x32 : kShape64x64);
       const int bm = gemm_bm(shape), bn = gemm_bn(shape);
       const int id = (int)probs.size();
       const int nsl = p.kchunk > 0 ? (p.seg[0].K + p.kchunk - 1) / p.kchunk : 1;
@@ -860,8 +865,17 @@ class Engine final : public IEngine {
       upload(xwork_, w, &bytes_);
       nxwork_ = (int)w.size();
     }
+    build_fp64_plans(planLadder_, planI4_, planRing_, -1, nullptr);
+  }
+  // The grouped FP64 GEMM plans of the residual; bucket >= 0 keeps only the problems of
+  // that N bucket, shapes overrides the engine's tile shape per bucket.
+  void build_fp64_plans(Plan &ladder, Plan &i4, Plan &ring, int bucket, const int *shapes) {
+    const Layout &L = *L_;
+    const int nc = L.fam[3].count();
     {  // R' += V_pppp' T' + T' I9'
       PlanBuilder b;
+      b.shape_of = shapes ? shapes : gemm_shape_;
+      b.only_bucket = bucket;
       int64_t hoff = 0, voff = 0;
       for (int c = 0; c < nc; ++c) {
         const auto &pk = L.pk[c];
@@ -877,10 +891,12 @@ class Engine final : public IEngine {
         hoff += (int64_t)pk.H * pk.H;
         voff += (int64_t)pk.P * pk.P;
       }
-      finalize_plan(planLadder_, b);
+      finalize_plan(ladder, b);
     }
     {  // I4 = W + 1/2 V_ph T_ph ; R_ph = T_ph I4
       PlanBuilder b4, br;
+      b4.shape_of = br.shape_of = shapes ? shapes : gemm_shape_;
+      b4.only_bucket = br.only_bucket = bucket;
       int64_t toff = 0, ioff = 0;
       for (int q = 0; q < L.ph[1].count(); ++q) {
         const int nph = L.ph[1].side1[q].size(), nhp = L.ph[1].side2[q].size();
@@ -901,9 +917,54 @@ class Engine final : public IEngine {
         toff += (int64_t)nph * nhp;
         ioff += (int64_t)nhp * nhp;
       }
-      finalize_plan(planI4_, b4);
-      finalize_plan(planRing_, br);
+      finalize_plan(i4, b4);
+      finalize_plan(ring, br);
     }
+  }
+
+  // Autotuner of the grouped FP64 GEMM: for each N bucket, time the residual's ladder,
+  // I4 and ring problems of that bucket with each tile shape (best of 3 launches, CUDA
+  // events on the engine stream), keep the faster shape and rebuild every plan.  The
+  // timed launches only write buffers that each residual evaluation rewrites.
+  void autotune(int shapes[4], double ms[8]) override {
+    require_ready();
+    cudaEvent_t a, b;
+    CK(cudaEventCreate(&a));
+    CK(cudaEventCreate(&b));
+    const int64_t held = bytes_;  // the trial plans are freed again below
+    for (int k = 0; k < 4; ++k) {
+      double best = 1e300;
+      int pick = gemm_shape_[k];
+      for (int sh = 0; sh < 2; ++sh) {
+        const int tab[4] = {sh, sh, sh, sh};
+        Plan pl, p4, pr;
+        build_fp64_plans(pl, p4, pr, k, tab);
+        double t = 0.0;
+        for (const Plan *p : {&pl, &p4, &pr}) {
+          float tbest = 1e30f;
+          for (int rep = 0; rep < 3; ++rep) {
+            CK(cudaEventRecord(a, st_));
+            run_plan(*p);
+            CK(cudaEventRecord(b, st_));
+            CK(cudaEventSynchronize(b));
+            float x = 0.f;
+            CK(cudaEventElapsedTime(&x, a, b));
+            tbest = std::min(tbest, x);
+          }
+          t += tbest;
+        }
+        ms[2 * k + sh] = t;
+        if (t < best) { best = t; pick = sh; }
+      }
+      gemm_shape_[k] = pick;
+      shapes[k] = pick;
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    bytes_ = held;
+    build_fp64_plans(planLadder_, planI4_, planRing_, -1, nullptr);
+    mixed_ready_ = false;  // the mixed residual's FP64 plans are rebuilt with the new shapes
+    oz_ready_ = false;
   }
 
   // ================================================================== iteration
@@ -1667,6 +1728,7 @@ class Engine final : public IEngine {
     // FP64 plans of the re-base: PP_b = V_pppp' T, and R' += T I9
     {
       PlanBuilder bp, bh;
+      bp.shape_of = bh.shape_of = gemm_shape_;
       int64_t hoff = 0, voff = 0;
       for (int c = 0; c < nc; ++c) {
         const auto &pk = L.pk[c];
@@ -1873,6 +1935,7 @@ class Engine final : public IEngine {
   SplitPlan spStatic_, spTphb_, spIter1_, spIter2_;
   double *host_res_ = nullptr;
   int host_flag_ = 0;
+  int gemm_shape_[4] = {kShape128x32, kShape128x32, kShape64x64, kShape64x64};
   cudaStream_t cs_ = nullptr;       // copy stream of ccx_set_vblocks
   cudaEvent_t sev_[5] = {};         // copied[2], packed[2], compute-stream mark
   DBuf stage2_;

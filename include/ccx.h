@@ -285,6 +285,15 @@ int ccx_ccd_iter(ccx_engine *e, const ccx_iter_opts *opt, ccx_iter_result *res);
 int ccx_ccd_iter_batch(ccx_engine *const *engines, int32_t n, const ccx_iter_opts *opt, ccx_iter_result *res,
                        double *seconds);
 
+/* Tile-shape autotuner of the grouped FP64 GEMM (ladder, I4, ring, and the mixed
+ * residual's FP64 products).  For each bucket of the problems' column count N (<= 16,
+ * <= 32, <= 64, > 64) it times the engine's own problems of that bucket with each tile
+ * shape (0: 64 x 64 with 4 x 4 per thread, 1: 128 x 32 with 8 x 2), keeps the faster
+ * shape and rebuilds the plans.  shapes[k]: the choice of bucket k; ms[2 k + s]: the
+ * time of shape s on bucket k (ms, best of 3).  Needs the interaction and amplitudes;
+ * call it between solves. */
+int ccx_engine_autotune(ccx_engine *e, int32_t shapes[4], double ms[8]);
+
 /* ---- (T) -------------------------------------------------------------- */
 /* pert_triples2, ccm_triples.f90:528-735 (NN part): E(T) from the current T2 with
  * the V_hppp / V_hhhp blocks of setup_vnn_hppp_block (ccm_iter.f90:1361-1810). */

@@ -272,3 +272,16 @@ def test_twisted_lattice(ccx, O):
     ro = o.ccd_iter(mode=O.MODE_STANDARD, tol=1e-10)
     re_ = e.ccd_iter(mode=ccx.MODE_STANDARD, tol=1e-10)
     assert abs(re_["e_ccd"] - ro["e_ccd"]) < 1e-10 * abs(ro["e_ccd"])
+
+
+def test_autotune_keeps_results(ccx, O):
+    """The GEMM tile-shape autotuner only changes how the products are tiled."""
+    o, L, e = make(ccx, O, **C1)
+    e.setup_t_amplitudes()
+    r0 = e.ccd_iter(mode=ccx.MODE_STANDARD, tol=1e-10)
+    shapes, ms = e.autotune()
+    assert len(shapes) == 4 and all(s in (0, 1) for s in shapes)
+    assert all(t >= 0 for row in ms for t in row)
+    e.setup_t_amplitudes()
+    r1 = e.ccd_iter(mode=ccx.MODE_STANDARD, tol=1e-10)
+    assert r1["converged"] and abs(r1["e_ccd"] - r0["e_ccd"]) < 1e-12 * abs(r0["e_ccd"])
