@@ -1634,7 +1634,8 @@ class Engine final : public IEngine {
     auto nkf = [&](int x) { return (x + tk - 1) / tk; };
     const int nc = L.fam[3].count(), nq = L.ph[1].count();
     // sizes
-    TileBuf *bufs[8] = {&tVpp_, &tD_, &tVph_, &tDphB_, &tTphbA_, &tDphA_, &tdI4B_, &tI4B_};
+    TileBuf *bufs[12] = {&tVpp_, &tD_, &tVph_, &tDphB_, &tTphbA_, &tDphA_, &tdI4B_, &tI4B_,
+                         &tDA_, &tI9B_, &tTbA_, &tdI9B_};
     for (TileBuf *b : bufs) b->n = 0;
     for (int c = 0; c < nc; ++c) {
       const auto &pk = L.pk[c];
@@ -1642,6 +1643,10 @@ class Engine final : public IEngine {
       if (pk.H > 256) throw EngineError(1, "mixed precision: an hhpp channel has more than 256 packed hole pairs");
       tVpp_.n += (int64_t)mpad(pk.P) * nkf(pk.P) * tk;
       tD_.n += (int64_t)npadf(pk.H) * nkf(pk.P) * tk;
+      tDA_.n += (int64_t)mpad(pk.P) * nkf(pk.H) * tk;    // A = dT' (P x H)
+      tTbA_.n += (int64_t)mpad(pk.P) * nkf(pk.H) * tk;   // A = T_b' (P x H)
+      tI9B_.n += (int64_t)npadf(pk.H) * nkf(pk.H) * tk;  // B = I9' (K H, N H)
+      tdI9B_.n += (int64_t)npadf(pk.H) * nkf(pk.H) * tk; // B = I9' - I9_b'
     }
     for (int q = 0; q < nq; ++q) {
       const int nph = L.ph[1].side1[q].size(), nhp = L.ph[1].side2[q].size();
@@ -1668,22 +1673,36 @@ class Engine final : public IEngine {
     Rphb_.alloc(std::max<int64_t>(n_ph_, 1) * sz, &bytes_);
     I4b_.alloc(std::max<int64_t>(n_i4_, 1) * sz, &bytes_);
     dI4_.alloc(std::max<int64_t>(n_i4_, 1) * sz, &bytes_);
+    Xb_.alloc(std::max<int64_t>(n_hh2_, 1) * sz, &bytes_);
+    dI9_.alloc(std::max<int64_t>(n_hh2_, 1) * sz, &bytes_);
+    HHb_.alloc(std::max<int64_t>(n_t_, 1) * sz, &bytes_);
     tcerr_.alloc(sizeof(int), &bytes_);
     CK(cudaMemset(tcerr_.p, 0, sizeof(int)));
-    std::vector<TcSplitJob> js_static, js_tphb, js_it1, js_it2;
-    TcList pp, p4, pr1, pr2;
+    std::vector<TcSplitJob> js_static, js_tphb, js_it1, js_it2, js_it3;
+    TcList pp, p4, pr1, pr2, lh1, lh2;
     {
-      int64_t oa = 0, ob = 0, voff = 0;
+      int64_t oa = 0, ob = 0, voff = 0, hoff = 0, oda = 0, otb = 0, oi9 = 0;
       for (int c = 0; c < nc; ++c) {
         const auto &pk = L.pk[c];
         if (pk.P > 0 && pk.H > 0) {
+          S *t = T_.as<S>() + pk.t_off, *tb = Tb_.as<S>() + pk.t_off;
           add_split(js_static, Vpp_.as<S>() + voff, nullptr, pk.P, 1, pk.P, pk.P, 128, mpad(pk.P), tVpp_, oa);
-          add_split(js_it1, T_.as<S>() + pk.t_off, Tb_.as<S>() + pk.t_off, pk.P, 1, pk.H, pk.P, npadf(pk.H),
-                    npadf(pk.H), tD_, ob);
+          add_split(js_it1, t, tb, pk.P, 1, pk.H, pk.P, npadf(pk.H), npadf(pk.H), tD_, ob);
           add_tc(pp, tVpp_, oa, tD_, ob, pk.P, pk.H, pk.P, R_.as<S>() + pk.t_off, 1, pk.P, 1.0);
+          // hh-ladder: R' += HH_b + dT' I9' + T_b' (I9' - I9_b')
+          add_split(js_it1, t, tb, 1, pk.P, pk.P, pk.H, 128, mpad(pk.P), tDA_, oda);
+          add_split(js_tphb, tb, nullptr, 1, pk.P, pk.P, pk.H, 128, mpad(pk.P), tTbA_, otb);
+          add_split(js_it3, I9_.as<S>() + hoff, nullptr, pk.H, 1, pk.H, pk.H, npadf(pk.H), npadf(pk.H), tI9B_, oi9);
+          add_split(js_it3, dI9_.as<S>() + hoff, nullptr, pk.H, 1, pk.H, pk.H, npadf(pk.H), npadf(pk.H), tdI9B_, oi9);
+          add_tc(lh1, tDA_, oda, tI9B_, oi9, pk.P, pk.H, pk.H, R_.as<S>() + pk.t_off, 1, pk.P, 1.0);
+          add_tc(lh2, tTbA_, otb, tdI9B_, oi9, pk.P, pk.H, pk.H, R_.as<S>() + pk.t_off, 1, pk.P, 1.0);
           oa += (int64_t)mpad(pk.P) * nkf(pk.P) * tk;
           ob += (int64_t)npadf(pk.H) * nkf(pk.P) * tk;
+          oda += (int64_t)mpad(pk.P) * nkf(pk.H) * tk;
+          otb += (int64_t)mpad(pk.P) * nkf(pk.H) * tk;
+          oi9 += (int64_t)npadf(pk.H) * nkf(pk.H) * tk;
         }
+        hoff += (int64_t)pk.H * pk.H;
         voff += (int64_t)pk.P * pk.P;
       }
     }
@@ -1721,6 +1740,9 @@ class Engine final : public IEngine {
     finalize_split(spTphb_, js_tphb);
     finalize_split(spIter1_, js_it1);
     finalize_split(spIter2_, js_it2);
+    finalize_split(spIter3_, js_it3);
+    finalize_tc(tcHH1_, lh1);
+    finalize_tc(tcHH2_, lh2);
     finalize_tc(tcPP_, pp);
     finalize_tc(tcI4_, p4);
     finalize_tc(tcR1_, pr1);
@@ -1743,7 +1765,7 @@ class Engine final : public IEngine {
           h.nseg = 1;
           h.M = pk.P; h.N = pk.H;
           h.seg[0] = GemmSeg<S>{T_.as<S>() + pk.t_off, I9_.as<S>() + hoff, 1, pk.P, 1, pk.H, pk.H, 1.0};
-          h.C = R_.as<S>() + pk.t_off; h.sCm = 1; h.sCn = pk.P; h.accumulate = 1;
+          h.C = HHb_.as<S>() + pk.t_off; h.sCm = 1; h.sCn = pk.P; h.accumulate = 0;
           bh.add(h, (int64_t)pk.P * pk.H * pk.H);
         }
         hoff += (int64_t)pk.H * pk.H;
@@ -1763,6 +1785,7 @@ class Engine final : public IEngine {
   void set_base_zero() {
     CK(cudaMemsetAsync(Tb_.p, 0, Tb_.bytes, st_));
     CK(cudaMemsetAsync(PPb_.p, 0, PPb_.bytes, st_));
+    CK(cudaMemsetAsync(Xb_.p, 0, Xb_.bytes, st_));
     CK(cudaMemsetAsync(Tphb_.p, 0, Tphb_.bytes, st_));
     CK(cudaMemsetAsync(Rphb_.p, 0, Rphb_.bytes, st_));
     CK(cudaMemcpyAsync(I4b_.p, W_.p, std::max<int64_t>(n_i4_, 1) * sizeof(S), cudaMemcpyDeviceToDevice, st_));
@@ -1825,11 +1848,14 @@ class Engine final : public IEngine {
       run_plan(planPP_);
       kend();
     }
-    launch_axpy<S>(n_t_, PPb_.as<S>(), R_.as<S>(), st_);
     kbegin(kKHH64);
-    run_plan(planHH_);
+    run_plan(planHH_);  // HH_b = T' I9'
     kend();
+    // the cached products of the new base, PP_b + HH_b, and R' += them
+    launch_axpy<S>(n_t_, HHb_.as<S>(), PPb_.as<S>(), st_);
+    launch_axpy<S>(n_t_, PPb_.as<S>(), R_.as<S>(), st_);
     // the new base
+    CK(cudaMemcpyAsync(Xb_.p, X_.p, std::max<int64_t>(n_hh2_, 1) * sizeof(S), cudaMemcpyDeviceToDevice, st_));
     CK(cudaMemcpyAsync(Tb_.p, T_.p, n_t_ * sizeof(S), cudaMemcpyDeviceToDevice, st_));
     CK(cudaMemcpyAsync(Tphb_.p, Tph_.p, std::max<int64_t>(n_ph_, 1) * sizeof(S), cudaMemcpyDeviceToDevice, st_));
     CK(cudaMemcpyAsync(Rphb_.p, Rph_.p, std::max<int64_t>(n_ph_, 1) * sizeof(S), cudaMemcpyDeviceToDevice, st_));
@@ -1845,19 +1871,26 @@ class Engine final : public IEngine {
   void residual_mixed() {
     mark(0);
     launch_gather_tph<S>(D_, T_.as<S>(), Tph_.as<S>(), st_);
+    kbegin(kKSplit);
+    run_split(spIter1_);  // dT' (B and A), dT_ph (B and A)
+    kend();
     mark(1);
+    // X in FP64: it feeds the dressed hole denominators of every amplitude through I7
+    // (a tensor-core X, X_b + V_hhpp'^T dT', costs the solve an iteration); I9' - I9_b'
+    // = X - X_b for the hh-ladder correction
     kbegin(kKX);
     run_x();
     kend();
+    launch_sub<S>(n_hh2_, X_.as<S>(), Xb_.as<S>(), dI9_.as<S>(), st_);
     launch_i7<S>(D_, X_.as<S>(), fdiag_.as<S>(), f7_.as<S>(), d2ij_.as<S>(), i7off_.as<S>(), st_);
     launch_i9<S>(D_, n_hh2_, Vhh_.as<S>(), X_.as<S>(), I9_.as<S>(), st_);
+    kbegin(kKSplit);
+    run_split(spIter3_);  // I9' (B), I9' - I9_b' (B)
+    kend();
     mark(2);
     launch_i6<S>(D_, (const int2 *)i6rows_.p, ni6rows_, i6dots_.as<S>(), T_.as<S>(), Vhp_.as<S>(), fdiag_.as<S>(),
                  f6_.as<S>(), d2ab_.as<S>(), i6off_.as<S>(), st_);
     mark(3);
-    kbegin(kKSplit);
-    run_split(spIter1_);  // dT (B), dT_ph (B and A)
-    kend();
     CK(cudaMemsetAsync(dI4_.p, 0, std::max<int64_t>(n_i4_, 1) * sizeof(S), st_));
     kbegin(kKTcI4);
     run_tc(tcI4_);  // dI4 = 1/2 V_ph dT_ph
@@ -1877,15 +1910,18 @@ class Engine final : public IEngine {
     mark(5);
     launch_rinit<S>(D_, T_.as<S>(), Vhp_.as<S>(), Rph_.as<S>(), i6off_.as<S>(), i7off_.as<S>(), R_.as<S>(), st_);
     mark(6);
-    launch_axpy<S>(n_t_, PPb_.as<S>(), R_.as<S>(), st_);
+    launch_axpy<S>(n_t_, PPb_.as<S>(), R_.as<S>(), st_);  // PP_b + HH_b
     kbegin(kKTcPP);
     run_tc(tcPP_);  // R' += V_pppp' dT
     kend();
-    kbegin(kKHH64);
-    run_plan(planHH_);
+    kbegin(kKHHTc);
+    run_tc(tcHH1_);  // R' += dT' I9'
+    kend();
+    kbegin(kKHHTc);
+    run_tc(tcHH2_);  // R' += T_b' (I9' - I9_b')
     kend();
     mark(7);
-    launches_ += 7;
+    launches_ += 8;
     if (timing_) accumulate_timers(0, 7);
   }
 
@@ -1924,15 +1960,15 @@ class Engine final : public IEngine {
   bool mixed_ready_ = false;
   int tc_kind_ = 0;
   int64_t v_version_ = 0, mixed_v_version_ = -1;
-  DBuf Tb_, PPb_, Tphb_, Rphb_, I4b_, dI4_, tcerr_;
+  DBuf Tb_, PPb_, Tphb_, Rphb_, I4b_, dI4_, tcerr_, Xb_, dI9_, HHb_;
   OzBuf ozVpp_, ozTb_, ozVph_, ozTphB_, ozTphA_, ozI4B_;
   OzSplitPlan ozsV_, ozsTb_, ozsTph_, ozsI4_;
   OzPlan ozPP_, ozI4_, ozRing_;
   bool oz_ready_ = false;
   int64_t oz_v_version_ = -1;
-  TileBuf tVpp_, tD_, tVph_, tDphB_, tTphbA_, tDphA_, tdI4B_, tI4B_;
-  TcPlan tcPP_, tcI4_, tcR1_, tcR2_;
-  SplitPlan spStatic_, spTphb_, spIter1_, spIter2_;
+  TileBuf tVpp_, tD_, tVph_, tDphB_, tTphbA_, tDphA_, tdI4B_, tI4B_, tDA_, tI9B_, tTbA_, tdI9B_;
+  TcPlan tcPP_, tcI4_, tcR1_, tcR2_, tcHH1_, tcHH2_;
+  SplitPlan spStatic_, spTphb_, spIter1_, spIter2_, spIter3_;
   double *host_res_ = nullptr;
   int host_flag_ = 0;
   int gemm_shape_[4] = {kShape128x32, kShape128x32, kShape64x64, kShape64x64};

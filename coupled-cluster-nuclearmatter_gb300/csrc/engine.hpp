@@ -53,6 +53,7 @@ enum KernelSlot {
   kKPPOz = 10,  // k_oz_gemm: V_pppp' T' at a re-base as exact digit products
   kKI4Oz = 11,  // k_oz_gemm: I4 at a re-base as exact digit products
   kKRingOz = 12,  // k_oz_gemm: ring at a re-base as exact digit products
+  kKHHTc = 14,  // k_tc_gemm: hh-ladder corrections (two launches per residual)
   kKernelSlots = 16
 };
 

@@ -106,6 +106,8 @@ double measure_fp64_peak(int device);
 // y += x ; z = x + y (n elements)
 template <typename S> void launch_axpy(int64_t n, const S *x, S *y, cudaStream_t st);
 template <typename S> void launch_add(int64_t n, const S *x, const S *y, S *z, cudaStream_t st);
+// z = x - y
+template <typename S> void launch_sub(int64_t n, const S *x, const S *y, S *z, cudaStream_t st);
 template <typename S> void launch_mp2(const DevLayout &L, const S *Vhp, const S *fdiag, S *T, cudaStream_t st);
 template <typename S> void launch_pack_t(const DevLayout &L, int ch, int n_pp, const double *stage, S *T, int *flag, cudaStream_t st);
 template <typename S>

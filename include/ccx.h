@@ -357,7 +357,7 @@ int ccx_engine_timers(const ccx_engine *e, double ms[10]);
  * [5] hh-ladder of the mixed residual (FP64), [6] pp-ladder correction (tensor cores),
  * [7] dI4 correction (tensor cores), [8] ring corrections (tensor cores),
  * [9] operand splits, [10] pp-ladder, [11] I4 and [12] ring at a re-base as digit products
- * (tensor cores), [13..15] unused */
+ * (tensor cores), [13] unused, [14] hh-ladder corrections (tensor cores), [15] unused */
 int ccx_engine_kernel_timers(const ccx_engine *e, double ms[16], int64_t launches[16]);
 
 #ifdef __cplusplus
