@@ -230,6 +230,33 @@ template <typename S> void launch_gather_tph(const DevLayout &L, const S *T, S *
 // in K chunks, each warp owns rows m (lanes stride over k), and the lane partials are
 // reduced with shuffles at the end, in a fixed order.
 // ============================================================================
+template <typename S, int NJ>
+__device__ __forceinline__ void xdot_rows(const S *__restrict__ V, const S (*Ts)[kXK], int64_t off, int P, int H, int m0,
+                                          int k0, int kn, int warp, int lane, S (&acc)[kXM / 8][kXJ]) {
+  constexpr int RPW = kXM / 8;
+#pragma unroll
+  for (int r = 0; r < RPW; ++r) {
+    const int m = m0 + warp + 8 * r;
+    if (m >= H) break;
+    const S *vc = V + off + (int64_t)P * m + k0;
+    int k = lane;
+    // two independent loads in flight per iteration
+    for (; k + 32 < kn; k += 64) {
+      const S v0 = vc[k], v1 = vc[k + 32];
+#pragma unroll
+      for (int j = 0; j < NJ; ++j) {
+        acc[r][j] += v0 * Ts[j][k];
+        acc[r][j] += v1 * Ts[j][k + 32];
+      }
+    }
+    if (k < kn) {
+      const S v = vc[k];
+#pragma unroll
+      for (int j = 0; j < NJ; ++j) acc[r][j] += v * Ts[j][k];
+    }
+  }
+}
+
 template <typename S>
 __global__ void __launch_bounds__(256) k_xdot(DevLayout L, const int4 *__restrict__ work, const S *__restrict__ V,
                                               const S *__restrict__ T, S *__restrict__ X) {
@@ -253,17 +280,16 @@ __global__ void __launch_bounds__(256) k_xdot(DevLayout L, const int4 *__restric
       Ts[j][k] = (j < nj && k < kn) ? T[off + (int64_t)P * (j0 + j) + k0 + k] : S(0.0);
     }
     __syncthreads();
-#pragma unroll
-    for (int r = 0; r < RPW; ++r) {
-      const int m = m0 + warp + 8 * r;
-      if (m < H) {
-        const S *vc = V + off + (int64_t)P * m + k0;
-        for (int k = lane; k < kn; k += 32) {
-          const S v = vc[k];
-#pragma unroll
-          for (int j = 0; j < kXJ; ++j) acc[r][j] += v * Ts[j][k];
-        }
-      }
+    // no FP64 work on the padding columns of a partial column block
+    switch (nj) {
+      case 8: xdot_rows<S, 8>(V, Ts, off, P, H, m0, k0, kn, warp, lane, acc); break;
+      case 7: xdot_rows<S, 7>(V, Ts, off, P, H, m0, k0, kn, warp, lane, acc); break;
+      case 6: xdot_rows<S, 6>(V, Ts, off, P, H, m0, k0, kn, warp, lane, acc); break;
+      case 5: xdot_rows<S, 5>(V, Ts, off, P, H, m0, k0, kn, warp, lane, acc); break;
+      case 4: xdot_rows<S, 4>(V, Ts, off, P, H, m0, k0, kn, warp, lane, acc); break;
+      case 3: xdot_rows<S, 3>(V, Ts, off, P, H, m0, k0, kn, warp, lane, acc); break;
+      case 2: xdot_rows<S, 2>(V, Ts, off, P, H, m0, k0, kn, warp, lane, acc); break;
+      default: xdot_rows<S, 1>(V, Ts, off, P, H, m0, k0, kn, warp, lane, acc); break;
     }
     __syncthreads();
   }
