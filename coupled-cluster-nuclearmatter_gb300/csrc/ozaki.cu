@@ -1,6 +1,7 @@
 // FP64-accurate GEMM by exact digit products on the BF16 tensor cores (sm_103a).
 //
-// One CTA per (128-row tile, up to kOzN columns) of one problem, six warps:
+// Persistent: one CTA per SM walks the (128-row tile, up to kOzN columns) tiles of the
+// problem list; six warps:
 //   warp 4 (one lane) streams the digit tiles with cp.async.bulk: per K tile, the
 //     kOzSlices B digit tiles into one of two B buffers, then the kOzSlices A digit
 //     tiles one by one through a ring of kOzStages stages;
@@ -40,17 +41,18 @@ __device__ __forceinline__ double pow2(int e) {
   return __longlong_as_double((long long)(e + 1023) << 52);
 }
 
+__device__ __forceinline__ bool oz_tile_ok(const OzProb &P, const OzTile &tl) {
+  const int nc = min(kOzN, P.npad - tl.n0);
+  return nc >= 16 && !(nc & 15) && P.npad <= 256 && !(P.npad & 15) && !(tl.n0 & 7) && P.nk >= 1;
+}
+
+// Persistent: CTA b handles tiles b, b + gridDim.x, ...  The producer, the MMA issuer and
+// the drain warps walk the same tile sequence; stage, B-buffer and chunk counters run on
+// across tiles, so the next tile's digits stream in while the last chunk drains.
 __global__ void __launch_bounds__(kOzThreads, 1) k_oz_gemm(const OzProb *__restrict__ probs,
-                                                           const OzTile *__restrict__ tiles, int *err) {
+                                                           const OzTile *__restrict__ tiles, int ntiles, int *err) {
   extern __shared__ __align__(1024) uint8_t smem[];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const OzTile tl = tiles[blockIdx.x];
-  const OzProb P = probs[tl.prob];
-  const int nc = min(kOzN, P.npad - tl.n0);
-  if (nc < 16 || (nc & 15) || P.npad > 256 || (P.npad & 15) || (tl.n0 & 7) || P.nk < 1) {
-    if (tid == 0) atomicExch(err, 4);
-    return;
-  }
   uint8_t *abuf = smem;
   uint8_t *bbuf = smem + kOzStages * kATile;
   uint64_t *bars = (uint64_t *)(smem + kBarOff);
@@ -82,8 +84,6 @@ __global__ void __launch_bounds__(kOzThreads, 1) k_oz_gemm(const OzProb *__restr
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
-  const int nk = P.nk;
-  const int nchunk = (nk + kOzChunkTiles - 1) / kOzChunkTiles;
 
   // bounded wait that also ends when another thread has given up
   auto wait = [&](uint64_t *bar, uint32_t parity) -> bool {
@@ -101,29 +101,35 @@ __global__ void __launch_bounds__(kOzThreads, 1) k_oz_gemm(const OzProb *__restr
 
   if (warp == 4) {
     if (lane == 0) {  // producer
-      const uint8_t *A0 = (const uint8_t *)P.A + (size_t)tl.mt * nk * kATile;
-      const uint8_t *B0 = (const uint8_t *)P.B + (size_t)tl.n0 * 128;
-      const size_t ap = (size_t)P.a_plane * 2, bp = (size_t)P.b_plane * 2, bt = (size_t)P.npad * 128;
-      const uint32_t bbytes = (uint32_t)nc * 128u;
       int na[kOzStages] = {}, nb[2] = {0, 0};
-      int cnt = 0;
+      int cnt = 0, bk = 0;
       bool ok = true;
-      for (int kt = 0; kt < nk && ok; ++kt) {
-        const int bb = kt & 1;
-        if (kt >= 2 && !wait(&bempty[bb], (uint32_t)((kt / 2 - 1) & 1))) { ok = false; break; }
-        const uint32_t fb = smem_u32(&bfull[bb]);
-        mbar_expect_tx(fb, (uint32_t)kOzSlices * bbytes);
-        for (int j = 0; j < kOzSlices; ++j)
-          bulk_g2s(smem_u32(bbuf + bb * kBBuf + j * kBSlot), B0 + j * bp + (size_t)kt * bt, bbytes, fb);
-        ++nb[bb];
-        for (int i = 0; i < kOzSlices; ++i) {
-          const int s = cnt % kOzStages;
-          if (cnt >= kOzStages && !wait(&aempty[s], (uint32_t)((cnt / kOzStages - 1) & 1))) { ok = false; break; }
-          const uint32_t fa = smem_u32(&afull[s]);
-          mbar_expect_tx(fa, kATile);
-          bulk_g2s(smem_u32(abuf + s * kATile), A0 + i * ap + (size_t)kt * kATile, kATile, fa);
-          ++na[s];
-          ++cnt;
+      for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+        const OzTile tl = tiles[t];
+        const OzProb P = probs[tl.prob];
+        if (!oz_tile_ok(P, tl)) continue;
+        const int nc = min(kOzN, P.npad - tl.n0), nk = P.nk;
+        const uint8_t *A0 = (const uint8_t *)P.A + (size_t)tl.mt * nk * kATile;
+        const uint8_t *B0 = (const uint8_t *)P.B + (size_t)tl.n0 * 128;
+        const size_t ap = (size_t)P.a_plane * 2, bp = (size_t)P.b_plane * 2, bt = (size_t)P.npad * 128;
+        const uint32_t bbytes = (uint32_t)nc * 128u;
+        for (int kt = 0; kt < nk && ok; ++kt, ++bk) {
+          const int bb = bk & 1;
+          if (bk >= 2 && !wait(&bempty[bb], (uint32_t)(((bk >> 1) - 1) & 1))) { ok = false; break; }
+          const uint32_t fb = smem_u32(&bfull[bb]);
+          mbar_expect_tx(fb, (uint32_t)kOzSlices * bbytes);
+          for (int j = 0; j < kOzSlices; ++j)
+            bulk_g2s(smem_u32(bbuf + bb * kBBuf + j * kBSlot), B0 + j * bp + (size_t)kt * bt, bbytes, fb);
+          ++nb[bb];
+          for (int i = 0; i < kOzSlices; ++i) {
+            const int s = cnt % kOzStages;
+            if (cnt >= kOzStages && !wait(&aempty[s], (uint32_t)((cnt / kOzStages - 1) & 1))) { ok = false; break; }
+            const uint32_t fa = smem_u32(&afull[s]);
+            mbar_expect_tx(fa, kATile);
+            bulk_g2s(smem_u32(abuf + s * kATile), A0 + i * ap + (size_t)kt * kATile, kATile, fa);
+            ++na[s];
+            ++cnt;
+          }
         }
       }
       if (!ok) atomicExch(err, 1);
@@ -135,37 +141,47 @@ __global__ void __launch_bounds__(kOzThreads, 1) k_oz_gemm(const OzProb *__restr
     }
   } else if (warp == 5) {
     if (lane == 0) {  // MMA issuer
-      const uint32_t idesc = instr_desc<kTcBF16>(128, nc);
-      int cnt = 0;
+      int cnt = 0, bk = 0, ck = 0;
       bool ok = true;
-      for (int c = 0; c < nchunk && ok; ++c) {
-        if (c > 0 && !wait(drained, (uint32_t)((c - 1) & 1))) { ok = false; break; }
-        tc_fence_after();
-        const int k_beg = c * kOzChunkTiles, k_end = min(nk, k_beg + kOzChunkTiles);
-        for (int kt = k_beg; kt < k_end && ok; ++kt) {
-          const int bb = kt & 1;
-          if (!wait(&bfull[bb], (uint32_t)((kt / 2) & 1))) { ok = false; break; }
-          tc_fence_after();
-          const uint32_t sb = smem_u32(bbuf + bb * kBBuf);
-          for (int i = 0; i < kOzSlices; ++i) {
-            const int s = cnt % kOzStages;
-            if (!wait(&afull[s], (uint32_t)((cnt / kOzStages) & 1))) { ok = false; break; }
-            tc_fence_after();
-            const uint32_t sa = smem_u32(abuf + s * kATile);
-            for (int j = 0; i + j < kOzSlices; ++j) {
-              const uint32_t d = tmem + (uint32_t)((i + j) * kOzN);
-#pragma unroll
-              for (int ks = 0; ks < 4; ++ks) {
-                const uint32_t acc = (kt > k_beg || i > 0 || ks > 0) ? 1u : 0u;
-                tc_mma<kTcBF16>(d, smem_desc(sa + ks * 256), smem_desc(sb + j * kBSlot + ks * 256), idesc, acc);
-              }
-            }
-            tc_commit(smem_u32(&aempty[s]));
-            ++cnt;
-          }
-          if (ok) tc_commit(smem_u32(&bempty[bb]));
+      for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+        const OzTile tl = tiles[t];
+        const OzProb P = probs[tl.prob];
+        if (!oz_tile_ok(P, tl)) {
+          atomicExch(err, 4);
+          continue;
         }
-        if (ok) tc_commit(smem_u32(done));
+        const int nc = min(kOzN, P.npad - tl.n0), nk = P.nk;
+        const uint32_t idesc = instr_desc<kTcBF16>(128, nc);
+        const int nchunk = (nk + kOzChunkTiles - 1) / kOzChunkTiles;
+        for (int c = 0; c < nchunk && ok; ++c, ++ck) {
+          if (ck > 0 && !wait(drained, (uint32_t)((ck - 1) & 1))) { ok = false; break; }
+          tc_fence_after();
+          const int k_beg = c * kOzChunkTiles, k_end = min(nk, k_beg + kOzChunkTiles);
+          for (int kt = k_beg; kt < k_end && ok; ++kt, ++bk) {
+            const int bb = bk & 1;
+            if (!wait(&bfull[bb], (uint32_t)((bk >> 1) & 1))) { ok = false; break; }
+            tc_fence_after();
+            const uint32_t sb = smem_u32(bbuf + bb * kBBuf);
+            for (int i = 0; i < kOzSlices; ++i) {
+              const int s = cnt % kOzStages;
+              if (!wait(&afull[s], (uint32_t)((cnt / kOzStages) & 1))) { ok = false; break; }
+              tc_fence_after();
+              const uint32_t sa = smem_u32(abuf + s * kATile);
+              for (int j = 0; i + j < kOzSlices; ++j) {
+                const uint32_t d = tmem + (uint32_t)((i + j) * kOzN);
+#pragma unroll
+                for (int ks = 0; ks < 4; ++ks) {
+                  const uint32_t acc = (kt > k_beg || i > 0 || ks > 0) ? 1u : 0u;
+                  tc_mma<kTcBF16>(d, smem_desc(sa + ks * 256), smem_desc(sb + j * kBSlot + ks * 256), idesc, acc);
+                }
+              }
+              tc_commit(smem_u32(&aempty[s]));
+              ++cnt;
+            }
+            if (ok) tc_commit(smem_u32(&bempty[bb]));
+          }
+          if (ok) tc_commit(smem_u32(done));
+        }
       }
       if (!ok) atomicExch(err, 2);
       // every MMA this thread issued completes before the tensor memory is freed
@@ -174,49 +190,59 @@ __global__ void __launch_bounds__(kOzThreads, 1) k_oz_gemm(const OzProb *__restr
     }
   } else {  // warps 0-3: drain the level accumulators of every chunk into C
     const int row = warp * 32 + lane;
-    const int m = tl.mt * 128 + row;
-    const bool live = m < P.M;
     const uint32_t tbase = tmem + ((uint32_t)(warp * 32) << 16);
-    const int eAm = live ? P.eA[m] : 0;
-    double *crow = P.C + (int64_t)(live ? m : 0) * P.sCm;
-    for (int c = 0; c < nchunk; ++c) {
-      const bool got = __all_sync(0xffffffffu, wait(done, (uint32_t)(c & 1)));
-      if (!got) {
-        if (lane == 0) atomicExch(err, 3);
-        break;
-      }
-      tc_fence_after();
-      for (int cb = 0; cb < nc; cb += 16) {
-        long long zh[16], zl[16];
-#pragma unroll
-        for (int q = 0; q < 16; ++q) zh[q] = zl[q] = 0;
-#pragma unroll
-        for (int lv = 0; lv < kOzLevels; ++lv) {
-          uint32_t r[16];
-          tmem_ld16(tbase + (uint32_t)(lv * kOzN + cb), r);
-          tmem_ld_wait();
-#pragma unroll
-          for (int q = 0; q < 16; ++q) {
-            // an exact integer below 2^24 in magnitude
-            const long long v = (long long)__float2int_rz(__uint_as_float(r[q]));
-            if (lv < 4) zh[q] += v * (1ll << (kOzBits * (3 - lv)));
-            else zl[q] += v * (1ll << (kOzBits * (8 - lv)));
-          }
+    int ck = 0;
+    bool ok = true;
+    for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+      const OzTile tl = tiles[t];
+      const OzProb P = probs[tl.prob];
+      if (!oz_tile_ok(P, tl)) continue;
+      const int nc = min(kOzN, P.npad - tl.n0), nk = P.nk;
+      const int nchunk = (nk + kOzChunkTiles - 1) / kOzChunkTiles;
+      const int m = tl.mt * 128 + row;
+      const bool live = m < P.M;
+      const int eAm = live ? P.eA[m] : 0;
+      double *crow = P.C + (int64_t)(live ? m : 0) * P.sCm;
+      for (int c = 0; c < nchunk; ++c, ++ck) {
+        const bool got = __all_sync(0xffffffffu, wait(done, (uint32_t)(ck & 1)));
+        if (!got) {
+          if (lane == 0) atomicExch(err, 3);
+          ok = false;
+          break;
         }
-        if (live) {
+        tc_fence_after();
+        for (int cb = 0; cb < nc; cb += 16) {
+          long long zh[16], zl[16];
 #pragma unroll
-          for (int q = 0; q < 16; ++q) {
-            const int n = tl.n0 + cb + q;
-            if (n < P.N) {
-              const double z = fma((double)zh[q], 0x1p-30, (double)zl[q] * 0x1p-60);
-              crow[(int64_t)n * P.sCn] += P.alpha * (z * pow2(eAm + P.eB[n]));
+          for (int q = 0; q < 16; ++q) zh[q] = zl[q] = 0;
+#pragma unroll
+          for (int lv = 0; lv < kOzLevels; ++lv) {
+            uint32_t r[16];
+            tmem_ld16(tbase + (uint32_t)(lv * kOzN + cb), r);
+            tmem_ld_wait();
+#pragma unroll
+            for (int q = 0; q < 16; ++q) {
+              // an exact integer below 2^24 in magnitude
+              const long long v = (long long)__float2int_rz(__uint_as_float(r[q]));
+              if (lv < 4) zh[q] += v * (1ll << (kOzBits * (3 - lv)));
+              else zl[q] += v * (1ll << (kOzBits * (8 - lv)));
+            }
+          }
+          if (live) {
+#pragma unroll
+            for (int q = 0; q < 16; ++q) {
+              const int n = tl.n0 + cb + q;
+              if (n < P.N) {
+                const double z = fma((double)zh[q], 0x1p-30, (double)zl[q] * 0x1p-60);
+                crow[(int64_t)n * P.sCn] += P.alpha * (z * pow2(eAm + P.eB[n]));
+              }
             }
           }
         }
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(smem_u32(drained));
       }
-      tc_fence_before();
-      __syncwarp();
-      if (lane == 0) mbar_arrive(smem_u32(drained));
     }
   }
   tc_fence_before();
@@ -300,8 +326,12 @@ __global__ void __launch_bounds__(256) k_oz_digits(const OzSplitJob *__restrict_
 
 void launch_oz_gemm(const OzProb *probs, const OzTile *tiles, int ntiles, int *err, cudaStream_t st) {
   if (ntiles <= 0) return;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (sms <= 0) sms = 1;
   cudaFuncSetAttribute(k_oz_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kOzSmem);
-  k_oz_gemm<<<ntiles, kOzThreads, kOzSmem, st>>>(probs, tiles, err);
+  k_oz_gemm<<<std::min(ntiles, sms), kOzThreads, kOzSmem, st>>>(probs, tiles, ntiles, err);
 }
 
 std::vector<int4> oz_split_chunks(const std::vector<OzSplitJob> &jobs) {
