@@ -1388,22 +1388,28 @@ class Engine final : public IEngine {
     }
   }
   // C (S units, strides sCm, sCn) += alpha A B with A (M x K) in tile buffer a at ao and
-  // B (N x K) in b at bo
+  // B (N x K) in b at bo.  N beyond one accumulator (256 columns) runs as column blocks
+  // of at most 256 that step through the whole B operand's K tiles.
   void add_tc(TcList &l, TileBuf &a, int64_t ao, TileBuf &b, int64_t bo, int M, int N, int K, S *C, int64_t sCm,
               int64_t sCn, double alpha) {
     const size_t es = tc_kind_ == kTcBF16 ? 2 : 4;
     const int tk = tc_tile_k(tc_kind_);
+    const int npad_all = (N + 15) / 16 * 16;
     auto one = [&](int ca, int cb, int cc, double al, int ph) {
-      TcProb p{};
-      p.Ahi = (char *)a.hi.p + (ao + ca * a.n) * es;
-      p.Alo = (char *)a.lo.p + (ao + ca * a.n) * es;
-      p.Bhi = (char *)b.hi.p + (bo + cb * b.n) * es;
-      p.Blo = (char *)b.lo.p + (bo + cb * b.n) * es;
-      p.M = M; p.N = N; p.nk = (K + tk - 1) / tk; p.npad = (N + 15) / 16 * 16;
-      p.C = (double *)C + cc; p.sCm = sCm * kNComp; p.sCn = sCn * kNComp; p.alpha = al;
-      for (int mt = 0; mt < (M + 127) / 128; ++mt) l.tiles.push_back(TcTile{(int)l.probs.size(), mt});
-      l.probs.push_back(p);
-      l.phase.push_back(ph);
+      for (int n0 = 0; n0 < N; n0 += 256) {
+        const int nb = std::min(256, N - n0);
+        TcProb p{};
+        p.Ahi = (char *)a.hi.p + (ao + ca * a.n) * es;
+        p.Alo = (char *)a.lo.p + (ao + ca * a.n) * es;
+        p.Bhi = (char *)b.hi.p + (bo + cb * b.n) * es + (size_t)n0 * 128;
+        p.Blo = (char *)b.lo.p + (bo + cb * b.n) * es + (size_t)n0 * 128;
+        p.M = M; p.N = nb; p.nk = (K + tk - 1) / tk; p.npad = (nb + 15) / 16 * 16;
+        p.bstride = npad_all > 256 ? (int64_t)npad_all * 128 : 0;
+        p.C = (double *)C + cc + (int64_t)n0 * sCn * kNComp; p.sCm = sCm * kNComp; p.sCn = sCn * kNComp; p.alpha = al;
+        for (int mt = 0; mt < (M + 127) / 128; ++mt) l.tiles.push_back(TcTile{(int)l.probs.size(), mt});
+        l.probs.push_back(p);
+        l.phase.push_back(ph);
+      }
     };
     if (kNComp == 1) {
       one(0, 0, 0, alpha, 0);
@@ -1534,7 +1540,6 @@ class Engine final : public IEngine {
     for (int c = 0; c < nc; ++c) {
       const auto &pk = L.pk[c];
       if (pk.P <= 0 || pk.H <= 0) continue;
-      if (pk.H > 256) throw EngineError(1, "digit-product re-base: an hhpp channel has more than 256 packed hole pairs");
       pa += (int64_t)mpad(pk.P) * nkf(pk.P) * 64;
       pb += (int64_t)npadf(pk.H) * nkf(pk.P) * 64;
       ra += pk.P;
@@ -1544,7 +1549,6 @@ class Engine final : public IEngine {
     for (int q = 0; q < nq; ++q) {
       const int nph = L.ph[1].side1[q].size(), nhp = L.ph[1].side2[q].size();
       if (nph <= 0 || nhp <= 0) continue;
-      if (nhp > 256) throw EngineError(1, "digit-product re-base: a ring channel has more than 256 hole-particle pairs");
       pv += (int64_t)mpad(nhp) * nkf(nph) * 64;   // A = V_ph (n_hp x n_ph)
       pt += (int64_t)npadf(nhp) * nkf(nph) * 64;  // B = T_ph (K n_ph, N n_hp)
       pr += (int64_t)mpad(nph) * nkf(nhp) * 64;   // A = T_ph (n_ph x n_hp)
@@ -1640,7 +1644,6 @@ class Engine final : public IEngine {
     for (int c = 0; c < nc; ++c) {
       const auto &pk = L.pk[c];
       if (pk.P <= 0 || pk.H <= 0) continue;
-      if (pk.H > 256) throw EngineError(1, "mixed precision: an hhpp channel has more than 256 packed hole pairs");
       tVpp_.n += (int64_t)mpad(pk.P) * nkf(pk.P) * tk;
       tD_.n += (int64_t)npadf(pk.H) * nkf(pk.P) * tk;
       tDA_.n += (int64_t)mpad(pk.P) * nkf(pk.H) * tk;    // A = dT' (P x H)
@@ -1651,7 +1654,6 @@ class Engine final : public IEngine {
     for (int q = 0; q < nq; ++q) {
       const int nph = L.ph[1].side1[q].size(), nhp = L.ph[1].side2[q].size();
       if (nph <= 0 || nhp <= 0) continue;
-      if (nhp > 256) throw EngineError(1, "mixed precision: a ring channel has more than 256 hole-particle pairs");
       tVph_.n += (int64_t)mpad(nhp) * nkf(nph) * tk;
       tDphB_.n += (int64_t)npadf(nhp) * nkf(nph) * tk;
       tTphbA_.n += (int64_t)mpad(nph) * nkf(nhp) * tk;

@@ -43,7 +43,7 @@ __device__ __forceinline__ double pow2(int e) {
 
 __device__ __forceinline__ bool oz_tile_ok(const OzProb &P, const OzTile &tl) {
   const int nc = min(kOzN, P.npad - tl.n0);
-  return nc >= 16 && !(nc & 15) && P.npad <= 256 && !(P.npad & 15) && !(tl.n0 & 7) && P.nk >= 1;
+  return nc >= 16 && !(nc & 15) && !(P.npad & 15) && !(tl.n0 & 7) && P.nk >= 1;
 }
 
 // Persistent: CTA b handles tiles b, b + gridDim.x, ...  The producer, the MMA issuer and

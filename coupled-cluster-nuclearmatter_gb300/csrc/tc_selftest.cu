@@ -41,7 +41,7 @@ static void oz_selftest(int nprob, const int *Ms, const int *Ns, const int *Ks, 
   for (int i = 0; i < nprob; ++i) {
     Host &x = h[i];
     x.M = Ms[i]; x.N = Ns[i]; x.K = Ks[i];
-    if (x.M <= 0 || x.N <= 0 || x.N > 256 || x.K <= 0) throw EngineError(1, "selftest: bad problem shape");
+    if (x.M <= 0 || x.N <= 0 || x.N > 2048 || x.K <= 0) throw EngineError(1, "selftest: bad problem shape");
     x.nk = (x.K + 63) / 64;
     x.npad = (x.N + 15) / 16 * 16;
     x.mpad = (x.M + 127) / 128 * 128;
@@ -167,11 +167,10 @@ void tc_selftest(int device, int kind, int nprob, const int *Ms, const int *Ns, 
     x.M = Ms[i];
     x.N = Ns[i];
     x.K = Ks[i];
-    if (x.M <= 0 || x.N <= 0 || x.N > 256 || x.K <= 0) throw EngineError(1, "selftest: bad problem shape");
+    if (x.M <= 0 || x.N <= 0 || x.N > 2048 || x.K <= 0) throw EngineError(1, "selftest: bad problem shape");
     x.nk = (x.K + tk - 1) / tk;
     x.npad = (x.N + 15) / 16 * 16;
     x.mpad = (x.M + 127) / 128 * 128;
-    npad_max = std::max(npad_max, x.npad);
     x.A.resize((size_t)x.M * x.K);
     x.B.resize((size_t)x.K * x.N);
     x.C.resize((size_t)x.M * x.N);
@@ -208,12 +207,19 @@ void tc_selftest(int device, int kind, int nprob, const int *Ms, const int *Ns, 
     jb.hi = (char *)tBh.p + tb * es; jb.lo = (char *)tBl.p + tb * es; jb.scale = 1.0;
     jobs.push_back(ja);
     jobs.push_back(jb);
-    TcProb p{};
-    p.Ahi = ja.hi; p.Alo = use_alo ? ja.lo : nullptr; p.Bhi = jb.hi; p.Blo = jb.lo;
-    p.M = x.M; p.N = x.N; p.nk = x.nk; p.npad = x.npad;
-    p.C = (double *)dC.p + oc; p.sCm = 1; p.sCn = x.M; p.alpha = 0.5;
-    for (int mt = 0; mt < x.mpad / 128; ++mt) tiles.push_back(TcTile{i, mt});
-    probs.push_back(p);
+    // N beyond one accumulator: column blocks of <= 256 stepping through the whole B
+    for (int n0 = 0; n0 < x.N; n0 += 256) {
+      const int nb = std::min(256, x.N - n0);
+      TcProb p{};
+      p.Ahi = ja.hi; p.Alo = use_alo ? ja.lo : nullptr;
+      p.Bhi = (char *)jb.hi + (size_t)n0 * 128; p.Blo = (char *)jb.lo + (size_t)n0 * 128;
+      p.M = x.M; p.N = nb; p.nk = x.nk; p.npad = (nb + 15) / 16 * 16;
+      p.bstride = x.npad > 256 ? (int64_t)x.npad * 128 : 0;
+      p.C = (double *)dC.p + oc + (size_t)n0 * x.M; p.sCm = 1; p.sCn = x.M; p.alpha = 0.5;
+      for (int mt = 0; mt < x.mpad / 128; ++mt) tiles.push_back(TcTile{(int)probs.size(), mt});
+      probs.push_back(p);
+      npad_max = std::max(npad_max, p.npad);
+    }
     oa += x.A.size(); ob += x.B.size(); oc += x.C.size(); ta += x.a_el; tb += x.b_el;
   }
   Dev dJ(jobs.size() * sizeof(TcSplitJob)), dP(probs.size() * sizeof(TcProb)), dT(tiles.size() * sizeof(TcTile)), dE(4);

@@ -39,6 +39,7 @@ __global__ void __launch_bounds__(128) k_tc_gemm(const TcProb *__restrict__ prob
   }
   constexpr uint32_t a_bytes = 128u * 128u;
   const uint32_t b_bytes = (uint32_t)npad * 128u;
+  const size_t bstep = P.bstride ? (size_t)P.bstride : (size_t)b_bytes;
   const uint32_t stage_bytes = 2u * a_bytes + 2u * (uint32_t)npad_max * 128u;
   uint64_t *full = (uint64_t *)(smem + (size_t)stages * stage_bytes);
   uint64_t *empty = full + stages;
@@ -78,8 +79,8 @@ __global__ void __launch_bounds__(128) k_tc_gemm(const TcProb *__restrict__ prob
       mbar_expect_tx(fb, tx);
       bulk_g2s(smem_u32(st), Ahi + (size_t)kt * a_bytes, a_bytes, fb);
       if (two_a) bulk_g2s(smem_u32(st + a_bytes), Alo + (size_t)kt * a_bytes, a_bytes, fb);
-      bulk_g2s(smem_u32(st + 2 * a_bytes), Bhi + (size_t)kt * b_bytes, b_bytes, fb);
-      bulk_g2s(smem_u32(st + 2 * a_bytes + (size_t)npad_max * 128), Blo + (size_t)kt * b_bytes, b_bytes, fb);
+      bulk_g2s(smem_u32(st + 2 * a_bytes), Bhi + (size_t)kt * bstep, b_bytes, fb);
+      bulk_g2s(smem_u32(st + 2 * a_bytes + (size_t)npad_max * 128), Blo + (size_t)kt * bstep, b_bytes, fb);
       ++issued[s];
     };
     const uint32_t idesc = instr_desc<KIND>(128, npad);

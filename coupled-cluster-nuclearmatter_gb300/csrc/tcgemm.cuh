@@ -25,6 +25,9 @@ struct TcProb {
   double *C;              // C(m, n) at C[m * sCm + n * sCn]
   int64_t sCm, sCn;
   double alpha;
+  int64_t bstride;        // bytes between B K tiles (0: npad * 128, the whole B operand); a
+                          // column block of a wider B points Bhi/Blo at its first row and
+                          // steps by the full operand's K-tile size
 };
 struct TcTile {
   int prob, mt;

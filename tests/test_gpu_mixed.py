@@ -124,3 +124,25 @@ def test_mixed_rejects_unsupported(ccx):
         er.ccd_iter(mode=ccx.MODE_REFERENCE, precision=ccx.PREC_MIXED)
     with pytest.raises(ccx.CcxError):
         er.ccd_iter(mode=ccx.MODE_STANDARD, precision=ccx.PREC_MIXED, rebase=7)
+
+
+def test_mixed_ring_channels_wider_than_256(ccx):
+    """A twisted SNM lattice whose ring channels hold more than 256 hole-particle pairs:
+    the tensor-core products run as 256-column blocks.  Two iterations from MP2 (a mixed
+    one, then a digit-product re-base) stay with the FP64 iteration to the BF16x3 level."""
+    th = (-1.068, -1.068, -1.068)
+    L = ccx.Layout.from_basis(3, 132, 0.16, snm=True, theta=th)
+    nhp = max(L.channel(ccx.CH_PH_PHHP, q)[2] for q in range(L.counts()["ph_phhp"]))
+    assert nhp > 256
+    out = []
+    for prec in (ccx.PREC_FP64, ccx.PREC_MIXED):
+        e = ccx.Engine(L, real=True)
+        e.generate()
+        e.setup_t_amplitudes()
+        out.append(e.ccd_iter(mode=ccx.MODE_STANDARD, precision=prec, rebase=ccx.REBASE_DIGITS, max_iter=2,
+                              defect_period=1, tol=1e-10))
+        del e
+    r64, rm = out
+    assert rm["mixed_iterations"] == 1 and rm["fp64_sweeps"] == 1
+    assert abs(rm["e_ccd"] - r64["e_ccd"]) < 1e-4 * abs(r64["e_ccd"])
+    assert abs(rm["res_norm"] - r64["res_norm"]) < 1e-3 * r64["res_norm"]

@@ -38,3 +38,13 @@ def test_ozaki_digit_gemm_is_fp64_accurate(ccx, shapes):
     ~sqrt(K) 2^-53 relative to sum |a||b|, here ~1e-14 of max |AB|)."""
     err, ms = ccx.selftest_tc_gemm(shapes, kind=2)
     assert err < 1e-13, err
+
+
+WIDE = [(200, 300, 150), (129, 520, 700), (300, 16, 90)]
+
+
+@pytest.mark.parametrize("kind", [0, 2], ids=["bf16x3", "digits"])
+def test_wide_n_column_blocks(ccx, kind):
+    """N beyond one 256-column accumulator: column blocks that step through the whole B."""
+    err, _ = ccx.selftest_tc_gemm(WIDE, kind=kind)
+    assert err < (2e-4 if kind == 0 else 1e-13), err
