@@ -458,6 +458,8 @@ def run_e2e(args, ccx, torch, L, e, local, real, solve):
 TWIST_LATTICES = {
     "pnm66": dict(nmax=4, A=66, rho=0.16, snm=False, desc="PNM A=66, rho=0.16 fm^-3, nmax=4 (1458 states), Minnesota"),
     "snm132n3": dict(nmax=3, A=132, rho=0.16, snm=True, desc="SNM A=132, rho=0.16 fm^-3, nmax=3 (1372 states), Minnesota"),
+    "snm132n3chiral": dict(nmax=3, A=132, rho=0.16, snm=True, potential=1,
+                           desc="SNM A=132, rho=0.16 fm^-3, nmax=3 (1372 states), chiral-like (complex)"),
 }
 
 
@@ -490,8 +492,9 @@ def run_twists(args):
     engines = []
     for th, _ in grid:
         L = ccx.Layout.from_basis(lat["nmax"], lat["A"], lat["rho"], snm=lat["snm"], theta=th)
-        e = ccx.Engine(L, real=True)
-        e.generate()
+        pot = lat.get("potential", 0)
+        e = ccx.Engine(L, real=pot == 0)
+        e.generate(potential=pot)
         e.setup_t_amplitudes()
         e.ccd_iter(mode=ccx.MODE_STANDARD, **opts)  # warm-up: operand tiles and digit planes
         engines.append(e)
