@@ -191,32 +191,31 @@ def kernel_work(P, H, ring, precision):
     x = sum(2.0 * h * h * p for p, h in zip(P, H))
     i4 = sum(2.0 * nhp * nhp * nph for nph, nhp in ring)
     rg = sum(2.0 * nph * nhp * nhp for nph, nhp in ring)
-    b_pp = sum(2 * es * (p * p + p * h) + 16.0 * p * h for p, h in zip(P, H))
+    # pp-ladder launch: V_pppp' dT' plus the two hh-ladder corrections (dT' I9', T_b' dI9')
+    # into one accumulator; R' read and written, PP_b + HH_b read
+    b_pp = sum(2 * es * (p * p + p * h) + 2 * 2 * es * (p * h + h * h) + 24.0 * p * h for p, h in zip(P, H))
     b_i4 = sum(2 * es * (2.0 * nhp * nph) + 16.0 * nhp * nhp for nph, nhp in ring)
-    b_ring = sum(2 * es * (nph * nhp + nhp * nhp) + 16.0 * nph * nhp for nph, nhp in ring)
+    # ring launch: T_ph,b dI4 + dT_ph I4 into one accumulator; R_ph,b read, R_ph written
+    b_ring = sum(2 * 2 * es * (nph * nhp + nhp * nhp) + 16.0 * nph * nhp for nph, nhp in ring)
     # digit-product GEMM: 9 BF16 digit planes of V_pppp' and of T_b read once, C written
     b_oz = sum(9 * 2.0 * (p * p + p * h) + 16.0 * p * h for p, h in zip(P, H))
     b_i4_oz = sum(9 * 2.0 * (2.0 * nhp * nph) + 16.0 * nhp * nhp for nph, nhp in ring)
-    # one hh-ladder correction launch: A (P x H) and B (H x H) split operands, R' read and written
-    b_hh = sum(2 * es * (p * h + h * h) + 16.0 * p * h for p, h in zip(P, H))
     b_ring_oz = sum(9 * 2.0 * (nph * nhp + nhp * nhp) + 16.0 * nph * nhp for nph, nhp in ring)
     return {"x_fp64": ("flop", x), "i4_fp64": ("flop", i4), "ring_fp64": ("flop", rg),
             "ladder_fp64": ("flop", pp + hh), "pp_rebase_fp64": ("flop", pp), "hh_fp64": ("flop", hh),
             "pp_tc": ("byte", b_pp), "i4_tc": ("byte", b_i4), "ring_tc": ("byte", b_ring),
             "pp_rebase_digits": ("byte", b_oz), "i4_rebase_digits": ("byte", b_i4_oz),
-            "ring_rebase_digits": ("byte", b_ring_oz),
-            "hh_tc": ("byte", b_hh)}
+            "ring_rebase_digits": ("byte", b_ring_oz)}
 
 
 KERNEL_NAMES = {"x_fp64": "k_gemm<double> X = V_hhpp' T' (split-K)", "i4_fp64": "k_gemm<double> I4",
                 "ring_fp64": "k_gemm<double> ring", "ladder_fp64": "k_gemm<double> fused pp+hh ladder",
                 "pp_rebase_fp64": "k_gemm<double> pp-ladder at a re-base", "hh_fp64": "k_gemm<double> hh-ladder",
-                "pp_tc": "k_tc_gemm pp-ladder correction", "i4_tc": "k_tc_gemm dI4 correction",
-                "ring_tc": "k_tc_gemm ring corrections", "split": "k_tc_split",
+                "pp_tc": "k_tc_gemm pp + hh ladder corrections (3 products, one accumulator)", "i4_tc": "k_tc_gemm dI4 correction",
+                "ring_tc": "k_tc_gemm ring corrections (2 products, one accumulator)", "split": "k_tc_split",
                 "pp_rebase_digits": "k_oz_gemm pp-ladder at a re-base (exact digit products)",
                 "i4_rebase_digits": "k_oz_gemm I4 at a re-base (exact digit products)",
-                "ring_rebase_digits": "k_oz_gemm ring at a re-base (exact digit products)",
-                "hh_tc": "k_tc_gemm hh-ladder corrections"}
+                "ring_rebase_digits": "k_oz_gemm ring at a re-base (exact digit products)"}
 
 
 def replica_theta(rank: int):

@@ -177,14 +177,17 @@ def device_fp64_peak(device: int = 0) -> float:
     return x.value
 
 
-def selftest_tc_gemm(shapes, kind: int = 0, use_alo: bool = True, seed: int = 1, device: int = 0):
+def selftest_tc_gemm(shapes, kind: int = 0, use_alo: bool = True, seed: int = 1, device: int = 0,
+                     segments: bool = False):
     """Tensor-core split GEMM against FP64 on random problems [(M, N, K), ...].
+    segments: K cut into up to three separately tiled products accumulated into one
+    tile plus a C0 term (even problems overwrite C, odd ones accumulate).
     Returns (max relative error, kernel ms)."""
     M = np.array([s[0] for s in shapes], np.int32)
     N = np.array([s[1] for s in shapes], np.int32)
     K = np.array([s[2] for s in shapes], np.int32)
     err, ms = C.c_double(), C.c_double()
-    _check(lib().ccx_selftest_tc_gemm(device, kind, len(shapes), _ptr(M), _ptr(N), _ptr(K), int(use_alo), seed,
+    _check(lib().ccx_selftest_tc_gemm(device, kind, len(shapes), _ptr(M), _ptr(N), _ptr(K), int(use_alo) | (2 if segments else 0), seed,
                                       C.byref(err), C.byref(ms)))
     return err.value, ms.value
 
@@ -533,7 +536,7 @@ class Engine:
 
     KERNEL_SLOTS = ("x_fp64", "i4_fp64", "ring_fp64", "ladder_fp64", "pp_rebase_fp64", "hh_fp64",
                     "pp_tc", "i4_tc", "ring_tc", "split", "pp_rebase_digits", "i4_rebase_digits",
-                    "ring_rebase_digits", "unused13", "hh_tc")
+                    "ring_rebase_digits")
 
     def autotune(self):
         """Pick the FP64 GEMM tile shape per N bucket by timing; returns (shapes, ms)."""

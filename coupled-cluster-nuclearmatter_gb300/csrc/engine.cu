@@ -1339,8 +1339,10 @@ class Engine final : public IEngine {
       const int ph = l.phase[t.prob];
       const int k = p.npad <= 32 ? 0 : p.npad <= 64 ? 1 : p.npad <= 128 ? 2 : 3;
       b[ph][k].push_back(t);
+      int nk = p.nk;
+      for (int e = 0; e < p.next; ++e) nk += p.ext[e].nk;
       pl.npad_max[ph][k] = std::max(pl.npad_max[ph][k], p.npad);
-      pl.max_nk[ph][k] = std::max(pl.max_nk[ph][k], p.nk);
+      pl.max_nk[ph][k] = std::max(pl.max_nk[ph][k], nk);
     }
     for (int ph = 0; ph < 2; ++ph)
       for (int k = 0; k < kTcBuckets; ++k) {
@@ -1406,6 +1408,62 @@ class Engine final : public IEngine {
         p.M = M; p.N = nb; p.nk = (K + tk - 1) / tk; p.npad = (nb + 15) / 16 * 16;
         p.bstride = npad_all > 256 ? (int64_t)npad_all * 128 : 0;
         p.C = (double *)C + cc + (int64_t)n0 * sCn * kNComp; p.sCm = sCm * kNComp; p.sCn = sCn * kNComp; p.alpha = al;
+        for (int mt = 0; mt < (M + 127) / 128; ++mt) l.tiles.push_back(TcTile{(int)l.probs.size(), mt});
+        l.probs.push_back(p);
+        l.phase.push_back(ph);
+      }
+    };
+    if (kNComp == 1) {
+      one(0, 0, 0, alpha, 0);
+    } else {
+      one(0, 0, 0, alpha, 0);
+      one(0, 1, 1, alpha, 0);
+      one(1, 1, 0, -alpha, 1);
+      one(1, 0, 1, alpha, 1);
+    }
+  }
+  // Up to three products accumulated into one output tile and written once:
+  // C = (overwrite ? 0 : C) + C0 + alpha sum_op A_op B_op, every op with the same M, N.
+  struct TcOp {
+    TileBuf *a;
+    int64_t ao;
+    TileBuf *b;
+    int64_t bo;
+    int K;
+  };
+  void add_tc_multi(TcList &l, const std::vector<TcOp> &ops, int M, int N, S *C, int64_t sCm, int64_t sCn, double alpha,
+                    const S *C0, int overwrite) {
+    const size_t es = tc_kind_ == kTcBF16 ? 2 : 4;
+    const int tk = tc_tile_k(tc_kind_);
+    const int npad_all = (N + 15) / 16 * 16;
+    // ca / cb: operand components, cc: output component; C0 and overwrite apply in phase 0
+    auto one = [&](int ca, int cb, int cc, double al, int ph) {
+      for (int n0 = 0; n0 < N; n0 += 256) {
+        const int nb = std::min(256, N - n0);
+        TcProb p{};
+        for (size_t q = 0; q < ops.size(); ++q) {
+          const TcOp &o = ops[q];
+          TcSeg g{};
+          g.Ahi = (char *)o.a->hi.p + (o.ao + ca * o.a->n) * es;
+          g.Alo = (char *)o.a->lo.p + (o.ao + ca * o.a->n) * es;
+          g.Bhi = (char *)o.b->hi.p + (o.bo + cb * o.b->n) * es + (size_t)n0 * 128;
+          g.Blo = (char *)o.b->lo.p + (o.bo + cb * o.b->n) * es + (size_t)n0 * 128;
+          g.nk = (o.K + tk - 1) / tk;
+          g.bstride = npad_all > 256 ? (int64_t)npad_all * 128 : 0;
+          if (q == 0) {
+            p.Ahi = g.Ahi; p.Alo = g.Alo; p.Bhi = g.Bhi; p.Blo = g.Blo; p.nk = g.nk; p.bstride = g.bstride;
+          } else {
+            p.ext[q - 1] = g;
+          }
+        }
+        p.next = (int)ops.size() - 1;
+        p.M = M; p.N = nb; p.npad = (nb + 15) / 16 * 16;
+        const int64_t coff = cc + (int64_t)n0 * sCn * kNComp;
+        p.C = (double *)C + coff; p.sCm = sCm * kNComp; p.sCn = sCn * kNComp; p.alpha = al;
+        if (ph == 0) {
+          p.C0 = C0 ? (const double *)C0 + coff : nullptr;
+          p.overwrite = overwrite;
+        }
         for (int mt = 0; mt < (M + 127) / 128; ++mt) l.tiles.push_back(TcTile{(int)l.probs.size(), mt});
         l.probs.push_back(p);
         l.phase.push_back(ph);
@@ -1681,7 +1739,7 @@ class Engine final : public IEngine {
     tcerr_.alloc(sizeof(int), &bytes_);
     CK(cudaMemset(tcerr_.p, 0, sizeof(int)));
     std::vector<TcSplitJob> js_static, js_tphb, js_it1, js_it2, js_it3;
-    TcList pp, p4, pr1, pr2, lh1, lh2;
+    TcList pp, p4, pr1;
     {
       int64_t oa = 0, ob = 0, voff = 0, hoff = 0, oda = 0, otb = 0, oi9 = 0;
       for (int c = 0; c < nc; ++c) {
@@ -1690,14 +1748,14 @@ class Engine final : public IEngine {
           S *t = T_.as<S>() + pk.t_off, *tb = Tb_.as<S>() + pk.t_off;
           add_split(js_static, Vpp_.as<S>() + voff, nullptr, pk.P, 1, pk.P, pk.P, 128, mpad(pk.P), tVpp_, oa);
           add_split(js_it1, t, tb, pk.P, 1, pk.H, pk.P, npadf(pk.H), npadf(pk.H), tD_, ob);
-          add_tc(pp, tVpp_, oa, tD_, ob, pk.P, pk.H, pk.P, R_.as<S>() + pk.t_off, 1, pk.P, 1.0);
           // hh-ladder: R' += HH_b + dT' I9' + T_b' (I9' - I9_b')
           add_split(js_it1, t, tb, 1, pk.P, pk.P, pk.H, 128, mpad(pk.P), tDA_, oda);
           add_split(js_tphb, tb, nullptr, 1, pk.P, pk.P, pk.H, 128, mpad(pk.P), tTbA_, otb);
           add_split(js_it3, I9_.as<S>() + hoff, nullptr, pk.H, 1, pk.H, pk.H, npadf(pk.H), npadf(pk.H), tI9B_, oi9);
           add_split(js_it3, dI9_.as<S>() + hoff, nullptr, pk.H, 1, pk.H, pk.H, npadf(pk.H), npadf(pk.H), tdI9B_, oi9);
-          add_tc(lh1, tDA_, oda, tI9B_, oi9, pk.P, pk.H, pk.H, R_.as<S>() + pk.t_off, 1, pk.P, 1.0);
-          add_tc(lh2, tTbA_, otb, tdI9B_, oi9, pk.P, pk.H, pk.H, R_.as<S>() + pk.t_off, 1, pk.P, 1.0);
+          // R' += PP_b + HH_b + V_pppp' dT' + dT' I9' + T_b' (I9' - I9_b'), written once
+          add_tc_multi(pp, {{&tVpp_, oa, &tD_, ob, pk.P}, {&tDA_, oda, &tI9B_, oi9, pk.H}, {&tTbA_, otb, &tdI9B_, oi9, pk.H}},
+                       pk.P, pk.H, R_.as<S>() + pk.t_off, 1, pk.P, 1.0, PPb_.as<S>() + pk.t_off, 0);
           oa += (int64_t)mpad(pk.P) * nkf(pk.P) * tk;
           ob += (int64_t)npadf(pk.H) * nkf(pk.P) * tk;
           oda += (int64_t)mpad(pk.P) * nkf(pk.H) * tk;
@@ -1725,8 +1783,9 @@ class Engine final : public IEngine {
           add_split(js_it2, dI4_.as<S>() + ioff, nullptr, nhp, 1, nhp, nhp, npadf(nhp), npadf(nhp), tdI4B_, oi);
           add_split(js_it2, I4_.as<S>() + ioff, nullptr, nhp, 1, nhp, nhp, npadf(nhp), npadf(nhp), tI4B_, oib);
           add_tc(p4, tVph_, ov, tDphB_, odb, nhp, nhp, nph, dI4_.as<S>() + ioff, 1, nhp, 0.5);
-          add_tc(pr1, tTphbA_, ota, tdI4B_, oi, nph, nhp, nhp, Rph_.as<S>() + toff, 1, nph, 1.0);
-          add_tc(pr2, tDphA_, oda, tI4B_, oib, nph, nhp, nhp, Rph_.as<S>() + toff, 1, nph, 1.0);
+          // R_ph = R_ph,b + T_ph,b dI4 + dT_ph I4, written once
+          add_tc_multi(pr1, {{&tTphbA_, ota, &tdI4B_, oi, nhp}, {&tDphA_, oda, &tI4B_, oib, nhp}}, nph, nhp,
+                       Rph_.as<S>() + toff, 1, nph, 1.0, Rphb_.as<S>() + toff, 1);
           ov += (int64_t)mpad(nhp) * nkf(nph) * tk;
           odb += (int64_t)npadf(nhp) * nkf(nph) * tk;
           ota += (int64_t)mpad(nph) * nkf(nhp) * tk;
@@ -1743,12 +1802,9 @@ class Engine final : public IEngine {
     finalize_split(spIter1_, js_it1);
     finalize_split(spIter2_, js_it2);
     finalize_split(spIter3_, js_it3);
-    finalize_tc(tcHH1_, lh1);
-    finalize_tc(tcHH2_, lh2);
     finalize_tc(tcPP_, pp);
     finalize_tc(tcI4_, p4);
     finalize_tc(tcR1_, pr1);
-    finalize_tc(tcR2_, pr2);
     // FP64 plans of the re-base: PP_b = V_pppp' T, and R' += T I9
     {
       PlanBuilder bp, bh;
@@ -1902,28 +1958,17 @@ class Engine final : public IEngine {
     run_split(spIter2_);  // dI4 (B), I4 (B)
     kend();
     mark(4);
-    CK(cudaMemcpyAsync(Rph_.p, Rphb_.p, std::max<int64_t>(n_ph_, 1) * sizeof(S), cudaMemcpyDeviceToDevice, st_));
     kbegin(kKTcRing);
-    run_tc(tcR1_);  // R_ph += T_ph,b dI4
-    kend();
-    kbegin(kKTcRing);
-    run_tc(tcR2_);  // R_ph += dT_ph I4
+    run_tc(tcR1_);  // R_ph = R_ph,b + T_ph,b dI4 + dT_ph I4
     kend();
     mark(5);
     launch_rinit<S>(D_, T_.as<S>(), Vhp_.as<S>(), Rph_.as<S>(), i6off_.as<S>(), i7off_.as<S>(), R_.as<S>(), st_);
     mark(6);
-    launch_axpy<S>(n_t_, PPb_.as<S>(), R_.as<S>(), st_);  // PP_b + HH_b
     kbegin(kKTcPP);
-    run_tc(tcPP_);  // R' += V_pppp' dT
-    kend();
-    kbegin(kKHHTc);
-    run_tc(tcHH1_);  // R' += dT' I9'
-    kend();
-    kbegin(kKHHTc);
-    run_tc(tcHH2_);  // R' += T_b' (I9' - I9_b')
+    run_tc(tcPP_);  // R' += PP_b + HH_b + V_pppp' dT' + dT' I9' + T_b' (I9' - I9_b')
     kend();
     mark(7);
-    launches_ += 8;
+    launches_ += 7;  // gather, sub, i7, i9, i6, add, rinit
     if (timing_) accumulate_timers(0, 7);
   }
 
@@ -1969,7 +2014,7 @@ class Engine final : public IEngine {
   bool oz_ready_ = false;
   int64_t oz_v_version_ = -1;
   TileBuf tVpp_, tD_, tVph_, tDphB_, tTphbA_, tDphA_, tdI4B_, tI4B_, tDA_, tI9B_, tTbA_, tdI9B_;
-  TcPlan tcPP_, tcI4_, tcR1_, tcR2_, tcHH1_, tcHH2_;
+  TcPlan tcPP_, tcI4_, tcR1_;
   SplitPlan spStatic_, spTphb_, spIter1_, spIter2_, spIter3_;
   double *host_res_ = nullptr;
   int host_flag_ = 0;

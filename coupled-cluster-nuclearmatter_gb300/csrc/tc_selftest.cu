@@ -152,11 +152,16 @@ void tc_selftest(int device, int kind, int nprob, const int *Ms, const int *Ns, 
   }
   const int tk = kind == kTcBF16 ? 64 : 32;
   const int es = kind == kTcBF16 ? 2 : 4;
+  // use_alo bit 1: K cut into up to three separately tiled segments accumulated into one
+  // tile, with a C0 term; even problems C = C0 + 1/2 A B, odd ones C += C0 + 1/2 A B
+  const bool segmented = (use_alo & 2) != 0;
+  use_alo &= 1;
   std::mt19937_64 rng(seed);
   std::uniform_real_distribution<double> U(-1.0, 1.0);
   struct Host {
     int M, N, K, nk, npad, mpad;
-    std::vector<double> A, B, C;
+    std::vector<double> A, B, C, C0;
+    std::vector<int> kseg;  // segment boundaries in K (multiples of the K tile)
     size_t a_el, b_el;
   };
   std::vector<Host> h(nprob);
@@ -178,8 +183,18 @@ void tc_selftest(int device, int kind, int nprob, const int *Ms, const int *Ns, 
     for (double &v : x.A) v = U(rng) * std::pow(10.0, -3.0 * std::fabs(U(rng)));
     for (double &v : x.B) v = U(rng) * std::pow(10.0, -3.0 * std::fabs(U(rng)));
     for (double &v : x.C) v = U(rng);
-    x.a_el = (size_t)x.mpad * x.nk * tk;
-    x.b_el = (size_t)x.npad * x.nk * tk;
+    x.kseg = {0};
+    const int nseg = segmented ? std::min(3, x.nk) : 1;
+    for (int g = 1; g < nseg; ++g) x.kseg.push_back(x.nk * g / nseg * tk);
+    x.kseg.push_back(x.K);
+    if (segmented) {
+      x.C0.resize(x.C.size());
+      for (double &v : x.C0) v = U(rng);
+    }
+    int nk_all = 0;
+    for (size_t g = 0; g + 1 < x.kseg.size(); ++g) nk_all += (x.kseg[g + 1] - x.kseg[g] + tk - 1) / tk;
+    x.a_el = (size_t)x.mpad * nk_all * tk;
+    x.b_el = (size_t)x.npad * nk_all * tk;
     a_tot += x.a_el;
     b_tot += x.b_el;
     c_tot += x.C.size();
@@ -187,7 +202,8 @@ void tc_selftest(int device, int kind, int nprob, const int *Ms, const int *Ns, 
   // FP64 device copies of the inputs (A row-major M x K, B column-major K x N, C col-major)
   size_t fa = 0, fb = 0;
   for (auto &x : h) { fa += x.A.size(); fb += x.B.size(); }
-  Dev dA(fa * 8), dB(fb * 8), dC(c_tot * 8), tAh(a_tot * es), tAl(a_tot * es), tBh(b_tot * es), tBl(b_tot * es);
+  Dev dA(fa * 8), dB(fb * 8), dC(c_tot * 8), dC0(segmented ? c_tot * 8 : 8), tAh(a_tot * es), tAl(a_tot * es),
+      tBh(b_tot * es), tBl(b_tot * es);
   std::vector<TcSplitJob> jobs;
   std::vector<TcProb> probs;
   std::vector<TcTile> tiles;
@@ -197,24 +213,47 @@ void tc_selftest(int device, int kind, int nprob, const int *Ms, const int *Ns, 
     sck(cudaMemcpy((double *)dA.p + oa, x.A.data(), x.A.size() * 8, cudaMemcpyHostToDevice), "copy A");
     sck(cudaMemcpy((double *)dB.p + ob, x.B.data(), x.B.size() * 8, cudaMemcpyHostToDevice), "copy B");
     sck(cudaMemcpy((double *)dC.p + oc, x.C.data(), x.C.size() * 8, cudaMemcpyHostToDevice), "copy C");
-    TcSplitJob ja{};
-    ja.src = (double *)dA.p + oa; ja.sub = nullptr; ja.sr = x.K; ja.sk = 1;
-    ja.rows = x.M; ja.cols = x.K; ja.tile_rows = 128; ja.nk = x.nk; ja.rows_pad = x.mpad;
-    ja.hi = (char *)tAh.p + ta * es; ja.lo = (char *)tAl.p + ta * es; ja.scale = 1.0;
-    TcSplitJob jb{};
-    jb.src = (double *)dB.p + ob; jb.sub = nullptr; jb.sr = x.K; jb.sk = 1;  // B(n, k) = B_colmajor[k + K n]
-    jb.rows = x.N; jb.cols = x.K; jb.tile_rows = x.npad; jb.nk = x.nk; jb.rows_pad = x.npad;
-    jb.hi = (char *)tBh.p + tb * es; jb.lo = (char *)tBl.p + tb * es; jb.scale = 1.0;
-    jobs.push_back(ja);
-    jobs.push_back(jb);
+    if (segmented)
+      sck(cudaMemcpy((double *)dC0.p + oc, x.C0.data(), x.C0.size() * 8, cudaMemcpyHostToDevice), "copy C0");
+    std::vector<TcSeg> segs;
+    size_t sa = ta, sb = tb;
+    for (size_t g = 0; g + 1 < x.kseg.size(); ++g) {
+      const int k0 = x.kseg[g], kg = x.kseg[g + 1] - k0, nkg = (kg + tk - 1) / tk;
+      TcSplitJob ja{};
+      ja.src = (double *)dA.p + oa + k0; ja.sub = nullptr; ja.sr = x.K; ja.sk = 1;
+      ja.rows = x.M; ja.cols = kg; ja.tile_rows = 128; ja.nk = nkg; ja.rows_pad = x.mpad;
+      ja.hi = (char *)tAh.p + sa * es; ja.lo = (char *)tAl.p + sa * es; ja.scale = 1.0;
+      TcSplitJob jb{};
+      jb.src = (double *)dB.p + ob + k0; jb.sub = nullptr; jb.sr = x.K; jb.sk = 1;  // B(n, k) = B_colmajor[k + K n]
+      jb.rows = x.N; jb.cols = kg; jb.tile_rows = x.npad; jb.nk = nkg; jb.rows_pad = x.npad;
+      jb.hi = (char *)tBh.p + sb * es; jb.lo = (char *)tBl.p + sb * es; jb.scale = 1.0;
+      jobs.push_back(ja);
+      jobs.push_back(jb);
+      segs.push_back(TcSeg{ja.hi, use_alo ? ja.lo : nullptr, jb.hi, jb.lo, nkg, 0});
+      sa += (size_t)x.mpad * nkg * tk;
+      sb += (size_t)x.npad * nkg * tk;
+    }
     // N beyond one accumulator: column blocks of <= 256 stepping through the whole B
     for (int n0 = 0; n0 < x.N; n0 += 256) {
       const int nb = std::min(256, x.N - n0);
+      const int64_t bst = x.npad > 256 ? (int64_t)x.npad * 128 : 0;
       TcProb p{};
-      p.Ahi = ja.hi; p.Alo = use_alo ? ja.lo : nullptr;
-      p.Bhi = (char *)jb.hi + (size_t)n0 * 128; p.Blo = (char *)jb.lo + (size_t)n0 * 128;
-      p.M = x.M; p.N = nb; p.nk = x.nk; p.npad = (nb + 15) / 16 * 16;
-      p.bstride = x.npad > 256 ? (int64_t)x.npad * 128 : 0;
+      p.Ahi = segs[0].Ahi; p.Alo = segs[0].Alo;
+      p.Bhi = (const char *)segs[0].Bhi + (size_t)n0 * 128; p.Blo = (const char *)segs[0].Blo + (size_t)n0 * 128;
+      p.M = x.M; p.N = nb; p.nk = segs[0].nk; p.npad = (nb + 15) / 16 * 16;
+      p.bstride = bst;
+      for (size_t g = 1; g < segs.size(); ++g) {
+        TcSeg e = segs[g];
+        e.Bhi = (const char *)e.Bhi + (size_t)n0 * 128;
+        e.Blo = (const char *)e.Blo + (size_t)n0 * 128;
+        e.bstride = bst;
+        p.ext[g - 1] = e;
+      }
+      p.next = (int)segs.size() - 1;
+      if (segmented) {
+        p.C0 = (const double *)dC0.p + oc + (size_t)n0 * x.M;
+        p.overwrite = (&x - h.data()) % 2 == 0 ? 1 : 0;
+      }
       p.C = (double *)dC.p + oc + (size_t)n0 * x.M; p.sCm = 1; p.sCn = x.M; p.alpha = 0.5;
       for (int mt = 0; mt < x.mpad / 128; ++mt) tiles.push_back(TcTile{(int)probs.size(), mt});
       probs.push_back(p);
@@ -237,8 +276,8 @@ void tc_selftest(int device, int kind, int nprob, const int *Ms, const int *Ns, 
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   cudaEventRecord(e0);
-  int max_nk = 1;
-  for (const auto &x : h) max_nk = std::max(max_nk, x.nk);
+  int max_nk = 1;  // K tiles of all segments
+  for (const auto &x : h) max_nk = std::max<int>(max_nk, (int)(x.a_el / ((size_t)x.mpad * tk)));
   launch_tc_gemm(kind, (const TcProb *)dP.p, (const TcTile *)dT.p, (int)tiles.size(), npad_max, max_nk, (int *)dE.p, 0);
   cudaEventRecord(e1);
   sck(cudaGetLastError(), "tc gemm launch");
@@ -263,7 +302,10 @@ void tc_selftest(int device, int kind, int nprob, const int *Ms, const int *Ns, 
         for (int k = 0; k < x.K; ++k) ref += x.A[(size_t)m * x.K + k] * x.B[(size_t)k + (size_t)x.K * n];
         const double prod = 0.5 * ref;
         scale = std::max(scale, std::fabs(prod));
-        diff = std::max(diff, std::fabs(c[m + (size_t)x.M * n] - (x.C[m + (size_t)x.M * n] + prod)));
+        const size_t e = m + (size_t)x.M * n;
+        double want = x.C[e] + prod;
+        if (segmented) want = ((&x - h.data()) % 2 == 0 ? 0.0 : x.C[e]) + x.C0[e] + prod;
+        diff = std::max(diff, std::fabs(c[e] - want));
       }
     worst = std::max(worst, diff / std::max(scale, 1e-300));
     oc += x.C.size();

@@ -3,9 +3,10 @@
 // C(fp64) += alpha * (A_hi B_hi + A_hi B_lo + A_lo B_hi), with the hi/lo pairs of BF16
 // (kind::f16) or TF32 (kind::tf32) operands, FP32 accumulation in tensor memory.
 // One CTA of 128 threads per 128-row tile of one problem, all N (<= 256) columns in one
-// accumulator.  Thread 0 streams the pre-tiled K tiles of A and B into a ring of
-// shared-memory stages with cp.async.bulk (one contiguous copy per operand tile,
-// completion on an mbarrier) and issues the MMAs; tcgen05.commit releases each stage.
+// accumulator, which may sum up to three products with the same M, N (segments).  Lane 0
+// of warp 1 streams the pre-tiled K tiles of A and B into a ring of shared-memory stages
+// with cp.async.bulk (one contiguous copy per operand tile, completion on an mbarrier);
+// lane 0 of warp 0 issues the MMAs, and tcgen05.commit hands each stage back.
 // The four warps then read their 32 TMEM lanes (rows) with tcgen05.ld and add into C.
 // Every mbarrier wait is bounded by a clock budget: on expiry the kernel records an
 // error code, lets its own copies land, frees its TMEM and returns.
@@ -24,22 +25,31 @@ namespace {
 
 using namespace tcptx;
 
+// K tiles of segment e of a problem (e = 0: the problem's own operands)
+__device__ __forceinline__ TcSeg tc_segment(const TcProb *__restrict__ pp, int e) {
+  if (e == 0) return TcSeg{pp->Ahi, pp->Alo, pp->Bhi, pp->Blo, pp->nk, pp->bstride};
+  return pp->ext[e - 1];
+}
+
 template <int KIND>
 __global__ void __launch_bounds__(128) k_tc_gemm(const TcProb *__restrict__ probs, const TcTile *__restrict__ tiles,
                                                 int stages, int npad_max, int *err) {
   extern __shared__ __align__(1024) uint8_t smem[];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const TcTile tl = tiles[blockIdx.x];
-  // by value: the epilogue's stores to C must not force re-reads of the descriptor
-  const TcProb P = probs[tl.prob];
-  const int npad = P.npad, nk = P.nk;
-  if (npad < 16 || npad > 256 || (npad & 15) || npad > npad_max) {
+  const TcProb *__restrict__ pp = probs + tl.prob;
+  // scalars of the descriptor in registers: the epilogue's stores to C must not force
+  // re-reads of it
+  const int npad = pp->npad;
+  const int nseg = 1 + min(max(pp->next, 0), 2);
+  int nk = 0;
+  for (int e = 0; e < nseg; ++e) nk += tc_segment(pp, e).nk;
+  if (npad < 16 || npad > 256 || (npad & 15) || npad > npad_max || nk < 1) {
     if (tid == 0) atomicExch(err, 4);
     return;
   }
   constexpr uint32_t a_bytes = 128u * 128u;
   const uint32_t b_bytes = (uint32_t)npad * 128u;
-  const size_t bstep = P.bstride ? (size_t)P.bstride : (size_t)b_bytes;
   const uint32_t stage_bytes = 2u * a_bytes + 2u * (uint32_t)npad_max * 128u;
   uint64_t *full = (uint64_t *)(smem + (size_t)stages * stage_bytes);
   uint64_t *empty = full + stages;
@@ -47,9 +57,15 @@ __global__ void __launch_bounds__(128) k_tc_gemm(const TcProb *__restrict__ prob
   uint32_t *tmem_slot = (uint32_t *)(done + 1);
   uint32_t ncols = 32;
   while (ncols < (uint32_t)npad) ncols <<= 1;
+  // one FP32 accumulator per segment while they fit in the 512 TMEM columns (a segment
+  // beyond that adds into the last one): each product then keeps the rounding of its
+  // own accumulation, and the epilogue sums them in FP64
+  int nacc = nseg;
+  while (nacc > 1 && (uint32_t)nacc * ncols > 512u) --nacc;
+  const uint32_t alloc_cols = ncols * (nacc == 3 ? 4u : (uint32_t)nacc);
 
   if (warp == 0) {
-    tmem_alloc(smem_u32(tmem_slot), ncols);
+    tmem_alloc(smem_u32(tmem_slot), alloc_cols);
     tmem_relinquish();
   }
   if (tid == 0) {
@@ -64,68 +80,84 @@ __global__ void __launch_bounds__(128) k_tc_gemm(const TcProb *__restrict__ prob
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
-  const bool two_a = P.Alo != nullptr;
 
   if (tid == 0) {
-    const uint8_t *Ahi = (const uint8_t *)P.Ahi + (size_t)tl.mt * nk * a_bytes;
-    const uint8_t *Alo = two_a ? (const uint8_t *)P.Alo + (size_t)tl.mt * nk * a_bytes : nullptr;
-    const uint8_t *Bhi = (const uint8_t *)P.Bhi;
-    const uint8_t *Blo = (const uint8_t *)P.Blo;
-    const uint32_t tx = (two_a ? 2u : 1u) * a_bytes + 2u * b_bytes;
-    int issued[8] = {0, 0, 0, 0, 0, 0, 0, 0}, landed[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    auto load = [&](int kt, int s) {
-      uint8_t *st = smem + (size_t)s * stage_bytes;
-      const uint32_t fb = smem_u32(&full[s]);
-      mbar_expect_tx(fb, tx);
-      bulk_g2s(smem_u32(st), Ahi + (size_t)kt * a_bytes, a_bytes, fb);
-      if (two_a) bulk_g2s(smem_u32(st + a_bytes), Alo + (size_t)kt * a_bytes, a_bytes, fb);
-      bulk_g2s(smem_u32(st + 2 * a_bytes), Bhi + (size_t)kt * bstep, b_bytes, fb);
-      bulk_g2s(smem_u32(st + 2 * a_bytes + (size_t)npad_max * 128), Blo + (size_t)kt * bstep, b_bytes, fb);
-      ++issued[s];
-    };
+    // MMA issuer: the K tiles of every segment, one after the other, into one
+    // accumulator; tcgen05.commit hands each stage back to the producer
     const uint32_t idesc = instr_desc<KIND>(128, npad);
-    const int pre = min(stages, nk);
-    for (int s = 0; s < pre; ++s) load(s, s);
-    int code = 0;
-    for (int kt = 0; kt < nk; ++kt) {
-      const int s = kt % stages;
-      const uint32_t ph = (uint32_t)(kt / stages) & 1u;
-      if (!mbar_wait(smem_u32(&full[s]), ph)) {
-        code = 1;
-        break;
-      }
-      ++landed[s];
-      tc_fence_after();
-      const uint32_t sa = smem_u32(smem + (size_t)s * stage_bytes);
-      const uint32_t sal = sa + a_bytes;
-      const uint32_t sb = sa + 2 * a_bytes;
-      const uint32_t sbl = sb + (uint32_t)npad_max * 128u;
-#pragma unroll
-      for (int ks = 0; ks < 4; ++ks) {
-        const uint32_t o = (uint32_t)ks * 256u;
-        const uint32_t acc0 = (kt > 0 || ks > 0) ? 1u : 0u;
-        tc_mma<KIND>(tmem, smem_desc(sa + o), smem_desc(sb + o), idesc, acc0);
-        tc_mma<KIND>(tmem, smem_desc(sa + o), smem_desc(sbl + o), idesc, 1u);
-        if (two_a) tc_mma<KIND>(tmem, smem_desc(sal + o), smem_desc(sb + o), idesc, 1u);
-      }
-      tc_commit(smem_u32(&empty[s]));
-      if (kt + stages < nk) {
-        if (!mbar_wait(smem_u32(&empty[s]), ph)) {
-          code = 2;
+    int code = 0, s = 0;
+    uint32_t ph = 0;
+    for (int e = 0; e < nseg && !code; ++e) {
+      const TcSeg g = tc_segment(pp, e);
+      const bool two_a = g.Alo != nullptr;
+      const uint32_t acc = tmem + (uint32_t)min(e, nacc - 1) * ncols;
+      bool first = e < nacc;  // this segment opens its accumulator
+      for (int kl = 0; kl < g.nk; ++kl) {
+        if (!mbar_wait(smem_u32(&full[s]), ph)) {
+          code = 1;
           break;
         }
-        load(kt + stages, s);
+        tc_fence_after();
+        const uint32_t sa = smem_u32(smem + (size_t)s * stage_bytes);
+        const uint32_t sal = sa + a_bytes;
+        const uint32_t sb = sa + 2 * a_bytes;
+        const uint32_t sbl = sb + (uint32_t)npad_max * 128u;
+#pragma unroll
+        for (int ks = 0; ks < 4; ++ks) {
+          const uint32_t o = (uint32_t)ks * 256u;
+          tc_mma<KIND>(acc, smem_desc(sa + o), smem_desc(sb + o), idesc, first ? 0u : 1u);
+          first = false;
+          tc_mma<KIND>(acc, smem_desc(sa + o), smem_desc(sbl + o), idesc, 1u);
+          if (two_a) tc_mma<KIND>(acc, smem_desc(sal + o), smem_desc(sb + o), idesc, 1u);
+        }
+        tc_commit(smem_u32(&empty[s]));
+        if (++s == stages) {
+          s = 0;
+          ph ^= 1u;
+        }
       }
     }
     tc_commit(smem_u32(done));
-    if (code) {
-      atomicExch(err, code);
-      // let this CTA's own copies land before the shared memory goes away
-      for (int s = 0; s < stages; ++s)
-        while (landed[s] < issued[s]) {
-          if (!mbar_wait(smem_u32(&full[s]), (uint32_t)landed[s] & 1u)) break;
-          ++landed[s];
+    if (code) atomicExch(err, code);
+  } else if (tid == 32) {
+    // producer: one bulk copy per operand tile into the stage ring; a stage is refilled
+    // once the MMAs that read it have completed
+    int code = 0, s = 0, kt = 0;
+    uint32_t ph = 0;
+    for (int e = 0; e < nseg && !code; ++e) {
+      const TcSeg g = tc_segment(pp, e);
+      const bool two_a = g.Alo != nullptr;
+      const size_t bst = g.bstride ? (size_t)g.bstride : (size_t)b_bytes;
+      const uint8_t *Ahi = (const uint8_t *)g.Ahi + (size_t)tl.mt * g.nk * a_bytes;
+      const uint8_t *Alo = two_a ? (const uint8_t *)g.Alo + (size_t)tl.mt * g.nk * a_bytes : nullptr;
+      const uint8_t *Bhi = (const uint8_t *)g.Bhi, *Blo = (const uint8_t *)g.Blo;
+      const uint32_t tx = (two_a ? 2u : 1u) * a_bytes + 2u * b_bytes;
+      for (int kl = 0; kl < g.nk; ++kl) {
+        // refill j = kt / stages of stage s waits for consumption j - 1 (parity ph ^ 1)
+        if (kt >= stages && !mbar_wait(smem_u32(&empty[s]), ph ^ 1u)) {
+          code = 2;
+          break;
         }
+        uint8_t *st = smem + (size_t)s * stage_bytes;
+        const uint32_t fb = smem_u32(&full[s]);
+        mbar_expect_tx(fb, tx);
+        bulk_g2s(smem_u32(st), Ahi + (size_t)kl * a_bytes, a_bytes, fb);
+        if (two_a) bulk_g2s(smem_u32(st + a_bytes), Alo + (size_t)kl * a_bytes, a_bytes, fb);
+        bulk_g2s(smem_u32(st + 2 * a_bytes), Bhi + (size_t)kl * bst, b_bytes, fb);
+        bulk_g2s(smem_u32(st + 2 * a_bytes + (size_t)npad_max * 128), Blo + (size_t)kl * bst, b_bytes, fb);
+        ++kt;
+        if (++s == stages) {
+          s = 0;
+          ph ^= 1u;
+        }
+      }
+    }
+    if (code) atomicExch(err, code);
+    // every copy this CTA issued lands before the shared memory goes away: stage q
+    // received loads 0 .. n_q - 1, the last of them completing phase n_q - 1 of full[q]
+    for (int q = 0; q < stages; ++q) {
+      const int n_q = kt > q ? (kt - q + stages - 1) / stages : 0;
+      if (n_q > 0 && !mbar_wait(smem_u32(&full[q]), (uint32_t)(n_q - 1) & 1u)) break;
     }
   }
   __syncwarp();
@@ -135,29 +167,55 @@ __global__ void __launch_bounds__(128) k_tc_gemm(const TcProb *__restrict__ prob
   const int row = warp * 32 + lane;
   const int m = tl.mt * 128 + row;
   const uint32_t tl_addr = tmem + ((uint32_t)(warp * 32) << 16);
-  double *__restrict__ crow = P.C + (int64_t)m * P.sCm;
-  const int64_t sCn = P.sCn;
-  const double alpha = P.alpha;
-  const int nvalid = P.N;
-  // 32 columns per TMEM read (npad rounded up to 32 stays inside the allocated columns)
+  const int64_t sCm = pp->sCm, sCn = pp->sCn;
+  double *__restrict__ crow = pp->C + (int64_t)m * sCm;
+  const double *C0 = pp->C0;
+  const double *__restrict__ c0row = C0 ? C0 + (int64_t)m * sCm : nullptr;
+  const bool keep = pp->overwrite == 0;
+  const double alpha = pp->alpha;
+  const int nvalid = pp->N, mvalid = pp->M;
+  // 32 columns per TMEM read (npad rounded up to 32 stays inside each accumulator)
   for (int c0 = 0; c0 < npad; c0 += 32) {
     uint32_t r[32];
     tmem_ld32(tl_addr + (uint32_t)c0, r);
     tmem_ld_wait();
-    if (fin && m < P.M) {
-      double old[32];
+    double sum[32];
 #pragma unroll
-      for (int j = 0; j < 32; ++j) old[j] = (c0 + j < nvalid) ? crow[(int64_t)(c0 + j) * sCn] : 0.0;
+    for (int j = 0; j < 32; ++j) sum[j] = (double)__uint_as_float(r[j]);
+    for (int a = 1; a < nacc; ++a) {
+      tmem_ld32(tl_addr + (uint32_t)a * ncols + (uint32_t)c0, r);
+      tmem_ld_wait();
+#pragma unroll
+      for (int j = 0; j < 32; ++j) sum[j] += (double)__uint_as_float(r[j]);
+    }
+    if (fin && m < mvalid) {
+      // the mode is uniform over the CTA: branch outside the unrolled loops so that the
+      // 32 loads of a row are issued back to back
+      double old[32];
+      if (keep) {
+#pragma unroll
+        for (int j = 0; j < 32; ++j) old[j] = (c0 + j < nvalid) ? crow[(int64_t)(c0 + j) * sCn] : 0.0;
+      } else {
+#pragma unroll
+        for (int j = 0; j < 32; ++j) old[j] = 0.0;
+      }
+      if (c0row) {
+        double add[32];
+#pragma unroll
+        for (int j = 0; j < 32; ++j) add[j] = (c0 + j < nvalid) ? c0row[(int64_t)(c0 + j) * sCn] : 0.0;
+#pragma unroll
+        for (int j = 0; j < 32; ++j) old[j] += add[j];
+      }
 #pragma unroll
       for (int j = 0; j < 32; ++j)
-        if (c0 + j < nvalid) crow[(int64_t)(c0 + j) * sCn] = old[j] + alpha * (double)__uint_as_float(r[j]);
+        if (c0 + j < nvalid) crow[(int64_t)(c0 + j) * sCn] = old[j] + alpha * sum[j];
     }
   }
   tc_fence_before();
   __syncthreads();
   if (warp == 0) {
     tc_fence_after();
-    tmem_dealloc(tmem, ncols);
+    tmem_dealloc(tmem, alloc_cols);
   }
 }
 

@@ -18,6 +18,14 @@ namespace ccx {
 // i.e. the canonical SWIZZLE_NONE K-major layout with LBO = 128 B, SBO = 1024 B.
 enum TcKind { kTcBF16 = 0, kTcTF32 = 1 };
 
+// A further product accumulated into the same output tile (same M, N): its own operands
+// and K-tile count.
+struct TcSeg {
+  const void *Ahi, *Alo, *Bhi, *Blo;
+  int nk;
+  int64_t bstride;  // as TcProb::bstride
+};
+
 struct TcProb {
   const void *Ahi, *Alo;  // pre-tiled A (this problem), nullptr Alo: A taken as hi only
   const void *Bhi, *Blo;  // pre-tiled B
@@ -28,6 +36,10 @@ struct TcProb {
   int64_t bstride;        // bytes between B K tiles (0: npad * 128, the whole B operand); a
                           // column block of a wider B points Bhi/Blo at its first row and
                           // steps by the full operand's K-tile size
+  TcSeg ext[2];           // further products into the same accumulator (next of them)
+  int next;
+  const double *C0;       // optional term added once, at C's strides
+  int overwrite;          // 1: C = C0 + alpha acc; 0: C += C0 + alpha acc
 };
 struct TcTile {
   int prob, mt;
@@ -37,8 +49,8 @@ struct TcTile {
 inline int tc_tile_k(int kind) { return kind == kTcBF16 ? 64 : 32; }
 
 // error codes written to *err (0 = ok): 1 load wait timed out, 2 MMA wait timed out,
-// 3 final wait timed out, 4 bad problem (npad > 256 or not a multiple of 16)
-// max_nk: largest K-tile count among the tiles (caps the shared-memory stages)
+// 3 final wait timed out, 4 bad problem (npad > 256 or not a multiple of 16, no K tiles)
+// max_nk: largest K-tile count (all segments) among the tiles (caps the shared-memory stages)
 void launch_tc_gemm(int kind, const TcProb *probs, const TcTile *tiles, int ntiles, int npad_max, int max_nk, int *err,
                     cudaStream_t st);
 

@@ -339,7 +339,9 @@ int ccx_device_fp64_peak(int32_t device, double *tflops);
 /* Self-test of the tensor-core split GEMM used by CCX_PREC_MIXED: nprob random
  * problems C += 1/2 A B (M_i x K_i times K_i x N_i, N_i <= 256) through the same
  * operand tiling and tcgen05 kernel, against an FP64 host product.
- * kind 0: BF16 hi/lo split, kind 1: TF32 hi/lo split; use_alo 0 drops the A_lo term;
+ * kind 0: BF16 hi/lo split, kind 1: TF32 hi/lo split; use_alo bit 0 clear drops the A_lo
+ * term; use_alo bit 1 cuts K into up to three separately tiled products accumulated in one
+ * tile with a C0 term (even problems C = C0 + 1/2 A B, odd ones C += C0 + 1/2 A B);
  * kind 2: the FP64-accurate digit-product (Ozaki) GEMM, checked against long double.
  * *max_rel_err = max |C - C_ref| / max |1/2 A B| over the problems; *ms kernel time. */
 int ccx_selftest_tc_gemm(int32_t device, int32_t kind, int32_t nprob, const int32_t *M, const int32_t *N,
@@ -354,10 +356,11 @@ int ccx_engine_timers(const ccx_engine *e, double ms[10]);
  * ccx_ccd_iter (CUDA events on the engine stream around each launch or launch group):
  * [0] X = V_hhpp' T' (FP64 split-K GEMM + reduce), [1] I4 (FP64), [2] ring (FP64),
  * [3] fused pp+hh ladder (FP64), [4] V_pppp' T' at a mixed-precision re-base (FP64),
- * [5] hh-ladder of the mixed residual (FP64), [6] pp-ladder correction (tensor cores),
- * [7] dI4 correction (tensor cores), [8] ring corrections (tensor cores),
+ * [5] hh-ladder of the mixed residual (FP64), [6] pp-ladder and hh-ladder corrections
+ * with the cached base terms, one launch (tensor cores), [7] dI4 correction (tensor
+ * cores), [8] ring corrections with the cached base ring, one launch (tensor cores),
  * [9] operand splits, [10] pp-ladder, [11] I4 and [12] ring at a re-base as digit products
- * (tensor cores), [13] unused, [14] hh-ladder corrections (tensor cores), [15] unused */
+ * (tensor cores), [13] .. [15] unused */
 int ccx_engine_kernel_timers(const ccx_engine *e, double ms[16], int64_t launches[16]);
 
 #ifdef __cplusplus

@@ -48,3 +48,12 @@ def test_wide_n_column_blocks(ccx, kind):
     """N beyond one 256-column accumulator: column blocks that step through the whole B."""
     err, _ = ccx.selftest_tc_gemm(WIDE, kind=kind)
     assert err < (2e-4 if kind == 0 else 1e-13), err
+
+
+@pytest.mark.parametrize("kind", [0, 1], ids=["bf16x3", "tf32x3"])
+def test_segmented_products_one_accumulator(ccx, kind):
+    """Several products (K cut into separately tiled segments) accumulated into one tile and
+    written once with a C0 term, overwriting C or adding to it; wide N in column blocks."""
+    shapes = RAGGED + WIDE
+    err, _ = ccx.selftest_tc_gemm(shapes, kind=kind, segments=True)
+    assert err < (2e-4 if kind == 0 else 5e-5), err
