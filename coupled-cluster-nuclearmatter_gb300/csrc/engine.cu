@@ -1344,8 +1344,17 @@ class Engine final : public IEngine {
       pl.npad_max[ph][k] = std::max(pl.npad_max[ph][k], p.npad);
       pl.max_nk[ph][k] = std::max(pl.max_nk[ph][k], nk);
     }
+    // longest tiles first: the persistent CTAs take tiles in strides of the grid
+    auto work = [&](const TcTile &t) {
+      const TcProb &p = l.probs[t.prob];
+      int nk = p.nk;
+      for (int e = 0; e < p.next; ++e) nk += p.ext[e].nk;
+      return nk;
+    };
     for (int ph = 0; ph < 2; ++ph)
       for (int k = 0; k < kTcBuckets; ++k) {
+        std::stable_sort(b[ph][k].begin(), b[ph][k].end(),
+                         [&](const TcTile &x, const TcTile &y) { return work(x) > work(y); });
         upload(pl.tiles[ph][k], b[ph][k], &bytes_);
         pl.ntiles[ph][k] = (int)b[ph][k].size();
       }
@@ -1733,6 +1742,9 @@ class Engine final : public IEngine {
     Rphb_.alloc(std::max<int64_t>(n_ph_, 1) * sz, &bytes_);
     I4b_.alloc(std::max<int64_t>(n_i4_, 1) * sz, &bytes_);
     dI4_.alloc(std::max<int64_t>(n_i4_, 1) * sz, &bytes_);
+    // the tensor-core product overwrites dI4 block by block; blocks of channels without
+    // particle-hole pairs (K = 0) have no product and stay zero
+    CK(cudaMemset(dI4_.p, 0, std::max<int64_t>(n_i4_, 1) * sz));
     Xb_.alloc(std::max<int64_t>(n_hh2_, 1) * sz, &bytes_);
     dI9_.alloc(std::max<int64_t>(n_hh2_, 1) * sz, &bytes_);
     HHb_.alloc(std::max<int64_t>(n_t_, 1) * sz, &bytes_);
@@ -1782,7 +1794,8 @@ class Engine final : public IEngine {
           // after dI4: B = dI4 and B = I4 (rows n_hp, K = n_hp)
           add_split(js_it2, dI4_.as<S>() + ioff, nullptr, nhp, 1, nhp, nhp, npadf(nhp), npadf(nhp), tdI4B_, oi);
           add_split(js_it2, I4_.as<S>() + ioff, nullptr, nhp, 1, nhp, nhp, npadf(nhp), npadf(nhp), tI4B_, oib);
-          add_tc(p4, tVph_, ov, tDphB_, odb, nhp, nhp, nph, dI4_.as<S>() + ioff, 1, nhp, 0.5);
+          // dI4 = 1/2 V_ph dT_ph, written without reading it
+          add_tc_multi(p4, {{&tVph_, ov, &tDphB_, odb, nph}}, nhp, nhp, dI4_.as<S>() + ioff, 1, nhp, 0.5, nullptr, 1);
           // R_ph = R_ph,b + T_ph,b dI4 + dT_ph I4, written once
           add_tc_multi(pr1, {{&tTphbA_, ota, &tdI4B_, oi, nhp}, {&tDphA_, oda, &tI4B_, oib, nhp}}, nph, nhp,
                        Rph_.as<S>() + toff, 1, nph, 1.0, Rphb_.as<S>() + toff, 1);
@@ -1949,7 +1962,6 @@ class Engine final : public IEngine {
     launch_i6<S>(D_, (const int2 *)i6rows_.p, ni6rows_, i6dots_.as<S>(), T_.as<S>(), Vhp_.as<S>(), fdiag_.as<S>(),
                  f6_.as<S>(), d2ab_.as<S>(), i6off_.as<S>(), st_);
     mark(3);
-    CK(cudaMemsetAsync(dI4_.p, 0, std::max<int64_t>(n_i4_, 1) * sizeof(S), st_));
     kbegin(kKTcI4);
     run_tc(tcI4_);  // dI4 = 1/2 V_ph dT_ph
     kend();

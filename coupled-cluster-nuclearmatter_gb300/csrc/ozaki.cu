@@ -113,6 +113,10 @@ __global__ void __launch_bounds__(kOzThreads, 1) k_oz_gemm(const OzProb *__restr
         const uint8_t *B0 = (const uint8_t *)P.B + (size_t)tl.n0 * 128;
         const size_t ap = (size_t)P.a_plane * 2, bp = (size_t)P.b_plane * 2, bt = (size_t)P.npad * 128;
         const uint32_t bbytes = (uint32_t)nc * 128u;
+        // live 8-row groups of each A digit tile (1 KiB each); the MMA's rows beyond them
+        // read stale shared memory and give level sums that are never stored
+        const int live_rows = min(128, P.M - tl.mt * 128);
+        const uint32_t a_copy = (uint32_t)((live_rows + 7) / 8) * 1024u;
         for (int kt = 0; kt < nk && ok; ++kt, ++bk) {
           const int bb = bk & 1;
           if (bk >= 2 && !wait(&bempty[bb], (uint32_t)(((bk >> 1) - 1) & 1))) { ok = false; break; }
@@ -125,8 +129,8 @@ __global__ void __launch_bounds__(kOzThreads, 1) k_oz_gemm(const OzProb *__restr
             const int s = cnt % kOzStages;
             if (cnt >= kOzStages && !wait(&aempty[s], (uint32_t)((cnt / kOzStages - 1) & 1))) { ok = false; break; }
             const uint32_t fa = smem_u32(&afull[s]);
-            mbar_expect_tx(fa, kATile);
-            bulk_g2s(smem_u32(abuf + s * kATile), A0 + i * ap + (size_t)kt * kATile, kATile, fa);
+            mbar_expect_tx(fa, a_copy);
+            bulk_g2s(smem_u32(abuf + s * kATile), A0 + i * ap + (size_t)kt * kATile, a_copy, fa);
             ++na[s];
             ++cnt;
           }
@@ -211,7 +215,8 @@ __global__ void __launch_bounds__(kOzThreads, 1) k_oz_gemm(const OzProb *__restr
           break;
         }
         tc_fence_after();
-        for (int cb = 0; cb < nc; cb += 16) {
+        // a warp none of whose rows is stored skips the drain
+        for (int cb = 0; cb < nc && tl.mt * 128 + warp * 32 < P.M; cb += 16) {
           long long zh[16], zl[16];
 #pragma unroll
           for (int q = 0; q < 16; ++q) zh[q] = zl[q] = 0;
@@ -229,12 +234,21 @@ __global__ void __launch_bounds__(kOzThreads, 1) k_oz_gemm(const OzProb *__restr
             }
           }
           if (live) {
+            // all loads of the row first (the stores could alias them), then the stores
+            double old[16];
+            int eb[16];
+#pragma unroll
+            for (int q = 0; q < 16; ++q) {
+              const int n = tl.n0 + cb + q;
+              old[q] = n < P.N ? crow[(int64_t)n * P.sCn] : 0.0;
+              eb[q] = n < P.N ? P.eB[n] : 0;
+            }
 #pragma unroll
             for (int q = 0; q < 16; ++q) {
               const int n = tl.n0 + cb + q;
               if (n < P.N) {
                 const double z = fma((double)zh[q], 0x1p-30, (double)zl[q] * 0x1p-60);
-                crow[(int64_t)n * P.sCn] += P.alpha * (z * pow2(eAm + P.eB[n]));
+                crow[(int64_t)n * P.sCn] = old[q] + P.alpha * (z * pow2(eAm + eb[q]));
               }
             }
           }

@@ -2,12 +2,14 @@
 //
 // C(fp64) += alpha * (A_hi B_hi + A_hi B_lo + A_lo B_hi), with the hi/lo pairs of BF16
 // (kind::f16) or TF32 (kind::tf32) operands, FP32 accumulation in tensor memory.
-// One CTA of 128 threads per 128-row tile of one problem, all N (<= 256) columns in one
-// accumulator, which may sum up to three products with the same M, N (segments).  Lane 0
-// of warp 1 streams the pre-tiled K tiles of A and B into a ring of shared-memory stages
-// with cp.async.bulk (one contiguous copy per operand tile, completion on an mbarrier);
-// lane 0 of warp 0 issues the MMAs, and tcgen05.commit hands each stage back.
-// The four warps then read their 32 TMEM lanes (rows) with tcgen05.ld and add into C.
+// Persistent: one CTA per SM walks the tile list (a tile = 128 rows of one problem, all N
+// <= 256 columns); a tile may sum up to three products with the same M, N (segments).
+// Lane 0 of warp 4 streams the pre-tiled K tiles of A and B into a ring of shared-memory
+// stages with cp.async.bulk (one contiguous copy per operand tile, completion on an
+// mbarrier); the ring runs on across tiles.  Lane 0 of warp 5 issues the MMAs into one
+// of two tensor-memory halves, alternating by tile, and tcgen05.commit hands each stage
+// back.  Warps 0-3 read their 32 TMEM lanes (rows) of the finished half with tcgen05.ld
+// and add into C while the next tile accumulates in the other half.
 // Every mbarrier wait is bounded by a clock budget: on expiry the kernel records an
 // error code, lets its own copies land, frees its TMEM and returns.
 #include <cuda_bf16.h>
@@ -25,47 +27,55 @@ namespace {
 
 using namespace tcptx;
 
+constexpr int kTcThreads = 192;   // warps 0-3 epilogue, warp 4 producer, warp 5 MMA issuer
+constexpr int kTcHalfCols = 256;  // tensor-memory columns of one accumulator half
+constexpr int kTcMaxStages = 8;
+
 // K tiles of segment e of a problem (e = 0: the problem's own operands)
 __device__ __forceinline__ TcSeg tc_segment(const TcProb *__restrict__ pp, int e) {
   if (e == 0) return TcSeg{pp->Ahi, pp->Alo, pp->Bhi, pp->Blo, pp->nk, pp->bstride};
   return pp->ext[e - 1];
 }
 
+// What every role of the kernel derives from a tile's problem, identically.
+struct TcGeom {
+  int npad, nseg, ncols, nacc;
+  bool ok;
+};
+__device__ __forceinline__ TcGeom tc_geom(const TcProb *__restrict__ pp, int npad_max) {
+  TcGeom g;
+  g.npad = pp->npad;
+  g.nseg = 1 + min(max(pp->next, 0), 2);
+  int nk = 0;
+  for (int e = 0; e < g.nseg; ++e) nk += tc_segment(pp, e).nk;
+  g.ok = g.npad >= 16 && g.npad <= 256 && (g.npad & 15) == 0 && g.npad <= npad_max && nk >= 1;
+  g.ncols = 32;
+  while (g.ncols < g.npad) g.ncols <<= 1;
+  // one FP32 accumulator per segment while they fit in half of the tensor memory (the
+  // other half holds the next tile's accumulators); a segment beyond that adds into the
+  // last one.  Each product then keeps the rounding of its own accumulation, and the
+  // epilogue sums them in FP64.
+  g.nacc = g.nseg;
+  while (g.nacc > 1 && g.nacc * g.ncols > kTcHalfCols) --g.nacc;
+  return g;
+}
+
 template <int KIND>
-__global__ void __launch_bounds__(128) k_tc_gemm(const TcProb *__restrict__ probs, const TcTile *__restrict__ tiles,
-                                                int stages, int npad_max, int *err) {
+__global__ void __launch_bounds__(kTcThreads, 1) k_tc_gemm(const TcProb *__restrict__ probs,
+                                                          const TcTile *__restrict__ tiles, int ntiles, int stages,
+                                                          int npad_max, int *err) {
   extern __shared__ __align__(1024) uint8_t smem[];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const TcTile tl = tiles[blockIdx.x];
-  const TcProb *__restrict__ pp = probs + tl.prob;
-  // scalars of the descriptor in registers: the epilogue's stores to C must not force
-  // re-reads of it
-  const int npad = pp->npad;
-  const int nseg = 1 + min(max(pp->next, 0), 2);
-  int nk = 0;
-  for (int e = 0; e < nseg; ++e) nk += tc_segment(pp, e).nk;
-  if (npad < 16 || npad > 256 || (npad & 15) || npad > npad_max || nk < 1) {
-    if (tid == 0) atomicExch(err, 4);
-    return;
-  }
   constexpr uint32_t a_bytes = 128u * 128u;
-  const uint32_t b_bytes = (uint32_t)npad * 128u;
   const uint32_t stage_bytes = 2u * a_bytes + 2u * (uint32_t)npad_max * 128u;
   uint64_t *full = (uint64_t *)(smem + (size_t)stages * stage_bytes);
   uint64_t *empty = full + stages;
-  uint64_t *done = empty + stages;
-  uint32_t *tmem_slot = (uint32_t *)(done + 1);
-  uint32_t ncols = 32;
-  while (ncols < (uint32_t)npad) ncols <<= 1;
-  // one FP32 accumulator per segment while they fit in the 512 TMEM columns (a segment
-  // beyond that adds into the last one): each product then keeps the rounding of its
-  // own accumulation, and the epilogue sums them in FP64
-  int nacc = nseg;
-  while (nacc > 1 && (uint32_t)nacc * ncols > 512u) --nacc;
-  const uint32_t alloc_cols = ncols * (nacc == 3 ? 4u : (uint32_t)nacc);
+  uint64_t *tfull = empty + stages, *tempty = tfull + 2, *fin = tempty + 2;
+  uint32_t *tmem_slot = (uint32_t *)(fin + 1);
+  volatile int *abort_flag = (volatile int *)(tmem_slot + 1);
 
   if (warp == 0) {
-    tmem_alloc(smem_u32(tmem_slot), alloc_cols);
+    tmem_alloc(smem_u32(tmem_slot), 2 * kTcHalfCols);
     tmem_relinquish();
   }
   if (tid == 0) {
@@ -73,7 +83,12 @@ __global__ void __launch_bounds__(128) k_tc_gemm(const TcProb *__restrict__ prob
       mbar_init(smem_u32(&full[s]), 1);
       mbar_init(smem_u32(&empty[s]), 1);
     }
-    mbar_init(smem_u32(done), 1);
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(smem_u32(&tfull[b]), 1);
+      mbar_init(smem_u32(&tempty[b]), 4);
+    }
+    mbar_init(smem_u32(fin), 1);
+    *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   tc_fence_before();
@@ -81,141 +96,209 @@ __global__ void __launch_bounds__(128) k_tc_gemm(const TcProb *__restrict__ prob
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
 
-  if (tid == 0) {
-    // MMA issuer: the K tiles of every segment, one after the other, into one
-    // accumulator; tcgen05.commit hands each stage back to the producer
-    const uint32_t idesc = instr_desc<KIND>(128, npad);
-    int code = 0, s = 0;
-    uint32_t ph = 0;
-    for (int e = 0; e < nseg && !code; ++e) {
-      const TcSeg g = tc_segment(pp, e);
-      const bool two_a = g.Alo != nullptr;
-      const uint32_t acc = tmem + (uint32_t)min(e, nacc - 1) * ncols;
-      bool first = e < nacc;  // this segment opens its accumulator
-      for (int kl = 0; kl < g.nk; ++kl) {
-        if (!mbar_wait(smem_u32(&full[s]), ph)) {
-          code = 1;
+  // bounded wait that also ends when another thread has given up
+  auto wait = [&](uint64_t *bar, uint32_t parity) -> bool {
+    const uint32_t b = smem_u32(bar);
+    const long long t0 = clock64();
+    while (!mbar_try_wait(b, parity)) {
+      if (*abort_flag) return false;
+      if (clock64() - t0 > kWaitBudget) {
+        *abort_flag = 1;
+        return false;
+      }
+    }
+    return true;
+  };
+
+  if (warp == 4) {
+    if (lane == 0) {
+      // producer: one bulk copy per operand tile into the stage ring, which runs on
+      // across tiles; a stage is refilled once the MMAs that read it have completed
+      int cnt = 0;
+      bool ok = true;
+      for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+        const TcTile tl = tiles[t];
+        const TcProb *__restrict__ pp = probs + tl.prob;
+        const TcGeom G = tc_geom(pp, npad_max);
+        if (!G.ok) continue;
+        const uint32_t b_bytes = (uint32_t)G.npad * 128u;
+        // live 8-row groups of the A tile (1 KiB each); the MMA's rows beyond them read
+        // stale shared memory and produce rows that are never stored
+        const int live_rows = min(128, pp->M - tl.mt * 128);
+        const uint32_t a_copy = (uint32_t)((live_rows + 7) / 8) * 1024u;
+        for (int e = 0; e < G.nseg && ok; ++e) {
+          const TcSeg g = tc_segment(pp, e);
+          const bool two_a = g.Alo != nullptr;
+          const size_t bst = g.bstride ? (size_t)g.bstride : (size_t)b_bytes;
+          const uint8_t *Ahi = (const uint8_t *)g.Ahi + (size_t)tl.mt * g.nk * a_bytes;
+          const uint8_t *Alo = two_a ? (const uint8_t *)g.Alo + (size_t)tl.mt * g.nk * a_bytes : nullptr;
+          const uint8_t *Bhi = (const uint8_t *)g.Bhi, *Blo = (const uint8_t *)g.Blo;
+          const uint32_t tx = (two_a ? 2u : 1u) * a_copy + 2u * b_bytes;
+          for (int kl = 0; kl < g.nk; ++kl, ++cnt) {
+            const int s = cnt % stages;
+            // fill j = cnt / stages of stage s waits for consumption j - 1
+            if (cnt >= stages && !wait(&empty[s], (uint32_t)((cnt / stages - 1) & 1))) {
+              ok = false;
+              break;
+            }
+            uint8_t *st = smem + (size_t)s * stage_bytes;
+            const uint32_t fb = smem_u32(&full[s]);
+            mbar_expect_tx(fb, tx);
+            bulk_g2s(smem_u32(st), Ahi + (size_t)kl * a_bytes, a_copy, fb);
+            if (two_a) bulk_g2s(smem_u32(st + a_bytes), Alo + (size_t)kl * a_bytes, a_copy, fb);
+            bulk_g2s(smem_u32(st + 2 * a_bytes), Bhi + (size_t)kl * bst, b_bytes, fb);
+            bulk_g2s(smem_u32(st + 2 * a_bytes + (size_t)npad_max * 128), Blo + (size_t)kl * bst, b_bytes, fb);
+          }
+        }
+      }
+      if (!ok) atomicExch(err, 1);
+      // every copy this CTA issued lands before the shared memory goes away: stage s
+      // received fills 0 .. n_s - 1, the last completing phase n_s - 1 of full[s]
+      for (int s = 0; s < stages; ++s) {
+        const int n_s = cnt > s ? (cnt - s + stages - 1) / stages : 0;
+        if (n_s > 0) mbar_wait(smem_u32(&full[s]), (uint32_t)((n_s - 1) & 1));
+      }
+    }
+  } else if (warp == 5) {
+    if (lane == 0) {
+      // MMA issuer: the K tiles of every segment of a tile into its accumulators in
+      // tensor-memory half b = (local tile) & 1, then tcgen05.commit to tfull[b]
+      int cnt = 0, lt = 0;
+      bool ok = true;
+      for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+        const TcTile tl = tiles[t];
+        const TcProb *__restrict__ pp = probs + tl.prob;
+        const TcGeom G = tc_geom(pp, npad_max);
+        if (!G.ok) {
+          atomicExch(err, 4);
+          continue;
+        }
+        const int b = lt & 1;
+        if (lt >= 2 && !wait(&tempty[b], (uint32_t)(((lt >> 1) - 1) & 1))) {
+          ok = false;
           break;
         }
         tc_fence_after();
-        const uint32_t sa = smem_u32(smem + (size_t)s * stage_bytes);
-        const uint32_t sal = sa + a_bytes;
-        const uint32_t sb = sa + 2 * a_bytes;
-        const uint32_t sbl = sb + (uint32_t)npad_max * 128u;
+        const uint32_t idesc = instr_desc<KIND>(128, G.npad);
+        for (int e = 0; e < G.nseg && ok; ++e) {
+          const TcSeg g = tc_segment(pp, e);
+          const bool two_a = g.Alo != nullptr;
+          const uint32_t acc = tmem + (uint32_t)(b * kTcHalfCols + min(e, G.nacc - 1) * G.ncols);
+          bool first = e < G.nacc;  // this segment opens its accumulator
+          for (int kl = 0; kl < g.nk; ++kl, ++cnt) {
+            const int s = cnt % stages;
+            if (!wait(&full[s], (uint32_t)((cnt / stages) & 1))) {
+              ok = false;
+              break;
+            }
+            tc_fence_after();
+            const uint32_t sa = smem_u32(smem + (size_t)s * stage_bytes);
+            const uint32_t sal = sa + a_bytes;
+            const uint32_t sb = sa + 2 * a_bytes;
+            const uint32_t sbl = sb + (uint32_t)npad_max * 128u;
 #pragma unroll
-        for (int ks = 0; ks < 4; ++ks) {
-          const uint32_t o = (uint32_t)ks * 256u;
-          tc_mma<KIND>(acc, smem_desc(sa + o), smem_desc(sb + o), idesc, first ? 0u : 1u);
-          first = false;
-          tc_mma<KIND>(acc, smem_desc(sa + o), smem_desc(sbl + o), idesc, 1u);
-          if (two_a) tc_mma<KIND>(acc, smem_desc(sal + o), smem_desc(sb + o), idesc, 1u);
+            for (int ks = 0; ks < 4; ++ks) {
+              const uint32_t o = (uint32_t)ks * 256u;
+              tc_mma<KIND>(acc, smem_desc(sa + o), smem_desc(sb + o), idesc, first ? 0u : 1u);
+              first = false;
+              tc_mma<KIND>(acc, smem_desc(sa + o), smem_desc(sbl + o), idesc, 1u);
+              if (two_a) tc_mma<KIND>(acc, smem_desc(sal + o), smem_desc(sb + o), idesc, 1u);
+            }
+            tc_commit(smem_u32(&empty[s]));
+          }
         }
-        tc_commit(smem_u32(&empty[s]));
-        if (++s == stages) {
-          s = 0;
-          ph ^= 1u;
+        if (ok) tc_commit(smem_u32(&tfull[b]));
+        ++lt;
+      }
+      if (!ok) atomicExch(err, 2);
+      // every MMA this thread issued completes before the tensor memory is freed
+      tc_commit(smem_u32(fin));
+      mbar_wait(smem_u32(fin), 0);
+    }
+  } else {
+    // warps 0-3: warp w reads tensor-memory lanes 32w .. 32w + 31 (rows of the tile)
+    const int row = warp * 32 + lane;
+    const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+    int lt = 0;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+      const TcTile tl = tiles[t];
+      const TcProb *__restrict__ pp = probs + tl.prob;
+      const TcGeom G = tc_geom(pp, npad_max);
+      if (!G.ok) continue;
+      const int b = lt & 1;
+      const bool got = __all_sync(0xffffffffu, wait(&tfull[b], (uint32_t)((lt >> 1) & 1)));
+      if (!got) {
+        if (lane == 0) atomicExch(err, 3);
+        break;
+      }
+      tc_fence_after();
+      const int m = tl.mt * 128 + row;
+      const int64_t sCm = pp->sCm, sCn = pp->sCn;
+      double *__restrict__ crow = pp->C + (int64_t)m * sCm;
+      const double *C0 = pp->C0;
+      const double *__restrict__ c0row = C0 ? C0 + (int64_t)m * sCm : nullptr;
+      const bool keep = pp->overwrite == 0;
+      const double alpha = pp->alpha;
+      const int nvalid = pp->N;
+      const bool live = m < pp->M;
+      const bool warp_live = tl.mt * 128 + warp * 32 < pp->M;  // uniform over the warp
+      if (!warp_live) {  // no row of this warp's lanes is stored
+        if (lane == 0) mbar_arrive(smem_u32(&tempty[b]));
+        ++lt;
+        continue;
+      }
+      const uint32_t acc0 = lane_base + (uint32_t)(b * kTcHalfCols);
+      // 32 columns per read (npad rounded up to 32 stays inside each accumulator)
+      for (int c0 = 0; c0 < G.npad; c0 += 32) {
+        uint32_t r[32];
+        tmem_ld32(acc0 + (uint32_t)c0, r);
+        tmem_ld_wait();
+        double sum[32];
+#pragma unroll
+        for (int j = 0; j < 32; ++j) sum[j] = (double)__uint_as_float(r[j]);
+        for (int a = 1; a < G.nacc; ++a) {
+          tmem_ld32(acc0 + (uint32_t)(a * G.ncols + c0), r);
+          tmem_ld_wait();
+#pragma unroll
+          for (int j = 0; j < 32; ++j) sum[j] += (double)__uint_as_float(r[j]);
+        }
+        if (c0 + 32 >= G.npad) {
+          // the accumulators of this half are read: hand it back to the MMA issuer
+          tc_fence_before();
+          __syncwarp();
+          if (lane == 0) mbar_arrive(smem_u32(&tempty[b]));
+        }
+        if (live) {
+          // the mode is uniform over the tile: branch outside the unrolled loops so that
+          // the 32 loads of a row are issued back to back
+          double old[32];
+          if (keep) {
+#pragma unroll
+            for (int j = 0; j < 32; ++j) old[j] = (c0 + j < nvalid) ? crow[(int64_t)(c0 + j) * sCn] : 0.0;
+          } else {
+#pragma unroll
+            for (int j = 0; j < 32; ++j) old[j] = 0.0;
+          }
+          if (c0row) {
+            double add[32];
+#pragma unroll
+            for (int j = 0; j < 32; ++j) add[j] = (c0 + j < nvalid) ? c0row[(int64_t)(c0 + j) * sCn] : 0.0;
+#pragma unroll
+            for (int j = 0; j < 32; ++j) old[j] += add[j];
+          }
+#pragma unroll
+          for (int j = 0; j < 32; ++j)
+            if (c0 + j < nvalid) crow[(int64_t)(c0 + j) * sCn] = old[j] + alpha * sum[j];
         }
       }
-    }
-    tc_commit(smem_u32(done));
-    if (code) atomicExch(err, code);
-  } else if (tid == 32) {
-    // producer: one bulk copy per operand tile into the stage ring; a stage is refilled
-    // once the MMAs that read it have completed
-    int code = 0, s = 0, kt = 0;
-    uint32_t ph = 0;
-    for (int e = 0; e < nseg && !code; ++e) {
-      const TcSeg g = tc_segment(pp, e);
-      const bool two_a = g.Alo != nullptr;
-      const size_t bst = g.bstride ? (size_t)g.bstride : (size_t)b_bytes;
-      const uint8_t *Ahi = (const uint8_t *)g.Ahi + (size_t)tl.mt * g.nk * a_bytes;
-      const uint8_t *Alo = two_a ? (const uint8_t *)g.Alo + (size_t)tl.mt * g.nk * a_bytes : nullptr;
-      const uint8_t *Bhi = (const uint8_t *)g.Bhi, *Blo = (const uint8_t *)g.Blo;
-      const uint32_t tx = (two_a ? 2u : 1u) * a_bytes + 2u * b_bytes;
-      for (int kl = 0; kl < g.nk; ++kl) {
-        // refill j = kt / stages of stage s waits for consumption j - 1 (parity ph ^ 1)
-        if (kt >= stages && !mbar_wait(smem_u32(&empty[s]), ph ^ 1u)) {
-          code = 2;
-          break;
-        }
-        uint8_t *st = smem + (size_t)s * stage_bytes;
-        const uint32_t fb = smem_u32(&full[s]);
-        mbar_expect_tx(fb, tx);
-        bulk_g2s(smem_u32(st), Ahi + (size_t)kl * a_bytes, a_bytes, fb);
-        if (two_a) bulk_g2s(smem_u32(st + a_bytes), Alo + (size_t)kl * a_bytes, a_bytes, fb);
-        bulk_g2s(smem_u32(st + 2 * a_bytes), Bhi + (size_t)kl * bst, b_bytes, fb);
-        bulk_g2s(smem_u32(st + 2 * a_bytes + (size_t)npad_max * 128), Blo + (size_t)kl * bst, b_bytes, fb);
-        ++kt;
-        if (++s == stages) {
-          s = 0;
-          ph ^= 1u;
-        }
-      }
-    }
-    if (code) atomicExch(err, code);
-    // every copy this CTA issued lands before the shared memory goes away: stage q
-    // received loads 0 .. n_q - 1, the last of them completing phase n_q - 1 of full[q]
-    for (int q = 0; q < stages; ++q) {
-      const int n_q = kt > q ? (kt - q + stages - 1) / stages : 0;
-      if (n_q > 0 && !mbar_wait(smem_u32(&full[q]), (uint32_t)(n_q - 1) & 1u)) break;
-    }
-  }
-  __syncwarp();
-  const bool fin = mbar_wait(smem_u32(done), 0);
-  if (!fin && lane == 0) atomicExch(err, 3);
-  tc_fence_after();
-  const int row = warp * 32 + lane;
-  const int m = tl.mt * 128 + row;
-  const uint32_t tl_addr = tmem + ((uint32_t)(warp * 32) << 16);
-  const int64_t sCm = pp->sCm, sCn = pp->sCn;
-  double *__restrict__ crow = pp->C + (int64_t)m * sCm;
-  const double *C0 = pp->C0;
-  const double *__restrict__ c0row = C0 ? C0 + (int64_t)m * sCm : nullptr;
-  const bool keep = pp->overwrite == 0;
-  const double alpha = pp->alpha;
-  const int nvalid = pp->N, mvalid = pp->M;
-  // 32 columns per TMEM read (npad rounded up to 32 stays inside each accumulator)
-  for (int c0 = 0; c0 < npad; c0 += 32) {
-    uint32_t r[32];
-    tmem_ld32(tl_addr + (uint32_t)c0, r);
-    tmem_ld_wait();
-    double sum[32];
-#pragma unroll
-    for (int j = 0; j < 32; ++j) sum[j] = (double)__uint_as_float(r[j]);
-    for (int a = 1; a < nacc; ++a) {
-      tmem_ld32(tl_addr + (uint32_t)a * ncols + (uint32_t)c0, r);
-      tmem_ld_wait();
-#pragma unroll
-      for (int j = 0; j < 32; ++j) sum[j] += (double)__uint_as_float(r[j]);
-    }
-    if (fin && m < mvalid) {
-      // the mode is uniform over the CTA: branch outside the unrolled loops so that the
-      // 32 loads of a row are issued back to back
-      double old[32];
-      if (keep) {
-#pragma unroll
-        for (int j = 0; j < 32; ++j) old[j] = (c0 + j < nvalid) ? crow[(int64_t)(c0 + j) * sCn] : 0.0;
-      } else {
-#pragma unroll
-        for (int j = 0; j < 32; ++j) old[j] = 0.0;
-      }
-      if (c0row) {
-        double add[32];
-#pragma unroll
-        for (int j = 0; j < 32; ++j) add[j] = (c0 + j < nvalid) ? c0row[(int64_t)(c0 + j) * sCn] : 0.0;
-#pragma unroll
-        for (int j = 0; j < 32; ++j) old[j] += add[j];
-      }
-#pragma unroll
-      for (int j = 0; j < 32; ++j)
-        if (c0 + j < nvalid) crow[(int64_t)(c0 + j) * sCn] = old[j] + alpha * sum[j];
+      ++lt;
     }
   }
   tc_fence_before();
   __syncthreads();
   if (warp == 0) {
     tc_fence_after();
-    tmem_dealloc(tmem, alloc_cols);
+    tmem_dealloc(tmem, 2 * kTcHalfCols);
   }
 }
 
@@ -351,19 +434,24 @@ __global__ void __launch_bounds__(256) k_tc_split(const TcSplitJob *__restrict__
 
 void launch_tc_gemm(int kind, const TcProb *probs, const TcTile *tiles, int ntiles, int npad_max, int max_nk, int *err,
                     cudaStream_t st) {
+  (void)max_nk;  // the stage ring runs on across tiles
   if (ntiles <= 0) return;
   const size_t stage_bytes = 2 * 128 * 128 + 2 * (size_t)npad_max * 128;
   const size_t budget = 227 * 1024 - 256;
-  int stages = (int)std::min<size_t>(4, budget / stage_bytes);
-  stages = std::min(stages, std::max(max_nk, 1));
+  int stages = (int)std::min<size_t>(kTcMaxStages, budget / stage_bytes);
   if (stages < 1) stages = 1;
-  const size_t smem = (size_t)stages * stage_bytes + (2 * stages + 1) * 8 + 16;
+  const size_t smem = (size_t)stages * stage_bytes + (2 * stages + 5) * 8 + 16;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (sms <= 0) sms = 1;
+  const int grid = std::min(ntiles, sms);  // persistent: one CTA per SM walks the tile list
   if (kind == kTcBF16) {
     cudaFuncSetAttribute(k_tc_gemm<kTcBF16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_tc_gemm<kTcBF16><<<ntiles, 128, smem, st>>>(probs, tiles, stages, npad_max, err);
+    k_tc_gemm<kTcBF16><<<grid, kTcThreads, smem, st>>>(probs, tiles, ntiles, stages, npad_max, err);
   } else {
     cudaFuncSetAttribute(k_tc_gemm<kTcTF32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_tc_gemm<kTcTF32><<<ntiles, 128, smem, st>>>(probs, tiles, stages, npad_max, err);
+    k_tc_gemm<kTcTF32><<<grid, kTcThreads, smem, st>>>(probs, tiles, ntiles, stages, npad_max, err);
   }
 }
 

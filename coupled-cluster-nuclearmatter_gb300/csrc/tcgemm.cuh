@@ -50,7 +50,8 @@ inline int tc_tile_k(int kind) { return kind == kTcBF16 ? 64 : 32; }
 
 // error codes written to *err (0 = ok): 1 load wait timed out, 2 MMA wait timed out,
 // 3 final wait timed out, 4 bad problem (npad > 256 or not a multiple of 16, no K tiles)
-// max_nk: largest K-tile count (all segments) among the tiles (caps the shared-memory stages)
+// max_nk: largest K-tile count (all segments) among the tiles (unused: the persistent
+// kernel's stage ring runs on across tiles)
 void launch_tc_gemm(int kind, const TcProb *probs, const TcTile *tiles, int ntiles, int npad_max, int max_nk, int *err,
                     cudaStream_t st);
 
