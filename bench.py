@@ -451,7 +451,11 @@ def run_e2e(args, ccx, torch, L, e, local, real, solve):
     return {"value": ms * 1e-3, "unit": "s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
             "host_wall_s": wall, "iterations": r["iterations"],
             "path": "ccx_set_fock + ccx_set_vblocks (all HHPP/PPPP/HHHH/HPHP blocks, one call per family) + "
-                    "ccx_setup_t_amplitudes + ccx_ccd_iter + ccx_get_t2_all"}
+                    "ccx_setup_t_amplitudes + ccx_ccd_iter + ccx_get_t2_all",
+            "host_buffers": "pinned: the packing kernels read the reference-layout blocks in place over "
+                            "NVLink-C2C (only the cache lines of unique pairs) and the amplitudes are "
+                            "unpacked straight into the host buffer; h2d_bytes_per_step is the size of "
+                            "the host inputs"}
 
 
 TWIST_LATTICES = {

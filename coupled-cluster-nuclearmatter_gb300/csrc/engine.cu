@@ -28,6 +28,20 @@ void ck(cudaError_t e, const char *what) {
 }
 #define CK(x) ck((x), #x)
 
+// Device address of host memory that the current device can read and write in place
+// (allocated or registered pinned with CUDA, hence mapped), else null: such blocks are
+// read by the packing kernels directly instead of through staging copies.
+double *device_view(const void *p) {
+  if (!p) return nullptr;
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();  // an unknown pointer is not an error here
+    return nullptr;
+  }
+  if (a.type != cudaMemoryTypeHost || !a.devicePointer) return nullptr;
+  return (double *)a.devicePointer;
+}
+
 // RAII device buffer
 struct DBuf {
   void *p = nullptr;
@@ -199,14 +213,68 @@ class Engine final : public IEngine {
 
   // one block; the host buffer is read before the call returns
   void set_vblock(int kind, int ch, const double *v) override {
-    set_vblock_async(kind, ch, v, 0);
+    if (double *dv = (kind == 1 || kind == 3 || kind == 6) ? device_view(v) : nullptr) set_vblock_direct(kind, ch, dv);
+    else set_vblock_async(kind, ch, v, 0);
     finish_vblocks();
+  }
+  // a block in device-addressable host memory, packed in place on the compute stream
+  void set_vblock_direct(int kind, int ch, const double *src) {
+    const Layout &L = *L_;
+    int rows = 0, target = -1, rp = 0, cp = 0;
+    if (kind == 3 || kind == 6) {
+      check_ch(ch, L.fam[3].count());
+      const auto &pk = L.pk[ch];
+      target = ch;
+      rows = kind == 3 ? pk.n_hh : pk.n_pp;
+      rp = kind == 3 ? pk.H : pk.P;
+      cp = pk.P;
+    } else {
+      check_ch(ch, L.fam[1].count());
+      rows = L.fam[1].side1[ch].size();
+      target = hhhh_to_hhpp_[ch];
+      if (target < 0) return;  // an hhhh channel without an hhpp partner is not used by CCD
+      rp = cp = L.pk[target].H;
+    }
+    S *dst = kind == 3 ? Vhp_.as<S>() : kind == 6 ? Vpp_.as<S>() : Vhh_.as<S>();
+    launch_pack_vblock_host<S>(D_, kind, target, rows, rp, cp, src, dst, flag_.as<int>(), st_);
+    ++launches_;
+    dirty_ = true;
+    ++v_version_;
+  }
+  // HPHP blocks in device-addressable host memory: one batched copy launch
+  void set_v4_direct(int n, const int *chs, double *const *src) {
+    const Layout &L = *L_;
+    std::vector<CopyJob> jobs(n);
+    for (int i = 0; i < n; ++i) {
+      check_ch(chs[i], L.fam[4].count());
+      const int64_t m = L.fam[4].side1[chs[i]].size();
+      jobs[i] = CopyJob{src[i], v4_.as<double>() + 2 * v4_off_h_[chs[i]], m * m * 2};
+    }
+    copyjobs_.alloc(std::max<size_t>(jobs.size(), 1) * sizeof(CopyJob), &bytes_);
+    CK(cudaMemcpyAsync(copyjobs_.p, jobs.data(), jobs.size() * sizeof(CopyJob), cudaMemcpyHostToDevice, st_));
+    launch_copy_jobs((const CopyJob *)copyjobs_.p, n, st_);
+    CK(cudaStreamSynchronize(st_));  // the job table on the host goes out of scope
+    ++launches_;
+    dirty_ = true;
+    ++v_version_;
   }
   // Many blocks of one kind with one synchronisation at the end.  Staged blocks
   // alternate between two staging buffers: the host-to-device copies run back to back
   // on a copy stream while the compute stream packs the previous block.
   void set_vblocks(int kind, int n, const int *chs, const double *const *vs) override {
     const bool staged = kind == 1 || kind == 3 || kind == 6;
+    if (n > 0 && (staged || kind == 4)) {
+      // blocks in device-addressable host memory are read in place: no staging copies
+      std::vector<double *> dv(n);
+      bool direct = true;
+      for (int i = 0; i < n && direct; ++i) direct = (dv[i] = device_view(vs[i])) != nullptr;
+      if (direct) {
+        if (kind == 4) set_v4_direct(n, chs, dv.data());
+        else for (int i = 0; i < n; ++i) set_vblock_direct(kind, chs[i], dv[i]);
+        finish_vblocks();
+        return;
+      }
+    }
     if (staged && n > 1) {
       if (!cs_) {
         CK(cudaStreamCreateWithFlags(&cs_, cudaStreamNonBlocking));
@@ -430,6 +498,17 @@ class Engine final : public IEngine {
   }
   void get_t2_all(double *t) override {
     const Layout &L = *L_;
+    if (double *dt = device_view(t)) {
+      // device-addressable host memory: every channel unpacked in place, one sync
+      for (int c = 0; c < L.fam[3].count(); ++c) {
+        const auto &P = L.pk[c];
+        launch_unpack_t<S>(D_, c, P.n_pp, pp_sgn_.as<int>() + ppsgn_off_[c], hh_sgn_.as<int>() + hhsgn_off_[c], P.n_hh,
+                           T_.as<S>(), dt + 2 * P.amp_off, st_);
+        ++launches_;
+      }
+      CK(cudaStreamSynchronize(st_));
+      return;
+    }
     for (int c = 0; c < L.fam[3].count(); ++c) get_t2(c, t + 2 * L.pk[c].amp_off);
   }
   void get_denominators(double *d2ij, double *d2ab) override {
@@ -2033,7 +2112,7 @@ class Engine final : public IEngine {
   int gemm_shape_[4] = {kShape128x32, kShape128x32, kShape64x64, kShape64x64};
   cudaStream_t cs_ = nullptr;       // copy stream of ccx_set_vblocks
   cudaEvent_t sev_[5] = {};         // copied[2], packed[2], compute-stream mark
-  DBuf stage2_;
+  DBuf stage2_, copyjobs_;
   double e0_[2] = {0, 0};
   double last_rn_ = 0.0;
   bool have_fock_ = false, have_t_ = false, dirty_ = true, vph_ready_ = false, generated_ = false;

@@ -682,6 +682,64 @@ void launch_pack_vblock(const DevLayout &L, int kind, int ch, int n_rows, const 
   k_pack_vblock<S><<<1216, 256, 0, st>>>(L, kind, ch, n_rows, stage, dst, flag);
 }
 
+// Kinds 3 and 6 from host memory: dst(r, c) at base + r * P + c (row-major) from the
+// reference block's (row_map[r], col_map[c]) element (column-major, leading dimension
+// n_rows).  A 32 x 32 tile is read down its columns (consecutive source rows, so each
+// host cache line is fetched once) and written along its rows.
+template <typename S>
+__global__ void __launch_bounds__(256) k_pack_vblock_tr(DevLayout L, int kind, int ch, int n_rows, int R, int P,
+                                                        const double *__restrict__ src, S *__restrict__ dst, int *flag) {
+  __shared__ S tile[32][33];
+  const int r0 = blockIdx.y * 32, c0 = blockIdx.x * 32;
+  const int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 8
+  const int *row_map = kind == 3 ? L.hh_row + L.hh_off[ch] : L.pp_row + L.pp_off[ch];
+  const int *col_map = L.pp_row + L.pp_off[ch];
+  const int64_t base = kind == 3 ? L.t_off[ch] : L.vpp_off[ch];
+  const int r = r0 + tx;
+  const int64_t srow = r < R ? row_map[r] : 0;
+#pragma unroll
+  for (int j = 0; j < 32; j += 8) {
+    const int c = c0 + ty + j;
+    if (r < R && c < P) tile[ty + j][tx] = cvt_in<S>(src + 2 * (srow + (int64_t)n_rows * col_map[c]), flag);
+  }
+  __syncthreads();
+#pragma unroll
+  for (int j = 0; j < 32; j += 8) {
+    const int rr = r0 + ty + j, c = c0 + tx;
+    if (rr < R && c < P) dst[base + (int64_t)rr * P + c] = tile[tx][ty + j];
+  }
+}
+template <typename S>
+void launch_pack_vblock_host(const DevLayout &L, int kind, int ch, int n_rows, int rows_packed, int cols_packed,
+                             const double *src, S *dst, int *flag, cudaStream_t st) {
+  if (rows_packed <= 0 || cols_packed <= 0) return;
+  if (kind == 3 || kind == 6) {
+    const dim3 grid((cols_packed + 31) / 32, (rows_packed + 31) / 32);
+    k_pack_vblock_tr<S><<<grid, dim3(32, 8), 0, st>>>(L, kind, ch, n_rows, rows_packed, cols_packed, src, dst, flag);
+  } else {
+    // kind 1 reads consecutive source rows already
+    k_pack_vblock<S><<<1216, 256, 0, st>>>(L, kind, ch, n_rows, src, dst, flag);
+  }
+}
+
+// one CTA per job; 16-byte copies where both ends and the length allow
+__global__ void k_copy_jobs(const CopyJob *__restrict__ jobs) {
+  const CopyJob j = jobs[blockIdx.x];
+  const bool vec = ((reinterpret_cast<uintptr_t>(j.src) | reinterpret_cast<uintptr_t>(j.dst)) & 15) == 0;
+  if (vec) {
+    const int64_t n2 = j.n / 2;
+    const double2 *s2 = reinterpret_cast<const double2 *>(j.src);
+    double2 *d2 = reinterpret_cast<double2 *>(j.dst);
+    for (int64_t i = threadIdx.x; i < n2; i += blockDim.x) d2[i] = s2[i];
+    if ((j.n & 1) && threadIdx.x == 0) j.dst[j.n - 1] = j.src[j.n - 1];
+  } else {
+    for (int64_t i = threadIdx.x; i < j.n; i += blockDim.x) j.dst[i] = j.src[i];
+  }
+}
+void launch_copy_jobs(const CopyJob *jobs, int njobs, cudaStream_t st) {
+  if (njobs > 0) k_copy_jobs<<<njobs, 256, 0, st>>>(jobs);
+}
+
 // W(ia, jb) = -V_hphp(ib, ja), the constant part of I4 (ccm_t2_eqn.f90:740-780)
 template <typename S>
 __global__ void k_build_w(DevLayout L, const int2 *__restrict__ hp4_slot, const int64_t *__restrict__ v4_off,
@@ -999,6 +1057,8 @@ void launch_unpack_t(const DevLayout &L, int ch, int n_pp, const int *pp_signed,
   template void launch_diis_gram<S>(int64_t, const S *const *, int, double *, double *, cudaStream_t);                \
   template void launch_combine<S>(int64_t, const S *const *, const double *, int, S *, cudaStream_t);                 \
   template void launch_pack_vblock<S>(const DevLayout &, int, int, int, const double *, S *, int *, cudaStream_t);    \
+  template void launch_pack_vblock_host<S>(const DevLayout &, int, int, int, int, int, const double *, S *, int *,      \
+                                           cudaStream_t);                                                              \
   template void launch_build_w<S>(const DevLayout &, const int2 *, const int64_t *, const int *, const double *, S *,  \
                                   int *, cudaStream_t);                                                                \
   template void launch_build_vph<S>(const DevLayout &, const S *, S *, cudaStream_t);                                 \

@@ -87,6 +87,21 @@ void launch_combine(int64_t n, const S *const *xs, const double *coef /* host, 2
 // ---- interaction -----------------------------------------------------------
 template <typename S>
 void launch_pack_vblock(const DevLayout &L, int kind, int ch, int n_rows, const double *stage, S *dst, int *flag, cudaStream_t st);
+// The same packing read straight from host memory the device can address (pinned and
+// mapped): reads follow the block's column-major order (consecutive rows), through a
+// shared-memory transpose where the packed layout is row-major (kinds 3 and 6).
+// rows_packed / cols_packed: the channel's packed extents (kind 3: H, P; 6: P, P; 1: H, H).
+template <typename S>
+void launch_pack_vblock_host(const DevLayout &L, int kind, int ch, int n_rows, int rows_packed, int cols_packed,
+                             const double *src, S *dst, int *flag, cudaStream_t st);
+// Copies of many blocks in one launch (n doubles from src to dst per job); src may be
+// mapped host memory.
+struct CopyJob {
+  const double *src;
+  double *dst;
+  int64_t n;
+};
+void launch_copy_jobs(const CopyJob *jobs, int njobs, cudaStream_t st);
 template <typename S>
 void launch_build_w(const DevLayout &L, const int2 *hp4_slot, const int64_t *v4_off, const int *n4, const double *v4,
                     S *W, int *flag, cudaStream_t st);

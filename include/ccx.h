@@ -179,7 +179,10 @@ int ccx_set_vblock(ccx_engine *e, int32_t kind, int32_t ch, const double *v);
 /* The same for n blocks of one kind (channels chs[i], buffers v[i]) in one call: the
  * copies are queued back to back and the call returns once all have been read, so a
  * host that hands over every channel of a family pays one synchronisation.  Same
- * reference arrays as ccx_set_vblock. */
+ * reference arrays as ccx_set_vblock.  When every buffer is pinned host memory the
+ * device can address (cudaHostAlloc / cudaHostRegister), the packing kernels read the
+ * blocks in place, touching only the cache lines of the unique pairs, with no staging
+ * copies; ccx_set_vblock does the same for one block. */
 int ccx_set_vblocks(ccx_engine *e, int32_t kind, int32_t n, const int32_t *chs, const double *const *v);
 
 /* Generate Fock, E0 and every V block on the device from a synthetic potential
@@ -214,7 +217,8 @@ int ccx_set_t2(ccx_engine *e, int32_t ch, const double *t);
 int ccx_get_t2(ccx_engine *e, int32_t ch, double *t);
 /* t2_ccm_eqn(ch)%val after ccx_t2_intermediate */
 int ccx_get_t2_eqn(ccx_engine *e, int32_t ch, double *r);
-/* all channels concatenated in channel order (n_amps complex values) */
+/* all channels concatenated in channel order (n_amps complex values); ccx_get_t2_all
+ * unpacks straight into pinned device-addressable host memory, one synchronisation */
 int ccx_set_t2_all(ccx_engine *e, const double *t);
 int ccx_get_t2_all(ccx_engine *e, double *t);
 /* d2ij(1:A), d2ab(A+1:n) of the last residual, complex interleaved */

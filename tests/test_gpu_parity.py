@@ -255,6 +255,56 @@ def test_set_vblocks_matches_single_blocks(ccx, O):
     assert ex.value.code == 1
 
 
+def test_pinned_host_blocks_are_read_in_place(ccx, O):
+    """V blocks and the T2 output in pinned (device-addressable) host memory take the
+    in-place path: packing kernels read the host blocks directly and the amplitudes are
+    unpacked straight into the host buffer.  The engine must equal one fed from pageable
+    memory through staging copies, bit for bit."""
+    torch = pytest.importorskip("torch")
+    import ctypes as C
+    o, L, eg = make(ccx, O, **C1)
+    e1 = ccx.Engine(L, real=True)
+    e2 = ccx.Engine(L, real=True)
+    for e in (e1, e2):
+        e.set_fock(o.fock(), o.e0())
+    fams = {ccx.CH_HHPP: {c: o.v_hhpp(c) for c in range(o.n_channels(3))},
+            ccx.V_PPPP: {c: o.v_pppp(c) for c in range(o.n_channels(3))},
+            ccx.CH_HHHH: {c: o.v_hhhh(c) for c in range(o.n_channels(1))},
+            ccx.CH_HPHP: {c: o.v_hphp(c) for c in range(o.n_channels(4))}}
+    keep = []
+
+    def pinned_call(e, kind, blocks):
+        bufs = []
+        for b in blocks.values():
+            f = ccx._cplx_fortran(b)
+            t = torch.empty(f.size, dtype=torch.float64, pin_memory=True)
+            t.numpy()[:] = f
+            bufs.append(t)
+        keep.extend(bufs)
+        chs = (C.c_int32 * len(bufs))(*blocks.keys())
+        ptrs = (C.c_void_p * len(bufs))(*[t.data_ptr() for t in bufs])
+        return ccx.lib().ccx_set_vblocks(e._h, kind, len(bufs), chs, ptrs)
+
+    for kind, blocks in fams.items():
+        e1.set_vblocks(kind, blocks)
+        assert pinned_call(e2, kind, blocks) == 0
+    for e in (e1, e2):
+        e.setup_t_amplitudes()
+        e.t2_intermediate()
+    for c in range(o.n_channels(3)):
+        assert np.array_equal(e1.t2_eqn(c), e2.t2_eqn(c))
+    r1 = e1.ccd_iter(mode=ccx.MODE_STANDARD, tol=1e-10)
+    r2 = e2.ccd_iter(mode=ccx.MODE_STANDARD, tol=1e-10)
+    assert r1["e_ccd"] == r2["e_ccd"]
+    n = L.counts()["amps"]
+    out = torch.zeros(2 * n, dtype=torch.float64, pin_memory=True)
+    ccx._check(ccx.lib().ccx_get_t2_all(e2._h, C.c_void_p(out.data_ptr())))
+    assert np.array_equal(out.numpy().view(np.complex128), e1.t2_all())
+    # a non-zero imaginary part in pinned memory is rejected like a pageable one
+    bad = {0: o.v_hhpp(0), 1: o.v_hhpp(1) + 1e-3j}
+    assert pinned_call(e2, ccx.CH_HHPP, bad) == 1
+
+
 def test_complex_block_into_real_engine_is_rejected(ccx, O):
     o = O.Oracle(O.Config(nmax=1, A=2, rho=0.08))
     L = ccx.Layout.from_basis(1, 2, 0.08)
