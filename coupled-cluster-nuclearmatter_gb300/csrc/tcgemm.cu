@@ -4,12 +4,13 @@
 // (kind::f16) or TF32 (kind::tf32) operands, FP32 accumulation in tensor memory.
 // Persistent: one CTA per SM walks the tile list (a tile = 128 rows of one problem, all N
 // <= 256 columns); a tile may sum up to three products with the same M, N (segments).
-// Lane 0 of warp 4 streams the pre-tiled K tiles of A and B into a ring of shared-memory
+// Lane 0 of warp 8 streams the pre-tiled K tiles of A and B into a ring of shared-memory
 // stages with cp.async.bulk (one contiguous copy per operand tile, completion on an
-// mbarrier); the ring runs on across tiles.  Lane 0 of warp 5 issues the MMAs into one
+// mbarrier); the ring runs on across tiles.  Lane 0 of warp 9 issues the MMAs into one
 // of two tensor-memory halves, alternating by tile, and tcgen05.commit hands each stage
-// back.  Warps 0-3 read their 32 TMEM lanes (rows) of the finished half with tcgen05.ld
-// and add into C while the next tile accumulates in the other half.
+// back.  Warps 0-3 drain the tiles of half 0 and warps 4-7 those of half 1: each reads
+// its 32 TMEM lanes (rows) with tcgen05.ld and adds into C while the next tile
+// accumulates in the other half.
 // Every mbarrier wait is bounded by a clock budget: on expiry the kernel records an
 // error code, lets its own copies land, frees its TMEM and returns.
 #include <cuda_bf16.h>
@@ -27,9 +28,28 @@ namespace {
 
 using namespace tcptx;
 
-constexpr int kTcThreads = 192;   // warps 0-3 epilogue, warp 4 producer, warp 5 MMA issuer
+constexpr int kTcThreads = 320;   // warps 0-7 epilogue, warp 8 producer, warp 9 MMA issuer
 constexpr int kTcHalfCols = 256;  // tensor-memory columns of one accumulator half
 constexpr int kTcMaxStages = 8;
+
+// FP32 bit pattern -> the same value as FP64, exactly, with integer operations only (a
+// float-to-double conversion would run on this GPU's narrow FP64 pipe)
+__device__ __forceinline__ double f32_bits_to_f64(uint32_t u) {
+  const unsigned long long sign = (unsigned long long)(u >> 31) << 63;
+  const uint32_t e = (u >> 23) & 0xffu, m = u & 0x7fffffu;
+  unsigned long long bits;
+  if (e == 0xffu) {  // infinities and NaNs
+    bits = sign | (0x7ffull << 52) | ((unsigned long long)m << 29);
+  } else if (e != 0) {  // normal: exponent rebiased from 127 to 1023
+    bits = sign | ((unsigned long long)(e + 896u) << 52) | ((unsigned long long)m << 29);
+  } else if (m == 0) {
+    bits = sign;
+  } else {  // subnormal m 2^-149, normalised on its leading bit p
+    const int p = 31 - __clz((int)m);
+    bits = sign | ((unsigned long long)(p - 149 + 1023) << 52) | (((unsigned long long)m << (52 - p)) & 0xFFFFFFFFFFFFFull);
+  }
+  return __longlong_as_double((long long)bits);
+}
 
 // K tiles of segment e of a problem (e = 0: the problem's own operands)
 __device__ __forceinline__ TcSeg tc_segment(const TcProb *__restrict__ pp, int e) {
@@ -85,7 +105,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_gemm(const TcProb *__restr
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(smem_u32(&tfull[b]), 1);
-      mbar_init(smem_u32(&tempty[b]), 4);
+      mbar_init(smem_u32(&tempty[b]), 4);  // the four warps of drain group b
     }
     mbar_init(smem_u32(fin), 1);
     *abort_flag = 0;
@@ -110,7 +130,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_gemm(const TcProb *__restr
     return true;
   };
 
-  if (warp == 4) {
+  if (warp == 8) {
     if (lane == 0) {
       // producer: one bulk copy per operand tile into the stage ring, which runs on
       // across tiles; a stage is refilled once the MMAs that read it have completed
@@ -159,7 +179,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_gemm(const TcProb *__restr
         if (n_s > 0) mbar_wait(smem_u32(&full[s]), (uint32_t)((n_s - 1) & 1));
       }
     }
-  } else if (warp == 5) {
+  } else if (warp == 9) {
     if (lane == 0) {
       // MMA issuer: the K tiles of every segment of a tile into its accumulators in
       // tensor-memory half b = (local tile) & 1, then tcgen05.commit to tfull[b]
@@ -216,9 +236,11 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_gemm(const TcProb *__restr
       mbar_wait(smem_u32(fin), 0);
     }
   } else {
-    // warps 0-3: warp w reads tensor-memory lanes 32w .. 32w + 31 (rows of the tile)
-    const int row = warp * 32 + lane;
-    const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+    // warps 0-7: two groups of four, group g draining the tiles of tensor-memory half g,
+    // so two tiles' C updates are in flight; warp w reads lanes 32 (w % 4) .. + 31
+    const int grp = warp >> 2, quad = warp & 3;
+    const int row = quad * 32 + lane;
+    const uint32_t lane_base = tmem + ((uint32_t)(quad * 32) << 16);
     int lt = 0;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
       const TcTile tl = tiles[t];
@@ -226,6 +248,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_gemm(const TcProb *__restr
       const TcGeom G = tc_geom(pp, npad_max);
       if (!G.ok) continue;
       const int b = lt & 1;
+      if (b != grp) {
+        ++lt;
+        continue;
+      }
       const bool got = __all_sync(0xffffffffu, wait(&tfull[b], (uint32_t)((lt >> 1) & 1)));
       if (!got) {
         if (lane == 0) atomicExch(err, 3);
@@ -241,26 +267,45 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_gemm(const TcProb *__restr
       const double alpha = pp->alpha;
       const int nvalid = pp->N;
       const bool live = m < pp->M;
-      const bool warp_live = tl.mt * 128 + warp * 32 < pp->M;  // uniform over the warp
-      if (!warp_live) {  // no row of this warp's lanes is stored
+      if (tl.mt * 128 + quad * 32 >= pp->M) {  // no row of this warp's lanes is stored
         if (lane == 0) mbar_arrive(smem_u32(&tempty[b]));
         ++lt;
         continue;
       }
-      const uint32_t acc0 = lane_base + (uint32_t)(b * kTcHalfCols);
+      const uint32_t accb = lane_base + (uint32_t)(b * kTcHalfCols);
       // 32 columns per read (npad rounded up to 32 stays inside each accumulator)
       for (int c0 = 0; c0 < G.npad; c0 += 32) {
-        uint32_t r[32];
-        tmem_ld32(acc0 + (uint32_t)c0, r);
-        tmem_ld_wait();
-        double sum[32];
+        // the C and C0 loads go first, so that their latency overlaps the tensor-memory
+        // reads; the mode is uniform over the tile, so the branches sit outside the
+        // unrolled loops and the 32 loads of a row issue back to back
+        double v[32];
+        if (live && keep) {
 #pragma unroll
-        for (int j = 0; j < 32; ++j) sum[j] = (double)__uint_as_float(r[j]);
-        for (int a = 1; a < G.nacc; ++a) {
-          tmem_ld32(acc0 + (uint32_t)(a * G.ncols + c0), r);
+          for (int j = 0; j < 32; ++j) v[j] = (c0 + j < nvalid) ? crow[(int64_t)(c0 + j) * sCn] : 0.0;
+        } else {
+#pragma unroll
+          for (int j = 0; j < 32; ++j) v[j] = 0.0;
+        }
+        if (live && c0row) {
+          double add[32];
+#pragma unroll
+          for (int j = 0; j < 32; ++j) add[j] = (c0 + j < nvalid) ? c0row[(int64_t)(c0 + j) * sCn] : 0.0;
+          if (keep) {
+#pragma unroll
+            for (int j = 0; j < 32; ++j) v[j] += add[j];
+          } else {
+#pragma unroll
+            for (int j = 0; j < 32; ++j) v[j] = add[j];
+          }
+        }
+        // one FP64 multiply-add per accumulator and element: the FP32 values widen on
+        // the integer pipe
+        for (int a = 0; a < G.nacc; ++a) {
+          uint32_t r[32];
+          tmem_ld32(accb + (uint32_t)(a * G.ncols + c0), r);
           tmem_ld_wait();
 #pragma unroll
-          for (int j = 0; j < 32; ++j) sum[j] += (double)__uint_as_float(r[j]);
+          for (int j = 0; j < 32; ++j) v[j] = fma(alpha, f32_bits_to_f64(r[j]), v[j]);
         }
         if (c0 + 32 >= G.npad) {
           // the accumulators of this half are read: hand it back to the MMA issuer
@@ -269,26 +314,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_gemm(const TcProb *__restr
           if (lane == 0) mbar_arrive(smem_u32(&tempty[b]));
         }
         if (live) {
-          // the mode is uniform over the tile: branch outside the unrolled loops so that
-          // the 32 loads of a row are issued back to back
-          double old[32];
-          if (keep) {
-#pragma unroll
-            for (int j = 0; j < 32; ++j) old[j] = (c0 + j < nvalid) ? crow[(int64_t)(c0 + j) * sCn] : 0.0;
-          } else {
-#pragma unroll
-            for (int j = 0; j < 32; ++j) old[j] = 0.0;
-          }
-          if (c0row) {
-            double add[32];
-#pragma unroll
-            for (int j = 0; j < 32; ++j) add[j] = (c0 + j < nvalid) ? c0row[(int64_t)(c0 + j) * sCn] : 0.0;
-#pragma unroll
-            for (int j = 0; j < 32; ++j) old[j] += add[j];
-          }
 #pragma unroll
           for (int j = 0; j < 32; ++j)
-            if (c0 + j < nvalid) crow[(int64_t)(c0 + j) * sCn] = old[j] + alpha * sum[j];
+            if (c0 + j < nvalid) crow[(int64_t)(c0 + j) * sCn] = v[j];
         }
       }
       ++lt;
