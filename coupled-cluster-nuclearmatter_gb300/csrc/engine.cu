@@ -1423,6 +1423,20 @@ class Engine final : public IEngine {
       pl.npad_max[ph][k] = std::max(pl.npad_max[ph][k], p.npad);
       pl.max_nk[ph][k] = std::max(pl.max_nk[ph][k], nk);
     }
+    // One launch per phase when the widest bucket still leaves the kernel 3 shared-memory
+    // stages (A tiles dominate a stage): the persistent grid then has no tail per bucket.
+    for (int ph = 0; ph < 2; ++ph) {
+      int np = 16, nk = 1;
+      for (int k = 0; k < kTcBuckets; ++k)
+        if (!b[ph][k].empty()) { np = std::max(np, pl.npad_max[ph][k]); nk = std::max(nk, pl.max_nk[ph][k]); }
+      if (tc_stages(np) < 3) continue;
+      for (int k = 1; k < kTcBuckets; ++k) {
+        b[ph][0].insert(b[ph][0].end(), b[ph][k].begin(), b[ph][k].end());
+        b[ph][k].clear();
+      }
+      pl.npad_max[ph][0] = np;
+      pl.max_nk[ph][0] = nk;
+    }
     // longest tiles first: the persistent CTAs take tiles in strides of the grid
     auto work = [&](const TcTile &t) {
       const TcProb &p = l.probs[t.prob];

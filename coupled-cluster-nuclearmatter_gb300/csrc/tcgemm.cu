@@ -460,14 +460,18 @@ __global__ void __launch_bounds__(256) k_tc_split(const TcSplitJob *__restrict__
 
 }  // namespace
 
+int tc_stages(int npad_max) {
+  const size_t stage_bytes = 2 * 128 * 128 + 2 * (size_t)npad_max * 128;
+  const size_t budget = 227 * 1024 - 256;
+  return std::max(1, (int)std::min<size_t>(kTcMaxStages, budget / stage_bytes));
+}
+
 void launch_tc_gemm(int kind, const TcProb *probs, const TcTile *tiles, int ntiles, int npad_max, int max_nk, int *err,
                     cudaStream_t st) {
   (void)max_nk;  // the stage ring runs on across tiles
   if (ntiles <= 0) return;
   const size_t stage_bytes = 2 * 128 * 128 + 2 * (size_t)npad_max * 128;
-  const size_t budget = 227 * 1024 - 256;
-  int stages = (int)std::min<size_t>(kTcMaxStages, budget / stage_bytes);
-  if (stages < 1) stages = 1;
+  const int stages = tc_stages(npad_max);
   const size_t smem = (size_t)stages * stage_bytes + (2 * stages + 5) * 8 + 16;
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);

@@ -54,6 +54,8 @@ inline int tc_tile_k(int kind) { return kind == kTcBF16 ? 64 : 32; }
 // kernel's stage ring runs on across tiles)
 void launch_tc_gemm(int kind, const TcProb *probs, const TcTile *tiles, int ntiles, int npad_max, int max_nk, int *err,
                     cudaStream_t st);
+// shared-memory stages launch_tc_gemm uses for tiles up to npad_max columns
+int tc_stages(int npad_max);
 
 // FP64 matrix (rows x cols, element (r, k) at src[r*sr + k*sk], optionally minus sub at
 // the same strides) -> pre-tiled hi/lo pair, zero padded.  tile_rows = 128 for an A
