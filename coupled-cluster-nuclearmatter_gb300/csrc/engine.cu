@@ -1487,7 +1487,6 @@ class Engine final : public IEngine {
       j.rows = rows; j.cols = cols; j.tile_rows = tile_rows; j.nk = (cols + tk - 1) / tk; j.rows_pad = rows_pad;
       j.hi = (char *)b.hi.p + (off + c * b.n) * es;
       j.lo = (char *)b.lo.p + (off + c * b.n) * es;
-      j.scale = 1.0;
       js.push_back(j);
     }
   }

@@ -222,11 +222,11 @@ void tc_selftest(int device, int kind, int nprob, const int *Ms, const int *Ns, 
       TcSplitJob ja{};
       ja.src = (double *)dA.p + oa + k0; ja.sub = nullptr; ja.sr = x.K; ja.sk = 1;
       ja.rows = x.M; ja.cols = kg; ja.tile_rows = 128; ja.nk = nkg; ja.rows_pad = x.mpad;
-      ja.hi = (char *)tAh.p + sa * es; ja.lo = (char *)tAl.p + sa * es; ja.scale = 1.0;
+      ja.hi = (char *)tAh.p + sa * es; ja.lo = (char *)tAl.p + sa * es;
       TcSplitJob jb{};
       jb.src = (double *)dB.p + ob + k0; jb.sub = nullptr; jb.sr = x.K; jb.sk = 1;  // B(n, k) = B_colmajor[k + K n]
       jb.rows = x.N; jb.cols = kg; jb.tile_rows = x.npad; jb.nk = nkg; jb.rows_pad = x.npad;
-      jb.hi = (char *)tBh.p + sb * es; jb.lo = (char *)tBl.p + sb * es; jb.scale = 1.0;
+      jb.hi = (char *)tBh.p + sb * es; jb.lo = (char *)tBl.p + sb * es;
       jobs.push_back(ja);
       jobs.push_back(jb);
       segs.push_back(TcSeg{ja.hi, use_alo ? ja.lo : nullptr, jb.hi, jb.lo, nkg, 0});

@@ -331,12 +331,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_gemm(const TcProb *__restr
 }
 
 // ---- operand preparation ---------------------------------------------------------
-// x = hi + lo split of an FP64 value into two narrow floats (BF16: 8 significant bits
-// each; TF32: 11), computed on the bit pattern with integer operations: the FP64 pipe
-// of this GPU is narrow, and a float conversion of a double runs on it.  hi is x
-// rounded to NB significant bits (half away from zero), lo the exact remainder rounded
-// the same way, so |x - hi - lo| <= 2^(-2 NB) |x|.  Values below the float range
-// (2^-126) become zero.
+// x = hi + lo split of an FP64 value (or of a difference a - b of two) into two narrow
+// floats (BF16: 8 significant bits each; TF32: 11), computed on the bit patterns with
+// integer operations only: the FP64 pipe of this GPU is narrow, and both a float
+// conversion of a double and an FP64 subtraction run on it.  hi is x rounded to NB
+// significant bits (half away from zero), lo the remainder rounded the same way, so
+// |x - hi - lo| <= 2^(-2 NB) |x| (plus 2^-60 |a| for a difference, whose smaller
+// operand is truncated below the larger one's 62-bit grid).  Values below the float
+// range (2^-126) and FP64 subnormals become zero.
 template <int NB>
 struct BitSplit {
   // float bit pattern of sign * sig * 2^(e2 - (NB - 1)), sig in [2^(NB-1), 2^NB)
@@ -345,85 +347,115 @@ struct BitSplit {
     if (biased <= 0) return sign << 31;
     return (sign << 31) | ((uint32_t)biased << 23) | ((sig & ((1u << (NB - 1)) - 1)) << (24 - NB));
   }
-  __device__ static void split(double x, uint32_t &hi, uint32_t &lo) {
-    const unsigned long long u = (unsigned long long)__double_as_longlong(x);
-    const uint32_t sign = (uint32_t)(u >> 63);
-    const int e = (int)((u >> 52) & 0x7ff);
-    if (e == 0) {  // zero (and FP64 subnormals, far below the float range)
+  // one NB-bit rounding of mag 2^ex (mag > 0, up to 63 bits): its significand, the
+  // exponent e2 of pack(), and the signed remainder mag - sig 2^drop
+  __device__ static void round_nb(unsigned long long mag, int ex, uint32_t &sig, int &e2, long long &rem) {
+    const int p = 63 - __clzll((long long)mag);  // leading bit
+    const int drop = p + 1 - NB;
+    if (drop <= 0) {
+      sig = (uint32_t)(mag << (-drop));
+      e2 = ex + p;
+      rem = 0;
+      return;
+    }
+    unsigned long long h = (mag + (1ull << (drop - 1))) >> drop;
+    rem = (long long)(mag - (h << drop));
+    e2 = ex + p;
+    if (h == (1ull << NB)) {  // rounded up to the next power of two
+      h >>= 1;
+      ++e2;
+    }
+    sig = (uint32_t)h;
+  }
+  // x = (-1)^sign mag 2^ex
+  __device__ static void split_mag(uint32_t sign, unsigned long long mag, int ex, uint32_t &hi, uint32_t &lo) {
+    if (mag == 0) {
       hi = lo = sign << 31;
       return;
     }
-    const long long full = (long long)((u & 0xFFFFFFFFFFFFFull) | (1ull << 52));  // 53-bit significand
-    constexpr int drop = 53 - NB;
-    uint32_t h = (uint32_t)((full + (1ll << (drop - 1))) >> drop);
-    const long long rem = full - ((long long)h << drop);  // |rem| <= 2^(drop-1)
-    int eh = e - 1023;
-    if (h == (1u << NB)) { h >>= 1; ++eh; }
+    uint32_t h, l;
+    int eh, el;
+    long long rem, rem2;
+    round_nb(mag, ex, h, eh, rem);
     hi = pack(sign, eh, h);
     if (rem == 0) {
       lo = 0;
       return;
     }
-    const unsigned long long a = (unsigned long long)(rem < 0 ? -rem : rem);
-    const int pos = 63 - __clzll((long long)a);  // leading bit of the remainder
-    uint32_t l;
-    int el = e - 1075 + pos;
-    if (pos >= NB) {
-      const int sh = pos - (NB - 1);
-      l = (uint32_t)((a + (1ull << (sh - 1))) >> sh);
-      if (l == (1u << NB)) { l >>= 1; ++el; }
-    } else {
-      l = (uint32_t)(a << ((NB - 1) - pos));
-    }
+    round_nb((unsigned long long)(rem < 0 ? -rem : rem), ex, l, el, rem2);
     lo = pack(sign ^ (rem < 0 ? 1u : 0u), el, l);
   }
+  // sign, 53-bit significand and exponent (value = sig 2^ex) of an FP64 bit pattern;
+  // zero and subnormals give sig = 0
+  __device__ static void decode(unsigned long long u, uint32_t &sign, unsigned long long &sig, int &ex) {
+    sign = (uint32_t)(u >> 63);
+    const int e = (int)((u >> 52) & 0x7ff);
+    sig = e == 0 ? 0ull : (u & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+    ex = e - 1075;
+  }
+  __device__ static void split(double x, uint32_t &hi, uint32_t &lo) {
+    uint32_t sign;
+    unsigned long long sig;
+    int ex;
+    decode((unsigned long long)__double_as_longlong(x), sign, sig, ex);
+    split_mag(sign, sig, ex, hi, lo);
+  }
+  // split of a - b: both significands on the 62-bit grid of the larger exponent, added
+  // as signed 64-bit integers (the magnitudes stay below 2^62, their sum below 2^63)
+  __device__ static void split_diff(double a, double b, uint32_t &hi, uint32_t &lo) {
+    uint32_t sa, sb;
+    unsigned long long ma, mb;
+    int ea, eb;
+    decode((unsigned long long)__double_as_longlong(a), sa, ma, ea);
+    decode((unsigned long long)__double_as_longlong(b), sb, mb, eb);
+    sb ^= 1u;  // a + (-b)
+    if (mb == 0) {
+      split_mag(sa, ma, ea, hi, lo);
+      return;
+    }
+    if (ma == 0) {
+      split_mag(sb, mb, eb, hi, lo);
+      return;
+    }
+    const int e = max(ea, eb);
+    const int da = e - ea, db = e - eb;
+    const long long va = da >= 62 ? 0 : (long long)((ma << 9) >> da);
+    const long long vb = db >= 62 ? 0 : (long long)((mb << 9) >> db);
+    const long long r = (sa ? -va : va) + (sb ? -vb : vb);
+    split_mag(r < 0 ? 1u : 0u, (unsigned long long)(r < 0 ? -r : r), e - 9, hi, lo);
+  }
 };
+// elements per 16-byte unit and the float bit patterns of one unit
 template <int KIND> struct Half;
 template <> struct Half<kTcBF16> {
-  static constexpr int per16 = 8;  // elements per 16 bytes
-  // one 16-byte unit of hi and of lo from 8 values
-  __device__ static void split8(const double (&x)[8], uint4 &hi, uint4 &lo) {
-    uint32_t h[8], l[8];
-#pragma unroll
-    for (int j = 0; j < 8; ++j) BitSplit<8>::split(x[j], h[j], l[j]);
-    hi = make_uint4((h[0] >> 16) | (h[1] & 0xFFFF0000u), (h[2] >> 16) | (h[3] & 0xFFFF0000u),
-                    (h[4] >> 16) | (h[5] & 0xFFFF0000u), (h[6] >> 16) | (h[7] & 0xFFFF0000u));
-    lo = make_uint4((l[0] >> 16) | (l[1] & 0xFFFF0000u), (l[2] >> 16) | (l[3] & 0xFFFF0000u),
-                    (l[4] >> 16) | (l[5] & 0xFFFF0000u), (l[6] >> 16) | (l[7] & 0xFFFF0000u));
+  static constexpr int per16 = 8;
+  static constexpr int nb = 8;
+  __device__ static uint4 pack(const uint32_t (&f)[8]) {  // the upper halves of 8 floats
+    return make_uint4((f[0] >> 16) | (f[1] & 0xFFFF0000u), (f[2] >> 16) | (f[3] & 0xFFFF0000u),
+                      (f[4] >> 16) | (f[5] & 0xFFFF0000u), (f[6] >> 16) | (f[7] & 0xFFFF0000u));
   }
 };
 template <> struct Half<kTcTF32> {
   static constexpr int per16 = 4;
-  __device__ static void split4(const double (&x)[4], uint4 &hi, uint4 &lo) {
-    uint32_t h[4], l[4];
-#pragma unroll
-    for (int j = 0; j < 4; ++j) BitSplit<11>::split(x[j], h[j], l[j]);
-    hi = make_uint4(h[0], h[1], h[2], h[3]);
-    lo = make_uint4(l[0], l[1], l[2], l[3]);
-  }
+  static constexpr int nb = 11;
+  __device__ static uint4 pack(const uint32_t (&f)[4]) { return make_uint4(f[0], f[1], f[2], f[3]); }
 };
-template <int KIND, int N> __device__ inline void split_unit(const double (&x)[N], uint4 &hi, uint4 &lo);
-template <> __device__ inline void split_unit<kTcBF16, 8>(const double (&x)[8], uint4 &hi, uint4 &lo) {
-  Half<kTcBF16>::split8(x, hi, lo);
-}
-template <> __device__ inline void split_unit<kTcTF32, 4>(const double (&x)[4], uint4 &hi, uint4 &lo) {
-  Half<kTcTF32>::split4(x, hi, lo);
-}
 
 // One thread per 16-byte unit of the tiled output (one core-matrix row: 8 BF16 or 4
 // TF32 values of one operand row).  Inside a tile the units are ordered
 // (row group, K chunk, row in group), so a warp reads 8 rows x 4 consecutive K chunks
-// and writes 512 contiguous bytes.  Blocks cover kSplitChunk units of one job.
+// and writes 512 contiguous bytes.  Blocks cover kSplitChunk units of one job.  No FP64
+// arithmetic: a job with sub splits src - sub through BitSplit::split_diff.
 template <int KIND>
 __global__ void __launch_bounds__(256) k_tc_split(const TcSplitJob *__restrict__ jobs, const int4 *__restrict__ chunks) {
   using H = Half<KIND>;
+  using B = BitSplit<H::nb>;
   constexpr int cme = H::per16;  // elements per unit
   constexpr int tk = 8 * cme;    // elements per 128-byte tile row
   const int4 ck = chunks[blockIdx.x];
   const TcSplitJob J = jobs[ck.x];
   const int tile_units = J.tile_rows * 8;
   const int end = ck.z;
-  const bool scaled = J.scale != 1.0;
   uint4 *hi = (uint4 *)J.hi, *lo = (uint4 *)J.lo;
   for (int u = ck.y + threadIdx.x; u < end; u += blockDim.x) {
     const int t = u / tile_units, w = u - t * tile_units;
@@ -431,26 +463,25 @@ __global__ void __launch_bounds__(256) k_tc_split(const TcSplitJob *__restrict__
     const int g = w >> 6, kc = (w >> 3) & 7, r8 = w & 7;
     const int row = rt * J.tile_rows + g * 8 + r8;
     const int k0 = kt * tk + kc * cme;
-    double x[cme];
     const bool live = row < J.rows && k0 < J.cols;
     if (live) {
       const double *src = J.src + (int64_t)row * J.sr;
-      const double *sub = J.sub ? J.sub + (int64_t)row * J.sr : nullptr;
+      double a[cme], b[cme];
 #pragma unroll
-      for (int j = 0; j < cme; ++j) {
-        const int k = k0 + j;
-        double v = 0.0;
-        if (k < J.cols) {
-          v = src[(int64_t)k * J.sk];
-          if (sub) v -= sub[(int64_t)k * J.sk];
-          if (scaled) v *= J.scale;
-        }
-        x[j] = v;
+      for (int j = 0; j < cme; ++j) a[j] = (k0 + j < J.cols) ? src[(int64_t)(k0 + j) * J.sk] : 0.0;
+      uint32_t h[cme], l[cme];
+      if (J.sub) {
+        const double *sub = J.sub + (int64_t)row * J.sr;
+#pragma unroll
+        for (int j = 0; j < cme; ++j) b[j] = (k0 + j < J.cols) ? sub[(int64_t)(k0 + j) * J.sk] : 0.0;
+#pragma unroll
+        for (int j = 0; j < cme; ++j) B::split_diff(a[j], b[j], h[j], l[j]);
+      } else {
+#pragma unroll
+        for (int j = 0; j < cme; ++j) B::split(a[j], h[j], l[j]);
       }
-      uint4 h, l;
-      split_unit<KIND, cme>(x, h, l);
-      hi[u] = h;
-      if (lo) lo[u] = l;
+      hi[u] = H::pack(h);
+      if (lo) lo[u] = H::pack(l);
     } else {
       hi[u] = make_uint4(0, 0, 0, 0);
       if (lo) lo[u] = make_uint4(0, 0, 0, 0);

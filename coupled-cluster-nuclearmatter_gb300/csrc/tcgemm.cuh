@@ -65,7 +65,6 @@ struct TcSplitJob {
   int64_t sr, sk;
   int rows, cols, tile_rows, nk, rows_pad;
   void *hi, *lo;
-  double scale;
 };
 // Work list of the split kernels: (job, first unit, end unit) per block, at most
 // kSplitChunk 16-byte units, covering only the row groups of each tile that hold rows of
