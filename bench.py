@@ -208,7 +208,7 @@ def kernel_work(P, H, ring, precision):
             "ring_rebase_digits": ("byte", b_ring_oz)}
 
 
-KERNEL_NAMES = {"x_fp64": "k_gemm<double> X = V_hhpp' T' (split-K)", "i4_fp64": "k_gemm<double> I4",
+KERNEL_NAMES = {"x_fp64": "k_xdot X = V_hhpp'^T T' (FP64 column dots)", "i4_fp64": "k_gemm<double> I4",
                 "ring_fp64": "k_gemm<double> ring", "ladder_fp64": "k_gemm<double> fused pp+hh ladder",
                 "pp_rebase_fp64": "k_gemm<double> pp-ladder at a re-base", "hh_fp64": "k_gemm<double> hh-ladder",
                 "pp_tc": "k_tc_gemm pp + hh ladder corrections (3 products, one accumulator)", "i4_tc": "k_tc_gemm dI4 correction",

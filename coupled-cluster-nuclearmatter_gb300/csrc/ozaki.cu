@@ -6,7 +6,8 @@
 //     kOzSlices B digit tiles into one of two B buffers, then the kOzSlices A digit
 //     tiles one by one through a ring of kOzStages stages;
 //   warp 5 (one lane) issues tcgen05.mma: A digit i times B digits j = 0 .. 8 - i into
-//     the tensor-memory accumulator of level i + j, and commits each stage back;
+//     the tensor-memory accumulators of levels i + j, all j in one MMA over the stacked
+//     B digit tiles, and commits each stage back;
 //   warps 0-3 drain the kOzLevels accumulators after every K chunk (kOzChunkTiles K
 //     tiles, short enough for every level sum to stay an exact FP32 integer), combine
 //     them in two 64-bit integers, convert to FP64 once, scale by 2^(eA + eB) and add
@@ -154,8 +155,7 @@ __global__ void __launch_bounds__(kOzThreads, 1) k_oz_gemm(const OzProb *__restr
           atomicExch(err, 4);
           continue;
         }
-        const int nc = min(kOzN, P.npad - tl.n0), nk = P.nk;
-        const uint32_t idesc = instr_desc<kTcBF16>(128, nc);
+        const int nk = P.nk;
         const int nchunk = (nk + kOzChunkTiles - 1) / kOzChunkTiles;
         for (int c = 0; c < nchunk && ok; ++c, ++ck) {
           if (ck > 0 && !wait(drained, (uint32_t)((ck - 1) & 1))) { ok = false; break; }
@@ -170,13 +170,20 @@ __global__ void __launch_bounds__(kOzThreads, 1) k_oz_gemm(const OzProb *__restr
               const int s = cnt % kOzStages;
               if (!wait(&afull[s], (uint32_t)((cnt / kOzStages) & 1))) { ok = false; break; }
               tc_fence_after();
-              const uint32_t sa = smem_u32(abuf + s * kATile);
-              for (int j = 0; i + j < kOzSlices; ++j) {
-                const uint32_t d = tmem + (uint32_t)((i + j) * kOzN);
+              // A digit i times B digits j = 0 .. 8 - i lands in levels i .. 8: the B digit
+              // tiles sit one after the other (kOzN rows each) and the level accumulators
+              // kOzN columns apart, so one MMA of N = kOzN (9 - i) covers them all (two
+              // when that exceeds 256 columns).  Columns beyond a narrow tile's nc come
+              // from stale B rows and are never drained.
+              const uint64_t da = smem_desc(smem_u32(abuf + s * kATile));
 #pragma unroll
-                for (int ks = 0; ks < 4; ++ks) {
-                  const uint32_t acc = (kt > k_beg || i > 0 || ks > 0) ? 1u : 0u;
-                  tc_mma<kTcBF16>(d, smem_desc(sa + ks * 256), smem_desc(sb + j * kBSlot + ks * 256), idesc, acc);
+              for (int ks = 0; ks < 4; ++ks) {
+                const uint32_t acc = (kt > k_beg || i > 0 || ks > 0) ? 1u : 0u;
+                for (int j0 = 0; j0 < kOzSlices - i; j0 += 256 / kOzN) {
+                  const int nj = min(kOzSlices - i - j0, 256 / kOzN);
+                  tc_mma<kTcBF16>(tmem + (uint32_t)((i + j0) * kOzN), da + (uint64_t)(ks * 16),
+                                  smem_desc(sb + (uint32_t)j0 * kBSlot) + (uint64_t)(ks * 16),
+                                  instr_desc<kTcBF16>(128, nj * kOzN), acc);
                 }
               }
               tc_commit(smem_u32(&aempty[s]));
@@ -207,7 +214,12 @@ __global__ void __launch_bounds__(kOzThreads, 1) k_oz_gemm(const OzProb *__restr
       const bool live = m < P.M;
       const int eAm = live ? P.eA[m] : 0;
       double *crow = P.C + (int64_t)(live ? m : 0) * P.sCm;
+      // a warp none of whose rows is stored skips the drain
+      const bool warp_live = tl.mt * 128 + warp * 32 < P.M;
       for (int c = 0; c < nchunk; ++c, ++ck) {
+        double v[kOzN];  // this chunk's contribution to the row, scaled
+#pragma unroll
+        for (int q = 0; q < kOzN; ++q) v[q] = 0.0;
         const bool got = __all_sync(0xffffffffu, wait(done, (uint32_t)(ck & 1)));
         if (!got) {
           if (lane == 0) atomicExch(err, 3);
@@ -215,47 +227,53 @@ __global__ void __launch_bounds__(kOzThreads, 1) k_oz_gemm(const OzProb *__restr
           break;
         }
         tc_fence_after();
-        // a warp none of whose rows is stored skips the drain
-        for (int cb = 0; cb < nc && tl.mt * 128 + warp * 32 < P.M; cb += 16) {
-          long long zh[16], zl[16];
+        // 8 columns at a time: two 64-bit level sums per column stay in registers
 #pragma unroll
-          for (int q = 0; q < 16; ++q) zh[q] = zl[q] = 0;
+        for (int cb = 0; cb < kOzN; cb += 8) {
+          if (!warp_live || cb >= nc) break;
+          int eb[8];
+#pragma unroll
+          for (int q = 0; q < 8; ++q) eb[q] = (tl.n0 + cb + q < P.N) ? P.eB[tl.n0 + cb + q] : 0;
+          long long zh[8], zl[8];
+#pragma unroll
+          for (int q = 0; q < 8; ++q) zh[q] = zl[q] = 0;
 #pragma unroll
           for (int lv = 0; lv < kOzLevels; ++lv) {
-            uint32_t r[16];
-            tmem_ld16(tbase + (uint32_t)(lv * kOzN + cb), r);
+            uint32_t r[8];
+            tmem_ld8(tbase + (uint32_t)(lv * kOzN + cb), r);
             tmem_ld_wait();
 #pragma unroll
-            for (int q = 0; q < 16; ++q) {
+            for (int q = 0; q < 8; ++q) {
               // an exact integer below 2^24 in magnitude
-              const long long v = (long long)__float2int_rz(__uint_as_float(r[q]));
-              if (lv < 4) zh[q] += v * (1ll << (kOzBits * (3 - lv)));
-              else zl[q] += v * (1ll << (kOzBits * (8 - lv)));
+              const long long x = (long long)__float2int_rz(__uint_as_float(r[q]));
+              if (lv < 4) zh[q] += x * (1ll << (kOzBits * (3 - lv)));
+              else zl[q] += x * (1ll << (kOzBits * (8 - lv)));
             }
           }
-          if (live) {
-            // all loads of the row first (the stores could alias them), then the stores
-            double old[16];
-            int eb[16];
 #pragma unroll
-            for (int q = 0; q < 16; ++q) {
-              const int n = tl.n0 + cb + q;
-              old[q] = n < P.N ? crow[(int64_t)n * P.sCn] : 0.0;
-              eb[q] = n < P.N ? P.eB[n] : 0;
-            }
-#pragma unroll
-            for (int q = 0; q < 16; ++q) {
-              const int n = tl.n0 + cb + q;
-              if (n < P.N) {
-                const double z = fma((double)zh[q], 0x1p-30, (double)zl[q] * 0x1p-60);
-                crow[(int64_t)n * P.sCn] = old[q] + P.alpha * (z * pow2(eAm + eb[q]));
-              }
-            }
+          for (int q = 0; q < 8; ++q) {
+            const double z = fma((double)zh[q], 0x1p-30, (double)zl[q] * 0x1p-60);
+            v[cb + q] = P.alpha * (z * pow2(eAm + eb[q]));
           }
         }
+        // the level accumulators are read: the next chunk's MMAs may start while this
+        // chunk's sums go to C (all loads of the row first, then the stores)
         tc_fence_before();
         __syncwarp();
         if (lane == 0) mbar_arrive(smem_u32(drained));
+        if (live) {
+          double old[kOzN];
+#pragma unroll
+          for (int q = 0; q < kOzN; ++q) {
+            const int n = tl.n0 + q;
+            old[q] = (q < nc && n < P.N) ? crow[(int64_t)n * P.sCn] : 0.0;
+          }
+#pragma unroll
+          for (int q = 0; q < kOzN; ++q) {
+            const int n = tl.n0 + q;
+            if (q < nc && n < P.N) crow[(int64_t)n * P.sCn] = old[q] + v[q];
+          }
+        }
       }
     }
   }
