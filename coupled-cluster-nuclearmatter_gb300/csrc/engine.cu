@@ -918,8 +918,9 @@ class Engine final : public IEngine {
     }
   }
   void run_x() {
-    launch_xdot<S>(D_, (const int4 *)xwork_.p, nxwork_, Vhp_.as<S>(), T_.as<S>(), X_.as<S>(), st_);
-    ++launches_;
+    launch_xdot<S>(D_, (const int4 *)xwork_.p, nxwork_, (const int4 *)xgroups_.p, nxgroups_, Vhp_.as<S>(), T_.as<S>(),
+                   xpart_.as<S>(), X_.as<S>(), st_);
+    launches_ += 2;
   }
   void build_gemm_plans() {
     const Layout &L = *L_;
@@ -933,16 +934,34 @@ class Engine final : public IEngine {
       ni6rows_ = (int)rt.size();
       i6dots_.alloc((size_t)std::max<int64_t>(3 * n_t_, 1) * sizeof(S), &bytes_);
     }
-    {  // X = V_hhpp' T'  (H x H, K = P): column-dot work items
-      std::vector<int4> w;
+    {  // X = V_hhpp' T'  (H x H, K = P): column-dot items of at most kXSlice K each,
+       // longest first; their partial tiles are summed per X tile in slice order
+      std::vector<int4> w, gr;
+      std::vector<int> klen;
+      int slot = 0;
       for (int c = 0; c < nc; ++c) {
         const auto &pk = L.pk[c];
         if (pk.H <= 0 || pk.P <= 0) continue;
+        const int nsl = (pk.P + kXSlice - 1) / kXSlice;
         for (int m0 = 0; m0 < pk.H; m0 += kXM)
-          for (int j0 = 0; j0 < pk.H; j0 += kXJ) w.push_back(make_int4(c, m0, j0, 0));
+          for (int j0 = 0; j0 < pk.H; j0 += kXJ) {
+            gr.push_back(make_int4(c, m0 | (j0 << 16), slot, nsl));
+            for (int ks = 0; ks < nsl; ++ks) {
+              w.push_back(make_int4(c, m0 | (j0 << 16), ks, slot++));
+              klen.push_back(std::min(pk.P, (ks + 1) * kXSlice) - ks * kXSlice);
+            }
+          }
       }
-      upload(xwork_, w, &bytes_);
-      nxwork_ = (int)w.size();
+      std::vector<int> ord(w.size());
+      for (size_t i = 0; i < ord.size(); ++i) ord[i] = (int)i;
+      std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) { return klen[x] > klen[y]; });
+      std::vector<int4> ws(w.size());
+      for (size_t i = 0; i < ord.size(); ++i) ws[i] = w[ord[i]];
+      upload(xwork_, ws, &bytes_);
+      upload(xgroups_, gr, &bytes_);
+      nxwork_ = (int)ws.size();
+      nxgroups_ = (int)gr.size();
+      xpart_.alloc((size_t)std::max(slot, 1) * kXM * kXJ * sizeof(S), &bytes_);
     }
     build_fp64_plans(planLadder_, planI4_, planRing_, -1, nullptr);
   }
@@ -2104,8 +2123,8 @@ class Engine final : public IEngine {
   DBuf onx_, ony_, onz_, osz_, otz_, okx_, oky_, okz_, oe_;
   // state
   DBuf T_, R_, Vhp_, Vpp_, Vhh_, X_, I9_, Tph_, Rph_, Vph_, W_, I4_, fdiag_, f6_, f7_, d2ij_, d2ab_, i6off_, i7off_;
-  DBuf partial_, res_, flag_, stage_, hist_, hist_t_, hist_e_, xwork_, i6rows_, i6dots_;
-  int nxwork_ = 0, ni6rows_ = 0;
+  DBuf partial_, res_, flag_, stage_, hist_, hist_t_, hist_e_, xwork_, xgroups_, xpart_, i6rows_, i6dots_;
+  int nxwork_ = 0, nxgroups_ = 0, ni6rows_ = 0;
   Plan planLadder_, planI4_, planRing_, planPP_, planHH_;
   // mixed precision
   bool mixed_ready_ = false;

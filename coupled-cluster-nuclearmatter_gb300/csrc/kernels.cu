@@ -259,12 +259,14 @@ __device__ __forceinline__ void xdot_rows(const S *__restrict__ V, const S (*Ts)
 
 template <typename S>
 __global__ void __launch_bounds__(256) k_xdot(DevLayout L, const int4 *__restrict__ work, const S *__restrict__ V,
-                                              const S *__restrict__ T, S *__restrict__ X) {
+                                              const S *__restrict__ T, S *__restrict__ part) {
   constexpr int RPW = kXM / 8;  // rows per warp
   __shared__ S Ts[kXJ][kXK];
-  const int4 w = work[blockIdx.x];
-  const int ch = w.x, m0 = w.y, j0 = w.z;
-  const int P = L.P[ch], H = L.H[ch];
+  const int4 w = work[blockIdx.x];  // (channel, m0 | j0 << 16, K slice, partial slot)
+  const int ch = w.x, m0 = w.y & 0xffff, j0 = w.y >> 16;
+  const int H = L.H[ch];
+  const int kbeg = w.z * kXSlice;
+  const int P = min(L.P[ch], kbeg + kXSlice);  // this item's K range is [kbeg, P)
   const int64_t off = L.t_off[ch];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nj = min(kXJ, H - j0);
@@ -273,41 +275,58 @@ __global__ void __launch_bounds__(256) k_xdot(DevLayout L, const int4 *__restric
   for (int r = 0; r < RPW; ++r)
 #pragma unroll
     for (int j = 0; j < kXJ; ++j) acc[r][j] = S(0.0);
-  for (int k0 = 0; k0 < P; k0 += kXK) {
+  const int ld = L.P[ch];  // column length of V' and T'
+  for (int k0 = kbeg; k0 < P; k0 += kXK) {
     const int kn = min(kXK, P - k0);
     for (int x = threadIdx.x; x < kXJ * kXK; x += blockDim.x) {
       const int j = x / kXK, k = x % kXK;
-      Ts[j][k] = (j < nj && k < kn) ? T[off + (int64_t)P * (j0 + j) + k0 + k] : S(0.0);
+      Ts[j][k] = (j < nj && k < kn) ? T[off + (int64_t)ld * (j0 + j) + k0 + k] : S(0.0);
     }
     __syncthreads();
     // no FP64 work on the padding columns of a partial column block
     switch (nj) {
-      case 8: xdot_rows<S, 8>(V, Ts, off, P, H, m0, k0, kn, warp, lane, acc); break;
-      case 7: xdot_rows<S, 7>(V, Ts, off, P, H, m0, k0, kn, warp, lane, acc); break;
-      case 6: xdot_rows<S, 6>(V, Ts, off, P, H, m0, k0, kn, warp, lane, acc); break;
-      case 5: xdot_rows<S, 5>(V, Ts, off, P, H, m0, k0, kn, warp, lane, acc); break;
-      case 4: xdot_rows<S, 4>(V, Ts, off, P, H, m0, k0, kn, warp, lane, acc); break;
-      case 3: xdot_rows<S, 3>(V, Ts, off, P, H, m0, k0, kn, warp, lane, acc); break;
-      case 2: xdot_rows<S, 2>(V, Ts, off, P, H, m0, k0, kn, warp, lane, acc); break;
-      default: xdot_rows<S, 1>(V, Ts, off, P, H, m0, k0, kn, warp, lane, acc); break;
+      case 8: xdot_rows<S, 8>(V, Ts, off, ld, H, m0, k0, kn, warp, lane, acc); break;
+      case 7: xdot_rows<S, 7>(V, Ts, off, ld, H, m0, k0, kn, warp, lane, acc); break;
+      case 6: xdot_rows<S, 6>(V, Ts, off, ld, H, m0, k0, kn, warp, lane, acc); break;
+      case 5: xdot_rows<S, 5>(V, Ts, off, ld, H, m0, k0, kn, warp, lane, acc); break;
+      case 4: xdot_rows<S, 4>(V, Ts, off, ld, H, m0, k0, kn, warp, lane, acc); break;
+      case 3: xdot_rows<S, 3>(V, Ts, off, ld, H, m0, k0, kn, warp, lane, acc); break;
+      case 2: xdot_rows<S, 2>(V, Ts, off, ld, H, m0, k0, kn, warp, lane, acc); break;
+      default: xdot_rows<S, 1>(V, Ts, off, ld, H, m0, k0, kn, warp, lane, acc); break;
     }
     __syncthreads();
   }
-  S *xc = X + L.hh2_off[ch];
+  // the item's kXM x kXJ partial tile, row-major, in its slot
+  S *pc = part + (int64_t)w.w * (kXM * kXJ);
 #pragma unroll
   for (int r = 0; r < RPW; ++r) {
-    const int m = m0 + warp + 8 * r;
-    if (m >= H) continue;
+    const int mr = warp + 8 * r;
 #pragma unroll
     for (int j = 0; j < kXJ; ++j) {
       const S tot = from2<S>(warp_sum2(to2(acc[r][j])));
-      if (lane == 0 && j < nj) xc[m + (int64_t)H * (j0 + j)] = tot;
+      if (lane == 0) pc[mr * kXJ + j] = tot;
     }
   }
 }
+// X tile (channel, m0 | j0 << 16, first slot, slices): the K-slice partials summed in
+// slice order, so the result does not depend on which item finished first
 template <typename S>
-void launch_xdot(const DevLayout &L, const int4 *work, int nwork, const S *V, const S *T, S *X, cudaStream_t st) {
-  if (nwork > 0) k_xdot<S><<<nwork, 256, 0, st>>>(L, work, V, T, X);
+__global__ void __launch_bounds__(kXM * kXJ) k_xreduce(DevLayout L, const int4 *__restrict__ groups,
+                                                       const S *__restrict__ part, S *__restrict__ X) {
+  const int4 g = groups[blockIdx.x];
+  const int ch = g.x, m0 = g.y & 0xffff, j0 = g.y >> 16, H = L.H[ch];
+  const int mr = threadIdx.x / kXJ, j = threadIdx.x % kXJ;
+  if (m0 + mr >= H || j0 + j >= H) return;
+  S tot = part[(int64_t)g.z * (kXM * kXJ) + threadIdx.x];
+  for (int s = 1; s < g.w; ++s) tot += part[(int64_t)(g.z + s) * (kXM * kXJ) + threadIdx.x];
+  X[L.hh2_off[ch] + (m0 + mr) + (int64_t)H * (j0 + j)] = tot;
+}
+template <typename S>
+void launch_xdot(const DevLayout &L, const int4 *work, int nwork, const int4 *groups, int ngroups, const S *V,
+                 const S *T, S *part, S *X, cudaStream_t st) {
+  if (nwork <= 0) return;
+  k_xdot<S><<<nwork, 256, 0, st>>>(L, work, V, T, part);
+  k_xreduce<S><<<ngroups, kXM * kXJ, 0, st>>>(L, groups, part, X);
 }
 
 // ============================================================================
@@ -1046,7 +1065,8 @@ void launch_unpack_t(const DevLayout &L, int ch, int n_pp, const int *pp_signed,
   template void launch_gather_tph<S>(const DevLayout &, const S *, S *, cudaStream_t);                                 \
   template void launch_i7<S>(const DevLayout &, const S *, const S *, const S *, S *, S *, cudaStream_t);             \
   template void launch_i9<S>(const DevLayout &, int64_t, const S *, const S *, S *, cudaStream_t);                     \
-  template void launch_xdot<S>(const DevLayout &, const int4 *, int, const S *, const S *, S *, cudaStream_t);        \
+  template void launch_xdot<S>(const DevLayout &, const int4 *, int, const int4 *, int, const S *, const S *, S *, S *, \
+                              cudaStream_t);        \
   template void launch_i6<S>(const DevLayout &, const int2 *, int, S *, const S *, const S *, const S *, const S *,   \
                              S *, S *, cudaStream_t);                                                                  \
   template void launch_rinit<S>(const DevLayout &, const S *, const S *, const S *, const S *, const S *, S *,         \

@@ -57,7 +57,12 @@ struct DevPotential {
 template <typename S> void launch_gather_tph(const DevLayout &L, const S *T, S *Tph, cudaStream_t st);
 // X' = V_hhpp'^T T' per channel; work items (channel, first row, first column, 0)
 constexpr int kXM = 32, kXJ = 8, kXK = 256;
-template <typename S> void launch_xdot(const DevLayout &L, const int4 *work, int nwork, const S *V, const S *T, S *X, cudaStream_t st);
+constexpr int kXSlice = 512;  // K per X work item: long channels are split, partials summed in order
+// X = V_hhpp'^T T' as K-sliced column-dot items into partial slots, then the slices
+// summed in order (work and groups built by the engine)
+template <typename S>
+void launch_xdot(const DevLayout &L, const int4 *work, int nwork, const int4 *groups, int ngroups, const S *V,
+                 const S *T, S *part, S *X, cudaStream_t st);
 template <typename S> void launch_i7(const DevLayout &L, const S *X, const S *fdiag, const S *f7, S *d2ij, S *i7off, cudaStream_t st);
 template <typename S> void launch_i9(const DevLayout &L, int64_t n, const S *Vhh, const S *X, S *I9, cudaStream_t st);
 // I6 in two passes; rowtile: (channel, first packed pp row) per block of kI6Rows rows;
