@@ -24,6 +24,23 @@ __device__ inline double2 warp_sum2(double2 v) {
   }
   return v;
 }
+__device__ inline double shfl_xor(double x, int o) { return __shfl_xor_sync(0xffffffffu, x, o); }
+__device__ inline cplx shfl_xor(cplx x, int o) { return cplx(shfl_xor(x.re, o), shfl_xor(x.im, o)); }
+// Butterfly reduce-scatter of 32 values per lane over the warp: afterwards v[0] of lane
+// l holds the warp total of value l.  31 additions per lane instead of 5 per value.
+template <typename S>
+__device__ inline void warp_reduce_scatter32(S (&v)[32], int lane) {
+#pragma unroll
+  for (int o = 16, n = 32; o >= 1; o >>= 1, n >>= 1) {
+    const bool upper = (lane & o) != 0;
+#pragma unroll
+    for (int i = 0; i < n / 2; ++i) {
+      const S give = upper ? v[i] : v[i + n / 2];
+      const S keep = upper ? v[i + n / 2] : v[i];
+      v[i] = keep + shfl_xor(give, o);
+    }
+  }
+}
 __device__ inline double2 to2(double x) { return make_double2(x, 0.0); }
 __device__ inline double2 to2(cplx x) { return make_double2(x.re, x.im); }
 template <typename S> __device__ inline S from2(double2 v);
@@ -296,17 +313,16 @@ __global__ void __launch_bounds__(256) k_xdot(DevLayout L, const int4 *__restric
     }
     __syncthreads();
   }
-  // the item's kXM x kXJ partial tile, row-major, in its slot
-  S *pc = part + (int64_t)w.w * (kXM * kXJ);
+  // the item's kXM x kXJ partial tile, row-major, in its slot: lane l of the warp ends
+  // with value l = (r, j) = (l / kXJ, l % kXJ) of the warp's rows
+  static_assert(RPW * kXJ == 32, "one value per lane after the reduce-scatter");
+  S vals[32];
 #pragma unroll
-  for (int r = 0; r < RPW; ++r) {
-    const int mr = warp + 8 * r;
+  for (int r = 0; r < RPW; ++r)
 #pragma unroll
-    for (int j = 0; j < kXJ; ++j) {
-      const S tot = from2<S>(warp_sum2(to2(acc[r][j])));
-      if (lane == 0) pc[mr * kXJ + j] = tot;
-    }
-  }
+    for (int j = 0; j < kXJ; ++j) vals[r * kXJ + j] = acc[r][j];
+  warp_reduce_scatter32(vals, lane);
+  part[(int64_t)w.w * (kXM * kXJ) + (warp + 8 * (lane / kXJ)) * kXJ + lane % kXJ] = vals[0];
 }
 // X tile (channel, m0 | j0 << 16, first slot, slices): the K-slice partials summed in
 // slice order, so the result does not depend on which item finished first
@@ -536,7 +552,7 @@ __global__ void k_update(DevLayout L, int mode, S *__restrict__ T, const S *__re
     if (mode == 2) {
       const S pr = t * vij;
       v[0] += real_(pr);
-      v[1] += imag_(pr);
+      if constexpr (ScalarOf<S>::complex) v[1] += imag_(pr);
       continue;
     }
     const int ij = e / P, ab = e - ij * P;
@@ -557,7 +573,7 @@ __global__ void k_update(DevLayout L, int mode, S *__restrict__ T, const S *__re
     }
     const S pr = tn * vij;
     v[0] += real_(pr);
-    v[1] += imag_(pr);
+    if constexpr (ScalarOf<S>::complex) v[1] += imag_(pr);
   }
   block_partial<3>(v, partial);
 }
@@ -588,9 +604,13 @@ __global__ void k_dots(int64_t n, const S *__restrict__ a, PtrPack<S> bs, int nb
 #pragma unroll
     for (int k = 0; k < kMaxDots; ++k) {
       if (k < nb) {
-        const S pr = av * bs.p[k][x];
-        v[2 * k] += real_(pr);
-        v[2 * k + 1] += imag_(pr);
+        if constexpr (ScalarOf<S>::complex) {
+          const S pr = av * bs.p[k][x];
+          v[2 * k] += real_(pr);
+          v[2 * k + 1] += imag_(pr);
+        } else {  // no FP64 additions of a zero imaginary part
+          v[2 * k] = fma(real_(av), real_(bs.p[k][x]), v[2 * k]);
+        }
       }
     }
   }
