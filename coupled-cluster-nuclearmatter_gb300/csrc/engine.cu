@@ -1509,6 +1509,30 @@ class Engine final : public IEngine {
       js.push_back(j);
     }
   }
+  // Map and gather jobs filling tile region (b, off) from the packed split of T - T_b:
+  // element (r, k) is packed entry ind ? ind[base + r sr + k sk] : base + r sr + k sk
+  // (scalar elements), one job per scalar component
+  void add_gather(std::vector<TcMapJob> &mj, std::vector<TcGatherJob> &gj, int64_t base, const int32_t *ind,
+                  int64_t sr, int64_t sk, int rows, int cols, int tile_rows, int rows_pad, TileBuf &b, DBuf &map,
+                  int64_t off) {
+    const size_t es = tc_kind_ == kTcBF16 ? 2 : 4;
+    const int tk = tc_tile_k(tc_kind_);
+    for (int c = 0; c < kNComp; ++c) {
+      TcMapJob m{};
+      m.base = base; m.sr = sr; m.sk = sk;
+      m.rows = rows; m.cols = cols; m.tile_rows = tile_rows; m.nk = (cols + tk - 1) / tk; m.rows_pad = rows_pad;
+      m.ind = ind;
+      m.map = map.as<int32_t>() + off + c * b.n;
+      mj.push_back(m);
+      TcGatherJob g{};
+      g.map = m.map;
+      g.phi = (const char *)phi_.p + (size_t)c * n_t_ * es;
+      g.plo = (const char *)plo_.p + (size_t)c * n_t_ * es;
+      g.hi = (char *)b.hi.p + (off + c * b.n) * es;
+      g.lo = (char *)b.lo.p + (off + c * b.n) * es;
+      gj.push_back(g);
+    }
+  }
   // C (S units, strides sCm, sCn) += alpha A B with A (M x K) in tile buffer a at ao and
   // B (N x K) in b at bo.  N beyond one accumulator (256 columns) runs as column blocks
   // of at most 256 that step through the whole B operand's K tiles.
@@ -1861,18 +1885,29 @@ class Engine final : public IEngine {
     HHb_.alloc(std::max<int64_t>(n_t_, 1) * sz, &bytes_);
     tcerr_.alloc(sizeof(int), &bytes_);
     CK(cudaMemset(tcerr_.p, 0, sizeof(int)));
-    std::vector<TcSplitJob> js_static, js_tphb, js_it1, js_it2, js_it3;
+    std::vector<TcSplitJob> js_static, js_tphb, js_it2, js_it3;
+    // dT' is split once into packed hi/lo arrays per iteration; its tiled copies (dT' as
+    // A and B, dT_ph as A and B) are gathered through maps built here, once per layout
+    phi_.alloc(std::max<int64_t>(n_t_, 1) * kNComp * es, &bytes_);
+    plo_.alloc(std::max<int64_t>(n_t_, 1) * kNComp * es, &bytes_);
+    tphmap_.alloc(std::max<int64_t>(n_ph_, 1) * sizeof(int32_t), &bytes_);
+    launch_tph_map(D_, tphmap_.as<int32_t>(), st_);
+    for (auto pr : {std::make_pair(&mD_, &tD_), std::make_pair(&mDA_, &tDA_), std::make_pair(&mDphB_, &tDphB_),
+                    std::make_pair(&mDphA_, &tDphA_)})
+      pr.first->alloc((size_t)pr.second->n * kNComp * sizeof(int32_t), &bytes_);
+    std::vector<TcMapJob> mjobs;
+    std::vector<TcGatherJob> gjobs;
     TcList pp, p4, pr1;
     {
       int64_t oa = 0, ob = 0, voff = 0, hoff = 0, oda = 0, otb = 0, oi9 = 0;
       for (int c = 0; c < nc; ++c) {
         const auto &pk = L.pk[c];
         if (pk.P > 0 && pk.H > 0) {
-          S *t = T_.as<S>() + pk.t_off, *tb = Tb_.as<S>() + pk.t_off;
+          S *tb = Tb_.as<S>() + pk.t_off;
           add_split(js_static, Vpp_.as<S>() + voff, nullptr, pk.P, 1, pk.P, pk.P, 128, mpad(pk.P), tVpp_, oa);
-          add_split(js_it1, t, tb, pk.P, 1, pk.H, pk.P, npadf(pk.H), npadf(pk.H), tD_, ob);
+          add_gather(mjobs, gjobs, pk.t_off, nullptr, pk.P, 1, pk.H, pk.P, npadf(pk.H), npadf(pk.H), tD_, mD_, ob);
           // hh-ladder: R' += HH_b + dT' I9' + T_b' (I9' - I9_b')
-          add_split(js_it1, t, tb, 1, pk.P, pk.P, pk.H, 128, mpad(pk.P), tDA_, oda);
+          add_gather(mjobs, gjobs, pk.t_off, nullptr, 1, pk.P, pk.P, pk.H, 128, mpad(pk.P), tDA_, mDA_, oda);
           add_split(js_tphb, tb, nullptr, 1, pk.P, pk.P, pk.H, 128, mpad(pk.P), tTbA_, otb);
           add_split(js_it3, I9_.as<S>() + hoff, nullptr, pk.H, 1, pk.H, pk.H, npadf(pk.H), npadf(pk.H), tI9B_, oi9);
           add_split(js_it3, dI9_.as<S>() + hoff, nullptr, pk.H, 1, pk.H, pk.H, npadf(pk.H), npadf(pk.H), tdI9B_, oi9);
@@ -1894,12 +1929,13 @@ class Engine final : public IEngine {
       for (int q = 0; q < nq; ++q) {
         const int nph = L.ph[1].side1[q].size(), nhp = L.ph[1].side2[q].size();
         if (nph > 0 && nhp > 0) {
-          S *tph = Tph_.as<S>() + toff, *tphb = Tphb_.as<S>() + toff;
+          S *tphb = Tphb_.as<S>() + toff;
           // static A = V_ph (n_hp x n_ph, column-major)
           add_split(js_static, Vph_.as<S>() + toff, nullptr, 1, nhp, nhp, nph, 128, mpad(nhp), tVph_, ov);
-          // per iteration: B = dTph (rows n_hp, K = n_ph), A = dTph (rows n_ph, K = n_hp)
-          add_split(js_it1, tph, tphb, nph, 1, nhp, nph, npadf(nhp), npadf(nhp), tDphB_, odb);
-          add_split(js_it1, tph, tphb, 1, nph, nph, nhp, 128, mpad(nph), tDphA_, oda);
+          // per iteration, gathered: B = dT_ph (rows n_hp, K = n_ph), A = dT_ph (rows n_ph, K = n_hp)
+          add_gather(mjobs, gjobs, toff, tphmap_.as<int32_t>(), nph, 1, nhp, nph, npadf(nhp), npadf(nhp), tDphB_, mDphB_,
+                     odb);
+          add_gather(mjobs, gjobs, toff, tphmap_.as<int32_t>(), 1, nph, nph, nhp, 128, mpad(nph), tDphA_, mDphA_, oda);
           // at re-base: A = Tph_b
           add_split(js_tphb, tphb, nullptr, 1, nph, nph, nhp, 128, mpad(nph), tTphbA_, ota);
           // after dI4: B = dI4 and B = I4 (rows n_hp, K = n_hp)
@@ -1923,7 +1959,18 @@ class Engine final : public IEngine {
     }
     finalize_split(spStatic_, js_static);
     finalize_split(spTphb_, js_tphb);
-    finalize_split(spIter1_, js_it1);
+    {  // the maps, and the gather plan over the same units
+      std::vector<int4> ch;
+      for (size_t j = 0; j < mjobs.size(); ++j)
+        split_ranges((int)j, mjobs[j].rows, mjobs[j].rows_pad, mjobs[j].tile_rows, mjobs[j].nk, ch);
+      DBuf mj;
+      upload(mj, mjobs, &bytes_);
+      upload(gplan_.chunks, ch, &bytes_);
+      upload(gplan_.jobs, gjobs, &bytes_);
+      gplan_.nchunks = (int)ch.size();
+      launch_tc_build_map(tc_kind_, (const TcMapJob *)mj.p, (const int4 *)gplan_.chunks.p, gplan_.nchunks, st_);
+      CK(cudaStreamSynchronize(st_));  // the map job table goes out of scope
+    }
     finalize_split(spIter2_, js_it2);
     finalize_split(spIter3_, js_it3);
     finalize_tc(tcPP_, pp);
@@ -2052,9 +2099,15 @@ class Engine final : public IEngine {
   // contractions as cached FP64 products at T_b plus tensor-core corrections
   void residual_mixed() {
     mark(0);
-    launch_gather_tph<S>(D_, T_.as<S>(), Tph_.as<S>(), st_);
     kbegin(kKSplit);
-    run_split(spIter1_);  // dT' (B and A), dT_ph (B and A)
+    // dT' = T' - T_b' split once; dT' (B and A) and dT_ph (B and A) gathered from it
+    // (T_ph itself is not needed in FP64 between re-bases)
+    for (int c = 0; c < kNComp; ++c)
+      launch_tc_split_packed(tc_kind_, (const double *)T_.p + c, (const double *)Tb_.p + c, n_t_, kNComp,
+                             (char *)phi_.p + (size_t)c * n_t_ * (tc_kind_ == kTcBF16 ? 2 : 4),
+                             (char *)plo_.p + (size_t)c * n_t_ * (tc_kind_ == kTcBF16 ? 2 : 4), st_);
+    launch_tc_gather(tc_kind_, (const TcGatherJob *)gplan_.jobs.p, (const int4 *)gplan_.chunks.p, gplan_.nchunks, st_);
+    launches_ += kNComp + 1;
     kend();
     mark(1);
     // X in FP64: it feeds the dressed hole denominators of every amplitude through I7
@@ -2091,7 +2144,7 @@ class Engine final : public IEngine {
     run_tc(tcPP_);  // R' += PP_b + HH_b + V_pppp' dT' + dT' I9' + T_b' (I9' - I9_b')
     kend();
     mark(7);
-    launches_ += 7;  // gather, sub, i7, i9, i6, add, rinit
+    launches_ += 6;  // sub, i7, i9, i6, add, rinit
     if (timing_) accumulate_timers(0, 7);
   }
 
@@ -2138,7 +2191,9 @@ class Engine final : public IEngine {
   int64_t oz_v_version_ = -1;
   TileBuf tVpp_, tD_, tVph_, tDphB_, tTphbA_, tDphA_, tdI4B_, tI4B_, tDA_, tI9B_, tTbA_, tdI9B_;
   TcPlan tcPP_, tcI4_, tcR1_;
-  SplitPlan spStatic_, spTphb_, spIter1_, spIter2_, spIter3_;
+  SplitPlan spStatic_, spTphb_, spIter2_, spIter3_;
+  DBuf phi_, plo_, tphmap_, mD_, mDA_, mDphB_, mDphA_;  // packed split of dT', gather maps
+  SplitPlan gplan_;                                     // gather jobs (TcGatherJob) and chunks
   double *host_res_ = nullptr;
   int host_flag_ = 0;
   int gemm_shape_[4] = {kShape128x32, kShape128x32, kShape64x64, kShape64x64};

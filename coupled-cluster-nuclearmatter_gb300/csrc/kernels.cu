@@ -238,6 +238,31 @@ __global__ void k_gather_tph(DevLayout L, const S *__restrict__ T, S *__restrict
 template <typename S> void launch_gather_tph(const DevLayout &L, const S *T, S *Tph, cudaStream_t st) {
   if (L.nphtile) k_gather_tph<S><<<L.nphtile, 256, 0, st>>>(L, T, Tph);
 }
+// the same walk as k_gather_tph, recording the signed source index instead of the value
+__global__ void k_tph_map(DevLayout L, int32_t *__restrict__ map) {
+  const int2 tl = L.phtile[blockIdx.x];
+  const int q = tl.x;
+  const int nph = L.n_ph[q], nhp = L.n_hp[q];
+  const int n = nph * nhp;
+  const int end = min(tl.y + kTileElems, n);
+  for (int e = tl.y + threadIdx.x; e < end; e += blockDim.x) {
+    const int c = e / nph, r = e - c * nph;
+    const int2 ai = L.ph_orb[L.ph_off[q] + r];
+    const int2 jb = L.hp_orb[L.hp_off[q] + c];
+    const int2 sab = L.pp_slot[(int64_t)(ai.x - L.A) * L.NP + (jb.y - L.A)];
+    const int2 sij = L.hh_slot[ai.y * L.A + jb.x];
+    int32_t m = 0;
+    if (sab.y != 0 && sij.y != 0) {
+      const int ch = sab.x;
+      const int32_t idx = (int32_t)(L.t_off[ch] + sidx(sab.y) + (int64_t)L.P[ch] * sidx(sij.y)) + 1;
+      m = (ssign(sab.y) * ssign(sij.y)) < 0 ? -idx : idx;
+    }
+    map[L.tph_off[q] + e] = m;
+  }
+}
+void launch_tph_map(const DevLayout &L, int32_t *map, cudaStream_t st) {
+  if (L.nphtile) k_tph_map<<<L.nphtile, 256, 0, st>>>(L, map);
+}
 
 // ============================================================================
 // X'(m, j) = sum_k V'(k, m) T'(k, j) per hhpp channel (the V_hhpp T product of the I9

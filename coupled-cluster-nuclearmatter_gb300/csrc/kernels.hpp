@@ -55,6 +55,8 @@ struct DevPotential {
 
 // ---- residual pieces --------------------------------------------------------
 template <typename S> void launch_gather_tph(const DevLayout &L, const S *T, S *Tph, cudaStream_t st);
+// where each T_ph entry comes from: +/-(packed T' index + 1), 0 for a zero entry
+void launch_tph_map(const DevLayout &L, int32_t *map, cudaStream_t st);
 // X' = V_hhpp'^T T' per channel; work items (channel, first row, first column, 0)
 constexpr int kXM = 32, kXJ = 8, kXK = 256;
 constexpr int kXSlice = 512;  // K per X work item: long channels are split, partials summed in order

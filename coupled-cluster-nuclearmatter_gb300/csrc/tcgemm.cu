@@ -489,7 +489,130 @@ __global__ void __launch_bounds__(256) k_tc_split(const TcSplitJob *__restrict__
   }
 }
 
+// element (row, k) of unit u of a job with the split kernels' tile geometry
+template <int CME>
+__device__ __forceinline__ void unit_rc(int u, int tile_rows, int nk, int &row, int &k0) {
+  constexpr int tk = 8 * CME;
+  const int tile_units = tile_rows * 8;
+  const int t = u / tile_units, w = u - t * tile_units;
+  const int rt = t / nk, kt = t - rt * nk;
+  const int g = w >> 6, kc = (w >> 3) & 7, r8 = w & 7;
+  row = rt * tile_rows + g * 8 + r8;
+  k0 = kt * tk + kc * CME;
+}
+
+template <int KIND>
+__global__ void __launch_bounds__(256) k_tc_build_map(const TcMapJob *__restrict__ jobs, const int4 *__restrict__ chunks) {
+  constexpr int cme = Half<KIND>::per16;
+  const int4 ck = chunks[blockIdx.x];
+  const TcMapJob J = jobs[ck.x];
+  for (int u = ck.y + threadIdx.x; u < ck.z; u += blockDim.x) {
+    int row, k0;
+    unit_rc<cme>(u, J.tile_rows, J.nk, row, k0);
+#pragma unroll
+    for (int j = 0; j < cme; ++j) {
+      int32_t m = 0;
+      if (row < J.rows && k0 + j < J.cols) {
+        const int64_t e = J.base + (int64_t)row * J.sr + (int64_t)(k0 + j) * J.sk;
+        m = J.ind ? J.ind[e] : (int32_t)(e + 1);
+      }
+      J.map[(int64_t)u * cme + j] = m;
+    }
+  }
+}
+
+// the hi and lo bit patterns of packed entry |m| - 1, sign flipped for m < 0
+template <int KIND>
+__device__ __forceinline__ void gather_one(const void *phi, const void *plo, int32_t m, uint32_t &h, uint32_t &l) {
+  if (m == 0) {
+    h = l = 0;
+    return;
+  }
+  const int64_t i = (m > 0 ? m : -m) - 1;
+  if (KIND == kTcBF16) {
+    const uint32_t sg = m < 0 ? 0x8000u : 0u;
+    h = (uint32_t)((const uint16_t *)phi)[i] ^ sg;
+    l = (uint32_t)((const uint16_t *)plo)[i] ^ sg;
+  } else {
+    const uint32_t sg = m < 0 ? 0x80000000u : 0u;
+    h = ((const uint32_t *)phi)[i] ^ sg;
+    l = ((const uint32_t *)plo)[i] ^ sg;
+  }
+}
+
+template <int KIND>
+__global__ void __launch_bounds__(256) k_tc_gather(const TcGatherJob *__restrict__ jobs, const int4 *__restrict__ chunks) {
+  constexpr int cme = Half<KIND>::per16;
+  const int4 ck = chunks[blockIdx.x];
+  const TcGatherJob J = jobs[ck.x];
+  uint4 *hi = (uint4 *)J.hi, *lo = (uint4 *)J.lo;
+  for (int u = ck.y + threadIdx.x; u < ck.z; u += blockDim.x) {
+    int32_t m[cme];
+    const int4 *mp = (const int4 *)J.map + (int64_t)u * (cme / 4);  // the unit's map entries
+#pragma unroll
+    for (int q = 0; q < cme / 4; ++q) {
+      const int4 a = mp[q];
+      m[4 * q] = a.x;
+      m[4 * q + 1] = a.y;
+      m[4 * q + 2] = a.z;
+      m[4 * q + 3] = a.w;
+    }
+    uint32_t h[cme], l[cme];
+#pragma unroll
+    for (int j = 0; j < cme; ++j) gather_one<KIND>(J.phi, J.plo, m[j], h[j], l[j]);
+    uint32_t hw[4], lw[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      if constexpr (cme == 8) {  // two BF16 per word
+        hw[q] = h[2 * q] | (h[2 * q + 1] << 16);
+        lw[q] = l[2 * q] | (l[2 * q + 1] << 16);
+      } else {
+        hw[q] = h[q];
+        lw[q] = l[q];
+      }
+    }
+    hi[u] = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+    lo[u] = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+  }
+}
+
+template <int KIND>
+__global__ void __launch_bounds__(256) k_tc_split_packed(const double *__restrict__ src, const double *__restrict__ sub,
+                                                         int64_t n, int stride, void *phi, void *plo) {
+  using B = BitSplit<Half<KIND>::nb>;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    uint32_t h, l;
+    if (sub) B::split_diff(src[i * stride], sub[i * stride], h, l);
+    else B::split(src[i * stride], h, l);
+    if (KIND == kTcBF16) {
+      ((uint16_t *)phi)[i] = (uint16_t)(h >> 16);
+      ((uint16_t *)plo)[i] = (uint16_t)(l >> 16);
+    } else {
+      ((uint32_t *)phi)[i] = h;
+      ((uint32_t *)plo)[i] = l;
+    }
+  }
+}
+
 }  // namespace
+
+void launch_tc_build_map(int kind, const TcMapJob *jobs, const int4 *chunks, int nchunks, cudaStream_t st) {
+  if (nchunks <= 0) return;
+  if (kind == kTcBF16) k_tc_build_map<kTcBF16><<<nchunks, 256, 0, st>>>(jobs, chunks);
+  else k_tc_build_map<kTcTF32><<<nchunks, 256, 0, st>>>(jobs, chunks);
+}
+void launch_tc_gather(int kind, const TcGatherJob *jobs, const int4 *chunks, int nchunks, cudaStream_t st) {
+  if (nchunks <= 0) return;
+  if (kind == kTcBF16) k_tc_gather<kTcBF16><<<nchunks, 256, 0, st>>>(jobs, chunks);
+  else k_tc_gather<kTcTF32><<<nchunks, 256, 0, st>>>(jobs, chunks);
+}
+void launch_tc_split_packed(int kind, const double *src, const double *sub, int64_t n, int stride, void *phi, void *plo,
+                            cudaStream_t st) {
+  if (n <= 0) return;
+  const int grid = (int)std::min<int64_t>((n + 255) / 256, 4096);
+  if (kind == kTcBF16) k_tc_split_packed<kTcBF16><<<grid, 256, 0, st>>>(src, sub, n, stride, phi, plo);
+  else k_tc_split_packed<kTcTF32><<<grid, 256, 0, st>>>(src, sub, n, stride, phi, plo);
+}
 
 int tc_stages(int npad_max) {
   const size_t stage_bytes = 2 * 128 * 128 + 2 * (size_t)npad_max * 128;

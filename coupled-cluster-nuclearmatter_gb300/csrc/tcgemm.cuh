@@ -75,4 +75,31 @@ void split_ranges(int job, int rows, int rows_pad, int tile_rows, int nk, std::v
 std::vector<int4> tc_split_chunks(const std::vector<TcSplitJob> &jobs);
 void launch_tc_split(int kind, const TcSplitJob *jobs, const int4 *chunks, int nchunks, cudaStream_t st);
 
+// Split once, place many times.  An operand whose entries are signed copies of one
+// packed vector (T' and its particle-hole rearrangement T_ph hold every packed amplitude
+// up to four times, in two tilings each) is split once into packed hi/lo arrays, and
+// each tiled operand is then filled by a gather through a per-element map parallel to
+// the tile buffer: m > 0 takes packed entry m - 1, m < 0 its negation, 0 a zero.
+//
+// Map building, once per layout: element (r, k) of a TcSplitJob-shaped region maps to
+// ind ? ind[base + r sr + k sk] : base + r sr + k sk + 1 (indices in scalar elements).
+struct TcMapJob {
+  int64_t base, sr, sk;
+  int rows, cols, tile_rows, nk, rows_pad;
+  const int32_t *ind;
+  int32_t *map;  // parallel to the tile region: element j of unit u at map[u * per16 + j]
+};
+void launch_tc_build_map(int kind, const TcMapJob *jobs, const int4 *chunks, int nchunks, cudaStream_t st);
+// the gather: unit u of job j from its map and the packed arrays of its scalar component
+struct TcGatherJob {
+  const int32_t *map;
+  const void *phi, *plo;  // packed hi / lo (BF16 or TF32 bit patterns)
+  void *hi, *lo;          // tile region
+};
+void launch_tc_gather(int kind, const TcGatherJob *jobs, const int4 *chunks, int nchunks, cudaStream_t st);
+// packed split of src - sub, n entries at a stride of `stride` doubles (the scalar
+// components of complex data are split as separate vectors by their offsets)
+void launch_tc_split_packed(int kind, const double *src, const double *sub, int64_t n, int stride, void *phi, void *plo,
+                            cudaStream_t st);
+
 }  // namespace ccx
