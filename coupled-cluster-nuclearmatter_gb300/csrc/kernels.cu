@@ -52,18 +52,31 @@ template <int NV>
 __device__ void block_partial(double (&v)[NV], double *partial) {
   __shared__ double red[NV][32];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if constexpr (NV == 32) {
+    // butterfly reduce-scatter: lane k ends with the warp total of value k (31 additions
+    // per lane instead of 5 per value)
+    warp_reduce_scatter32(v, lane);
+    red[lane][wid] = v[0];
+  } else {
 #pragma unroll
-  for (int k = 0; k < NV; ++k) {
-    double x = warp_sum(v[k]);
-    if (lane == 0) red[k][wid] = x;
+    for (int k = 0; k < NV; ++k) {
+      double x = warp_sum(v[k]);
+      if (lane == 0) red[k][wid] = x;
+    }
   }
   __syncthreads();
   if (wid == 0) {
+    if constexpr (NV == 32) {  // lane k sums value k over the warps, in warp order
+      double x = 0.0;
+      for (int w = 0; w < nw; ++w) x += red[lane][w];
+      partial[(int64_t)blockIdx.x * NV + lane] = x;
+    } else {
 #pragma unroll
-    for (int k = 0; k < NV; ++k) {
-      double x = lane < nw ? red[k][lane] : 0.0;
-      x = warp_sum(x);
-      if (lane == 0) partial[(int64_t)blockIdx.x * NV + k] = x;
+      for (int k = 0; k < NV; ++k) {
+        double x = lane < nw ? red[k][lane] : 0.0;
+        x = warp_sum(x);
+        if (lane == 0) partial[(int64_t)blockIdx.x * NV + k] = x;
+      }
     }
   }
 }
