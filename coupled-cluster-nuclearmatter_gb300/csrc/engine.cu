@@ -1526,8 +1526,7 @@ class Engine final : public IEngine {
       mj.push_back(m);
       TcGatherJob g{};
       g.map = m.map;
-      g.phi = (const char *)phi_.p + (size_t)c * n_t_ * es;
-      g.plo = (const char *)plo_.p + (size_t)c * n_t_ * es;
+      g.phl = (const char *)phl_.p + (size_t)c * n_t_ * 2 * es;
       g.hi = (char *)b.hi.p + (off + c * b.n) * es;
       g.lo = (char *)b.lo.p + (off + c * b.n) * es;
       gj.push_back(g);
@@ -1888,8 +1887,7 @@ class Engine final : public IEngine {
     std::vector<TcSplitJob> js_static, js_tphb, js_it2, js_it3;
     // dT' is split once into packed hi/lo arrays per iteration; its tiled copies (dT' as
     // A and B, dT_ph as A and B) are gathered through maps built here, once per layout
-    phi_.alloc(std::max<int64_t>(n_t_, 1) * kNComp * es, &bytes_);
-    plo_.alloc(std::max<int64_t>(n_t_, 1) * kNComp * es, &bytes_);
+    phl_.alloc(std::max<int64_t>(n_t_, 1) * kNComp * 2 * es, &bytes_);
     tphmap_.alloc(std::max<int64_t>(n_ph_, 1) * sizeof(int32_t), &bytes_);
     launch_tph_map(D_, tphmap_.as<int32_t>(), st_);
     for (auto pr : {std::make_pair(&mD_, &tD_), std::make_pair(&mDA_, &tDA_), std::make_pair(&mDphB_, &tDphB_),
@@ -2104,8 +2102,7 @@ class Engine final : public IEngine {
     // (T_ph itself is not needed in FP64 between re-bases)
     for (int c = 0; c < kNComp; ++c)
       launch_tc_split_packed(tc_kind_, (const double *)T_.p + c, (const double *)Tb_.p + c, n_t_, kNComp,
-                             (char *)phi_.p + (size_t)c * n_t_ * (tc_kind_ == kTcBF16 ? 2 : 4),
-                             (char *)plo_.p + (size_t)c * n_t_ * (tc_kind_ == kTcBF16 ? 2 : 4), st_);
+                             (char *)phl_.p + (size_t)c * n_t_ * (tc_kind_ == kTcBF16 ? 4 : 8), st_);
     launch_tc_gather(tc_kind_, (const TcGatherJob *)gplan_.jobs.p, (const int4 *)gplan_.chunks.p, gplan_.nchunks, st_);
     launches_ += kNComp + 1;
     kend();
@@ -2192,7 +2189,7 @@ class Engine final : public IEngine {
   TileBuf tVpp_, tD_, tVph_, tDphB_, tTphbA_, tDphA_, tdI4B_, tI4B_, tDA_, tI9B_, tTbA_, tdI9B_;
   TcPlan tcPP_, tcI4_, tcR1_;
   SplitPlan spStatic_, spTphb_, spIter2_, spIter3_;
-  DBuf phi_, plo_, tphmap_, mD_, mDA_, mDphB_, mDphA_;  // packed split of dT', gather maps
+  DBuf phl_, tphmap_, mD_, mDA_, mDphB_, mDphA_;  // packed split of dT' (hi/lo pairs), gather maps
   SplitPlan gplan_;                                     // gather jobs (TcGatherJob) and chunks
   double *host_res_ = nullptr;
   int host_flag_ = 0;

@@ -521,22 +521,23 @@ __global__ void __launch_bounds__(256) k_tc_build_map(const TcMapJob *__restrict
   }
 }
 
-// the hi and lo bit patterns of packed entry |m| - 1, sign flipped for m < 0
+// the hi and lo bit patterns of packed entry |m| - 1 (hi and lo interleaved in one word:
+// BF16 hi | lo << 16, TF32 hi | lo << 32), sign flipped for m < 0
 template <int KIND>
-__device__ __forceinline__ void gather_one(const void *phi, const void *plo, int32_t m, uint32_t &h, uint32_t &l) {
+__device__ __forceinline__ void gather_one(const void *phl, int32_t m, uint32_t &h, uint32_t &l) {
   if (m == 0) {
     h = l = 0;
     return;
   }
   const int64_t i = (m > 0 ? m : -m) - 1;
   if (KIND == kTcBF16) {
-    const uint32_t sg = m < 0 ? 0x8000u : 0u;
-    h = (uint32_t)((const uint16_t *)phi)[i] ^ sg;
-    l = (uint32_t)((const uint16_t *)plo)[i] ^ sg;
+    const uint32_t w = ((const uint32_t *)phl)[i] ^ (m < 0 ? 0x80008000u : 0u);
+    h = w & 0xFFFFu;
+    l = w >> 16;
   } else {
-    const uint32_t sg = m < 0 ? 0x80000000u : 0u;
-    h = ((const uint32_t *)phi)[i] ^ sg;
-    l = ((const uint32_t *)plo)[i] ^ sg;
+    const unsigned long long w = ((const unsigned long long *)phl)[i] ^ (m < 0 ? 0x8000000080000000ull : 0ull);
+    h = (uint32_t)w;
+    l = (uint32_t)(w >> 32);
   }
 }
 
@@ -559,7 +560,7 @@ __global__ void __launch_bounds__(256) k_tc_gather(const TcGatherJob *__restrict
     }
     uint32_t h[cme], l[cme];
 #pragma unroll
-    for (int j = 0; j < cme; ++j) gather_one<KIND>(J.phi, J.plo, m[j], h[j], l[j]);
+    for (int j = 0; j < cme; ++j) gather_one<KIND>(J.phl, m[j], h[j], l[j]);
     uint32_t hw[4], lw[4];
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
@@ -578,19 +579,14 @@ __global__ void __launch_bounds__(256) k_tc_gather(const TcGatherJob *__restrict
 
 template <int KIND>
 __global__ void __launch_bounds__(256) k_tc_split_packed(const double *__restrict__ src, const double *__restrict__ sub,
-                                                         int64_t n, int stride, void *phi, void *plo) {
+                                                         int64_t n, int stride, void *phl) {
   using B = BitSplit<Half<KIND>::nb>;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     uint32_t h, l;
     if (sub) B::split_diff(src[i * stride], sub[i * stride], h, l);
     else B::split(src[i * stride], h, l);
-    if (KIND == kTcBF16) {
-      ((uint16_t *)phi)[i] = (uint16_t)(h >> 16);
-      ((uint16_t *)plo)[i] = (uint16_t)(l >> 16);
-    } else {
-      ((uint32_t *)phi)[i] = h;
-      ((uint32_t *)plo)[i] = l;
-    }
+    if (KIND == kTcBF16) ((uint32_t *)phl)[i] = (h >> 16) | (l & 0xFFFF0000u);
+    else ((unsigned long long *)phl)[i] = (unsigned long long)h | ((unsigned long long)l << 32);
   }
 }
 
@@ -606,12 +602,12 @@ void launch_tc_gather(int kind, const TcGatherJob *jobs, const int4 *chunks, int
   if (kind == kTcBF16) k_tc_gather<kTcBF16><<<nchunks, 256, 0, st>>>(jobs, chunks);
   else k_tc_gather<kTcTF32><<<nchunks, 256, 0, st>>>(jobs, chunks);
 }
-void launch_tc_split_packed(int kind, const double *src, const double *sub, int64_t n, int stride, void *phi, void *plo,
+void launch_tc_split_packed(int kind, const double *src, const double *sub, int64_t n, int stride, void *phl,
                             cudaStream_t st) {
   if (n <= 0) return;
   const int grid = (int)std::min<int64_t>((n + 255) / 256, 4096);
-  if (kind == kTcBF16) k_tc_split_packed<kTcBF16><<<grid, 256, 0, st>>>(src, sub, n, stride, phi, plo);
-  else k_tc_split_packed<kTcTF32><<<grid, 256, 0, st>>>(src, sub, n, stride, phi, plo);
+  if (kind == kTcBF16) k_tc_split_packed<kTcBF16><<<grid, 256, 0, st>>>(src, sub, n, stride, phl);
+  else k_tc_split_packed<kTcTF32><<<grid, 256, 0, st>>>(src, sub, n, stride, phl);
 }
 
 int tc_stages(int npad_max) {

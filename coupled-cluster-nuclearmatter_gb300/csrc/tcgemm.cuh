@@ -93,13 +93,13 @@ void launch_tc_build_map(int kind, const TcMapJob *jobs, const int4 *chunks, int
 // the gather: unit u of job j from its map and the packed arrays of its scalar component
 struct TcGatherJob {
   const int32_t *map;
-  const void *phi, *plo;  // packed hi / lo (BF16 or TF32 bit patterns)
-  void *hi, *lo;          // tile region
+  const void *phl;  // packed hi/lo pairs: BF16 hi | lo << 16 (32 bits), TF32 hi | lo << 32 (64 bits)
+  void *hi, *lo;    // tile region
 };
 void launch_tc_gather(int kind, const TcGatherJob *jobs, const int4 *chunks, int nchunks, cudaStream_t st);
 // packed split of src - sub, n entries at a stride of `stride` doubles (the scalar
 // components of complex data are split as separate vectors by their offsets)
-void launch_tc_split_packed(int kind, const double *src, const double *sub, int64_t n, int stride, void *phi, void *plo,
+void launch_tc_split_packed(int kind, const double *src, const double *sub, int64_t n, int stride, void *phl,
                             cudaStream_t st);
 
 }  // namespace ccx
