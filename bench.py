@@ -369,8 +369,18 @@ def run_ours(args, wl):
     return 0
 
 
-# DRAM bytes per launch of the dominant kernel from an ncu capture (workload, precision, slot)
-PROFILED_TRAFFIC = {}
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from ncu
+# captures of `bench.py --steps 1 --warmup 1 --no-e2e --no-cpu-baseline` on this workload:
+# (workload, precision, kernel slot) -> bytes
+PROFILED_TRAFFIC = {
+    ("pnm66", "bf16x3", "x_fp64"): 32.0e6,
+    ("pnm66", "bf16x3", "pp_tc"): 643.7e6,
+    ("pnm66", "bf16x3", "ring_tc"): 275.5e6,
+    ("pnm66", "bf16x3", "i4_tc"): 98.8e6,
+    ("pnm66", "bf16x3", "pp_rebase_digits"): 2426.5e6,
+    ("pnm66", "bf16x3", "i4_rebase_digits"): 506.5e6,
+    ("pnm66", "bf16x3", "ring_rebase_digits"): 505.4e6,
+}
 
 
 def reference_iterations(e, ccx):
