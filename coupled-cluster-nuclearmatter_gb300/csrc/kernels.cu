@@ -388,28 +388,37 @@ void launch_xdot(const DevLayout &L, const int4 *work, int nwork, const int4 *gr
 // packed X = V_hhpp' T'; only k in {i, partner(i)} is non-zero.  The diagonal
 // becomes d2ij (ccm_t2_eqn.f90:81-84).
 // ============================================================================
+// one warp per (y, which): the lanes take the l of the sum, reduced in a fixed order
 template <typename S>
 __global__ void k_i7(DevLayout L, const S *__restrict__ X, const S *__restrict__ fdiag, const S *__restrict__ f7,
                      S *d2ij, S *i7off) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int t = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
   if (t >= 2 * L.A) return;
   const int y = t >> 1, which = t & 1;
   const int c = which ? L.partner[y] : y;
-  if (which && (c < 0 || c >= L.A)) { i7off[y] = S(0.0); return; }
-  S acc = which ? f7[y] : fdiag[y];
-  for (int l = 0; l < L.A; ++l) {
+  if (which && (c < 0 || c >= L.A)) {
+    if (lane == 0) i7off[y] = S(0.0);
+    return;
+  }
+  S acc = S(0.0);
+  for (int l = lane; l < L.A; l += 32) {
     const int2 s1 = L.hh_slot[c * L.A + l], s2 = L.hh_slot[y * L.A + l];
     if (s1.y == 0 || s2.y == 0) continue;
     const int ch = s1.x;
     acc += (ssign(s1.y) * ssign(s2.y)) * X[L.hh2_off[ch] + sidx(s1.y) + (int64_t)L.H[ch] * sidx(s2.y)];
   }
-  if (which) i7off[y] = acc;
-  else d2ij[y] = acc;
+  const S tot = from2<S>(warp_sum2(to2(acc)));
+  if (lane == 0) {
+    const S val = (which ? f7[y] : fdiag[y]) + tot;
+    if (which) i7off[y] = val;
+    else d2ij[y] = val;
+  }
 }
 template <typename S>
 void launch_i7(const DevLayout &L, const S *X, const S *fdiag, const S *f7, S *d2ij, S *i7off, cudaStream_t st) {
-  const int n = 2 * L.A;
-  k_i7<S><<<(n + 127) / 128, 128, 0, st>>>(L, X, fdiag, f7, d2ij, i7off);
+  const int64_t threads = (int64_t)2 * L.A * 32;
+  k_i7<S><<<(int)((threads + 127) / 128), 128, 0, st>>>(L, X, fdiag, f7, d2ij, i7off);
 }
 
 template <typename S>
@@ -435,10 +444,15 @@ template <typename S> void launch_i9(const DevLayout &, int64_t n, const S *Vhh,
 template <typename S>
 __global__ void k_i6_rows(DevLayout L, const int2 *__restrict__ rowtile, const S *__restrict__ T,
                           const S *__restrict__ Vhp, S *__restrict__ D) {
+  __shared__ S red[kI6Parts][kI6Rows][3];
   const int2 rt = rowtile[blockIdx.x];
-  const int ch = rt.x, rho = rt.y + threadIdx.x;
+  const int r = threadIdx.x % kI6Rows, part = threadIdx.x / kI6Rows;  // a warp: 32 rows, one part
+  const int ch = rt.x, rho = rt.y + r;
   const int P = L.P[ch];
-  if (rho >= P) return;
+  if (rho >= P) {
+    __syncthreads();  // every thread of the block reaches the barrier
+    return;
+  }
   const int H = L.H[ch], A = L.A, NP = L.NP;
   const int64_t off = L.t_off[ch];
   const int2 po = L.pp_orb[L.pp_off[ch] + rho];
@@ -458,34 +472,51 @@ __global__ void k_i6_rows(DevLayout L, const int2 *__restrict__ rowtile, const S
   }
   S d0 = S(0.0), d1 = S(0.0), d2 = S(0.0);
   const S *tc = T + off, *vc = Vhp + off;
-  for (int k = 0; k < H; ++k) {
+  for (int k = part; k < H; k += kI6Parts) {
     const int64_t o = (int64_t)P * k;
     const S t = tc[o + rho];
     d0 += t * vc[o + rho];
     if (i1 >= 0) d1 += t * vc[o + i1];
     if (i2 >= 0) d2 += t * vc[o + i2];
   }
-  S *dr = D + 3 * (off + rho);
-  dr[0] = d0;
-  dr[1] = sg1 * d1;
-  dr[2] = sg2 * d2;
+  // the kI6Parts interleaved k partials of a row, summed in part order
+  red[part][r][0] = d0;
+  red[part][r][1] = d1;
+  red[part][r][2] = d2;
+  __syncthreads();
+  if (part == 0) {
+#pragma unroll
+    for (int q = 1; q < kI6Parts; ++q) {
+      d0 += red[q][r][0];
+      d1 += red[q][r][1];
+      d2 += red[q][r][2];
+    }
+    S *dr = D + 3 * (off + rho);
+    dr[0] = d0;
+    dr[1] = sg1 * d1;
+    dr[2] = sg2 * d2;
+  }
 }
 
+// one block of kI6SumThreads per (a, c): the threads take the d of the sum, reduced in a
+// fixed order (lanes by shuffles, then the warps in order)
+constexpr int kI6SumThreads = 128;
 template <typename S>
-__global__ void k_i6_sum(DevLayout L, const S *__restrict__ D, const S *__restrict__ fdiag, const S *__restrict__ f6,
-                         S *d2ab, S *i6off) {
-  const int w = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
-  const int lane = threadIdx.x & 31;
-  if (w >= 2 * L.NP) return;
+__global__ void __launch_bounds__(kI6SumThreads) k_i6_sum(DevLayout L, const S *__restrict__ D,
+                                                          const S *__restrict__ fdiag, const S *__restrict__ f6,
+                                                          S *d2ab, S *i6off) {
+  __shared__ S red[kI6SumThreads / 32];
+  const int w = blockIdx.x;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int u = w >> 1, which = w & 1;
   const int x = L.A + u;
   const int c = which ? L.partner[x] : x;
   if (which && c < L.A) {
-    if (lane == 0) i6off[u] = S(0.0);
+    if (threadIdx.x == 0) i6off[u] = S(0.0);
     return;
   }
   S acc = S(0.0);
-  for (int d = lane; d < L.NP; d += 32) {
+  for (int d = threadIdx.x; d < L.NP; d += kI6SumThreads) {
     const int2 s = L.pp_slot[(int64_t)u * L.NP + d];
     if (s.y == 0) continue;
     const int ch = s.x, rho = sidx(s.y);
@@ -493,8 +524,12 @@ __global__ void k_i6_sum(DevLayout L, const S *__restrict__ D, const S *__restri
     if (!which) acc += dr[0];
     else acc += (L.pp_orb[L.pp_off[ch] + rho].x == x) ? dr[1] : dr[2];
   }
-  const S tot = from2<S>(warp_sum2(to2(acc)));
-  if (lane == 0) {
+  const S ws = from2<S>(warp_sum2(to2(acc)));
+  if (lane == 0) red[wid] = ws;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    S tot = red[0];
+    for (int q = 1; q < kI6SumThreads / 32; ++q) tot += red[q];
     const S val = (which ? f6[u] : fdiag[x]) - tot;
     if (which) i6off[u] = val;
     else d2ab[u] = val;
@@ -503,9 +538,8 @@ __global__ void k_i6_sum(DevLayout L, const S *__restrict__ D, const S *__restri
 template <typename S>
 void launch_i6(const DevLayout &L, const int2 *rowtile, int nrowtile, S *D, const S *T, const S *Vhp, const S *fdiag,
                const S *f6, S *d2ab, S *i6off, cudaStream_t st) {
-  if (nrowtile > 0) k_i6_rows<S><<<nrowtile, kI6Rows, 0, st>>>(L, rowtile, T, Vhp, D);
-  const int64_t threads = (int64_t)2 * L.NP * 32;
-  k_i6_sum<S><<<(int)((threads + 255) / 256), 256, 0, st>>>(L, D, fdiag, f6, d2ab, i6off);
+  if (nrowtile > 0) k_i6_rows<S><<<nrowtile, kI6Rows * kI6Parts, 0, st>>>(L, rowtile, T, Vhp, D);
+  if (L.NP > 0) k_i6_sum<S><<<2 * L.NP, kI6SumThreads, 0, st>>>(L, D, fdiag, f6, d2ab, i6off);
 }
 
 // ============================================================================

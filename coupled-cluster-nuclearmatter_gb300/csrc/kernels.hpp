@@ -70,6 +70,7 @@ template <typename S> void launch_i9(const DevLayout &L, int64_t n, const S *Vhh
 // I6 in two passes; rowtile: (channel, first packed pp row) per block of kI6Rows rows;
 // D: 3 values per packed row, at 3 * (t_off[ch] + row)
 constexpr int kI6Rows = 128;
+constexpr int kI6Parts = 4;  // threads per row: interleaved slices of the hole-pair sum
 template <typename S> void launch_i6(const DevLayout &L, const int2 *rowtile, int nrowtile, S *D, const S *T, const S *Vhp,
                                      const S *fdiag, const S *f6, S *d2ab, S *i6off, cudaStream_t st);
 template <typename S> void launch_rinit(const DevLayout &L, const S *T, const S *Vhp, const S *Rph, const S *i6off, const S *i7off, S *R, cudaStream_t st);
