@@ -394,18 +394,16 @@ int ccx_ccd_iter_batch(ccx_engine *const *engines, int32_t n, const ccx_iter_opt
       for (auto *e : act) {
         e->std_launch_residual();
         e->std_launch_update();
+        e->std_launch_dots();
       }
-      std::vector<ccx::IEngine *> next;
       for (auto *e : act) e->sync();
+      std::vector<ccx::IEngine *> next;
       for (auto *e : act)
-        if (!e->std_after_update()) next.push_back(e);
-      for (auto *e : next) e->std_launch_dots();
-      for (auto *e : next) e->sync();
-      act.clear();
-      for (auto *e : next) {
-        e->std_after_dots();
-        if (!e->std_done()) act.push_back(e);
-      }
+        if (!e->std_after_update()) {
+          e->std_after_dots();
+          if (!e->std_done()) next.push_back(e);
+        }
+      act.swap(next);
     }
     const double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     for (int32_t i = 0; i < n; ++i) {

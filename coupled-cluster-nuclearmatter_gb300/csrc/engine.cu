@@ -1223,8 +1223,11 @@ class Engine final : public IEngine {
   // or every defect_period iterations, and only an FP64 residual can end the solve.
   //
   // The loop is a state machine so that a batch of engines can run it in lockstep:
-  //   std_begin; repeat { std_launch_residual; std_launch_update; [sync]
-  //   std_after_update (true: finished); std_launch_dots; [sync] std_after_dots }.
+  //   std_begin; repeat { std_launch_residual; std_launch_update; std_launch_dots; [sync]
+  //   std_after_update (true: finished); std_after_dots }.  The DIIS Gram row needs no
+  //   host decision, so the dots are queued behind the update and one synchronisation
+  //   per iteration serves both.
+  static constexpr int kDotsAt = 16;  // host_res_ offset of the DIIS Gram row (2 doubles per entry, <= 15)
   struct StdState {
     IterOpts o;
     IterResult *r = nullptr;
@@ -1343,14 +1346,16 @@ class Engine final : public IEngine {
     for (int j = 0; j < s.nh; ++j) es[j] = hist_e_.as<S>() + (int64_t)j * n_t_;
     launch_dots<S>(n_t_, s.he, es.data(), s.nh, 1, partial_.as<double>(), res_.as<double>(), st_);
     launches_ += 2;
-    CK(cudaMemcpyAsync(host_res_, res_.p, 2 * s.nh * sizeof(double), cudaMemcpyDeviceToHost, st_));
+    // queued right behind the update, before the host has read its result: the Gram row
+    // lands in its own part of the host buffer
+    CK(cudaMemcpyAsync(host_res_ + kDotsAt, res_.p, 2 * s.nh * sizeof(double), cudaMemcpyDeviceToHost, st_));
   }
   void std_after_dots() override {
     StdState &s = ss_;
     const int m = s.m, nh = s.nh, slot = s.head;
     for (int j = 0; j < nh; ++j) {
-      s.B[slot + (size_t)m * j] = host_res_[2 * j];
-      s.B[j + (size_t)m * slot] = host_res_[2 * j];
+      s.B[slot + (size_t)m * j] = host_res_[kDotsAt + 2 * j];
+      s.B[j + (size_t)m * slot] = host_res_[kDotsAt + 2 * j];
     }
     s.head = (s.head + 1) % m;
     std::vector<double> coef;
@@ -1390,10 +1395,9 @@ class Engine final : public IEngine {
     while (!ss_.done) {
       std_launch_residual();
       std_launch_update();
+      std_launch_dots();  // needs no host decision: one synchronisation per iteration
       sync();
       if (std_after_update()) break;
-      std_launch_dots();
-      sync();
       std_after_dots();
     }
   }
