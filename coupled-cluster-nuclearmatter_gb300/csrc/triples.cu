@@ -56,9 +56,10 @@ __device__ inline S t2_at(const DevLayout &L, const S *T, int a, int b, int i, i
   return (ssign(sab.y) * ssign(sij.y)) * T[L.t_off[ch] + sidx(sab.y) + (int64_t)L.P[ch] * sidx(sij.y)];
 }
 
-// sum_d conj(<cb|V|kd>) T(ad, ij)
+// sum_d conj(<cb|V|kd>) T(ad, ij).  Not inlined: the 18 calls of a pair would otherwise
+// unroll into a body larger than the instruction cache, and the warps stall on fetches.
 template <typename S>
-__device__ S one_particle(const TriplesDev &D, const DevLayout &L, const S *T, const S *V5, int a, int b, int c, int i,
+__device__ __noinline__ S one_particle(const TriplesDev &D, const DevLayout &L, const S *T, const S *V5, int a, int b, int c, int i,
                           int j, int k) {
   const int nxd = D.nx[i] + D.nx[j] - D.nx[a], nyd = D.ny[i] + D.ny[j] - D.ny[a];
   const int nzd = D.nz[i] + D.nz[j] - D.nz[a], tzd = D.tz[i] + D.tz[j] - D.tz[a];
@@ -77,9 +78,9 @@ __device__ S one_particle(const TriplesDev &D, const DevLayout &L, const S *T, c
   return sum;
 }
 
-// sum_l conj(<jk|V|lc>) T(ab, il)
+// sum_l conj(<jk|V|lc>) T(ab, il) (not inlined, as one_particle)
 template <typename S>
-__device__ S one_hole(const TriplesDev &D, const DevLayout &L, const S *T, const S *V2, int a, int b, int c, int i, int j,
+__device__ __noinline__ S one_hole(const TriplesDev &D, const DevLayout &L, const S *T, const S *V2, int a, int b, int c, int i, int j,
                       int k) {
   const int nxl = D.nx[k] + D.nx[j] - D.nx[c], nyl = D.ny[k] + D.ny[j] - D.ny[c];
   const int nzl = D.nz[k] + D.nz[j] - D.nz[c], tzl = D.tz[k] + D.tz[j] - D.tz[c];
