@@ -6,7 +6,11 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
+#include <cmath>
 #include <stdexcept>
+#include <thread>
+#include <utility>
 #include <vector>
 
 #include "common.cuh"
@@ -359,35 +363,82 @@ class Triples final : public ITriples<S> {
         for (int c = b + 1; c < A; ++c)
           hhh[key(B.tz[a] + B.tz[b] + B.tz[c], B.nx[a] + B.nx[b] + B.nx[c], B.ny[a] + B.ny[b] + B.ny[c],
                   B.nz[a] + B.nz[b] + B.nz[c])].push_back(make_int3(a, b, c));
-    std::vector<std::vector<int3>> ppp(nkeys);
-    for (int a = A; a < ns; ++a)
-      for (int b = a + 1; b < ns; ++b) {
-        const int t2 = B.tz[a] + B.tz[b], x2 = B.nx[a] + B.nx[b], y2 = B.ny[a] + B.ny[b], z2 = B.nz[a] + B.nz[b];
-        for (int c = b + 1; c < ns; ++c) {
-          const size_t k = key(t2 + B.tz[c], x2 + B.nx[c], y2 + B.ny[c], z2 + B.nz[c]);
-          if (!hhh[k].empty()) ppp[k].push_back(make_int3(a, b, c));
+    // particle triples a < b < c of every key that has hole triples, enumerated by host
+    // threads over slices of the a range in two passes (count, then fill), laid out key
+    // by key in ascending key order and, within a key, in the serial (a, b, c) order
+    std::vector<int> live(nkeys, -1);
+    int nlive = 0;
+    for (size_t k = 0; k < nkeys; ++k)
+      if (!hhh[k].empty()) live[k] = nlive++;
+    const int nthr = std::max(1, std::min<int>(64, (int)std::thread::hardware_concurrency()));
+    const int nsl = std::max(1, std::min(ns - A, 4 * nthr));
+    auto bound = [&](int q) {  // slices of about equal work: a costs about (ns - a)^2 / 2
+      if (q >= nsl) return ns;
+      return A + (int)std::lround((1.0 - std::cbrt(1.0 - (double)q / nsl)) * (ns - A));
+    };
+    auto sweep = [&](int sl, auto &&emit) {
+      for (int a = bound(sl); a < bound(sl + 1); ++a)
+        for (int b = a + 1; b < ns; ++b) {
+          const int t2 = B.tz[a] + B.tz[b], x2 = B.nx[a] + B.nx[b], y2 = B.ny[a] + B.ny[b], z2 = B.nz[a] + B.nz[b];
+          for (int c = b + 1; c < ns; ++c) {
+            const int id = live[key(t2 + B.tz[c], x2 + B.nx[c], y2 + B.ny[c], z2 + B.nz[c])];
+            if (id >= 0) emit(id, a, b, c);
+          }
         }
+    };
+    auto parallel = [&](auto &&fn) {
+      std::atomic<int> next{0};
+      auto loop = [&]() {
+        for (int sl = next++; sl < nsl; sl = next++) fn(sl);
+      };
+      std::vector<std::thread> pool;
+      for (int t = 1; t < nthr; ++t) pool.emplace_back(loop);
+      loop();
+      for (auto &t : pool) t.join();
+    };
+    std::vector<int64_t> cnt((size_t)nsl * nlive, 0);
+    parallel([&](int sl) {
+      int64_t *c = &cnt[(size_t)sl * nlive];
+      sweep(sl, [&](int id, int, int, int) { ++c[id]; });
+    });
+    std::vector<int64_t> kcount(nlive, 0), kstart(nlive + 1, 0);
+    for (int sl = 0; sl < nsl; ++sl)
+      for (int id = 0; id < nlive; ++id) kcount[id] += cnt[(size_t)sl * nlive + id];
+    for (int id = 0; id < nlive; ++id) kstart[id + 1] = kstart[id] + kcount[id];
+    // cnt becomes each slice's write position per key
+    for (int id = 0; id < nlive; ++id) {
+      int64_t pos = kstart[id];
+      for (int sl = 0; sl < nsl; ++sl) {
+        const int64_t n = cnt[(size_t)sl * nlive + id];
+        cnt[(size_t)sl * nlive + id] = pos;
+        pos += n;
       }
+    }
+    std::vector<int3> pflat(kstart[nlive]);
+    parallel([&](int sl) {
+      int64_t *w = &cnt[(size_t)sl * nlive];
+      sweep(sl, [&](int id, int a, int b, int c) { pflat[w[id]++] = make_int3(a, b, c); });
+    });
     std::vector<int64_t> eoff(1, 0), hoff, poff;
     std::vector<int> nbra;
-    std::vector<int3> hl, pl;
+    std::vector<int3> hl;
     for (int t = tlo; t <= thi; t += 2)
       for (int x = lo[0]; x <= hi[0]; ++x)
         for (int y = lo[1]; y <= hi[1]; ++y)
           for (int z = lo[2]; z <= hi[2]; ++z) {
             const size_t k = key(t, x, y, z);
-            if (hhh[k].empty() || ppp[k].empty()) continue;
+            if (live[k] < 0 || kcount[live[k]] == 0) continue;
+            const int id = live[k];
             hoff.push_back((int64_t)hl.size());
-            poff.push_back((int64_t)pl.size());
+            poff.push_back(kstart[id]);  // the key's particle triples, in place in pflat
             nbra.push_back((int)hhh[k].size());
             hl.insert(hl.end(), hhh[k].begin(), hhh[k].end());
-            pl.insert(pl.end(), ppp[k].begin(), ppp[k].end());
-            eoff.push_back(eoff.back() + (int64_t)hhh[k].size() * ppp[k].size());
+            eoff.push_back(eoff.back() + (int64_t)hhh[k].size() * kcount[id]);
           }
     TD_.nt3 = (int)nbra.size();
     total_ = eoff.back();
     eoff.push_back(eoff.back());  // sentinel so the channel walk never reads past the end
-    elem_off_.put(eoff); nbra_.put(nbra); hhh_off_.put(hoff); ppp_off_.put(poff); hhh_.put(hl); ppp_.put(pl);
+    elem_off_.put(eoff); nbra_.put(nbra); hhh_off_.put(hoff); ppp_off_.put(poff); hhh_.put(hl); ppp_.put(pflat);
     TD_.elem_off = elem_off_.as<int64_t>(); TD_.nbra = nbra_.as<int>();
     TD_.hhh_off = hhh_off_.as<int64_t>(); TD_.ppp_off = ppp_off_.as<int64_t>();
     TD_.hhh = hhh_.as<int3>(); TD_.ppp = ppp_.as<int3>();
