@@ -51,56 +51,67 @@ __device__ inline int t_orbitof(const TriplesDev &D, int x, int y, int z, int s,
   return D.orbit_of[idx];
 }
 
+constexpr unsigned long long kSignBit = 0x8000000000000000ull;
+// x with its sign bits flipped where m has them: a sign change on the integer pipe
+__device__ __forceinline__ double flip(double x, unsigned long long m) {
+  return __longlong_as_double((long long)((unsigned long long)__double_as_longlong(x) ^ m));
+}
+__device__ __forceinline__ cplx flip(cplx x, unsigned long long m) { return cplx(flip(x.re, m), flip(x.im, m)); }
+
+// T(ab, ij) with the antisymmetry signs of both pair slots, and the extra sign m
 template <typename S>
-__device__ inline S t2_at(const DevLayout &L, const S *T, int a, int b, int i, int j) {
+__device__ inline S t2_at(const DevLayout &L, const S *T, int a, int b, int i, int j, unsigned long long m) {
   const int2 sab = L.pp_slot[(int64_t)(a - L.A) * L.NP + (b - L.A)];
   const int2 sij = L.hh_slot[i * L.A + j];
   if (sab.y == 0 || sij.y == 0) return S(0.0);
   const int ch = sab.x;
-  return (ssign(sab.y) * ssign(sij.y)) * T[L.t_off[ch] + sidx(sab.y) + (int64_t)L.P[ch] * sidx(sij.y)];
+  if ((sab.y < 0) != (sij.y < 0)) m ^= kSignBit;
+  return flip(T[L.t_off[ch] + sidx(sab.y) + (int64_t)L.P[ch] * sidx(sij.y)], m);
 }
+__device__ __forceinline__ double madd_conj(double v, double t, double acc) { return fma(v, t, acc); }
+__device__ __forceinline__ cplx madd_conj(cplx v, cplx t, cplx acc) { return acc + conj_(v) * t; }
 
 // sum_d conj(<cb|V|kd>) T(ad, ij).  Not inlined: the 18 calls of a pair would otherwise
 // unroll into a body larger than the instruction cache, and the warps stall on fetches.
+// acc + sign * sum_d conj(<cb|V|kd>) T(ad, ij), the sign as a mask of sign bits
 template <typename S>
-__device__ __noinline__ S one_particle(const TriplesDev &D, const DevLayout &L, const S *T, const S *V5, int a, int b, int c, int i,
-                          int j, int k) {
+__device__ __noinline__ S one_particle(const TriplesDev &D, const DevLayout &L, const S *T, const S *V5, int a, int b,
+                                       int c, int i, int j, int k, unsigned long long m, S acc) {
   const int nxd = D.nx[i] + D.nx[j] - D.nx[a], nyd = D.ny[i] + D.ny[j] - D.ny[a];
   const int nzd = D.nz[i] + D.nz[j] - D.nz[a], tzd = D.tz[i] + D.tz[j] - D.tz[a];
-  S sum = S(0.0);
-  if (abs(nxd) > D.nk0 || abs(nyd) > D.nk1 || abs(nzd) > D.nk2 || abs(tzd) > 1) return sum;
+  if (abs(nxd) > D.nk0 || abs(nyd) > D.nk1 || abs(nzd) > D.nk2 || abs(tzd) > 1) return acc;
+  const int2 cl = D.pp5_slot[(int64_t)(c - D.A) * D.NP + (b - D.A)];
+  if (cl.x < 0) return acc;
   for (int sd = -1; sd <= 1; sd += 2) {
     const int d = t_orbitof(D, nxd, nyd, nzd, sd, tzd);
     if (d < D.A) continue;
-    const S t = t2_at<S>(L, T, a, d, i, j);
     const int2 r = D.hp5_slot[(int64_t)k * D.NP + (d - D.A)];
-    const int2 cl = D.pp5_slot[(int64_t)(c - D.A) * D.NP + (b - D.A)];
-    if (r.x < 0 || cl.x < 0) continue;
-    const S v = V5[D.v5_off[r.x] + r.y + (int64_t)D.n5[r.x] * cl.y];
-    sum += conj_(v) * t;
+    if (r.x < 0) continue;
+    const S t = t2_at<S>(L, T, a, d, i, j, m);
+    acc = madd_conj(V5[D.v5_off[r.x] + r.y + (int64_t)D.n5[r.x] * cl.y], t, acc);
   }
-  return sum;
+  return acc;
 }
 
 // sum_l conj(<jk|V|lc>) T(ab, il) (not inlined, as one_particle)
+// acc + sign * sum_l conj(<jk|V|lc>) T(ab, il)
 template <typename S>
-__device__ __noinline__ S one_hole(const TriplesDev &D, const DevLayout &L, const S *T, const S *V2, int a, int b, int c, int i, int j,
-                      int k) {
+__device__ __noinline__ S one_hole(const TriplesDev &D, const DevLayout &L, const S *T, const S *V2, int a, int b,
+                                   int c, int i, int j, int k, unsigned long long m, S acc) {
   const int nxl = D.nx[k] + D.nx[j] - D.nx[c], nyl = D.ny[k] + D.ny[j] - D.ny[c];
   const int nzl = D.nz[k] + D.nz[j] - D.nz[c], tzl = D.tz[k] + D.tz[j] - D.tz[c];
-  S sum = S(0.0);
-  if (abs(nxl) > D.nk0 || abs(nyl) > D.nk1 || abs(nzl) > D.nk2 || abs(tzl) > 1) return sum;
+  if (abs(nxl) > D.nk0 || abs(nyl) > D.nk1 || abs(nzl) > D.nk2 || abs(tzl) > 1) return acc;
+  const int2 r = D.hh2_slot[j * D.A + k];
+  if (r.x < 0) return acc;
   for (int sl = -1; sl <= 1; sl += 2) {
     const int l = t_orbitof(D, nxl, nyl, nzl, sl, tzl);
     if (l < 0 || l >= D.A) continue;
-    const S t = t2_at<S>(L, T, a, b, i, l);
-    const int2 r = D.hh2_slot[j * D.A + k];
     const int2 cl = D.hp2_slot[(int64_t)l * D.NP + (c - D.A)];
-    if (r.x < 0 || cl.x < 0) continue;
-    const S v = V2[D.v2_off[r.x] + r.y + (int64_t)D.n2[r.x] * cl.y];
-    sum += conj_(v) * t;
+    if (cl.x < 0) continue;
+    const S t = t2_at<S>(L, T, a, b, i, l, m);
+    acc = madd_conj(V2[D.v2_off[r.x] + r.y + (int64_t)D.n2[r.x] * cl.y], t, acc);
   }
-  return sum;
+  return acc;
 }
 
 template <int NV>
@@ -120,10 +131,20 @@ __device__ void block_sum(double (&v)[NV], double *partial) {
     }
 }
 
+// Fock sums of every hole triple (f_ii + f_jj + f_kk) and particle triple, once per (T)
+template <typename S>
+__global__ void k_triple_fock(const int3 *__restrict__ t, int64_t n, const S *__restrict__ fd, S *__restrict__ e) {
+  for (int64_t x = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; x < n; x += (int64_t)gridDim.x * blockDim.x) {
+    const int3 q = t[x];
+    e[x] = fd[q.x] + fd[q.y] + fd[q.z];
+  }
+}
+
 template <typename S>
 __global__ void __launch_bounds__(256) k_triples(TriplesDev D, DevLayout L, const S *__restrict__ T,
                                                  const S *__restrict__ V5, const S *__restrict__ V2,
-                                                 const S *__restrict__ fd, int64_t total, double *partial) {
+                                                 const S *__restrict__ eh, const S *__restrict__ ep, int64_t total,
+                                                 double *partial) {
   double acc[2] = {0.0, 0.0};
   int ch = 0;
   for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < total; g += (int64_t)gridDim.x * blockDim.x) {
@@ -134,18 +155,29 @@ __global__ void __launch_bounds__(256) k_triples(TriplesDev D, DevLayout L, cons
     const int3 abc = D.ppp[D.ppp_off[ch] + ket];
     const int3 ijk = D.hhh[D.hhh_off[ch] + bra];
     const int a = abc.x, b = abc.y, c = abc.z, i = ijk.x, j = ijk.y, k = ijk.z;
-    const S spen = fd[i] + fd[j] + fd[k] - fd[a] - fd[b] - fd[c];
-    S tc = one_particle<S>(D, L, T, V5, a, b, c, i, j, k) - one_particle<S>(D, L, T, V5, b, a, c, i, j, k) -
-           one_particle<S>(D, L, T, V5, c, b, a, i, j, k) - one_particle<S>(D, L, T, V5, a, b, c, k, j, i) -
-           one_particle<S>(D, L, T, V5, a, b, c, i, k, j) + one_particle<S>(D, L, T, V5, c, b, a, i, k, j) +
-           one_particle<S>(D, L, T, V5, c, b, a, k, j, i) + one_particle<S>(D, L, T, V5, b, a, c, i, k, j) +
-           one_particle<S>(D, L, T, V5, b, a, c, k, j, i);
-    const S th = one_hole<S>(D, L, T, V2, a, b, c, i, j, k) - one_hole<S>(D, L, T, V2, a, c, b, i, j, k) -
-                 one_hole<S>(D, L, T, V2, c, b, a, i, j, k) - one_hole<S>(D, L, T, V2, a, b, c, k, j, i) -
-                 one_hole<S>(D, L, T, V2, a, b, c, j, i, k) + one_hole<S>(D, L, T, V2, c, b, a, j, i, k) +
-                 one_hole<S>(D, L, T, V2, c, b, a, k, j, i) + one_hole<S>(D, L, T, V2, a, c, b, j, i, k) +
-                 one_hole<S>(D, L, T, V2, a, c, b, k, j, i);
-    tc = tc - th;
+    const S spen = eh[D.hhh_off[ch] + bra] - ep[D.ppp_off[ch] + ket];
+    // W = the 9 particle terms minus the 9 hole terms, accumulated in one sum with the
+    // permutation signs applied as sign-bit flips
+    constexpr unsigned long long P = 0, N = kSignBit;
+    S tc = S(0.0);
+    tc = one_particle<S>(D, L, T, V5, a, b, c, i, j, k, P, tc);
+    tc = one_particle<S>(D, L, T, V5, b, a, c, i, j, k, N, tc);
+    tc = one_particle<S>(D, L, T, V5, c, b, a, i, j, k, N, tc);
+    tc = one_particle<S>(D, L, T, V5, a, b, c, k, j, i, N, tc);
+    tc = one_particle<S>(D, L, T, V5, a, b, c, i, k, j, N, tc);
+    tc = one_particle<S>(D, L, T, V5, c, b, a, i, k, j, P, tc);
+    tc = one_particle<S>(D, L, T, V5, c, b, a, k, j, i, P, tc);
+    tc = one_particle<S>(D, L, T, V5, b, a, c, i, k, j, P, tc);
+    tc = one_particle<S>(D, L, T, V5, b, a, c, k, j, i, P, tc);
+    tc = one_hole<S>(D, L, T, V2, a, b, c, i, j, k, N, tc);
+    tc = one_hole<S>(D, L, T, V2, a, c, b, i, j, k, P, tc);
+    tc = one_hole<S>(D, L, T, V2, c, b, a, i, j, k, P, tc);
+    tc = one_hole<S>(D, L, T, V2, a, b, c, k, j, i, P, tc);
+    tc = one_hole<S>(D, L, T, V2, a, b, c, j, i, k, P, tc);
+    tc = one_hole<S>(D, L, T, V2, c, b, a, j, i, k, N, tc);
+    tc = one_hole<S>(D, L, T, V2, c, b, a, k, j, i, N, tc);
+    tc = one_hole<S>(D, L, T, V2, a, c, b, j, i, k, N, tc);
+    tc = one_hole<S>(D, L, T, V2, a, c, b, k, j, i, N, tc);
     const S term = (conj_(tc) * tc) / spen;
     acc[0] += real_(term);
     acc[1] += imag_(term);
@@ -306,9 +338,12 @@ class Triples final : public ITriples<S> {
   void energy(const S *T, const S *fdiag, double et[2], cudaStream_t st) override {
     if (!has_v()) throw EngineError(4, "(T): V_hppp and V_hhhp blocks are not set");
     if (total_ > 0) {
-      k_triples<S><<<kBlocks, 256, 0, st>>>(TD_, D_, T, V5_.as<S>(), V2_.as<S>(), fdiag, total_, partial_.as<double>());
+      k_triple_fock<S><<<1024, 256, 0, st>>>(hhh_.as<int3>(), n_hhh_, fdiag, eh_.as<S>());
+      k_triple_fock<S><<<1024, 256, 0, st>>>(ppp_.as<int3>(), n_ppp_, fdiag, ep_.as<S>());
+      k_triples<S><<<kBlocks, 256, 0, st>>>(TD_, D_, T, V5_.as<S>(), V2_.as<S>(), eh_.as<S>(), ep_.as<S>(), total_,
+                                            partial_.as<double>());
       k_finish2<<<2, 256, 0, st>>>(partial_.as<double>(), kBlocks, res_.as<double>());
-      launches_ += 2;
+      launches_ += 4;
       tck(cudaGetLastError(), "(T) kernel");
       double h[2];
       tck(cudaMemcpyAsync(h, res_.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, st), "(T) result");
@@ -439,6 +474,10 @@ class Triples final : public ITriples<S> {
     total_ = eoff.back();
     eoff.push_back(eoff.back());  // sentinel so the channel walk never reads past the end
     elem_off_.put(eoff); nbra_.put(nbra); hhh_off_.put(hoff); ppp_off_.put(poff); hhh_.put(hl); ppp_.put(pflat);
+    n_hhh_ = (int64_t)hl.size();
+    n_ppp_ = (int64_t)pflat.size();
+    eh_.zeros((size_t)std::max<int64_t>(n_hhh_, 1) * sizeof(S));
+    ep_.zeros((size_t)std::max<int64_t>(n_ppp_, 1) * sizeof(S));
     TD_.elem_off = elem_off_.as<int64_t>(); TD_.nbra = nbra_.as<int>();
     TD_.hhh_off = hhh_off_.as<int64_t>(); TD_.ppp_off = ppp_off_.as<int64_t>();
     TD_.hhh = hhh_.as<int3>(); TD_.ppp = ppp_.as<int3>();
@@ -449,7 +488,8 @@ class Triples final : public ITriples<S> {
   TriplesDev TD_{};
   DB orbit_of_, hp5_slot_, pp5_slot_, hh2_slot_, hp2_slot_, v5_off_, n5_, v2_off_, n2_;
   DB rows5_, cols5_, rows2_, cols2_, nc5_, ro5_, co5_, nc2_, ro2_, co2_;
-  DB V5_, V2_, elem_off_, nbra_, hhh_off_, ppp_off_, hhh_, ppp_, partial_, res_;
+  DB V5_, V2_, elem_off_, nbra_, hhh_off_, ppp_off_, hhh_, ppp_, partial_, res_, eh_, ep_;
+  int64_t n_hhh_ = 0, n_ppp_ = 0;
   std::vector<int64_t> off5_h_, off2_h_;
   std::vector<int> nr5_h_, nc5_h_, nr2_h_, nc2_h_;
   int64_t n_v5_ = 0, n_v2_ = 0, total_ = 0, launches_ = 0;
