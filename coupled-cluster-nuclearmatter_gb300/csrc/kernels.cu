@@ -632,16 +632,26 @@ __global__ void k_update(DevLayout L, int mode, S *__restrict__ T, const S *__re
     const int2 ho = L.hh_orb[L.hh_off[ch] + ij];
     const S D = ((d2ij[ho.x] + d2ij[ho.y]) - d2ab[po.x - A]) - d2ab[po.y - A];
     const S r = R[g];
-    v[2] += abs2(r - D * t);
+    const S q = r - D * t;  // the Jacobi step times D
+    v[2] += abs2(q);
     S tn = t;
     if (mode == 0) {
       tn = 0.75 * t + 0.25 * (r / D);
       T[g] = tn;
       hist_t[g] = tn;
     } else if (mode == 1) {
-      const S tj = r / D;
-      hist_t[g] = tj;
-      hist_e[g] = tj - t;
+      if constexpr (ScalarOf<S>::complex) {
+        const S tj = r / D;
+        hist_t[g] = tj;
+        hist_e[g] = tj - t;
+      } else {
+        // the step q / D to FP32 accuracy (an FP64 division is a long sequence on this
+        // GPU's narrow FP64 pipe); t + step keeps the fixed point exact, since the step
+        // vanishes with the residual
+        const S step = (S)__fdiv_rn(__double2float_rn(q), __double2float_rn(D));
+        hist_t[g] = t + step;
+        hist_e[g] = step;
+      }
     }
     const S pr = tn * vij;
     v[0] += real_(pr);
