@@ -156,6 +156,8 @@ void draw_lecs(uint64_t seed, double out[9]) {
 
 template <typename S>
 class Engine final : public IEngine {
+  using E = typename StepOf<S>::type;  // DIIS step vectors of the standard mode
+
  public:
   Engine(std::shared_ptr<const Layout> L, int device) : L_(std::move(L)) {
     int ndev = 0;
@@ -1235,7 +1237,8 @@ class Engine final : public IEngine {
     int m = 8, nh = 0, head = 0, it = 0, stall = 0, since = 0;
     double e[2] = {0, 0}, phase_r0 = -1.0, best = 1e300;
     std::vector<double> B;
-    S *ht = nullptr, *he = nullptr;
+    S *ht = nullptr;
+    E *he = nullptr;
   };
   StdState ss_;
   static constexpr double kRebaseDrop = 1e-4;
@@ -1262,7 +1265,7 @@ class Engine final : public IEngine {
     }
     s.m = std::max(2, std::min(o.diis_dim, 15));
     hist_t_.alloc((size_t)s.m * n_t_ * sizeof(S), &bytes_);
-    hist_e_.alloc((size_t)s.m * n_t_ * sizeof(S), &bytes_);
+    hist_e_.alloc((size_t)s.m * n_t_ * sizeof(E), &bytes_);
     s.B.assign((size_t)s.m * s.m, 0.0);
     s.e[0] = r.e_mbpt2[0];
     s.e[1] = r.e_mbpt2[1];
@@ -1285,7 +1288,7 @@ class Engine final : public IEngine {
   void std_launch_update() override {
     StdState &s = ss_;
     s.ht = hist_t_.as<S>() + (int64_t)s.head * n_t_;
-    s.he = hist_e_.as<S>() + (int64_t)s.head * n_t_;
+    s.he = hist_e_.as<E>() + (int64_t)s.head * n_t_;
     mark(7);
     launch_update<S>(D_, 1, T_.as<S>(), R_.as<S>(), Vhp_.as<S>(), d2ij_.as<S>(), d2ab_.as<S>(), s.ht, s.he,
                      partial_.as<double>(), res_.as<double>(), st_);
@@ -1342,9 +1345,12 @@ class Engine final : public IEngine {
   void std_launch_dots() override {
     StdState &s = ss_;
     if (s.nh < s.m) ++s.nh;
-    std::vector<const S *> es(s.nh);
-    for (int j = 0; j < s.nh; ++j) es[j] = hist_e_.as<S>() + (int64_t)j * n_t_;
-    launch_dots<S>(n_t_, s.he, es.data(), s.nh, 1, partial_.as<double>(), res_.as<double>(), st_);
+    std::vector<const E *> es(s.nh);
+    for (int j = 0; j < s.nh; ++j) es[j] = hist_e_.as<E>() + (int64_t)j * n_t_;
+    if constexpr (ScalarOf<S>::complex)
+      launch_dots<S>(n_t_, s.he, es.data(), s.nh, 1, partial_.as<double>(), res_.as<double>(), st_);
+    else
+      launch_dots_f32(n_t_, s.he, es.data(), s.nh, partial_.as<double>(), res_.as<double>(), st_);
     launches_ += 2;
     // queued right behind the update, before the host has read its result: the Gram row
     // lands in its own part of the host buffer

@@ -609,7 +609,7 @@ void launch_rinit(const DevLayout &L, const S *T, const S *Vhp, const S *Rph, co
 template <typename S>
 __global__ void k_update(DevLayout L, int mode, S *__restrict__ T, const S *__restrict__ R, const S *__restrict__ Vhp,
                          const S *__restrict__ d2ij, const S *__restrict__ d2ab, S *__restrict__ hist_t,
-                         S *__restrict__ hist_e, double *partial) {
+                         typename StepOf<S>::type *__restrict__ hist_e, double *partial) {
   const int2 tl = L.ttile[blockIdx.x];
   const int ch = tl.x;
   const int P = L.P[ch], H = L.H[ch];
@@ -648,8 +648,8 @@ __global__ void k_update(DevLayout L, int mode, S *__restrict__ T, const S *__re
         // the step q / D to FP32 accuracy (an FP64 division is a long sequence on this
         // GPU's narrow FP64 pipe); t + step keeps the fixed point exact, since the step
         // vanishes with the residual
-        const S step = (S)__fdiv_rn(__double2float_rn(q), __double2float_rn(D));
-        hist_t[g] = t + step;
+        const float step = __fdiv_rn(__double2float_rn(q), __double2float_rn(D));
+        hist_t[g] = t + (S)step;
         hist_e[g] = step;
       }
     }
@@ -661,7 +661,7 @@ __global__ void k_update(DevLayout L, int mode, S *__restrict__ T, const S *__re
 }
 template <typename S>
 void launch_update(const DevLayout &L, int mode, S *T, const S *R, const S *Vhp, const S *d2ij, const S *d2ab, S *hist_t,
-                   S *hist_e, double *partial, double *out4, cudaStream_t st) {
+                   typename StepOf<S>::type *hist_e, double *partial, double *out4, cudaStream_t st) {
   if (!L.nttile) return;
   k_update<S><<<L.nttile, 256, 0, st>>>(L, mode, T, R, Vhp, d2ij, d2ab, hist_t, hist_e, partial);
   finish(partial, L.nttile, 3, out4, st);
@@ -704,6 +704,33 @@ void launch_dots(int64_t n, const S *a, const S *const *bs, int nb, int conj_a, 
   for (int k = 0; k < nb && k < kMaxDots; ++k) pk.p[k] = bs[k];
   const int blocks = 608;
   k_dots<S><<<blocks, 256, 0, st>>>(n, a, pk, nb, conj_a, partial);
+  finish(partial, blocks, 2 * kMaxDots, out, st);
+}
+
+__global__ void k_dots_f32(int64_t n, const float *__restrict__ a, PtrPack<float> bs, int nb, double *partial) {
+  float f[kMaxDots];
+#pragma unroll
+  for (int k = 0; k < kMaxDots; ++k) f[k] = 0.0f;
+  for (int64_t x = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; x < n; x += (int64_t)gridDim.x * blockDim.x) {
+    const float av = a[x];
+#pragma unroll
+    for (int k = 0; k < kMaxDots; ++k)
+      if (k < nb) f[k] = fmaf(av, bs.p[k][x], f[k]);
+  }
+  double v[2 * kMaxDots];
+#pragma unroll
+  for (int k = 0; k < kMaxDots; ++k) {
+    v[2 * k] = (double)f[k];
+    v[2 * k + 1] = 0.0;
+  }
+  block_partial<2 * kMaxDots>(v, partial);
+}
+void launch_dots_f32(int64_t n, const float *a, const float *const *bs, int nb, double *partial, double *out,
+                     cudaStream_t st) {
+  PtrPack<float> pk{};
+  for (int k = 0; k < nb && k < kMaxDots; ++k) pk.p[k] = bs[k];
+  const int blocks = 608;
+  k_dots_f32<<<blocks, 256, 0, st>>>(n, a, pk, nb, partial);
   finish(partial, blocks, 2 * kMaxDots, out, st);
 }
 
@@ -1173,7 +1200,8 @@ void launch_unpack_t(const DevLayout &L, int ch, int n_pp, const int *pp_signed,
                              S *, S *, cudaStream_t);                                                                  \
   template void launch_rinit<S>(const DevLayout &, const S *, const S *, const S *, const S *, const S *, S *,         \
                                 cudaStream_t);                                                                         \
-  template void launch_update<S>(const DevLayout &, int, S *, const S *, const S *, const S *, const S *, S *, S *,    \
+  template void launch_update<S>(const DevLayout &, int, S *, const S *, const S *, const S *, const S *, S *,         \
+                                 typename StepOf<S>::type *,                                                            \
                                  double *, double *, cudaStream_t);                                                    \
   template void launch_dots<S>(int64_t, const S *, const S *const *, int, int, double *, double *, cudaStream_t);     \
   template void launch_diis_gram<S>(int64_t, const S *const *, int, double *, double *, cudaStream_t);                \

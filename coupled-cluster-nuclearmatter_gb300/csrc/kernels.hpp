@@ -79,12 +79,19 @@ template <typename S> void launch_rinit(const DevLayout &L, const S *T, const S 
 // mode 0: reference update T <- 0.75 T + 0.25 R/D, history column written
 // mode 1: Jacobi T_jac = R/D into hist_t, step into hist_e, T untouched
 // mode 2: energy only (no update); mode 3: residual norm + energy, no update
+// the DIIS step vectors of the standard mode: FP32 for real engines (the step is computed
+// to FP32 accuracy), S for complex ones
+template <typename S> struct StepOf { using type = S; };
+template <> struct StepOf<double> { using type = float; };
 template <typename S>
 void launch_update(const DevLayout &L, int mode, S *T, const S *R, const S *Vhp, const S *d2ij, const S *d2ab,
-                   S *hist_t, S *hist_e, double *partial, double *out4, cudaStream_t st);
+                   S *hist_t, typename StepOf<S>::type *hist_e, double *partial, double *out4, cudaStream_t st);
 // dot products: out[j] = sum_x w(a[x]) * b_j[x] for j < nb; conj on a when conj_a
 template <typename S>
 void launch_dots(int64_t n, const S *a, const S *const *bs, int nb, int conj_a, double *partial, double *out, cudaStream_t st);
+// the same over FP32 step vectors: FP32 products and per-thread sums, FP64 across threads
+void launch_dots_f32(int64_t n, const float *a, const float *const *bs, int nb, double *partial, double *out,
+                     cudaStream_t st);
 // reference DIIS Gram matrix of differences of nstep history columns (no conjugation)
 template <typename S>
 void launch_diis_gram(int64_t n, const S *const *cols, int nstep, double *partial, double *out, cudaStream_t st);
