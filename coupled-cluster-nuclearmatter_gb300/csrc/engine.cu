@@ -170,6 +170,11 @@ class Engine final : public IEngine {
     for (auto &e : kev_) CK(cudaEventCreate(&e));
     build_tables();
     alloc_state();
+    // where each packed amplitude's one-body and ring terms come from (layout only)
+    omap_.alloc(std::max<int64_t>(n_t_, 1) * sizeof(int4), &bytes_);
+    rmap_.alloc(std::max<int64_t>(n_t_, 1) * sizeof(int4), &bytes_);
+    launch_rinit_maps(D_, omap_.as<int4>(), rmap_.as<int4>(), st_);
+    CK(cudaStreamSynchronize(st_));
   }
   ~Engine() override {
     cudaSetDevice(device_);
@@ -1092,7 +1097,8 @@ class Engine final : public IEngine {
     run_plan(planRing_);
     kend();
     mark(5);
-    launch_rinit<S>(D_, T_.as<S>(), Vhp_.as<S>(), Rph_.as<S>(), i6off_.as<S>(), i7off_.as<S>(), R_.as<S>(), st_);
+    launch_rinit<S>(D_, omap_.as<int4>(), rmap_.as<int4>(), T_.as<S>(), Vhp_.as<S>(), Rph_.as<S>(), i6off_.as<S>(),
+                    i7off_.as<S>(), R_.as<S>(), st_);
     mark(6);
     kbegin(kKLadder);
     run_plan(planLadder_);
@@ -2070,7 +2076,8 @@ class Engine final : public IEngine {
       kend();
     }
     mark(5);
-    launch_rinit<S>(D_, T_.as<S>(), Vhp_.as<S>(), Rph_.as<S>(), i6off_.as<S>(), i7off_.as<S>(), R_.as<S>(), st_);
+    launch_rinit<S>(D_, omap_.as<int4>(), rmap_.as<int4>(), T_.as<S>(), Vhp_.as<S>(), Rph_.as<S>(), i6off_.as<S>(),
+                    i7off_.as<S>(), R_.as<S>(), st_);
     mark(6);
     if (digits) {
       kbegin(kKSplit);
@@ -2145,7 +2152,8 @@ class Engine final : public IEngine {
     run_tc(tcR1_);  // R_ph = R_ph,b + T_ph,b dI4 + dT_ph I4
     kend();
     mark(5);
-    launch_rinit<S>(D_, T_.as<S>(), Vhp_.as<S>(), Rph_.as<S>(), i6off_.as<S>(), i7off_.as<S>(), R_.as<S>(), st_);
+    launch_rinit<S>(D_, omap_.as<int4>(), rmap_.as<int4>(), T_.as<S>(), Vhp_.as<S>(), Rph_.as<S>(), i6off_.as<S>(),
+                    i7off_.as<S>(), R_.as<S>(), st_);
     mark(6);
     kbegin(kKTcPP);
     run_tc(tcPP_);  // R' += PP_b + HH_b + V_pppp' dT' + dT' I9' + T_b' (I9' - I9_b')
@@ -2183,7 +2191,7 @@ class Engine final : public IEngine {
   DBuf onx_, ony_, onz_, osz_, otz_, okx_, oky_, okz_, oe_;
   // state
   DBuf T_, R_, Vhp_, Vpp_, Vhh_, X_, I9_, Tph_, Rph_, Vph_, W_, I4_, fdiag_, f6_, f7_, d2ij_, d2ab_, i6off_, i7off_;
-  DBuf partial_, res_, flag_, stage_, hist_, hist_t_, hist_e_, xwork_, xgroups_, xpart_, i6rows_, i6dots_;
+  DBuf partial_, res_, flag_, stage_, hist_, hist_t_, hist_e_, xwork_, xgroups_, xpart_, i6rows_, i6dots_, omap_, rmap_;
   int nxwork_ = 0, nxgroups_ = 0, ni6rows_ = 0;
   Plan planLadder_, planI4_, planRing_, planPP_, planHH_;
   // mixed precision

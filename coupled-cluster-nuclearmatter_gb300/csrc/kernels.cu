@@ -555,50 +555,107 @@ __device__ inline S ring_at(const DevLayout &L, const S *__restrict__ Rph, int a
   return Rph[L.tph_off[q] + s1.y + (int64_t)L.n_ph[q] * s2.y];
 }
 
-template <typename S>
-__global__ void k_rinit(DevLayout L, const S *__restrict__ T, const S *__restrict__ Vhp, const S *__restrict__ Rph,
-                        const S *__restrict__ i6off, const S *__restrict__ i7off, S *__restrict__ R) {
+// Where the one-body and ring terms of each packed element come from, once per layout:
+// omap = signed T' positions (+-(index + 1), 0 = absent) of the I6(b, b'), I6(a, a'),
+// I7(j, j') and I7(i, i') terms; rmap = R_ph positions (+1, 0 = absent) of the four
+// P(ab)P(ij) ring entries (a i j b), (b i j a), (a j i b), (b j i a).
+__global__ void k_rinit_maps(DevLayout L, int4 *__restrict__ omap, int4 *__restrict__ rmap) {
   const int2 tl = L.ttile[blockIdx.x];
   const int ch = tl.x;
   const int P = L.P[ch], H = L.H[ch];
-  const int n = P * H;  // < 2^31 per channel
+  const int n = P * H;
   const int end = min(tl.y + kTileElems, n);
-  const S *tc = T + L.t_off[ch];
   const int A = L.A, NP = L.NP;
+  const int64_t base = L.t_off[ch];
+  auto tpos = [&](int2 s, int64_t rel) -> int {  // signed position of T' entry base + rel
+    const int v = (int)(base + rel) + 1;
+    return s.y > 0 ? v : -v;
+  };
+  auto rpos = [&](int a, int i, int j, int b) -> int {
+    const int2 s1 = L.ph_slot[(int64_t)(a - A) * A + i];
+    const int2 s2 = L.hp_slot[(int64_t)j * NP + (b - A)];
+    if (s1.x < 0 || s2.x < 0) return 0;
+    return (int)(L.tph_off[s1.x] + s1.y + (int64_t)L.n_ph[s1.x] * s2.y) + 1;
+  };
   for (int e = tl.y + threadIdx.x; e < end; e += blockDim.x) {
     const int ij = e / P, ab = e - ij * P;
     const int2 po = L.pp_orb[L.pp_off[ch] + ab];
     const int2 ho = L.hh_orb[L.hh_off[ch] + ij];
     const int a = po.x, b = po.y, i = ho.x, j = ho.y;
-    S r = conj_(Vhp[L.t_off[ch] + e]);
+    int4 o = make_int4(0, 0, 0, 0);
     const int bb = L.partner[b];
     if (bb >= A) {
       const int2 s = L.pp_slot[(int64_t)(a - A) * NP + (bb - A)];
-      if (s.y) r += i6off[b - A] * (ssign(s.y) * tc[sidx(s.y) + (int64_t)P * ij]);
+      if (s.y) o.x = tpos(s, sidx(s.y) + (int64_t)P * ij);
     }
     const int aa = L.partner[a];
     if (aa >= A) {
       const int2 s = L.pp_slot[(int64_t)(b - A) * NP + (aa - A)];
-      if (s.y) r -= i6off[a - A] * (ssign(s.y) * tc[sidx(s.y) + (int64_t)P * ij]);
+      if (s.y) o.y = tpos(s, sidx(s.y) + (int64_t)P * ij);
     }
     const int jj = L.partner[j];
     if (jj >= 0 && jj < A) {
       const int2 s = L.hh_slot[i * A + jj];
-      if (s.y) r -= i7off[j] * (ssign(s.y) * tc[ab + (int64_t)P * sidx(s.y)]);
+      if (s.y) o.z = tpos(s, ab + (int64_t)P * sidx(s.y));
     }
     const int ii = L.partner[i];
     if (ii >= 0 && ii < A) {
       const int2 s = L.hh_slot[j * A + ii];
-      if (s.y) r += i7off[i] * (ssign(s.y) * tc[ab + (int64_t)P * sidx(s.y)]);
+      if (s.y) o.w = tpos(s, ab + (int64_t)P * sidx(s.y));
     }
-    r += ring_at<S>(L, Rph, a, i, j, b) - ring_at<S>(L, Rph, b, i, j, a) - ring_at<S>(L, Rph, a, j, i, b) +
-         ring_at<S>(L, Rph, b, j, i, a);
-    R[L.t_off[ch] + e] = r;
+    omap[base + e] = o;
+    rmap[base + e] = make_int4(rpos(a, i, j, b), rpos(b, i, j, a), rpos(a, j, i, b), rpos(b, j, i, a));
+  }
+}
+void launch_rinit_maps(const DevLayout &L, int4 *omap, int4 *rmap, cudaStream_t st) {
+  if (L.nttile) k_rinit_maps<<<L.nttile, 256, 0, st>>>(L, omap, rmap);
+}
+
+template <typename S>
+__device__ __forceinline__ S signed_at(const S *__restrict__ T, int m) {
+  return m > 0 ? T[m - 1] : S(0.0) - T[-m - 1];
+}
+template <typename S>
+__device__ __forceinline__ S at_or_zero(const S *__restrict__ X, int m) {
+  return m ? X[m - 1] : S(0.0);
+}
+
+// R' = conj(V) + the one-body I6 / I7 terms + the ring scatter, through the maps
+template <typename S>
+__global__ void k_rinit(DevLayout L, const int4 *__restrict__ omap, const int4 *__restrict__ rmap, const S *__restrict__ T,
+                        const S *__restrict__ Vhp, const S *__restrict__ Rph, const S *__restrict__ i6off,
+                        const S *__restrict__ i7off, S *__restrict__ R) {
+  const int2 tl = L.ttile[blockIdx.x];
+  const int ch = tl.x;
+  const int P = L.P[ch], H = L.H[ch];
+  const int n = P * H;  // < 2^31 per channel
+  const int end = min(tl.y + kTileElems, n);
+  const int A = L.A;
+  const int64_t base = L.t_off[ch];
+  for (int e = tl.y + threadIdx.x; e < end; e += blockDim.x) {
+    const int4 o = omap[base + e];
+    const int4 m = rmap[base + e];
+    S r = conj_(Vhp[base + e]);
+    if (o.x | o.y) {
+      const int ab = e % P;
+      const int2 po = L.pp_orb[L.pp_off[ch] + ab];
+      if (o.x) r += i6off[po.y - A] * signed_at(T, o.x);
+      if (o.y) r -= i6off[po.x - A] * signed_at(T, o.y);
+    }
+    if (o.z | o.w) {
+      const int ij = e / P;
+      const int2 ho = L.hh_orb[L.hh_off[ch] + ij];
+      if (o.z) r -= i7off[ho.y] * signed_at(T, o.z);
+      if (o.w) r += i7off[ho.x] * signed_at(T, o.w);
+    }
+    r += at_or_zero(Rph, m.x) - at_or_zero(Rph, m.y) - at_or_zero(Rph, m.z) + at_or_zero(Rph, m.w);
+    R[base + e] = r;
   }
 }
 template <typename S>
-void launch_rinit(const DevLayout &L, const S *T, const S *Vhp, const S *Rph, const S *i6off, const S *i7off, S *R, cudaStream_t st) {
-  if (L.nttile) k_rinit<S><<<L.nttile, 256, 0, st>>>(L, T, Vhp, Rph, i6off, i7off, R);
+void launch_rinit(const DevLayout &L, const int4 *omap, const int4 *rmap, const S *T, const S *Vhp, const S *Rph,
+                  const S *i6off, const S *i7off, S *R, cudaStream_t st) {
+  if (L.nttile) k_rinit<S><<<L.nttile, 256, 0, st>>>(L, omap, rmap, T, Vhp, Rph, i6off, i7off, R);
 }
 
 // ============================================================================
@@ -1198,8 +1255,8 @@ void launch_unpack_t(const DevLayout &L, int ch, int n_pp, const int *pp_signed,
                               cudaStream_t);        \
   template void launch_i6<S>(const DevLayout &, const int2 *, int, S *, const S *, const S *, const S *, const S *,   \
                              S *, S *, cudaStream_t);                                                                  \
-  template void launch_rinit<S>(const DevLayout &, const S *, const S *, const S *, const S *, const S *, S *,         \
-                                cudaStream_t);                                                                         \
+  template void launch_rinit<S>(const DevLayout &, const int4 *, const int4 *, const S *, const S *, const S *,      \
+                               const S *, const S *, S *, cudaStream_t);                                                                         \
   template void launch_update<S>(const DevLayout &, int, S *, const S *, const S *, const S *, const S *, S *,         \
                                  typename StepOf<S>::type *,                                                            \
                                  double *, double *, cudaStream_t);                                                    \
