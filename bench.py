@@ -264,48 +264,61 @@ def run_ours(args, wl):
                             rebase=ccx.REBASE_DIGITS if (precision and args.rebase == "digits") else ccx.REBASE_FP64)
 
     def timed(precision, steps, sample_clocks):
+        """The timed solves, without the per-term event records (profiling off)."""
         if dist:
             dist.barrier()
         torch.cuda.synchronize()
+        e.set_profiling(False)
         clocks = ClockSampler(local) if sample_clocks else None
         launches0 = e.launches()
         ev0 = torch.cuda.Event(enable_timing=True)
         ev1 = torch.cuda.Event(enable_timing=True)
         ev0.record(stream)
-        results, timers, ktimers = [], {}, {}
+        results = []
         for _ in range(steps):
             results.append(solve(e, precision))
-            for k, v in e.timers().items():
-                timers[k] = timers.get(k, 0.0) + v
-            for k, (ms_k, n_k) in e.kernel_timers().items():
-                a, b = ktimers.get(k, (0.0, 0))
-                ktimers[k] = (a + ms_k, b + n_k)
         ev1.record(stream)
         ev1.synchronize()
         torch.cuda.synchronize()
         clk = clocks.stop() if clocks else None
         ms = ev0.elapsed_time(ev1) / steps
         ms = max_over_ranks(ms, dist, "cuda")
-        return ms, results, timers, ktimers, e.launches() - launches0, clk
+        return ms, results, e.launches() - launches0, clk
+
+    def breakdown(precision, steps):
+        """Per-term and per-kernel device times from the same number of solves with
+        profiling on, after the timed region."""
+        timers, ktimers = {}, {}
+        e.set_profiling(True)
+        for _ in range(steps):
+            solve(e, precision)
+            for k, v in e.timers().items():
+                timers[k] = timers.get(k, 0.0) + v
+            for k, (ms_k, n_k) in e.kernel_timers().items():
+                a, b = ktimers.get(k, (0.0, 0))
+                ktimers[k] = (a + ms_k, b + n_k)
+        e.set_profiling(False)
+        return timers, ktimers
 
     # warm-up: both forms (tensor-core tiles are prepared by the first mixed solve)
     for _ in range(args.warmup):
         solve(e, prec)
         if prec:
             solve(e, 0)
-    ms, results, timers, ktimers, launches, clk = timed(prec, args.steps, True)
+    ms, results, launches, clk = timed(prec, args.steps, True)
     r = results[-1]
     iters = sum(x["iterations"] for x in results) / len(results)
     ea = (e.e0() + r["e_ccd"]).real / wl["A"]
     if prec:
-        ms64, res64, _, _, _, _ = timed(0, args.steps, False)
+        ms64, res64, _, _ = timed(0, args.steps, False)
         ea64 = (e.e0() + res64[-1]["e_ccd"]).real / wl["A"]
         plain = {"s": ms64 * 1e-3, "iterations": res64[-1]["iterations"], "E_per_A_MeV": ea64,
                  "res_norm": res64[-1]["res_norm"]}
     else:
         ms64, ea64, plain = ms, ea, None
 
-    # ---- roofline of the dominant kernel (largest device time in the timed solves) ----
+    # ---- roofline of the dominant kernel (largest device time in the profiled solves) ----
+    timers, ktimers = breakdown(prec, args.steps)
     work = kernel_work(P, H, ring, prec)
     dom = max((k for k in ktimers if k in work and ktimers[k][1] > 0), key=lambda k: ktimers[k][0])
     kms, kn = ktimers[dom]
@@ -353,6 +366,8 @@ def run_ours(args, wl):
             "plain_fp64": plain, "speedup_vs_plain_fp64": (ms64 / ms) if prec else None,
             "dE_per_A_keV_vs_fp64": abs(ea - ea64) * 1e3 if prec else 0.0,
             "gflop_per_iteration": flops["total"] / 1e9,
+            "breakdown": "term_ms_per_solve and kernel_ms_per_solve (and the roofline's launch time) from "
+                         "as many further solves with per-term CUDA events on, after the timed region",
             "term_ms_per_solve": {k: v / args.steps for k, v in timers.items()},
             "kernel_ms_per_solve": kernel_ms,
             "roofline": roofline, "clocks": clk, "gpu_launches": launches, "e2e": e2e}

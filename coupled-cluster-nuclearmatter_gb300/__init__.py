@@ -106,6 +106,7 @@ def lib():
         "ccx_engine_destroy": ([vp], C.c_int),
         "ccx_engine_memory": ([vp, C.POINTER(i64)], C.c_int),
         "ccx_engine_launches": ([vp, C.POINTER(i64)], C.c_int),
+        "ccx_engine_set_profiling": ([vp, i32], C.c_int),
         "ccx_engine_timers": ([vp, vp], C.c_int),
         "ccx_set_fock": ([vp, vp, vp], C.c_int),
         "ccx_set_vblock": ([vp, i32, i32, vp], C.c_int),
@@ -551,6 +552,11 @@ class Engine:
         n = np.zeros(16, np.int64)
         _check(lib().ccx_engine_kernel_timers(self._h, _ptr(ms), _ptr(n)))
         return {k: (float(ms[i]), int(n[i])) for i, k in enumerate(self.KERNEL_SLOTS)}
+
+    def set_profiling(self, on: bool) -> None:
+        """Per-term and per-kernel event timers of ccd_iter (off by default: only the
+        total time is recorded; on costs ~20 event records per iteration)."""
+        _check(lib().ccx_engine_set_profiling(self._h, int(bool(on))))
 
     def timers(self) -> dict:
         z = np.zeros(10)

@@ -353,6 +353,7 @@ int ccx_engine_launches(const ccx_engine *e, int64_t *n) {
   if (!n) return fail(CCX_EINVAL, "null argument");
   ENGINE_CALL(e, *n = e->E->launches());
 }
+int ccx_engine_set_profiling(ccx_engine *e, int32_t on) { ENGINE_CALL(e, e->E->set_profiling(on != 0)); }
 int ccx_engine_timers(const ccx_engine *e, double ms[10]) {
   if (!ms) return fail(CCX_EINVAL, "null argument");
   ENGINE_CALL(e, e->E->timers(ms));

@@ -584,7 +584,7 @@ class Engine final : public IEngine {
     for (double &t : ktimers_) t = 0.0;
     for (int64_t &c : kcount_) c = 0;
     kn_ = 0;
-    timing_ = true;
+    timing_ = profiling_;
     CK(cudaEventRecord(ev_[10], st_));
     if (o.mode == 0) iterate_reference(o, r);
     else iterate_standard(o, r);
@@ -1235,7 +1235,7 @@ class Engine final : public IEngine {
   //   std_after_update (true: finished); std_after_dots }.  The DIIS Gram row needs no
   //   host decision, so the dots are queued behind the update and one synchronisation
   //   per iteration serves both.
-  static constexpr int kDotsAt = 16;  // host_res_ offset of the DIIS Gram row (2 doubles per entry, <= 15)
+  static constexpr int kDotsAt = 16;  // host_res_ offset of the DIIS Gram row (<= 15 entries, 2 or 1 doubles each)
   struct StdState {
     IterOpts o;
     IterResult *r = nullptr;
@@ -1296,12 +1296,28 @@ class Engine final : public IEngine {
     s.ht = hist_t_.as<S>() + (int64_t)s.head * n_t_;
     s.he = hist_e_.as<E>() + (int64_t)s.head * n_t_;
     mark(7);
-    launch_update<S>(D_, 1, T_.as<S>(), R_.as<S>(), Vhp_.as<S>(), d2ij_.as<S>(), d2ab_.as<S>(), s.ht, s.he,
-                     partial_.as<double>(), res_.as<double>(), st_);
+    if constexpr (ScalarOf<S>::complex) {
+      launch_update<S>(D_, 1, T_.as<S>(), R_.as<S>(), Vhp_.as<S>(), d2ij_.as<S>(), d2ab_.as<S>(), s.ht, s.he,
+                       partial_.as<double>(), res_.as<double>(), st_);
+    } else {  // the Gram row of the new step against every stored one rides on the same pass
+      const int nh = std::min(s.nh + 1, s.m);
+      if (nh > 16 || s.head >= nh) throw EngineError(1, "DIIS history larger than the fused Gram row");
+      std::vector<const E *> es(nh);
+      for (int j = 0; j < nh; ++j) es[j] = hist_e_.as<E>() + (int64_t)j * n_t_;
+      launch_update_std(D_, T_.as<S>(), R_.as<S>(), Vhp_.as<S>(), d2ij_.as<S>(), d2ab_.as<S>(), s.ht, s.he, es.data(),
+                        nh, s.head, s.mixed ? tcerr_.as<int>() : nullptr, partial_.as<double>(), res_.as<double>(),
+                        st_);
+    }
     launches_ += 2;
-    // the tensor-core error word rides on the same synchronisation as the energy
-    if (s.mixed) CK(cudaMemcpyAsync((int *)(host_res_ + 63), tcerr_.p, sizeof(int), cudaMemcpyDeviceToHost, st_));
-    CK(cudaMemcpyAsync(host_res_, res_.p, 3 * sizeof(double), cudaMemcpyDeviceToHost, st_));
+    // the tensor-core error word rides on the same synchronisation as the energy (real
+    // engines: energy, norm, error word and Gram row in one copy)
+    if constexpr (ScalarOf<S>::complex) {
+      if (s.mixed) CK(cudaMemcpyAsync((int *)(host_res_ + 63), tcerr_.p, sizeof(int), cudaMemcpyDeviceToHost, st_));
+      CK(cudaMemcpyAsync(host_res_, res_.p, 3 * sizeof(double), cudaMemcpyDeviceToHost, st_));
+    } else {
+      CK(cudaMemcpyAsync(host_res_, res_.p, (4 + std::min(s.nh + 1, s.m)) * sizeof(double), cudaMemcpyDeviceToHost,
+                         st_));
+    }
   }
   bool std_after_update() override {
     StdState &s = ss_;
@@ -1313,9 +1329,9 @@ class Engine final : public IEngine {
     s.e[0] = host_res_[0];
     s.e[1] = host_res_[1];
     const double rn = 2.0 * std::sqrt(host_res_[2]);
-    const int *tc_word = (const int *)(host_res_ + 63);
-    if (s.mixed && *tc_word) {
-      const int err = *tc_word;
+    const int tc_word = ScalarOf<S>::complex ? *(const int *)(host_res_ + 63) : (int)host_res_[3];
+    if (s.mixed && tc_word) {
+      const int err = tc_word;
       CK(cudaMemsetAsync(tcerr_.p, 0, sizeof(int), st_));
       throw EngineError(2, "tensor-core GEMM reported error code " + std::to_string(err));
     }
@@ -1351,23 +1367,24 @@ class Engine final : public IEngine {
   void std_launch_dots() override {
     StdState &s = ss_;
     if (s.nh < s.m) ++s.nh;
-    std::vector<const E *> es(s.nh);
-    for (int j = 0; j < s.nh; ++j) es[j] = hist_e_.as<E>() + (int64_t)j * n_t_;
-    if constexpr (ScalarOf<S>::complex)
-      launch_dots<S>(n_t_, s.he, es.data(), s.nh, 1, partial_.as<double>(), res_.as<double>(), st_);
-    else
-      launch_dots_f32(n_t_, s.he, es.data(), s.nh, partial_.as<double>(), res_.as<double>(), st_);
-    launches_ += 2;
     // queued right behind the update, before the host has read its result: the Gram row
-    // lands in its own part of the host buffer
-    CK(cudaMemcpyAsync(host_res_ + kDotsAt, res_.p, 2 * s.nh * sizeof(double), cudaMemcpyDeviceToHost, st_));
+    // lands in its own part of the host buffer (real engines: computed by the update)
+    if constexpr (ScalarOf<S>::complex) {
+      std::vector<const E *> es(s.nh);
+      for (int j = 0; j < s.nh; ++j) es[j] = hist_e_.as<E>() + (int64_t)j * n_t_;
+      launch_dots<S>(n_t_, s.he, es.data(), s.nh, 1, partial_.as<double>(), res_.as<double>(), st_);
+      launches_ += 2;
+      CK(cudaMemcpyAsync(host_res_ + kDotsAt, res_.p, 2 * s.nh * sizeof(double), cudaMemcpyDeviceToHost, st_));
+    }
   }
   void std_after_dots() override {
     StdState &s = ss_;
     const int m = s.m, nh = s.nh, slot = s.head;
+    // (re, im) pairs of the dots launch, or the real Gram row copied with the update's sums
+    constexpr int at = ScalarOf<S>::complex ? kDotsAt : 4, stride = ScalarOf<S>::complex ? 2 : 1;
     for (int j = 0; j < nh; ++j) {
-      s.B[slot + (size_t)m * j] = host_res_[kDotsAt + 2 * j];
-      s.B[j + (size_t)m * slot] = host_res_[kDotsAt + 2 * j];
+      s.B[slot + (size_t)m * j] = host_res_[at + stride * j];
+      s.B[j + (size_t)m * slot] = host_res_[at + stride * j];
     }
     s.head = (s.head + 1) % m;
     std::vector<double> coef;
@@ -1401,6 +1418,7 @@ class Engine final : public IEngine {
   }
   void sync() override { CK(cudaStreamSynchronize(st_)); }
   void set_timing(bool on) override { timing_ = on; }
+  void set_profiling(bool on) override { profiling_ = on; }
 
   void iterate_standard(const IterOpts &o, IterResult &r) {
     std_begin(o, r);
@@ -1510,7 +1528,7 @@ class Engine final : public IEngine {
   // split jobs of one matrix operand (element (r, k) at src[r sr + k sk] in S units,
   // minus sub when given), one per scalar component, into tile buffer b at offset off
   void add_split(std::vector<TcSplitJob> &js, const S *src, const S *sub, int64_t sr, int64_t sk, int rows, int cols,
-                 int tile_rows, int rows_pad, TileBuf &b, int64_t off) {
+                 int tile_rows, int rows_pad, TileBuf &b, int64_t off, bool add = false) {
     const size_t es = tc_kind_ == kTcBF16 ? 2 : 4;
     const int tk = tc_tile_k(tc_kind_);
     for (int c = 0; c < kNComp; ++c) {
@@ -1520,6 +1538,7 @@ class Engine final : public IEngine {
       j.sr = sr * kNComp;
       j.sk = sk * kNComp;
       j.rows = rows; j.cols = cols; j.tile_rows = tile_rows; j.nk = (cols + tk - 1) / tk; j.rows_pad = rows_pad;
+      j.add = add ? 1 : 0;
       j.hi = (char *)b.hi.p + (off + c * b.n) * es;
       j.lo = (char *)b.lo.p + (off + c * b.n) * es;
       js.push_back(j);
@@ -1952,9 +1971,11 @@ class Engine final : public IEngine {
           add_gather(mjobs, gjobs, toff, tphmap_.as<int32_t>(), 1, nph, nph, nhp, 128, mpad(nph), tDphA_, mDphA_, oda);
           // at re-base: A = Tph_b
           add_split(js_tphb, tphb, nullptr, 1, nph, nph, nhp, 128, mpad(nph), tTphbA_, ota);
-          // after dI4: B = dI4 and B = I4 (rows n_hp, K = n_hp)
+          // after dI4: B = dI4 and B = I4 = I4_b + dI4 (rows n_hp, K = n_hp; I4 is split
+          // from its two parts and never formed in FP64 between re-bases)
           add_split(js_it2, dI4_.as<S>() + ioff, nullptr, nhp, 1, nhp, nhp, npadf(nhp), npadf(nhp), tdI4B_, oi);
-          add_split(js_it2, I4_.as<S>() + ioff, nullptr, nhp, 1, nhp, nhp, npadf(nhp), npadf(nhp), tI4B_, oib);
+          add_split(js_it2, I4b_.as<S>() + ioff, dI4_.as<S>() + ioff, nhp, 1, nhp, nhp, npadf(nhp), npadf(nhp), tI4B_,
+                    oib, true);
           // dI4 = 1/2 V_ph dT_ph, written without reading it
           add_tc_multi(p4, {{&tVph_, ov, &tDphB_, odb, nph}}, nhp, nhp, dI4_.as<S>() + ioff, 1, nhp, 0.5, nullptr, 1);
           // R_ph = R_ph,b + T_ph,b dI4 + dT_ph I4, written once
@@ -2143,9 +2164,8 @@ class Engine final : public IEngine {
     kbegin(kKTcI4);
     run_tc(tcI4_);  // dI4 = 1/2 V_ph dT_ph
     kend();
-    launch_add<S>(n_i4_, I4b_.as<S>(), dI4_.as<S>(), I4_.as<S>(), st_);
     kbegin(kKSplit);
-    run_split(spIter2_);  // dI4 (B), I4 (B)
+    run_split(spIter2_);  // dI4 (B), I4 = I4_b + dI4 (B)
     kend();
     mark(4);
     kbegin(kKTcRing);
@@ -2159,7 +2179,7 @@ class Engine final : public IEngine {
     run_tc(tcPP_);  // R' += PP_b + HH_b + V_pppp' dT' + dT' I9' + T_b' (I9' - I9_b')
     kend();
     mark(7);
-    launches_ += 6;  // sub, i7, i9, i6, add, rinit
+    launches_ += 5;  // sub, i7, i9, i6, rinit
     if (timing_) accumulate_timers(0, 7);
   }
 
@@ -2169,7 +2189,7 @@ class Engine final : public IEngine {
   cudaStream_t st_ = nullptr;
   cudaEvent_t ev_[12] = {};
   double timers_[10] = {};
-  bool timing_ = false;
+  bool timing_ = false, profiling_ = false;
   static constexpr int kKernelEvents = 32;
   cudaEvent_t kev_[2 * kKernelEvents] = {};
   int kslot_[kKernelEvents] = {};

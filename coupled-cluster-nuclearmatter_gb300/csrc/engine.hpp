@@ -97,6 +97,8 @@ class IEngine {
   virtual void std_after_dots() = 0;
   virtual void sync() = 0;
   virtual void set_timing(bool on) = 0;
+  // per-term and per-kernel event timers of ccd_iter (off by default)
+  virtual void set_profiling(bool on) = 0;
   // FP64 GEMM tile-shape autotuner: chosen shape per N bucket, ms[2 k + shape]
   virtual void autotune(int shapes[4], double ms[8]) = 0;
   // device view for the learned warm start (real engines only; false for complex)

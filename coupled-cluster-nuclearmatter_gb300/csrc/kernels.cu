@@ -764,31 +764,94 @@ void launch_dots(int64_t n, const S *a, const S *const *bs, int nb, int conj_a, 
   finish(partial, blocks, 2 * kMaxDots, out, st);
 }
 
-__global__ void k_dots_f32(int64_t n, const float *__restrict__ a, PtrPack<float> bs, int nb, double *partial) {
-  float f[kMaxDots];
+// Standard-mode update of real amplitudes with the Gram row of its step in the same pass.
+// Per amplitude: D from the dressed denominators (hole-pair sums staged per tile in
+// shared memory, the same association as k_update), q = R - D t in FP64, the step q/D
+// to FP32 accuracy, hist_t = t + step, hist_e = step; the energy sum t V in FP64, and
+// |q|^2 and step . hist_e[j] in FP32 per thread (FP64 across warps and blocks).  One
+// pass, one launch and one host copy per iteration instead of an update and a dots pass.
+constexpr int kUpdStdBlocks = 608;
+constexpr int kUpdStdNV = 4 + kMaxDots;  // E re, E im (0), |q|^2, error word, Gram row
+__device__ inline float warp_sum_f(float x) {
+  for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+  return x;
+}
+__global__ void __launch_bounds__(256) k_update_std(DevLayout L, const double *__restrict__ T,
+                                                    const double *__restrict__ R, const double *__restrict__ Vhp,
+                                                    const double *__restrict__ d2ij, const double *__restrict__ d2ab,
+                                                    double *__restrict__ hist_t, float *__restrict__ hist_e,
+                                                    PtrPack<float> es, int nb, int self, const int *err,
+                                                    double *partial) {
+  __shared__ double sdij[kTileElems];  // hole-pair sums of one tile (at most kTileElems rows)
+  __shared__ double red[kUpdStdNV][8];
+  double e = 0.0;
+  float r2 = 0.0f, f[kMaxDots];
 #pragma unroll
   for (int k = 0; k < kMaxDots; ++k) f[k] = 0.0f;
-  for (int64_t x = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; x < n; x += (int64_t)gridDim.x * blockDim.x) {
-    const float av = a[x];
+  const int A = L.A;
+  for (int tix = blockIdx.x; tix < L.nttile; tix += gridDim.x) {
+    const int2 tl = L.ttile[tix];
+    const int ch = tl.x;
+    const int P = L.P[ch];
+    const int end = min(tl.y + kTileElems, P * L.H[ch]);
+    const int ij0 = tl.y / P, nij = (end - 1) / P - ij0 + 1;
+    __syncthreads();  // the previous tile's sums are no longer read
+    for (int i = threadIdx.x; i < nij; i += blockDim.x) {
+      const int2 ho = L.hh_orb[L.hh_off[ch] + ij0 + i];
+      sdij[i] = d2ij[ho.x] + d2ij[ho.y];
+    }
+    __syncthreads();
+    const int64_t base = L.t_off[ch];
+    const int2 *pporb = L.pp_orb + L.pp_off[ch];
+    for (int el = tl.y + threadIdx.x; el < end; el += blockDim.x) {
+      const int64_t g = base + el;
+      const double t = T[g], vij = Vhp[g], r = R[g];
+      const int ij = el / P, ab = el - ij * P;
+      const int2 po = pporb[ab];
+      const double D = (sdij[ij - ij0] - d2ab[po.x - A]) - d2ab[po.y - A];
+      const double q = r - D * t;
+      const float qf = __double2float_rn(q);
+      r2 = fmaf(qf, qf, r2);
+      const float step = __fdiv_rn(qf, __double2float_rn(D));
+      hist_t[g] = t + (double)step;
+      hist_e[g] = step;
+      e = fma(t, vij, e);
 #pragma unroll
-    for (int k = 0; k < kMaxDots; ++k)
-      if (k < nb) f[k] = fmaf(av, bs.p[k][x], f[k]);
+      for (int k = 0; k < kMaxDots; ++k)
+        if (k < nb) f[k] = fmaf(step, k == self ? step : es.p[k][g], f[k]);
+    }
   }
-  double v[2 * kMaxDots];
+  // warp sums (FP32 values in FP32), then FP64 across the warps
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  e = warp_sum(e);
+  r2 = warp_sum_f(r2);
 #pragma unroll
-  for (int k = 0; k < kMaxDots; ++k) {
-    v[2 * k] = (double)f[k];
-    v[2 * k + 1] = 0.0;
+  for (int k = 0; k < kMaxDots; ++k)
+    if (k < nb) f[k] = warp_sum_f(f[k]);
+  if (lane == 0) {
+    red[0][wid] = e;
+    red[1][wid] = 0.0;
+    red[2][wid] = (double)r2;
+    red[3][wid] = (err && blockIdx.x == 0 && wid == 0) ? (double)*err : 0.0;  // carried to the host in the same copy
+#pragma unroll
+    for (int k = 0; k < kMaxDots; ++k) red[4 + k][wid] = k < nb ? (double)f[k] : 0.0;
   }
-  block_partial<2 * kMaxDots>(v, partial);
+  __syncthreads();
+  if (threadIdx.x < kUpdStdNV) {
+    double x = 0.0;
+    for (int w = 0; w < nw; ++w) x += red[threadIdx.x][w];
+    partial[(int64_t)blockIdx.x * kUpdStdNV + threadIdx.x] = x;
+  }
 }
-void launch_dots_f32(int64_t n, const float *a, const float *const *bs, int nb, double *partial, double *out,
-                     cudaStream_t st) {
+void launch_update_std(const DevLayout &L, const double *T, const double *R, const double *Vhp, const double *d2ij,
+                       const double *d2ab, double *hist_t, float *hist_e, const float *const *es, int nb, int self,
+                       const int *err, double *partial, double *out, cudaStream_t st) {
+  if (!L.nttile) return;
   PtrPack<float> pk{};
-  for (int k = 0; k < nb && k < kMaxDots; ++k) pk.p[k] = bs[k];
-  const int blocks = 608;
-  k_dots_f32<<<blocks, 256, 0, st>>>(n, a, pk, nb, partial);
-  finish(partial, blocks, 2 * kMaxDots, out, st);
+  for (int k = 0; k < nb; ++k) pk.p[k] = es[k];
+  const int blocks = std::min(L.nttile, kUpdStdBlocks);
+  k_update_std<<<blocks, 256, 0, st>>>(L, T, R, Vhp, d2ij, d2ab, hist_t, hist_e, pk, nb, self, err, partial);
+  finish(partial, blocks, kUpdStdNV, out, st);
 }
 
 // Gram matrix of consecutive differences d_i = t_{i+1} - t_i, B_ij = sum d_i d_j

@@ -93,9 +93,13 @@ void launch_update(const DevLayout &L, int mode, S *T, const S *R, const S *Vhp,
 // dot products: out[j] = sum_x w(a[x]) * b_j[x] for j < nb; conj on a when conj_a
 template <typename S>
 void launch_dots(int64_t n, const S *a, const S *const *bs, int nb, int conj_a, double *partial, double *out, cudaStream_t st);
-// the same over FP32 step vectors: FP32 products and per-thread sums, FP64 across threads
-void launch_dots_f32(int64_t n, const float *a, const float *const *bs, int nb, double *partial, double *out,
-                     cudaStream_t st);
+// mode-1 update of real amplitudes and the Gram row of its step in one pass:
+// out[0] = E, out[1] = 0, out[2] = |R - D T|^2, out[3] = *err (0 when err is null),
+// out[4 + j] = step . es[j] for j < nb (1 <= nb <= 16); es[self] is hist_e, the step
+// this pass writes.  partial holds 20 doubles for each of up to 608 blocks.
+void launch_update_std(const DevLayout &L, const double *T, const double *R, const double *Vhp, const double *d2ij,
+                       const double *d2ab, double *hist_t, float *hist_e, const float *const *es, int nb, int self,
+                       const int *err, double *partial, double *out, cudaStream_t st);
 // reference DIIS Gram matrix of differences of nstep history columns (no conjugation)
 template <typename S>
 void launch_diis_gram(int64_t n, const S *const *cols, int nstep, double *partial, double *out, cudaStream_t st);

@@ -470,7 +470,13 @@ __global__ void __launch_bounds__(256) k_tc_split(const TcSplitJob *__restrict__
 #pragma unroll
       for (int j = 0; j < cme; ++j) a[j] = (k0 + j < J.cols) ? src[(int64_t)(k0 + j) * J.sk] : 0.0;
       uint32_t h[cme], l[cme];
-      if (J.sub) {
+      if (J.sub && J.add) {  // the FP64 sum, then the plain split
+        const double *sub = J.sub + (int64_t)row * J.sr;
+#pragma unroll
+        for (int j = 0; j < cme; ++j) b[j] = (k0 + j < J.cols) ? sub[(int64_t)(k0 + j) * J.sk] : 0.0;
+#pragma unroll
+        for (int j = 0; j < cme; ++j) B::split(a[j] + b[j], h[j], l[j]);
+      } else if (J.sub) {
         const double *sub = J.sub + (int64_t)row * J.sr;
 #pragma unroll
         for (int j = 0; j < cme; ++j) b[j] = (k0 + j < J.cols) ? sub[(int64_t)(k0 + j) * J.sk] : 0.0;

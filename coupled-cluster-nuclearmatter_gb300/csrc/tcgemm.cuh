@@ -58,12 +58,13 @@ void launch_tc_gemm(int kind, const TcProb *probs, const TcTile *tiles, int ntil
 int tc_stages(int npad_max);
 
 // FP64 matrix (rows x cols, element (r, k) at src[r*sr + k*sk], optionally minus sub at
-// the same strides) -> pre-tiled hi/lo pair, zero padded.  tile_rows = 128 for an A
-// operand, npad for a B operand; nk = ceil(cols / tile_k).
+// the same strides, or plus sub (one FP64 addition) when add is set) -> pre-tiled hi/lo
+// pair, zero padded.
+// tile_rows = 128 for an A operand, npad for a B operand; nk = ceil(cols / tile_k).
 struct TcSplitJob {
   const double *src, *sub;
   int64_t sr, sk;
-  int rows, cols, tile_rows, nk, rows_pad;
+  int rows, cols, tile_rows, nk, rows_pad, add;
   void *hi, *lo;
 };
 // Work list of the split kernels: (job, first unit, end unit) per block, at most

@@ -352,12 +352,17 @@ int ccx_selftest_tc_gemm(int32_t device, int32_t kind, int32_t nprob, const int3
                          const int32_t *K, int32_t use_alo, uint64_t seed, double *max_rel_err, double *ms);
 /* kernel launches issued by this engine since creation */
 int ccx_engine_launches(const ccx_engine *e, int64_t *launches);
-/* per-term device milliseconds of the last ccx_ccd_iter:
+/* on: ccx_ccd_iter records CUDA events around every residual term and tensor-core
+ * launch (about 20 records per iteration, ~5% of a solve) so that ccx_engine_timers and
+ * ccx_engine_kernel_timers report the breakdown; off (the default): only the solve's
+ * total time is recorded and the breakdown reads zero. */
+int ccx_engine_set_profiling(ccx_engine *e, int32_t on);
+/* per-term device milliseconds of the last ccx_ccd_iter (profiling on):
  * [0] T_ph gather, [1] I9/I7, [2] I6, [3] I4, [4] ring, [5] R init, [6] ladders,
  * [7] update/energy, [8] DIIS, [9] total */
 int ccx_engine_timers(const ccx_engine *e, double ms[10]);
 /* device milliseconds and timed brackets of individual kernel launches in the last
- * ccx_ccd_iter (CUDA events on the engine stream around each launch or launch group):
+ * ccx_ccd_iter with profiling on (CUDA events on the engine stream around each launch or launch group):
  * [0] X = V_hhpp' T' (FP64 split-K GEMM + reduce), [1] I4 (FP64), [2] ring (FP64),
  * [3] fused pp+hh ladder (FP64), [4] V_pppp' T' at a mixed-precision re-base (FP64),
  * [5] hh-ladder of the mixed residual (FP64), [6] pp-ladder and hh-ladder corrections
