@@ -184,6 +184,7 @@ class Engine final : public IEngine {
     if (st_) cudaStreamDestroy(st_);
     if (cs_) cudaStreamDestroy(cs_);
     for (auto &e : sev_) if (e) cudaEventDestroy(e);
+    for (auto &r : replay_) if (r.exec) cudaGraphExecDestroy(r.exec);
     if (host_res_) cudaFreeHost(host_res_);
   }
 
@@ -975,6 +976,7 @@ class Engine final : public IEngine {
   // The grouped FP64 GEMM plans of the residual; bucket >= 0 keeps only the problems of
   // that N bucket, shapes overrides the engine's tile shape per bucket.
   void build_fp64_plans(Plan &ladder, Plan &i4, Plan &ring, int bucket, const int *shapes) {
+    ++plan_epoch_;
     const Layout &L = *L_;
     const int nc = L.fam[3].count();
     {  // R' += V_pppp' T' + T' I9'
@@ -1075,6 +1077,50 @@ class Engine final : public IEngine {
   // ================================================================== iteration
   void mark(int i) {
     if (timing_) CK(cudaEventRecord(ev_[i], st_));
+  }
+  // The residual launch sequences replayed as CUDA graphs, one per kind (plain FP64,
+  // FP64 re-base, digit re-base, mixed).  Their arguments are fixed device buffers and
+  // plans; plan_epoch_ moves whenever a plan or buffer they use is rebuilt, and the
+  // graph of that kind is captured again.  With the event timers on, launched directly.
+  struct Replay {
+    cudaGraphExec_t exec = nullptr;
+    int64_t launches = 0, epoch = -1;
+  };
+  Replay replay_[4];
+  int64_t plan_epoch_ = 0;
+  template <class F>
+  void replayed(int kind, F &&body) {
+    if (timing_) {
+      body();
+      return;
+    }
+    Replay &r = replay_[kind];
+    if (r.exec && r.epoch != plan_epoch_) {
+      CK(cudaGraphExecDestroy(r.exec));
+      r.exec = nullptr;
+    }
+    if (!r.exec) {
+      const int64_t l0 = launches_;
+      cudaGraph_t g = nullptr;
+      CK(cudaStreamBeginCapture(st_, cudaStreamCaptureModeRelaxed));
+      try {
+        body();
+      } catch (...) {
+        cudaStreamEndCapture(st_, &g);
+        if (g) cudaGraphDestroy(g);
+        launches_ = l0;
+        throw;
+      }
+      CK(cudaStreamEndCapture(st_, &g));
+      const cudaError_t ie = cudaGraphInstantiate(&r.exec, g, 0);
+      cudaGraphDestroy(g);
+      CK(ie);
+      r.launches = launches_ - l0;
+      r.epoch = plan_epoch_;
+      launches_ = l0;
+    }
+    CK(cudaGraphLaunch(r.exec, st_));
+    launches_ += r.launches;
   }
   void residual(bool /*unused*/) {
     mark(0);
@@ -1282,12 +1328,13 @@ class Engine final : public IEngine {
     StdState &s = ss_;
     ++s.it;
     s.exact = !s.mixed || s.need_fp64;
-    if (!s.mixed) residual(true);
+    if (!s.mixed) replayed(0, [&] { residual(true); });
     else if (s.exact) {
-      residual_fp64_rebase(s.o.rebase == 1);
+      const bool digits = s.o.rebase == 1;
+      replayed(digits ? 2 : 1, [&] { residual_fp64_rebase(digits); });
       ++s.r->fp64_sweeps;
     } else {
-      residual_mixed();
+      replayed(3, [&] { residual_mixed(); });
       ++s.r->mixed_iterations;
     }
   }
@@ -1851,6 +1898,7 @@ class Engine final : public IEngine {
     CK(cudaStreamSynchronize(st_));
     oz_ready_ = true;
     oz_v_version_ = v_version_;
+    ++plan_epoch_;
   }
 
   // Tile buffers, split jobs and tensor-core problem lists of the mixed residual.
@@ -2043,6 +2091,7 @@ class Engine final : public IEngine {
     CK(cudaStreamSynchronize(st_));
     mixed_ready_ = true;
     mixed_v_version_ = v_version_;
+    ++plan_epoch_;
   }
 
   // base T_b = 0: every cached product vanishes except I4_b = W
