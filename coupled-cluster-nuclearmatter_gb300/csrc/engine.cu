@@ -165,7 +165,12 @@ class Engine final : public IEngine {
     if (device < 0 || device >= ndev) throw EngineError(1, "device ordinal out of range");
     device_ = device;
     CK(cudaSetDevice(device_));
-    CK(cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking));
+    // the residual's X chain runs on a lower-priority side stream beside the main one
+    int prio_low = 0, prio_high = 0;
+    CK(cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high));
+    CK(cudaStreamCreateWithPriority(&st_, cudaStreamNonBlocking, prio_high));
+    CK(cudaStreamCreateWithPriority(&xs_, cudaStreamNonBlocking, prio_low));
+    for (auto &e : xev_) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     for (auto &e : ev_) CK(cudaEventCreate(&e));
     for (auto &e : kev_) CK(cudaEventCreate(&e));
     build_tables();
@@ -181,7 +186,10 @@ class Engine final : public IEngine {
     if (st_) cudaStreamSynchronize(st_);
     for (auto &e : ev_) if (e) cudaEventDestroy(e);
     for (auto &e : kev_) if (e) cudaEventDestroy(e);
+    if (xs_) cudaStreamSynchronize(xs_);
     if (st_) cudaStreamDestroy(st_);
+    if (xs_) cudaStreamDestroy(xs_);
+    for (auto &e : xev_) if (e) cudaEventDestroy(e);
     if (cs_) cudaStreamDestroy(cs_);
     for (auto &e : sev_) if (e) cudaEventDestroy(e);
     for (auto &r : replay_) if (r.exec) cudaGraphExecDestroy(r.exec);
@@ -925,9 +933,9 @@ class Engine final : public IEngine {
       ++launches_;
     }
   }
-  void run_x() {
+  void run_x(cudaStream_t s = nullptr) {
     launch_xdot<S>(D_, (const int4 *)xwork_.p, nxwork_, (const int4 *)xgroups_.p, nxgroups_, Vhp_.as<S>(), T_.as<S>(),
-                   xpart_.as<S>(), X_.as<S>(), st_);
+                   xpart_.as<S>(), X_.as<S>(), s ? s : st_);
     launches_ += 2;
   }
   void build_gemm_plans() {
@@ -1121,6 +1129,20 @@ class Engine final : public IEngine {
     }
     CK(cudaGraphLaunch(r.exec, st_));
     launches_ += r.launches;
+  }
+  // X = V_hhpp'^T T' and what hangs on it (I9, I7, their splits) need only T: they go to
+  // the side stream, forked at the start of a residual and joined before the R' pieces
+  // that read them.  Serial on the main stream while the event timers are on.
+  cudaStream_t fork_side() {
+    if (timing_) return st_;
+    CK(cudaEventRecord(xev_[0], st_));
+    CK(cudaStreamWaitEvent(xs_, xev_[0], 0));
+    return xs_;
+  }
+  void join_side(cudaStream_t xs) {
+    if (xs == st_) return;
+    CK(cudaEventRecord(xev_[1], xs));
+    CK(cudaStreamWaitEvent(st_, xev_[1], 0));
   }
   void residual(bool /*unused*/) {
     mark(0);
@@ -1567,9 +1589,9 @@ class Engine final : public IEngine {
         ++launches_;
       }
   }
-  void run_split(const SplitPlan &pl) {
+  void run_split(const SplitPlan &pl, cudaStream_t s = nullptr) {
     if (!pl.nchunks) return;
-    launch_tc_split(tc_kind_, (const TcSplitJob *)pl.jobs.p, (const int4 *)pl.chunks.p, pl.nchunks, st_);
+    launch_tc_split(tc_kind_, (const TcSplitJob *)pl.jobs.p, (const int4 *)pl.chunks.p, pl.nchunks, s ? s : st_);
     ++launches_;
   }
   // split jobs of one matrix operand (element (r, k) at src[r sr + k sk] in S units,
@@ -2109,13 +2131,14 @@ class Engine final : public IEngine {
   // digits, PP_b = V_pppp' T comes from the exact digit-product GEMM
   void residual_fp64_rebase(bool digits) {
     mark(0);
+    const cudaStream_t xs = fork_side();
     launch_gather_tph<S>(D_, T_.as<S>(), Tph_.as<S>(), st_);
     mark(1);
     kbegin(kKX);
-    run_x();
+    run_x(xs);
     kend();
-    launch_i7<S>(D_, X_.as<S>(), fdiag_.as<S>(), f7_.as<S>(), d2ij_.as<S>(), i7off_.as<S>(), st_);
-    launch_i9<S>(D_, n_hh2_, Vhh_.as<S>(), X_.as<S>(), I9_.as<S>(), st_);
+    launch_i7<S>(D_, X_.as<S>(), fdiag_.as<S>(), f7_.as<S>(), d2ij_.as<S>(), i7off_.as<S>(), xs);
+    launch_i9<S>(D_, n_hh2_, Vhh_.as<S>(), X_.as<S>(), I9_.as<S>(), xs);
     mark(2);
     launch_i6<S>(D_, (const int2 *)i6rows_.p, ni6rows_, i6dots_.as<S>(), T_.as<S>(), Vhp_.as<S>(), fdiag_.as<S>(),
                  f6_.as<S>(), d2ab_.as<S>(), i6off_.as<S>(), st_);
@@ -2146,6 +2169,7 @@ class Engine final : public IEngine {
       kend();
     }
     mark(5);
+    join_side(xs);
     launch_rinit<S>(D_, omap_.as<int4>(), rmap_.as<int4>(), T_.as<S>(), Vhp_.as<S>(), Rph_.as<S>(), i6off_.as<S>(),
                     i7off_.as<S>(), R_.as<S>(), st_);
     mark(6);
@@ -2184,6 +2208,7 @@ class Engine final : public IEngine {
   // contractions as cached FP64 products at T_b plus tensor-core corrections
   void residual_mixed() {
     mark(0);
+    const cudaStream_t xs = fork_side();
     kbegin(kKSplit);
     // dT' = T' - T_b' split once; dT' (B and A) and dT_ph (B and A) gathered from it
     // (T_ph itself is not needed in FP64 between re-bases)
@@ -2198,13 +2223,13 @@ class Engine final : public IEngine {
     // (a tensor-core X, X_b + V_hhpp'^T dT', costs the solve an iteration); I9' - I9_b'
     // = X - X_b for the hh-ladder correction
     kbegin(kKX);
-    run_x();
+    run_x(xs);
     kend();
-    launch_sub<S>(n_hh2_, X_.as<S>(), Xb_.as<S>(), dI9_.as<S>(), st_);
-    launch_i7<S>(D_, X_.as<S>(), fdiag_.as<S>(), f7_.as<S>(), d2ij_.as<S>(), i7off_.as<S>(), st_);
-    launch_i9<S>(D_, n_hh2_, Vhh_.as<S>(), X_.as<S>(), I9_.as<S>(), st_);
+    launch_sub<S>(n_hh2_, X_.as<S>(), Xb_.as<S>(), dI9_.as<S>(), xs);
+    launch_i7<S>(D_, X_.as<S>(), fdiag_.as<S>(), f7_.as<S>(), d2ij_.as<S>(), i7off_.as<S>(), xs);
+    launch_i9<S>(D_, n_hh2_, Vhh_.as<S>(), X_.as<S>(), I9_.as<S>(), xs);
     kbegin(kKSplit);
-    run_split(spIter3_);  // I9' (B), I9' - I9_b' (B)
+    run_split(spIter3_, xs);  // I9' (B), I9' - I9_b' (B)
     kend();
     mark(2);
     launch_i6<S>(D_, (const int2 *)i6rows_.p, ni6rows_, i6dots_.as<S>(), T_.as<S>(), Vhp_.as<S>(), fdiag_.as<S>(),
@@ -2221,6 +2246,7 @@ class Engine final : public IEngine {
     run_tc(tcR1_);  // R_ph = R_ph,b + T_ph,b dI4 + dT_ph I4
     kend();
     mark(5);
+    join_side(xs);
     launch_rinit<S>(D_, omap_.as<int4>(), rmap_.as<int4>(), T_.as<S>(), Vhp_.as<S>(), Rph_.as<S>(), i6off_.as<S>(),
                     i7off_.as<S>(), R_.as<S>(), st_);
     mark(6);
@@ -2235,7 +2261,8 @@ class Engine final : public IEngine {
   // ================================================================== state
   std::shared_ptr<const Layout> L_;
   int device_ = 0;
-  cudaStream_t st_ = nullptr;
+  cudaStream_t st_ = nullptr, xs_ = nullptr;
+  cudaEvent_t xev_[2] = {};
   cudaEvent_t ev_[12] = {};
   double timers_[10] = {};
   bool timing_ = false, profiling_ = false;
