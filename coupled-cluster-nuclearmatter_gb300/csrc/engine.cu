@@ -921,15 +921,16 @@ class Engine final : public IEngine {
     upload(pl.splits, b.splits, &bytes_);
     pl.nsplit = (int)b.splits.size();
   }
-  void run_plan(const Plan &pl) {
+  void run_plan(const Plan &pl, cudaStream_t s = nullptr) {
+    if (!s) s = st_;
     const GemmProb<S> *pr = (const GemmProb<S> *)pl.probs.p;
     for (int sh = 0; sh < 2; ++sh)
       if (pl.ntiles[sh]) {
-        launch_gemm<S>(sh, pr, (const GemmTile *)pl.tiles[sh].p, pl.ntiles[sh], st_);
+        launch_gemm<S>(sh, pr, (const GemmTile *)pl.tiles[sh].p, pl.ntiles[sh], s);
         ++launches_;
       }
     if (pl.nsplit) {
-      launch_splitk_reduce<S>(pr, (const int *)pl.splits.p, pl.nsplit, st_);
+      launch_splitk_reduce<S>(pr, (const int *)pl.splits.p, pl.nsplit, s);
       ++launches_;
     }
   }
@@ -1139,10 +1140,10 @@ class Engine final : public IEngine {
     CK(cudaStreamWaitEvent(xs_, xev_[0], 0));
     return xs_;
   }
-  void join_side(cudaStream_t xs) {
+  void join_side(cudaStream_t xs, int ev = 1) {
     if (xs == st_) return;
-    CK(cudaEventRecord(xev_[1], xs));
-    CK(cudaStreamWaitEvent(st_, xev_[1], 0));
+    CK(cudaEventRecord(xev_[ev], xs));
+    CK(cudaStreamWaitEvent(st_, xev_[ev], 0));
   }
   void residual(bool /*unused*/) {
     mark(0);
@@ -2170,6 +2171,7 @@ class Engine final : public IEngine {
     }
     mark(5);
     join_side(xs);
+    if (xs != st_) run_plan(planHH_, xs);  // HH_b = T' I9' beside the pp-ladder product
     launch_rinit<S>(D_, omap_.as<int4>(), rmap_.as<int4>(), T_.as<S>(), Vhp_.as<S>(), Rph_.as<S>(), i6off_.as<S>(),
                     i7off_.as<S>(), R_.as<S>(), st_);
     mark(6);
@@ -2186,9 +2188,12 @@ class Engine final : public IEngine {
       run_plan(planPP_);
       kend();
     }
-    kbegin(kKHH64);
-    run_plan(planHH_);  // HH_b = T' I9'
-    kend();
+    if (xs == st_) {
+      kbegin(kKHH64);
+      run_plan(planHH_);  // HH_b = T' I9'
+      kend();
+    }
+    join_side(xs, 2);
     // the cached products of the new base, PP_b + HH_b, and R' += them
     launch_axpy<S>(n_t_, HHb_.as<S>(), PPb_.as<S>(), st_);
     launch_axpy<S>(n_t_, PPb_.as<S>(), R_.as<S>(), st_);
@@ -2262,7 +2267,7 @@ class Engine final : public IEngine {
   std::shared_ptr<const Layout> L_;
   int device_ = 0;
   cudaStream_t st_ = nullptr, xs_ = nullptr;
-  cudaEvent_t xev_[2] = {};
+  cudaEvent_t xev_[3] = {};
   cudaEvent_t ev_[12] = {};
   double timers_[10] = {};
   bool timing_ = false, profiling_ = false;
