@@ -194,7 +194,9 @@ def kernel_work(P, H, ring, precision):
     # pp-ladder launch: V_pppp' dT' plus the two hh-ladder corrections (dT' I9', T_b' dI9')
     # into one accumulator; R' read and written, PP_b + HH_b read
     b_pp = sum(2 * es * (p * p + p * h) + 2 * 2 * es * (p * h + h * h) + 24.0 * p * h for p, h in zip(P, H))
-    b_i4 = sum(2 * es * (2.0 * nhp * nph) + 16.0 * nhp * nhp for nph, nhp in ring)
+    # dI4 launch: 1/2 V_ph dT_ph, and dX = V_hhpp'^T dT' (H x H, K = P) for I9' - I9_b'
+    b_i4 = (sum(2 * es * (2.0 * nhp * nph) + 16.0 * nhp * nhp for nph, nhp in ring)
+            + sum(2 * es * (2.0 * h * p) + 16.0 * h * h for p, h in zip(P, H)))
     # ring launch: T_ph,b dI4 + dT_ph I4 into one accumulator; R_ph,b read, R_ph written
     b_ring = sum(2 * 2 * es * (nph * nhp + nhp * nhp) + 16.0 * nph * nhp for nph, nhp in ring)
     # digit-product GEMM: 9 BF16 digit planes of V_pppp' and of T_b read once, C written
@@ -211,11 +213,12 @@ def kernel_work(P, H, ring, precision):
 KERNEL_NAMES = {"x_fp64": "k_xdot X = V_hhpp'^T T' (FP64 column dots)", "i4_fp64": "k_gemm<double> I4",
                 "ring_fp64": "k_gemm<double> ring", "ladder_fp64": "k_gemm<double> fused pp+hh ladder",
                 "pp_rebase_fp64": "k_gemm<double> pp-ladder at a re-base", "hh_fp64": "k_gemm<double> hh-ladder",
-                "pp_tc": "k_tc_gemm pp + hh ladder corrections (3 products, one accumulator)", "i4_tc": "k_tc_gemm dI4 correction",
+                "pp_tc": "k_tc_gemm pp + hh ladder corrections (3 products, one accumulator)", "i4_tc": "k_tc_gemm dI4 and dX corrections",
                 "ring_tc": "k_tc_gemm ring corrections (2 products, one accumulator)", "split": "k_tc_split",
                 "pp_rebase_digits": "k_oz_gemm pp-ladder at a re-base (exact digit products)",
                 "i4_rebase_digits": "k_oz_gemm I4 at a re-base (exact digit products)",
-                "ring_rebase_digits": "k_oz_gemm ring at a re-base (exact digit products)"}
+                "ring_rebase_digits": "k_oz_gemm ring at a re-base (exact digit products)",
+                "i7_fp64": "k_i7dots I7 of a mixed residual (FP64 column dots)"}
 
 
 def replica_theta(rank: int):

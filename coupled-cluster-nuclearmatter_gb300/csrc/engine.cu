@@ -1945,13 +1945,14 @@ class Engine final : public IEngine {
     auto nkf = [&](int x) { return (x + tk - 1) / tk; };
     const int nc = L.fam[3].count(), nq = L.ph[1].count();
     // sizes
-    TileBuf *bufs[12] = {&tVpp_, &tD_, &tVph_, &tDphB_, &tTphbA_, &tDphA_, &tdI4B_, &tI4B_,
-                         &tDA_, &tI9B_, &tTbA_, &tdI9B_};
+    TileBuf *bufs[13] = {&tVpp_, &tD_, &tVph_, &tDphB_, &tTphbA_, &tDphA_, &tdI4B_, &tI4B_,
+                         &tDA_, &tI9B_, &tTbA_, &tdI9B_, &tVhT_};
     for (TileBuf *b : bufs) b->n = 0;
     for (int c = 0; c < nc; ++c) {
       const auto &pk = L.pk[c];
       if (pk.P <= 0 || pk.H <= 0) continue;
       tVpp_.n += (int64_t)mpad(pk.P) * nkf(pk.P) * tk;
+      tVhT_.n += (int64_t)mpad(pk.H) * nkf(pk.P) * tk;   // A = V_hhpp'^T (H x P)
       tD_.n += (int64_t)npadf(pk.H) * nkf(pk.P) * tk;
       tDA_.n += (int64_t)mpad(pk.P) * nkf(pk.H) * tk;    // A = dT' (P x H)
       tTbA_.n += (int64_t)mpad(pk.P) * nkf(pk.H) * tk;   // A = T_b' (P x H)
@@ -1987,6 +1988,10 @@ class Engine final : public IEngine {
     CK(cudaMemset(dI4_.p, 0, std::max<int64_t>(n_i4_, 1) * sz));
     Xb_.alloc(std::max<int64_t>(n_hh2_, 1) * sz, &bytes_);
     dI9_.alloc(std::max<int64_t>(n_hh2_, 1) * sz, &bytes_);
+    // dX = V_hhpp'^T dT' is written block by block by the tensor cores; blocks of channels
+    // without pp pairs stay zero
+    CK(cudaMemset(dI9_.p, 0, std::max<int64_t>(n_hh2_, 1) * sz));
+    xd7_.alloc((size_t)std::max(2 * D_.A * D_.A, 1) * sz, &bytes_);
     HHb_.alloc(std::max<int64_t>(n_t_, 1) * sz, &bytes_);
     tcerr_.alloc(sizeof(int), &bytes_);
     CK(cudaMemset(tcerr_.p, 0, sizeof(int)));
@@ -2003,12 +2008,17 @@ class Engine final : public IEngine {
     std::vector<TcGatherJob> gjobs;
     TcList pp, p4, pr1;
     {
-      int64_t oa = 0, ob = 0, voff = 0, hoff = 0, oda = 0, otb = 0, oi9 = 0;
+      int64_t oa = 0, ob = 0, voff = 0, hoff = 0, oda = 0, otb = 0, oi9 = 0, ovt = 0;
       for (int c = 0; c < nc; ++c) {
         const auto &pk = L.pk[c];
         if (pk.P > 0 && pk.H > 0) {
           S *tb = Tb_.as<S>() + pk.t_off;
           add_split(js_static, Vpp_.as<S>() + voff, nullptr, pk.P, 1, pk.P, pk.P, 128, mpad(pk.P), tVpp_, oa);
+          // dX = X - X_b = V_hhpp'^T dT' (H x H, K = P): static A = V_hhpp'^T, B = dT' as
+          // the pp-ladder reads it; in the dI4 launch, written over dI9 = I9' - I9_b'
+          add_split(js_static, Vhp_.as<S>() + pk.t_off, nullptr, pk.P, 1, pk.H, pk.P, 128, mpad(pk.H), tVhT_, ovt);
+          add_tc_multi(p4, {{&tVhT_, ovt, &tD_, ob, pk.P}}, pk.H, pk.H, dI9_.as<S>() + hoff, 1, pk.H, 1.0, nullptr, 1);
+          ovt += (int64_t)mpad(pk.H) * nkf(pk.P) * tk;
           add_gather(mjobs, gjobs, pk.t_off, nullptr, pk.P, 1, pk.H, pk.P, npadf(pk.H), npadf(pk.H), tD_, mD_, ob);
           // hh-ladder: R' += HH_b + dT' I9' + T_b' (I9' - I9_b')
           add_gather(mjobs, gjobs, pk.t_off, nullptr, 1, pk.P, pk.P, pk.H, 128, mpad(pk.P), tDA_, mDA_, oda);
@@ -2227,24 +2237,23 @@ class Engine final : public IEngine {
     // X in FP64: it feeds the dressed hole denominators of every amplitude through I7
     // (a tensor-core X, X_b + V_hhpp'^T dT', costs the solve an iteration); I9' - I9_b'
     // = X - X_b for the hh-ladder correction
-    kbegin(kKX);
-    run_x(xs);
-    kend();
-    launch_sub<S>(n_hh2_, X_.as<S>(), Xb_.as<S>(), dI9_.as<S>(), xs);
-    launch_i7<S>(D_, X_.as<S>(), fdiag_.as<S>(), f7_.as<S>(), d2ij_.as<S>(), i7off_.as<S>(), xs);
-    launch_i9<S>(D_, n_hh2_, Vhh_.as<S>(), X_.as<S>(), I9_.as<S>(), xs);
-    kbegin(kKSplit);
-    run_split(spIter3_, xs);  // I9' (B), I9' - I9_b' (B)
+    // I7 in FP64 from the X entries it reads, beside the tensor-core work; the rest of
+    // X enters only through I9' - I9_b' = dX, a tensor-core correction in the dI4 launch
+    kbegin(kKI7);
+    launch_i7_direct<S>(D_, Vhp_.as<S>(), T_.as<S>(), xd7_.as<S>(), fdiag_.as<S>(), f7_.as<S>(), d2ij_.as<S>(),
+                        i7off_.as<S>(), xs);
     kend();
     mark(2);
     launch_i6<S>(D_, (const int2 *)i6rows_.p, ni6rows_, i6dots_.as<S>(), T_.as<S>(), Vhp_.as<S>(), fdiag_.as<S>(),
                  f6_.as<S>(), d2ab_.as<S>(), i6off_.as<S>(), st_);
     mark(3);
     kbegin(kKTcI4);
-    run_tc(tcI4_);  // dI4 = 1/2 V_ph dT_ph
+    run_tc(tcI4_);  // dI4 = 1/2 V_ph dT_ph, dI9 = dX = V_hhpp'^T dT'
     kend();
+    launch_i9b<S>(n_hh2_, Vhh_.as<S>(), Xb_.as<S>(), dI9_.as<S>(), I9_.as<S>(), st_);
     kbegin(kKSplit);
     run_split(spIter2_);  // dI4 (B), I4 = I4_b + dI4 (B)
+    run_split(spIter3_);  // I9' (B), I9' - I9_b' (B)
     kend();
     mark(4);
     kbegin(kKTcRing);
@@ -2259,7 +2268,7 @@ class Engine final : public IEngine {
     run_tc(tcPP_);  // R' += PP_b + HH_b + V_pppp' dT' + dT' I9' + T_b' (I9' - I9_b')
     kend();
     mark(7);
-    launches_ += 5;  // sub, i7, i9, i6, rinit
+    launches_ += 6;  // i7 (2), i9, i6 (2), rinit
     if (timing_) accumulate_timers(0, 7);
   }
 
@@ -2299,13 +2308,13 @@ class Engine final : public IEngine {
   bool mixed_ready_ = false;
   int tc_kind_ = 0;
   int64_t v_version_ = 0, mixed_v_version_ = -1;
-  DBuf Tb_, PPb_, Tphb_, Rphb_, I4b_, dI4_, tcerr_, Xb_, dI9_, HHb_;
+  DBuf Tb_, PPb_, Tphb_, Rphb_, I4b_, dI4_, tcerr_, Xb_, dI9_, HHb_, xd7_;
   OzBuf ozVpp_, ozTb_, ozVph_, ozTphB_, ozTphA_, ozI4B_;
   OzSplitPlan ozsV_, ozsTb_, ozsTph_, ozsI4_;
   OzPlan ozPP_, ozI4_, ozRing_;
   bool oz_ready_ = false;
   int64_t oz_v_version_ = -1;
-  TileBuf tVpp_, tD_, tVph_, tDphB_, tTphbA_, tDphA_, tdI4B_, tI4B_, tDA_, tI9B_, tTbA_, tdI9B_;
+  TileBuf tVpp_, tD_, tVph_, tDphB_, tTphbA_, tDphA_, tdI4B_, tI4B_, tDA_, tI9B_, tTbA_, tdI9B_, tVhT_;
   TcPlan tcPP_, tcI4_, tcR1_;
   SplitPlan spStatic_, spTphb_, spIter2_, spIter3_;
   DBuf phl_, tphmap_, mD_, mDA_, mDphB_, mDphA_;  // packed split of dT' (hi/lo pairs), gather maps

@@ -53,6 +53,7 @@ enum KernelSlot {
   kKPPOz = 10,  // k_oz_gemm: V_pppp' T' at a re-base as exact digit products
   kKI4Oz = 11,  // k_oz_gemm: I4 at a re-base as exact digit products
   kKRingOz = 12,  // k_oz_gemm: ring at a re-base as exact digit products
+  kKI7 = 13,    // k_i7dots + k_i7sum: I7 of a mixed residual from the X entries it reads
   kKernelSlots = 16
 };
 

@@ -421,6 +421,71 @@ void launch_i7(const DevLayout &L, const S *X, const S *fdiag, const S *f7, S *d
   k_i7<S><<<(int)((threads + 127) / 128), 128, 0, st>>>(L, X, fdiag, f7, d2ij, i7off);
 }
 
+// The same I7 without X: the entries of X it reads, X(slot(c,l), slot(y,l)) for c in
+// {y, partner(y)}, as dots of column slot(c,l) of V_hhpp' with column slot(y,l) of T'
+// over the channel's packed pp rows (one warp per dot, the sign of both slots applied),
+// then the sums over l in the order of k_i7.  About 2 A^2 dots instead of all of X.
+template <typename S>
+__global__ void k_i7dots(DevLayout L, const S *__restrict__ V, const S *__restrict__ T, S *__restrict__ xd) {
+  const int64_t t = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31, A = L.A;
+  if (t >= (int64_t)2 * A * A) return;
+  const int yw = (int)(t / A), l = (int)(t - (int64_t)yw * A);
+  const int y = yw >> 1, which = yw & 1;
+  const int c = which ? L.partner[y] : y;
+  S acc = S(0.0);
+  if (!which || (c >= 0 && c < A)) {
+    const int2 s1 = L.hh_slot[c * A + l], s2 = L.hh_slot[y * A + l];
+    if (s1.y != 0 && s2.y != 0) {
+      const int ch = s1.x, P = L.P[ch];
+      const S *v = V + L.t_off[ch] + (int64_t)P * sidx(s1.y);
+      const S *u = T + L.t_off[ch] + (int64_t)P * sidx(s2.y);
+      for (int k = lane; k < P; k += 32) acc += v[k] * u[k];
+      acc = (ssign(s1.y) * ssign(s2.y)) * from2<S>(warp_sum2(to2(acc)));
+    }
+  }
+  if (lane == 0) xd[t] = acc;
+}
+template <typename S>
+__global__ void k_i7sum(DevLayout L, const S *__restrict__ xd, const S *__restrict__ fdiag, const S *__restrict__ f7,
+                        S *d2ij, S *i7off) {
+  const int t = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (t >= 2 * L.A) return;
+  const int y = t >> 1, which = t & 1;
+  const int c = which ? L.partner[y] : y;
+  if (which && (c < 0 || c >= L.A)) {
+    if (lane == 0) i7off[y] = S(0.0);
+    return;
+  }
+  S acc = S(0.0);
+  for (int l = lane; l < L.A; l += 32) acc += xd[(int64_t)t * L.A + l];
+  const S tot = from2<S>(warp_sum2(to2(acc)));
+  if (lane == 0) {
+    const S val = (which ? f7[y] : fdiag[y]) + tot;
+    if (which) i7off[y] = val;
+    else d2ij[y] = val;
+  }
+}
+template <typename S>
+void launch_i7_direct(const DevLayout &L, const S *V, const S *T, S *xd, const S *fdiag, const S *f7, S *d2ij, S *i7off,
+                      cudaStream_t st) {
+  const int64_t t1 = (int64_t)2 * L.A * L.A * 32, t2 = (int64_t)2 * L.A * 32;
+  if (t1 == 0) return;
+  k_i7dots<S><<<(int)((t1 + 255) / 256), 256, 0, st>>>(L, V, T, xd);
+  k_i7sum<S><<<(int)((t2 + 127) / 128), 128, 0, st>>>(L, xd, fdiag, f7, d2ij, i7off);
+}
+// I9 = V_hhhh + (X_b + dX)
+template <typename S>
+__global__ void k_i9b(int64_t n, const S *__restrict__ Vhh, const S *__restrict__ Xb, const S *__restrict__ dX, S *I9) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    I9[i] = Vhh[i] + (Xb[i] + dX[i]);
+}
+template <typename S>
+void launch_i9b(int64_t n, const S *Vhh, const S *Xb, const S *dX, S *I9, cudaStream_t st) {
+  if (n > 0) k_i9b<S><<<(int)std::min<int64_t>((n + 255) / 256, 4096), 256, 0, st>>>(n, Vhh, Xb, dX, I9);
+}
+
 template <typename S>
 __global__ void k_i9(int64_t n, const S *__restrict__ Vhh, const S *__restrict__ X, S *I9) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
@@ -1313,6 +1378,9 @@ void launch_unpack_t(const DevLayout &L, int ch, int n_pp, const int *pp_signed,
   template void launch_splitk_reduce<S>(const GemmProb<S> *, const int *, int, cudaStream_t);                          \
   template void launch_gather_tph<S>(const DevLayout &, const S *, S *, cudaStream_t);                                 \
   template void launch_i7<S>(const DevLayout &, const S *, const S *, const S *, S *, S *, cudaStream_t);             \
+  template void launch_i7_direct<S>(const DevLayout &, const S *, const S *, S *, const S *, const S *, S *, S *,      \
+                                    cudaStream_t);                                                                  \
+  template void launch_i9b<S>(int64_t, const S *, const S *, const S *, S *, cudaStream_t);                         \
   template void launch_i9<S>(const DevLayout &, int64_t, const S *, const S *, S *, cudaStream_t);                     \
   template void launch_xdot<S>(const DevLayout &, const int4 *, int, const int4 *, int, const S *, const S *, S *, S *, \
                               cudaStream_t);        \

@@ -67,6 +67,13 @@ void launch_xdot(const DevLayout &L, const int4 *work, int nwork, const int4 *gr
                  const S *T, S *part, S *X, cudaStream_t st);
 template <typename S> void launch_i7(const DevLayout &L, const S *X, const S *fdiag, const S *f7, S *d2ij, S *i7off, cudaStream_t st);
 template <typename S> void launch_i9(const DevLayout &L, int64_t n, const S *Vhh, const S *X, S *I9, cudaStream_t st);
+// I7 without X: the X entries it reads as 2 A^2 column dots of V_hhpp' and T' into xd
+// (2 A^2 scalars), then summed as launch_i7 does
+template <typename S>
+void launch_i7_direct(const DevLayout &L, const S *V, const S *T, S *xd, const S *fdiag, const S *f7, S *d2ij, S *i7off,
+                      cudaStream_t st);
+// I9 = Vhh + (Xb + dX), n entries
+template <typename S> void launch_i9b(int64_t n, const S *Vhh, const S *Xb, const S *dX, S *I9, cudaStream_t st);
 // I6 in two passes; rowtile: (channel, first packed pp row) per block of kI6Rows rows;
 // D: 3 values per packed row, at 3 * (t_off[ch] + row)
 constexpr int kI6Rows = 128;

@@ -369,7 +369,8 @@ int ccx_engine_timers(const ccx_engine *e, double ms[10]);
  * with the cached base terms, one launch (tensor cores), [7] dI4 correction (tensor
  * cores), [8] ring corrections with the cached base ring, one launch (tensor cores),
  * [9] operand splits, [10] pp-ladder, [11] I4 and [12] ring at a re-base as digit products
- * (tensor cores), [13] .. [15] unused */
+ * (tensor cores), [13] I7 of a mixed residual from the X entries it reads (FP64 column
+ * dots), [14] .. [15] unused */
 int ccx_engine_kernel_timers(const ccx_engine *e, double ms[16], int64_t launches[16]);
 
 #ifdef __cplusplus
