@@ -394,7 +394,6 @@ PROFILED_TRAFFIC = {
     ("pnm66", "bf16x3", "x_fp64"): 32.0e6,
     ("pnm66", "bf16x3", "pp_tc"): 643.7e6,
     ("pnm66", "bf16x3", "ring_tc"): 275.5e6,
-    ("pnm66", "bf16x3", "i4_tc"): 98.8e6,
     ("pnm66", "bf16x3", "pp_rebase_digits"): 2426.5e6,
     ("pnm66", "bf16x3", "i4_rebase_digits"): 506.5e6,
     ("pnm66", "bf16x3", "ring_rebase_digits"): 505.4e6,
