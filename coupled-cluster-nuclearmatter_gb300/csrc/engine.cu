@@ -1598,7 +1598,8 @@ class Engine final : public IEngine {
   // split jobs of one matrix operand (element (r, k) at src[r sr + k sk] in S units,
   // minus sub when given), one per scalar component, into tile buffer b at offset off
   void add_split(std::vector<TcSplitJob> &js, const S *src, const S *sub, int64_t sr, int64_t sk, int rows, int cols,
-                 int tile_rows, int rows_pad, TileBuf &b, int64_t off, bool add = false) {
+                 int tile_rows, int rows_pad, TileBuf &b, int64_t off, int add = 0, TileBuf *b2 = nullptr,
+                 int64_t off2 = 0) {
     const size_t es = tc_kind_ == kTcBF16 ? 2 : 4;
     const int tk = tc_tile_k(tc_kind_);
     for (int c = 0; c < kNComp; ++c) {
@@ -1608,7 +1609,11 @@ class Engine final : public IEngine {
       j.sr = sr * kNComp;
       j.sk = sk * kNComp;
       j.rows = rows; j.cols = cols; j.tile_rows = tile_rows; j.nk = (cols + tk - 1) / tk; j.rows_pad = rows_pad;
-      j.add = add ? 1 : 0;
+      j.add = add;
+      if (add == 2) {  // src into b, src + sub into b2 (same geometry)
+        j.hi2 = (char *)b2->hi.p + (off2 + c * b2->n) * es;
+        j.lo2 = (char *)b2->lo.p + (off2 + c * b2->n) * es;
+      }
       j.hi = (char *)b.hi.p + (off + c * b.n) * es;
       j.lo = (char *)b.lo.p + (off + c * b.n) * es;
       js.push_back(j);
@@ -2054,9 +2059,8 @@ class Engine final : public IEngine {
           add_split(js_tphb, tphb, nullptr, 1, nph, nph, nhp, 128, mpad(nph), tTphbA_, ota);
           // after dI4: B = dI4 and B = I4 = I4_b + dI4 (rows n_hp, K = n_hp; I4 is split
           // from its two parts and never formed in FP64 between re-bases)
-          add_split(js_it2, dI4_.as<S>() + ioff, nullptr, nhp, 1, nhp, nhp, npadf(nhp), npadf(nhp), tdI4B_, oi);
-          add_split(js_it2, I4b_.as<S>() + ioff, dI4_.as<S>() + ioff, nhp, 1, nhp, nhp, npadf(nhp), npadf(nhp), tI4B_,
-                    oib, true);
+          add_split(js_it2, dI4_.as<S>() + ioff, I4b_.as<S>() + ioff, nhp, 1, nhp, nhp, npadf(nhp), npadf(nhp), tdI4B_,
+                    oi, 2, &tI4B_, oib);
           // dI4 = 1/2 V_ph dT_ph, written without reading it
           add_tc_multi(p4, {{&tVph_, ov, &tDphB_, odb, nph}}, nhp, nhp, dI4_.as<S>() + ioff, 1, nhp, 0.5, nullptr, 1);
           // R_ph = R_ph,b + T_ph,b dI4 + dT_ph I4, written once
@@ -2152,7 +2156,7 @@ class Engine final : public IEngine {
     launch_i9<S>(D_, n_hh2_, Vhh_.as<S>(), X_.as<S>(), I9_.as<S>(), xs);
     mark(2);
     launch_i6<S>(D_, (const int2 *)i6rows_.p, ni6rows_, i6dots_.as<S>(), T_.as<S>(), Vhp_.as<S>(), fdiag_.as<S>(),
-                 f6_.as<S>(), d2ab_.as<S>(), i6off_.as<S>(), st_);
+                 f6_.as<S>(), d2ab_.as<S>(), i6off_.as<S>(), xs);
     mark(3);
     if (digits) {  // I4 = W + 1/2 V_ph T_ph and R_ph = T_ph I4 as digit products
       kbegin(kKSplit);
@@ -2245,7 +2249,7 @@ class Engine final : public IEngine {
     kend();
     mark(2);
     launch_i6<S>(D_, (const int2 *)i6rows_.p, ni6rows_, i6dots_.as<S>(), T_.as<S>(), Vhp_.as<S>(), fdiag_.as<S>(),
-                 f6_.as<S>(), d2ab_.as<S>(), i6off_.as<S>(), st_);
+                 f6_.as<S>(), d2ab_.as<S>(), i6off_.as<S>(), xs);
     mark(3);
     kbegin(kKTcI4);
     run_tc(tcI4_);  // dI4 = 1/2 V_ph dT_ph, dI9 = dX = V_hhpp'^T dT'

@@ -474,8 +474,18 @@ __global__ void __launch_bounds__(256) k_tc_split(const TcSplitJob *__restrict__
         const double *sub = J.sub + (int64_t)row * J.sr;
 #pragma unroll
         for (int j = 0; j < cme; ++j) b[j] = (k0 + j < J.cols) ? sub[(int64_t)(k0 + j) * J.sk] : 0.0;
+        if (J.add == 2) {  // src itself as well, into the second tile pair
+          uint32_t h2[cme], l2[cme];
 #pragma unroll
-        for (int j = 0; j < cme; ++j) B::split(a[j] + b[j], h[j], l[j]);
+          for (int j = 0; j < cme; ++j) B::split(a[j] + b[j], h2[j], l2[j]);
+          ((uint4 *)J.hi2)[u] = H::pack(h2);
+          ((uint4 *)J.lo2)[u] = H::pack(l2);
+#pragma unroll
+          for (int j = 0; j < cme; ++j) B::split(a[j], h[j], l[j]);
+        } else {
+#pragma unroll
+          for (int j = 0; j < cme; ++j) B::split(a[j] + b[j], h[j], l[j]);
+        }
       } else if (J.sub) {
         const double *sub = J.sub + (int64_t)row * J.sr;
 #pragma unroll
@@ -491,6 +501,10 @@ __global__ void __launch_bounds__(256) k_tc_split(const TcSplitJob *__restrict__
     } else {
       hi[u] = make_uint4(0, 0, 0, 0);
       if (lo) lo[u] = make_uint4(0, 0, 0, 0);
+      if (J.add == 2) {
+        ((uint4 *)J.hi2)[u] = make_uint4(0, 0, 0, 0);
+        ((uint4 *)J.lo2)[u] = make_uint4(0, 0, 0, 0);
+      }
     }
   }
 }

@@ -58,14 +58,15 @@ void launch_tc_gemm(int kind, const TcProb *probs, const TcTile *tiles, int ntil
 int tc_stages(int npad_max);
 
 // FP64 matrix (rows x cols, element (r, k) at src[r*sr + k*sk], optionally minus sub at
-// the same strides, or plus sub (one FP64 addition) when add is set) -> pre-tiled hi/lo
-// pair, zero padded.
+// the same strides, or plus sub (one FP64 addition) when add is 1) -> pre-tiled hi/lo
+// pair, zero padded.  add = 2: src itself into hi/lo and src + sub into hi2/lo2 (two
+// operands of the same tile geometry from one read of src).
 // tile_rows = 128 for an A operand, npad for a B operand; nk = ceil(cols / tile_k).
 struct TcSplitJob {
   const double *src, *sub;
   int64_t sr, sk;
   int rows, cols, tile_rows, nk, rows_pad, add;
-  void *hi, *lo;
+  void *hi, *lo, *hi2, *lo2;
 };
 // Work list of the split kernels: (job, first unit, end unit) per block, at most
 // kSplitChunk 16-byte units, covering only the row groups of each tile that hold rows of
