@@ -1167,7 +1167,7 @@ class Engine final : public IEngine {
     kend();
     mark(5);
     launch_rinit<S>(D_, omap_.as<int4>(), rmap_.as<int4>(), T_.as<S>(), Vhp_.as<S>(), Rph_.as<S>(), i6off_.as<S>(),
-                    i7off_.as<S>(), R_.as<S>(), st_);
+                    i7off_.as<S>(), nullptr, nullptr, R_.as<S>(), st_);
     mark(6);
     kbegin(kKLadder);
     run_plan(planLadder_);
@@ -1985,7 +1985,7 @@ class Engine final : public IEngine {
     Tb_.alloc(std::max<int64_t>(n_t_, 1) * sz, &bytes_);
     PPb_.alloc(std::max<int64_t>(n_t_, 1) * sz, &bytes_);
     Tphb_.alloc(std::max<int64_t>(n_ph_, 1) * sz, &bytes_);
-    Rphb_.alloc(std::max<int64_t>(n_ph_, 1) * sz, &bytes_);
+    Rringb_.alloc(std::max<int64_t>(n_t_, 1) * sz, &bytes_);
     I4b_.alloc(std::max<int64_t>(n_i4_, 1) * sz, &bytes_);
     dI4_.alloc(std::max<int64_t>(n_i4_, 1) * sz, &bytes_);
     // the tensor-core product overwrites dI4 block by block; blocks of channels without
@@ -2063,9 +2063,10 @@ class Engine final : public IEngine {
                     oi, 2, &tI4B_, oib);
           // dI4 = 1/2 V_ph dT_ph, written without reading it
           add_tc_multi(p4, {{&tVph_, ov, &tDphB_, odb, nph}}, nhp, nhp, dI4_.as<S>() + ioff, 1, nhp, 0.5, nullptr, 1);
-          // R_ph = R_ph,b + T_ph,b dI4 + dT_ph I4, written once
+          // dR_ph = R_ph - R_ph,b = T_ph,b dI4 + dT_ph I4, written without reading it; R_ph,b
+          // enters R' through the ring terms the re-base stored per amplitude
           add_tc_multi(pr1, {{&tTphbA_, ota, &tdI4B_, oi, nhp}, {&tDphA_, oda, &tI4B_, oib, nhp}}, nph, nhp,
-                       Rph_.as<S>() + toff, 1, nph, 1.0, Rphb_.as<S>() + toff, 1);
+                       Rph_.as<S>() + toff, 1, nph, 1.0, nullptr, 1);
           ov += (int64_t)mpad(nhp) * nkf(nph) * tk;
           odb += (int64_t)npadf(nhp) * nkf(nph) * tk;
           ota += (int64_t)mpad(nph) * nkf(nhp) * tk;
@@ -2137,7 +2138,7 @@ class Engine final : public IEngine {
     CK(cudaMemsetAsync(PPb_.p, 0, PPb_.bytes, st_));
     CK(cudaMemsetAsync(Xb_.p, 0, Xb_.bytes, st_));
     CK(cudaMemsetAsync(Tphb_.p, 0, Tphb_.bytes, st_));
-    CK(cudaMemsetAsync(Rphb_.p, 0, Rphb_.bytes, st_));
+    CK(cudaMemsetAsync(Rringb_.p, 0, Rringb_.bytes, st_));
     CK(cudaMemcpyAsync(I4b_.p, W_.p, std::max<int64_t>(n_i4_, 1) * sizeof(S), cudaMemcpyDeviceToDevice, st_));
     run_split(spTphb_);
   }
@@ -2187,7 +2188,7 @@ class Engine final : public IEngine {
     join_side(xs);
     if (xs != st_) run_plan(planHH_, xs);  // HH_b = T' I9' beside the pp-ladder product
     launch_rinit<S>(D_, omap_.as<int4>(), rmap_.as<int4>(), T_.as<S>(), Vhp_.as<S>(), Rph_.as<S>(), i6off_.as<S>(),
-                    i7off_.as<S>(), R_.as<S>(), st_);
+                    i7off_.as<S>(), nullptr, Rringb_.as<S>(), R_.as<S>(), st_);
     mark(6);
     if (digits) {
       kbegin(kKSplit);
@@ -2215,7 +2216,6 @@ class Engine final : public IEngine {
     CK(cudaMemcpyAsync(Xb_.p, X_.p, std::max<int64_t>(n_hh2_, 1) * sizeof(S), cudaMemcpyDeviceToDevice, st_));
     CK(cudaMemcpyAsync(Tb_.p, T_.p, n_t_ * sizeof(S), cudaMemcpyDeviceToDevice, st_));
     CK(cudaMemcpyAsync(Tphb_.p, Tph_.p, std::max<int64_t>(n_ph_, 1) * sizeof(S), cudaMemcpyDeviceToDevice, st_));
-    CK(cudaMemcpyAsync(Rphb_.p, Rph_.p, std::max<int64_t>(n_ph_, 1) * sizeof(S), cudaMemcpyDeviceToDevice, st_));
     CK(cudaMemcpyAsync(I4b_.p, I4_.p, std::max<int64_t>(n_i4_, 1) * sizeof(S), cudaMemcpyDeviceToDevice, st_));
     run_split(spTphb_);
     mark(7);
@@ -2261,12 +2261,12 @@ class Engine final : public IEngine {
     kend();
     mark(4);
     kbegin(kKTcRing);
-    run_tc(tcR1_);  // R_ph = R_ph,b + T_ph,b dI4 + dT_ph I4
+    run_tc(tcR1_);  // dR_ph = T_ph,b dI4 + dT_ph I4 (R_ph,b enters through the stored ring terms)
     kend();
     mark(5);
     join_side(xs);
     launch_rinit<S>(D_, omap_.as<int4>(), rmap_.as<int4>(), T_.as<S>(), Vhp_.as<S>(), Rph_.as<S>(), i6off_.as<S>(),
-                    i7off_.as<S>(), R_.as<S>(), st_);
+                    i7off_.as<S>(), Rringb_.as<S>(), nullptr, R_.as<S>(), st_);
     mark(6);
     kbegin(kKTcPP);
     run_tc(tcPP_);  // R' += PP_b + HH_b + V_pppp' dT' + dT' I9' + T_b' (I9' - I9_b')
@@ -2312,7 +2312,7 @@ class Engine final : public IEngine {
   bool mixed_ready_ = false;
   int tc_kind_ = 0;
   int64_t v_version_ = 0, mixed_v_version_ = -1;
-  DBuf Tb_, PPb_, Tphb_, Rphb_, I4b_, dI4_, tcerr_, Xb_, dI9_, HHb_, xd7_;
+  DBuf Tb_, PPb_, Tphb_, Rringb_, I4b_, dI4_, tcerr_, Xb_, dI9_, HHb_, xd7_;
   OzBuf ozVpp_, ozTb_, ozVph_, ozTphB_, ozTphA_, ozI4B_;
   OzSplitPlan ozsV_, ozsTb_, ozsTph_, ozsI4_;
   OzPlan ozPP_, ozI4_, ozRing_;

@@ -48,7 +48,7 @@ enum KernelSlot {
   kKHH64 = 5,   // k_gemm: T' I9' hh-ladder of the mixed-precision residual (FP64)
   kKTcPP = 6,   // k_tc_gemm: V_pppp' dT' + dT' I9' + T_b' dI9' + PP_b + HH_b, one launch
   kKTcI4 = 7,   // k_tc_gemm: dI4 = 1/2 V_ph dT_ph
-  kKTcRing = 8, // k_tc_gemm: R_ph = R_ph,b + T_ph,b dI4 + dT_ph I4, one launch
+  kKTcRing = 8, // k_tc_gemm: dR_ph = T_ph,b dI4 + dT_ph I4, one launch
   kKSplit = 9,  // k_tc_split: per-iteration operand splits
   kKPPOz = 10,  // k_oz_gemm: V_pppp' T' at a re-base as exact digit products
   kKI4Oz = 11,  // k_oz_gemm: I4 at a re-base as exact digit products

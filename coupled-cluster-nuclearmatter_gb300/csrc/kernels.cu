@@ -689,7 +689,8 @@ __device__ __forceinline__ S at_or_zero(const S *__restrict__ X, int m) {
 template <typename S>
 __global__ void k_rinit(DevLayout L, const int4 *__restrict__ omap, const int4 *__restrict__ rmap, const S *__restrict__ T,
                         const S *__restrict__ Vhp, const S *__restrict__ Rph, const S *__restrict__ i6off,
-                        const S *__restrict__ i7off, S *__restrict__ R) {
+                        const S *__restrict__ i7off, const S *__restrict__ ring_base, S *__restrict__ ring_out,
+                        S *__restrict__ R) {
   const int2 tl = L.ttile[blockIdx.x];
   const int ch = tl.x;
   const int P = L.P[ch], H = L.H[ch];
@@ -713,14 +714,17 @@ __global__ void k_rinit(DevLayout L, const int4 *__restrict__ omap, const int4 *
       if (o.z) r -= i7off[ho.y] * signed_at(T, o.z);
       if (o.w) r += i7off[ho.x] * signed_at(T, o.w);
     }
-    r += at_or_zero(Rph, m.x) - at_or_zero(Rph, m.y) - at_or_zero(Rph, m.z) + at_or_zero(Rph, m.w);
+    const S ring = at_or_zero(Rph, m.x) - at_or_zero(Rph, m.y) - at_or_zero(Rph, m.z) + at_or_zero(Rph, m.w);
+    if (ring_out) ring_out[base + e] = ring;  // the ring term of this R_ph, kept per amplitude
+    r += ring_base ? ring_base[base + e] + ring : ring;
     R[base + e] = r;
   }
 }
 template <typename S>
 void launch_rinit(const DevLayout &L, const int4 *omap, const int4 *rmap, const S *T, const S *Vhp, const S *Rph,
-                  const S *i6off, const S *i7off, S *R, cudaStream_t st) {
-  if (L.nttile) k_rinit<S><<<L.nttile, 256, 0, st>>>(L, omap, rmap, T, Vhp, Rph, i6off, i7off, R);
+                  const S *i6off, const S *i7off, const S *ring_base, S *ring_out, S *R, cudaStream_t st) {
+  if (L.nttile)
+    k_rinit<S><<<L.nttile, 256, 0, st>>>(L, omap, rmap, T, Vhp, Rph, i6off, i7off, ring_base, ring_out, R);
 }
 
 // ============================================================================
@@ -1387,7 +1391,7 @@ void launch_unpack_t(const DevLayout &L, int ch, int n_pp, const int *pp_signed,
   template void launch_i6<S>(const DevLayout &, const int2 *, int, S *, const S *, const S *, const S *, const S *,   \
                              S *, S *, cudaStream_t);                                                                  \
   template void launch_rinit<S>(const DevLayout &, const int4 *, const int4 *, const S *, const S *, const S *,      \
-                               const S *, const S *, S *, cudaStream_t);                                                                         \
+                               const S *, const S *, const S *, S *, S *, cudaStream_t);                                                         \
   template void launch_update<S>(const DevLayout &, int, S *, const S *, const S *, const S *, const S *, S *,         \
                                  typename StepOf<S>::type *,                                                            \
                                  double *, double *, cudaStream_t);                                                    \

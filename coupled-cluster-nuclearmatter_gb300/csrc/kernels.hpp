@@ -80,11 +80,13 @@ constexpr int kI6Rows = 128;
 constexpr int kI6Parts = 4;  // threads per row: interleaved slices of the hole-pair sum
 template <typename S> void launch_i6(const DevLayout &L, const int2 *rowtile, int nrowtile, S *D, const S *T, const S *Vhp,
                                      const S *fdiag, const S *f6, S *d2ab, S *i6off, cudaStream_t st);
-// R' initialisation; omap / rmap (int4 per packed amplitude) from launch_rinit_maps
+// R' initialisation; omap / rmap (int4 per packed amplitude) from launch_rinit_maps.
+// The ring term gathered from Rph is stored per amplitude into ring_out when given, and
+// ring_base (per amplitude) is added to it when given: a ring split as R_ph,b + dR_ph.
 void launch_rinit_maps(const DevLayout &L, int4 *omap, int4 *rmap, cudaStream_t st);
 template <typename S>
 void launch_rinit(const DevLayout &L, const int4 *omap, const int4 *rmap, const S *T, const S *Vhp, const S *Rph,
-                  const S *i6off, const S *i7off, S *R, cudaStream_t st);
+                  const S *i6off, const S *i7off, const S *ring_base, S *ring_out, S *R, cudaStream_t st);
 
 // ---- update / energy / norms (per-block partial sums, then a fixed-order finish) --
 // mode 0: reference update T <- 0.75 T + 0.25 R/D, history column written

@@ -367,7 +367,7 @@ int ccx_engine_timers(const ccx_engine *e, double ms[10]);
  * [3] fused pp+hh ladder (FP64), [4] V_pppp' T' at a mixed-precision re-base (FP64),
  * [5] hh-ladder of the mixed residual (FP64), [6] pp-ladder and hh-ladder corrections
  * with the cached base terms, one launch (tensor cores), [7] dI4 correction (tensor
- * cores), [8] ring corrections with the cached base ring, one launch (tensor cores),
+ * cores), [8] ring corrections dR_ph, one launch (tensor cores),
  * [9] operand splits, [10] pp-ladder, [11] I4 and [12] ring at a re-base as digit products
  * (tensor cores), [13] I7 of a mixed residual from the X entries it reads (FP64 column
  * dots), [14] .. [15] unused */
