@@ -255,11 +255,13 @@ class Engine final : public IEngine {
     launch_pack_vblock_host<S>(D_, kind, target, rows, rp, cp, src, dst, flag_.as<int>(), st_);
     ++launches_;
     dirty_ = true;
+    user_set_ |= 1u << kind;
     ++v_version_;
   }
   // HPHP blocks in device-addressable host memory: one batched copy launch
   void set_v4_direct(int n, const int *chs, double *const *src) {
     const Layout &L = *L_;
+    adopt_hphp();
     std::vector<CopyJob> jobs(n);
     for (int i = 0; i < n; ++i) {
       check_ch(chs[i], L.fam[4].count());
@@ -272,6 +274,7 @@ class Engine final : public IEngine {
     CK(cudaStreamSynchronize(st_));  // the job table on the host goes out of scope
     ++launches_;
     dirty_ = true;
+    user_set_ |= 1u << 4;
     ++v_version_;
   }
   // Many blocks of one kind with one synchronisation at the end.  Staged blocks
@@ -341,9 +344,11 @@ class Engine final : public IEngine {
       }
       case 4: {
         check_ch(ch, L.fam[4].count());
+        adopt_hphp();
         const int n = L.fam[4].side1[ch].size();
         CK(cudaMemcpyAsync(v4_.as<double>() + 2 * v4_off_h_[ch], v, (size_t)n * n * 2 * sizeof(double),
                            cudaMemcpyHostToDevice, st_));
+        user_set_ |= 1u << 4;
         dirty_ = true;
         ++v_version_;
         return;
@@ -379,6 +384,7 @@ class Engine final : public IEngine {
     }
     ++launches_;
     dirty_ = true;
+    user_set_ |= 1u << kind;
     ++v_version_;
   }
 
@@ -397,11 +403,39 @@ class Engine final : public IEngine {
     e0_[1] = host_res_[1];
     have_fock_ = true;
     generated_ = true;
+    w_generated_ = true;
+    user_set_ = 0;
     pot_ = pot;
     dirty_ = true;
     ++v_version_;
     vph_ready_ = false;
     commit();
+  }
+  // The first caller HPHP block on a generated engine: W is rebuilt from the stored
+  // reference-layout blocks from now on, so every HPHP block of the generated
+  // interaction is written there first (channels the caller does not set keep it).
+  void adopt_hphp() {
+    if (!w_generated_) return;
+    const Layout &L = *L_;
+    const ChannelFamily &F = L.fam[4];
+    std::vector<int2> pairs;
+    std::vector<int64_t> first(F.count());
+    for (int ch = 0; ch < F.count(); ++ch) {
+      first[ch] = (int64_t)pairs.size();
+      const PairList &pl = F.side1[ch];
+      for (int i = 0; i < pl.size(); ++i) pairs.push_back(make_int2(pl.p[i], pl.q[i]));
+    }
+    DBuf dp;
+    upload(dp, pairs, nullptr);
+    for (int ch = 0; ch < F.count(); ++ch) {
+      const int n = F.side1[ch].size();
+      if (n <= 0) continue;
+      const int2 *pr = dp.as<int2>() + first[ch];
+      launch_gen_ordered<S>(O_, pot_, pr, pr, n, n, 0, v4_.as<double>() + 2 * v4_off_h_[ch], st_);
+      ++launches_;
+    }
+    CK(cudaStreamSynchronize(st_));  // the pair table goes out of scope
+    w_generated_ = false;
   }
   void get_e0(double e0[2]) override { e0[0] = e0_[0]; e0[1] = e0_[1]; }
   void *stream() const override { return (void *)st_; }
@@ -425,7 +459,12 @@ class Engine final : public IEngine {
     const int nr = rows.size(), nc = cols.size();
     const size_t bytes = (size_t)nr * nc * 2 * sizeof(double);
     if (bytes > stage_.bytes) stage_.alloc(bytes, &bytes_);
-    if (generated_) {
+    if (kind == 4 && !w_generated_ && (user_set_ >> 4 & 1u)) {  // the caller's HPHP block, as stored
+      CK(cudaMemcpyAsync(v, v4_.as<double>() + 2 * v4_off_h_[ch], bytes, cudaMemcpyDeviceToHost, st_));
+      CK(cudaStreamSynchronize(st_));
+      return;
+    }
+    if (generated_ && !(user_set_ >> kind & 1u)) {
       std::vector<int2> r(nr), c(nc);
       for (int i = 0; i < nr; ++i) r[i] = make_int2(rows.p[i], rows.q[i]);
       for (int i = 0; i < nc; ++i) c[i] = make_int2(cols.p[i], cols.q[i]);
@@ -676,7 +715,7 @@ class Engine final : public IEngine {
     if (!dirty_ && vph_ready_) return;
     launch_build_vph<S>(D_, Vhp_.as<S>(), Vph_.as<S>(), st_);
     ++launches_;
-    if (!generated_) {
+    if (!w_generated_) {
       launch_build_w<S>(D_, hp4_slot_.as<int2>(), v4_off_.as<int64_t>(), n4_.as<int>(), v4_.as<double>(), W_.as<S>(),
                         flag_.as<int>(), st_);
       ++launches_;
@@ -2332,6 +2371,9 @@ class Engine final : public IEngine {
   double e0_[2] = {0, 0};
   double last_rn_ = 0.0;
   bool have_fock_ = false, have_t_ = false, dirty_ = true, vph_ready_ = false, generated_ = false;
+  // W built on the device by generate(); caller V block kinds since then (bit = kind)
+  bool w_generated_ = false;
+  unsigned user_set_ = 0;
   int subspace_ = 0, diis_step_ = 6, nstep_ = 0;
   std::vector<int> phys_;
   std::unique_ptr<ITriples<S>> tr_;

@@ -195,6 +195,8 @@ typedef struct {
   uint64_t lec_seed;         /* chiral-like contact LEC draw */
   int32_t f32_literals;      /* 1: Minnesota constants rounded to 4-byte reals like the reference */
 } ccx_potential;
+/* Blocks set with ccx_set_vblock(s) after this call replace the generated ones of their
+ * channels; the other channels of every family keep the generated interaction. */
 int ccx_generate_interaction(ccx_engine *e, const ccx_potential *pot);
 /* E0 = sum_i t_ii + 1/2 sum_ij <ij|V|ij> (ccm_main.f90:1661-1684) of the interaction
  * generated on the device, or the value passed to ccx_set_fock */

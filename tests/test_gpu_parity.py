@@ -357,3 +357,33 @@ def test_profiling_switch_keeps_results(ccx, O, prec, rebase):
     assert t1["update"] > 0 and t1["ladders"] > 0 and sum(n for _, n in k1.values()) > 0
     assert r0["converged"] and r1["iterations"] == r0["iterations"]
     assert abs(r1["e_ccd"] - r0["e_ccd"]) <= 1e-13 * abs(r0["e_ccd"])
+
+
+def test_replayed_residuals_follow_plan_and_interaction_changes(ccx, O):
+    """The residual kinds replay captured CUDA graphs.  A tile-shape autotune (new FP64
+    plans) and new V blocks between mixed solves must give what a fresh engine gives."""
+    o, L, e = make(ccx, O, **C1)
+    kw = dict(mode=ccx.MODE_STANDARD, tol=1e-10, precision=ccx.PREC_MIXED, rebase=ccx.REBASE_DIGITS)
+    e.setup_t_amplitudes()
+    r0 = e.ccd_iter(**kw)
+    e.autotune()
+    e.setup_t_amplitudes()
+    r1 = e.ccd_iter(**kw)
+    assert r0["converged"] and r1["iterations"] == r0["iterations"]
+    assert abs(r1["e_ccd"] - r0["e_ccd"]) < 1e-12 * abs(r0["e_ccd"])
+    # a 10% weaker interaction, handed over to the engine that has replayed its graphs
+    # and to a fresh one
+    s = 0.9
+    fresh = ccx.Engine(L, real=True)
+    for eng in (e, fresh):
+        eng.set_fock(o.fock(), o.e0())
+        eng.set_vblocks(ccx.CH_HHPP, {c: s * o.v_hhpp(c) for c in range(o.n_channels(3))})
+        eng.set_vblocks(ccx.V_PPPP, {c: s * o.v_pppp(c) for c in range(o.n_channels(3))})
+        eng.set_vblocks(ccx.CH_HHHH, {c: s * o.v_hhhh(c) for c in range(o.n_channels(1))})
+        eng.set_vblocks(ccx.CH_HPHP, {c: s * o.v_hphp(c) for c in range(o.n_channels(4))})
+        eng.setup_t_amplitudes()
+    r2 = e.ccd_iter(**kw)
+    r3 = fresh.ccd_iter(**kw)
+    assert r2["converged"] and r3["converged"]
+    assert abs(r2["e_ccd"] - r0["e_ccd"]) > 1e-3 * abs(r0["e_ccd"])  # the new V is in use
+    assert abs(r2["e_ccd"] - r3["e_ccd"]) < 1e-11 * abs(r3["e_ccd"])
