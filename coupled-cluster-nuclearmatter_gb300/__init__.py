@@ -25,6 +25,7 @@ POT_MINNESOTA, POT_CHIRAL_LIKE = 0, 1
 MODE_REFERENCE, MODE_STANDARD = 0, 1
 PREC_FP64, PREC_MIXED, PREC_MIXED_TF32 = 0, 1, 2
 REBASE_FP64, REBASE_DIGITS = 0, 1
+CKPT_ANY_TWIST = 1
 SCALAR_COMPLEX, SCALAR_REAL = 0, 1
 
 
@@ -117,6 +118,8 @@ def lib():
         "ccx_get_t2": ([vp, i32, vp], C.c_int),
         "ccx_get_t2_eqn": ([vp, i32, vp], C.c_int),
         "ccx_set_t2_all": ([vp, vp], C.c_int),
+        "ccx_t2_checkpoint_write": ([vp, C.c_char_p, vp], C.c_int),
+        "ccx_t2_checkpoint_read": ([vp, C.c_char_p, i32, vp], C.c_int),
         "ccx_get_t2_all": ([vp, vp], C.c_int),
         "ccx_get_denominators": ([vp, vp, vp], C.c_int),
         "ccx_t2_intermediate": ([vp], C.c_int),
@@ -362,6 +365,20 @@ class Layout:
         _check(lib().ccx_layout_pairs(self._h, kind, ch, _ptr(a), _ptr(b)))
         return a[:n1], b[:n2]
 
+    def write_t2_checkpoint(self, path: str, t2_all: np.ndarray) -> None:
+        """Write amplitudes of this lattice (the t2_all() vector) to a checkpoint file."""
+        z = np.ascontiguousarray(np.asarray(t2_all, np.complex128)).view(np.float64)
+        if z.size != 2 * self.counts()["amps"]:
+            raise CcxError(1, "amplitude vector does not match the lattice")
+        _check(lib().ccx_t2_checkpoint_write(self._h, os.fsencode(path), _ptr(z)))
+
+    def read_t2_checkpoint(self, path: str, any_twist: bool = False) -> np.ndarray:
+        """Amplitudes of this lattice from a checkpoint file; any_twist accepts the same
+        channel structure at another twist or box length."""
+        z = np.zeros(2 * self.counts()["amps"])
+        _check(lib().ccx_t2_checkpoint_read(self._h, os.fsencode(path), CKPT_ANY_TWIST if any_twist else 0, _ptr(z)))
+        return z.view(np.complex128)
+
     def hash(self) -> int:
         h = C.c_uint64()
         _check(lib().ccx_layout_hash(self._h, C.byref(h)))
@@ -477,6 +494,14 @@ class Engine:
     def set_t2_all(self, flat: np.ndarray):
         z = np.ascontiguousarray(np.asarray(flat, np.complex128)).view(np.float64)
         _check(lib().ccx_set_t2_all(self._h, _ptr(z)))
+
+    def save_t2(self, path: str) -> None:
+        """Checkpoint the current amplitudes (resume a solve, or harvest them)."""
+        self.layout.write_t2_checkpoint(path, self.t2_all())
+
+    def load_t2(self, path: str, any_twist: bool = False) -> None:
+        """Amplitudes from a checkpoint of this lattice (any_twist: of another twist)."""
+        self.set_t2_all(self.layout.read_t2_checkpoint(path, any_twist))
 
     def denominators(self):
         orb = self.layout.orbits()

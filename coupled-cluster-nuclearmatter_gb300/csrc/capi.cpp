@@ -11,6 +11,7 @@
 #include <vector>
 
 #include "ccx.h"
+#include "checkpoint.hpp"
 #include "engine.hpp"
 #include "layout.hpp"
 
@@ -323,6 +324,16 @@ int ccx_layout_hash(const ccx_layout *l, uint64_t *h) {
   if (!l || !h) return fail(CCX_EINVAL, "null argument");
   *h = l->L->hash();
   return CCX_OK;
+}
+
+int ccx_t2_checkpoint_write(const ccx_layout *l, const char *path, const double *t2) {
+  if (!l || !path || !t2) return fail(CCX_EINVAL, "null argument");
+  return guard([&] { ccx::write_t2_checkpoint(*l->L, path, t2); });
+}
+int ccx_t2_checkpoint_read(const ccx_layout *l, const char *path, int32_t flags, double *t2) {
+  if (!l || !path || !t2) return fail(CCX_EINVAL, "null argument");
+  if (flags & ~CCX_CKPT_ANY_TWIST) return fail(CCX_EINVAL, "unknown checkpoint flags");
+  return guard([&] { ccx::read_t2_checkpoint(*l->L, path, (flags & CCX_CKPT_ANY_TWIST) != 0, t2); });
 }
 
 int ccx_engine_create(const ccx_layout *l, const ccx_engine_options *opt, ccx_engine **out) {

@@ -223,6 +223,17 @@ int ccx_get_t2_eqn(ccx_engine *e, int32_t ch, double *r);
  * unpacks straight into pinned device-addressable host memory, one synchronisation */
 int ccx_set_t2_all(ccx_engine *e, const double *t);
 int ccx_get_t2_all(ccx_engine *e, double *t);
+/* T2 checkpoint files (host only, no engine or GPU needed): the ccx_get_t2_all buffer
+ * (2 * n_amps doubles) behind a header with the layout hash, a hash of the orbital
+ * momenta and box length (the twist), and a checksum of the data.  The write goes to
+ * path + ".part" and is renamed into place.  The read checks magic, version, byte
+ * order, lattice (layout hash, states, holes, amplitude count), the momenta and box
+ * length unless CCX_CKPT_ANY_TWIST is given (a twist that reorders the orbitals changes
+ * the layout hash as well), and the checksum; on any error t2 is left untouched and
+ * CCX_EINVAL is returned.  Not in the reference (its runs always start from MP2). */
+#define CCX_CKPT_ANY_TWIST 1
+int ccx_t2_checkpoint_write(const ccx_layout *l, const char *path, const double *t2);
+int ccx_t2_checkpoint_read(const ccx_layout *l, const char *path, int32_t flags, double *t2);
 /* d2ij(1:A), d2ab(A+1:n) of the last residual, complex interleaved */
 int ccx_get_denominators(ccx_engine *e, double *d2ij, double *d2ab);
 

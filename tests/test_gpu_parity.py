@@ -387,3 +387,20 @@ def test_replayed_residuals_follow_plan_and_interaction_changes(ccx, O):
     assert r2["converged"] and r3["converged"]
     assert abs(r2["e_ccd"] - r0["e_ccd"]) > 1e-3 * abs(r0["e_ccd"])  # the new V is in use
     assert abs(r2["e_ccd"] - r3["e_ccd"]) < 1e-11 * abs(r3["e_ccd"])
+
+
+def test_checkpoint_resumes_a_converged_solve(ccx, O, tmp_path):
+    """Amplitudes saved after a converged solve and loaded into a fresh engine of the same
+    lattice: the loaded engine is already converged (one FP64 sweep confirms it)."""
+    o, L, e = make(ccx, O, **C1)
+    e.setup_t_amplitudes()
+    r0 = e.ccd_iter(mode=ccx.MODE_STANDARD, tol=1e-10)
+    p = str(tmp_path / "c1.t2")
+    e.save_t2(p)
+    f = ccx.Engine(L, real=True)
+    f.generate()
+    f.load_t2(p)
+    assert np.array_equal(f.t2_all(), e.t2_all())
+    r1 = f.ccd_iter(mode=ccx.MODE_STANDARD, tol=1e-10)
+    assert r1["converged"] and r1["iterations"] <= 1
+    assert abs(r1["e_ccd"] - r0["e_ccd"]) < 1e-11 * abs(r0["e_ccd"])
