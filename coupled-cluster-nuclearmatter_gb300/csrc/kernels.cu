@@ -1273,21 +1273,6 @@ __global__ void k_axpy(int64_t n, const S *__restrict__ x, S *__restrict__ y) {
 template <typename S> void launch_axpy(int64_t n, const S *x, S *y, cudaStream_t st) {
   if (n > 0) k_axpy<S><<<(int)std::min<int64_t>((n + 255) / 256, 2432), 256, 0, st>>>(n, x, y);
 }
-template <typename S>
-__global__ void k_add(int64_t n, const S *__restrict__ x, const S *__restrict__ y, S *__restrict__ z) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) z[i] = x[i] + y[i];
-}
-template <typename S> void launch_add(int64_t n, const S *x, const S *y, S *z, cudaStream_t st) {
-  if (n > 0) k_add<S><<<(int)std::min<int64_t>((n + 255) / 256, 2432), 256, 0, st>>>(n, x, y, z);
-}
-template <typename S>
-__global__ void k_sub(int64_t n, const S *__restrict__ x, const S *__restrict__ y, S *__restrict__ z) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    z[i] = x[i] - y[i];
-}
-template <typename S> void launch_sub(int64_t n, const S *x, const S *y, S *z, cudaStream_t st) {
-  if (n > 0) k_sub<S><<<(int)std::min<int64_t>((n + 255) / 256, 2432), 256, 0, st>>>(n, x, y, z);
-}
 
 // register-only FMA chains; one store per thread
 __global__ void k_fp64_probe(double *out, int iters) {
@@ -1409,8 +1394,6 @@ void launch_unpack_t(const DevLayout &L, int ch, int n_pp, const int *pp_signed,
   template void launch_mp2<S>(const DevLayout &, const S *, const S *, S *, cudaStream_t);                            \
   template void launch_pack_t<S>(const DevLayout &, int, int, const double *, S *, int *, cudaStream_t);          \
   template void launch_axpy<S>(int64_t, const S *, S *, cudaStream_t);                                                 \
-  template void launch_add<S>(int64_t, const S *, const S *, S *, cudaStream_t);                                       \
-  template void launch_sub<S>(int64_t, const S *, const S *, S *, cudaStream_t);                                       \
   template void launch_gen_ordered<S>(const DevOrbits &, const DevPotential &, const int2 *, const int2 *, int, int,  \
                                       int, double *, cudaStream_t);                                                    \
   template void launch_unpack_vblock<S>(const DevLayout &, int, int, int, int, const int *, const int *, const S *,  \

@@ -150,11 +150,8 @@ template <typename S>
 void launch_unpack_vblock(const DevLayout &L, int kind, int ch, int n_rows, int n_cols, const int *row_sgn,
                           const int *col_sgn, const S *src, double *out, cudaStream_t st);
 double measure_fp64_peak(int device);
-// y += x ; z = x + y (n elements)
+// y += x (n elements)
 template <typename S> void launch_axpy(int64_t n, const S *x, S *y, cudaStream_t st);
-template <typename S> void launch_add(int64_t n, const S *x, const S *y, S *z, cudaStream_t st);
-// z = x - y
-template <typename S> void launch_sub(int64_t n, const S *x, const S *y, S *z, cudaStream_t st);
 template <typename S> void launch_mp2(const DevLayout &L, const S *Vhp, const S *fdiag, S *T, cudaStream_t st);
 template <typename S> void launch_pack_t(const DevLayout &L, int ch, int n_pp, const double *stage, S *T, int *flag, cudaStream_t st);
 template <typename S>
