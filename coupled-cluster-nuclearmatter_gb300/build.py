@@ -1,7 +1,9 @@
 """Builds libccx.so (the CUDA engine and its C ABI) for sm_103a, in-tree.
 
 Sources: csrc/*.cu (nvcc) and csrc/*.cpp (host C++), linked into build/libccx.so.
-Translation units compile in parallel; only stale objects are rebuilt.
+Translation units compile in parallel; only stale objects are rebuilt.  The host
+program harness/ccx_run.cpp, which drives the C ABI as the reference's driver drives
+its solver, links against it as build/ccx_run.
 """
 from __future__ import annotations
 
@@ -16,6 +18,8 @@ SRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "build")
 INC = os.path.join(os.path.dirname(HERE), "include")
 LIB = os.path.join(OUT, "libccx.so")
+RUN_SRC = os.path.join(HERE, "harness", "ccx_run.cpp")
+RUN = os.path.join(OUT, "ccx_run")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -76,6 +80,9 @@ def build(verbose: bool = False) -> str:
         list(ex.map(run, jobs))
     if jobs or not os.path.exists(LIB):
         run([nvcc, *ARCH, "-shared", "-o", LIB, *objs, "-lcudart"])
+    if _stale(RUN, RUN_SRC, [LIB, os.path.join(INC, "ccx.h")]):
+        run(["g++", "-std=c++17", "-O2", "-Wall", f"-I{INC}", RUN_SRC, "-o", RUN, f"-L{OUT}", "-lccx",
+             "-Wl,-rpath,$ORIGIN"])
     return LIB
 
 
