@@ -35,7 +35,7 @@ struct Args {
   std::string deck, load, save, blocks = "generated", loop, mode, precision, rebase = "digits", pot;
   int nmax = -1, A = -1, snm = -1, device = 0, max_iter = -1, diis = 8, scalar = -1;
   double density = -1.0, theta[3] = {0, 0, 0}, tol = -1.0;
-  bool triples = false, layout_only = false, has_theta = false;
+  bool triples = false, layout_only = false, has_theta = false, f64_literals = false;
 };
 
 [[noreturn]] void usage(const char *msg) {
@@ -45,7 +45,7 @@ struct Args {
                "               [--potential minnesota|chiral_like] [--real|--complex] [--blocks generated|host]\n"
                "               [--loop shim|solver] [--mode reference|standard] [--precision fp64|bf16x3|tf32x3]\n"
                "               [--rebase fp64|digits] [--tol T] [--max-iter N] [--diis N] [--triples]\n"
-               "               [--load FILE] [--save FILE] [--device D] [--layout-only]\n");
+               "               [--load FILE] [--save FILE] [--device D] [--layout-only] [--f64-literals]\n");
   std::exit(2);
 }
 
@@ -96,6 +96,7 @@ Args parse(int argc, char **argv) {
     else if (k == "--save") a.save = val("--save");
     else if (k == "--device") a.device = (int)num("--device");
     else if (k == "--layout-only") a.layout_only = true;
+    else if (k == "--f64-literals") a.f64_literals = true;
     else if (k == "-h" || k == "--help") usage(nullptr);
     else usage(("unknown option " + k).c_str());
   }
@@ -205,6 +206,9 @@ int main(int argc, char **argv) {
   ccx_potential p{};
   p.kind = pot == "chiral_like" ? CCX_POT_CHIRAL_LIKE : CCX_POT_MINNESOTA;
   p.lec_seed = have_deck ? d.lec_seed : 20261203ull;
+  // the reference writes the Minnesota constants and the nucleon mass as default-real
+  // (4-byte) literals; --f64-literals keeps them in double precision
+  p.f32_literals = a.f64_literals ? 0 : 1;
   ccx_engine_options eo{};
   eo.device = a.device;
   eo.scalar = a.scalar >= 0 ? a.scalar : (p.kind == CCX_POT_CHIRAL_LIKE ? CCX_SCALAR_COMPLEX : CCX_SCALAR_REAL);
