@@ -27,7 +27,7 @@ typedef double _Complex zd;
 #define HBARC 197.326968
 #define P_MASS ((double)939.565f)
 
-/* chiral-like synthetic potential constants (BASELINE config C3) */
+/* chiral-like synthetic potential constants (the complex SNM workloads) */
 #define CL_GA 1.27
 #define CL_FPI 92.4
 #define CL_MPI 138.0

@@ -6,7 +6,7 @@ import os
 import numpy as np
 import pytest
 
-C1 = dict(nmax=1, A=14, density=0.08)
+PNM14_NMAX1 = dict(nmax=1, A=14, density=0.08)
 
 
 def amps(ccx, L, seed=7):
@@ -16,7 +16,7 @@ def amps(ccx, L, seed=7):
 
 
 def test_round_trip_is_bit_exact(ccx, tmp_path):
-    L = ccx.Layout.from_basis(**C1)
+    L = ccx.Layout.from_basis(**PNM14_NMAX1)
     t = amps(ccx, L)
     p = str(tmp_path / "t2.ckpt")
     L.write_t2_checkpoint(p, t)
@@ -25,11 +25,11 @@ def test_round_trip_is_bit_exact(ccx, tmp_path):
     back = L.read_t2_checkpoint(p)
     assert np.array_equal(back.view(np.float64), t.view(np.float64))
     # a second layout object of the same lattice reads it too
-    assert np.array_equal(ccx.Layout.from_basis(**C1).read_t2_checkpoint(p), t)
+    assert np.array_equal(ccx.Layout.from_basis(**PNM14_NMAX1).read_t2_checkpoint(p), t)
 
 
 def test_other_lattice_is_refused(ccx, tmp_path):
-    L = ccx.Layout.from_basis(**C1)
+    L = ccx.Layout.from_basis(**PNM14_NMAX1)
     p = str(tmp_path / "t2.ckpt")
     L.write_t2_checkpoint(p, amps(ccx, L))
     other = ccx.Layout.from_basis(nmax=2, A=14, density=0.08)
@@ -40,7 +40,7 @@ def test_other_lattice_is_refused(ccx, tmp_path):
 
 def test_other_momenta_need_the_flag(ccx, tmp_path):
     # another density: the same orbitals and channel tables, other momenta and box
-    L0 = ccx.Layout.from_basis(**C1)
+    L0 = ccx.Layout.from_basis(**PNM14_NMAX1)
     L1 = ccx.Layout.from_basis(nmax=1, A=14, density=0.16)
     assert L0.hash() == L1.hash()
     t = amps(ccx, L0)
@@ -53,7 +53,7 @@ def test_other_momenta_need_the_flag(ccx, tmp_path):
 
 
 def test_corrupted_truncated_and_missing_files(ccx, tmp_path):
-    L = ccx.Layout.from_basis(**C1)
+    L = ccx.Layout.from_basis(**PNM14_NMAX1)
     t = amps(ccx, L)
     p = str(tmp_path / "t2.ckpt")
     L.write_t2_checkpoint(p, t)
@@ -84,7 +84,7 @@ def test_corrupted_truncated_and_missing_files(ccx, tmp_path):
 
 def test_failed_read_leaves_the_buffer_untouched(ccx, tmp_path):
     import ctypes as C
-    L = ccx.Layout.from_basis(**C1)
+    L = ccx.Layout.from_basis(**PNM14_NMAX1)
     p = str(tmp_path / "t2.ckpt")
     L.write_t2_checkpoint(p, amps(ccx, L))
     with open(p, "r+b") as f:  # corrupt the last amplitude

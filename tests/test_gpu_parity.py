@@ -11,7 +11,7 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-C1 = dict(nmax=2, A=14, rho=0.08, snm=False)
+PNM14 = dict(nmax=2, A=14, rho=0.08, snm=False)
 
 
 def make(ccx, O, nmax, A, rho, snm=False, pot=0, real=True, theta=(0.0, 0.0, 0.0)):
@@ -37,7 +37,7 @@ def check_blocks(o, e, get_o, get_e, tol):
 
 
 def test_e0_and_mp2(ccx, O):
-    o, L, e = make(ccx, O, **C1)
+    o, L, e = make(ccx, O, **PNM14)
     assert abs(e.e0() - o.e0()) < 1e-12 * abs(o.e0())
     o.mp2()
     e.setup_t_amplitudes()
@@ -46,7 +46,7 @@ def test_e0_and_mp2(ccx, O):
 
 
 def test_residual_matches_oracle_at_mp2(ccx, O):
-    o, L, e = make(ccx, O, **C1)
+    o, L, e = make(ccx, O, **PNM14)
     o.mp2()
     e.setup_t_amplitudes()
     o.t2_intermediate()
@@ -60,7 +60,7 @@ def test_residual_matches_oracle_at_mp2(ccx, O):
 
 def test_residual_matches_oracle_at_iterated_t(ccx, O):
     """Residual of a non-MP2 amplitude: the oracle's T after 4 reference steps."""
-    o, L, e = make(ccx, O, **C1)
+    o, L, e = make(ccx, O, **PNM14)
     o.mp2()
     o.diis_setup()
     cnt = 0
@@ -84,7 +84,7 @@ def test_reference_iteration_step_by_step(ccx, O):
     (ccm_diis.f90:134-173) whose condition number is ~1e15 here, so a different
     summation order alone moves the extrapolated energy by ~1e-7 relative; after the
     first DIIS step the trajectories are compared at the spec bar (1e-6)."""
-    o, L, e = make(ccx, O, **C1)
+    o, L, e = make(ccx, O, **PNM14)
     o.mp2()
     e.setup_t_amplitudes()
     o.diis_setup(6, 6)
@@ -102,7 +102,7 @@ def test_reference_iteration_step_by_step(ccx, O):
 
 
 def test_ccd_iter_reference_mode(ccx, O):
-    o, L, e = make(ccx, O, **C1)
+    o, L, e = make(ccx, O, **PNM14)
     o.mp2()
     e.setup_t_amplitudes()
     ro = o.ccd_iter(mode=O.MODE_REFERENCE)
@@ -114,7 +114,7 @@ def test_ccd_iter_reference_mode(ccx, O):
 
 
 def test_ccd_iter_standard_mode_converges_to_1e10(ccx, O):
-    o, L, e = make(ccx, O, **C1)
+    o, L, e = make(ccx, O, **PNM14)
     o.mp2()
     e.setup_t_amplitudes()
     ro = o.ccd_iter(mode=O.MODE_STANDARD, tol=1e-10)
@@ -128,7 +128,7 @@ def test_ccd_iter_standard_mode_converges_to_1e10(ccx, O):
 
 
 def test_complex_engine_matches_real_engine(ccx, O):
-    _, L, er = make(ccx, O, **C1)
+    _, L, er = make(ccx, O, **PNM14)
     ec = ccx.Engine(L, real=False)
     ec.generate()
     er.setup_t_amplitudes()
@@ -177,7 +177,7 @@ def test_iterate_before_amplitudes_is_a_state_error(ccx):
 
 
 def test_triples_matches_oracle(ccx, O):
-    o, L, e = make(ccx, O, **C1)
+    o, L, e = make(ccx, O, **PNM14)
     o.mp2()
     e.setup_t_amplitudes()
     o.ccd_iter(mode=O.MODE_STANDARD, tol=1e-10)
@@ -199,7 +199,7 @@ def test_triples_chiral_like_snm(ccx, O):
 
 def test_caller_supplied_blocks_match_generated(ccx, O):
     """The drop-in path: the Fortran host hands over fock_mtx and the vnn_* blocks."""
-    o, L, eg = make(ccx, O, **C1)
+    o, L, eg = make(ccx, O, **PNM14)
     e = ccx.Engine(L, real=True)
     e.set_fock(o.fock(), o.e0())
     for c in range(o.n_channels(3)):
@@ -229,7 +229,7 @@ def test_caller_supplied_blocks_match_generated(ccx, O):
 
 def test_set_vblocks_matches_single_blocks(ccx, O):
     """ccx_set_vblocks (one call per block family) gives the same engine as one call per block."""
-    o, L, eg = make(ccx, O, **C1)
+    o, L, eg = make(ccx, O, **PNM14)
     e1 = ccx.Engine(L, real=True)
     e2 = ccx.Engine(L, real=True)
     for e in (e1, e2):
@@ -262,7 +262,7 @@ def test_pinned_host_blocks_are_read_in_place(ccx, O):
     memory through staging copies, bit for bit."""
     torch = pytest.importorskip("torch")
     import ctypes as C
-    o, L, eg = make(ccx, O, **C1)
+    o, L, eg = make(ccx, O, **PNM14)
     e1 = ccx.Engine(L, real=True)
     e2 = ccx.Engine(L, real=True)
     for e in (e1, e2):
@@ -326,7 +326,7 @@ def test_twisted_lattice(ccx, O):
 
 def test_autotune_keeps_results(ccx, O):
     """The GEMM tile-shape autotuner only changes how the products are tiled."""
-    o, L, e = make(ccx, O, **C1)
+    o, L, e = make(ccx, O, **PNM14)
     e.setup_t_amplitudes()
     r0 = e.ccd_iter(mode=ccx.MODE_STANDARD, tol=1e-10)
     shapes, ms = e.autotune()
@@ -341,7 +341,7 @@ def test_autotune_keeps_results(ccx, O):
 def test_profiling_switch_keeps_results(ccx, O, prec, rebase):
     """Per-term event timers only observe: the solve is the same with them on (launches
     issued one by one) or off (each residual kind replayed as a captured CUDA graph)."""
-    o, L, e = make(ccx, O, **C1)
+    o, L, e = make(ccx, O, **PNM14)
     kw = dict(mode=ccx.MODE_STANDARD, tol=1e-10, precision=prec, rebase=rebase)
     for _ in range(2):  # the second solve replays the graphs captured by the first
         e.setup_t_amplitudes()
@@ -362,7 +362,7 @@ def test_profiling_switch_keeps_results(ccx, O, prec, rebase):
 def test_replayed_residuals_follow_plan_and_interaction_changes(ccx, O):
     """The residual kinds replay captured CUDA graphs.  A tile-shape autotune (new FP64
     plans) and new V blocks between mixed solves must give what a fresh engine gives."""
-    o, L, e = make(ccx, O, **C1)
+    o, L, e = make(ccx, O, **PNM14)
     kw = dict(mode=ccx.MODE_STANDARD, tol=1e-10, precision=ccx.PREC_MIXED, rebase=ccx.REBASE_DIGITS)
     e.setup_t_amplitudes()
     r0 = e.ccd_iter(**kw)
@@ -392,7 +392,7 @@ def test_replayed_residuals_follow_plan_and_interaction_changes(ccx, O):
 def test_checkpoint_resumes_a_converged_solve(ccx, O, tmp_path):
     """Amplitudes saved after a converged solve and loaded into a fresh engine of the same
     lattice: the loaded engine is already converged (one FP64 sweep confirms it)."""
-    o, L, e = make(ccx, O, **C1)
+    o, L, e = make(ccx, O, **PNM14)
     e.setup_t_amplitudes()
     r0 = e.ccd_iter(mode=ccx.MODE_STANDARD, tol=1e-10)
     p = str(tmp_path / "c1.t2")

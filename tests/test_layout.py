@@ -71,8 +71,8 @@ def test_layout_hash_changes_with_basis(ccx):
     assert h1 == h3 and h1 != h2
 
 
-def test_c2_sizes(ccx):
-    """PNM 66 at nmax=4 (1458 states): the survey's channel statistics."""
+def test_pnm66_nmax4_sizes(ccx):
+    """PNM 66 at nmax=4 (1458 states): channel counts and block sizes."""
     L = ccx.Layout.from_basis(4, 66, 0.16)
     c = L.counts()
     assert c["hhpp"] == 185
