@@ -1,20 +1,27 @@
 """Benchmark: time to a converged CCD E/A on one lattice per GPU.
 
-Workload (default): pure neutron matter, A=66 at rho=0.16 fm^-3 on the nmax=4
-lattice (9^3 momenta x 2 spins = 1458 states), synthetic Minnesota interaction,
-single twist, MP2 start.  A step is one full solve: MP2 amplitudes, then CCD
-iterations (Jacobi + DIIS(8)) until the FP64 residual ||R - D T|| < 1e-10, with the
+Workload (default, --workload snm132n4): symmetric nuclear matter, A=132 at rho=0.16
+fm^-3 on the nmax=4 lattice (9^3 momenta x 4 spin-isospin states = 2916 states), the
+synthetic chiral-like interaction (regulated one-pion exchange plus contact terms; its
+V is complex), single twist, MP2 start.  A step is one full solve: MP2 amplitudes, then
+CCD iterations (Jacobi + DIIS(8)) until the FP64 residual ||R - D T|| < 1e-10, with the
 interaction resident in HBM.  value = seconds per solve of the mixed-precision form
 (--precision bf16x3, default; tf32x3; or fp64 for the plain form), device time from
 CUDA events on the engine's stream.  The plain FP64 solve of the same lattice is timed
 beside it (plain_fp64, speedup_vs_plain_fp64), and the E/A difference between the two
 is reported in keV.  e2e = the same solve driven through the C ABI from pinned host
 buffers holding the reference-layout V blocks and Fock matrix, with the host->device
-copies and the T2 readback inside the timed region.
+copies and the T2 readback inside the timed region.  --workload pnm66 runs pure
+neutron matter A=66 at nmax=4 with the Minnesota interaction instead.
 
 --impl reference times the CPU path (the oracle restatement of the reference's
 complex<double> solver, all host cores) on a bounded sample: single CCD iterations
 of the same lattice, scaled by the reference algorithm's iteration count.
+
+--twists N runs the twist-averaged form instead: N twists of the 4x4x4 Gauss-Legendre
+grid on [-pi, pi]^3 of one lattice, each converged to ||R - D T|| < 1e-10, solved in
+lockstep batches of as many twists as the device holds, against the plain FP64 GPU
+solve of the same twists.
 
 Multi-GPU: the lattice is one twist; N GPUs solve N independent twists (replicas,
 no collective); value is the slowest rank's time, scaling "weak".
@@ -38,14 +45,19 @@ ORACLE_DIR = os.path.join(ROOT, "oracle")
 
 METRIC = "time-to-converged E/A (<1 keV vs FP64) mixed+batched+learned vs plain GPU"
 WORKLOADS = {
+    "snm132n4": dict(nmax=4, A=132, rho=0.16, snm=True, potential=1,
+                     desc="SNM A=132, rho=0.16 fm^-3, nmax=4 (2916 states), chiral-like (complex V), theta=0"),
+    "snm132n3": dict(nmax=3, A=132, rho=0.16, snm=True, potential=1,
+                     desc="SNM A=132, rho=0.16 fm^-3, nmax=3 (1372 states), chiral-like (complex V), theta=0"),
     "pnm66": dict(nmax=4, A=66, rho=0.16, snm=False, potential=0,
                   desc="PNM A=66, rho=0.16 fm^-3, nmax=4 (1458 states), Minnesota, theta=0"),
     "pnm14": dict(nmax=2, A=14, rho=0.08, snm=False, potential=0,
                   desc="PNM A=14, rho=0.08 fm^-3, nmax=2 (250 states), Minnesota, theta=0"),
 }
 # Iterations the reference algorithm (0.75/0.25 mixing + DIIS every 6, |dE| < 1e-6 MeV,
-# ccm_iter.f90:67-96) takes on each lattice, as run by the engine's reference mode.
-REFERENCE_ITERATIONS = {"pnm66": 13, "pnm14": 13}
+# ccm_iter.f90:67-96) takes on each lattice, as run by the engine's reference mode
+# (None: measured by the engine when needed).
+REFERENCE_ITERATIONS = {"pnm66": 13, "pnm14": 13, "snm132n4": None, "snm132n3": None}
 
 
 def load_pkg():
@@ -146,15 +158,26 @@ def oracle_sample(wl: dict, iters: int, warm: int):
     return statistics.mean(times), O.num_threads(), o
 
 
+# Oracle iterations per timed step and warm-up of the reference arm are capped so that
+# the whole run stays within a few minutes on the larger lattices (one SNM 132 nmax=4
+# iteration takes about 20 s on 16 cores, after about 40 s of V set-up).
+REFERENCE_ARM_CAP = {"snm132n4": (3, 1), "snm132n3": (5, 1)}
+
+
 def run_reference(args, wl):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
     n_ref = REFERENCE_ITERATIONS[args.workload]
-    per_it, cores, _ = oracle_sample(wl, args.steps, args.warmup)
+    if n_ref is None:
+        raise SystemExit("no reference-mode iteration count recorded for " + args.workload)
+    cap_s, cap_w = REFERENCE_ARM_CAP.get(args.workload, (args.steps, args.warmup))
+    steps, warm = max(1, min(args.steps, cap_s)), min(args.warmup, cap_w)
+    per_it, cores, _ = oracle_sample(wl, steps, warm)
     value = per_it * n_ref
-    sample = (f"{args.steps} timed CCD iterations (after {args.warmup} warm-up) of the oracle restatement "
-              f"(complex<double> ordered blocks, as the reference), x {n_ref} reference-mode iterations")
+    sample = (f"{steps} timed CCD iterations (after {warm} warm-up) of the oracle restatement "
+              f"(complex<double> ordered blocks, as the reference) on the full lattice, x {n_ref} "
+              f"reference-mode iterations (extrapolated)")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_it * 1e3, "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
@@ -179,35 +202,53 @@ def hbm_peak():
         return FALLBACK_HBM_GBS, "fallback 6.8 TB/s (of fallback)"
 
 
-def kernel_work(P, H, ring, precision):
-    """Algorithmic work of one timed bracket per kernel slot: ('flop', F) or ('byte', B).
+def kernel_work(P, H, ring, precision, real=True):
+    """Algorithmic work of one timed bracket per kernel slot: ('flop', F) or ('byte', B),
+    and the bytes of the operand representation the kernel actually streams.
 
-    FP64 GEMMs count 2 flops per multiply-add on unique pairs.  Tensor-core launches are
-    HBM-bound (arithmetic intensity far below the BF16 ridge): their bytes are the split
-    operands read once (hi + lo, es bytes each), C read and written in FP64."""
-    es = 2 if precision == 1 else 4
-    pp = sum(2.0 * p * p * h for p, h in zip(P, H))
-    hh = sum(2.0 * p * h * h for p, h in zip(P, H))
-    x = sum(2.0 * h * h * p for p, h in zip(P, H))
-    i4 = sum(2.0 * nhp * nhp * nph for nph, nhp in ring)
-    rg = sum(2.0 * nph * nhp * nhp for nph, nhp in ring)
-    # pp-ladder launch: V_pppp' dT' plus the two hh-ladder corrections (dT' I9', T_b' dI9')
-    # into one accumulator; R' read and written, PP_b + HH_b read
-    b_pp = sum(2 * es * (p * p + p * h) + 2 * 2 * es * (p * h + h * h) + 24.0 * p * h for p, h in zip(P, H))
-    # dI4 launch: 1/2 V_ph dT_ph, and dX = V_hhpp'^T dT' (H x H, K = P) for I9' - I9_b'
-    b_i4 = (sum(2 * es * (2.0 * nhp * nph) + 16.0 * nhp * nhp for nph, nhp in ring)
-            + sum(2 * es * (2.0 * h * p) + 16.0 * h * h for p, h in zip(P, H)))
-    # ring launch: dR_ph = T_ph,b dI4 + dT_ph I4 (two accumulators), written without reading
-    b_ring = sum(2 * 2 * es * (nph * nhp + nhp * nhp) + 8.0 * nph * nhp for nph, nhp in ring)
-    # digit-product GEMM: 9 BF16 digit planes of V_pppp' and of T_b read once, C written
-    b_oz = sum(9 * 2.0 * (p * p + p * h) + 16.0 * p * h for p, h in zip(P, H))
-    b_i4_oz = sum(9 * 2.0 * (2.0 * nhp * nph) + 16.0 * nhp * nhp for nph, nhp in ring)
-    b_ring_oz = sum(9 * 2.0 * (nph * nhp + nhp * nhp) + 16.0 * nph * nhp for nph, nhp in ring)
-    return {"x_fp64": ("flop", x), "i4_fp64": ("flop", i4), "ring_fp64": ("flop", rg),
-            "ladder_fp64": ("flop", pp + hh), "pp_rebase_fp64": ("flop", pp), "hh_fp64": ("flop", hh),
-            "pp_tc": ("byte", b_pp), "i4_tc": ("byte", b_i4), "ring_tc": ("byte", b_ring),
-            "pp_rebase_digits": ("byte", b_oz), "i4_rebase_digits": ("byte", b_i4_oz),
-            "ring_rebase_digits": ("byte", b_ring_oz)}
+    Unique pairs (a<b, i<j) throughout.  FP64 GEMMs count 2 flops per real multiply-add
+    (8 per complex one).  Tensor-core launches are HBM-bound (arithmetic intensity far
+    below the BF16 ridge): their algorithmic bytes are the FP64 (or complex FP64)
+    elements of every matrix the product reads, once, and of C written once, e = 8 (16)
+    bytes per element.  The representation the kernel streams instead -- BF16 (TF32)
+    hi/lo halves or the 9 BF16 digit planes of the exact digit products -- is returned
+    beside it, so that the report can show both."""
+    e = 8.0 if real else 16.0
+    nc = 1 if real else 2                     # real components per element
+    mac = 2.0 if real else 8.0
+    es = 2 if precision == 1 else 4           # bytes of one hi or lo half
+    pp = sum(mac * p * p * h for p, h in zip(P, H))
+    hh = sum(mac * p * h * h for p, h in zip(P, H))
+    x = sum(mac * h * h * p for p, h in zip(P, H))
+    i4 = sum(mac * nhp * nhp * nph for nph, nhp in ring)
+    rg = sum(mac * nph * nhp * nhp for nph, nhp in ring)
+    PH = sum(p * h for p, h in zip(P, H))
+    P2 = sum(p * p for p in P)
+    H2 = sum(h * h for h in H)
+    PHr = sum(nph * nhp for nph, nhp in ring)
+    HP2 = sum(nhp * nhp for nph, nhp in ring)
+    # pp-ladder launch: V_pppp' dT' + dT' I9' + T_b' dI9' into R' (read and written) with
+    # PP_b + HH_b read: V_pppp', dT', T_b', I9', dI9', R' (2x), PP_b, HH_b
+    a_pp = e * (P2 + 6 * PH + 2 * H2)
+    r_pp = nc * (2 * es * (P2 + PH) + 2 * 2 * es * (PH + H2)) + e * 4 * PH
+    # dI4 launch: dI4 = 1/2 V_ph dT_ph (n_hp x n_hp) and dX = V_hhpp'^T dT' (H x H)
+    a_i4 = e * (2 * PHr + HP2) + e * (2 * PH + H2)
+    r_i4 = nc * (2 * es * (2 * PHr) + 2 * es * 2 * PH) + e * (HP2 + H2)
+    # ring launch: dR_ph = T_ph,b dI4 + dT_ph I4 (written without reading)
+    a_rg = e * (2 * PHr + 2 * HP2 + PHr)
+    r_rg = nc * 2 * 2 * es * (PHr + HP2) + e * PHr
+    # digit products at a re-base: A, B read once, C written once
+    a_oz = e * (P2 + 2 * PH)
+    r_oz = nc * 9 * 2.0 * (P2 + PH) + e * PH
+    a_i4_oz = e * (2 * PHr + HP2)
+    r_i4_oz = nc * 9 * 2.0 * (2 * PHr) + e * HP2
+    a_rg_oz = e * (2 * PHr + HP2)
+    r_rg_oz = nc * 9 * 2.0 * (PHr + HP2) + e * PHr
+    return {"x_fp64": ("flop", x, None), "i4_fp64": ("flop", i4, None), "ring_fp64": ("flop", rg, None),
+            "ladder_fp64": ("flop", pp + hh, None), "pp_rebase_fp64": ("flop", pp, None), "hh_fp64": ("flop", hh, None),
+            "pp_tc": ("byte", a_pp, r_pp), "i4_tc": ("byte", a_i4, r_i4), "ring_tc": ("byte", a_rg, r_rg),
+            "pp_rebase_digits": ("byte", a_oz, r_oz), "i4_rebase_digits": ("byte", a_i4_oz, r_i4_oz),
+            "ring_rebase_digits": ("byte", a_rg_oz, r_rg_oz)}
 
 
 KERNEL_NAMES = {"x_fp64": "k_xdot X = V_hhpp'^T T' (FP64 column dots)", "i4_fp64": "k_gemm<double> I4",
@@ -250,8 +291,8 @@ def run_ours(args, wl):
     torch.cuda.set_device(local)
     theta = replica_theta(rank)
     L = ccx.Layout.from_basis(wl["nmax"], wl["A"], wl["rho"], snm=wl["snm"], theta=theta)
-    real = wl["potential"] == ccx.POT_MINNESOTA
-    prec = PRECISIONS[args.precision] if real else 0
+    real = wl["potential"] == ccx.POT_MINNESOTA and not any(theta)
+    prec = PRECISIONS[args.precision]
     e = ccx.Engine(L, device=local, real=real)
     e.generate(potential=wl["potential"])
     e.setup_t_amplitudes()
@@ -303,30 +344,33 @@ def run_ours(args, wl):
         e.set_profiling(False)
         return timers, ktimers
 
-    # warm-up: both forms (tensor-core tiles are prepared by the first mixed solve)
+    # warm-up: the headline form W times (tensor-core tiles and digit planes are prepared
+    # by the first mixed solve), the plain FP64 form once
     for _ in range(args.warmup):
         solve(e, prec)
-        if prec:
-            solve(e, 0)
+    if prec:
+        solve(e, 0)
     ms, results, launches, clk = timed(prec, args.steps, True)
     r = results[-1]
     iters = sum(x["iterations"] for x in results) / len(results)
     ea = (e.e0() + r["e_ccd"]).real / wl["A"]
     if prec:
-        ms64, res64, _, _ = timed(0, args.steps, False)
+        # the plain FP64 solve is 10-20x slower: a bounded number of timed solves
+        n64 = max(1, min(args.steps, args.plain_steps))
+        ms64, res64, _, _ = timed(0, n64, False)
         ea64 = (e.e0() + res64[-1]["e_ccd"]).real / wl["A"]
-        plain = {"s": ms64 * 1e-3, "iterations": res64[-1]["iterations"], "E_per_A_MeV": ea64,
-                 "res_norm": res64[-1]["res_norm"]}
+        plain = {"s": ms64 * 1e-3, "solves_timed": n64, "iterations": res64[-1]["iterations"],
+                 "E_per_A_MeV": ea64, "res_norm": res64[-1]["res_norm"]}
     else:
         ms64, ea64, plain = ms, ea, None
 
     # ---- roofline of the dominant kernel (largest device time in the profiled solves) ----
     timers, ktimers = breakdown(prec, args.steps)
-    work = kernel_work(P, H, ring, prec)
+    work = kernel_work(P, H, ring, prec, real=real)
     dom = max((k for k in ktimers if k in work and ktimers[k][1] > 0), key=lambda k: ktimers[k][0])
     kms, kn = ktimers[dom]
     per_launch_ms = kms / kn
-    kind, amount = work[dom]
+    kind, amount, rep = work[dom]
     if kind == "flop":
         peak = ccx.device_fp64_peak(local)
         achieved = amount / (per_launch_ms * 1e-3) / 1e12
@@ -338,9 +382,15 @@ def run_ours(args, wl):
         peak, src = hbm_peak()
         achieved = amount / (per_launch_ms * 1e-3) / 1e9
         roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                    "peak_source": src, "bytes_per_launch": amount}
+                    "peak_source": src, "bytes_per_launch": amount,
+                    "bytes_basis": "algorithmic: unique-pair %s elements of every operand read once and of C "
+                                   "written once" % ("FP64" if real else "complex FP64"),
+                    "representation_bytes_per_launch": rep,
+                    "representation_frac": rep / (per_launch_ms * 1e-3) / 1e9 / peak}
+    traffic = PROFILED_TRAFFIC.get((args.workload, args.precision, dom))
     roofline.update({"kernel": KERNEL_NAMES[dom], "ms_per_launch": per_launch_ms, "launches_timed": kn,
-                     "traffic": PROFILED_TRAFFIC.get((args.workload, args.precision, dom))})
+                     "traffic": traffic,
+                     "traffic_over_algorithmic": (traffic / amount) if (traffic and kind == "byte") else None})
     kernel_ms = {k: {"ms": v[0] / args.steps, "brackets": v[1] // args.steps} for k, v in ktimers.items() if v[1]}
 
     # ---- end to end through the C ABI from pinned host buffers ----
@@ -352,34 +402,38 @@ def run_ours(args, wl):
             2: "mixed TF32x3 + FP64 defect correction"}[prec]
     if prec and args.rebase == "digits":
         form += " (re-base products as exact digit products on the tensor cores)"
+    form += " (packed unique pairs, real arithmetic)" if real else " (packed unique pairs, complex arithmetic)"
+    e_bytes = 8 if real else 16
     line = {"metric": METRIC, "value": ms * 1e-3, "unit": "s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64" if real else "c128", "data": "synthetic",
-            "form": form + " (packed unique pairs, real arithmetic)" if real else form,
+            "form": form,
             "config": {"workload": wl["desc"], "solver": f"Jacobi + DIIS(8) to ||R-DT||<{args.tol:g} (FP64 residual)",
                        "precision": args.precision if prec else "fp64",
                        "defect_period": args.defect_period or "adaptive",
                        "rebase": args.rebase if prec else None,
                        "gemm_tile_shapes_by_N_bucket": tuned_shapes,
                        "l2": "inputs larger than L2 (V_pppp packed, %.2f GB, read every iteration)"
-                             % (sum(p * p for p in P) * 8 / 1e9),
+                             % (sum(p * p for p in P) * e_bytes / 1e9),
                        "replicas": world},
             "iterations": iters, "fp64_sweeps": r["fp64_sweeps"], "mixed_iterations": r["mixed_iterations"],
             "ccd_iterations_per_s": iters / (ms * 1e-3), "E_per_A_MeV": ea, "res_norm": r["res_norm"],
             "plain_fp64": plain, "speedup_vs_plain_fp64": (ms64 / ms) if prec else None,
             "dE_per_A_keV_vs_fp64": abs(ea - ea64) * 1e3 if prec else 0.0,
             "gflop_per_iteration": flops["total"] / 1e9,
+            "device_GB": e.memory() / 1e9,
             "breakdown": "term_ms_per_solve and kernel_ms_per_solve (and the roofline's launch time) from "
                          "as many further solves with per-term CUDA events on, after the timed region",
             "term_ms_per_solve": {k: v / args.steps for k, v in timers.items()},
             "kernel_ms_per_solve": kernel_ms,
             "roofline": roofline, "clocks": clk, "gpu_launches": launches, "e2e": e2e}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        n_ref = REFERENCE_ITERATIONS[args.workload] or reference_iterations(e, ccx)
-        per_it, cores, _ = oracle_sample(wl, 1, 0)
+        n_ref = REFERENCE_ITERATIONS.get(args.workload) or reference_iterations(e, ccx)
+        per_it, cores, o = oracle_sample(wl, 1, 0)
+        o.close()
         line["cpu_baseline"] = {"value": per_it * n_ref, "unit": "s", "cores": cores, "kind": "port",
                                 "sample": f"1 CCD iteration of the oracle (complex<double>, as the reference) on the "
-                                          f"full lattice, x {n_ref} reference-mode iterations"}
+                                          f"full lattice, x {n_ref} reference-mode iterations (extrapolated)"}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:
@@ -404,84 +458,108 @@ def reference_iterations(e, ccx):
     return e.ccd_iter(mode=ccx.MODE_REFERENCE)["iterations"]
 
 
+class PinnedHost:
+    """One page-locked host buffer (numpy memory registered with CUDA, so that the device
+    can address it in place) holding many blocks back to back."""
+
+    def __init__(self, torch, ndoubles: int):
+        import numpy as np
+        self.torch = torch
+        self.a = np.empty(max(int(ndoubles), 1), np.float64)
+        self.a[::512] = 0.0  # touch the pages before registering them
+        rc = torch.cuda.cudart().cudaHostRegister(self.a.ctypes.data, self.a.nbytes, 3)  # portable | mapped
+        if int(rc) != 0:
+            raise RuntimeError(f"cudaHostRegister failed ({rc})")
+        self.used = 0
+
+    def take(self, n: int) -> int:
+        """Pointer to the next n doubles."""
+        p = self.a.ctypes.data + 8 * self.used
+        self.used += n
+        return p
+
+    def close(self):
+        if self.a is not None:
+            self.torch.cuda.cudart().cudaHostUnregister(self.a.ctypes.data)
+            self.a = None
+
+
 def run_e2e(args, ccx, torch, L, e, local, real, solve):
     lib = ccx.lib()
     c = L.counts()
     dims = L.hhpp_dims()
     n = len(L.orbits()["nx"])
-    # reference-layout host blocks (pinned), exported once from the resident interaction
-    blocks = []
-
-    def pinned(nd):
-        return torch.empty(nd, dtype=torch.float64, pin_memory=True)
-
-    def export(kind, ch, rows, cols):
-        buf = pinned(2 * rows * cols)
-        ccx._check(lib.ccx_get_vblock(e._h, kind, ch, C.c_void_p(buf.data_ptr())))
-        blocks.append((kind, ch, buf))
-
-    for ch in range(c["hhpp"]):
-        nh, npp = dims[ch]
-        export(ccx.CH_HHPP, ch, nh, npp)
-        export(ccx.V_PPPP, ch, npp, npp)
-    for ch in range(c["hhhh"]):
-        _, nh, _ = L.channel(ccx.CH_HHHH, ch)
-        export(ccx.CH_HHHH, ch, nh, nh)
-    for ch in range(c["hphp"]):
-        _, nhp, _ = L.channel(ccx.CH_HPHP, ch)
-        export(ccx.CH_HPHP, ch, nhp, nhp)
-    fock = pinned(2 * n * n)
-    ccx._check(lib.ccx_get_fock(e._h, C.c_void_p(fock.data_ptr())))
+    # reference-layout host blocks in one registered buffer per family, exported once from
+    # the resident interaction
+    fams = {ccx.CH_HHPP: [(ch, nh, npp) for ch, (nh, npp) in enumerate(dims)],
+            ccx.V_PPPP: [(ch, npp, npp) for ch, (nh, npp) in enumerate(dims)],
+            ccx.CH_HHHH: [(ch, L.channel(ccx.CH_HHHH, ch)[1], L.channel(ccx.CH_HHHH, ch)[1])
+                          for ch in range(c["hhhh"])],
+            ccx.CH_HPHP: [(ch, L.channel(ccx.CH_HPHP, ch)[1], L.channel(ccx.CH_HPHP, ch)[1])
+                          for ch in range(c["hphp"])]}
+    bufs, calls = [], []
+    h2d = 0
+    for kind, lst in fams.items():
+        tot = sum(2 * r * q for _, r, q in lst)
+        buf = PinnedHost(torch, tot)
+        bufs.append(buf)
+        ptrs = []
+        for ch, r, q in lst:
+            ptr = buf.take(2 * r * q)
+            ccx._check(lib.ccx_get_vblock(e._h, kind, ch, C.c_void_p(ptr)))
+            ptrs.append(ptr)
+        h2d += 8 * tot
+        chs = (C.c_int32 * len(lst))(*[ch for ch, _, _ in lst])
+        calls.append((kind, len(lst), chs, (C.c_void_p * len(lst))(*ptrs)))
+    fb = PinnedHost(torch, 2 * n * n)
+    fock = fb.take(2 * n * n)
+    ccx._check(lib.ccx_get_fock(e._h, C.c_void_p(fock)))
+    h2d += 16 * n * n
     e0 = e.e0()
     e0buf = (C.c_double * 2)(e0.real, e0.imag)
-    t_out = pinned(2 * c["amps"])
-    h2d = sum(b.numel() * 8 for _, _, b in blocks) + fock.numel() * 8
-    d2h = t_out.numel() * 8 + 16
+    tb = PinnedHost(torch, 2 * c["amps"])
+    t_out = tb.take(2 * c["amps"])
+    d2h = 16 * c["amps"] + 16
+    bufs += [fb, tb]
     eb = ccx.Engine(L, device=local, real=real)
     stream = torch.cuda.ExternalStream(eb.stream(), device=local)
 
-    # one ccx_set_vblocks call per block family
-    families = {}
-    for kind, ch, buf in blocks:
-        families.setdefault(kind, []).append((ch, buf))
-    calls = []
-    for kind, lst in families.items():
-        chs = (C.c_int32 * len(lst))(*[ch for ch, _ in lst])
-        ptrs = (C.c_void_p * len(lst))(*[buf.data_ptr() for _, buf in lst])
-        calls.append((kind, len(lst), chs, ptrs))
-
     def step():
-        ccx._check(lib.ccx_set_fock(eb._h, C.c_void_p(fock.data_ptr()), e0buf))
-        for kind, n, chs, ptrs in calls:
-            ccx._check(lib.ccx_set_vblocks(eb._h, kind, n, chs, ptrs))
+        ccx._check(lib.ccx_set_fock(eb._h, C.c_void_p(fock), e0buf))
+        for kind, nb, chs, ptrs in calls:
+            ccx._check(lib.ccx_set_vblocks(eb._h, kind, nb, chs, ptrs))
         r = solve(eb)
-        ccx._check(lib.ccx_get_t2_all(eb._h, C.c_void_p(t_out.data_ptr())))
+        ccx._check(lib.ccx_get_t2_all(eb._h, C.c_void_p(t_out)))
         return r
 
-    for _ in range(max(1, args.warmup // 2)):
+    try:
+        for _ in range(max(1, args.warmup // 2)):
+            step()
+        eb.autotune()  # once per engine, as a host would after handing over the interaction
         step()
-    eb.autotune()  # once per engine, as a host would after handing over the interaction
-    step()
-    torch.cuda.synchronize()
-    ev0 = torch.cuda.Event(enable_timing=True)
-    ev1 = torch.cuda.Event(enable_timing=True)
-    t0 = time.perf_counter()
-    ev0.record(stream)
-    for _ in range(args.steps):
-        r = step()
-    ev1.record(stream)
-    ev1.synchronize()
-    wall = (time.perf_counter() - t0) / args.steps
-    ms = ev0.elapsed_time(ev1) / args.steps
-    eb.close()
+        torch.cuda.synchronize()
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        t0 = time.perf_counter()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            r = step()
+        ev1.record(stream)
+        ev1.synchronize()
+        wall = (time.perf_counter() - t0) / args.steps
+        ms = ev0.elapsed_time(ev1) / args.steps
+    finally:
+        eb.close()
+        for b in bufs:
+            b.close()
     return {"value": ms * 1e-3, "unit": "s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
             "host_wall_s": wall, "iterations": r["iterations"],
             "path": "ccx_set_fock + ccx_set_vblocks (all HHPP/PPPP/HHHH/HPHP blocks, one call per family) + "
                     "ccx_setup_t_amplitudes + ccx_ccd_iter + ccx_get_t2_all",
-            "host_buffers": "pinned: the packing kernels read the reference-layout blocks in place over "
-                            "NVLink-C2C (only the cache lines of unique pairs) and the amplitudes are "
-                            "unpacked straight into the host buffer; h2d_bytes_per_step is the size of "
-                            "the host inputs"}
+            "host_buffers": "page-locked (cudaHostRegister): the packing kernels read the reference-layout "
+                            "blocks in place over NVLink-C2C (only the cache lines of unique pairs) and the "
+                            "amplitudes are unpacked straight into the host buffer; h2d_bytes_per_step is the "
+                            "size of the host inputs"}
 
 
 TWIST_LATTICES = {
@@ -505,54 +583,130 @@ def gauss_legendre_twists():
 
 
 def run_twists(args):
-    """Twist batch: the same lattice at N twists, solved as one lockstep batch
-    (ccx_ccd_iter_batch) against a per-twist sequential loop (ccx_ccd_iter), both in the
-    mixed form with digit-product re-bases, MP2 start, ||R - D T|| < tol."""
+    """Twist-averaged E/A of one lattice at N twists (ccm_main.f90:163-279 solves them one
+    after the other).  The headline form (mixed precision, digit-product re-bases) runs the
+    twists in lockstep batches (ccx_ccd_iter_batch) of as many twists as the device holds;
+    the per-twist sequential loop of the same form and the plain FP64 GPU solve are timed
+    beside it.  Every step covers the whole job: engines (layout on the host, interaction
+    generated on the device, operand tiles and digit planes) are built per batch, so
+    total_s includes that set-up; solve_s counts only the solves.  The plain FP64 form is
+    timed on a seeded sample of the twists (plain_twists) and scaled to N."""
+    import random
     import torch
     ccx = load_pkg()
     lat = TWIST_LATTICES[args.lattice]
     grid = gauss_legendre_twists()
-    # a spread subset when fewer than 64 twists are asked for
     step = max(1, len(grid) // args.twists)
     grid = grid[::step][:args.twists]
+    pot = lat.get("potential", 0)
     prec = PRECISIONS[args.precision]
     rb = ccx.REBASE_DIGITS if (prec and args.rebase == "digits") else ccx.REBASE_FP64
     opts = dict(precision=prec, rebase=rb, tol=args.tol, max_iter=200, diis_dim=8)
-    engines = []
-    for th, _ in grid:
+
+    def build(th, precision, rebase):
         L = ccx.Layout.from_basis(lat["nmax"], lat["A"], lat["rho"], snm=lat["snm"], theta=th)
-        pot = lat.get("potential", 0)
-        e = ccx.Engine(L, real=pot == 0)
+        e = ccx.Engine(L, real=(pot == 0 and not any(th)))
         e.generate(potential=pot)
         e.setup_t_amplitudes()
-        e.ccd_iter(mode=ccx.MODE_STANDARD, **opts)  # warm-up: operand tiles and digit planes
-        engines.append(e)
-    seq, bat = [], []
+        e.prepare(precision=precision, rebase=rebase)
+        return e
+
+    # engines per batch: the device memory of one prepared engine of the largest twist
+    probe = build(grid[0][0], prec, rb)
+    per = probe.memory()
+    probe.close()
+    del probe
+    torch.cuda.synchronize()
+    free = torch.cuda.mem_get_info()[0]
+    wave = max(1, min(len(grid), int(0.9 * free / (per * 1.15))))
+    if args.twist_batch:
+        wave = min(wave, args.twist_batch)
+
+    def batched_pass():
+        """All twists, batch after batch; returns (total_s, solve_s, results)."""
+        res = [None] * len(grid)
+        solve_s = 0.0
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for w0 in range(0, len(grid), wave):
+            engines = [build(th, prec, rb) for th, _ in grid[w0:w0 + wave]]
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            rs, _ = ccx.ccd_iter_batch(engines, **opts)
+            torch.cuda.synchronize()
+            solve_s += time.perf_counter() - t1
+            for k, (e, r) in enumerate(zip(engines, rs)):
+                res[w0 + k] = (e.e0(), r)
+                e.close()
+            del engines
+        torch.cuda.synchronize()
+        return time.perf_counter() - t0, solve_s, res
+
+    def sequential_pass(idx, precision, rebase, sample_clocks=False):
+        """The twists idx one after the other, one engine at a time."""
+        res = {}
+        solve_s = 0.0
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for k in idx:
+            e = build(grid[k][0], precision, rebase)
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            r = e.ccd_iter(mode=ccx.MODE_STANDARD, precision=precision, rebase=rebase, tol=args.tol, max_iter=200,
+                           diis_dim=8)
+            solve_s += time.perf_counter() - t1
+            res[k] = (e.e0(), r)
+            e.close()
+        torch.cuda.synchronize()
+        return time.perf_counter() - t0, solve_s, res
+
+    def twist_average(res_by_index):
+        wsum = sum(grid[k][1] for k in res_by_index)
+        return sum(grid[k][1] * (e0 + r["e_ccd"]).real / lat["A"] for k, (e0, r) in res_by_index.items()) / wsum
+
+    for _ in range(args.warmup if args.warmup < 2 else 1):
+        batched_pass()
+    clocks = ClockSampler(0)
+    tot, sol = [], []
     for _ in range(args.steps):
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        rs = []
-        for e in engines:
-            e.setup_t_amplitudes()
-            rs.append(e.ccd_iter(mode=ccx.MODE_STANDARD, **opts))
-        torch.cuda.synchronize()
-        seq.append(time.perf_counter() - t0)
-        t0 = time.perf_counter()
-        for e in engines:
-            e.setup_t_amplitudes()
-        rb_, _ = ccx.ccd_iter_batch(engines, **opts)
-        torch.cuda.synchronize()
-        bat.append(time.perf_counter() - t0)
-    wsum = sum(w for _, w in grid)
-    ea = sum(w * (e.e0() + r["e_ccd"]).real / lat["A"] for (_, w), e, r in zip(grid, engines, rb_)) / wsum
-    ea_seq = sum(w * (e.e0() + r["e_ccd"]).real / lat["A"] for (_, w), e, r in zip(grid, engines, rs)) / wsum
-    line = {"metric": "time to converged twist-averaged E/A", "impl": "ours", "workload": "twist batch",
-            "lattice": lat["desc"], "twists": len(grid), "form": args.precision + " + " + args.rebase + " re-base",
-            "batched_s": statistics.median(bat), "sequential_s": statistics.median(seq),
-            "speedup_batched_vs_sequential": statistics.median(seq) / statistics.median(bat),
-            "iterations": [r["iterations"] for r in rb_], "E_per_A_twist_averaged_MeV": ea,
-            "dE_per_A_keV_batched_vs_sequential": abs(ea - ea_seq) * 1e3, "steps": args.steps,
-            "device_GB_per_engine": engines[0].memory() / 1e9}
+        t, so, res = batched_pass()
+        tot.append(t)
+        sol.append(so)
+    clk = clocks.stop()
+    res_b = {k: v for k, v in enumerate(res)}
+    ea = twist_average(res_b)
+    # the same form, per twist in sequence (one pass)
+    seq_t, seq_s, res_s = sequential_pass(range(len(grid)), prec, rb)
+    ea_seq = twist_average(res_s)
+    # plain FP64 on a seeded sample of the twists, scaled to all of them
+    rng = random.Random(20261203)
+    sample = sorted(rng.sample(range(len(grid)), min(args.plain_twists, len(grid))))
+    p_t, p_s, res_p = sequential_pass(sample, 0, ccx.REBASE_FP64)
+    scale = len(grid) / len(sample)
+    d_kev = max(abs((res_p[k][0] + res_p[k][1]["e_ccd"]).real - (res_b[k][0] + res_b[k][1]["e_ccd"]).real)
+                / lat["A"] for k in sample) * 1e3
+    value = statistics.median(tot)
+    line = {"metric": METRIC, "impl": "ours", "value": value, "unit": "s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": value * 1e3, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "c128" if pot else "f64", "data": "synthetic",
+            "config": {"workload": f"twist-averaged {lat['desc']}, {len(grid)} twists of the 4x4x4 "
+                                   f"Gauss-Legendre grid on [-pi, pi]^3",
+                       "form": f"{args.precision} + {args.rebase} re-bases, lockstep batches of {wave} twists",
+                       "start": "MP2 (the learned start is not used: it costs an iteration here)",
+                       "solver": f"Jacobi + DIIS(8) to ||R-DT||<{args.tol:g} (FP64 residual) per twist"},
+            "twists": len(grid), "twists_per_batch": wave, "device_GB_per_twist": per / 1e9,
+            "total_s": value, "solve_s": statistics.median(sol),
+            "sequential_same_form": {"total_s": seq_t, "solve_s": seq_s},
+            "speedup_batched_vs_sequential_solve": seq_s / statistics.median(sol),
+            "plain_fp64_gpu": {"twists_timed": len(sample), "total_s_sample": p_t, "solve_s_sample": p_s,
+                               "total_s_scaled": p_t * scale, "solve_s_scaled": p_s * scale,
+                               "iterations": [res_p[k][1]["iterations"] for k in sample]},
+            "speedup_vs_plain_fp64_gpu": p_t * scale / value,
+            "iterations": [res_b[k][1]["iterations"] for k in range(len(grid))],
+            "E_per_A_twist_averaged_MeV": ea,
+            "dE_per_A_keV_batched_vs_sequential": abs(ea - ea_seq) * 1e3,
+            "max_dE_per_A_keV_vs_fp64_on_sample": d_kev,
+            "clocks": clk}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -563,13 +717,16 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="pnm66", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="snm132n4", choices=sorted(WORKLOADS))
+    ap.add_argument("--plain-steps", type=int, default=2, help="timed plain FP64 solves beside the headline form")
     ap.add_argument("--tol", type=float, default=1e-10)
     ap.add_argument("--precision", default="bf16x3", choices=sorted(PRECISIONS))
     ap.add_argument("--defect-period", type=int, default=0, help="FP64 re-base every k iterations (0: adaptive)")
     ap.add_argument("--twists", type=int, default=0,
                     help="run the twist-batch comparison with this many twists instead of the headline")
-    ap.add_argument("--lattice", default="pnm66", choices=sorted(TWIST_LATTICES))
+    ap.add_argument("--lattice", default="snm132n3chiral", choices=sorted(TWIST_LATTICES))
+    ap.add_argument("--twist-batch", type=int, default=0, help="cap on the twists per lockstep batch (0: memory)")
+    ap.add_argument("--plain-twists", type=int, default=4, help="twists of the plain FP64 GPU sample")
     ap.add_argument("--rebase", default="digits", choices=["fp64", "digits"],
                     help="pp-ladder product of a re-base: FP64 FMA GEMM or exact digit products on the tensor cores")
     ap.add_argument("--no-e2e", action="store_true")

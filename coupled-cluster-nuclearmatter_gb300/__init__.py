@@ -135,6 +135,9 @@ def lib():
         "ccx_device_fp64_peak": ([i32, C.POINTER(dbl)], C.c_int),
         "ccx_selftest_tc_gemm": ([i32, i32, i32, vp, vp, vp, i32, C.c_uint64, C.POINTER(dbl), C.POINTER(dbl)], C.c_int),
         "ccx_ccd_energy_noalloc": ([i32, vp, vp, vp, vp, vp], C.c_int),
+        "ccx_selftest_tc_wait": ([i32, C.c_int64, C.POINTER(i32)], C.c_int),
+        "ccx_engine_prepare": ([vp, C.POINTER(_IterOpts)], C.c_int),
+        "ccx_engine_diis_fallbacks": ([vp, C.POINTER(C.c_int64)], C.c_int),
         "ccx_engine_kernel_timers": ([vp, vp, vp], C.c_int),
         "ccx_set_vblocks": ([vp, i32, i32, vp, vp], C.c_int),
         "ccx_ccd_iter_batch": ([vp, i32, vp, vp, C.POINTER(C.c_double)], C.c_int),
@@ -194,6 +197,14 @@ def selftest_tc_gemm(shapes, kind: int = 0, use_alo: bool = True, seed: int = 1,
     _check(lib().ccx_selftest_tc_gemm(device, kind, len(shapes), _ptr(M), _ptr(N), _ptr(K), int(use_alo) | (2 if segments else 0), seed,
                                       C.byref(err), C.byref(ms)))
     return err.value, ms.value
+
+
+def selftest_tc_wait(wait_cycles: int, device: int = 0) -> int:
+    """Tensor-core self-test with every pipeline wait limited to wait_cycles; returns the
+    kernel's error word (0: completed and checked, else the wait that ran out)."""
+    err = C.c_int32()
+    _check(lib().ccx_selftest_tc_wait(device, int(wait_cycles), C.byref(err)))
+    return err.value
 
 
 def ccd_energy_noalloc(nch: int, dims_ptr: int, t2_ptr: int, vhhpp_ptr: int, energy_ptr: int, stream: int = 0):
@@ -544,6 +555,11 @@ class Engine:
                 "res_norm": r.res_norm, "seconds": r.seconds, "fp64_sweeps": r.fp64_sweeps,
                 "mixed_iterations": r.mixed_iterations}
 
+    def prepare(self, mode=MODE_STANDARD, precision=PREC_FP64, diis_dim=8, rebase=REBASE_FP64):
+        """The one-time set-up of a solve with these options, without solving."""
+        o = _IterOpts(mode, precision, 1, 1e-10, diis_dim, 0, 0, rebase)
+        _check(lib().ccx_engine_prepare(self._h, C.byref(o)))
+
     def pert_triples(self) -> complex:
         z = np.zeros(2)
         _check(lib().ccx_pert_triples(self._h, _ptr(z)))
@@ -558,6 +574,12 @@ class Engine:
     def launches(self) -> int:
         x = C.c_int64()
         _check(lib().ccx_engine_launches(self._h, C.byref(x)))
+        return x.value
+
+    def diis_fallbacks(self) -> int:
+        """DIIS systems found singular since creation (each kept the plain step)."""
+        x = C.c_int64()
+        _check(lib().ccx_engine_diis_fallbacks(self._h, C.byref(x)))
         return x.value
 
     KERNEL_SLOTS = ("x_fp64", "i4_fp64", "ring_fp64", "ladder_fp64", "pp_rebase_fp64", "hh_fp64",

@@ -360,6 +360,10 @@ int ccx_engine_memory(const ccx_engine *e, int64_t *bytes) {
   if (!bytes) return fail(CCX_EINVAL, "null argument");
   ENGINE_CALL(e, *bytes = e->E->device_bytes());
 }
+int ccx_engine_diis_fallbacks(const ccx_engine *e, int64_t *n) {
+  if (!n) return fail(CCX_EINVAL, "null argument");
+  ENGINE_CALL(e, *n = e->E->diis_fallbacks());
+}
 int ccx_engine_launches(const ccx_engine *e, int64_t *n) {
   if (!n) return fail(CCX_EINVAL, "null argument");
   ENGINE_CALL(e, *n = e->E->launches());
@@ -555,6 +559,18 @@ int ccx_selftest_tc_gemm(int32_t device, int32_t kind, int32_t nprob, const int3
     return fail(CCX_EINVAL, "bad selftest arguments");
   return guard([&] { ccx::tc_selftest(device, kind, nprob, M, N, K, use_alo, seed, max_rel_err, ms); });
 }
+int ccx_selftest_tc_wait(int32_t device, int64_t wait_cycles, int32_t *kernel_error) {
+  if (!kernel_error || wait_cycles <= 0) return fail(CCX_EINVAL, "bad selftest arguments");
+  return guard([&] {
+    // two BF16x3 problems, 384 x 96 x 640 and 200 x 48 x 300, through the persistent kernel
+    const int32_t M[2] = {384, 200}, N[2] = {96, 48}, K[2] = {640, 300};
+    double rel = 0.0, ms = 0.0;
+    int err = 0;
+    ccx::tc_selftest(device, 0, 2, M, N, K, 1, 7, &rel, &ms, wait_cycles, &err);
+    *kernel_error = err;
+    if (err == 0 && !(rel < 1e-12)) throw ccx::EngineError(CCX_ENUMERIC, "tensor-core self-test product is wrong");
+  });
+}
 int ccx_setup_t_amplitudes(ccx_engine *e) { ENGINE_CALL(e, e->E->mp2()); }
 int ccx_set_t2(ccx_engine *e, int32_t ch, const double *t) {
   if (!t) return fail(CCX_EINVAL, "null T2 block");
@@ -597,6 +613,21 @@ int ccx_ccd_energy(ccx_engine *e, double ener[2]) {
 int ccx_residual_norm(ccx_engine *e, double *norm) {
   if (!norm) return fail(CCX_EINVAL, "null argument");
   ENGINE_CALL(e, *norm = e->E->residual_norm());
+}
+int ccx_engine_prepare(ccx_engine *e, const ccx_iter_opts *opt) {
+  if (!opt) return fail(CCX_EINVAL, "null argument");
+  ENGINE_CALL(e, {
+    ccx::IterOpts o;
+    o.mode = opt->mode;
+    o.precision = opt->precision;
+    o.max_iter = opt->max_iter;
+    o.tol = opt->tol;
+    o.diis_dim = opt->diis_dim;
+    o.defect_period = opt->defect_period;
+    o.rebase = opt->rebase;
+    o.verbose = opt->verbose;
+    e->E->prepare(o);
+  });
 }
 int ccx_ccd_iter(ccx_engine *e, const ccx_iter_opts *opt, ccx_iter_result *res) {
   if (!opt || !res) return fail(CCX_EINVAL, "null argument");

@@ -165,6 +165,7 @@ class Engine final : public IEngine {
     if (device < 0 || device >= ndev) throw EngineError(1, "device ordinal out of range");
     device_ = device;
     CK(cudaSetDevice(device_));
+    check_memory_plan();
     // the residual's X chain runs on a lower-priority side stream beside the main one
     int prio_low = 0, prio_high = 0;
     CK(cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high));
@@ -199,6 +200,7 @@ class Engine final : public IEngine {
   bool is_complex() const override { return ScalarOf<S>::complex; }
   int64_t device_bytes() const override { return bytes_; }
   int64_t launches() const override { return launches_; }
+  int64_t diis_fallbacks() const override { return diis_fallbacks_; }
   void timers(double ms[10]) const override { for (int i = 0; i < 10; ++i) ms[i] = timers_[i]; }
   void kernel_timers(double ms[kKernelSlots], int64_t n[kKernelSlots]) const override {
     for (int i = 0; i < kKernelSlots; ++i) { ms[i] = ktimers_[i]; n[i] = kcount_[i]; }
@@ -308,12 +310,9 @@ class Engine final : public IEngine {
     if (staged && n > 1) CK(cudaStreamSynchronize(cs_));
     finish_vblocks();
   }
-  // the copies have been read once this returns; a real engine also reports here
-  // whether any block it packed had a non-zero imaginary part
-  void finish_vblocks() {
-    if (!ScalarOf<S>::complex) check_flag("V block has a non-zero imaginary part but the engine is real");
-    else CK(cudaStreamSynchronize(st_));
-  }
+  // the copies have been read once this returns; reports here whether any block it
+  // packed held a NaN or Inf, or (real engine) a non-zero imaginary part
+  void finish_vblocks() { check_flag("V block has a non-zero imaginary part but the engine is real"); }
   // slot 0: stage through stage_ on the compute stream; slots 1, 2: stage_ / stage2_
   // with the copy on the copy stream (reuse waits for the slot's previous pack)
   void set_vblock_async(int kind, int ch, const double *v, int slot, bool reuse = false) {
@@ -665,6 +664,9 @@ class Engine final : public IEngine {
     if (!ScalarOf<S>::complex && im != 0.0) throw EngineError(1, "complex input given to a real engine");
     return make_scalar<S>(re, im);
   }
+  // Input checks of the packing kernels (cvt_in): a NaN or Inf is CCX_ENUMERIC, a
+  // complex value given to a real engine CCX_EINVAL with msg.  The flag is cleared
+  // either way, so the engine stays usable once the caller hands over a valid block.
   void check_flag(const char *msg) {
     int f = 0;
     CK(cudaMemcpyAsync(&host_flag_, flag_.p, sizeof(int), cudaMemcpyDeviceToHost, st_));
@@ -672,6 +674,8 @@ class Engine final : public IEngine {
     f = host_flag_;
     if (f) {
       CK(cudaMemsetAsync(flag_.p, 0, sizeof(int), st_));
+      CK(cudaStreamSynchronize(st_));
+      if (f & 2) throw EngineError(5, "input holds NaN or Inf");
       throw EngineError(1, msg);
     }
   }
@@ -723,6 +727,37 @@ class Engine final : public IEngine {
     }
     dirty_ = false;
     vph_ready_ = true;
+  }
+
+  // Device bytes of the resident state (amplitudes, residual, interaction blocks, ring
+  // blocks, per-amplitude maps and pair slots), from the layout alone.  A layout that
+  // does not fit in the device's free memory is rejected with CCX_ENOMEM before the
+  // engine allocates anything.
+  void check_memory_plan() const {
+    const Layout &L = *L_;
+    const int64_t ns = L.b.ns, A = L.b.A, NP = ns - A;
+    int64_t vpp = 0, hh2 = 0, ph = 0, i4 = 0;
+    for (int c = 0; c < L.fam[3].count(); ++c) {
+      vpp += (int64_t)L.pk[c].P * L.pk[c].P;
+      hh2 += (int64_t)L.pk[c].H * L.pk[c].H;
+    }
+    for (int q = 0; q < L.ph[1].count(); ++q) {
+      const int64_t a = L.ph[1].side1[q].size(), b = L.ph[1].side2[q].size();
+      ph += a * b;
+      i4 += b * b;
+    }
+    const double need = (double)sizeof(S) * (3.0 * L.n_tpacked + vpp + 3.0 * hh2 + 3.0 * ph + 2.0 * i4) +
+                        2.0 * 16.0 * L.n_tpacked + 8.0 * (NP * NP + A * A);
+    size_t free_b = 0, total_b = 0;
+    CK(cudaMemGetInfo(&free_b, &total_b));
+    if (need > (double)free_b) {
+      char msg[256];
+      std::snprintf(msg, sizeof msg,
+                    "layout needs %.1f GB of device memory for its resident state (V_pppp' alone %.1f GB); "
+                    "the device has %.1f GB free",
+                    need / 1e9, (double)sizeof(S) * vpp / 1e9, (double)free_b / 1e9);
+      throw EngineError(3, msg);
+    }
   }
 
   void build_tables() {
@@ -1296,7 +1331,16 @@ class Engine final : public IEngine {
     for (int i = 0; i < nd; ++i) { B[i + (size_t)ns * nd] = -1.0; B[nd + (size_t)ns * i] = -1.0; }
     B[nd + (size_t)ns * nd] = 0.0;
     sol[nd] = -1.0;
-    if (!zsolve(ns, B, sol)) throw EngineError(5, "singular DIIS matrix");
+    // A singular system (the reference prints ZGESV's info and goes on with an undefined
+    // solution, ccm_diis.f90:173-180) keeps the damped step already written to T.
+    bool ok = zsolve(ns, B, sol);
+    for (int i = 0; i < ns && ok; ++i) ok = std::isfinite(sol[i].real()) && std::isfinite(sol[i].imag());
+    if (!ok) {
+      ++diis_fallbacks_;
+      mark(9);
+      if (timing_) accumulate_timers(8, 9);
+      return;
+    }
     std::vector<double> coef(2 * nd);
     for (int i = 0; i < nd; ++i) { coef[2 * i] = sol[i].real(); coef[2 * i + 1] = ScalarOf<S>::complex ? sol[i].imag() : 0.0; }
     launch_combine<S>(n_t_, cols.data(), coef.data(), nd, T_.as<S>(), st_);
@@ -1384,6 +1428,23 @@ class Engine final : public IEngine {
     s.e[0] = r.e_mbpt2[0];
     s.e[1] = r.e_mbpt2[1];
     s.done = o.max_iter < 1;
+  }
+  // the one-time set-up a solve with these options needs (operand tiles, digit planes
+  // of the interaction, DIIS history), without solving
+  void prepare(const IterOpts &o) override {
+    require_ready();
+    if (o.precision < 0 || o.precision > 2) throw EngineError(1, "unknown precision");
+    if (o.rebase < 0 || o.rebase > 1) throw EngineError(1, "unknown re-base product kind");
+    if (o.precision != 0) {
+      prepare_mixed(o.precision == 2 ? kTcTF32 : kTcBF16);
+      if (o.rebase == 1) prepare_oz();
+    }
+    if (o.mode == 1) {
+      const int m = std::max(2, std::min(o.diis_dim, 15));
+      hist_t_.alloc((size_t)m * n_t_ * sizeof(S), &bytes_);
+      hist_e_.alloc((size_t)m * n_t_ * sizeof(E), &bytes_);
+    }
+    CK(cudaStreamSynchronize(st_));
   }
   bool std_done() const override { return ss_.done; }
   void std_launch_residual() override {
@@ -1506,6 +1567,8 @@ class Engine final : public IEngine {
       for (int i = 0; i < nh; ++i) { Bm[i + (size_t)n1 * nh] = -1.0; Bm[nh + (size_t)n1 * i] = -1.0; }
       rhs[nh] = -1.0;
       ok = dsolve(n1, Bm, rhs);
+      for (int i = 0; i < n1 && ok; ++i) ok = std::isfinite(rhs[i]);
+      if (!ok) ++diis_fallbacks_;
       if (ok) {
         coef.resize(2 * nh);
         for (int i = 0; i < nh; ++i) { coef[2 * i] = rhs[i]; coef[2 * i + 1] = 0.0; }
@@ -2323,6 +2386,7 @@ class Engine final : public IEngine {
   cudaEvent_t ev_[12] = {};
   double timers_[10] = {};
   bool timing_ = false, profiling_ = false;
+  int64_t diis_fallbacks_ = 0;  // DIIS systems found singular: the plain step was kept
   static constexpr int kKernelEvents = 32;
   cudaEvent_t kev_[2 * kKernelEvents] = {};
   int kslot_[kKernelEvents] = {};

@@ -63,6 +63,7 @@ class IEngine {
   virtual bool is_complex() const = 0;
   virtual int64_t device_bytes() const = 0;
   virtual int64_t launches() const = 0;
+  virtual int64_t diis_fallbacks() const = 0;
   virtual void timers(double ms[10]) const = 0;
   virtual void kernel_timers(double ms[kKernelSlots], int64_t n[kKernelSlots]) const = 0;
   virtual void set_fock(const double *fock, const double e0[2]) = 0;
@@ -90,6 +91,7 @@ class IEngine {
   // standard-mode iteration as a state machine (see Engine::iterate_standard), for
   // solving several engines in lockstep
   virtual void std_begin(const IterOpts &o, IterResult &r) = 0;
+  virtual void prepare(const IterOpts &o) = 0;
   virtual bool std_done() const = 0;
   virtual void std_launch_residual() = 0;
   virtual void std_launch_update() = 0;
@@ -117,6 +119,7 @@ double fp64_peak(int device);
 void set_last_error(const std::string &msg);
 // tensor-core split GEMM self-test (tc_selftest.cu)
 void tc_selftest(int device, int kind, int nprob, const int *Ms, const int *Ns, const int *Ks, int use_alo, uint64_t seed,
-                 double *max_rel, double *ms);
+                 double *max_rel, double *ms,
+                 long long wait_budget = 0, int *kernel_err = nullptr);
 
 }  // namespace ccx

@@ -101,12 +101,18 @@ void finish(const double *partial, int nb, int nv, double *out, cudaStream_t st)
   k_finish<<<nv, 256, 0, st>>>(partial, nb, nv, out);
 }
 
+// An input value (re, im) in the engine's scalar.  Flag bits: 1 a non-zero imaginary
+// part given to a real engine, 2 a NaN or Inf.
 template <typename S> __device__ inline S cvt_in(const double *p, int *flag);
 template <> __device__ inline double cvt_in<double>(const double *p, int *flag) {
-  if (p[1] != 0.0) atomicExch(flag, 1);
+  if (p[1] != 0.0) atomicOr(flag, 1);
+  if (!isfinite(p[0]) || !isfinite(p[1])) atomicOr(flag, 2);
   return p[0];
 }
-template <> __device__ inline cplx cvt_in<cplx>(const double *p, int *) { return cplx(p[0], p[1]); }
+template <> __device__ inline cplx cvt_in<cplx>(const double *p, int *flag) {
+  if (!isfinite(p[0]) || !isfinite(p[1])) atomicOr(flag, 2);
+  return cplx(p[0], p[1]);
+}
 
 }  // namespace
 

@@ -9,11 +9,15 @@
 // kMaxChannels channels (512 KiB), held by every GPU that loads the library until the
 // process exits.
 //
-// Set-up: the first call on a device (with that device current) looks up the device
-// address of g_energy_slots with cudaGetSymbolAddress; make that first call before
-// any stream capture.  Every call on a device shares the one array and it keeps the
-// last call's contents: each call rewrites every slot it reads, and calls whose work
-// overlaps on the GPU race on it.
+// Set-up: the first call in a CUDA context (with that context's device current) looks
+// up the device address of g_energy_slots with cudaGetSymbolAddress; make that first
+// call before any stream capture.  The address is cached with the context's unique id
+// (cuCtxGetId), so a context that is destroyed and created again (cudaDeviceReset, a
+// reset primary context, a caller's own context) is seen as new and its address is
+// looked up again on its first call.  Every call in a context shares the one array and
+// it keeps the last call's contents: each call rewrites every slot it reads, and calls
+// whose work overlaps on the GPU race on it.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -34,8 +38,38 @@ struct __align__(16) EnergySlot {
 
 static __device__ __align__(256) EnergySlot g_energy_slots[kMaxChannels];
 
-EnergySlot *g_slot_addr[kMaxDevices] = {};
+// per device: the context the cached address belongs to, and the address
+struct SlotCache {
+  unsigned long long ctx_id = 0;
+  EnergySlot *addr = nullptr;
+};
+SlotCache g_slot_cache[kMaxDevices];
 std::mutex g_setup_mutex;
+
+using CtxGetCurrentFn = CUresult (*)(CUcontext *);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long *);
+
+// Unique id of the calling thread's current context, 0 if there is none yet.  The two
+// driver functions are reached through the runtime, so the library needs no libcuda
+// at link time.
+unsigned long long current_context_id() {
+  static CtxGetCurrentFn get_current = nullptr;
+  static CtxGetIdFn get_id = nullptr;
+  if (!get_current || !get_id) {
+    void *f0 = nullptr, *f1 = nullptr;
+    cudaDriverEntryPointQueryResult q0 = cudaDriverEntryPointSymbolNotFound, q1 = q0;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f0, 12000, cudaEnableDefault, &q0) != cudaSuccess ||
+        cudaGetDriverEntryPointByVersion("cuCtxGetId", &f1, 12000, cudaEnableDefault, &q1) != cudaSuccess ||
+        q0 != cudaDriverEntryPointSuccess || q1 != cudaDriverEntryPointSuccess || !f0 || !f1)
+      return 0;
+    get_current = (CtxGetCurrentFn)f0;
+    get_id = (CtxGetIdFn)f1;
+  }
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (get_current(&ctx) != CUDA_SUCCESS || !ctx || get_id(ctx, &id) != CUDA_SUCCESS) return 0;
+  return id;
+}
 
 // exclusive prefix sum of n_hh * n_pp into the slot offsets (one block)
 __global__ void k_noalloc_offsets(int nch, const int *__restrict__ dims, EnergySlot *slots) {
@@ -139,16 +173,21 @@ extern "C" int ccx_ccd_energy_noalloc(int32_t nch, const int32_t *dims, const do
   EnergySlot *slots = nullptr;
   {
     std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if (!g_slot_addr[dev]) {
+    SlotCache &c = g_slot_cache[dev];
+    const unsigned long long id = current_context_id();
+    if (id == 0 || id != c.ctx_id || !c.addr) {
+      // first call in this context (or no context yet): look the address up; the
+      // lookup creates the device's primary context if the thread has none
       void *p = nullptr;
       const cudaError_t e = cudaGetSymbolAddress(&p, g_energy_slots);
       if (e != cudaSuccess || !p) {
         ccx::set_last_error(cudaGetErrorString(e));
         return CCX_ECUDA;
       }
-      g_slot_addr[dev] = (EnergySlot *)p;
+      c.addr = (EnergySlot *)p;
+      c.ctx_id = current_context_id();
     }
-    slots = g_slot_addr[dev];
+    slots = c.addr;
   }
   cudaStream_t st = (cudaStream_t)stream;
   k_noalloc_offsets<<<1, 1024, 0, st>>>(nch, dims, slots);

@@ -143,8 +143,11 @@ static void oz_selftest(int nprob, const int *Ms, const int *Ns, const int *Ks, 
 
 // problems: M_i, N_i, K_i for i < nprob.  Returns max |C - C_ref| / max |C_ref| over all
 // problems and the kernel time (ms).  kind 2: the Ozaki digit-product GEMM.
+// wait_budget > 0: the clock-cycle budget of the kernel's pipeline waits; kernel_err
+// non-null: the kernel's error word is returned there instead of raised, and the product
+// is checked only when it is 0.
 void tc_selftest(int device, int kind, int nprob, const int *Ms, const int *Ns, const int *Ks, int use_alo, uint64_t seed,
-                 double *max_rel, double *ms) {
+                 double *max_rel, double *ms, long long wait_budget, int *kernel_err) {
   sck(cudaSetDevice(device), "cudaSetDevice");
   if (kind == 2) {
     oz_selftest(nprob, Ms, Ns, Ks, seed, max_rel, ms);
@@ -278,7 +281,8 @@ void tc_selftest(int device, int kind, int nprob, const int *Ms, const int *Ns, 
   cudaEventRecord(e0);
   int max_nk = 1;  // K tiles of all segments
   for (const auto &x : h) max_nk = std::max<int>(max_nk, (int)(x.a_el / ((size_t)x.mpad * tk)));
-  launch_tc_gemm(kind, (const TcProb *)dP.p, (const TcTile *)dT.p, (int)tiles.size(), npad_max, max_nk, (int *)dE.p, 0);
+  launch_tc_gemm(kind, (const TcProb *)dP.p, (const TcTile *)dT.p, (int)tiles.size(), npad_max, max_nk, (int *)dE.p, 0,
+                 wait_budget);
   cudaEventRecord(e1);
   sck(cudaGetLastError(), "tc gemm launch");
   sck(cudaEventSynchronize(e1), "tc gemm");
@@ -289,6 +293,11 @@ void tc_selftest(int device, int kind, int nprob, const int *Ms, const int *Ns, 
   *ms = t;
   int err = 0;
   sck(cudaMemcpy(&err, dE.p, 4, cudaMemcpyDeviceToHost), "copy err");
+  if (kernel_err) *kernel_err = err;
+  if (err && kernel_err) {
+    *max_rel = -1.0;
+    return;
+  }
   if (err) throw EngineError(2, "tensor-core GEMM reported error code " + std::to_string(err));
   double worst = 0.0;
   oc = 0;

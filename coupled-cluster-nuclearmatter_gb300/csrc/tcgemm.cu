@@ -83,7 +83,7 @@ __device__ __forceinline__ TcGeom tc_geom(const TcProb *__restrict__ pp, int npa
 template <int KIND>
 __global__ void __launch_bounds__(kTcThreads, 1) k_tc_gemm(const TcProb *__restrict__ probs,
                                                           const TcTile *__restrict__ tiles, int ntiles, int stages,
-                                                          int npad_max, int *err) {
+                                                          int npad_max, int *err, long long budget) {
   extern __shared__ __align__(1024) uint8_t smem[];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   constexpr uint32_t a_bytes = 128u * 128u;
@@ -116,13 +116,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_gemm(const TcProb *__restr
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
 
-  // bounded wait that also ends when another thread has given up
+  // bounded wait (budget cycles) that also ends when another thread has given up; the
+  // final waits for copies and MMAs in flight keep the full kWaitBudget
   auto wait = [&](uint64_t *bar, uint32_t parity) -> bool {
     const uint32_t b = smem_u32(bar);
     const long long t0 = clock64();
     while (!mbar_try_wait(b, parity)) {
       if (*abort_flag) return false;
-      if (clock64() - t0 > kWaitBudget) {
+      if (clock64() - t0 > budget) {
         *abort_flag = 1;
         return false;
       }
@@ -637,7 +638,8 @@ int tc_stages(int npad_max) {
 }
 
 void launch_tc_gemm(int kind, const TcProb *probs, const TcTile *tiles, int ntiles, int npad_max, int max_nk, int *err,
-                    cudaStream_t st) {
+                    cudaStream_t st, long long wait_budget) {
+  if (wait_budget <= 0) wait_budget = tcptx::kWaitBudget;
   (void)max_nk;  // the stage ring runs on across tiles
   if (ntiles <= 0) return;
   const size_t stage_bytes = 2 * 128 * 128 + 2 * (size_t)npad_max * 128;
@@ -650,10 +652,10 @@ void launch_tc_gemm(int kind, const TcProb *probs, const TcTile *tiles, int ntil
   const int grid = std::min(ntiles, sms);  // persistent: one CTA per SM walks the tile list
   if (kind == kTcBF16) {
     cudaFuncSetAttribute(k_tc_gemm<kTcBF16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_tc_gemm<kTcBF16><<<grid, kTcThreads, smem, st>>>(probs, tiles, ntiles, stages, npad_max, err);
+    k_tc_gemm<kTcBF16><<<grid, kTcThreads, smem, st>>>(probs, tiles, ntiles, stages, npad_max, err, wait_budget);
   } else {
     cudaFuncSetAttribute(k_tc_gemm<kTcTF32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_tc_gemm<kTcTF32><<<grid, kTcThreads, smem, st>>>(probs, tiles, ntiles, stages, npad_max, err);
+    k_tc_gemm<kTcTF32><<<grid, kTcThreads, smem, st>>>(probs, tiles, ntiles, stages, npad_max, err, wait_budget);
   }
 }
 

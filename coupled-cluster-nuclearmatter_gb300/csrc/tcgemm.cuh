@@ -51,9 +51,11 @@ inline int tc_tile_k(int kind) { return kind == kTcBF16 ? 64 : 32; }
 // error codes written to *err (0 = ok): 1 load wait timed out, 2 MMA wait timed out,
 // 3 final wait timed out, 4 bad problem (npad > 256 or not a multiple of 16, no K tiles)
 // max_nk: largest K-tile count (all segments) among the tiles (unused: the persistent
-// kernel's stage ring runs on across tiles)
+// kernel's stage ring runs on across tiles).  wait_budget: clock cycles each pipeline
+// wait may take before the kernel gives up with an error code (<= 0: the default of
+// about 2 s); the final waits for copies and MMAs in flight always keep the default.
 void launch_tc_gemm(int kind, const TcProb *probs, const TcTile *tiles, int ntiles, int npad_max, int max_nk, int *err,
-                    cudaStream_t st);
+                    cudaStream_t st, long long wait_budget = 0);
 // shared-memory stages launch_tc_gemm uses for tiles up to npad_max columns
 int tc_stages(int npad_max);
 

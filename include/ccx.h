@@ -258,7 +258,9 @@ int ccx_ccd_energy(ccx_engine *e, double ener[2]);
  * device, 2 doubles.  Asynchronous on stream (NULL: the legacy default stream).
  * Scratch is a static device array of 16384 channel slots (512 KiB) held by each
  * GPU that loads the library until exit; nch > 16384 is rejected.  The first call
- * on a device looks up that array's address -- make it before any stream capture.
+ * in a CUDA context looks up that array's address -- make it before any stream
+ * capture; the address is cached with the context's id, so after cudaDeviceReset (or
+ * in a caller's own context) the next call looks it up again.
  * All calls share the array: calls that overlap on the GPU race. */
 int ccx_ccd_energy_noalloc(int32_t nch, const int32_t *dims, const double *t2, const double *vhhpp, double *energy,
                            void *stream);
@@ -293,6 +295,11 @@ typedef struct {
 
 /* ccd_iter loop, ccm_iter.f90:67-133 */
 int ccx_ccd_iter(ccx_engine *e, const ccx_iter_opts *opt, ccx_iter_result *res);
+/* The one-time device set-up that the first ccx_ccd_iter with these options would do
+ * (tensor-core operand tiles, digit planes of the interaction, DIIS history), without
+ * solving, so that a host can keep set-up out of a timed or latency-critical solve.
+ * Needs the interaction and amplitudes.  No counterpart in the reference. */
+int ccx_engine_prepare(ccx_engine *e, const ccx_iter_opts *opt);
 /* n engines on one device (for example the twists of a twist-averaged run,
  * ccm_main.f90:163-279, which the reference solves one after the other) solved
  * together in the standard mode: the iterations run in lockstep, each engine's kernels
@@ -365,6 +372,18 @@ int ccx_selftest_tc_gemm(int32_t device, int32_t kind, int32_t nprob, const int3
                          const int32_t *K, int32_t use_alo, uint64_t seed, double *max_rel_err, double *ms);
 /* kernel launches issued by this engine since creation */
 int ccx_engine_launches(const ccx_engine *e, int64_t *launches);
+/* DIIS systems found singular (or with a non-finite solution) since creation; each one
+ * kept the plain step instead of the extrapolation.  The reference prints ZGESV's info
+ * and goes on with an undefined solution (ccm_diis.f90:173-180). */
+int ccx_engine_diis_fallbacks(const ccx_engine *e, int64_t *n);
+/* Failure path of the tensor-core kernel's bounded waits: runs the BF16x3 self-test
+ * problems with each pipeline wait limited to wait_cycles clock cycles.  A limit too
+ * short for the copies and MMAs to land makes the kernel give up: it records an error
+ * word (1 load wait, 2 MMA wait, 3 drain wait ran out), waits with the full limit for its
+ * own copies and MMAs in flight, frees its tensor memory and returns, and the context
+ * stays usable.  *kernel_error receives that word (0: the product completed and was
+ * checked against FP64). */
+int ccx_selftest_tc_wait(int32_t device, int64_t wait_cycles, int32_t *kernel_error);
 /* on: ccx_ccd_iter records CUDA events around every residual term and tensor-core
  * launch (about 20 records per iteration, ~5% of a solve) so that ccx_engine_timers and
  * ccx_engine_kernel_timers report the breakdown; off (the default): only the solve's

@@ -835,6 +835,7 @@ ocl_t *ocl_create(const ocl_params *p) {
   build_basis(o);
   build_channels(o);
   build_ph_channels(o);
+  if (p->layout_only) return o;
   build_vblocks(o);
   alloc_amplitudes(o);
   return o;

@@ -42,6 +42,7 @@ typedef struct {
   int potential;       /* OCL_POT_* */
   uint64_t lec_seed;   /* seed of the chiral-like contact LEC draw */
   int minnesota_f32_literals; /* 1: reproduce the reference's default-real literals */
+  int layout_only;     /* 1: basis and channel tables only (no V blocks, no amplitudes) */
 } ocl_params;
 
 typedef struct ocl ocl_t;

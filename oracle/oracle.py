@@ -41,6 +41,7 @@ class _Params(C.Structure):
         ("potential", C.c_int),
         ("lec_seed", C.c_uint64),
         ("minnesota_f32_literals", C.c_int),
+        ("layout_only", C.c_int),
     ]
 
 
@@ -133,6 +134,7 @@ class Config:
     potential: int = POT_MINNESOTA
     lec_seed: int = 20261203
     minnesota_f32_literals: bool = True
+    layout_only: bool = False  # basis and channel tables only: no V blocks, no amplitudes
 
 
 class Oracle:
@@ -147,6 +149,7 @@ class Oracle:
         p.potential = cfg.potential
         p.lec_seed = cfg.lec_seed
         p.minnesota_f32_literals = int(cfg.minnesota_f32_literals)
+        p.layout_only = int(cfg.layout_only)
         self._L = lib()
         self._h = self._L.ocl_create(C.byref(p))
         if not self._h:

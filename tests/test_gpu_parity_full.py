@@ -1,0 +1,120 @@
+"""GPU engine against the CPU oracle at the benchmark lattices, through the C ABI.
+
+The small-lattice parity lives in test_gpu_parity.py.  Here the same checks run at the
+sizes the benchmark measures:
+
+- PNM 66 at nmax=4 (1458 states, Minnesota): one residual at the MP2 amplitudes, block
+  by block (t2_intermediate, ccm_t2_eqn.f90:4-1304), and the converged E/A of the mixed
+  form (BF16x3 corrections, digit-product re-bases) against the oracle's converged FP64
+  E/A in the standard mode;
+- SNM 132 at nmax=3 (1372 states, chiral-like complex interaction): one residual at
+  theta = 0 and at one twist of the 4x4x4 Gauss-Legendre grid on [-pi, pi]^3;
+- (T) (pert_triples2, ccm_triples.f90:528-735) on SNM 76 at nmax=2 with the chiral-like
+  interaction, on the amplitudes the engine converged, handed to the oracle.
+
+Tolerances: residual blocks to 1e-12 (real) or 1e-11 (complex) of the largest block
+entry; energies far inside the spec bars (1e-6 relative in E/A, 1e-5 in E(T)).
+The oracle runs these on all host cores; each lattice takes seconds to a minute.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+GL_X = (0.8611363115940526, 0.3399810435848563)
+
+
+def _pair(ccx, O, nmax, A, rho, snm=False, pot=0, real=True, theta=(0.0, 0.0, 0.0)):
+    o = O.Oracle(O.Config(nmax=nmax, A=A, rho=rho, snm=snm, theta=theta, potential=pot))
+    L = ccx.Layout.from_basis(nmax, A, rho, snm=snm, theta=theta)
+    e = ccx.Engine(L, real=real)
+    e.generate(potential=pot)
+    return o, L, e
+
+
+def _residual_blocks(o, e, tol):
+    """Worst |R_engine - R_oracle| over every hhpp block, relative to the largest |R|."""
+    n = o.n_channels(3)
+    ro = [o.r2(c) for c in range(n)]
+    scale = max(np.abs(r).max() for r in ro)
+    worst = max(np.abs(e.t2_eqn(c) - ro[c]).max() for c in range(n)) / scale
+    assert worst < tol, worst
+    return worst
+
+
+@pytest.fixture(scope="module")
+def pnm66(ccx, O):
+    o, L, e = _pair(ccx, O, nmax=4, A=66, rho=0.16)
+    yield o, L, e
+    e.close()
+    o.close()
+
+
+def test_pnm66_residual_at_mp2(pnm66):
+    o, L, e = pnm66
+    assert abs(e.e0() - o.e0()) < 1e-12 * abs(o.e0())
+    o.mp2()
+    e.setup_t_amplitudes()
+    assert abs(e.ccd_energy() - o.energy()) < 1e-12 * abs(o.energy())
+    o.t2_intermediate()
+    e.t2_intermediate()
+    _residual_blocks(o, e, 1e-12)
+    d1o, d2o = o.denoms()
+    d1e, d2e = e.denominators()
+    assert np.abs(d1e - d1o).max() < 1e-13 * np.abs(d1o).max()
+    assert np.abs(d2e - d2o).max() < 1e-13 * np.abs(d2o).max()
+    assert abs(e.residual_norm() - o.residual_norm()) < 1e-10 * o.residual_norm()
+
+
+def test_pnm66_converged_mixed_energy_matches_oracle(ccx, O, pnm66):
+    """E/A of the mixed form (the benchmark's headline solve) against the oracle's FP64
+    solve to ||R - D T|| < 1e-10: the bar is 1e-6 relative (the benchmark spec) and 1 keV; the
+    engine reaches about 1e-12 relative."""
+    o, L, e = pnm66
+    o.mp2()
+    ro = o.ccd_iter(mode=O.MODE_STANDARD, tol=1e-10, max_iter=60)
+    e.setup_t_amplitudes()
+    re_ = e.ccd_iter(mode=ccx.MODE_STANDARD, precision=ccx.PREC_MIXED, rebase=ccx.REBASE_DIGITS, tol=1e-10,
+                     max_iter=60)
+    assert ro["converged"] and re_["converged"] and re_["res_norm"] < 1e-10
+    ea_o = (o.e0() + ro["e_ccd"]).real / 66
+    ea_e = (e.e0() + re_["e_ccd"]).real / 66
+    dkev = abs(ea_e - ea_o) * 1e3
+    assert abs(ea_e - ea_o) < 1e-6 * abs(ea_o) and dkev < 1.0, (ea_e, ea_o, dkev)
+    assert abs(ea_e - ea_o) < 1e-10 * abs(ea_o), (ea_e, ea_o, dkev)
+
+
+@pytest.mark.parametrize("theta", [(0.0, 0.0, 0.0), (np.pi * GL_X[0], -np.pi * GL_X[1], np.pi * GL_X[1])],
+                         ids=["theta0", "gl_twist"])
+def test_snm132_nmax3_chiral_residual(ccx, O, theta):
+    o, L, e = _pair(ccx, O, nmax=3, A=132, rho=0.16, snm=True, pot=1, real=False, theta=theta)
+    try:
+        assert abs(e.e0() - o.e0()) < 1e-11 * abs(o.e0())
+        o.mp2()
+        e.setup_t_amplitudes()
+        assert abs(e.ccd_energy() - o.energy()) < 1e-11 * abs(o.energy())
+        o.t2_intermediate()
+        e.t2_intermediate()
+        _residual_blocks(o, e, 1e-11)
+        assert abs(e.residual_norm() - o.residual_norm()) < 1e-9 * o.residual_norm()
+    finally:
+        e.close()
+        o.close()
+
+
+def test_triples_snm76_chiral_matches_oracle(ccx, O):
+    """(T) of the engine's converged amplitudes, recomputed by the oracle from the same
+    amplitudes: within 1e-9 relative (the spec bar is 1e-5)."""
+    o, L, e = _pair(ccx, O, nmax=2, A=76, rho=0.16, snm=True, pot=1, real=False)
+    try:
+        e.setup_t_amplitudes()
+        r = e.ccd_iter(mode=ccx.MODE_STANDARD, tol=1e-10, max_iter=80)
+        assert r["converged"]
+        for c in range(o.n_channels(3)):
+            o.set_t2(c, e.t2(c))
+        eo = o.triples()
+        ee = e.pert_triples()
+        assert abs(ee - eo) < 1e-9 * abs(eo), (ee, eo)
+    finally:
+        e.close()
+        o.close()

@@ -20,9 +20,29 @@ CONFIGS = [
 ]
 
 
-@pytest.mark.parametrize("c", CONFIGS, ids=lambda c: f"n{c['nmax']}A{c['A']}{'s' if c['snm'] else 'p'}")
+# The lattices of the benchmark workloads, where ties in |k|^2 decide the occupied set
+# (open shells under a twist): PNM 66 and SNM 132 at nmax=4, SNM 132 at nmax=3 at theta=0
+# and at two twists of the 4x4x4 Gauss-Legendre grid on [-pi, pi]^3.
+_GL = 0.8611363115940526 * np.pi, 0.3399810435848563 * np.pi
+FULL_SIZE = [
+    dict(nmax=4, A=66, snm=False, rho=0.16, theta=(0.0, 0.0, 0.0)),
+    dict(nmax=3, A=132, snm=True, rho=0.16, theta=(0.0, 0.0, 0.0)),
+    dict(nmax=3, A=132, snm=True, rho=0.16, theta=(_GL[0], -_GL[1], _GL[1])),
+    dict(nmax=3, A=132, snm=True, rho=0.16, theta=(-_GL[0], -_GL[0], _GL[0])),
+    dict(nmax=4, A=132, snm=True, rho=0.16, theta=(0.0, 0.0, 0.0)),
+    dict(nmax=4, A=66, snm=False, rho=0.16, theta=(_GL[1], _GL[0], -_GL[1])),
+]
+
+
+def _ids(c):
+    tw = "" if not any(c["theta"]) else "tw%+.2f%+.2f%+.2f" % tuple(c["theta"])
+    return f"n{c['nmax']}A{c['A']}{'s' if c['snm'] else 'p'}{tw}"
+
+
+@pytest.mark.parametrize("c", CONFIGS + FULL_SIZE, ids=_ids)
 def test_layout_matches_oracle(ccx, O, c):
-    o = O.Oracle(O.Config(nmax=c["nmax"], A=c["A"], snm=c["snm"], rho=c["rho"], theta=c["theta"]))
+    o = O.Oracle(O.Config(nmax=c["nmax"], A=c["A"], snm=c["snm"], rho=c["rho"], theta=c["theta"],
+                          layout_only=True))
     L = ccx.Layout.from_basis(c["nmax"], c["A"], c["rho"], snm=c["snm"], theta=c["theta"])
     a, b = o.orbits(), L.orbits()
     for k in ("nx", "ny", "nz", "sz", "tz"):

@@ -23,12 +23,10 @@ def _device_inputs(ccx, torch, L, e):
     return nch, d, t, w
 
 
-def test_noalloc_energy_matches_ccd_energy(ccx):
-    torch = pytest.importorskip("torch")
-    L = ccx.Layout.from_basis(2, 14, 0.08)
-    e = ccx.Engine(L, real=True)
-    e.generate()
-    e.setup_t_amplitudes()
+def _two_calls(ccx, torch, L, e):
+    """Two calls in a row on different amplitudes, each against ccx_ccd_energy; the
+    caller's device memory (torch's allocator and the device's free bytes) must be
+    the same before and after each call."""
     out = torch.zeros(2, dtype=torch.float64, device="cuda")
     results = []
     for step in range(2):
@@ -40,12 +38,44 @@ def test_noalloc_energy_matches_ccd_energy(ccx):
                 cnt = e.diis_t1t2(cnt + 1)
         ref = e.ccd_energy()
         nch, d, t, w = _device_inputs(ccx, torch, L, e)
+        torch.cuda.synchronize()
+        before = (torch.cuda.memory_allocated(), torch.cuda.mem_get_info()[0])
         ccx.ccd_energy_noalloc(nch, d.data_ptr(), t.data_ptr(), w.data_ptr(), out.data_ptr())
         torch.cuda.synchronize()
+        after = (torch.cuda.memory_allocated(), torch.cuda.mem_get_info()[0])
+        assert before == after, (step, before, after)
         got = complex(out[0].item(), out[1].item())
-        assert abs(got - ref) < 1e-12 * abs(ref), (step, got, ref)
+        assert abs(got.real - ref.real) < 1e-12 * abs(ref), (step, got, ref)
+        assert abs(got.imag - ref.imag) < 1e-12 * abs(ref), (step, got, ref)
         results.append(got)
     assert results[0] != results[1]
+    return results
+
+
+def test_noalloc_energy_matches_ccd_energy(ccx):
+    torch = pytest.importorskip("torch")
+    L = ccx.Layout.from_basis(2, 14, 0.08)
+    e = ccx.Engine(L, real=True)
+    e.generate()
+    e.setup_t_amplitudes()
+    _two_calls(ccx, torch, L, e)
+
+
+def test_noalloc_energy_matches_complex_engine(ccx):
+    """A complex engine (twisted SNM with the chiral-like interaction, whose V is
+    complex): the imaginary parts and the complex cross terms of the product are
+    checked against ccx_ccd_energy as well."""
+    torch = pytest.importorskip("torch")
+    L = ccx.Layout.from_basis(1, 4, 0.16, snm=True, theta=(0.3, -0.7, 1.1))
+    e = ccx.Engine(L, real=False)
+    e.generate(potential=ccx.POT_CHIRAL_LIKE)
+    e.setup_t_amplitudes()
+    v = np.concatenate([e.vblock(ccx.CH_HHPP, c).ravel() for c in range(len(L.hhpp_dims()))])
+    assert np.abs(v.imag).max() > 1e-6 * np.abs(v).max()
+    # a global phase on T makes the energy itself complex
+    e.set_t2_all(e.t2_all() * np.exp(0.4j))
+    res = _two_calls(ccx, torch, L, e)
+    assert abs(res[0].imag) > 0.1 * abs(res[0]), res
 
 
 def test_noalloc_rejects_too_many_channels(ccx):
