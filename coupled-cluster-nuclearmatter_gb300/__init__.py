@@ -22,6 +22,7 @@ CH_HHHH, CH_HHHP, CH_HHPP, CH_HPHP, CH_HPPP = 1, 2, 3, 4, 5
 CH_PH_PHHP, CH_PH_HPHP, CH_PH_HPPH = 11, 12, 13
 V_PPPP = 6
 POT_MINNESOTA, POT_CHIRAL_LIKE = 0, 1
+TRIPLES_FP64, TRIPLES_FP32 = 0, 1
 MODE_REFERENCE, MODE_STANDARD = 0, 1
 PREC_FP64, PREC_MIXED, PREC_MIXED_TF32 = 0, 1, 2
 REBASE_FP64, REBASE_DIGITS = 0, 1
@@ -137,6 +138,7 @@ def lib():
         "ccx_ccd_energy_noalloc": ([i32, vp, vp, vp, vp, vp], C.c_int),
         "ccx_selftest_tc_wait": ([i32, C.c_int64, C.POINTER(i32)], C.c_int),
         "ccx_engine_prepare": ([vp, C.POINTER(_IterOpts)], C.c_int),
+        "ccx_set_triples_precision": ([vp, i32], C.c_int),
         "ccx_engine_diis_fallbacks": ([vp, C.POINTER(C.c_int64)], C.c_int),
         "ccx_engine_kernel_timers": ([vp, vp, vp], C.c_int),
         "ccx_set_vblocks": ([vp, i32, i32, vp, vp], C.c_int),
@@ -559,6 +561,10 @@ class Engine:
         """The one-time set-up of a solve with these options, without solving."""
         o = _IterOpts(mode, precision, 1, 1e-10, diis_dim, 0, 0, rebase)
         _check(lib().ccx_engine_prepare(self._h, C.byref(o)))
+
+    def set_triples_precision(self, fp32: bool) -> None:
+        """(T) contractions in FP32 (default) or FP64; the |W|^2/D sum is FP64 either way."""
+        _check(lib().ccx_set_triples_precision(self._h, TRIPLES_FP32 if fp32 else TRIPLES_FP64))
 
     def pert_triples(self) -> complex:
         z = np.zeros(2)

@@ -360,6 +360,9 @@ int ccx_engine_memory(const ccx_engine *e, int64_t *bytes) {
   if (!bytes) return fail(CCX_EINVAL, "null argument");
   ENGINE_CALL(e, *bytes = e->E->device_bytes());
 }
+int ccx_set_triples_precision(ccx_engine *e, int32_t precision) {
+  ENGINE_CALL(e, e->E->set_triples_precision(precision));
+}
 int ccx_engine_diis_fallbacks(const ccx_engine *e, int64_t *n) {
   if (!n) return fail(CCX_EINVAL, "null argument");
   ENGINE_CALL(e, *n = e->E->diis_fallbacks());
@@ -568,7 +571,7 @@ int ccx_selftest_tc_wait(int32_t device, int64_t wait_cycles, int32_t *kernel_er
     int err = 0;
     ccx::tc_selftest(device, 0, 2, M, N, K, 1, 7, &rel, &ms, wait_cycles, &err);
     *kernel_error = err;
-    if (err == 0 && !(rel < 1e-12)) throw ccx::EngineError(CCX_ENUMERIC, "tensor-core self-test product is wrong");
+    if (err == 0 && !(rel < 2e-4)) throw ccx::EngineError(CCX_ENUMERIC, "tensor-core self-test product is wrong");
   });
 }
 int ccx_setup_t_amplitudes(ccx_engine *e) { ENGINE_CALL(e, e->E->mp2()); }

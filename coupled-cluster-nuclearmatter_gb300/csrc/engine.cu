@@ -201,6 +201,10 @@ class Engine final : public IEngine {
   int64_t device_bytes() const override { return bytes_; }
   int64_t launches() const override { return launches_; }
   int64_t diis_fallbacks() const override { return diis_fallbacks_; }
+  void set_triples_precision(int p) override {
+    if (p != 0 && p != 1) throw EngineError(1, "unknown (T) precision");
+    triples_fp32_ = p == 1;
+  }
   void timers(double ms[10]) const override { for (int i = 0; i < 10; ++i) ms[i] = timers_[i]; }
   void kernel_timers(double ms[kKernelSlots], int64_t n[kKernelSlots]) const override {
     for (int i = 0; i < kKernelSlots; ++i) { ms[i] = ktimers_[i]; n[i] = kcount_[i]; }
@@ -285,9 +289,11 @@ class Engine final : public IEngine {
   void set_vblocks(int kind, int n, const int *chs, const double *const *vs) override {
     const bool staged = kind == 1 || kind == 3 || kind == 6;
     if (n > 0 && (staged || kind == 4)) {
-      // blocks in device-addressable host memory are read in place: no staging copies
+      // blocks in device-addressable host memory are read in place: no staging copies.
+      // A family larger than kDirectMaxBytes goes through the copy engines instead: SM
+      // loads spread over that much host memory reach only a fraction of the link rate.
       std::vector<double *> dv(n);
-      bool direct = true;
+      bool direct = family_bytes(kind, n, chs) <= kDirectMaxBytes;
       for (int i = 0; i < n && direct; ++i) direct = (dv[i] = device_view(vs[i])) != nullptr;
       if (direct) {
         if (kind == 4) set_v4_direct(n, chs, dv.data());
@@ -309,6 +315,24 @@ class Engine final : public IEngine {
     for (int i = 0; i < n; ++i) set_vblock_async(kind, chs[i], vs[i], staged && n > 1 ? 1 + (i & 1) : 0, i >= 2);
     if (staged && n > 1) CK(cudaStreamSynchronize(cs_));
     finish_vblocks();
+  }
+  static constexpr double kDirectMaxBytes = 16e9;
+  // bytes of n reference-layout blocks of one family
+  double family_bytes(int kind, int n, const int *chs) const {
+    const Layout &L = *L_;
+    double b = 0.0;
+    for (int i = 0; i < n; ++i) {
+      const int ch = chs[i];
+      double r = 0, c = 0;
+      if ((kind == 3 || kind == 6) && ch >= 0 && ch < L.fam[3].count()) {
+        r = kind == 3 ? L.pk[ch].n_hh : L.pk[ch].n_pp;
+        c = L.pk[ch].n_pp;
+      } else if ((kind == 1 || kind == 4) && ch >= 0 && ch < L.fam[kind].count()) {
+        r = c = L.fam[kind].side1[ch].size();
+      }
+      b += 16.0 * r * c;
+    }
+    return b;
   }
   // the copies have been read once this returns; reports here whether any block it
   // packed held a NaN or Inf, or (real engine) a non-zero imaginary part
@@ -651,7 +675,7 @@ class Engine final : public IEngine {
       if (!generated_) throw EngineError(4, "(T) needs V_hhhp and V_hppp: set every HHHP and HPPP block, or generate the interaction");
       tr_->generate_v(pot_, st_);
     }
-    tr_->energy(T_.as<S>(), fdiag_.as<S>(), et, st_);
+    tr_->energy(T_.as<S>(), n_t_, fdiag_.as<S>(), et, st_, triples_fp32_);
     launches_ += tr_->launches();
   }
 
@@ -1387,7 +1411,6 @@ class Engine final : public IEngine {
   //   std_after_update (true: finished); std_after_dots }.  The DIIS Gram row needs no
   //   host decision, so the dots are queued behind the update and one synchronisation
   //   per iteration serves both.
-  static constexpr int kDotsAt = 16;  // host_res_ offset of the DIIS Gram row (<= 15 entries, 2 or 1 doubles each)
   struct StdState {
     IterOpts o;
     IterResult *r = nullptr;
@@ -1466,28 +1489,19 @@ class Engine final : public IEngine {
     s.ht = hist_t_.as<S>() + (int64_t)s.head * n_t_;
     s.he = hist_e_.as<E>() + (int64_t)s.head * n_t_;
     mark(7);
-    if constexpr (ScalarOf<S>::complex) {
-      launch_update<S>(D_, 1, T_.as<S>(), R_.as<S>(), Vhp_.as<S>(), d2ij_.as<S>(), d2ab_.as<S>(), s.ht, s.he,
-                       partial_.as<double>(), res_.as<double>(), st_);
-    } else {  // the Gram row of the new step against every stored one rides on the same pass
+    {  // the Gram row of the new step against every stored one rides on the same pass
       const int nh = std::min(s.nh + 1, s.m);
       if (nh > 16 || s.head >= nh) throw EngineError(1, "DIIS history larger than the fused Gram row");
       std::vector<const E *> es(nh);
       for (int j = 0; j < nh; ++j) es[j] = hist_e_.as<E>() + (int64_t)j * n_t_;
-      launch_update_std(D_, T_.as<S>(), R_.as<S>(), Vhp_.as<S>(), d2ij_.as<S>(), d2ab_.as<S>(), s.ht, s.he, es.data(),
-                        nh, s.head, s.mixed ? tcerr_.as<int>() : nullptr, partial_.as<double>(), res_.as<double>(),
-                        st_);
+      launch_update_std<S>(D_, T_.as<S>(), R_.as<S>(), Vhp_.as<S>(), d2ij_.as<S>(), d2ab_.as<S>(), s.ht, s.he,
+                           es.data(), nh, s.head, s.mixed ? tcerr_.as<int>() : nullptr, partial_.as<double>(),
+                           res_.as<double>(), st_);
     }
     launches_ += 2;
-    // the tensor-core error word rides on the same synchronisation as the energy (real
-    // engines: energy, norm, error word and Gram row in one copy)
-    if constexpr (ScalarOf<S>::complex) {
-      if (s.mixed) CK(cudaMemcpyAsync((int *)(host_res_ + 63), tcerr_.p, sizeof(int), cudaMemcpyDeviceToHost, st_));
-      CK(cudaMemcpyAsync(host_res_, res_.p, 3 * sizeof(double), cudaMemcpyDeviceToHost, st_));
-    } else {
-      CK(cudaMemcpyAsync(host_res_, res_.p, (4 + std::min(s.nh + 1, s.m)) * sizeof(double), cudaMemcpyDeviceToHost,
-                         st_));
-    }
+    // energy, norm, tensor-core error word and Gram row come back in one copy
+    CK(cudaMemcpyAsync(host_res_, res_.p, (4 + std::min(s.nh + 1, s.m)) * sizeof(double), cudaMemcpyDeviceToHost,
+                       st_));
   }
   bool std_after_update() override {
     StdState &s = ss_;
@@ -1499,7 +1513,7 @@ class Engine final : public IEngine {
     s.e[0] = host_res_[0];
     s.e[1] = host_res_[1];
     const double rn = 2.0 * std::sqrt(host_res_[2]);
-    const int tc_word = ScalarOf<S>::complex ? *(const int *)(host_res_ + 63) : (int)host_res_[3];
+    const int tc_word = (int)host_res_[3];
     if (s.mixed && tc_word) {
       const int err = tc_word;
       CK(cudaMemsetAsync(tcerr_.p, 0, sizeof(int), st_));
@@ -1533,28 +1547,18 @@ class Engine final : public IEngine {
     }
     return false;
   }
-  // Gram row of the new step against every stored step, with conjugation
+  // the Gram row of the new step (Re of the conjugated products) is computed by the update
+  // pass and copied with its sums: nothing to launch here
   void std_launch_dots() override {
     StdState &s = ss_;
     if (s.nh < s.m) ++s.nh;
-    // queued right behind the update, before the host has read its result: the Gram row
-    // lands in its own part of the host buffer (real engines: computed by the update)
-    if constexpr (ScalarOf<S>::complex) {
-      std::vector<const E *> es(s.nh);
-      for (int j = 0; j < s.nh; ++j) es[j] = hist_e_.as<E>() + (int64_t)j * n_t_;
-      launch_dots<S>(n_t_, s.he, es.data(), s.nh, 1, partial_.as<double>(), res_.as<double>(), st_);
-      launches_ += 2;
-      CK(cudaMemcpyAsync(host_res_ + kDotsAt, res_.p, 2 * s.nh * sizeof(double), cudaMemcpyDeviceToHost, st_));
-    }
   }
   void std_after_dots() override {
     StdState &s = ss_;
     const int m = s.m, nh = s.nh, slot = s.head;
-    // (re, im) pairs of the dots launch, or the real Gram row copied with the update's sums
-    constexpr int at = ScalarOf<S>::complex ? kDotsAt : 4, stride = ScalarOf<S>::complex ? 2 : 1;
     for (int j = 0; j < nh; ++j) {
-      s.B[slot + (size_t)m * j] = host_res_[at + stride * j];
-      s.B[j + (size_t)m * slot] = host_res_[at + stride * j];
+      s.B[slot + (size_t)m * j] = host_res_[4 + j];
+      s.B[j + (size_t)m * slot] = host_res_[4 + j];
     }
     s.head = (s.head + 1) % m;
     std::vector<double> coef;
@@ -2387,6 +2391,7 @@ class Engine final : public IEngine {
   double timers_[10] = {};
   bool timing_ = false, profiling_ = false;
   int64_t diis_fallbacks_ = 0;  // DIIS systems found singular: the plain step was kept
+  bool triples_fp32_ = true;    // (T) contractions in FP32 (FP64 accumulation)
   static constexpr int kKernelEvents = 32;
   cudaEvent_t kev_[2 * kKernelEvents] = {};
   int kslot_[kKernelEvents] = {};

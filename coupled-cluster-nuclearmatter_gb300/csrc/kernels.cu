@@ -775,7 +775,8 @@ __global__ void k_update(DevLayout L, int mode, S *__restrict__ T, const S *__re
       if constexpr (ScalarOf<S>::complex) {
         const S tj = r / D;
         hist_t[g] = tj;
-        hist_e[g] = tj - t;
+        const S st = tj - t;
+        hist_e[g] = cplxf{__double2float_rn(st.re), __double2float_rn(st.im)};
       } else {
         // the step q / D to FP32 accuracy (an FP64 division is a long sequence on this
         // GPU's narrow FP64 pipe); t + step keeps the fixed point exact, since the step
@@ -839,27 +840,48 @@ void launch_dots(int64_t n, const S *a, const S *const *bs, int nb, int conj_a, 
   finish(partial, blocks, 2 * kMaxDots, out, st);
 }
 
-// Standard-mode update of real amplitudes with the Gram row of its step in the same pass.
-// Per amplitude: D from the dressed denominators (hole-pair sums staged per tile in
-// shared memory, the same association as k_update), q = R - D t in FP64, the step q/D
-// to FP32 accuracy, hist_t = t + step, hist_e = step; the energy sum t V in FP64, and
-// |q|^2 and step . hist_e[j] in FP32 per thread (FP64 across warps and blocks).  One
-// pass, one launch and one host copy per iteration instead of an update and a dots pass.
+// Standard-mode update with the Gram row of its step in the same pass.  Per amplitude:
+// D from the dressed denominators (hole-pair sums staged per tile in shared memory, the
+// same association as k_update), q = R - D t in FP64, the step q/D to FP32 accuracy,
+// hist_t = t + step, hist_e = step; the energy sum t V in FP64, and |q|^2 and
+// Re(conj(step) hist_e[j]) in FP32 per thread (FP64 across warps and blocks).  One pass,
+// one launch and one host copy per iteration instead of an update and a dots pass.  The
+// FP32 step vanishes with the residual, so the fixed point is the FP64 one.
 constexpr int kUpdStdBlocks = 608;
-constexpr int kUpdStdNV = 4 + kMaxDots;  // E re, E im (0), |q|^2, error word, Gram row
+constexpr int kUpdStdNV = 4 + kMaxDots;  // E re, E im, |q|^2, error word, Gram row
 __device__ inline float warp_sum_f(float x) {
   for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
   return x;
 }
-__global__ void __launch_bounds__(256) k_update_std(DevLayout L, const double *__restrict__ T,
-                                                    const double *__restrict__ R, const double *__restrict__ Vhp,
-                                                    const double *__restrict__ d2ij, const double *__restrict__ d2ab,
-                                                    double *__restrict__ hist_t, float *__restrict__ hist_e,
-                                                    PtrPack<float> es, int nb, int self, const int *err,
-                                                    double *partial) {
-  __shared__ double sdij[kTileElems];  // hole-pair sums of one tile (at most kTileElems rows)
+// the step q / D to FP32 accuracy (an FP64 division is a long sequence on this GPU's
+// narrow FP64 pipe), its |q|^2 contribution and its Gram products
+__device__ inline float upd_step(double q, double D, float &r2) {
+  const float qf = __double2float_rn(q);
+  r2 = fmaf(qf, qf, r2);
+  return __fdiv_rn(qf, __double2float_rn(D));
+}
+__device__ inline cplxf upd_step(cplx q, cplx D, float &r2) {
+  const float qr = __double2float_rn(q.re), qi = __double2float_rn(q.im);
+  const float dr = __double2float_rn(D.re), di = __double2float_rn(D.im);
+  r2 = fmaf(qr, qr, fmaf(qi, qi, r2));
+  const float den = fmaf(dr, dr, di * di);
+  return cplxf{__fdiv_rn(fmaf(qr, dr, qi * di), den), __fdiv_rn(fmaf(qi, dr, -qr * di), den)};
+}
+__device__ inline double add_step(double t, float s) { return t + (double)s; }
+__device__ inline cplx add_step(cplx t, cplxf s) { return cplx(t.re + (double)s.re, t.im + (double)s.im); }
+__device__ inline float gram_dot(float a, float b) { return a * b; }
+__device__ inline float gram_dot(cplxf a, cplxf b) { return fmaf(a.re, b.re, a.im * b.im); }
+template <typename S>
+__global__ void __launch_bounds__(256) k_update_std(DevLayout L, const S *__restrict__ T, const S *__restrict__ R,
+                                                    const S *__restrict__ Vhp, const S *__restrict__ d2ij,
+                                                    const S *__restrict__ d2ab, S *__restrict__ hist_t,
+                                                    typename StepOf<S>::type *__restrict__ hist_e,
+                                                    PtrPack<typename StepOf<S>::type> es, int nb, int self,
+                                                    const int *err, double *partial) {
+  using E = typename StepOf<S>::type;
+  __shared__ S sdij[kTileElems];  // hole-pair sums of one tile (at most kTileElems rows)
   __shared__ double red[kUpdStdNV][8];
-  double e = 0.0;
+  double e_re = 0.0, e_im = 0.0;
   float r2 = 0.0f, f[kMaxDots];
 #pragma unroll
   for (int k = 0; k < kMaxDots; ++k) f[k] = 0.0f;
@@ -880,32 +902,37 @@ __global__ void __launch_bounds__(256) k_update_std(DevLayout L, const double *_
     const int2 *pporb = L.pp_orb + L.pp_off[ch];
     for (int el = tl.y + threadIdx.x; el < end; el += blockDim.x) {
       const int64_t g = base + el;
-      const double t = T[g], vij = Vhp[g], r = R[g];
+      const S t = T[g], vij = Vhp[g], r = R[g];
       const int ij = el / P, ab = el - ij * P;
       const int2 po = pporb[ab];
-      const double D = (sdij[ij - ij0] - d2ab[po.x - A]) - d2ab[po.y - A];
-      const double q = r - D * t;
-      const float qf = __double2float_rn(q);
-      r2 = fmaf(qf, qf, r2);
-      const float step = __fdiv_rn(qf, __double2float_rn(D));
-      hist_t[g] = t + (double)step;
+      const S D = (sdij[ij - ij0] - d2ab[po.x - A]) - d2ab[po.y - A];
+      const S q = r - D * t;
+      const E step = upd_step(q, D, r2);
+      hist_t[g] = add_step(t, step);
       hist_e[g] = step;
-      e = fma(t, vij, e);
+      if constexpr (ScalarOf<S>::complex) {
+        const S pr = t * vij;
+        e_re += real_(pr);
+        e_im += imag_(pr);
+      } else {
+        e_re = fma(t, vij, e_re);
+      }
 #pragma unroll
       for (int k = 0; k < kMaxDots; ++k)
-        if (k < nb) f[k] = fmaf(step, k == self ? step : es.p[k][g], f[k]);
+        if (k < nb) f[k] += gram_dot(step, k == self ? step : es.p[k][g]);
     }
   }
   // warp sums (FP32 values in FP32), then FP64 across the warps
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  e = warp_sum(e);
+  e_re = warp_sum(e_re);
+  e_im = warp_sum(e_im);
   r2 = warp_sum_f(r2);
 #pragma unroll
   for (int k = 0; k < kMaxDots; ++k)
     if (k < nb) f[k] = warp_sum_f(f[k]);
   if (lane == 0) {
-    red[0][wid] = e;
-    red[1][wid] = 0.0;
+    red[0][wid] = e_re;
+    red[1][wid] = e_im;
     red[2][wid] = (double)r2;
     red[3][wid] = (err && blockIdx.x == 0 && wid == 0) ? (double)*err : 0.0;  // carried to the host in the same copy
 #pragma unroll
@@ -918,14 +945,15 @@ __global__ void __launch_bounds__(256) k_update_std(DevLayout L, const double *_
     partial[(int64_t)blockIdx.x * kUpdStdNV + threadIdx.x] = x;
   }
 }
-void launch_update_std(const DevLayout &L, const double *T, const double *R, const double *Vhp, const double *d2ij,
-                       const double *d2ab, double *hist_t, float *hist_e, const float *const *es, int nb, int self,
+template <typename S>
+void launch_update_std(const DevLayout &L, const S *T, const S *R, const S *Vhp, const S *d2ij, const S *d2ab, S *hist_t,
+                       typename StepOf<S>::type *hist_e, const typename StepOf<S>::type *const *es, int nb, int self,
                        const int *err, double *partial, double *out, cudaStream_t st) {
   if (!L.nttile) return;
-  PtrPack<float> pk{};
+  PtrPack<typename StepOf<S>::type> pk{};
   for (int k = 0; k < nb; ++k) pk.p[k] = es[k];
   const int blocks = std::min(L.nttile, kUpdStdBlocks);
-  k_update_std<<<blocks, 256, 0, st>>>(L, T, R, Vhp, d2ij, d2ab, hist_t, hist_e, pk, nb, self, err, partial);
+  k_update_std<S><<<blocks, 256, 0, st>>>(L, T, R, Vhp, d2ij, d2ab, hist_t, hist_e, pk, nb, self, err, partial);
   finish(partial, blocks, kUpdStdNV, out, st);
 }
 
@@ -1387,6 +1415,9 @@ void launch_unpack_t(const DevLayout &L, int ch, int n_pp, const int *pp_signed,
                                  typename StepOf<S>::type *,                                                            \
                                  double *, double *, cudaStream_t);                                                    \
   template void launch_dots<S>(int64_t, const S *, const S *const *, int, int, double *, double *, cudaStream_t);     \
+  template void launch_update_std<S>(const DevLayout &, const S *, const S *, const S *, const S *, const S *, S *,    \
+                                     typename StepOf<S>::type *, const typename StepOf<S>::type *const *, int, int,   \
+                                     const int *, double *, double *, cudaStream_t);                                   \
   template void launch_diis_gram<S>(int64_t, const S *const *, int, double *, double *, cudaStream_t);                \
   template void launch_combine<S>(int64_t, const S *const *, const double *, int, S *, cudaStream_t);                 \
   template void launch_pack_vblock<S>(const DevLayout &, int, int, int, const double *, S *, int *, cudaStream_t);    \

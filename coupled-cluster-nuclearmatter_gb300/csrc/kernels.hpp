@@ -92,22 +92,27 @@ void launch_rinit(const DevLayout &L, const int4 *omap, const int4 *rmap, const 
 // mode 0: reference update T <- 0.75 T + 0.25 R/D, history column written
 // mode 1: Jacobi T_jac = R/D into hist_t, step into hist_e, T untouched
 // mode 2: energy only (no update); mode 3: residual norm + energy, no update
-// the DIIS step vectors of the standard mode: FP32 for real engines (the step is computed
-// to FP32 accuracy), S for complex ones
-template <typename S> struct StepOf { using type = S; };
+// the DIIS step vectors of the standard mode: the step is computed to FP32 accuracy and
+// stored in FP32 (real engines) or as FP32 (re, im) pairs (complex engines)
+struct __align__(8) cplxf {
+  float re, im;
+};
+template <typename S> struct StepOf;
 template <> struct StepOf<double> { using type = float; };
+template <> struct StepOf<cplx> { using type = cplxf; };
 template <typename S>
 void launch_update(const DevLayout &L, int mode, S *T, const S *R, const S *Vhp, const S *d2ij, const S *d2ab,
                    S *hist_t, typename StepOf<S>::type *hist_e, double *partial, double *out4, cudaStream_t st);
 // dot products: out[j] = sum_x w(a[x]) * b_j[x] for j < nb; conj on a when conj_a
 template <typename S>
 void launch_dots(int64_t n, const S *a, const S *const *bs, int nb, int conj_a, double *partial, double *out, cudaStream_t st);
-// mode-1 update of real amplitudes and the Gram row of its step in one pass:
-// out[0] = E, out[1] = 0, out[2] = |R - D T|^2, out[3] = *err (0 when err is null),
-// out[4 + j] = step . es[j] for j < nb (1 <= nb <= 16); es[self] is hist_e, the step
+// mode-1 update and the Gram row of its step in one pass:
+// out[0] = E (re), out[1] = E (im, 0 for real engines), out[2] = |R - D T|^2, out[3] = *err (0 when err is null),
+// out[4 + j] = Re(conj(step) . es[j]) for j < nb (1 <= nb <= 16); es[self] is hist_e, the step
 // this pass writes.  partial holds 20 doubles for each of up to 608 blocks.
-void launch_update_std(const DevLayout &L, const double *T, const double *R, const double *Vhp, const double *d2ij,
-                       const double *d2ab, double *hist_t, float *hist_e, const float *const *es, int nb, int self,
+template <typename S>
+void launch_update_std(const DevLayout &L, const S *T, const S *R, const S *Vhp, const S *d2ij, const S *d2ab, S *hist_t,
+                       typename StepOf<S>::type *hist_e, const typename StepOf<S>::type *const *es, int nb, int self,
                        const int *err, double *partial, double *out, cudaStream_t st);
 // reference DIIS Gram matrix of differences of nstep history columns (no conjugation)
 template <typename S>

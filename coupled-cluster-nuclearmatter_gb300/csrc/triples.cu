@@ -51,32 +51,57 @@ __device__ inline int t_orbitof(const TriplesDev &D, int x, int y, int z, int s,
   return D.orbit_of[idx];
 }
 
-constexpr unsigned long long kSignBit = 0x8000000000000000ull;
-// x with its sign bits flipped where m has them: a sign change on the integer pipe
-__device__ __forceinline__ double flip(double x, unsigned long long m) {
-  return __longlong_as_double((long long)((unsigned long long)__double_as_longlong(x) ^ m));
+// The 18 gather-contractions of a pair run in the contraction type W: the engine's
+// scalar S (FP64), or its FP32 counterpart (float, or cplxf for complex engines) on
+// FP32 copies of T, V_hppp and V_hhhp.  GB300's FP64 pipe retires 2 FMA per clock per SM
+// against 128 for FP32, so the FP32 form takes the contractions off the narrow pipe; the
+// |W|^2 / D accumulation stays FP64 in both.
+template <typename S> struct LowOf;
+template <> struct LowOf<double> { using type = float; };
+template <> struct LowOf<cplx> { using type = cplxf; };
+
+template <typename W> __device__ __forceinline__ W wzero();
+template <> __device__ __forceinline__ double wzero<double>() { return 0.0; }
+template <> __device__ __forceinline__ float wzero<float>() { return 0.0f; }
+template <> __device__ __forceinline__ cplx wzero<cplx>() { return cplx(0.0, 0.0); }
+template <> __device__ __forceinline__ cplxf wzero<cplxf>() { return cplxf{0.0f, 0.0f}; }
+
+// x with its sign flipped when s is 1: a sign-bit flip on the integer pipe
+__device__ __forceinline__ double flip(double x, unsigned s) {
+  return __longlong_as_double((long long)((unsigned long long)__double_as_longlong(x) ^ ((unsigned long long)s << 63)));
 }
-__device__ __forceinline__ cplx flip(cplx x, unsigned long long m) { return cplx(flip(x.re, m), flip(x.im, m)); }
+__device__ __forceinline__ float flip(float x, unsigned s) { return __int_as_float(__float_as_int(x) ^ (int)(s << 31)); }
+__device__ __forceinline__ cplx flip(cplx x, unsigned s) { return cplx(flip(x.re, s), flip(x.im, s)); }
+__device__ __forceinline__ cplxf flip(cplxf x, unsigned s) { return cplxf{flip(x.re, s), flip(x.im, s)}; }
 
 // T(ab, ij) with the antisymmetry signs of both pair slots, and the extra sign m
-template <typename S>
-__device__ inline S t2_at(const DevLayout &L, const S *T, int a, int b, int i, int j, unsigned long long m) {
+template <typename W>
+__device__ inline W t2_at(const DevLayout &L, const W *T, int a, int b, int i, int j, unsigned m) {
   const int2 sab = L.pp_slot[(int64_t)(a - L.A) * L.NP + (b - L.A)];
   const int2 sij = L.hh_slot[i * L.A + j];
-  if (sab.y == 0 || sij.y == 0) return S(0.0);
+  if (sab.y == 0 || sij.y == 0) return wzero<W>();
   const int ch = sab.x;
-  if ((sab.y < 0) != (sij.y < 0)) m ^= kSignBit;
+  if ((sab.y < 0) != (sij.y < 0)) m ^= 1u;
   return flip(T[L.t_off[ch] + sidx(sab.y) + (int64_t)L.P[ch] * sidx(sij.y)], m);
 }
 __device__ __forceinline__ double madd_conj(double v, double t, double acc) { return fma(v, t, acc); }
 __device__ __forceinline__ cplx madd_conj(cplx v, cplx t, cplx acc) { return acc + conj_(v) * t; }
+__device__ __forceinline__ float madd_conj(float v, float t, float acc) { return fmaf(v, t, acc); }
+__device__ __forceinline__ cplxf madd_conj(cplxf v, cplxf t, cplxf acc) {
+  return cplxf{fmaf(v.re, t.re, fmaf(v.im, t.im, acc.re)), fmaf(v.re, t.im, fmaf(-v.im, t.re, acc.im))};
+}
+// |W|^2 in FP64 as the engine's scalar
+__device__ __forceinline__ double wnorm2(double w) { return w * w; }
+__device__ __forceinline__ double wnorm2(float w) { return (double)w * (double)w; }
+__device__ __forceinline__ double wnorm2(cplx w) { return w.re * w.re + w.im * w.im; }
+__device__ __forceinline__ double wnorm2(cplxf w) { return (double)w.re * (double)w.re + (double)w.im * (double)w.im; }
 
-// sum_d conj(<cb|V|kd>) T(ad, ij).  Not inlined: the 18 calls of a pair would otherwise
-// unroll into a body larger than the instruction cache, and the warps stall on fetches.
-// acc + sign * sum_d conj(<cb|V|kd>) T(ad, ij), the sign as a mask of sign bits
-template <typename S>
-__device__ __noinline__ S one_particle(const TriplesDev &D, const DevLayout &L, const S *T, const S *V5, int a, int b,
-                                       int c, int i, int j, int k, unsigned long long m, S acc) {
+// acc + sign * sum_d conj(<cb|V|kd>) T(ad, ij), the sign as a bit.  Not inlined: the 18
+// calls of a pair would otherwise unroll into a body larger than the instruction cache,
+// and the warps stall on fetches.
+template <typename W>
+__device__ __noinline__ W one_particle(const TriplesDev &D, const DevLayout &L, const W *T, const W *V5, int a, int b,
+                                       int c, int i, int j, int k, unsigned m, W acc) {
   const int nxd = D.nx[i] + D.nx[j] - D.nx[a], nyd = D.ny[i] + D.ny[j] - D.ny[a];
   const int nzd = D.nz[i] + D.nz[j] - D.nz[a], tzd = D.tz[i] + D.tz[j] - D.tz[a];
   if (abs(nxd) > D.nk0 || abs(nyd) > D.nk1 || abs(nzd) > D.nk2 || abs(tzd) > 1) return acc;
@@ -87,17 +112,16 @@ __device__ __noinline__ S one_particle(const TriplesDev &D, const DevLayout &L, 
     if (d < D.A) continue;
     const int2 r = D.hp5_slot[(int64_t)k * D.NP + (d - D.A)];
     if (r.x < 0) continue;
-    const S t = t2_at<S>(L, T, a, d, i, j, m);
+    const W t = t2_at<W>(L, T, a, d, i, j, m);
     acc = madd_conj(V5[D.v5_off[r.x] + r.y + (int64_t)D.n5[r.x] * cl.y], t, acc);
   }
   return acc;
 }
 
-// sum_l conj(<jk|V|lc>) T(ab, il) (not inlined, as one_particle)
-// acc + sign * sum_l conj(<jk|V|lc>) T(ab, il)
-template <typename S>
-__device__ __noinline__ S one_hole(const TriplesDev &D, const DevLayout &L, const S *T, const S *V2, int a, int b,
-                                   int c, int i, int j, int k, unsigned long long m, S acc) {
+// acc + sign * sum_l conj(<jk|V|lc>) T(ab, il) (not inlined, as one_particle)
+template <typename W>
+__device__ __noinline__ W one_hole(const TriplesDev &D, const DevLayout &L, const W *T, const W *V2, int a, int b,
+                                   int c, int i, int j, int k, unsigned m, W acc) {
   const int nxl = D.nx[k] + D.nx[j] - D.nx[c], nyl = D.ny[k] + D.ny[j] - D.ny[c];
   const int nzl = D.nz[k] + D.nz[j] - D.nz[c], tzl = D.tz[k] + D.tz[j] - D.tz[c];
   if (abs(nxl) > D.nk0 || abs(nyl) > D.nk1 || abs(nzl) > D.nk2 || abs(tzl) > 1) return acc;
@@ -108,10 +132,19 @@ __device__ __noinline__ S one_hole(const TriplesDev &D, const DevLayout &L, cons
     if (l < 0 || l >= D.A) continue;
     const int2 cl = D.hp2_slot[(int64_t)l * D.NP + (c - D.A)];
     if (cl.x < 0) continue;
-    const S t = t2_at<S>(L, T, a, b, i, l, m);
+    const W t = t2_at<W>(L, T, a, b, i, l, m);
     acc = madd_conj(V2[D.v2_off[r.x] + r.y + (int64_t)D.n2[r.x] * cl.y], t, acc);
   }
   return acc;
+}
+
+// FP32 copy of an FP64 array
+__device__ __forceinline__ float to_low(double x) { return __double2float_rn(x); }
+__device__ __forceinline__ cplxf to_low(cplx x) { return cplxf{__double2float_rn(x.re), __double2float_rn(x.im)}; }
+template <typename S>
+__global__ void k_to_low(const S *__restrict__ src, int64_t n, typename LowOf<S>::type *__restrict__ dst) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
+    dst[e] = to_low(src[e]);
 }
 
 template <int NV>
@@ -140,9 +173,9 @@ __global__ void k_triple_fock(const int3 *__restrict__ t, int64_t n, const S *__
   }
 }
 
-template <typename S>
-__global__ void __launch_bounds__(256) k_triples(TriplesDev D, DevLayout L, const S *__restrict__ T,
-                                                 const S *__restrict__ V5, const S *__restrict__ V2,
+template <typename S, typename W>
+__global__ void __launch_bounds__(256) k_triples(TriplesDev D, DevLayout L, const W *__restrict__ T,
+                                                 const W *__restrict__ V5, const W *__restrict__ V2,
                                                  const S *__restrict__ eh, const S *__restrict__ ep, int64_t total,
                                                  double *partial) {
   double acc[2] = {0.0, 0.0};
@@ -158,27 +191,27 @@ __global__ void __launch_bounds__(256) k_triples(TriplesDev D, DevLayout L, cons
     const S spen = eh[D.hhh_off[ch] + bra] - ep[D.ppp_off[ch] + ket];
     // W = the 9 particle terms minus the 9 hole terms, accumulated in one sum with the
     // permutation signs applied as sign-bit flips
-    constexpr unsigned long long P = 0, N = kSignBit;
-    S tc = S(0.0);
-    tc = one_particle<S>(D, L, T, V5, a, b, c, i, j, k, P, tc);
-    tc = one_particle<S>(D, L, T, V5, b, a, c, i, j, k, N, tc);
-    tc = one_particle<S>(D, L, T, V5, c, b, a, i, j, k, N, tc);
-    tc = one_particle<S>(D, L, T, V5, a, b, c, k, j, i, N, tc);
-    tc = one_particle<S>(D, L, T, V5, a, b, c, i, k, j, N, tc);
-    tc = one_particle<S>(D, L, T, V5, c, b, a, i, k, j, P, tc);
-    tc = one_particle<S>(D, L, T, V5, c, b, a, k, j, i, P, tc);
-    tc = one_particle<S>(D, L, T, V5, b, a, c, i, k, j, P, tc);
-    tc = one_particle<S>(D, L, T, V5, b, a, c, k, j, i, P, tc);
-    tc = one_hole<S>(D, L, T, V2, a, b, c, i, j, k, N, tc);
-    tc = one_hole<S>(D, L, T, V2, a, c, b, i, j, k, P, tc);
-    tc = one_hole<S>(D, L, T, V2, c, b, a, i, j, k, P, tc);
-    tc = one_hole<S>(D, L, T, V2, a, b, c, k, j, i, P, tc);
-    tc = one_hole<S>(D, L, T, V2, a, b, c, j, i, k, P, tc);
-    tc = one_hole<S>(D, L, T, V2, c, b, a, j, i, k, N, tc);
-    tc = one_hole<S>(D, L, T, V2, c, b, a, k, j, i, N, tc);
-    tc = one_hole<S>(D, L, T, V2, a, c, b, j, i, k, N, tc);
-    tc = one_hole<S>(D, L, T, V2, a, c, b, k, j, i, N, tc);
-    const S term = (conj_(tc) * tc) / spen;
+    constexpr unsigned P = 0, N = 1;
+    W tc = wzero<W>();
+    tc = one_particle<W>(D, L, T, V5, a, b, c, i, j, k, P, tc);
+    tc = one_particle<W>(D, L, T, V5, b, a, c, i, j, k, N, tc);
+    tc = one_particle<W>(D, L, T, V5, c, b, a, i, j, k, N, tc);
+    tc = one_particle<W>(D, L, T, V5, a, b, c, k, j, i, N, tc);
+    tc = one_particle<W>(D, L, T, V5, a, b, c, i, k, j, N, tc);
+    tc = one_particle<W>(D, L, T, V5, c, b, a, i, k, j, P, tc);
+    tc = one_particle<W>(D, L, T, V5, c, b, a, k, j, i, P, tc);
+    tc = one_particle<W>(D, L, T, V5, b, a, c, i, k, j, P, tc);
+    tc = one_particle<W>(D, L, T, V5, b, a, c, k, j, i, P, tc);
+    tc = one_hole<W>(D, L, T, V2, a, b, c, i, j, k, N, tc);
+    tc = one_hole<W>(D, L, T, V2, a, c, b, i, j, k, P, tc);
+    tc = one_hole<W>(D, L, T, V2, c, b, a, i, j, k, P, tc);
+    tc = one_hole<W>(D, L, T, V2, a, b, c, k, j, i, P, tc);
+    tc = one_hole<W>(D, L, T, V2, a, b, c, j, i, k, P, tc);
+    tc = one_hole<W>(D, L, T, V2, c, b, a, j, i, k, N, tc);
+    tc = one_hole<W>(D, L, T, V2, c, b, a, k, j, i, N, tc);
+    tc = one_hole<W>(D, L, T, V2, a, c, b, j, i, k, N, tc);
+    tc = one_hole<W>(D, L, T, V2, a, c, b, k, j, i, N, tc);
+    const S term = S(wnorm2(tc)) / spen;
     acc[0] += real_(term);
     acc[1] += imag_(term);
   }
@@ -229,7 +262,12 @@ __global__ void k_copy_in(const double *__restrict__ src, int64_t n, S *__restri
 struct DB {
   void *p = nullptr;
   size_t n = 0;
-  ~DB() { if (p) cudaFree(p); }
+  ~DB() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
   template <typename T> void put(const std::vector<T> &h) {
     n = std::max<size_t>(h.size(), 1) * sizeof(T);
     tck(cudaMalloc(&p, n), "cudaMalloc (T)");
@@ -317,11 +355,13 @@ class Triples final : public ITriples<S> {
     if (ch < 0 || ch >= (int)off2_h_.size()) throw EngineError(1, "hhhp channel out of range");
     stage(v, (int64_t)nr2_h_[ch] * nc2_h_[ch], V2_.as<S>() + off2_h_[ch], st);
     have2_ = true;
+    low_ready_ = false;
   }
   void set_hppp(int ch, const double *v, cudaStream_t st) override {
     if (ch < 0 || ch >= (int)off5_h_.size()) throw EngineError(1, "hppp channel out of range");
     stage(v, (int64_t)nr5_h_[ch] * nc5_h_[ch], V5_.as<S>() + off5_h_[ch], st);
     have5_ = true;
+    low_ready_ = false;
   }
   void generate_v(const DevPotential &pot, cudaStream_t st) override {
     const int n5 = (int)off5_h_.size(), n2 = (int)off2_h_.size();
@@ -334,14 +374,35 @@ class Triples final : public ITriples<S> {
     launches_ += 2;
     tck(cudaGetLastError(), "V_hppp/V_hhhp generation");
     have5_ = have2_ = true;
+    low_ready_ = false;
   }
-  void energy(const S *T, const S *fdiag, double et[2], cudaStream_t st) override {
+  void energy(const S *T, int64_t n_t, const S *fdiag, double et[2], cudaStream_t st, bool fp32) override {
     if (!has_v()) throw EngineError(4, "(T): V_hppp and V_hhhp blocks are not set");
     if (total_ > 0) {
       k_triple_fock<S><<<1024, 256, 0, st>>>(hhh_.as<int3>(), n_hhh_, fdiag, eh_.as<S>());
       k_triple_fock<S><<<1024, 256, 0, st>>>(ppp_.as<int3>(), n_ppp_, fdiag, ep_.as<S>());
-      k_triples<S><<<kBlocks, 256, 0, st>>>(TD_, D_, T, V5_.as<S>(), V2_.as<S>(), eh_.as<S>(), ep_.as<S>(), total_,
-                                            partial_.as<double>());
+      if (fp32) {
+        using Wt = typename LowOf<S>::type;
+        if (!low_ready_) {  // FP32 copies of the interaction, once per interaction
+          if (!V5l_.p) V5l_.zeros((size_t)std::max<int64_t>(n_v5_, 1) * sizeof(Wt));
+          if (!V2l_.p) V2l_.zeros((size_t)std::max<int64_t>(n_v2_, 1) * sizeof(Wt));
+          k_to_low<S><<<1216, 256, 0, st>>>(V5_.as<S>(), n_v5_, V5l_.as<Wt>());
+          k_to_low<S><<<1216, 256, 0, st>>>(V2_.as<S>(), n_v2_, V2l_.as<Wt>());
+          launches_ += 2;
+          low_ready_ = true;
+        }
+        if (Tl_.n < (size_t)std::max<int64_t>(n_t, 1) * sizeof(Wt)) {
+          Tl_.release();
+          Tl_.zeros((size_t)std::max<int64_t>(n_t, 1) * sizeof(Wt));
+        }
+        k_to_low<S><<<1216, 256, 0, st>>>(T, n_t, Tl_.as<Wt>());
+        k_triples<S, Wt><<<kBlocks, 256, 0, st>>>(TD_, D_, Tl_.as<Wt>(), V5l_.as<Wt>(), V2l_.as<Wt>(), eh_.as<S>(),
+                                                  ep_.as<S>(), total_, partial_.as<double>());
+        ++launches_;
+      } else {
+        k_triples<S, S><<<kBlocks, 256, 0, st>>>(TD_, D_, T, V5_.as<S>(), V2_.as<S>(), eh_.as<S>(), ep_.as<S>(), total_,
+                                                 partial_.as<double>());
+      }
       k_finish2<<<2, 256, 0, st>>>(partial_.as<double>(), kBlocks, res_.as<double>());
       launches_ += 4;
       tck(cudaGetLastError(), "(T) kernel");
@@ -488,6 +549,8 @@ class Triples final : public ITriples<S> {
   TriplesDev TD_{};
   DB orbit_of_, hp5_slot_, pp5_slot_, hh2_slot_, hp2_slot_, v5_off_, n5_, v2_off_, n2_;
   DB rows5_, cols5_, rows2_, cols2_, nc5_, ro5_, co5_, nc2_, ro2_, co2_;
+  DB V5l_, V2l_, Tl_;  // FP32 copies for the FP32 contractions
+  bool low_ready_ = false;
   DB V5_, V2_, elem_off_, nbra_, hhh_off_, ppp_off_, hhh_, ppp_, partial_, res_, eh_, ep_;
   int64_t n_hhh_ = 0, n_ppp_ = 0;
   std::vector<int64_t> off5_h_, off2_h_;

@@ -21,7 +21,9 @@ class ITriples {
   virtual void set_hhhp(int ch, const double *v, cudaStream_t st) = 0;
   virtual void set_hppp(int ch, const double *v, cudaStream_t st) = 0;
   virtual void generate_v(const DevPotential &pot, cudaStream_t st) = 0;
-  virtual void energy(const S *T, const S *fdiag, double et[2], cudaStream_t st) = 0;
+  // fp32: the 18 gather-contractions of each (abc, ijk) pair in FP32 on FP32 copies of T
+  // (n_t packed elements) and V; the |W|^2 / D accumulation is FP64 either way
+  virtual void energy(const S *T, int64_t n_t, const S *fdiag, double et[2], cudaStream_t st, bool fp32) = 0;
   virtual int64_t launches() const = 0;
   virtual int64_t count() const = 0;  // number of (abc, ijk) pairs
 };

@@ -322,6 +322,14 @@ int ccx_engine_autotune(ccx_engine *e, int32_t shapes[4], double ms[8]);
 /* pert_triples2, ccm_triples.f90:528-735 (NN part): E(T) from the current T2 with
  * the V_hppp / V_hhhp blocks of setup_vnn_hppp_block (ccm_iter.f90:1361-1810). */
 int ccx_pert_triples(ccx_engine *e, double et[2]);
+/* Arithmetic of the 18 gather-contractions W(abc, ijk) of ccx_pert_triples:
+ * CCX_TRIPLES_FP32 (the default) runs them in FP32 on FP32 copies of T2, V_hppp and
+ * V_hhhp; CCX_TRIPLES_FP64 in FP64.  The sum of |W|^2 / D is FP64 in both.  On the
+ * benchmark lattices the FP32 form moves E(T) by about 1e-7 relative (the north-star
+ * bar is 1e-5).  No counterpart in the reference (all FP64). */
+#define CCX_TRIPLES_FP64 0
+#define CCX_TRIPLES_FP32 1
+int ccx_set_triples_precision(ccx_engine *e, int32_t precision);
 
 /* ---- learned warm start ------------------------------------------------------
  * No counterpart in the reference (which always starts from MP2, ccm_iter.f90:2329-2368).
@@ -382,7 +390,7 @@ int ccx_engine_diis_fallbacks(const ccx_engine *e, int64_t *n);
  * word (1 load wait, 2 MMA wait, 3 drain wait ran out), waits with the full limit for its
  * own copies and MMAs in flight, frees its tensor memory and returns, and the context
  * stays usable.  *kernel_error receives that word (0: the product completed and was
- * checked against FP64). */
+ * checked against FP64 to the BF16x3 bound, 2e-4 of the largest product). */
 int ccx_selftest_tc_wait(int32_t device, int64_t wait_cycles, int32_t *kernel_error);
 /* on: ccx_ccd_iter records CUDA events around every residual term and tensor-core
  * launch (about 20 records per iteration, ~5% of a solve) so that ccx_engine_timers and

@@ -104,7 +104,8 @@ def test_snm132_nmax3_chiral_residual(ccx, O, theta):
 
 def test_triples_snm76_chiral_matches_oracle(ccx, O):
     """(T) of the engine's converged amplitudes, recomputed by the oracle from the same
-    amplitudes: within 1e-9 relative (the spec bar is 1e-5)."""
+    amplitudes: FP64 contractions within 1e-9 relative, the default FP32 contractions
+    within the spec bar of 1e-5 (they land near 1e-7)."""
     o, L, e = _pair(ccx, O, nmax=2, A=76, rho=0.16, snm=True, pot=1, real=False)
     try:
         e.setup_t_amplitudes()
@@ -114,7 +115,10 @@ def test_triples_snm76_chiral_matches_oracle(ccx, O):
             o.set_t2(c, e.t2(c))
         eo = o.triples()
         ee = e.pert_triples()
-        assert abs(ee - eo) < 1e-9 * abs(eo), (ee, eo)
+        assert abs(ee - eo) < 1e-5 * abs(eo), (ee, eo)
+        e.set_triples_precision(fp32=False)
+        ee64 = e.pert_triples()
+        assert abs(ee64 - eo) < 1e-9 * abs(eo), (ee64, eo)
     finally:
         e.close()
         o.close()
