@@ -32,6 +32,7 @@ import argparse
 import ctypes as C
 import importlib.util
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -524,12 +525,21 @@ def run_e2e(args, ccx, torch, L, e, local, real, solve):
     eb = ccx.Engine(L, device=local, real=real)
     stream = torch.cuda.ExternalStream(eb.stream(), device=local)
 
+    phase = {"set_fock_and_vblocks": 0.0, "solve": 0.0, "get_t2_all": 0.0}
+
     def step():
+        t0 = time.perf_counter()
         ccx._check(lib.ccx_set_fock(eb._h, C.c_void_p(fock), e0buf))
         for kind, nb, chs, ptrs in calls:
             ccx._check(lib.ccx_set_vblocks(eb._h, kind, nb, chs, ptrs))
+        t1 = time.perf_counter()
         r = solve(eb)
+        t2 = time.perf_counter()
         ccx._check(lib.ccx_get_t2_all(eb._h, C.c_void_p(t_out)))
+        t3 = time.perf_counter()
+        phase["set_fock_and_vblocks"] += t1 - t0
+        phase["solve"] += t2 - t1
+        phase["get_t2_all"] += t3 - t2
         return r
 
     try:
@@ -538,6 +548,8 @@ def run_e2e(args, ccx, torch, L, e, local, real, solve):
         eb.autotune()  # once per engine, as a host would after handing over the interaction
         step()
         torch.cuda.synchronize()
+        for k in phase:
+            phase[k] = 0.0
         ev0 = torch.cuda.Event(enable_timing=True)
         ev1 = torch.cuda.Event(enable_timing=True)
         t0 = time.perf_counter()
@@ -554,12 +566,13 @@ def run_e2e(args, ccx, torch, L, e, local, real, solve):
             b.close()
     return {"value": ms * 1e-3, "unit": "s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
             "host_wall_s": wall, "iterations": r["iterations"],
+            "host_phase_s_per_step": {k: v / args.steps for k, v in phase.items()},
             "path": "ccx_set_fock + ccx_set_vblocks (all HHPP/PPPP/HHHH/HPHP blocks, one call per family) + "
                     "ccx_setup_t_amplitudes + ccx_ccd_iter + ccx_get_t2_all",
-            "host_buffers": "page-locked (cudaHostRegister): the packing kernels read the reference-layout "
-                            "blocks in place over NVLink-C2C (only the cache lines of unique pairs) and the "
-                            "amplitudes are unpacked straight into the host buffer; h2d_bytes_per_step is the "
-                            "size of the host inputs"}
+            "host_buffers": "page-locked (cudaHostRegister): blocks are read in place over NVLink-C2C by the "
+                            "packing kernels (only the cache lines of unique pairs), or, for a block family above "
+                            "16 GB, staged through the copy engines; the amplitudes are unpacked straight into "
+                            "the host buffer; h2d_bytes_per_step is the size of the host inputs"}
 
 
 TWIST_LATTICES = {
@@ -592,6 +605,7 @@ def run_twists(args):
     total_s includes that set-up; solve_s counts only the solves.  The plain FP64 form is
     timed on a seeded sample of the twists (plain_twists) and scaled to N."""
     import random
+    from concurrent.futures import ThreadPoolExecutor
     import torch
     ccx = load_pkg()
     lat = TWIST_LATTICES[args.lattice]
@@ -603,13 +617,24 @@ def run_twists(args):
     rb = ccx.REBASE_DIGITS if (prec and args.rebase == "digits") else ccx.REBASE_FP64
     opts = dict(precision=prec, rebase=rb, tol=args.tol, max_iter=200, diis_dim=8)
 
-    def build(th, precision, rebase):
-        L = ccx.Layout.from_basis(lat["nmax"], lat["A"], lat["rho"], snm=lat["snm"], theta=th)
+    def layout(th):
+        return ccx.Layout.from_basis(lat["nmax"], lat["A"], lat["rho"], snm=lat["snm"], theta=th)
+
+    def engine(L, th, precision, rebase):
         e = ccx.Engine(L, real=(pot == 0 and not any(th)))
         e.generate(potential=pot)
         e.setup_t_amplitudes()
         e.prepare(precision=precision, rebase=rebase)
         return e
+
+    def build(th, precision, rebase):
+        return engine(layout(th), th, precision, rebase)
+
+    # host threads: the C library releases the interpreter lock in every call, so the
+    # layouts of the next batch are built while the current batch solves, and a batch's
+    # engines are set up side by side (each on its own stream)
+    workers = ThreadPoolExecutor(max_workers=max(1, min(16, os.cpu_count() or 1)))
+    ahead = ThreadPoolExecutor(max_workers=1)
 
     # engines per batch: the device memory of one prepared engine of the largest twist
     probe = build(grid[0][0], prec, rb)
@@ -622,14 +647,22 @@ def run_twists(args):
     if args.twist_batch:
         wave = min(wave, args.twist_batch)
 
+    def layouts(lo):
+        return list(workers.map(layout, [th for th, _ in grid[lo:lo + wave]]))
+
     def batched_pass():
         """All twists, batch after batch; returns (total_s, solve_s, results)."""
         res = [None] * len(grid)
         solve_s = 0.0
         torch.cuda.synchronize()
         t0 = time.perf_counter()
+        nxt = ahead.submit(layouts, 0)
         for w0 in range(0, len(grid), wave):
-            engines = [build(th, prec, rb) for th, _ in grid[w0:w0 + wave]]
+            Ls = nxt.result()
+            if w0 + wave < len(grid):
+                nxt = ahead.submit(layouts, w0 + wave)
+            ths = [th for th, _ in grid[w0:w0 + wave]]
+            engines = list(workers.map(lambda a: engine(a[0], a[1], prec, rb), zip(Ls, ths)))
             torch.cuda.synchronize()
             t1 = time.perf_counter()
             rs, _ = ccx.ccd_iter_batch(engines, **opts)
@@ -707,6 +740,82 @@ def run_twists(args):
             "dE_per_A_keV_batched_vs_sequential": abs(ea - ea_seq) * 1e3,
             "max_dE_per_A_keV_vs_fp64_on_sample": d_kev,
             "clocks": clk}
+    workers.shutdown()
+    ahead.shutdown()
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_learned(args):
+    """The learned warm start over a density sweep (17 densities 0.04 .. 0.20 fm^-3 of one
+    lattice at seeded twists).  The network is trained on the even-indexed densities of
+    the training twists, each sample with its prior: the converged-minus-MP2 correction
+    interpolated from the even densities on either side.  On held-out twists, the even
+    densities are converged from MP2, and every odd density is solved twice to ||R - D T||
+    < tol: from MP2 and from the network with the prior of its two even neighbours.  Both
+    reach the same E/A; the report gives the iterations and device seconds of both."""
+    import random
+    import torch
+    ccx = load_pkg()
+    lat = TWIST_LATTICES[args.lattice]
+    rhos = [round(0.04 + 0.01 * k, 2) for k in range(17)]
+    rng = random.Random(20261203)
+    twists = [tuple(rng.uniform(-math.pi, math.pi) for _ in range(3)) for _ in range(32)]
+    train_tw, eval_tw = twists[:args.learn_twists], twists[args.learn_twists:args.learn_twists + args.eval_twists]
+    prec = PRECISIONS[args.precision]
+    rb = ccx.REBASE_DIGITS if (prec and args.rebase == "digits") else ccx.REBASE_FP64
+    opts = dict(mode=ccx.MODE_STANDARD, precision=prec, rebase=rb, tol=args.tol, max_iter=200, diis_dim=8)
+
+    def converged(rho, th):
+        L = ccx.Layout.from_basis(lat["nmax"], lat["A"], rho, snm=lat["snm"], theta=th)
+        e = ccx.Engine(L, real=True)
+        e.generate(potential=lat.get("potential", 0))
+        e.setup_t_amplitudes()
+        r = e.ccd_iter(**opts)
+        return e, r
+
+    lrn = ccx.Learner(seed=20261203)
+    stride = max(1, args.learn_stride)
+    t0 = time.perf_counter()
+    for th in train_tw:
+        even = {k: converged(rhos[k], th)[0] for k in range(0, 17, 2)}
+        for k, e in even.items():
+            nb = [j for j in (k - 2, k + 2) if j in even]
+            lrn.set_prior([even[j] for j in nb], [1.0 / len(nb)] * len(nb))
+            lrn.add_solution(e, stride=stride)
+        for e in even.values():
+            e.close()
+    loss = lrn.train(steps=args.learn_steps, batch=8192, lr=2e-3, seed=1)
+    train_s = time.perf_counter() - t0
+    rows = []
+    for th in eval_tw:
+        even = {k: converged(rhos[k], th)[0] for k in range(0, 17, 2)}
+        for k in range(1, 17, 2):
+            e, r_mp2 = converged(rhos[k], th)
+            lrn.set_prior([even[k - 1], even[k + 1]], [0.5, 0.5])
+            lrn.warm_start(e)
+            r_ml = e.ccd_iter(**opts)
+            ea_mp2 = (e.e0() + r_mp2["e_ccd"]).real / lat["A"]
+            ea_ml = (e.e0() + r_ml["e_ccd"]).real / lat["A"]
+            rows.append((r_mp2["iterations"], r_ml["iterations"], r_mp2["seconds"], r_ml["seconds"],
+                         abs(ea_ml - ea_mp2) * 1e3, r_mp2["converged"] and r_ml["converged"]))
+            e.close()
+        for x in even.values():
+            x.close()
+    it0 = sum(x[0] for x in rows) / len(rows)
+    it1 = sum(x[1] for x in rows) / len(rows)
+    s0 = sum(x[2] for x in rows)
+    s1 = sum(x[3] for x in rows)
+    line = {"metric": "CCD iterations and device seconds to ||R - D T|| < %g, learned vs MP2 start" % args.tol,
+            "impl": "ours", "lattice": lat["desc"], "densities": rhos, "train_twists": len(train_tw),
+            "eval_twists": len(eval_tw), "held_out_solves": len(rows),
+            "form": args.precision + (" + " + args.rebase + " re-bases" if prec else ""),
+            "training": {"samples": lrn.samples(), "stride": stride, "steps": args.learn_steps, "loss": loss,
+                         "seconds_incl_solves": train_s},
+            "iterations_mp2_mean": it0, "iterations_learned_mean": it1,
+            "solve_s_mp2_total": s0, "solve_s_learned_total": s1, "speedup_learned": s0 / s1 if s1 else None,
+            "fewer_iterations_on": sum(1 for x in rows if x[1] < x[0]), "more_iterations_on": sum(1 for x in rows if x[1] > x[0]),
+            "max_dE_per_A_keV": max(x[4] for x in rows), "all_converged": all(x[5] for x in rows)}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -729,10 +838,18 @@ def main():
     ap.add_argument("--plain-twists", type=int, default=4, help="twists of the plain FP64 GPU sample")
     ap.add_argument("--rebase", default="digits", choices=["fp64", "digits"],
                     help="pp-ladder product of a re-base: FP64 FMA GEMM or exact digit products on the tensor cores")
+    ap.add_argument("--learned", action="store_true",
+                    help="run the learned-warm-start density sweep on --lattice instead of the headline")
+    ap.add_argument("--learn-twists", type=int, default=4)
+    ap.add_argument("--eval-twists", type=int, default=4)
+    ap.add_argument("--learn-steps", type=int, default=3000)
+    ap.add_argument("--learn-stride", type=int, default=4, help="every k-th amplitude as a training sample")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     wl = WORKLOADS[args.workload]
+    if args.learned and args.impl == "ours":
+        return run_learned(args)
     if args.twists > 0 and args.impl == "ours":
         return run_twists(args)
     if args.impl == "reference":

@@ -147,6 +147,8 @@ def lib():
         "ccx_learner_create": ([i32, C.c_uint64, C.POINTER(vp)], C.c_int),
         "ccx_learner_destroy": ([vp], C.c_int),
         "ccx_learner_add_solution": ([vp, vp], C.c_int),
+        "ccx_learner_add_solution_sampled": ([vp, vp, i32], C.c_int),
+        "ccx_learner_set_prior": ([vp, i32, vp, vp], C.c_int),
         "ccx_learner_clear": ([vp], C.c_int),
         "ccx_learner_samples": ([vp, vp], C.c_int),
         "ccx_learner_train": ([vp, i32, i32, C.c_double, C.c_uint64, C.POINTER(C.c_double)], C.c_int),
@@ -233,7 +235,7 @@ def ccd_iter_batch(engines, mode=MODE_STANDARD, precision=PREC_FP64, max_iter=20
     return out, sec.value
 
 
-ML_FEATURES, ML_PARAMS = 16, 35329
+ML_FEATURES, ML_PARAMS = 18, 35585
 
 
 class Learner:
@@ -255,8 +257,20 @@ class Learner:
         except Exception:
             pass
 
-    def add_solution(self, engine: "Engine"):
-        _check(lib().ccx_learner_add_solution(self._h, engine._h))
+    def add_solution(self, engine: "Engine", stride: int = 1):
+        """Training samples from the engine's converged T2 (every stride-th amplitude)."""
+        if stride == 1:
+            _check(lib().ccx_learner_add_solution(self._h, engine._h))
+        else:
+            _check(lib().ccx_learner_add_solution_sampled(self._h, engine._h, int(stride)))
+
+    def set_prior(self, engines=(), weights=()):
+        """Prior feature: sum_i weights[i] x the converged-minus-MP2 correction of
+        engines[i] (neighbouring densities of the same lattice); no engines clears it."""
+        n = len(engines)
+        hs = (vp * max(n, 1))(*[e._h for e in engines])
+        ws = (C.c_double * max(n, 1))(*[float(w) for w in weights])
+        _check(lib().ccx_learner_set_prior(self._h, n, hs, ws))
 
     def clear(self):
         _check(lib().ccx_learner_clear(self._h))

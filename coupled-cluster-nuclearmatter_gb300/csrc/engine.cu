@@ -417,8 +417,11 @@ class Engine final : public IEngine {
     pot.kind = p.kind;
     pot.f32_literals = p.f32_literals;
     draw_lecs(p.lec_seed, pot.lec);
+    const int npp = npp_total_, nhh = nhh_total_;
+    if (ScalarOf<S>::complex && p.kind == 1)
+      pairf_.alloc(((size_t)npp + nhh + (size_t)D_.A * D_.NP) * sizeof(double) + 8, &bytes_);
     launch_generate<S>(D_, O_, pot, Vhp_.as<S>(), Vpp_.as<S>(), Vhh_.as<S>(), W_.as<S>(), fdiag_.as<S>(), f6_.as<S>(),
-                       f7_.as<S>(), res_.as<double>(), st_);
+                       f7_.as<S>(), res_.as<double>(), pairf_.as<double>(), npp, nhh, st_);
     launches_ += 6;
     CK(cudaMemcpyAsync(host_res_, res_.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, st_));
     CK(cudaStreamSynchronize(st_));
@@ -896,6 +899,8 @@ class Engine final : public IEngine {
     upload(dt_off_, t_off, &bytes_); upload(dvpp_off_, vpp_off, &bytes_); upload(dhh2_off_, hh2_off, &bytes_);
     upload(dpp_off_, pp_off, &bytes_); upload(dhh_off_, hh_off, &bytes_);
     upload(dpp_orb_, pp_orb, &bytes_); upload(dhh_orb_, hh_orb, &bytes_);
+    npp_total_ = (int)pp_orb.size();
+    nhh_total_ = (int)hh_orb.size();
     upload(dpp_row_, pp_row, &bytes_); upload(dhh_row_, hh_row, &bytes_);
     upload(dpp_slot_, pp_slot, &bytes_); upload(dhh_slot_, hh_slot, &bytes_);
     upload(dpartner_, partner_, &bytes_);
@@ -2413,6 +2418,8 @@ class Engine final : public IEngine {
   DBuf onx_, ony_, onz_, osz_, otz_, okx_, oky_, okz_, oe_;
   // state
   DBuf T_, R_, Vhp_, Vpp_, Vhh_, X_, I9_, Tph_, Rph_, Vph_, W_, I4_, fdiag_, f6_, f7_, d2ij_, d2ab_, i6off_, i7off_;
+  DBuf pairf_;  // per-pair factors of the chiral-like generation
+  int npp_total_ = 0, nhh_total_ = 0;  // packed pp and hh pairs over all channels
   DBuf partial_, res_, flag_, stage_, hist_, hist_t_, hist_e_, xwork_, xgroups_, xpart_, i6rows_, i6dots_, omap_, rmap_;
   int nxwork_ = 0, nxgroups_ = 0, ni6rows_ = 0;
   Plan planLadder_, planI4_, planRing_, planPP_, planHH_;

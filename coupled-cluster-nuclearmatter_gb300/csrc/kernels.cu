@@ -1170,26 +1170,50 @@ template <typename S> void launch_build_vph(const DevLayout &L, const S *Vhp, S 
 // ============================================================================
 
 
+// antisymmetrised element; with pair factors (complex engines, chiral-like kind) the
+// relativity and regulator factors come from the per-pair table instead
 template <typename S>
-__global__ void k_gen_tblocks(DevLayout L, DevOrbits O, DevPotential P, S *Vhp) {
+__device__ inline S gen_anti(const DevOrbits &O, const DevPotential &P, int p, int q, int r, int s, const double *fpq,
+                             const double *frs) {
+  if constexpr (ScalarOf<S>::complex) {
+    if (fpq) return pot::chiral_anti_factored(O, P, p, q, r, s, *fpq, *frs);
+  }
+  return pot::vanti<S>(O, P, p, q, r, s);
+}
+// F(pq) (chiral_pair_factor) of every packed pp pair, every packed hh pair and every
+// (hole, particle) pair, once per generation: pairf = [pp | hh | hp (A x NP)]
+__global__ void k_pair_factors(DevLayout L, DevOrbits O, int npp, int nhh, double *pairf) {
+  const int64_t nhp = (int64_t)L.A * L.NP, n = npp + nhh + nhp;
+  for (int64_t x = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; x < n; x += (int64_t)gridDim.x * blockDim.x) {
+    int p, q;
+    if (x < npp) { p = L.pp_orb[x].x; q = L.pp_orb[x].y; }
+    else if (x < npp + nhh) { p = L.hh_orb[x - npp].x; q = L.hh_orb[x - npp].y; }
+    else { const int64_t y = x - npp - nhh; p = (int)(y / L.NP); q = L.A + (int)(y % L.NP); }
+    pairf[x] = pot::chiral_pair_factor(O, p, q);
+  }
+}
+template <typename S>
+__global__ void k_gen_tblocks(DevLayout L, DevOrbits O, DevPotential P, const double *ppf, const double *hhf, S *Vhp) {
   const int2 tl = L.ttile[blockIdx.x];
   const int ch = tl.x, Pc = L.P[ch], H = L.H[ch];
   const int64_t n = (int64_t)Pc * H, end = min((int64_t)tl.y + kTileElems, n);
   for (int64_t e = tl.y + threadIdx.x; e < end; e += blockDim.x) {
     const int ij = (int)(e / Pc), ab = (int)(e % Pc);  // Vhp'(ij', ab') at ij'*P + ab'
-    const int2 h = L.hh_orb[L.hh_off[ch] + ij], p = L.pp_orb[L.pp_off[ch] + ab];
-    Vhp[L.t_off[ch] + e] = pot::vanti<S>(O, P, h.x, h.y, p.x, p.y);
+    const int hi = L.hh_off[ch] + ij, pi = L.pp_off[ch] + ab;
+    const int2 h = L.hh_orb[hi], p = L.pp_orb[pi];
+    Vhp[L.t_off[ch] + e] = gen_anti<S>(O, P, h.x, h.y, p.x, p.y, hhf ? hhf + hi : nullptr, ppf ? ppf + pi : nullptr);
   }
 }
 template <typename S>
-__global__ void k_gen_vpp(DevLayout L, DevOrbits O, DevPotential P, S *Vpp) {
+__global__ void k_gen_vpp(DevLayout L, DevOrbits O, DevPotential P, const double *ppf, S *Vpp) {
   const int2 tl = L.vtile[blockIdx.x];
   const int ch = tl.x, Pc = L.P[ch];
   const int64_t n = (int64_t)Pc * Pc, end = min((int64_t)tl.y + kTileElems, n);
   for (int64_t e = tl.y + threadIdx.x; e < end; e += blockDim.x) {
     const int r = (int)(e / Pc), c = (int)(e % Pc);
-    const int2 x = L.pp_orb[L.pp_off[ch] + r], y = L.pp_orb[L.pp_off[ch] + c];
-    Vpp[L.vpp_off[ch] + e] = pot::vanti<S>(O, P, x.x, x.y, y.x, y.y);
+    const int ri = L.pp_off[ch] + r, ci = L.pp_off[ch] + c;
+    const int2 x = L.pp_orb[ri], y = L.pp_orb[ci];
+    Vpp[L.vpp_off[ch] + e] = gen_anti<S>(O, P, x.x, x.y, y.x, y.y, ppf ? ppf + ri : nullptr, ppf ? ppf + ci : nullptr);
   }
 }
 template <typename S>
@@ -1204,13 +1228,16 @@ __global__ void k_gen_vhh(DevLayout L, DevOrbits O, DevPotential P, S *Vhh) {
   }
 }
 template <typename S>
-__global__ void k_gen_w(DevLayout L, DevOrbits O, DevPotential P, S *W) {
+__global__ void k_gen_w(DevLayout L, DevOrbits O, DevPotential P, const double *hpf, S *W) {
   for (int q = blockIdx.x; q < L.nph; q += gridDim.x) {
     const int nhp = L.n_hp[q];
     for (int64_t e = threadIdx.x; e < (int64_t)nhp * nhp; e += blockDim.x) {
       const int r = (int)(e % nhp), c = (int)(e / nhp);
       const int2 ia = L.hp_orb[L.hp_off[q] + r], jb = L.hp_orb[L.hp_off[q] + c];
-      W[L.i4_off[q] + e] = S(0.0) - pot::vanti<S>(O, P, ia.x, jb.y, jb.x, ia.y);
+      // -<ib|V|ja>_A; pair factors F(ib), F(ja) from the (hole, particle) table
+      const double *fib = hpf ? hpf + (int64_t)ia.x * L.NP + (jb.y - L.A) : nullptr;
+      const double *fja = hpf ? hpf + (int64_t)jb.x * L.NP + (ia.y - L.A) : nullptr;
+      W[L.i4_off[q] + e] = S(0.0) - gen_anti<S>(O, P, ia.x, jb.y, jb.x, ia.y, fib, fja);
     }
   }
 }
@@ -1251,11 +1278,15 @@ __global__ void k_gen_e0(DevLayout L, DevOrbits O, DevPotential P, double *e0) {
 
 template <typename S>
 void launch_generate(const DevLayout &L, const DevOrbits &O, const DevPotential &pot, S *Vhp, S *Vpp, S *Vhh, S *W,
-                     S *fdiag, S *f6, S *f7, double *e0, cudaStream_t st) {
-  if (L.nttile) k_gen_tblocks<S><<<L.nttile, 256, 0, st>>>(L, O, pot, Vhp);
-  if (L.nvtile) k_gen_vpp<S><<<L.nvtile, 256, 0, st>>>(L, O, pot, Vpp);
+                     S *fdiag, S *f6, S *f7, double *e0, double *pairf, int npp, int nhh, cudaStream_t st) {
+  const bool factored = ScalarOf<S>::complex && pot.kind == 1 && pairf;
+  double *ppf = factored ? pairf : nullptr, *hhf = factored ? pairf + npp : nullptr;
+  double *hpf = factored ? pairf + npp + nhh : nullptr;
+  if (factored) k_pair_factors<<<1216, 256, 0, st>>>(L, O, npp, nhh, pairf);
+  if (L.nttile) k_gen_tblocks<S><<<L.nttile, 256, 0, st>>>(L, O, pot, ppf, hhf, Vhp);
+  if (L.nvtile) k_gen_vpp<S><<<L.nvtile, 256, 0, st>>>(L, O, pot, ppf, Vpp);
   if (L.nch) k_gen_vhh<S><<<min(L.nch, 4096), 128, 0, st>>>(L, O, pot, Vhh);
-  if (L.nph) k_gen_w<S><<<min(L.nph, 4096), 128, 0, st>>>(L, O, pot, W);
+  if (L.nph) k_gen_w<S><<<min(L.nph, 4096), 128, 0, st>>>(L, O, pot, hpf, W);
   k_gen_fock<S><<<(L.ns + 127) / 128, 128, 0, st>>>(L, O, pot, fdiag, f6, f7);
   k_gen_e0<S><<<1, 256, 0, st>>>(L, O, pot, e0);
 }
@@ -1427,7 +1458,7 @@ void launch_unpack_t(const DevLayout &L, int ch, int n_pp, const int *pp_signed,
                                   int *, cudaStream_t);                                                                \
   template void launch_build_vph<S>(const DevLayout &, const S *, S *, cudaStream_t);                                 \
   template void launch_generate<S>(const DevLayout &, const DevOrbits &, const DevPotential &, S *, S *, S *, S *,    \
-                                   S *, S *, S *, double *, cudaStream_t);                                             \
+                                   S *, S *, S *, double *, double *, int, int, cudaStream_t);                                             \
   template void launch_mp2<S>(const DevLayout &, const S *, const S *, S *, cudaStream_t);                            \
   template void launch_pack_t<S>(const DevLayout &, int, int, const double *, S *, int *, cudaStream_t);          \
   template void launch_axpy<S>(int64_t, const S *, S *, cudaStream_t);                                                 \

@@ -144,8 +144,10 @@ void launch_build_w(const DevLayout &L, const int2 *hp4_slot, const int64_t *v4_
                     S *W, int *flag, cudaStream_t st);
 template <typename S> void launch_build_vph(const DevLayout &L, const S *Vhp, S *Vph, cudaStream_t st);
 template <typename S>
+// pairf: npp + nhh + A (ns - A) doubles of scratch for the per-pair factors of the
+// chiral-like kind (complex engines; null: every element evaluated in full)
 void launch_generate(const DevLayout &L, const DevOrbits &O, const DevPotential &pot, S *Vhp, S *Vpp, S *Vhh, S *W,
-                     S *fdiag, S *f6, S *f7, double *e0, cudaStream_t st);
+                     S *fdiag, S *f6, S *f7, double *e0, double *pairf, int npp, int nhh, cudaStream_t st);
 // ordered block of <row|V|col> (or <col|V|row> when swap) into interleaved doubles
 template <typename S>
 void launch_gen_ordered(const DevOrbits &O, const DevPotential &pot, const int2 *rows, const int2 *cols, int nr, int nc,

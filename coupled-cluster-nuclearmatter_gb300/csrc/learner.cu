@@ -46,6 +46,7 @@ struct MLCtx {
   DevLayout L;
   DevOrbits O;
   const double *fd, *V;
+  const float *prior;  // per packed amplitude, or null
   float rho, kF, eF, vol, th[3];
 };
 
@@ -83,6 +84,9 @@ __device__ void ml_feat(const MLCtx &c, int ch, int e, float (&f)[kMlIn], double
   f[13] = (float)(c.O.sz[a] * c.O.sz[i]);
   f[14] = (float)(c.O.tz[a] * c.O.tz[b]);
   f[15] = (float)(c.O.tz[a] * c.O.tz[i]);
+  // the prior: the correction interpolated from neighbouring converged solutions
+  f[16] = c.prior ? c.prior[c.L.t_off[ch] + e] : 0.0f;
+  f[17] = c.prior ? 1.0f : 0.0f;
 }
 
 // Target: the correction of the amplitude numerator, y = (T - T_MP2) D vol / kMlNum, with
@@ -90,8 +94,29 @@ __device__ void ml_feat(const MLCtx &c, int ch, int e, float (&f)[kMlIn], double
 // error in y is a uniform error in the residual of the start.
 constexpr double kMlNum = 1000.0;  // MeV fm^3
 
-// training samples of a converged solution: X[g] features, y[g] the numerator correction
-__global__ void k_ml_extract(MLCtx c, const double *__restrict__ T, float *__restrict__ X, float *__restrict__ y) {
+// training samples of a converged solution, every stride-th packed amplitude g:
+// X[g / stride] features, y[g / stride] the numerator correction
+__global__ void k_ml_extract(MLCtx c, const double *__restrict__ T, int stride, float *__restrict__ X,
+                             float *__restrict__ y) {
+  const int2 tl = c.L.ttile[blockIdx.x];
+  const int ch = tl.x;
+  const int n = c.L.P[ch] * c.L.H[ch];
+  const int end = min(tl.y + kTileElems, n);
+  for (int e = tl.y + threadIdx.x; e < end; e += blockDim.x) {
+    const int64_t g = c.L.t_off[ch] + e;
+    if (g % stride) continue;
+    float f[kMlIn];
+    double tmp2;
+    ml_feat(c, ch, e, f, tmp2);
+    const int64_t o = g / stride;
+#pragma unroll
+    for (int q = 0; q < kMlIn; ++q) X[o * kMlIn + q] = f[q];
+    const double D = (double)f[4] * (double)c.eF;
+    y[o] = (float)((T[g] - tmp2) * D * (double)c.vol / kMlNum);
+  }
+}
+// prior += w * (the numerator correction of T), per packed amplitude (c.prior is null)
+__global__ void k_ml_prior(MLCtx c, const double *__restrict__ T, float w, int first, float *__restrict__ prior) {
   const int2 tl = c.L.ttile[blockIdx.x];
   const int ch = tl.x;
   const int n = c.L.P[ch] * c.L.H[ch];
@@ -101,10 +126,9 @@ __global__ void k_ml_extract(MLCtx c, const double *__restrict__ T, float *__res
     double tmp2;
     ml_feat(c, ch, e, f, tmp2);
     const int64_t g = c.L.t_off[ch] + e;
-#pragma unroll
-    for (int q = 0; q < kMlIn; ++q) X[g * kMlIn + q] = f[q];
     const double D = (double)f[4] * (double)c.eF;
-    y[g] = (float)((T[g] - tmp2) * D * (double)c.vol / kMlNum);
+    const float y = (float)((T[g] - tmp2) * D * (double)c.vol / kMlNum);
+    prior[g] = first ? w * y : fmaf(w, y, prior[g]);
   }
 }
 
@@ -315,7 +339,7 @@ __global__ void __launch_bounds__(128, 1) k_ml_infer(InferArgs g) {
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  // biases and output weights; zero feature padding (K columns 16..63, never rewritten)
+  // biases and output weights; zero feature padding (K columns 32..63 are never rewritten)
   for (int x = tid; x < kMlW; x += 128) {
     sp[x] = g.par[kMlOffB1 + x];
     sp[kMlW + x] = g.par[kMlOffB2 + x];
@@ -364,12 +388,16 @@ __global__ void __launch_bounds__(128, 1) k_ml_infer(InferArgs g) {
     }
     if (!live)
       for (int q = 0; q < kMlIn; ++q) f[q] = 0.0f;
-    {
-      uint32_t w[8];
+    {  // features into K columns 0 .. kMlIn - 1 of the tile, zeros up to column 31
+      uint32_t w[16];
 #pragma unroll
-      for (int q = 0; q < 8; ++q) w[q] = bf16_bits(f[2 * q]) | (bf16_bits(f[2 * q + 1]) << 16);
-      *(uint4 *)(smem + kFeatOff + cm_off(tid, 0)) = make_uint4(w[0], w[1], w[2], w[3]);
-      *(uint4 *)(smem + kFeatOff + cm_off(tid, 8)) = make_uint4(w[4], w[5], w[6], w[7]);
+      for (int q = 0; q < 16; ++q) {
+        const float lo = 2 * q < kMlIn ? f[2 * q] : 0.0f, hi = 2 * q + 1 < kMlIn ? f[2 * q + 1] : 0.0f;
+        w[q] = bf16_bits(lo) | (bf16_bits(hi) << 16);
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        *(uint4 *)(smem + kFeatOff + cm_off(tid, 8 * q)) = make_uint4(w[4 * q], w[4 * q + 1], w[4 * q + 2], w[4 * q + 3]);
     }
     float o = 0.0f;
     for (int layer = 0; layer < 3; ++layer) {
@@ -378,8 +406,11 @@ __global__ void __launch_bounds__(128, 1) k_ml_infer(InferArgs g) {
       __syncthreads();
       if (tid == 0) {
         tc_fence_after();
-        if (layer == 0) {
-          tc_mma<kTcBF16>(tmem, smem_desc(smem_u32(smem + kFeatOff)), smem_desc(smem_u32(smem)), idesc16, 0u);
+        if (layer == 0) {  // K = 32: the features and their zero padding
+#pragma unroll
+          for (int ks = 0; ks < 2; ++ks)
+            tc_mma<kTcBF16>(tmem, smem_desc(smem_u32(smem + kFeatOff) + ks * 256), smem_desc(smem_u32(smem) + ks * 256),
+                            idesc16, ks ? 1u : 0u);
         } else {
           const uint32_t wb = smem_u32(smem + (layer == 1 ? kWTile : 3 * kWTile));
 #pragma unroll
@@ -501,17 +532,38 @@ class Learner final : public ILearner {
     if (st_) cudaStreamDestroy(st_);
   }
 
-  void add_solution(const MLView &v) override {
+  void add_solution(const MLView &v, int stride) override {
     lck(cudaSetDevice(device_), "cudaSetDevice");
+    if (stride < 1) throw EngineError(1, "learner: sample stride must be >= 1");
     Chunk c;
-    c.n = v.n_t;
+    c.n = (v.n_t + stride - 1) / stride;
     c.X.alloc((size_t)c.n * kMlIn * 4);
     c.y.alloc((size_t)c.n * 4);
-    const MLCtx ctx = make_ctx(v);
-    if (v.L.nttile) k_ml_extract<<<v.L.nttile, 256, 0, v.st>>>(ctx, v.T, c.X.as<float>(), c.y.as<float>());
+    const MLCtx ctx = ctx_of(v);
+    if (v.L.nttile) k_ml_extract<<<v.L.nttile, 256, 0, v.st>>>(ctx, v.T, stride, c.X.as<float>(), c.y.as<float>());
     lck(cudaGetLastError(), "feature extraction");
     lck(cudaStreamSynchronize(v.st), "feature extraction");
     data_.push_back(std::move(c));
+  }
+  void set_prior(const MLView *views, const double *w, int n) override {
+    lck(cudaSetDevice(device_), "cudaSetDevice");
+    has_prior_ = false;
+    if (n <= 0) return;
+    const int64_t nt = views[0].n_t;
+    for (int i = 1; i < n; ++i)
+      if (views[i].n_t != nt || views[i].L.nch != views[0].L.nch)
+        throw EngineError(1, "learner: the prior's engines have different layouts");
+    if (prior_.bytes < (size_t)std::max<int64_t>(nt, 1) * 4) prior_.alloc((size_t)std::max<int64_t>(nt, 1) * 4);
+    for (int i = 0; i < n; ++i) {
+      MLCtx c = make_ctx(views[i]);
+      c.prior = nullptr;
+      if (views[i].L.nttile)
+        k_ml_prior<<<views[i].L.nttile, 256, 0, views[i].st>>>(c, views[i].T, (float)w[i], i == 0, prior_.as<float>());
+      lck(cudaGetLastError(), "prior");
+      lck(cudaStreamSynchronize(views[i].st), "prior");
+    }
+    prior_n_ = nt;
+    has_prior_ = true;
   }
   void clear() override { data_.clear(); }
   int64_t samples() const override {
@@ -576,7 +628,7 @@ class Learner final : public ILearner {
     lck(cudaSetDevice(device_), "cudaSetDevice");
     upload_weight_tiles();
     InferArgs a{};
-    a.c = make_ctx(v);
+    a.c = ctx_of(v);
     a.use_view = 1;
     a.T = v.T;
     a.wt = wt_.as<uint8_t>();
@@ -646,6 +698,16 @@ class Learner final : public ILearner {
     LBuf X, y;
     int64_t n = 0;
   };
+
+  // the feature context of a view, with the prior when one is set
+  MLCtx ctx_of(const MLView &v) const {
+    MLCtx c = make_ctx(v);
+    if (has_prior_) {
+      if (v.n_t != prior_n_) throw EngineError(1, "learner: the prior was set for another layout");
+      c.prior = prior_.as<float>();
+    }
+    return c;
+  }
 
   void ensure_batch(int b) {
     if (b <= cap_) return;
@@ -761,6 +823,9 @@ class Learner final : public ILearner {
   int64_t t_ = 0;
   bool weights_dirty_ = true;
   std::vector<Chunk> data_;
+  LBuf prior_;
+  int64_t prior_n_ = 0;
+  bool has_prior_ = false;
 };
 
 }  // namespace

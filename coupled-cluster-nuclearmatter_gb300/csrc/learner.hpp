@@ -1,6 +1,7 @@
 // Learned warm start: a 4-layer MLP (width 128, SiLU) that predicts, per packed T2
 // amplitude, the difference between the converged CCD amplitude and its MP2 value from
-// transferable features of the amplitude.  Trained in FP32 on amplitudes the solver
+// transferable features of the amplitude and, when the host sets one, a prior: the same
+// difference interpolated from solutions converged at neighbouring densities.  Trained in FP32 on amplitudes the solver
 // converged on other lattices (densities, twists); inference in BF16 on the tensor
 // cores writes T2 = T_MP2 + correction straight into an engine.  The CCD iteration that
 // follows is unchanged, so the converged energy does not depend on the start.
@@ -15,7 +16,7 @@
 
 namespace ccx {
 
-constexpr int kMlIn = 16;    // features (padded)
+constexpr int kMlIn = 18;    // features: 16 of the amplitude, the prior correction and its flag
 constexpr int kMlW = 128;    // hidden width
 // parameter vector: W1[128][16] b1[128] W2[128][128] b2[128] W3[128][128] b3[128] w4[128] b4
 constexpr int kMlOffW1 = 0, kMlOffB1 = kMlOffW1 + kMlW * kMlIn, kMlOffW2 = kMlOffB1 + kMlW,
@@ -38,8 +39,14 @@ struct MLView {
 class ILearner {
  public:
   virtual ~ILearner() = default;
-  // features and targets (converged T minus MP2) of the view's current amplitudes
-  virtual void add_solution(const MLView &v) = 0;
+  // features and targets (converged T minus MP2) of the view's current amplitudes, every
+  // stride-th packed amplitude
+  virtual void add_solution(const MLView &v, int stride) = 0;
+  // Prior for the features of later add_solution / warm_start calls: sum_i w[i] times the
+  // target correction of views[i]'s current (converged) amplitudes, per packed amplitude.
+  // The views share one layout (another density of the same lattice and twist).  n = 0
+  // clears it (the prior feature and its flag read 0).
+  virtual void set_prior(const MLView *views, const double *w, int n) = 0;
   virtual void clear() = 0;
   virtual int64_t samples() const = 0;
   // Adam on shuffled minibatches; returns the mean loss of the last 10 steps

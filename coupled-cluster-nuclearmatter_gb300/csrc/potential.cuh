@@ -48,6 +48,14 @@ __device__ inline double minnesota(const DevOrbits &O, const DevPotential &P, in
   return ((vs + vr) + vt) / O.volume;
 }
 
+constexpr double kLambda6 = 8.303765625e15;  // (450 MeV)^6 of the regulator exp(-(p/450)^6)
+
+// nucleon mass of a pair's isospin projection (the relativity factor's mass)
+__device__ inline double pair_mass(int t1, int t2) {
+  const int tsum = (t1 + t2) / 2;
+  return tsum < 0 ? 9.38272046000000046e+02 : (tsum == 0 ? 9.38918267117927371e+02 : 9.39565379000000007e+02);
+}
+
 __device__ inline cplx wsig(int ma, int mb, const double w[3]) {
   const int ia = ma > 0 ? 0 : 1, ib = mb > 0 ? 0 : 1;
   if (ia == 0 && ib == 0) return cplx(w[2], 0.0);
@@ -98,10 +106,64 @@ __device__ inline cplx chiral_like(const DevOrbits &O, const DevPotential &P, in
   const cplx cont_lo = cplx(c[0] * dm * dt + c[1] * ss * dt, 0.0);
   const cplx cont_nlo = cplx(c[2] * q2 * dm * dt + c[3] * km2 * dm * dt + c[4] * q2 * ss * dt + c[5] * km2 * ss * dt, 0.0) +
                         (c[6] * dt) * sl + (c[7] * dt) * sq + (c[8] * dt) * sk;
-  const double l2n = pow(450.0, 6.0);
-  const double freg = exp(-(pow(p2, 3.0) / l2n + pow(pp2, 3.0) / l2n));
+  const double l2n = kLambda6;
+  const double freg = exp(-((p2 * p2) * p2 / l2n + (pp2 * pp2) * pp2 / l2n));
   const cplx vdir = ((vlo + cont_lo) + cont_nlo) * (rel * freg);
   return (kHbarc * kHbarc * kHbarc) * vdir * (1.0 / O.volume);
+}
+
+// The chiral-like element factorised as m F(pq) F(rs) core(p, q, r, s): the relativity
+// factor m / ((m^2 + p^2)(m^2 + p'^2))^(1/4) and the regulator exp(-(p^6 + p'^6)/L^6)
+// depend on the relative momentum of one pair each, and both are unchanged when r and s
+// swap, so an antisymmetrised element is m F(pq) F(rs) (core(pqrs) - core(pqsr)).
+// F(pq) is evaluated once per pair; the core per element holds no transcendental.
+__device__ inline double chiral_pair_factor(const DevOrbits &O, int p, int q) {
+  const double x = 0.5 * (O.kx[p] * kHbarc - O.kx[q] * kHbarc), y = 0.5 * (O.ky[p] * kHbarc - O.ky[q] * kHbarc);
+  const double z = 0.5 * (O.kz[p] * kHbarc - O.kz[q] * kHbarc);
+  const double p2 = (x * x + y * y) + z * z;
+  const double mn = pair_mass(O.tz[p], O.tz[q]);
+  return exp(-(p2 * p2) * p2 / kLambda6) / sqrt(sqrt(mn * mn + p2));
+}
+__device__ inline cplx chiral_core(const DevOrbits &O, const DevPotential &P, int p, int q, int r, int s) {
+  if (O.nx[p] + O.nx[q] != O.nx[r] + O.nx[s] || O.ny[p] + O.ny[q] != O.ny[r] + O.ny[s] ||
+      O.nz[p] + O.nz[q] != O.nz[r] + O.nz[s] || O.tz[p] + O.tz[q] != O.tz[r] + O.tz[s])
+    return cplx(0.0, 0.0);
+  double pr[3], pp[3], km[3], qt[3], qxk[3];
+  const double k1[3] = {O.kx[p], O.ky[p], O.kz[p]}, k2[3] = {O.kx[q], O.ky[q], O.kz[q]};
+  const double k3[3] = {O.kx[r], O.ky[r], O.kz[r]}, k4[3] = {O.kx[s], O.ky[s], O.kz[s]};
+  for (int d = 0; d < 3; ++d) {
+    pr[d] = 0.5 * (k1[d] * kHbarc - k2[d] * kHbarc);
+    pp[d] = 0.5 * (k3[d] * kHbarc - k4[d] * kHbarc);
+    km[d] = 0.5 * (pr[d] + pp[d]);
+    qt[d] = pr[d] - pp[d];
+  }
+  const double km2 = (km[0] * km[0] + km[1] * km[1]) + km[2] * km[2];
+  const double q2 = (qt[0] * qt[0] + qt[1] * qt[1]) + qt[2] * qt[2];
+  qxk[0] = qt[1] * km[2] - qt[2] * km[1];
+  qxk[1] = qt[2] * km[0] - qt[0] * km[2];
+  qxk[2] = qt[0] * km[1] - qt[1] * km[0];
+  const int m1 = O.sz[p], m2 = O.sz[q], m3 = O.sz[r], m4 = O.sz[s];
+  const int t1 = O.tz[p], t2 = O.tz[q], t3 = O.tz[r], t4 = O.tz[s];
+  const double dm = kd(m1, m3) * kd(m2, m4), dt = kd(t1, t3) * kd(t2, t4);
+  const double tt = pauli_dot(t1, t2, t3, t4), ss = pauli_dot(m1, m2, m3, m4);
+  const cplx sq = wsig(m1, m3, qt) * wsig(m2, m4, qt);
+  const cplx sk = wsig(m1, m3, km) * wsig(m2, m4, km);
+  const cplx mi(0.0, -0.5);
+  const cplx sl = mi * wsig(m1, m3, qxk) * kd(m2, m4) + mi * wsig(m2, m4, qxk) * kd(m1, m3);
+  const double c2 = (1.27 * 1.27) / (4.0 * 92.4 * 92.4);
+  const double ope = -1.0 * c2 / (q2 + 138.0 * 138.0);
+  const cplx vlo = (ope * tt) * sq;
+  const double *c = P.lec;
+  const cplx cont_lo = cplx(c[0] * dm * dt + c[1] * ss * dt, 0.0);
+  const cplx cont_nlo = cplx(c[2] * q2 * dm * dt + c[3] * km2 * dm * dt + c[4] * q2 * ss * dt + c[5] * km2 * ss * dt, 0.0) +
+                        (c[6] * dt) * sl + (c[7] * dt) * sq + (c[8] * dt) * sk;
+  return (kHbarc * kHbarc * kHbarc) * ((vlo + cont_lo) + cont_nlo) * (1.0 / O.volume);
+}
+// antisymmetrised chiral-like element from the pair factors fpq = F(pq), frs = F(rs)
+__device__ inline cplx chiral_anti_factored(const DevOrbits &O, const DevPotential &P, int p, int q, int r, int s,
+                                            double fpq, double frs) {
+  const double w = pair_mass(O.tz[p], O.tz[q]) * fpq * frs;
+  return (chiral_core(O, P, p, q, r, s) - chiral_core(O, P, p, q, s, r)) * w;
 }
 
 template <typename S> __device__ S vbare(const DevOrbits &O, const DevPotential &P, int p, int q, int r, int s);

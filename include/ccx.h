@@ -333,21 +333,31 @@ int ccx_set_triples_precision(ccx_engine *e, int32_t precision);
 
 /* ---- learned warm start ------------------------------------------------------
  * No counterpart in the reference (which always starts from MP2, ccm_iter.f90:2329-2368).
- * A 4-layer MLP (16 features -> 128 -> 128 -> 128 -> 1, SiLU) predicts per packed T2
+ * A 4-layer MLP (18 features -> 128 -> 128 -> 128 -> 1, SiLU) predicts per packed T2
  * amplitude the difference between the converged CCD amplitude and its MP2 value, from
  * features that transfer across lattices: density, twist, bare denominator / e_F, bare
  * <ij|V|ab> and MP2 amplitude scaled by the volume, momentum transfers and pair momenta
- * / k_F, spin and isospin products.  Training (FP32, Adam) uses amplitudes the solver
- * converged on other lattices; inference runs in BF16 on the tensor cores.  Real
- * engines only.  The CCD iteration from the warm start is unchanged, so the converged
- * energy is the same as from MP2. */
+ * / k_F, spin and isospin products, and a prior with its flag: the same difference
+ * interpolated from solutions the solver converged at neighbouring densities of the
+ * same lattice and twist (ccx_learner_set_prior; 0 and flag 0 without one).  Training
+ * (FP32, Adam) uses amplitudes the solver converged on other lattices; inference runs in
+ * BF16 on the tensor cores.  Real engines only.  The CCD iteration from the warm start
+ * is unchanged, so the converged energy is the same as from MP2. */
 typedef struct ccx_learner ccx_learner;
-#define CCX_ML_FEATURES 16
-#define CCX_ML_PARAMS 35329    /* W1[128][16] b1 W2[128][128] b2 W3[128][128] b3 w4[128] b4, FP32 */
+#define CCX_ML_FEATURES 18
+#define CCX_ML_PARAMS 35585    /* W1[128][18] b1 W2[128][128] b2 W3[128][128] b3 w4[128] b4, FP32 */
 int ccx_learner_create(int32_t device, uint64_t seed, ccx_learner **out);
 int ccx_learner_destroy(ccx_learner *l);
 /* training samples (features, converged - MP2) from the engine's current T2 */
 int ccx_learner_add_solution(ccx_learner *l, ccx_engine *e);
+/* the same with every stride-th packed amplitude (large lattices, many solutions) */
+int ccx_learner_add_solution_sampled(ccx_learner *l, ccx_engine *e, int32_t stride);
+/* Prior of later add_solution / ccx_init_learned calls: sum_i weights[i] times the
+ * converged-minus-MP2 correction of engines[i]'s current T2, per packed amplitude, for
+ * example the two neighbouring densities of the same lattice and twist with weights
+ * 0.5 and 0.5.  The engines share the layout of the engines it is then used with; n = 0
+ * clears the prior. */
+int ccx_learner_set_prior(ccx_learner *l, int32_t n, ccx_engine *const *engines, const double *weights);
 int ccx_learner_clear(ccx_learner *l);
 int ccx_learner_samples(const ccx_learner *l, int64_t *n);
 /* Adam on shuffled minibatches; *loss = mean loss of the last 10 steps */

@@ -6,14 +6,14 @@ code has no learned component (its CCD always starts from MP2 amplitudes,
 ccm_iter.f90:2329-2368), so there is nothing to pin against the reference: the module
 is pinned by finite differences instead (tests/test_mlp_oracle.py).
 
-Network: 16 features -> 128 -> 128 -> 128 -> 1, SiLU after each hidden layer.
+Network: 18 features -> 128 -> 128 -> 128 -> 1, SiLU after each hidden layer.
 Parameter vector (float32 on the device, float64 here), row-major weights [out][in]:
-    W1[128][16] b1[128] W2[128][128] b2[128] W3[128][128] b3[128] w4[128] b4
+    W1[128][18] b1[128] W2[128][128] b2[128] W3[128][128] b3[128] w4[128] b4
 Loss: mean over the batch of (f(x) - y)^2.
 """
 import numpy as np
 
-F, W = 16, 128
+F, W = 18, 128
 OFF_W1 = 0
 OFF_B1 = OFF_W1 + W * F
 OFF_W2 = OFF_B1 + W

@@ -16,7 +16,7 @@ def test_oracle_gradient_matches_finite_differences():
     y = rng.normal(0, 1, 40)
     loss, g = mlp.loss_grad(p, X, y)
     idx = np.concatenate([rng.choice(np.arange(o, o + n), 6, replace=False)
-                          for o, n in ((mlp.OFF_W1, 2048), (mlp.OFF_B1, 128), (mlp.OFF_W2, 16384),
+                          for o, n in ((mlp.OFF_W1, 128 * mlp.F), (mlp.OFF_B1, 128), (mlp.OFF_W2, 16384),
                                        (mlp.OFF_B2, 128), (mlp.OFF_W3, 16384), (mlp.OFF_B3, 128),
                                        (mlp.OFF_W4, 128))] + [[mlp.OFF_B4]])
     h = 1e-6
@@ -30,4 +30,4 @@ def test_oracle_gradient_matches_finite_differences():
 
 
 def test_parameter_layout_size():
-    assert mlp.N_PARAMS == 35329
+    assert mlp.N_PARAMS == 35585 == 128 * 18 + 128 + 2 * (128 * 128 + 128) + 128 + 1
