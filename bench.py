@@ -50,6 +50,8 @@ WORKLOADS = {
                      desc="SNM A=132, rho=0.16 fm^-3, nmax=4 (2916 states), chiral-like (complex V), theta=0"),
     "snm132n3": dict(nmax=3, A=132, rho=0.16, snm=True, potential=1,
                      desc="SNM A=132, rho=0.16 fm^-3, nmax=3 (1372 states), chiral-like (complex V), theta=0"),
+    "snm76n2": dict(nmax=2, A=76, rho=0.16, snm=True, potential=1,
+                    desc="SNM A=76, rho=0.16 fm^-3, nmax=2 (500 states), chiral-like (complex V), theta=0"),
     "pnm66": dict(nmax=4, A=66, rho=0.16, snm=False, potential=0,
                   desc="PNM A=66, rho=0.16 fm^-3, nmax=4 (1458 states), Minnesota, theta=0"),
     "pnm14": dict(nmax=2, A=14, rho=0.08, snm=False, potential=0,
@@ -58,7 +60,7 @@ WORKLOADS = {
 # Iterations the reference algorithm (0.75/0.25 mixing + DIIS every 6, |dE| < 1e-6 MeV,
 # ccm_iter.f90:67-96) takes on each lattice, as run by the engine's reference mode
 # (None: measured by the engine when needed).
-REFERENCE_ITERATIONS = {"pnm66": 13, "pnm14": 13, "snm132n4": None, "snm132n3": None}
+REFERENCE_ITERATIONS = {"pnm66": 13, "pnm14": 13, "snm132n4": 19, "snm132n3": None, "snm76n2": None}
 
 
 def load_pkg():
@@ -460,29 +462,21 @@ def reference_iterations(e, ccx):
 
 
 class PinnedHost:
-    """One page-locked host buffer (numpy memory registered with CUDA, so that the device
-    can address it in place) holding many blocks back to back."""
+    """One page-locked, device-addressable host buffer (ccx_host_alloc) holding many blocks
+    back to back."""
 
     def __init__(self, torch, ndoubles: int):
-        import numpy as np
-        self.torch = torch
-        self.a = np.empty(max(int(ndoubles), 1), np.float64)
-        self.a[::512] = 0.0  # touch the pages before registering them
-        rc = torch.cuda.cudart().cudaHostRegister(self.a.ctypes.data, self.a.nbytes, 3)  # portable | mapped
-        if int(rc) != 0:
-            raise RuntimeError(f"cudaHostRegister failed ({rc})")
+        self.b = load_pkg().HostBuffer(ndoubles)
         self.used = 0
 
     def take(self, n: int) -> int:
         """Pointer to the next n doubles."""
-        p = self.a.ctypes.data + 8 * self.used
+        p = self.b.ptr + 8 * self.used
         self.used += n
         return p
 
     def close(self):
-        if self.a is not None:
-            self.torch.cuda.cudart().cudaHostUnregister(self.a.ctypes.data)
-            self.a = None
+        self.b.close()
 
 
 def run_e2e(args, ccx, torch, L, e, local, real, solve):
@@ -569,7 +563,7 @@ def run_e2e(args, ccx, torch, L, e, local, real, solve):
             "host_phase_s_per_step": {k: v / args.steps for k, v in phase.items()},
             "path": "ccx_set_fock + ccx_set_vblocks (all HHPP/PPPP/HHHH/HPHP blocks, one call per family) + "
                     "ccx_setup_t_amplitudes + ccx_ccd_iter + ccx_get_t2_all",
-            "host_buffers": "page-locked (cudaHostRegister): blocks are read in place over NVLink-C2C by the "
+            "host_buffers": "page-locked (ccx_host_alloc): blocks are read in place over NVLink-C2C by the "
                             "packing kernels (only the cache lines of unique pairs), or, for a block family above "
                             "16 GB, staged through the copy engines; the amplitudes are unpacked straight into "
                             "the host buffer; h2d_bytes_per_step is the size of the host inputs"}
@@ -820,6 +814,85 @@ def run_learned(args):
     return 0
 
 
+def run_precision_sweep(args, wl):
+    """Mixed-precision variants of one lattice against its plain FP64 solve: BF16x3 and
+    TF32x3 corrections with the adaptive re-base policy (drop factors 1e-4, 1e-5, 1e-6)
+    and with a fixed defect period k in {1, 2, 4, 8, 16}, digit-product re-bases.  For each:
+    iterations, FP64 re-bases, device seconds (best of --steps solves) and the E/A
+    difference to the FP64 solve in keV."""
+    import torch
+    ccx = load_pkg()
+    L = ccx.Layout.from_basis(wl["nmax"], wl["A"], wl["rho"], snm=wl["snm"])
+    real = wl["potential"] == ccx.POT_MINNESOTA
+    e = ccx.Engine(L, real=real)
+    e.generate(potential=wl["potential"])
+
+    def solve(precision, **kw):
+        best = None
+        for _ in range(max(1, args.steps)):
+            e.setup_t_amplitudes()
+            r = e.ccd_iter(mode=ccx.MODE_STANDARD, precision=precision, tol=args.tol, max_iter=200, diis_dim=8,
+                           rebase=ccx.REBASE_DIGITS if precision else ccx.REBASE_FP64, **kw)
+            if best is None or r["seconds"] < best["seconds"]:
+                best = r
+        return best
+
+    r64 = solve(0)
+    ea64 = (e.e0() + r64["e_ccd"]).real / wl["A"]
+    variants = [("bf16x3", 1, dict()), ("bf16x3", 1, dict(rebase_drop=1e-5)), ("bf16x3", 1, dict(rebase_drop=1e-6)),
+                ("tf32x3", 2, dict()), ("tf32x3", 2, dict(rebase_drop=1e-6))]
+    variants += [("bf16x3", 1, dict(defect_period=k)) for k in (1, 2, 4, 8, 16)]
+    rows = []
+    for name, pr, kw in variants:
+        solve(pr, **kw)  # warm-up: operand tiles of this kind
+        r = solve(pr, **kw)
+        ea = (e.e0() + r["e_ccd"]).real / wl["A"]
+        rows.append({"precision": name, "policy": kw or {"rebase_drop": 1e-4}, "converged": r["converged"],
+                     "iterations": r["iterations"], "fp64_rebases": r["fp64_sweeps"], "seconds": r["seconds"],
+                     "speedup_vs_fp64": r64["seconds"] / r["seconds"], "dE_per_A_keV": abs(ea - ea64) * 1e3})
+    line = {"metric": "mixed-precision variants vs plain FP64 GPU", "impl": "ours", "workload": wl["desc"],
+            "tol": args.tol, "fp64": {"iterations": r64["iterations"], "seconds": r64["seconds"], "E_per_A_MeV": ea64},
+            "variants": rows}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_triples(args, wl):
+    """CCD + (T) of one lattice: the mixed-precision CCD solve (digit-product re-bases) and
+    the plain FP64 one, then (T) on the converged amplitudes with FP32 contractions (the
+    default) and with FP64 contractions.  Reports the seconds of each, the CCD E/A of both
+    solves and the relative differences of E(T) between the forms."""
+    import torch
+    ccx = load_pkg()
+    L = ccx.Layout.from_basis(wl["nmax"], wl["A"], wl["rho"], snm=wl["snm"])
+    real = wl["potential"] == ccx.POT_MINNESOTA
+    e = ccx.Engine(L, real=real)
+    e.generate(potential=wl["potential"])
+    out = {}
+    for name, prec in (("fp64", 0), ("mixed", 1)):
+        e.setup_t_amplitudes()
+        r = e.ccd_iter(mode=ccx.MODE_STANDARD, precision=prec, tol=args.tol, max_iter=200, diis_dim=8,
+                       rebase=ccx.REBASE_DIGITS if prec else ccx.REBASE_FP64)
+        ts = {}
+        for tname, fp32 in (("fp32", True), ("fp64", False)):
+            e.set_triples_precision(fp32)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            et = e.pert_triples()
+            ts[tname] = {"seconds": time.perf_counter() - t0, "E_T_MeV": et.real}
+        out[name] = {"ccd_seconds": r["seconds"], "iterations": r["iterations"],
+                     "E_per_A_MeV": (e.e0() + r["e_ccd"]).real / wl["A"], "triples": ts}
+    ref = out["fp64"]["triples"]["fp64"]["E_T_MeV"]
+    line = {"metric": "CCD + (T) seconds and FP64-stated errors", "impl": "ours", "workload": wl["desc"],
+            "tol": args.tol, "forms": out,
+            "dE_per_A_keV_mixed_vs_fp64": abs(out["mixed"]["E_per_A_MeV"] - out["fp64"]["E_per_A_MeV"]) * 1e3,
+            "rel_dE_T_fp32_contractions": abs(out["fp64"]["triples"]["fp32"]["E_T_MeV"] - ref) / abs(ref),
+            "rel_dE_T_mixed_ccd_fp32_contractions": abs(out["mixed"]["triples"]["fp32"]["E_T_MeV"] - ref) / abs(ref),
+            "triples_pairs_note": "E(T) is summed over every (abc, ijk) pair of the triple channels"}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -844,12 +917,19 @@ def main():
     ap.add_argument("--eval-twists", type=int, default=4)
     ap.add_argument("--learn-steps", type=int, default=3000)
     ap.add_argument("--learn-stride", type=int, default=4, help="every k-th amplitude as a training sample")
+    ap.add_argument("--triples", action="store_true", help="run CCD + (T) on --workload instead")
+    ap.add_argument("--precision-sweep", action="store_true",
+                    help="run the mixed-precision variants of --workload against its FP64 solve instead")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     wl = WORKLOADS[args.workload]
     if args.learned and args.impl == "ours":
         return run_learned(args)
+    if args.precision_sweep and args.impl == "ours":
+        return run_precision_sweep(args, wl)
+    if args.triples and args.impl == "ours":
+        return run_triples(args, wl)
     if args.twists > 0 and args.impl == "ours":
         return run_twists(args)
     if args.impl == "reference":

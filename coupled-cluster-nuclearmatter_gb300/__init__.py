@@ -71,7 +71,8 @@ class _Potential(C.Structure):
 
 class _IterOpts(C.Structure):
     _fields_ = [("mode", C.c_int32), ("precision", C.c_int32), ("max_iter", C.c_int32), ("tol", C.c_double),
-                ("diis_dim", C.c_int32), ("defect_period", C.c_int32), ("verbose", C.c_int32), ("rebase", C.c_int32)]
+                ("diis_dim", C.c_int32), ("defect_period", C.c_int32), ("verbose", C.c_int32), ("rebase", C.c_int32),
+                ("rebase_drop", C.c_double)]
 
 
 class _IterResult(C.Structure):
@@ -138,6 +139,8 @@ def lib():
         "ccx_ccd_energy_noalloc": ([i32, vp, vp, vp, vp, vp], C.c_int),
         "ccx_selftest_tc_wait": ([i32, C.c_int64, C.POINTER(i32)], C.c_int),
         "ccx_engine_prepare": ([vp, C.POINTER(_IterOpts)], C.c_int),
+        "ccx_host_alloc": ([C.c_int64, C.POINTER(vp)], C.c_int),
+        "ccx_host_free": ([vp], C.c_int),
         "ccx_set_triples_precision": ([vp, i32], C.c_int),
         "ccx_engine_diis_fallbacks": ([vp, C.POINTER(C.c_int64)], C.c_int),
         "ccx_engine_kernel_timers": ([vp, vp, vp], C.c_int),
@@ -203,6 +206,30 @@ def selftest_tc_gemm(shapes, kind: int = 0, use_alo: bool = True, seed: int = 1,
     return err.value, ms.value
 
 
+class HostBuffer:
+    """Page-locked, device-addressable host memory (ccx_host_alloc) of n doubles."""
+
+    def __init__(self, ndoubles: int):
+        p = vp()
+        _check(lib().ccx_host_alloc(8 * max(int(ndoubles), 1), C.byref(p)))
+        self.ptr = p.value
+        self.n = max(int(ndoubles), 1)
+
+    def array(self) -> np.ndarray:
+        return np.ctypeslib.as_array((C.c_double * self.n).from_address(self.ptr))
+
+    def close(self):
+        if self.ptr:
+            lib().ccx_host_free(C.c_void_p(self.ptr))
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def selftest_tc_wait(wait_cycles: int, device: int = 0) -> int:
     """Tensor-core self-test with every pipeline wait limited to wait_cycles; returns the
     kernel's error word (0: completed and checked, else the wait that ran out)."""
@@ -218,11 +245,11 @@ def ccd_energy_noalloc(nch: int, dims_ptr: int, t2_ptr: int, vhhpp_ptr: int, ene
 
 
 def ccd_iter_batch(engines, mode=MODE_STANDARD, precision=PREC_FP64, max_iter=200, tol=1e-10, diis_dim=8,
-                   defect_period=0, verbose=False, rebase=REBASE_FP64):
+                   defect_period=0, verbose=False, rebase=REBASE_FP64, rebase_drop=0.0):
     """Solve several engines (e.g. twists) together in lockstep; returns (results, seconds)."""
     n = len(engines)
     hs = (vp * n)(*[e._h for e in engines])
-    o = _IterOpts(mode, precision, max_iter, tol, diis_dim, defect_period, int(verbose), rebase)
+    o = _IterOpts(mode, precision, max_iter, tol, diis_dim, defect_period, int(verbose), rebase, rebase_drop)
     rs = (_IterResult * n)()
     sec = C.c_double()
     _check(lib().ccx_ccd_iter_batch(hs, n, C.byref(o), rs, C.byref(sec)))
@@ -562,8 +589,8 @@ class Engine:
         return x.value
 
     def ccd_iter(self, mode=MODE_REFERENCE, precision=PREC_FP64, max_iter=100, tol=1e-6, diis_dim=8,
-                 defect_period=0, verbose=False, rebase=REBASE_FP64) -> dict:
-        o = _IterOpts(mode, precision, max_iter, tol, diis_dim, defect_period, int(verbose), rebase)
+                 defect_period=0, verbose=False, rebase=REBASE_FP64, rebase_drop=0.0) -> dict:
+        o = _IterOpts(mode, precision, max_iter, tol, diis_dim, defect_period, int(verbose), rebase, rebase_drop)
         r = _IterResult()
         _check(lib().ccx_ccd_iter(self._h, C.byref(o), C.byref(r)))
         return {"iterations": r.iterations, "converged": bool(r.converged),

@@ -399,6 +399,7 @@ int ccx_ccd_iter_batch(ccx_engine *const *engines, int32_t n, const ccx_iter_opt
     o.defect_period = opt->defect_period;
     o.verbose = opt->verbose;
     o.rebase = opt->rebase;
+    o.rebase_drop = opt->rebase_drop;
     std::vector<ccx::IterResult> rr(n);
     std::vector<ccx::IEngine *> act;
     for (int32_t i = 0; i < n; ++i) {
@@ -576,6 +577,21 @@ int ccx_selftest_tc_gemm(int32_t device, int32_t kind, int32_t nprob, const int3
     return fail(CCX_EINVAL, "bad selftest arguments");
   return guard([&] { ccx::tc_selftest(device, kind, nprob, M, N, K, use_alo, seed, max_rel_err, ms); });
 }
+int ccx_host_alloc(int64_t bytes, void **ptr) {
+  if (!ptr || bytes <= 0) return fail(CCX_EINVAL, "bad host allocation arguments");
+  *ptr = nullptr;
+  const cudaError_t e = cudaHostAlloc(ptr, (size_t)bytes, cudaHostAllocPortable | cudaHostAllocMapped);
+  if (e != cudaSuccess) {
+    *ptr = nullptr;
+    return fail(CCX_ENOMEM, std::string("cudaHostAlloc: ") + cudaGetErrorString(e));
+  }
+  return CCX_OK;
+}
+int ccx_host_free(void *ptr) {
+  if (!ptr) return CCX_OK;
+  const cudaError_t e = cudaFreeHost(ptr);
+  return e == cudaSuccess ? CCX_OK : fail(CCX_ECUDA, std::string("cudaFreeHost: ") + cudaGetErrorString(e));
+}
 int ccx_selftest_tc_wait(int32_t device, int64_t wait_cycles, int32_t *kernel_error) {
   if (!kernel_error || wait_cycles <= 0) return fail(CCX_EINVAL, "bad selftest arguments");
   return guard([&] {
@@ -642,6 +658,7 @@ int ccx_engine_prepare(ccx_engine *e, const ccx_iter_opts *opt) {
     o.diis_dim = opt->diis_dim;
     o.defect_period = opt->defect_period;
     o.rebase = opt->rebase;
+    o.rebase_drop = opt->rebase_drop;
     o.verbose = opt->verbose;
     e->E->prepare(o);
   });
@@ -659,6 +676,7 @@ int ccx_ccd_iter(ccx_engine *e, const ccx_iter_opts *opt, ccx_iter_result *res) 
     o.diis_dim = opt->diis_dim;
     o.defect_period = opt->defect_period;
     o.rebase = opt->rebase;
+    o.rebase_drop = opt->rebase_drop;
     o.verbose = opt->verbose;
     ccx::IterResult r;
     e->E->ccd_iter(o, r);

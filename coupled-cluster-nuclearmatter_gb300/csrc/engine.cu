@@ -1408,7 +1408,8 @@ class Engine final : public IEngine {
   // Standard mode: Jacobi step + Pulay DIIS on the steps.  With mixed precision the
   // residual is evaluated as R(T_b) [cached, FP64] + tensor-core corrections in
   // T - T_b (defect correction); an FP64 residual re-bases T_b when the mixed residual
-  // has dropped by kRebaseDrop since the last FP64 one, stalls, reaches the tolerance,
+  // has dropped by rebase_drop (default kRebaseDrop) since the last FP64 one, stalls,
+  // reaches the tolerance,
   // or every defect_period iterations, and only an FP64 residual can end the solve.
   //
   // The loop is a state machine so that a batch of engines can run it in lockstep:
@@ -1546,7 +1547,8 @@ class Engine final : public IEngine {
         if (s.phase_r0 < 0) s.phase_r0 = rn;
         if (rn < 0.9 * s.best) { s.best = rn; s.stall = 0; } else ++s.stall;
         const bool periodic = s.o.defect_period > 0 && s.since >= s.o.defect_period;
-        const bool dropped = s.o.defect_period <= 0 && rn < kRebaseDrop * s.phase_r0;
+        const double drop = s.o.rebase_drop > 0.0 ? s.o.rebase_drop : kRebaseDrop;
+        const bool dropped = s.o.defect_period <= 0 && rn < drop * s.phase_r0;
         if (rn < s.o.tol || s.stall >= 2 || periodic || dropped) s.need_fp64 = true;
       }
     }

@@ -25,6 +25,7 @@ struct IterOpts {
   int defect_period = 0;  // mixed: FP64 re-base every k iterations; 0 adaptive
   int verbose = 0;
   int rebase = 0;        // mixed: products of a re-base as 0 FP64 FMA GEMMs, 1 exact digit products (tensor cores)
+  double rebase_drop = 0.0;  // mixed, adaptive: re-base once the mixed residual fell by this factor (0: 1e-4)
 };
 struct IterResult {
   int iterations = 0, converged = 0;

@@ -112,7 +112,9 @@ __global__ void k_ml_extract(MLCtx c, const double *__restrict__ T, int stride, 
 #pragma unroll
     for (int q = 0; q < kMlIn; ++q) X[o * kMlIn + q] = f[q];
     const double D = (double)f[4] * (double)c.eF;
-    y[o] = (float)((T[g] - tmp2) * D * (double)c.vol / kMlNum);
+    // with a prior the network learns what the prior leaves over (a skip connection):
+    // the BF16 inference then perturbs only that small remainder
+    y[o] = (float)((T[g] - tmp2) * D * (double)c.vol / kMlNum) - f[16];
   }
 }
 // prior += w * (the numerator correction of T), per packed amplitude (c.prior is null)
@@ -456,6 +458,7 @@ __global__ void __launch_bounds__(128, 1) k_ml_infer(InferArgs g) {
     o += sp[4 * kMlW];
     if (live) {
       if (g.use_view) {
+        if (g.c.prior) o += g.c.prior[gidx];  // the skip connection of the prior, in FP32
         const double D = (double)f[4] * (double)g.c.eF;
         g.T[gidx] = D == 0.0 ? tmp2 : tmp2 + (double)o * kMlNum / (D * (double)g.c.vol);
       }

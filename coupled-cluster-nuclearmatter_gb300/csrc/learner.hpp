@@ -1,7 +1,9 @@
 // Learned warm start: a 4-layer MLP (width 128, SiLU) that predicts, per packed T2
 // amplitude, the difference between the converged CCD amplitude and its MP2 value from
 // transferable features of the amplitude and, when the host sets one, a prior: the same
-// difference interpolated from solutions converged at neighbouring densities.  Trained in FP32 on amplitudes the solver
+// difference interpolated from solutions converged at neighbouring densities.  With a
+// prior the network predicts what the prior leaves over, and the prior is added back in
+// FP32 (a skip connection), so the BF16 inference perturbs only that remainder.  Trained in FP32 on amplitudes the solver
 // converged on other lattices (densities, twists); inference in BF16 on the tensor
 // cores writes T2 = T_MP2 + correction straight into an engine.  The CCD iteration that
 // follows is unchanged, so the converged energy does not depend on the start.

@@ -277,6 +277,8 @@ typedef struct {
                                 (when the mixed residual has dropped 1e4x, stalls or meets tol) */
   int32_t verbose;
   int32_t rebase;            /* mixed precision: CCX_REBASE_* */
+  double rebase_drop;        /* mixed precision, adaptive policy: FP64 re-base once the mixed residual
+                                has fallen by this factor since the last one (0: the default 1e-4) */
 } ccx_iter_opts;
 #define CCX_REBASE_FP64 0      /* products of a re-base on the FP64 FMA pipe */
 #define CCX_REBASE_DIGITS 1    /* the pp-ladder, I4 and ring products of a re-base as exact 6-bit digit
@@ -339,7 +341,9 @@ int ccx_set_triples_precision(ccx_engine *e, int32_t precision);
  * <ij|V|ab> and MP2 amplitude scaled by the volume, momentum transfers and pair momenta
  * / k_F, spin and isospin products, and a prior with its flag: the same difference
  * interpolated from solutions the solver converged at neighbouring densities of the
- * same lattice and twist (ccx_learner_set_prior; 0 and flag 0 without one).  Training
+ * same lattice and twist (ccx_learner_set_prior; 0 and flag 0 without one).  With a
+ * prior the network predicts the remainder of the difference beyond the prior, which is
+ * added back in FP32 (a skip connection).  Training
  * (FP32, Adam) uses amplitudes the solver converged on other lattices; inference runs in
  * BF16 on the tensor cores.  Real engines only.  The CCD iteration from the warm start
  * is unchanged, so the converged energy is the same as from MP2. */
@@ -370,6 +374,14 @@ int ccx_learner_set_params(ccx_learner *l, const float *params);
 int ccx_learner_loss_grad(ccx_learner *l, const float *X, const float *y, int32_t n, double *loss, float *grad);
 /* network output on host features: tensor_cores 0 = FP32 training forward, 1 = BF16 kernel */
 int ccx_learner_infer(ccx_learner *l, const float *X, int32_t n, float *out, int32_t tensor_cores);
+
+/* ---- host buffers --------------------------------------------------------- */
+/* Page-locked host memory that every device can address (cudaHostAlloc, portable and
+ * mapped), for hosts that hand over large V families: ccx_set_vblock(s) reads blocks in
+ * such memory in place or through the copy engines at the link rate.  No counterpart in
+ * the reference (its blocks never leave the host). */
+int ccx_host_alloc(int64_t bytes, void **ptr);
+int ccx_host_free(void *ptr);
 
 /* ---- diagnostics -------------------------------------------------------- */
 const char *ccx_last_error(void);
