@@ -1930,18 +1930,27 @@ class Engine final : public IEngine {
       p.b_plane = b.n;
       p.M = M; p.N = N; p.nk = (K + 63) / 64; p.npad = (N + 15) / 16 * 16;
       p.C = (double *)C + cc; p.sCm = sCm * kNComp; p.sCn = sCn * kNComp; p.alpha = al;
-      for (int mt = 0; mt < (M + 127) / 128; ++mt)
-        for (int n0 = 0; n0 < p.npad; n0 += kOzN) l.tiles.push_back(OzTile{(int)l.probs.size(), mt, n0});
       l.probs.push_back(p);
       l.phase.push_back(ph);
+      return (int)l.probs.size() - 1;
+    };
+    // tiles of the problems that share an A operand side by side, so that the CTAs that
+    // read the same A digit tile run at the same time and the second read hits L2
+    auto tiles = [&](int pa, int pb) {
+      const OzProb &p = l.probs[pa];
+      for (int mt = 0; mt < (M + 127) / 128; ++mt)
+        for (int n0 = 0; n0 < p.npad; n0 += kOzN) {
+          l.tiles.push_back(OzTile{pa, mt, n0});
+          if (pb >= 0) l.tiles.push_back(OzTile{pb, mt, n0});
+        }
     };
     if (kNComp == 1) {
-      one(0, 0, 0, alpha, 0);
+      tiles(one(0, 0, 0, alpha, 0), -1);
     } else {
-      one(0, 0, 0, alpha, 0);
-      one(0, 1, 1, alpha, 0);
-      one(1, 1, 0, -alpha, 1);
-      one(1, 0, 1, alpha, 1);
+      const int p0 = one(0, 0, 0, alpha, 0), p1 = one(0, 1, 1, alpha, 0);
+      tiles(p0, p1);
+      const int p2 = one(1, 1, 0, -alpha, 1), p3 = one(1, 0, 1, alpha, 1);
+      tiles(p2, p3);
     }
   }
 
