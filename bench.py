@@ -571,6 +571,7 @@ def run_e2e(args, ccx, torch, L, e, local, real, solve):
 
 TWIST_LATTICES = {
     "pnm66": dict(nmax=4, A=66, rho=0.16, snm=False, desc="PNM A=66, rho=0.16 fm^-3, nmax=4 (1458 states), Minnesota"),
+    "pnm14": dict(nmax=2, A=14, rho=0.08, snm=False, desc="PNM A=14, nmax=2 (250 states), Minnesota"),
     "snm132n3": dict(nmax=3, A=132, rho=0.16, snm=True, desc="SNM A=132, rho=0.16 fm^-3, nmax=3 (1372 states), Minnesota"),
     "snm132n3chiral": dict(nmax=3, A=132, rho=0.16, snm=True, potential=1,
                            desc="SNM A=132, rho=0.16 fm^-3, nmax=3 (1372 states), chiral-like (complex)"),
@@ -787,12 +788,18 @@ def run_learned(args):
         for k in range(1, 17, 2):
             e, r_mp2 = converged(rhos[k], th)
             lrn.set_prior([even[k - 1], even[k + 1]], [0.5, 0.5])
+            # the residual norm at each start: one FP64 residual evaluation
+            e.setup_t_amplitudes()
+            s_mp2 = e.ccd_iter(mode=ccx.MODE_STANDARD, tol=args.tol, max_iter=1)["res_norm"]
+            lrn.warm_start(e)
+            s_ml = e.ccd_iter(mode=ccx.MODE_STANDARD, tol=args.tol, max_iter=1)["res_norm"]
             lrn.warm_start(e)
             r_ml = e.ccd_iter(**opts)
             ea_mp2 = (e.e0() + r_mp2["e_ccd"]).real / lat["A"]
             ea_ml = (e.e0() + r_ml["e_ccd"]).real / lat["A"]
             rows.append((r_mp2["iterations"], r_ml["iterations"], r_mp2["seconds"], r_ml["seconds"],
-                         abs(ea_ml - ea_mp2) * 1e3, r_mp2["converged"] and r_ml["converged"]))
+                         abs(ea_ml - ea_mp2) * 1e3, r_mp2["converged"] and r_ml["converged"],
+                         r_mp2["fp64_sweeps"], r_ml["fp64_sweeps"], s_mp2, s_ml))
             e.close()
         for x in even.values():
             x.close()
@@ -809,7 +816,10 @@ def run_learned(args):
             "iterations_mp2_mean": it0, "iterations_learned_mean": it1,
             "solve_s_mp2_total": s0, "solve_s_learned_total": s1, "speedup_learned": s0 / s1 if s1 else None,
             "fewer_iterations_on": sum(1 for x in rows if x[1] < x[0]), "more_iterations_on": sum(1 for x in rows if x[1] > x[0]),
-            "max_dE_per_A_keV": max(x[4] for x in rows), "all_converged": all(x[5] for x in rows)}
+            "max_dE_per_A_keV": max(x[4] for x in rows), "all_converged": all(x[5] for x in rows),
+            "fp64_rebases_mp2_mean": sum(x[6] for x in rows) / len(rows),
+            "fp64_rebases_learned_mean": sum(x[7] for x in rows) / len(rows),
+            "start_residual_ratio_learned_over_mp2_median": statistics.median(x[9] / x[8] for x in rows)}
     print(json.dumps(line), flush=True)
     return 0
 
