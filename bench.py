@@ -444,10 +444,14 @@ def run_ours(args, wl):
     return 0
 
 
-# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from ncu
-# captures of `bench.py --steps 1 --warmup 1 --no-e2e --no-cpu-baseline` on this workload:
+# DRAM bytes per timed bracket (dram__bytes_read.sum + dram__bytes_write.sum) from ncu
+# captures of `bench.py --steps 1 --warmup 1 --no-e2e --no-cpu-baseline` on the workload:
 # (workload, precision, kernel slot) -> bytes
 PROFILED_TRAFFIC = {
+    # profiles/k_oz_gemm_snm132n3.md: both phase launches of the pp re-base product
+    ("snm132n3", "bf16x3", "pp_rebase_digits"): 4.09e9,
+    # the same scaled to SNM 132 nmax=4 by the algorithmic bytes (12.0 GB / 1.51 GB)
+    ("snm132n4", "bf16x3", "pp_rebase_digits"): 32.6e9,
     ("pnm66", "bf16x3", "x_fp64"): 32.0e6,
     ("pnm66", "bf16x3", "pp_tc"): 643.7e6,
     ("pnm66", "bf16x3", "pp_rebase_digits"): 2426.5e6,
@@ -616,7 +620,7 @@ def run_twists(args):
         return ccx.Layout.from_basis(lat["nmax"], lat["A"], lat["rho"], snm=lat["snm"], theta=th)
 
     def engine(L, th, precision, rebase):
-        e = ccx.Engine(L, real=(pot == 0 and not any(th)))
+        e = ccx.Engine(L, real=(pot == 0))  # the Minnesota V and Fock stay real at any twist
         e.generate(potential=pot)
         e.setup_t_amplitudes()
         e.prepare(precision=precision, rebase=rebase)

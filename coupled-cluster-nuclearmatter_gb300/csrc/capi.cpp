@@ -402,22 +402,8 @@ int ccx_ccd_iter_batch(ccx_engine *const *engines, int32_t n, const ccx_iter_opt
     o.rebase_drop = opt->rebase_drop;
     std::vector<ccx::IterResult> rr(n);
     std::vector<ccx::IEngine *> act;
-    // the engines' persistent tensor-core kernels share the SMs (each at most its share
-    // of them) instead of queueing behind one another; restored when the batch ends
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int share = n > 1 && sms > 0 ? std::max(8, (sms + n - 1) / n) : 0;
-    struct CapGuard {
-      ccx_engine *const *e;
-      int32_t n;
-      ~CapGuard() {
-        for (int32_t i = 0; i < n; ++i) e[i]->E->set_sm_cap(0);
-      }
-    } guard_caps{engines, n};
     for (int32_t i = 0; i < n; ++i) {
       engines[i]->E->set_timing(false);
-      engines[i]->E->set_sm_cap(share);
       engines[i]->E->std_begin(o, rr[i]);
       if (!engines[i]->E->std_done()) act.push_back(engines[i]->E.get());
     }

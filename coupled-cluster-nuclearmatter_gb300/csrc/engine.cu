@@ -201,13 +201,6 @@ class Engine final : public IEngine {
   int64_t device_bytes() const override { return bytes_; }
   int64_t launches() const override { return launches_; }
   int64_t diis_fallbacks() const override { return diis_fallbacks_; }
-  // persistent tensor-core kernels use at most n CTAs (0: one per SM); the replayed
-  // residual graphs are captured again with the new grids
-  void set_sm_cap(int n) override {
-    if (n == sm_cap_) return;
-    sm_cap_ = n;
-    ++plan_epoch_;
-  }
   void set_triples_precision(int p) override {
     if (p != 0 && p != 1) throw EngineError(1, "unknown (T) precision");
     triples_fp32_ = p == 1;
@@ -1706,7 +1699,7 @@ class Engine final : public IEngine {
       for (int k = 0; k < kTcBuckets; ++k) {
         if (!pl.ntiles[ph][k]) continue;
         launch_tc_gemm(tc_kind_, (const TcProb *)pl.probs.p, (const TcTile *)pl.tiles[ph][k].p, pl.ntiles[ph][k],
-                       pl.npad_max[ph][k], pl.max_nk[ph][k], tcerr_.as<int>(), st_, 0, sm_cap_);
+                       pl.npad_max[ph][k], pl.max_nk[ph][k], tcerr_.as<int>(), st_);
         ++launches_;
       }
   }
@@ -1905,8 +1898,7 @@ class Engine final : public IEngine {
   void run_oz(const OzPlan &pl) {
     for (int ph = 0; ph < 2; ++ph) {
       if (!pl.ntiles[ph]) continue;
-      launch_oz_gemm((const OzProb *)pl.probs.p, (const OzTile *)pl.tiles[ph].p, pl.ntiles[ph], tcerr_.as<int>(), st_,
-                     sm_cap_);
+      launch_oz_gemm((const OzProb *)pl.probs.p, (const OzTile *)pl.tiles[ph].p, pl.ntiles[ph], tcerr_.as<int>(), st_);
       ++launches_;
     }
   }
@@ -2415,7 +2407,6 @@ class Engine final : public IEngine {
   double timers_[10] = {};
   bool timing_ = false, profiling_ = false;
   int64_t diis_fallbacks_ = 0;  // DIIS systems found singular: the plain step was kept
-  int sm_cap_ = 0;              // CTAs of the persistent tensor-core kernels (0: one per SM)
   bool triples_fp32_ = true;    // (T) contractions in FP32 (FP64 accumulation)
   static constexpr int kKernelEvents = 32;
   cudaEvent_t kev_[2 * kKernelEvents] = {};

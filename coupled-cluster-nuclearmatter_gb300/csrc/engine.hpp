@@ -65,7 +65,6 @@ class IEngine {
   virtual int64_t device_bytes() const = 0;
   virtual int64_t launches() const = 0;
   virtual int64_t diis_fallbacks() const = 0;
-  virtual void set_sm_cap(int n) = 0;  // CTAs of the persistent tensor-core kernels (0: one per SM)
   virtual void set_triples_precision(int p) = 0;  // 0 FP64 contractions, 1 FP32 contractions
   virtual void timers(double ms[10]) const = 0;
   virtual void kernel_timers(double ms[kKernelSlots], int64_t n[kKernelSlots]) const = 0;

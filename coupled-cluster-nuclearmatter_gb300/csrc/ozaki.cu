@@ -356,14 +356,13 @@ __global__ void __launch_bounds__(256) k_oz_digits(const OzSplitJob *__restrict_
 
 }  // namespace
 
-void launch_oz_gemm(const OzProb *probs, const OzTile *tiles, int ntiles, int *err, cudaStream_t st, int max_ctas) {
+void launch_oz_gemm(const OzProb *probs, const OzTile *tiles, int ntiles, int *err, cudaStream_t st) {
   if (ntiles <= 0) return;
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   if (sms <= 0) sms = 1;
   cudaFuncSetAttribute(k_oz_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kOzSmem);
-  if (max_ctas > 0) sms = std::min(sms, max_ctas);
   k_oz_gemm<<<std::min(ntiles, sms), kOzThreads, kOzSmem, st>>>(probs, tiles, ntiles, err);
 }
 

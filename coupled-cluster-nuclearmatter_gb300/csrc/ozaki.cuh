@@ -44,8 +44,7 @@ struct OzTile {
   int prob, mt, n0;    // 128-row tile mt, columns n0 .. n0 + min(kOzN, npad - n0)
 };
 // error codes written to *err: 1 load wait, 2 MMA wait, 3 drain wait timed out, 4 bad shape
-// max_ctas > 0 caps the persistent grid (default: one CTA per SM)
-void launch_oz_gemm(const OzProb *probs, const OzTile *tiles, int ntiles, int *err, cudaStream_t st, int max_ctas = 0);
+void launch_oz_gemm(const OzProb *probs, const OzTile *tiles, int ntiles, int *err, cudaStream_t st);
 
 // Exponents and digit planes of an FP64 matrix (rows x cols, element (r, k) at
 // src[r * sr + k * sk]), tiled like TcSplitJob (tile_rows 128 for A, npad for B).

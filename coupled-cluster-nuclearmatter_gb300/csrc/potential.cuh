@@ -34,10 +34,10 @@ __device__ inline double minnesota(const DevOrbits &O, const DevPotential &P, in
   } else {
     v0r = 200.0; v0t = 178.0; v0s = 91.85; kr = 1.487; kt = 0.639; ks = 0.465;
   }
-  const double pi15 = pow(kPi, 1.5);
-  double vr = v0r * pi15 * exp(-q2 / (4.0 * kr)) / pow(kr, 1.5);
-  double vt = -v0t * pi15 * exp(-q2 / (4.0 * kt)) / pow(kt, 1.5);
-  double vs = -v0s * pi15 * exp(-q2 / (4.0 * ks)) / pow(ks, 1.5);
+  const double pi15 = kPi * sqrt(kPi);  // x^1.5 as x sqrt(x): no pow on the FP64 pipe
+  double vr = v0r * pi15 * exp(-q2 / (4.0 * kr)) / (kr * sqrt(kr));
+  double vt = -v0t * pi15 * exp(-q2 / (4.0 * kt)) / (kt * sqrt(kt));
+  double vs = -v0s * pi15 * exp(-q2 / (4.0 * ks)) / (ks * sqrt(ks));
   const int m1 = O.sz[p], m2 = O.sz[q], m3 = O.sz[r], m4 = O.sz[s];
   const int t1 = O.tz[p], t2 = O.tz[q], t3 = O.tz[r], t4 = O.tz[s];
   const double dm = kd(m1, m3) * kd(m2, m4), dt = kd(t1, t3) * kd(t2, t4);

@@ -638,7 +638,7 @@ int tc_stages(int npad_max) {
 }
 
 void launch_tc_gemm(int kind, const TcProb *probs, const TcTile *tiles, int ntiles, int npad_max, int max_nk, int *err,
-                    cudaStream_t st, long long wait_budget, int max_ctas) {
+                    cudaStream_t st, long long wait_budget) {
   if (wait_budget <= 0) wait_budget = tcptx::kWaitBudget;
   (void)max_nk;  // the stage ring runs on across tiles
   if (ntiles <= 0) return;
@@ -649,8 +649,7 @@ void launch_tc_gemm(int kind, const TcProb *probs, const TcTile *tiles, int ntil
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   if (sms <= 0) sms = 1;
-  // persistent: one CTA per SM (or max_ctas) walks the tile list
-  const int grid = std::min(ntiles, max_ctas > 0 ? std::min(max_ctas, sms) : sms);
+  const int grid = std::min(ntiles, sms);  // persistent: one CTA per SM walks the tile list
   if (kind == kTcBF16) {
     cudaFuncSetAttribute(k_tc_gemm<kTcBF16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k_tc_gemm<kTcBF16><<<grid, kTcThreads, smem, st>>>(probs, tiles, ntiles, stages, npad_max, err, wait_budget);

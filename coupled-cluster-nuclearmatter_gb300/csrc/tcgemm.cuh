@@ -54,10 +54,8 @@ inline int tc_tile_k(int kind) { return kind == kTcBF16 ? 64 : 32; }
 // kernel's stage ring runs on across tiles).  wait_budget: clock cycles each pipeline
 // wait may take before the kernel gives up with an error code (<= 0: the default of
 // about 2 s); the final waits for copies and MMAs in flight always keep the default.
-// max_ctas > 0 caps the persistent grid (default: one CTA per SM), so that the kernels
-// of several engines solved together share the SMs instead of queueing.
 void launch_tc_gemm(int kind, const TcProb *probs, const TcTile *tiles, int ntiles, int npad_max, int max_nk, int *err,
-                    cudaStream_t st, long long wait_budget = 0, int max_ctas = 0);
+                    cudaStream_t st, long long wait_budget = 0);
 // shared-memory stages launch_tc_gemm uses for tiles up to npad_max columns
 int tc_stages(int npad_max);
 

@@ -183,8 +183,11 @@ __global__ void __launch_bounds__(256) k_triples(TriplesDev D, DevLayout L, cons
   for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < total; g += (int64_t)gridDim.x * blockDim.x) {
     while (g >= D.elem_off[ch + 1]) ++ch;
     const int64_t loc = g - D.elem_off[ch];
-    const int nb = D.nbra[ch];
-    const int ket = (int)(loc / nb), bra = (int)(loc % nb);
+    // neighbouring threads take neighbouring particle triples abc of one hole triple ijk:
+    // the pairs (a, d) of a particle term all lie in the hhpp channel of n_i + n_j, so a
+    // warp's T2 gathers fall in one column of that channel's block
+    const int64_t nkets = (D.elem_off[ch + 1] - D.elem_off[ch]) / D.nbra[ch];
+    const int bra = (int)(loc / nkets), ket = (int)(loc % nkets);
     const int3 abc = D.ppp[D.ppp_off[ch] + ket];
     const int3 ijk = D.hhh[D.hhh_off[ch] + bra];
     const int a = abc.x, b = abc.y, c = abc.z, i = ijk.x, j = ijk.y, k = ijk.z;

@@ -306,9 +306,7 @@ int ccx_engine_prepare(ccx_engine *e, const ccx_iter_opts *opt);
  * ccm_main.f90:163-279, which the reference solves one after the other) solved
  * together in the standard mode: the iterations run in lockstep, each engine's kernels
  * on its own stream so that the GPU overlaps the engines, with one host
- * synchronisation per step for the whole batch.  During the batch each engine's
- * persistent tensor-core kernels use at most their share of the SMs (at least 8), so
- * that the engines' kernels run side by side instead of queueing.  res[i] is engine i's result; every
+ * synchronisation per step for the whole batch.  res[i] is engine i's result; every
  * res[i].seconds and *seconds hold the wall time of the whole batch. */
 int ccx_ccd_iter_batch(ccx_engine *const *engines, int32_t n, const ccx_iter_opts *opt, ccx_iter_result *res,
                        double *seconds);
