@@ -780,7 +780,7 @@ def run_learned(args):
         even = {k: converged(rhos[k], th)[0] for k in range(0, 17, 2)}
         for k, e in even.items():
             nb = [j for j in (k - 2, k + 2) if j in even]
-            lrn.set_prior([even[j] for j in nb], [1.0 / len(nb)] * len(nb))
+            lrn.set_prior(e, [even[j] for j in nb], [1.0 / len(nb)] * len(nb))
             lrn.add_solution(e, stride=stride)
         for e in even.values():
             e.close()
@@ -790,8 +790,10 @@ def run_learned(args):
     for th in eval_tw:
         even = {k: converged(rhos[k], th)[0] for k in range(0, 17, 2)}
         for k in range(1, 17, 2):
-            e, r_mp2 = converged(rhos[k], th)
-            lrn.set_prior([even[k - 1], even[k + 1]], [0.5, 0.5])
+            e, _ = converged(rhos[k], th)  # the first solve also prepares the engine
+            e.setup_t_amplitudes()
+            r_mp2 = e.ccd_iter(**opts)
+            lrn.set_prior(e, [even[k - 1], even[k + 1]], [0.5, 0.5])
             # the residual norm at each start: one FP64 residual evaluation
             e.setup_t_amplitudes()
             s_mp2 = e.ccd_iter(mode=ccx.MODE_STANDARD, tol=args.tol, max_iter=1)["res_norm"]

@@ -151,7 +151,7 @@ def lib():
         "ccx_learner_destroy": ([vp], C.c_int),
         "ccx_learner_add_solution": ([vp, vp], C.c_int),
         "ccx_learner_add_solution_sampled": ([vp, vp, i32], C.c_int),
-        "ccx_learner_set_prior": ([vp, i32, vp, vp], C.c_int),
+        "ccx_learner_set_prior": ([vp, vp, i32, vp, vp], C.c_int),
         "ccx_learner_clear": ([vp], C.c_int),
         "ccx_learner_samples": ([vp, vp], C.c_int),
         "ccx_learner_train": ([vp, i32, i32, C.c_double, C.c_uint64, C.POINTER(C.c_double)], C.c_int),
@@ -291,13 +291,14 @@ class Learner:
         else:
             _check(lib().ccx_learner_add_solution_sampled(self._h, engine._h, int(stride)))
 
-    def set_prior(self, engines=(), weights=()):
-        """Prior feature: sum_i weights[i] x the converged-minus-MP2 correction of
-        engines[i] (neighbouring densities of the same lattice); no engines clears it."""
+    def set_prior(self, target: "Engine", engines=(), weights=()):
+        """Prior feature for target: sum_i weights[i] x the converged-minus-MP2 correction
+        of engines[i] (neighbouring densities of the same lattice), matched by quantum
+        numbers; no engines clears it."""
         n = len(engines)
         hs = (vp * max(n, 1))(*[e._h for e in engines])
         ws = (C.c_double * max(n, 1))(*[float(w) for w in weights])
-        _check(lib().ccx_learner_set_prior(self._h, n, hs, ws))
+        _check(lib().ccx_learner_set_prior(self._h, target._h, n, hs, ws))
 
     def clear(self):
         _check(lib().ccx_learner_clear(self._h))

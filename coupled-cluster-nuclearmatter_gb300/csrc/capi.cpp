@@ -478,14 +478,15 @@ int ccx_learner_add_solution_sampled(ccx_learner *l, ccx_engine *e, int32_t stri
   if (!e || stride < 1) return fail(CCX_EINVAL, "null engine or stride < 1");
   LEARNER_CALL(l, l->M->add_solution(ml_view_of(e, true), stride));
 }
-int ccx_learner_set_prior(ccx_learner *l, int32_t n, ccx_engine *const *engines, const double *weights) {
-  if (n < 0 || (n > 0 && (!engines || !weights))) return fail(CCX_EINVAL, "bad prior arguments");
+int ccx_learner_set_prior(ccx_learner *l, ccx_engine *target, int32_t n, ccx_engine *const *engines,
+                          const double *weights) {
+  if (!target || n < 0 || (n > 0 && (!engines || !weights))) return fail(CCX_EINVAL, "bad prior arguments");
   for (int32_t i = 0; i < n; ++i)
     if (!engines[i]) return fail(CCX_EINVAL, "null engine in the prior");
   LEARNER_CALL(l, {
     std::vector<ccx::MLView> vs;
     for (int32_t i = 0; i < n; ++i) vs.push_back(ml_view_of(engines[i], true));
-    l->M->set_prior(vs.data(), weights, n);
+    l->M->set_prior(ml_view_of(target, false), vs.data(), weights, n);
   });
 }
 int ccx_learner_clear(ccx_learner *l) { LEARNER_CALL(l, l->M->clear()); }

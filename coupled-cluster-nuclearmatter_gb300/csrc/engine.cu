@@ -720,6 +720,9 @@ class Engine final : public IEngine {
       v.Vhp = Vhp_.as<double>();
       v.T = T_.as<double>();
       v.n_t = n_t_;
+      v.okey = okey_.as<int>();
+      v.oof = oof_.as<int>();
+      v.nkeys = nkeys_;
       v.vol = b.L * b.L * b.L;
       v.rho = b.A / v.vol;
       const bool snm = b.tzmin != b.tzmax;
@@ -901,6 +904,15 @@ class Engine final : public IEngine {
     upload(dpp_orb_, pp_orb, &bytes_); upload(dhh_orb_, hh_orb, &bytes_);
     npp_total_ = (int)pp_orb.size();
     nhh_total_ = (int)hh_orb.size();
+    {  // orbitals by quantum numbers (the learned start's prior maps lattices through them)
+      const Basis &B = L.b;
+      std::vector<int> okey(std::max(B.ns, 1), -1);
+      for (size_t k = 0; k < B.orbit_of.size(); ++k)
+        if (B.orbit_of[k] >= 0) okey[B.orbit_of[k]] = (int)k;
+      upload(okey_, okey, &bytes_);
+      upload(oof_, B.orbit_of, &bytes_);
+      nkeys_ = (int)B.orbit_of.size();
+    }
     upload(dpp_row_, pp_row, &bytes_); upload(dhh_row_, hh_row, &bytes_);
     upload(dpp_slot_, pp_slot, &bytes_); upload(dhh_slot_, hh_slot, &bytes_);
     upload(dpartner_, partner_, &bytes_);
@@ -2431,6 +2443,8 @@ class Engine final : public IEngine {
   DBuf T_, R_, Vhp_, Vpp_, Vhh_, X_, I9_, Tph_, Rph_, Vph_, W_, I4_, fdiag_, f6_, f7_, d2ij_, d2ab_, i6off_, i7off_;
   DBuf pairf_;  // per-pair factors of the chiral-like generation
   int npp_total_ = 0, nhh_total_ = 0;  // packed pp and hh pairs over all channels
+  DBuf okey_, oof_;                    // orbital -> quantum-number slot, slot -> orbital
+  int nkeys_ = 0;
   DBuf partial_, res_, flag_, stage_, hist_, hist_t_, hist_e_, xwork_, xgroups_, xpart_, i6rows_, i6dots_, omap_, rmap_;
   int nxwork_ = 0, nxgroups_ = 0, ni6rows_ = 0;
   Plan planLadder_, planI4_, planRing_, planPP_, planHH_;

@@ -10,6 +10,7 @@
 #include <string>
 #include <vector>
 
+#include "common.cuh"
 #include "engine.hpp"
 #include "learner.hpp"
 #include "tc_ptx.cuh"
@@ -117,19 +118,42 @@ __global__ void k_ml_extract(MLCtx c, const double *__restrict__ T, int stride, 
     y[o] = (float)((T[g] - tmp2) * D * (double)c.vol / kMlNum) - f[16];
   }
 }
-// prior += w * (the numerator correction of T), per packed amplitude (c.prior is null)
-__global__ void k_ml_prior(MLCtx c, const double *__restrict__ T, float w, int first, float *__restrict__ prior) {
-  const int2 tl = c.L.ttile[blockIdx.x];
+// A solution the prior is taken from (another density of the same lattice and twist)
+struct PriorSrc {
+  DevLayout L;
+  const double *fd, *V, *T;
+  const int *oof;
+  double vol;
+};
+// prior += w * (the numerator correction of src's T), per packed amplitude g of the target
+// layout Lt: the target's orbitals a, b, i, j are mapped to src's by quantum numbers
+// (okey of the target, oof of src), and src's packed amplitude is read with the product of
+// its two pair-slot signs.  The correction (T - V/D) D vol / 1000 is src's own, which
+// makes it comparable across densities.
+__global__ void k_ml_prior(DevLayout Lt, const int *__restrict__ okey, PriorSrc src, float w, int first,
+                           float *__restrict__ prior) {
+  const int2 tl = Lt.ttile[blockIdx.x];
   const int ch = tl.x;
-  const int n = c.L.P[ch] * c.L.H[ch];
-  const int end = min(tl.y + kTileElems, n);
+  const int P = Lt.P[ch];
+  const int end = min(tl.y + kTileElems, P * Lt.H[ch]);
+  const DevLayout &L = src.L;
   for (int e = tl.y + threadIdx.x; e < end; e += blockDim.x) {
-    float f[kMlIn];
-    double tmp2;
-    ml_feat(c, ch, e, f, tmp2);
-    const int64_t g = c.L.t_off[ch] + e;
-    const double D = (double)f[4] * (double)c.eF;
-    const float y = (float)((T[g] - tmp2) * D * (double)c.vol / kMlNum);
+    const int ij = e / P, ab = e - ij * P;
+    const int2 po = Lt.pp_orb[Lt.pp_off[ch] + ab], ho = Lt.hh_orb[Lt.hh_off[ch] + ij];
+    const int a = src.oof[okey[po.x]], b = src.oof[okey[po.y]];
+    const int i = src.oof[okey[ho.x]], j = src.oof[okey[ho.y]];
+    float y = 0.0f;
+    if (a >= L.A && b >= L.A && i >= 0 && i < L.A && j >= 0 && j < L.A) {
+      const int2 sab = L.pp_slot[(int64_t)(a - L.A) * L.NP + (b - L.A)];
+      const int2 sij = L.hh_slot[i * L.A + j];
+      if (sab.y != 0 && sij.y != 0 && sab.x == sij.x) {
+        const int64_t gs = L.t_off[sab.x] + sidx(sab.y) + (int64_t)L.P[sab.x] * sidx(sij.y);
+        const double sg = ssign(sab.y) * ssign(sij.y);
+        const double D = ((0.0 - src.fd[a]) - src.fd[b] + src.fd[i]) + src.fd[j];
+        if (D != 0.0) y = (float)(sg * (src.T[gs] - src.V[gs] / D) * D * src.vol / kMlNum);
+      }
+    }
+    const int64_t g = Lt.t_off[ch] + e;
     prior[g] = first ? w * y : fmaf(w, y, prior[g]);
   }
 }
@@ -548,23 +572,26 @@ class Learner final : public ILearner {
     lck(cudaStreamSynchronize(v.st), "feature extraction");
     data_.push_back(std::move(c));
   }
-  void set_prior(const MLView *views, const double *w, int n) override {
+  void set_prior(const MLView &target, const MLView *views, const double *w, int n) override {
     lck(cudaSetDevice(device_), "cudaSetDevice");
     has_prior_ = false;
     if (n <= 0) return;
-    const int64_t nt = views[0].n_t;
-    for (int i = 1; i < n; ++i)
-      if (views[i].n_t != nt || views[i].L.nch != views[0].L.nch)
-        throw EngineError(1, "learner: the prior's engines have different layouts");
+    const int64_t nt = target.n_t;
+    for (int i = 0; i < n; ++i)
+      if (views[i].nkeys != target.nkeys || views[i].L.ns != target.L.ns || views[i].L.A != target.L.A)
+        throw EngineError(1, "learner: the prior's engines are not the target's lattice at another density");
     if (prior_.bytes < (size_t)std::max<int64_t>(nt, 1) * 4) prior_.alloc((size_t)std::max<int64_t>(nt, 1) * 4);
+    lck(cudaStreamSynchronize(target.st), "prior");
     for (int i = 0; i < n; ++i) {
-      MLCtx c = make_ctx(views[i]);
-      c.prior = nullptr;
-      if (views[i].L.nttile)
-        k_ml_prior<<<views[i].L.nttile, 256, 0, views[i].st>>>(c, views[i].T, (float)w[i], i == 0, prior_.as<float>());
+      const MLView &v = views[i];
+      lck(cudaStreamSynchronize(v.st), "prior");  // the source's amplitudes are final
+      const PriorSrc src{v.L, v.fdiag, v.Vhp, v.T, v.oof, v.vol};
+      if (target.L.nttile)
+        k_ml_prior<<<target.L.nttile, 256, 0, target.st>>>(target.L, target.okey, src, (float)w[i], i == 0,
+                                                            prior_.as<float>());
       lck(cudaGetLastError(), "prior");
-      lck(cudaStreamSynchronize(views[i].st), "prior");
     }
+    lck(cudaStreamSynchronize(target.st), "prior");
     prior_n_ = nt;
     has_prior_ = true;
   }

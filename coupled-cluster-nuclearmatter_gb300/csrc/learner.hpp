@@ -34,6 +34,12 @@ struct MLView {
   const double *Vhp = nullptr;    // packed V_hhpp' (same layout as T')
   double *T = nullptr;            // packed T'
   int64_t n_t = 0;
+  // orbitals by quantum numbers: okey[p] is orbital p's slot in the (nx, ny, nz, spin,
+  // isospin) table, oof[slot] the orbital there (-1 if none); nkeys slots.  The index
+  // sort orders the states of a degenerate shell by rounding-level differences of |k|^2,
+  // so one quantum-number state has different orbital numbers at different densities.
+  const int *okey = nullptr, *oof = nullptr;
+  int nkeys = 0;
   double rho = 0, kF = 0, eF = 0, vol = 0, theta[3] = {0, 0, 0};
   cudaStream_t st = nullptr;
 };
@@ -44,11 +50,11 @@ class ILearner {
   // features and targets (converged T minus MP2) of the view's current amplitudes, every
   // stride-th packed amplitude
   virtual void add_solution(const MLView &v, int stride) = 0;
-  // Prior for the features of later add_solution / warm_start calls: sum_i w[i] times the
-  // target correction of views[i]'s current (converged) amplitudes, per packed amplitude.
-  // The views share one layout (another density of the same lattice and twist).  n = 0
-  // clears it (the prior feature and its flag read 0).
-  virtual void set_prior(const MLView *views, const double *w, int n) = 0;
+  // Prior for the features of later add_solution / warm_start calls on target: per packed
+  // amplitude of target, sum_i w[i] times the target correction of views[i]'s current
+  // (converged) amplitudes at the same quantum numbers (the same lattice and twist at
+  // other densities).  n = 0 clears it (the prior feature and its flag read 0).
+  virtual void set_prior(const MLView &target, const MLView *views, const double *w, int n) = 0;
   virtual void clear() = 0;
   virtual int64_t samples() const = 0;
   // Adam on shuffled minibatches; returns the mean loss of the last 10 steps

@@ -356,12 +356,15 @@ int ccx_learner_destroy(ccx_learner *l);
 int ccx_learner_add_solution(ccx_learner *l, ccx_engine *e);
 /* the same with every stride-th packed amplitude (large lattices, many solutions) */
 int ccx_learner_add_solution_sampled(ccx_learner *l, ccx_engine *e, int32_t stride);
-/* Prior of later add_solution / ccx_init_learned calls: sum_i weights[i] times the
- * converged-minus-MP2 correction of engines[i]'s current T2, per packed amplitude, for
- * example the two neighbouring densities of the same lattice and twist with weights
- * 0.5 and 0.5.  The engines share the layout of the engines it is then used with; n = 0
- * clears the prior. */
-int ccx_learner_set_prior(ccx_learner *l, int32_t n, ccx_engine *const *engines, const double *weights);
+/* Prior of later add_solution / ccx_init_learned calls on target: per packed amplitude
+ * of target, sum_i weights[i] times the converged-minus-MP2 correction of engines[i]'s
+ * current T2 at the same quantum numbers, for example the two neighbouring densities of
+ * the same lattice and twist with weights 0.5 and 0.5.  Amplitudes are matched through
+ * the orbitals' quantum numbers, not their numbers: the index sort orders the states of a
+ * degenerate shell by rounding-level differences of |k|^2, so the orbital numbering
+ * differs between densities.  n = 0 clears the prior. */
+int ccx_learner_set_prior(ccx_learner *l, ccx_engine *target, int32_t n, ccx_engine *const *engines,
+                          const double *weights);
 int ccx_learner_clear(ccx_learner *l);
 int ccx_learner_samples(const ccx_learner *l, int64_t *n);
 /* Adam on shuffled minibatches; *loss = mean loss of the last 10 steps */

@@ -103,27 +103,34 @@ def test_learned_start_with_neighbour_prior_saves_iterations(ccx):
     """The C5 protocol in small: PNM 14 on the nmax=2 lattice at 9 densities, trained on
     the even-indexed ones (each with the prior interpolated from the even densities on
     either side), evaluated on the held-out odd-indexed ones (prior from the two even
-    neighbours).  On every held-out density the learned start converges to ||R|| < 1e-10
-    in fewer iterations than the MP2 start, to the same energy."""
+    neighbours).  The prior matches amplitudes by quantum numbers: the index sort numbers
+    the states of a degenerate shell differently at different densities.  On every
+    held-out density the learned start's residual is far below the MP2 start's, and it
+    converges to ||R|| < 1e-10 in fewer iterations, to the same energy."""
     rhos = [0.05 + 0.005 * k for k in range(9)]
     sweep = density_sweep(ccx, 14, 2, rhos)
     lrn = ccx.Learner(seed=5)
-    even = list(range(0, 9, 2))
-    for k in even:
+    for k in range(0, 9, 2):
         nb = [j for j in (k - 2, k + 2) if 0 <= j < 9]
-        lrn.set_prior([sweep[j][2] for j in nb], [1.0 / len(nb)] * len(nb))
+        lrn.set_prior(sweep[k][2], [sweep[j][2] for j in nb], [1.0 / len(nb)] * len(nb))
         lrn.add_solution(sweep[k][2])
     lrn.train(steps=2000, batch=4096, lr=2e-3, seed=3)
-    saved = []
+    saved, ratios = [], []
     for k in range(1, 9, 2):
-        _, L, e, r_ref = sweep[k]
+        _, L, e, _ = sweep[k]
+        e.setup_t_amplitudes()
+        s_mp2 = solve64(ccx, e, max_iter=1)["res_norm"]
         e.setup_t_amplitudes()
         r_mp2 = solve64(ccx, e)
-        lrn.set_prior([sweep[k - 1][2], sweep[k + 1][2]], [0.5, 0.5])
+        lrn.set_prior(e, [sweep[k - 1][2], sweep[k + 1][2]], [0.5, 0.5])
+        lrn.warm_start(e)
+        s_ml = solve64(ccx, e, max_iter=1)["res_norm"]
         lrn.warm_start(e)
         r_ml = solve64(ccx, e)
         assert r_mp2["converged"] and r_ml["converged"]
         e_conv = r_mp2["e_ccd"].real
         assert abs(r_ml["e_ccd"].real - e_conv) < 1e-10 * abs(e_conv)  # far inside 1 keV per nucleon
+        ratios.append(s_ml / s_mp2)
         saved.append(r_mp2["iterations"] - r_ml["iterations"])
-    assert all(s >= 1 for s in saved), saved
+    assert max(ratios) < 0.2, ratios
+    assert all(s >= 1 for s in saved), (saved, ratios)
