@@ -29,7 +29,7 @@ void tck(cudaError_t e, const char *what) {
 struct TriplesDev {
   int ns, A, NP, nk0, nk1, nk2, tzmin, tzmax;
   const int *orbit_of;                 // (nx, ny, nz, spin, isospin) -> orbital or -1
-  const int4 *nq;                      // per orbital (nx, ny, nz, tz) in one load
+  const int *nx, *ny, *nz, *tz;
   const int2 *hp5_slot, *pp5_slot;     // hppp blocks: (channel, row) / (channel, column)
   const int64_t *v5_off;
   const int *n5;                       // rows of each hppp block
@@ -99,12 +99,11 @@ __device__ __forceinline__ double wnorm2(cplxf w) { return (double)w.re * (doubl
 // acc + sign * sum_d conj(<cb|V|kd>) T(ad, ij), the sign as a bit.  Not inlined: the 18
 // calls of a pair would otherwise unroll into a body larger than the instruction cache,
 // and the warps stall on fetches.
-// (the momenta qa, qi, qj of orbitals a, i, j are loaded once per pair by the caller)
 template <typename W>
 __device__ __noinline__ W one_particle(const TriplesDev &D, const DevLayout &L, const W *T, const W *V5, int a, int b,
-                                       int c, int i, int j, int k, int4 qa, int4 qi, int4 qj, unsigned m, W acc) {
-  const int nxd = qi.x + qj.x - qa.x, nyd = qi.y + qj.y - qa.y;
-  const int nzd = qi.z + qj.z - qa.z, tzd = qi.w + qj.w - qa.w;
+                                       int c, int i, int j, int k, unsigned m, W acc) {
+  const int nxd = D.nx[i] + D.nx[j] - D.nx[a], nyd = D.ny[i] + D.ny[j] - D.ny[a];
+  const int nzd = D.nz[i] + D.nz[j] - D.nz[a], tzd = D.tz[i] + D.tz[j] - D.tz[a];
   if (abs(nxd) > D.nk0 || abs(nyd) > D.nk1 || abs(nzd) > D.nk2 || abs(tzd) > 1) return acc;
   const int2 cl = D.pp5_slot[(int64_t)(c - D.A) * D.NP + (b - D.A)];
   if (cl.x < 0) return acc;
@@ -120,12 +119,11 @@ __device__ __noinline__ W one_particle(const TriplesDev &D, const DevLayout &L, 
 }
 
 // acc + sign * sum_l conj(<jk|V|lc>) T(ab, il) (not inlined, as one_particle)
-// (the momenta qc, qj, qk of orbitals c, j, k are loaded once per pair by the caller)
 template <typename W>
 __device__ __noinline__ W one_hole(const TriplesDev &D, const DevLayout &L, const W *T, const W *V2, int a, int b,
-                                   int c, int i, int j, int k, int4 qc, int4 qj, int4 qk, unsigned m, W acc) {
-  const int nxl = qk.x + qj.x - qc.x, nyl = qk.y + qj.y - qc.y;
-  const int nzl = qk.z + qj.z - qc.z, tzl = qk.w + qj.w - qc.w;
+                                   int c, int i, int j, int k, unsigned m, W acc) {
+  const int nxl = D.nx[k] + D.nx[j] - D.nx[c], nyl = D.ny[k] + D.ny[j] - D.ny[c];
+  const int nzl = D.nz[k] + D.nz[j] - D.nz[c], tzl = D.tz[k] + D.tz[j] - D.tz[c];
   if (abs(nxl) > D.nk0 || abs(nyl) > D.nk1 || abs(nzl) > D.nk2 || abs(tzl) > 1) return acc;
   const int2 r = D.hh2_slot[j * D.A + k];
   if (r.x < 0) return acc;
@@ -185,37 +183,34 @@ __global__ void __launch_bounds__(256) k_triples(TriplesDev D, DevLayout L, cons
   for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < total; g += (int64_t)gridDim.x * blockDim.x) {
     while (g >= D.elem_off[ch + 1]) ++ch;
     const int64_t loc = g - D.elem_off[ch];
-    // neighbouring threads take neighbouring hole triples ijk of one particle triple abc
-    // (the other order, particle triples fastest, measured 15% slower)
     const int nb = D.nbra[ch];
     const int ket = (int)(loc / nb), bra = (int)(loc % nb);
     const int3 abc = D.ppp[D.ppp_off[ch] + ket];
     const int3 ijk = D.hhh[D.hhh_off[ch] + bra];
     const int a = abc.x, b = abc.y, c = abc.z, i = ijk.x, j = ijk.y, k = ijk.z;
-    const int4 qa = D.nq[a], qb = D.nq[b], qc = D.nq[c], qi = D.nq[i], qj = D.nq[j], qk = D.nq[k];
     const S spen = eh[D.hhh_off[ch] + bra] - ep[D.ppp_off[ch] + ket];
     // W = the 9 particle terms minus the 9 hole terms, accumulated in one sum with the
     // permutation signs applied as sign-bit flips
     constexpr unsigned P = 0, N = 1;
     W tc = wzero<W>();
-    tc = one_particle<W>(D, L, T, V5, a, b, c, i, j, k, qa, qi, qj, P, tc);
-    tc = one_particle<W>(D, L, T, V5, b, a, c, i, j, k, qb, qi, qj, N, tc);
-    tc = one_particle<W>(D, L, T, V5, c, b, a, i, j, k, qc, qi, qj, N, tc);
-    tc = one_particle<W>(D, L, T, V5, a, b, c, k, j, i, qa, qk, qj, N, tc);
-    tc = one_particle<W>(D, L, T, V5, a, b, c, i, k, j, qa, qi, qk, N, tc);
-    tc = one_particle<W>(D, L, T, V5, c, b, a, i, k, j, qc, qi, qk, P, tc);
-    tc = one_particle<W>(D, L, T, V5, c, b, a, k, j, i, qc, qk, qj, P, tc);
-    tc = one_particle<W>(D, L, T, V5, b, a, c, i, k, j, qb, qi, qk, P, tc);
-    tc = one_particle<W>(D, L, T, V5, b, a, c, k, j, i, qb, qk, qj, P, tc);
-    tc = one_hole<W>(D, L, T, V2, a, b, c, i, j, k, qc, qj, qk, N, tc);
-    tc = one_hole<W>(D, L, T, V2, a, c, b, i, j, k, qb, qj, qk, P, tc);
-    tc = one_hole<W>(D, L, T, V2, c, b, a, i, j, k, qa, qj, qk, P, tc);
-    tc = one_hole<W>(D, L, T, V2, a, b, c, k, j, i, qc, qj, qi, P, tc);
-    tc = one_hole<W>(D, L, T, V2, a, b, c, j, i, k, qc, qi, qk, P, tc);
-    tc = one_hole<W>(D, L, T, V2, c, b, a, j, i, k, qa, qi, qk, N, tc);
-    tc = one_hole<W>(D, L, T, V2, c, b, a, k, j, i, qa, qj, qi, N, tc);
-    tc = one_hole<W>(D, L, T, V2, a, c, b, j, i, k, qb, qi, qk, N, tc);
-    tc = one_hole<W>(D, L, T, V2, a, c, b, k, j, i, qb, qj, qi, N, tc);
+    tc = one_particle<W>(D, L, T, V5, a, b, c, i, j, k, P, tc);
+    tc = one_particle<W>(D, L, T, V5, b, a, c, i, j, k, N, tc);
+    tc = one_particle<W>(D, L, T, V5, c, b, a, i, j, k, N, tc);
+    tc = one_particle<W>(D, L, T, V5, a, b, c, k, j, i, N, tc);
+    tc = one_particle<W>(D, L, T, V5, a, b, c, i, k, j, N, tc);
+    tc = one_particle<W>(D, L, T, V5, c, b, a, i, k, j, P, tc);
+    tc = one_particle<W>(D, L, T, V5, c, b, a, k, j, i, P, tc);
+    tc = one_particle<W>(D, L, T, V5, b, a, c, i, k, j, P, tc);
+    tc = one_particle<W>(D, L, T, V5, b, a, c, k, j, i, P, tc);
+    tc = one_hole<W>(D, L, T, V2, a, b, c, i, j, k, N, tc);
+    tc = one_hole<W>(D, L, T, V2, a, c, b, i, j, k, P, tc);
+    tc = one_hole<W>(D, L, T, V2, c, b, a, i, j, k, P, tc);
+    tc = one_hole<W>(D, L, T, V2, a, b, c, k, j, i, P, tc);
+    tc = one_hole<W>(D, L, T, V2, a, b, c, j, i, k, P, tc);
+    tc = one_hole<W>(D, L, T, V2, c, b, a, j, i, k, N, tc);
+    tc = one_hole<W>(D, L, T, V2, c, b, a, k, j, i, N, tc);
+    tc = one_hole<W>(D, L, T, V2, a, c, b, j, i, k, N, tc);
+    tc = one_hole<W>(D, L, T, V2, a, c, b, k, j, i, N, tc);
     const S term = S(wnorm2(tc)) / spen;
     acc[0] += real_(term);
     acc[1] += imag_(term);
@@ -300,12 +295,7 @@ class Triples final : public ITriples<S> {
     TD_.tzmin = B.tzmin; TD_.tzmax = B.tzmax;
     orbit_of_.put(B.orbit_of);
     TD_.orbit_of = orbit_of_.as<int>();
-    {
-      std::vector<int4> nq(ns);
-      for (int p = 0; p < ns; ++p) nq[p] = make_int4(B.nx[p], B.ny[p], B.nz[p], B.tz[p]);
-      nq_.put(nq);
-      TD_.nq = nq_.as<int4>();
-    }
+    TD_.nx = O.nx; TD_.ny = O.ny; TD_.nz = O.nz; TD_.tz = O.tz;
     // hppp (kind 5) and hhhp (kind 2) blocks in the reference's ordered layout
     auto blocks = [&](int kind, std::vector<int2> &s1slot, std::vector<int2> &s2slot, bool s1_is_hh, DB &off, DB &nrow,
                       std::vector<int64_t> &offh, std::vector<int2> &rows, std::vector<int2> &cols, std::vector<int> &nr,
@@ -557,7 +547,7 @@ class Triples final : public ITriples<S> {
   DevLayout D_;
   DevOrbits O_;
   TriplesDev TD_{};
-  DB nq_, orbit_of_, hp5_slot_, pp5_slot_, hh2_slot_, hp2_slot_, v5_off_, n5_, v2_off_, n2_;
+  DB orbit_of_, hp5_slot_, pp5_slot_, hh2_slot_, hp2_slot_, v5_off_, n5_, v2_off_, n2_;
   DB rows5_, cols5_, rows2_, cols2_, nc5_, ro5_, co5_, nc2_, ro2_, co2_;
   DB V5l_, V2l_, Tl_;  // FP32 copies for the FP32 contractions
   bool low_ready_ = false;
