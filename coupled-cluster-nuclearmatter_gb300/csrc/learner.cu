@@ -43,6 +43,7 @@ struct LBuf {
 };
 
 // ---------------------------------------------------------------- features
+constexpr float kMlPriorUnit = 100.0f;  // the prior feature in units of 0.01, a typical correction
 struct MLCtx {
   DevLayout L;
   DevOrbits O;
@@ -86,7 +87,7 @@ __device__ void ml_feat(const MLCtx &c, int ch, int e, float (&f)[kMlIn], double
   f[14] = (float)(c.O.tz[a] * c.O.tz[b]);
   f[15] = (float)(c.O.tz[a] * c.O.tz[i]);
   // the prior: the correction interpolated from neighbouring converged solutions
-  f[16] = c.prior ? c.prior[c.L.t_off[ch] + e] : 0.0f;
+  f[16] = c.prior ? c.prior[c.L.t_off[ch] + e] * kMlPriorUnit : 0.0f;
   f[17] = c.prior ? 1.0f : 0.0f;
 }
 
@@ -115,7 +116,7 @@ __global__ void k_ml_extract(MLCtx c, const double *__restrict__ T, int stride, 
     const double D = (double)f[4] * (double)c.eF;
     // with a prior the network learns what the prior leaves over (a skip connection):
     // the BF16 inference then perturbs only that small remainder
-    y[o] = (float)((T[g] - tmp2) * D * (double)c.vol / kMlNum) - f[16];
+    y[o] = (float)((T[g] - tmp2) * D * (double)c.vol / kMlNum) - (c.prior ? c.prior[g] : 0.0f);
   }
 }
 // A solution the prior is taken from (another density of the same lattice and twist)
@@ -305,6 +306,9 @@ __global__ void k_ml_adam(float *__restrict__ p, float *__restrict__ m, float *_
   }
 }
 
+__global__ void k_ml_scale(float *__restrict__ x, int64_t n, float s) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) x[i] *= s;
+}
 __global__ void k_ml_fill(float *__restrict__ x, int64_t n, float v) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) x[i] = v;
 }
@@ -554,6 +558,7 @@ class Learner final : public ILearner {
     fill(kMlOffW3, kMlW * kMlW, kMlW, 1.0);
     fill(kMlOffW4, kMlW, kMlW, 0.1);
     set_params(p.data());
+    folded_ = false;  // the initial output layer is in the standardised units of training
   }
   ~Learner() override {
     if (st_) cudaStreamDestroy(st_);
@@ -618,6 +623,19 @@ class Learner final : public ILearner {
       lck(cudaMemcpyAsync(ya.as<float>() + o, c.y.p, (size_t)c.n * 4, cudaMemcpyDeviceToDevice, st_), "copy");
       o += c.n;
     }
+    // The network trains on targets divided by their RMS (fixed at the first training)
+    // and the output layer is scaled back afterwards, so that the loss is relative to the
+    // size of what is learned (with a prior, a small remainder)
+    if (yscale_ <= 0.0f) {
+      std::vector<float> yh(N);
+      lck(cudaMemcpyAsync(yh.data(), ya.p, (size_t)N * 4, cudaMemcpyDeviceToHost, st_), "targets");
+      lck(cudaStreamSynchronize(st_), "targets");
+      double ss = 0.0;
+      for (float v : yh) ss += (double)v * v;
+      yscale_ = (float)std::max(std::sqrt(ss / (double)N), 1e-12);
+    }
+    k_ml_scale<<<1216, 256, 0, st_>>>(ya.as<float>(), N, 1.0f / yscale_);
+    if (folded_) k_ml_scale<<<1, 256, 0, st_>>>(params_.as<float>() + kMlOffW4, kMlW + 1, 1.0f / yscale_);
     Xs.alloc((size_t)N * kMlIn * 4);
     ys.alloc((size_t)N * 4);
     perm.alloc((size_t)N * 8);
@@ -644,6 +662,10 @@ class Learner final : public ILearner {
       k_ml_adam<<<(kMlParams + 255) / 256, 256, 0, st_>>>(params_.as<float>(), m_.as<float>(), v_.as<float>(),
                                                            grad_.as<float>(), kMlParams, (float)lr, b1t, b2t);
     }
+    // the output layer back in the targets' units (the Adam moments stay with the
+    // standardised units of the next training)
+    k_ml_scale<<<1, 256, 0, st_>>>(params_.as<float>() + kMlOffW4, kMlW + 1, yscale_);
+    folded_ = true;
     lck(cudaGetLastError(), "training");
     lck(cudaMemcpyAsync(losses.data(), lossd.p, (size_t)steps * 8, cudaMemcpyDeviceToHost, st_), "loss");
     lck(cudaStreamSynchronize(st_), "training");
@@ -651,7 +673,7 @@ class Learner final : public ILearner {
     const int k0 = std::max(0, steps - 10);
     for (int s = k0; s < steps; ++s) tail += losses[s];
     weights_dirty_ = true;
-    return tail / (steps - k0);
+    return tail / (steps - k0) * (double)yscale_ * (double)yscale_;
   }
 
   void warm_start(const MLView &v) override {
@@ -673,6 +695,7 @@ class Learner final : public ILearner {
   }
   void set_params(const float *p) override {
     lck(cudaMemcpy(params_.p, p, kMlParams * 4, cudaMemcpyHostToDevice), "params");
+    folded_ = true;  // parameters from get_params: output layer in the targets' units
     lck(cudaMemset(m_.p, 0, kMlParams * 4), "adam");
     lck(cudaMemset(v_.p, 0, kMlParams * 4), "adam");
     t_ = 0;
@@ -856,6 +879,8 @@ class Learner final : public ILearner {
   LBuf prior_;
   int64_t prior_n_ = 0;
   bool has_prior_ = false;
+  float yscale_ = 0.0f;  // RMS of the training targets (0: not measured yet)
+  bool folded_ = false;  // the output layer is in the targets' units
 };
 
 }  // namespace
