@@ -632,7 +632,7 @@ class Engine:
 
     KERNEL_SLOTS = ("x_fp64", "i4_fp64", "ring_fp64", "ladder_fp64", "pp_rebase_fp64", "hh_fp64",
                     "pp_tc", "i4_tc", "ring_tc", "split", "pp_rebase_digits", "i4_rebase_digits",
-                    "ring_rebase_digits", "i7_fp64")
+                    "ring_rebase_digits", "i7_fp64", "x_rebase_digits", "hh_rebase_digits")
 
     def autotune(self):
         """Pick the FP64 GEMM tile shape per N bucket by timing; returns (shapes, ms)."""

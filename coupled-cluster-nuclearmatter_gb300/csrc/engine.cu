@@ -1981,7 +1981,7 @@ class Engine final : public IEngine {
     auto mpad = [](int x) { return (x + 127) / 128 * 128; };
     auto npadf = [](int x) { return (x + 15) / 16 * 16; };
     auto nkf = [](int x) { return (x + 63) / 64; };
-    int64_t pa = 0, pb = 0, ra = 0, rb = 0;
+    int64_t pa = 0, pb = 0, ra = 0, rb = 0, px = 0, rx = 0, pta = 0, rta = 0, pi9 = 0, ri9 = 0;
     for (int c = 0; c < nc; ++c) {
       const auto &pk = L.pk[c];
       if (pk.P <= 0 || pk.H <= 0) continue;
@@ -1989,6 +1989,12 @@ class Engine final : public IEngine {
       pb += (int64_t)npadf(pk.H) * nkf(pk.P) * 64;
       ra += pk.P;
       rb += npadf(pk.H);
+      px += (int64_t)mpad(pk.H) * nkf(pk.P) * 64;     // A = V_hhpp'^T (H x P)
+      rx += pk.H;
+      pta += (int64_t)mpad(pk.P) * nkf(pk.H) * 64;    // A = T' (P x H)
+      rta += pk.P;
+      pi9 += (int64_t)npadf(pk.H) * nkf(pk.H) * 64;   // B = I9' (K H, N H)
+      ri9 += npadf(pk.H);
     }
     int64_t pv = 0, pt = 0, pr = 0, pi = 0, rv = 0, rt = 0, rr = 0, ri = 0;
     for (int q = 0; q < nq; ++q) {
@@ -2006,26 +2012,44 @@ class Engine final : public IEngine {
     alloc_oz(ozTphB_, pt, rt);
     alloc_oz(ozTphA_, pr, rr);
     alloc_oz(ozI4B_, pi, ri);
+    alloc_oz(ozVhpA_, px, rx);
+    alloc_oz(ozTA_, pta, rta);
+    alloc_oz(ozI9B_, pi9, ri9);
     if (!tcerr_.p) {
       tcerr_.alloc(sizeof(int), &bytes_);
       CK(cudaMemset(tcerr_.p, 0, sizeof(int)));
     }
-    std::vector<OzSplitJob> jv, jb, jt, ji;
-    OzList lpp, l4, lr;
+    std::vector<OzSplitJob> jv, jb, jt, ji, j9;
+    OzList lpp, l4, lr, lx, lhh;
     {
-      int64_t qa = 0, qb = 0, xa = 0, xb = 0, voff = 0;
+      int64_t qa = 0, qb = 0, xa = 0, xb = 0, voff = 0, hoff = 0;
+      int64_t qx = 0, xx = 0, qta = 0, xta = 0, q9 = 0, x9 = 0;
       for (int c = 0; c < nc; ++c) {
         const auto &pk = L.pk[c];
         if (pk.P > 0 && pk.H > 0) {
           add_oz_split(jv, Vpp_.as<S>() + voff, pk.P, 1, pk.P, pk.P, 128, mpad(pk.P), ozVpp_, qa, xa);
           add_oz_split(jb, T_.as<S>() + pk.t_off, pk.P, 1, pk.H, pk.P, npadf(pk.H), npadf(pk.H), ozTb_, qb, xb);
           add_oz(lpp, ozVpp_, qa, xa, ozTb_, qb, xb, pk.P, pk.H, pk.P, PPb_.as<S>() + pk.t_off, 1, pk.P, 1.0);
+          // X(kl, ij) = sum_cd V_hhpp'(cd, kl) T'(cd, ij): A = V_hhpp'^T, B the T' digits above
+          add_oz_split(jv, Vhp_.as<S>() + pk.t_off, pk.P, 1, pk.H, pk.P, 128, mpad(pk.H), ozVhpA_, qx, xx);
+          add_oz(lx, ozVhpA_, qx, xx, ozTb_, qb, xb, pk.H, pk.H, pk.P, X_.as<S>() + hoff, 1, pk.H, 1.0);
+          // HH_b(ab, ij) = sum_kl T'(ab, kl) I9'(kl, ij)
+          add_oz_split(jb, T_.as<S>() + pk.t_off, 1, pk.P, pk.P, pk.H, 128, mpad(pk.P), ozTA_, qta, xta);
+          add_oz_split(j9, I9_.as<S>() + hoff, pk.H, 1, pk.H, pk.H, npadf(pk.H), npadf(pk.H), ozI9B_, q9, x9);
+          add_oz(lhh, ozTA_, qta, xta, ozI9B_, q9, x9, pk.P, pk.H, pk.H, PPb_.as<S>() + pk.t_off, 1, pk.P, 1.0);
           qa += (int64_t)mpad(pk.P) * nkf(pk.P) * 64;
           qb += (int64_t)npadf(pk.H) * nkf(pk.P) * 64;
           xa += pk.P;
           xb += npadf(pk.H);
+          qx += (int64_t)mpad(pk.H) * nkf(pk.P) * 64;
+          xx += pk.H;
+          qta += (int64_t)mpad(pk.P) * nkf(pk.H) * 64;
+          xta += pk.P;
+          q9 += (int64_t)npadf(pk.H) * nkf(pk.H) * 64;
+          x9 += npadf(pk.H);
         }
         voff += (int64_t)pk.P * pk.P;
+        hoff += (int64_t)pk.H * pk.H;
       }
     }
     {
@@ -2053,7 +2077,10 @@ class Engine final : public IEngine {
     finalize_oz_split(ozsTb_, jb);
     finalize_oz_split(ozsTph_, jt);
     finalize_oz_split(ozsI4_, ji);
+    finalize_oz_split(ozsI9_, j9);
     finalize_oz(ozPP_, lpp);
+    finalize_oz(ozX_, lx);
+    finalize_oz(ozHH_, lhh);
     finalize_oz(ozI4_, l4);
     finalize_oz(ozRing_, lr);
     run_oz_split(ozsV_);
@@ -2277,16 +2304,31 @@ class Engine final : public IEngine {
     run_split(spTphb_);
   }
 
-  // FP64 residual at T that also becomes the new base of the defect correction; with
-  // digits, PP_b = V_pppp' T comes from the exact digit-product GEMM
+  // FP64 residual at T that also becomes the new base of the defect correction.  With
+  // digits, every product of it on the FP64 pipe except the one-body dots moves to the
+  // exact digit-product GEMM: X = V_hhpp'^T T', I4, the ring, PP_b = V_pppp' T' and
+  // HH_b = T' I9'.
   void residual_fp64_rebase(bool digits) {
     mark(0);
-    const cudaStream_t xs = fork_side();
     launch_gather_tph<S>(D_, T_.as<S>(), Tph_.as<S>(), st_);
     mark(1);
-    kbegin(kKX);
-    run_x(xs);
-    kend();
+    cudaStream_t xs;
+    if (digits) {
+      // T' digits as the B operand (X, PP_b) and as the A operand (HH_b)
+      kbegin(kKSplit);
+      run_oz_split(ozsTb_);
+      kend();
+      CK(cudaMemsetAsync(X_.p, 0, std::max<int64_t>(n_hh2_, 1) * sizeof(S), st_));
+      kbegin(kKXOz);
+      run_oz(ozX_);
+      kend();
+      xs = fork_side();
+    } else {
+      xs = fork_side();
+      kbegin(kKX);
+      run_x(xs);
+      kend();
+    }
     launch_i7<S>(D_, X_.as<S>(), fdiag_.as<S>(), f7_.as<S>(), d2ij_.as<S>(), i7off_.as<S>(), xs);
     launch_i9<S>(D_, n_hh2_, Vhh_.as<S>(), X_.as<S>(), I9_.as<S>(), xs);
     mark(2);
@@ -2320,31 +2362,35 @@ class Engine final : public IEngine {
     }
     mark(5);
     join_side(xs);
-    if (xs != st_) run_plan(planHH_, xs);  // HH_b = T' I9' beside the pp-ladder product
+    if (!digits && xs != st_) run_plan(planHH_, xs);  // HH_b = T' I9' beside the pp-ladder product
     launch_rinit<S>(D_, omap_.as<int4>(), rmap_.as<int4>(), T_.as<S>(), Vhp_.as<S>(), Rph_.as<S>(), i6off_.as<S>(),
                     i7off_.as<S>(), nullptr, Rringb_.as<S>(), R_.as<S>(), st_);
     mark(6);
     if (digits) {
+      // PP_b and then HH_b accumulate into PP_b (two launches in stream order)
       kbegin(kKSplit);
-      run_oz_split(ozsTb_);
+      run_oz_split(ozsI9_);
       kend();
       CK(cudaMemsetAsync(PPb_.p, 0, n_t_ * sizeof(S), st_));
       kbegin(kKPPOz);
       run_oz(ozPP_);
       kend();
+      kbegin(kKHHOz);
+      run_oz(ozHH_);
+      kend();
     } else {
       kbegin(kKPP64);
       run_plan(planPP_);
       kend();
+      if (xs == st_) {
+        kbegin(kKHH64);
+        run_plan(planHH_);  // HH_b = T' I9'
+        kend();
+      }
+      join_side(xs, 2);
+      launch_axpy<S>(n_t_, HHb_.as<S>(), PPb_.as<S>(), st_);
     }
-    if (xs == st_) {
-      kbegin(kKHH64);
-      run_plan(planHH_);  // HH_b = T' I9'
-      kend();
-    }
-    join_side(xs, 2);
     // the cached products of the new base, PP_b + HH_b, and R' += them
-    launch_axpy<S>(n_t_, HHb_.as<S>(), PPb_.as<S>(), st_);
     launch_axpy<S>(n_t_, PPb_.as<S>(), R_.as<S>(), st_);
     // the new base
     CK(cudaMemcpyAsync(Xb_.p, X_.p, std::max<int64_t>(n_hh2_, 1) * sizeof(S), cudaMemcpyDeviceToDevice, st_));
@@ -2453,9 +2499,9 @@ class Engine final : public IEngine {
   int tc_kind_ = 0;
   int64_t v_version_ = 0, mixed_v_version_ = -1;
   DBuf Tb_, PPb_, Tphb_, Rringb_, I4b_, dI4_, tcerr_, Xb_, dI9_, HHb_, xd7_;
-  OzBuf ozVpp_, ozTb_, ozVph_, ozTphB_, ozTphA_, ozI4B_;
-  OzSplitPlan ozsV_, ozsTb_, ozsTph_, ozsI4_;
-  OzPlan ozPP_, ozI4_, ozRing_;
+  OzBuf ozVpp_, ozTb_, ozVph_, ozTphB_, ozTphA_, ozI4B_, ozVhpA_, ozTA_, ozI9B_;
+  OzSplitPlan ozsV_, ozsTb_, ozsTph_, ozsI4_, ozsI9_;
+  OzPlan ozPP_, ozI4_, ozRing_, ozX_, ozHH_;
   bool oz_ready_ = false;
   int64_t oz_v_version_ = -1;
   TileBuf tVpp_, tD_, tVph_, tDphB_, tTphbA_, tDphA_, tdI4B_, tI4B_, tDA_, tI9B_, tTbA_, tdI9B_, tVhT_;

@@ -55,6 +55,8 @@ enum KernelSlot {
   kKI4Oz = 11,  // k_oz_gemm: I4 at a re-base as exact digit products
   kKRingOz = 12,  // k_oz_gemm: ring at a re-base as exact digit products
   kKI7 = 13,    // k_i7dots + k_i7sum: I7 of a mixed residual from the X entries it reads
+  kKXOz = 14,   // k_oz_gemm: X = V_hhpp'^T T' at a re-base as exact digit products
+  kKHHOz = 15,  // k_oz_gemm: HH_b = T' I9' at a re-base as exact digit products
   kKernelSlots = 16
 };
 

@@ -20,7 +20,7 @@ namespace ccx {
 
 constexpr int kMlIn = 18;    // features: 16 of the amplitude, the prior correction and its flag
 constexpr int kMlW = 128;    // hidden width
-// parameter vector: W1[128][16] b1[128] W2[128][128] b2[128] W3[128][128] b3[128] w4[128] b4
+// parameter vector: W1[128][18] b1[128] W2[128][128] b2[128] W3[128][128] b3[128] w4[128] b4
 constexpr int kMlOffW1 = 0, kMlOffB1 = kMlOffW1 + kMlW * kMlIn, kMlOffW2 = kMlOffB1 + kMlW,
               kMlOffB2 = kMlOffW2 + kMlW * kMlW, kMlOffW3 = kMlOffB2 + kMlW, kMlOffB3 = kMlOffW3 + kMlW * kMlW,
               kMlOffW4 = kMlOffB3 + kMlW, kMlOffB4 = kMlOffW4 + kMlW, kMlParams = kMlOffB4 + 1;

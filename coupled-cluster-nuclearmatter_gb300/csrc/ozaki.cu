@@ -237,15 +237,17 @@ __global__ void __launch_bounds__(kOzThreads, 1) k_oz_gemm(const OzProb *__restr
           long long zh[8], zl[8];
 #pragma unroll
           for (int q = 0; q < 8; ++q) zh[q] = zl[q] = 0;
+          // all levels of the 8 columns in flight at once, one wait
+          uint32_t r[kOzLevels][8];
+#pragma unroll
+          for (int lv = 0; lv < kOzLevels; ++lv) tmem_ld8(tbase + (uint32_t)(lv * kOzN + cb), r[lv]);
+          tmem_ld_wait();
 #pragma unroll
           for (int lv = 0; lv < kOzLevels; ++lv) {
-            uint32_t r[8];
-            tmem_ld8(tbase + (uint32_t)(lv * kOzN + cb), r);
-            tmem_ld_wait();
 #pragma unroll
             for (int q = 0; q < 8; ++q) {
               // an exact integer below 2^24 in magnitude
-              const long long x = (long long)__float2int_rz(__uint_as_float(r[q]));
+              const long long x = (long long)__float2int_rz(__uint_as_float(r[lv][q]));
               if (lv < 4) zh[q] += x * (1ll << (kOzBits * (3 - lv)));
               else zl[q] += x * (1ll << (kOzBits * (8 - lv)));
             }
