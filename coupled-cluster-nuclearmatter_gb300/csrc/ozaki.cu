@@ -9,9 +9,9 @@
 //     the tensor-memory accumulators of levels i + j, all j in one MMA over the stacked
 //     B digit tiles, and commits each stage back;
 //   warps 0-3 drain the kOzLevels accumulators after every K chunk (kOzChunkTiles K
-//     tiles, short enough for every level sum to stay an exact FP32 integer), combine
-//     them in two 64-bit integers, convert to FP64 once, scale by 2^(eA + eB) and add
-//     into C.
+//     tiles, short enough for every level sum to stay an exact FP32 integer) into two
+//     64-bit integer sums per row and column, and after the tile's last chunk convert
+//     them to FP64 once, scale by 2^(eA + eB) and add into C.
 // Every wait is bounded: on expiry the waiting thread records an error code and raises
 // a shared abort flag that ends every other wait at once; the producer lets its own
 // copies land before the CTA frees its tensor memory and exits.
@@ -28,7 +28,7 @@ namespace {
 
 using namespace tcptx;
 
-constexpr int kOzStages = 8;
+constexpr int kOzStages = 6;
 constexpr uint32_t kATile = 128u * 128u;                   // one A digit tile: 128 rows x 64 BF16
 constexpr uint32_t kBSlot = (uint32_t)kOzN * 128u;         // one B digit tile of kOzN rows
 constexpr uint32_t kBBuf = (uint32_t)kOzSlices * kBSlot;   // all B digits of one K tile
@@ -199,7 +199,7 @@ __global__ void __launch_bounds__(kOzThreads, 1) k_oz_gemm(const OzProb *__restr
       tc_commit(smem_u32(fin));
       mbar_wait(smem_u32(fin), 0);
     }
-  } else {  // warps 0-3: drain the level accumulators of every chunk into C
+  } else {  // warps 0-3: drain the level accumulators of every chunk, C once per tile
     const int row = warp * 32 + lane;
     const uint32_t tbase = tmem + ((uint32_t)(warp * 32) << 16);
     int ck = 0;
@@ -212,14 +212,18 @@ __global__ void __launch_bounds__(kOzThreads, 1) k_oz_gemm(const OzProb *__restr
       const int nchunk = (nk + kOzChunkTiles - 1) / kOzChunkTiles;
       const int m = tl.mt * 128 + row;
       const bool live = m < P.M;
-      const int eAm = live ? P.eA[m] : 0;
-      double *crow = P.C + (int64_t)(live ? m : 0) * P.sCm;
       // a warp none of whose rows is stored skips the drain
       const bool warp_live = tl.mt * 128 + warp * 32 < P.M;
-      for (int c = 0; c < nchunk; ++c, ++ck) {
-        double v[kOzN];  // this chunk's contribution to the row, scaled
+      // The tile's row sums so far as exact integers in units of 2^-30 (levels 0-3) and
+      // 2^-60 (levels 4-8, kept below 2^30 by carrying into the first): each chunk adds
+      // its level sums with integer operations only, so the accumulators are free for the
+      // next chunk's MMAs after a few integer operations per level and column, and the
+      // FP64 work (conversion, scaling, the read-modify-write of C) runs once per tile,
+      // beside the next tile's MMAs.
+      long long ah[kOzN], al[kOzN];
 #pragma unroll
-        for (int q = 0; q < kOzN; ++q) v[q] = 0.0;
+      for (int q = 0; q < kOzN; ++q) ah[q] = al[q] = 0;
+      for (int c = 0; c < nchunk; ++c, ++ck) {
         const bool got = __all_sync(0xffffffffu, wait(done, (uint32_t)(ck & 1)));
         if (!got) {
           if (lane == 0) atomicExch(err, 3);
@@ -227,53 +231,55 @@ __global__ void __launch_bounds__(kOzThreads, 1) k_oz_gemm(const OzProb *__restr
           break;
         }
         tc_fence_after();
-        // 8 columns at a time: two 64-bit level sums per column stay in registers
 #pragma unroll
-        for (int cb = 0; cb < kOzN; cb += 8) {
+        for (int cb = 0; cb < kOzN; cb += 4) {
           if (!warp_live || cb >= nc) break;
-          int eb[8];
+          // all levels of 4 columns in flight at once, one wait
+          uint32_t r[kOzLevels][4];
 #pragma unroll
-          for (int q = 0; q < 8; ++q) eb[q] = (tl.n0 + cb + q < P.N) ? P.eB[tl.n0 + cb + q] : 0;
-          long long zh[8], zl[8];
-#pragma unroll
-          for (int q = 0; q < 8; ++q) zh[q] = zl[q] = 0;
-          // all levels of the 8 columns in flight at once, one wait
-          uint32_t r[kOzLevels][8];
-#pragma unroll
-          for (int lv = 0; lv < kOzLevels; ++lv) tmem_ld8(tbase + (uint32_t)(lv * kOzN + cb), r[lv]);
+          for (int lv = 0; lv < kOzLevels; ++lv) tmem_ld4(tbase + (uint32_t)(lv * kOzN + cb), r[lv]);
           tmem_ld_wait();
 #pragma unroll
           for (int lv = 0; lv < kOzLevels; ++lv) {
 #pragma unroll
-            for (int q = 0; q < 8; ++q) {
+            for (int q = 0; q < 4; ++q) {
               // an exact integer below 2^24 in magnitude
               const long long x = (long long)__float2int_rz(__uint_as_float(r[lv][q]));
-              if (lv < 4) zh[q] += x * (1ll << (kOzBits * (3 - lv)));
-              else zl[q] += x * (1ll << (kOzBits * (8 - lv)));
+              if (lv < 4) ah[cb + q] += x * (1ll << (kOzBits * (3 - lv)));
+              else al[cb + q] += x * (1ll << (kOzBits * (8 - lv)));
             }
           }
-#pragma unroll
-          for (int q = 0; q < 8; ++q) {
-            const double z = fma((double)zh[q], 0x1p-30, (double)zl[q] * 0x1p-60);
-            v[cb + q] = P.alpha * (z * pow2(eAm + eb[q]));
-          }
         }
-        // the level accumulators are read: the next chunk's MMAs may start while this
-        // chunk's sums go to C (all loads of the row first, then the stores)
+        // the level accumulators are read: the next chunk's MMAs may start
         tc_fence_before();
         __syncwarp();
         if (lane == 0) mbar_arrive(smem_u32(drained));
-        if (live) {
-          double old[kOzN];
 #pragma unroll
-          for (int q = 0; q < kOzN; ++q) {
+        for (int q = 0; q < kOzN; ++q) {
+          const long long carry = al[q] >> 30;  // floor: al stays in [0, 2^30)
+          ah[q] += carry;
+          al[q] -= carry * (1ll << 30);
+        }
+      }
+      if (ok && live) {
+        const int eAm = P.eA[m];
+        double *crow = P.C + (int64_t)m * P.sCm;
+        // 8 columns at a time: their loads of C in flight together, then the stores
+#pragma unroll
+        for (int q0 = 0; q0 < kOzN; q0 += 8) {
+          double old[8];
+#pragma unroll
+          for (int q = q0; q < q0 + 8; ++q) {
             const int n = tl.n0 + q;
-            old[q] = (q < nc && n < P.N) ? crow[(int64_t)n * P.sCn] : 0.0;
+            old[q - q0] = (q < nc && n < P.N) ? crow[(int64_t)n * P.sCn] : 0.0;
           }
 #pragma unroll
-          for (int q = 0; q < kOzN; ++q) {
+          for (int q = q0; q < q0 + 8; ++q) {
             const int n = tl.n0 + q;
-            if (q < nc && n < P.N) crow[(int64_t)n * P.sCn] = old[q] + v[q];
+            if (q < nc && n < P.N) {
+              const double z = fma((double)ah[q], 0x1p-30, (double)al[q] * 0x1p-60);
+              crow[(int64_t)n * P.sCn] = old[q - q0] + P.alpha * (z * pow2(eAm + P.eB[n]));
+            }
           }
         }
       }
