@@ -289,11 +289,12 @@ class Engine final : public IEngine {
   void set_vblocks(int kind, int n, const int *chs, const double *const *vs) override {
     const bool staged = kind == 1 || kind == 3 || kind == 6;
     if (n > 0 && (staged || kind == 4)) {
-      // blocks in device-addressable host memory are read in place: no staging copies.
-      // A family larger than kDirectMaxBytes goes through the copy engines instead: SM
-      // loads spread over that much host memory reach only a fraction of the link rate.
+      // blocks in device-addressable host memory are read in place: no staging copies,
+      // and only the cache lines that hold unique pairs cross the link.  V_pppp' is read
+      // a column at a time; another family larger than kDirectMaxBytes goes through the
+      // copy engines instead (its tile transposes spread over too many host pages).
       std::vector<double *> dv(n);
-      bool direct = family_bytes(kind, n, chs) <= kDirectMaxBytes;
+      bool direct = kind == 6 || family_bytes(kind, n, chs) <= kDirectMaxBytes;
       for (int i = 0; i < n && direct; ++i) direct = (dv[i] = device_view(vs[i])) != nullptr;
       if (direct) {
         if (kind == 4) set_v4_direct(n, chs, dv.data());

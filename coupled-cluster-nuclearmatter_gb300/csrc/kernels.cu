@@ -1080,11 +1080,31 @@ __global__ void __launch_bounds__(256) k_pack_vblock_tr(DevLayout L, int kind, i
     if (rr < R && c < P) dst[base + (int64_t)rr * P + c] = tile[tx][ty + j];
   }
 }
+// Kind 6 from host memory, one source column at a time: a block reads the rows of packed
+// column c from the reference block's column col_map[c] (contiguous in host memory) and
+// writes them down the packed column (stride P; the blocks on neighbouring columns fill
+// the same destination lines in L2).  The blocks in flight read a few contiguous columns
+// each, so the host pages they touch at once stay few: reads spread over 32 columns per
+// block (the tile kernel above) reach a fraction of the link rate on a family of tens of
+// GB.
+template <typename S>
+__global__ void __launch_bounds__(512) k_pack_vpp_cols(DevLayout L, int ch, int n_rows, int P,
+                                                       const double *__restrict__ src, S *__restrict__ dst, int *flag) {
+  const int *row_map = L.pp_row + L.pp_off[ch];
+  const int *col_map = L.pp_row + L.pp_off[ch];
+  const int64_t base = L.vpp_off[ch];
+  for (int c = blockIdx.x; c < P; c += gridDim.x) {
+    const double *col = src + 2 * (int64_t)n_rows * col_map[c];
+    for (int r = threadIdx.x; r < P; r += blockDim.x) dst[base + (int64_t)r * P + c] = cvt_in<S>(col + 2 * row_map[r], flag);
+  }
+}
 template <typename S>
 void launch_pack_vblock_host(const DevLayout &L, int kind, int ch, int n_rows, int rows_packed, int cols_packed,
                              const double *src, S *dst, int *flag, cudaStream_t st) {
   if (rows_packed <= 0 || cols_packed <= 0) return;
-  if (kind == 3 || kind == 6) {
+  if (kind == 6) {
+    k_pack_vpp_cols<S><<<std::min(cols_packed, 304), 512, 0, st>>>(L, ch, n_rows, cols_packed, src, dst, flag);
+  } else if (kind == 3) {
     const dim3 grid((cols_packed + 31) / 32, (rows_packed + 31) / 32);
     k_pack_vblock_tr<S><<<grid, dim3(32, 8), 0, st>>>(L, kind, ch, n_rows, rows_packed, cols_packed, src, dst, flag);
   } else {
