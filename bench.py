@@ -581,9 +581,9 @@ def run_e2e(args, ccx, torch, L, e, local, real, solve):
             "path": "ccx_set_fock + ccx_set_vblocks (all HHPP/PPPP/HHHH/HPHP blocks, one call per family) + "
                     "ccx_setup_t_amplitudes + ccx_ccd_iter + ccx_get_t2_all",
             "host_buffers": "page-locked (ccx_host_alloc): blocks are read in place over NVLink-C2C by the "
-                            "packing kernels (only the cache lines of unique pairs), or, for a block family above "
-                            "16 GB, staged through the copy engines; the amplitudes are unpacked straight into "
-                            "the host buffer; h2d_bytes_per_step is the size of the host inputs"}
+                            "packing kernels (only the cache lines of unique pairs; V_pppp a reference column "
+                            "per CTA); the amplitudes are unpacked straight into the host buffer; "
+                            "h2d_bytes_per_step is the size of the host inputs"}
 
 
 TWIST_LATTICES = {
