@@ -610,9 +610,9 @@ def gauss_legendre_twists():
 def run_twists(args):
     """Twist-averaged E/A of one lattice at N twists (ccm_main.f90:163-279 solves them one
     after the other).  The headline form (mixed precision, digit-product re-bases) runs the
-    twists in lockstep batches (ccx_ccd_iter_batch) of as many twists as the device holds;
-    the per-twist sequential loop of the same form and the plain FP64 GPU solve are timed
-    beside it.  Every step covers the whole job: engines (layout on the host, interaction
+    twists in lockstep batches (ccx_ccd_iter_batch) of half as many twists as the device
+    holds, the next batch built while one solves; the per-twist sequential loop of the same
+    form and the plain FP64 GPU solve are timed beside it.  Every step covers the whole job: engines (layout on the host, interaction
     generated on the device, operand tiles and digit planes) are built per batch, so
     total_s includes that set-up; solve_s counts only the solves.  The plain FP64 form is
     timed on a seeded sample of the twists (plain_twists) and scaled to N."""
@@ -656,11 +656,17 @@ def run_twists(args):
     torch.cuda.synchronize()
     free = torch.cuda.mem_get_info()[0]
     wave = max(1, min(len(grid), int(0.9 * free / (per * 1.15))))
-    if args.twist_batch:
-        wave = min(wave, args.twist_batch)
 
-    def layouts(lo):
-        return list(workers.map(layout, [th for th, _ in grid[lo:lo + wave]]))
+    # two batches in flight: the next batch's engines are built (layouts on host threads,
+    # interaction generated and operands prepared on their own streams) while the current
+    # batch solves, so each batch takes half of what the device holds
+    batch = max(1, wave // 2)
+    if args.twist_batch:
+        batch = min(batch, args.twist_batch)
+
+    def build_batch(w0):
+        ths = [th for th, _ in grid[w0:w0 + batch]]
+        return list(workers.map(lambda th: build(th, prec, rb), ths))
 
     def batched_pass():
         """All twists, batch after batch; returns (total_s, solve_s, results)."""
@@ -668,17 +674,13 @@ def run_twists(args):
         solve_s = 0.0
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        nxt = ahead.submit(layouts, 0)
-        for w0 in range(0, len(grid), wave):
-            Ls = nxt.result()
-            if w0 + wave < len(grid):
-                nxt = ahead.submit(layouts, w0 + wave)
-            ths = [th for th, _ in grid[w0:w0 + wave]]
-            engines = list(workers.map(lambda a: engine(a[0], a[1], prec, rb), zip(Ls, ths)))
-            torch.cuda.synchronize()
+        nxt = ahead.submit(build_batch, 0)
+        for w0 in range(0, len(grid), batch):
+            engines = nxt.result()
+            if w0 + batch < len(grid):
+                nxt = ahead.submit(build_batch, w0 + batch)
             t1 = time.perf_counter()
             rs, _ = ccx.ccd_iter_batch(engines, **opts)
-            torch.cuda.synchronize()
             solve_s += time.perf_counter() - t1
             for k, (e, r) in enumerate(zip(engines, rs)):
                 res[w0 + k] = (e.e0(), r)
@@ -736,10 +738,11 @@ def run_twists(args):
             "vs_baseline": None, "dtype": "c128" if pot else "f64", "data": "synthetic",
             "config": {"workload": f"twist-averaged {lat['desc']}, {len(grid)} twists of the 4x4x4 "
                                    f"Gauss-Legendre grid on [-pi, pi]^3",
-                       "form": f"{args.precision} + {args.rebase} re-bases, lockstep batches of {wave} twists",
+                       "form": f"{args.precision} + {args.rebase} re-bases, lockstep batches of {batch} twists, "
+                               f"the next batch built while one solves",
                        "start": "MP2 (the learned start is not used: it costs an iteration here)",
                        "solver": f"Jacobi + DIIS(8) to ||R-DT||<{args.tol:g} (FP64 residual) per twist"},
-            "twists": len(grid), "twists_per_batch": wave, "device_GB_per_twist": per / 1e9,
+            "twists": len(grid), "twists_per_batch": batch, "device_GB_per_twist": per / 1e9,
             "total_s": value, "solve_s": statistics.median(sol),
             "sequential_same_form": {"total_s": seq_t, "solve_s": seq_s},
             "speedup_batched_vs_sequential_solve": seq_s / statistics.median(sol),

@@ -1224,16 +1224,23 @@ __global__ void k_gen_tblocks(DevLayout L, DevOrbits O, DevPotential P, const do
     Vhp[L.t_off[ch] + e] = gen_anti<S>(O, P, h.x, h.y, p.x, p.y, hhf ? hhf + hi : nullptr, ppf ? ppf + pi : nullptr);
   }
 }
+// V_pppp' is Hermitian, <cd|V|ab> = conj(<ab|V|cd>): the elements on and above the
+// diagonal are generated and mirrored, which halves the FP64 work of the largest block
+// family.  The elements below the diagonal are written by the thread of their mirror.
 template <typename S>
 __global__ void k_gen_vpp(DevLayout L, DevOrbits O, DevPotential P, const double *ppf, S *Vpp) {
   const int2 tl = L.vtile[blockIdx.x];
   const int ch = tl.x, Pc = L.P[ch];
   const int64_t n = (int64_t)Pc * Pc, end = min((int64_t)tl.y + kTileElems, n);
+  S *V = Vpp + L.vpp_off[ch];
   for (int64_t e = tl.y + threadIdx.x; e < end; e += blockDim.x) {
     const int r = (int)(e / Pc), c = (int)(e % Pc);
+    if (r > c) continue;
     const int ri = L.pp_off[ch] + r, ci = L.pp_off[ch] + c;
     const int2 x = L.pp_orb[ri], y = L.pp_orb[ci];
-    Vpp[L.vpp_off[ch] + e] = gen_anti<S>(O, P, x.x, x.y, y.x, y.y, ppf ? ppf + ri : nullptr, ppf ? ppf + ci : nullptr);
+    const S v = gen_anti<S>(O, P, x.x, x.y, y.x, y.y, ppf ? ppf + ri : nullptr, ppf ? ppf + ci : nullptr);
+    V[e] = v;
+    if (r != c) V[(int64_t)c * Pc + r] = conj_(v);
   }
 }
 template <typename S>

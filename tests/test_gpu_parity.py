@@ -410,3 +410,24 @@ def test_checkpoint_resumes_a_converged_solve(ccx, O, tmp_path):
     r1 = f.ccd_iter(mode=ccx.MODE_STANDARD, tol=1e-10)
     assert r1["converged"] and r1["iterations"] <= 1
     assert abs(r1["e_ccd"] - r0["e_ccd"]) < 1e-11 * abs(r0["e_ccd"])
+
+
+@pytest.mark.parametrize("cfg", [dict(nmax=2, A=28, rho=0.16, snm=True, pot=1, real=False, theta=(0.7, -0.4, 1.9)),
+                                 dict(nmax=2, A=14, rho=0.08, snm=False, pot=0, real=True, theta=(-0.9, 0.3, 2.2))],
+                         ids=["snm28_chiral_twisted", "pnm14_minnesota_twisted"])
+def test_generated_interaction_twisted_residual(ccx, O, cfg):
+    """The device generator (V_pppp' written on and above the diagonal and mirrored: the
+    interaction is Hermitian) against the oracle's interaction at a twist, through the
+    residual at the MP2 amplitudes, block by block."""
+    o, L, e = make(ccx, O, **cfg)
+    try:
+        tol = 1e-12 if cfg["real"] else 1e-11
+        assert abs(e.e0() - o.e0()) < tol * abs(o.e0())
+        o.mp2()
+        e.setup_t_amplitudes()
+        o.t2_intermediate()
+        e.t2_intermediate()
+        check_blocks(o, e, o.r2, e.t2_eqn, tol)
+    finally:
+        e.close()
+        o.close()
