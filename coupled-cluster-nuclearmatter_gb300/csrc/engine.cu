@@ -1815,46 +1815,51 @@ class Engine final : public IEngine {
     const size_t es = tc_kind_ == kTcBF16 ? 2 : 4;
     const int tk = tc_tile_k(tc_kind_);
     const int npad_all = (N + 15) / 16 * 16;
-    // ca / cb: operand components, cc: output component; C0 and overwrite apply in phase 0
-    auto one = [&](int ca, int cb, int cc, double al, int ph) {
+    // One problem per output component cc, summing the products of every op with operand
+    // components (ca, cb) listed in parts (neg: subtracted).  A complex product is
+    // Re = Ar Br - Ai Bi and Im = Ar Bi + Ai Br: both outputs in one launch, each C
+    // element read and written once.
+    struct Part { int ca, cb, neg; };
+    auto one = [&](int cc, std::initializer_list<Part> parts) {
       for (int n0 = 0; n0 < N; n0 += 256) {
         const int nb = std::min(256, N - n0);
         TcProb p{};
-        for (size_t q = 0; q < ops.size(); ++q) {
-          const TcOp &o = ops[q];
-          TcSeg g{};
-          g.Ahi = (char *)o.a->hi.p + (o.ao + ca * o.a->n) * es;
-          g.Alo = (char *)o.a->lo.p + (o.ao + ca * o.a->n) * es;
-          g.Bhi = (char *)o.b->hi.p + (o.bo + cb * o.b->n) * es + (size_t)n0 * 128;
-          g.Blo = (char *)o.b->lo.p + (o.bo + cb * o.b->n) * es + (size_t)n0 * 128;
-          g.nk = (o.K + tk - 1) / tk;
-          g.bstride = npad_all > 256 ? (int64_t)npad_all * 128 : 0;
-          if (q == 0) {
-            p.Ahi = g.Ahi; p.Alo = g.Alo; p.Bhi = g.Bhi; p.Blo = g.Blo; p.nk = g.nk; p.bstride = g.bstride;
-          } else {
-            p.ext[q - 1] = g;
+        int q = 0;
+        for (const Part &pt : parts)
+          for (const TcOp &o : ops) {
+            TcSeg g{};
+            g.Ahi = (char *)o.a->hi.p + (o.ao + pt.ca * o.a->n) * es;
+            g.Alo = (char *)o.a->lo.p + (o.ao + pt.ca * o.a->n) * es;
+            g.Bhi = (char *)o.b->hi.p + (o.bo + pt.cb * o.b->n) * es + (size_t)n0 * 128;
+            g.Blo = (char *)o.b->lo.p + (o.bo + pt.cb * o.b->n) * es + (size_t)n0 * 128;
+            g.nk = (o.K + tk - 1) / tk;
+            g.bstride = npad_all > 256 ? (int64_t)npad_all * 128 : 0;
+            g.neg = pt.neg;
+            if (q == 0) {
+              if (g.neg) throw EngineError(2, "the first product of a tensor-core problem cannot be subtracted");
+              p.Ahi = g.Ahi; p.Alo = g.Alo; p.Bhi = g.Bhi; p.Blo = g.Blo; p.nk = g.nk; p.bstride = g.bstride;
+            } else {
+              if (q >= kTcMaxSegs) throw EngineError(2, "too many products for one tensor-core problem");
+              p.ext[q - 1] = g;
+            }
+            ++q;
           }
-        }
-        p.next = (int)ops.size() - 1;
+        p.next = q - 1;
         p.M = M; p.N = nb; p.npad = (nb + 15) / 16 * 16;
         const int64_t coff = cc + (int64_t)n0 * sCn * kNComp;
-        p.C = (double *)C + coff; p.sCm = sCm * kNComp; p.sCn = sCn * kNComp; p.alpha = al;
-        if (ph == 0) {
-          p.C0 = C0 ? (const double *)C0 + coff : nullptr;
-          p.overwrite = overwrite;
-        }
+        p.C = (double *)C + coff; p.sCm = sCm * kNComp; p.sCn = sCn * kNComp; p.alpha = alpha;
+        p.C0 = C0 ? (const double *)C0 + coff : nullptr;
+        p.overwrite = overwrite;
         for (int mt = 0; mt < (M + 127) / 128; ++mt) l.tiles.push_back(TcTile{(int)l.probs.size(), mt});
         l.probs.push_back(p);
-        l.phase.push_back(ph);
+        l.phase.push_back(0);
       }
     };
     if (kNComp == 1) {
-      one(0, 0, 0, alpha, 0);
+      one(0, {{0, 0, 0}});
     } else {
-      one(0, 0, 0, alpha, 0);
-      one(0, 1, 1, alpha, 0);
-      one(1, 1, 0, -alpha, 1);
-      one(1, 0, 1, alpha, 1);
+      one(0, {{0, 0, 0}, {1, 1, 1}});
+      one(1, {{0, 1, 0}, {1, 0, 0}});
     }
   }
 

@@ -3,7 +3,8 @@
 // C(fp64) += alpha * (A_hi B_hi + A_hi B_lo + A_lo B_hi), with the hi/lo pairs of BF16
 // (kind::f16) or TF32 (kind::tf32) operands, FP32 accumulation in tensor memory.
 // Persistent: one CTA per SM walks the tile list (a tile = 128 rows of one problem, all N
-// <= 256 columns); a tile may sum up to three products with the same M, N (segments).
+// <= 256 columns); a tile may sum up to six products with the same M, N (segments), each
+// added or subtracted.
 // Lane 0 of warp 8 streams the pre-tiled K tiles of A and B into a ring of shared-memory
 // stages with cp.async.bulk (one contiguous copy per operand tile, completion on an
 // mbarrier); the ring runs on across tiles.  Lane 0 of warp 9 issues the MMAs into one
@@ -53,7 +54,7 @@ __device__ __forceinline__ double f32_bits_to_f64(uint32_t u) {
 
 // K tiles of segment e of a problem (e = 0: the problem's own operands)
 __device__ __forceinline__ TcSeg tc_segment(const TcProb *__restrict__ pp, int e) {
-  if (e == 0) return TcSeg{pp->Ahi, pp->Alo, pp->Bhi, pp->Blo, pp->nk, pp->bstride};
+  if (e == 0) return TcSeg{pp->Ahi, pp->Alo, pp->Bhi, pp->Blo, pp->nk, pp->bstride, 0};
   return pp->ext[e - 1];
 }
 
@@ -65,7 +66,7 @@ struct TcGeom {
 __device__ __forceinline__ TcGeom tc_geom(const TcProb *__restrict__ pp, int npad_max) {
   TcGeom g;
   g.npad = pp->npad;
-  g.nseg = 1 + min(max(pp->next, 0), 2);
+  g.nseg = 1 + min(max(pp->next, 0), kTcMaxSegs - 1);
   int nk = 0;
   for (int e = 0; e < g.nseg; ++e) nk += tc_segment(pp, e).nk;
   g.ok = g.npad >= 16 && g.npad <= 256 && (g.npad & 15) == 0 && g.npad <= npad_max && nk >= 1;
@@ -204,6 +205,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_gemm(const TcProb *__restr
         for (int e = 0; e < G.nseg && ok; ++e) {
           const TcSeg g = tc_segment(pp, e);
           const bool two_a = g.Alo != nullptr;
+          // instruction-descriptor bit 14 negates B: a subtracted product
+          const uint32_t id = idesc | (g.neg ? (1u << 14) : 0u);
           const uint32_t acc = tmem + (uint32_t)(b * kTcHalfCols + min(e, G.nacc - 1) * G.ncols);
           bool first = e < G.nacc;  // this segment opens its accumulator
           for (int kl = 0; kl < g.nk; ++kl, ++cnt) {
@@ -220,10 +223,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_gemm(const TcProb *__restr
 #pragma unroll
             for (int ks = 0; ks < 4; ++ks) {
               const uint32_t o = (uint32_t)ks * 256u;
-              tc_mma<KIND>(acc, smem_desc(sa + o), smem_desc(sb + o), idesc, first ? 0u : 1u);
+              tc_mma<KIND>(acc, smem_desc(sa + o), smem_desc(sb + o), id, first ? 0u : 1u);
               first = false;
-              tc_mma<KIND>(acc, smem_desc(sa + o), smem_desc(sbl + o), idesc, 1u);
-              if (two_a) tc_mma<KIND>(acc, smem_desc(sal + o), smem_desc(sb + o), idesc, 1u);
+              tc_mma<KIND>(acc, smem_desc(sa + o), smem_desc(sbl + o), id, 1u);
+              if (two_a) tc_mma<KIND>(acc, smem_desc(sal + o), smem_desc(sb + o), id, 1u);
             }
             tc_commit(smem_u32(&empty[s]));
           }

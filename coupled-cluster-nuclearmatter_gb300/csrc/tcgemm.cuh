@@ -19,12 +19,14 @@ namespace ccx {
 enum TcKind { kTcBF16 = 0, kTcTF32 = 1 };
 
 // A further product accumulated into the same output tile (same M, N): its own operands
-// and K-tile count.
+// and K-tile count, optionally subtracted (the MMAs negate B).
 struct TcSeg {
   const void *Ahi, *Alo, *Bhi, *Blo;
   int nk;
   int64_t bstride;  // as TcProb::bstride
+  int neg;          // 1: the product is subtracted
 };
+constexpr int kTcMaxSegs = 6;  // products per output tile (the problem's own and ext)
 
 struct TcProb {
   const void *Ahi, *Alo;  // pre-tiled A (this problem), nullptr Alo: A taken as hi only
@@ -36,7 +38,7 @@ struct TcProb {
   int64_t bstride;        // bytes between B K tiles (0: npad * 128, the whole B operand); a
                           // column block of a wider B points Bhi/Blo at its first row and
                           // steps by the full operand's K-tile size
-  TcSeg ext[2];           // further products into the same accumulator (next of them)
+  TcSeg ext[kTcMaxSegs - 1];  // further products into the same accumulator (next of them)
   int next;
   const double *C0;       // optional term added once, at C's strides
   int overwrite;          // 1: C = C0 + alpha acc; 0: C += C0 + alpha acc
