@@ -327,7 +327,7 @@ int ccx_pert_triples(ccx_engine *e, double et[2]);
 /* Arithmetic of the 18 gather-contractions W(abc, ijk) of ccx_pert_triples:
  * CCX_TRIPLES_FP32 (the default) runs them in FP32 on FP32 copies of T2, V_hppp and
  * V_hhhp; CCX_TRIPLES_FP64 in FP64.  The sum of |W|^2 / D is FP64 in both.  On the
- * benchmark lattices the FP32 form moves E(T) by about 1e-7 relative (the north-star
+ * benchmark lattices the FP32 form moves E(T) by about 1e-7 relative (the accuracy
  * bar is 1e-5).  No counterpart in the reference (all FP64). */
 #define CCX_TRIPLES_FP64 0
 #define CCX_TRIPLES_FP32 1

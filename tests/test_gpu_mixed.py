@@ -2,7 +2,7 @@
 correction) against the FP64 solve of the same engine and the oracle.
 
 Only an FP64 residual can end a mixed solve, so at the same tolerance the converged
-E/A agrees with the FP64 one to rounding; the spec bar is 1 keV/nucleon."""
+E/A agrees with the FP64 one to rounding; the accuracy bar is 1 keV/nucleon."""
 import pytest
 
 pytestmark = pytest.mark.gpu

@@ -3,7 +3,7 @@
 Tolerances: FP64 path vs FP64 oracle.  The engine sums in a different order (packed
 a<b, i<j blocks, tiled GEMMs), so element-wise agreement is to ~1e-12 relative to the
 block's scale and energies to ~1e-10 relative.  The one exception is the reference's
-own DIIS step (see test_reference_iteration_step_by_step).  The spec bar (1e-6
+own DIIS step (see test_reference_iteration_step_by_step).  The accuracy bar (1e-6
 relative in E/A, 1e-5 in E(T)) is far looser.
 """
 import numpy as np
@@ -83,7 +83,7 @@ def test_reference_iteration_step_by_step(ccx, O):
     solves a bordered system of unconjugated dot products of consecutive differences
     (ccm_diis.f90:134-173) whose condition number is ~1e15 here, so a different
     summation order alone moves the extrapolated energy by ~1e-7 relative; after the
-    first DIIS step the trajectories are compared at the spec bar (1e-6)."""
+    first DIIS step the trajectories are compared at the accuracy bar (1e-6)."""
     o, L, e = make(ccx, O, **PNM14)
     o.mp2()
     e.setup_t_amplitudes()
@@ -121,7 +121,7 @@ def test_ccd_iter_standard_mode_converges_to_1e10(ccx, O):
     re_ = e.ccd_iter(mode=ccx.MODE_STANDARD, tol=1e-10)
     assert re_["converged"] and re_["res_norm"] < 1e-10
     assert abs(re_["e_ccd"] - ro["e_ccd"]) < 1e-11 * abs(ro["e_ccd"])
-    # E/A within 1e-6 relative of the oracle (the spec bar), here ~1e-12
+    # E/A within 1e-6 relative of the oracle (the accuracy bar), here ~1e-12
     ea_o = (o.e0() + ro["e_ccd"]).real / 14
     ea_e = (e.e0() + re_["e_ccd"]).real / 14
     assert abs(ea_e - ea_o) < 1e-6 * abs(ea_o)

@@ -13,7 +13,7 @@ sizes the benchmark measures:
   interaction, on the amplitudes the engine converged, handed to the oracle.
 
 Tolerances: residual blocks to 1e-12 (real) or 1e-11 (complex) of the largest block
-entry; energies far inside the spec bars (1e-6 relative in E/A, 1e-5 in E(T)).
+entry; energies far inside the accuracy bars (1e-6 relative in E/A, 1e-5 in E(T)).
 The oracle runs these on all host cores; each lattice takes seconds to a minute.
 """
 import numpy as np
@@ -68,7 +68,7 @@ def test_pnm66_residual_at_mp2(pnm66):
 
 def test_pnm66_converged_mixed_energy_matches_oracle(ccx, O, pnm66):
     """E/A of the mixed form (the benchmark's headline solve) against the oracle's FP64
-    solve to ||R - D T|| < 1e-10: the bar is 1e-6 relative (the benchmark spec) and 1 keV; the
+    solve to ||R - D T|| < 1e-10: the bar is 1e-6 relative and 1 keV; the
     engine reaches about 1e-12 relative."""
     o, L, e = pnm66
     o.mp2()
@@ -105,7 +105,7 @@ def test_snm132_nmax3_chiral_residual(ccx, O, theta):
 def test_triples_snm76_chiral_matches_oracle(ccx, O):
     """(T) of the engine's converged amplitudes, recomputed by the oracle from the same
     amplitudes: FP64 contractions within 1e-9 relative, the default FP32 contractions
-    within the spec bar of 1e-5 (they land near 1e-7)."""
+    within the accuracy bar of 1e-5 (they land near 1e-7)."""
     o, L, e = _pair(ccx, O, nmax=2, A=76, rho=0.16, snm=True, pot=1, real=False)
     try:
         e.setup_t_amplitudes()
