@@ -30,6 +30,11 @@ struct TriplesDev {
   int ns, A, NP, nk0, nk1, nk2, tzmin, tzmax;
   const int *orbit_of;                 // (nx, ny, nz, spin, isospin) -> orbital or -1
   const int *nx, *ny, *nz, *tz;
+  // quantum numbers of each orbital one per byte, biased by kQBias: nx, ny, nz, tz.  A
+  // momentum sum q_i + q_j - q_a stays bytewise (no carries, no borrows).
+  const unsigned *qn;
+  unsigned qlo, qspan;                 // per byte: smallest allowed value, allowed span
+  int tzlo;                            // the isospin of the smallest allowed byte-3 value
   const int2 *hp5_slot, *pp5_slot;     // hppp blocks: (channel, row) / (channel, column)
   const int64_t *v5_off;
   const int *n5;                       // rows of each hppp block
@@ -42,6 +47,23 @@ struct TriplesDev {
   const int64_t *hhh_off, *ppp_off;
   const int3 *hhh, *ppp;
 };
+
+constexpr int kQBias = 64;
+
+// Bytewise q_i + q_j - q_a of packed quantum numbers: the momentum and isospin of the
+// orbital that closes a pair (each byte stays in 0 .. 255 for |n| <= 21 per axis).
+__device__ __forceinline__ unsigned qsum(unsigned qi, unsigned qj, unsigned qa) { return __vsub4(__vadd4(qi, qj), qa); }
+
+// Index into orbit_of of packed quantum numbers q with spin -1 (spin +1 is two entries
+// further on), or -1 when q lies outside the lattice or the isospin range.
+__device__ __forceinline__ int64_t t_orbit_base(const TriplesDev &D, unsigned q) {
+  const unsigned d = __vsub4(q, D.qlo);  // per byte: n + nk, and tz - tzlo
+  if (__vcmpgtu4(d, D.qspan)) return -1;
+  const int x = (int)(d & 0xffu), y = (int)((d >> 8) & 0xffu), z = (int)((d >> 16) & 0xffu);
+  const int t = (int)(d >> 24) + D.tzlo;
+  const int ey = 2 * D.nk1 + 1, ez = 2 * D.nk2 + 1;
+  return ((((int64_t)x * ey + y) * ez + z) * 2) * 2 + (t > 0);
+}
 
 __device__ inline int t_orbitof(const TriplesDev &D, int x, int y, int z, int s, int t) {
   if (x < -D.nk0 || x > D.nk0 || y < -D.nk1 || y > D.nk1 || z < -D.nk2 || z > D.nk2) return -1;
@@ -102,13 +124,12 @@ __device__ __forceinline__ double wnorm2(cplxf w) { return (double)w.re * (doubl
 template <typename W>
 __device__ __noinline__ W one_particle(const TriplesDev &D, const DevLayout &L, const W *T, const W *V5, int a, int b,
                                        int c, int i, int j, int k, unsigned m, W acc) {
-  const int nxd = D.nx[i] + D.nx[j] - D.nx[a], nyd = D.ny[i] + D.ny[j] - D.ny[a];
-  const int nzd = D.nz[i] + D.nz[j] - D.nz[a], tzd = D.tz[i] + D.tz[j] - D.tz[a];
-  if (abs(nxd) > D.nk0 || abs(nyd) > D.nk1 || abs(nzd) > D.nk2 || abs(tzd) > 1) return acc;
+  const int64_t ob = t_orbit_base(D, qsum(D.qn[i], D.qn[j], D.qn[a]));  // d = i + j - a
+  if (ob < 0) return acc;
   const int2 cl = D.pp5_slot[(int64_t)(c - D.A) * D.NP + (b - D.A)];
   if (cl.x < 0) return acc;
-  for (int sd = -1; sd <= 1; sd += 2) {
-    const int d = t_orbitof(D, nxd, nyd, nzd, sd, tzd);
+  for (int sd = 0; sd < 4; sd += 2) {
+    const int d = D.orbit_of[ob + sd];
     if (d < D.A) continue;
     const int2 r = D.hp5_slot[(int64_t)k * D.NP + (d - D.A)];
     if (r.x < 0) continue;
@@ -122,13 +143,12 @@ __device__ __noinline__ W one_particle(const TriplesDev &D, const DevLayout &L, 
 template <typename W>
 __device__ __noinline__ W one_hole(const TriplesDev &D, const DevLayout &L, const W *T, const W *V2, int a, int b,
                                    int c, int i, int j, int k, unsigned m, W acc) {
-  const int nxl = D.nx[k] + D.nx[j] - D.nx[c], nyl = D.ny[k] + D.ny[j] - D.ny[c];
-  const int nzl = D.nz[k] + D.nz[j] - D.nz[c], tzl = D.tz[k] + D.tz[j] - D.tz[c];
-  if (abs(nxl) > D.nk0 || abs(nyl) > D.nk1 || abs(nzl) > D.nk2 || abs(tzl) > 1) return acc;
+  const int64_t ob = t_orbit_base(D, qsum(D.qn[k], D.qn[j], D.qn[c]));  // l = k + j - c
+  if (ob < 0) return acc;
   const int2 r = D.hh2_slot[j * D.A + k];
   if (r.x < 0) return acc;
-  for (int sl = -1; sl <= 1; sl += 2) {
-    const int l = t_orbitof(D, nxl, nyl, nzl, sl, tzl);
+  for (int sl = 0; sl < 4; sl += 2) {
+    const int l = D.orbit_of[ob + sl];
     if (l < 0 || l >= D.A) continue;
     const int2 cl = D.hp2_slot[(int64_t)l * D.NP + (c - D.A)];
     if (cl.x < 0) continue;
@@ -296,6 +316,24 @@ class Triples final : public ITriples<S> {
     orbit_of_.put(B.orbit_of);
     TD_.orbit_of = orbit_of_.as<int>();
     TD_.nx = O.nx; TD_.ny = O.ny; TD_.nz = O.nz; TD_.tz = O.tz;
+    {
+      const int nkm = std::max(B.nkmax[0], std::max(B.nkmax[1], B.nkmax[2]));
+      if (nkm > 21) throw EngineError(1, "(T): momentum range too large for packed quantum numbers");
+      std::vector<unsigned> q(ns);
+      for (int p = 0; p < ns; ++p)
+        q[p] = (unsigned)(B.nx[p] + kQBias) | (unsigned)(B.ny[p] + kQBias) << 8 | (unsigned)(B.nz[p] + kQBias) << 16 |
+               (unsigned)(B.tz[p] + kQBias) << 24;
+      qn_.put(q);
+      TD_.qn = qn_.as<unsigned>();
+      // allowed: |n| <= nk per axis, and the closing orbital's isospin in [tzmin, tzmax]
+      // and in [-1, 1]
+      const int tzlo = std::max(-1, B.tzmin), tzhi = std::min(1, B.tzmax);
+      TD_.tzlo = tzlo;
+      TD_.qlo = (unsigned)(kQBias - B.nkmax[0]) | (unsigned)(kQBias - B.nkmax[1]) << 8 |
+                (unsigned)(kQBias - B.nkmax[2]) << 16 | (unsigned)(kQBias + tzlo) << 24;
+      TD_.qspan = (unsigned)(2 * B.nkmax[0]) | (unsigned)(2 * B.nkmax[1]) << 8 | (unsigned)(2 * B.nkmax[2]) << 16 |
+                  (unsigned)std::max(0, tzhi - tzlo) << 24;
+    }
     // hppp (kind 5) and hhhp (kind 2) blocks in the reference's ordered layout
     auto blocks = [&](int kind, std::vector<int2> &s1slot, std::vector<int2> &s2slot, bool s1_is_hh, DB &off, DB &nrow,
                       std::vector<int64_t> &offh, std::vector<int2> &rows, std::vector<int2> &cols, std::vector<int> &nr,
@@ -547,7 +585,7 @@ class Triples final : public ITriples<S> {
   DevLayout D_;
   DevOrbits O_;
   TriplesDev TD_{};
-  DB orbit_of_, hp5_slot_, pp5_slot_, hh2_slot_, hp2_slot_, v5_off_, n5_, v2_off_, n2_;
+  DB orbit_of_, qn_, hp5_slot_, pp5_slot_, hh2_slot_, hp2_slot_, v5_off_, n5_, v2_off_, n2_;
   DB rows5_, cols5_, rows2_, cols2_, nc5_, ro5_, co5_, nc2_, ro2_, co2_;
   DB V5l_, V2l_, Tl_;  // FP32 copies for the FP32 contractions
   bool low_ready_ = false;
