@@ -65,14 +65,6 @@ __device__ __forceinline__ int64_t t_orbit_base(const TriplesDev &D, unsigned q)
   return ((((int64_t)x * ey + y) * ez + z) * 2) * 2 + (t > 0);
 }
 
-__device__ inline int t_orbitof(const TriplesDev &D, int x, int y, int z, int s, int t) {
-  if (x < -D.nk0 || x > D.nk0 || y < -D.nk1 || y > D.nk1 || z < -D.nk2 || z > D.nk2) return -1;
-  if (t < D.tzmin || t > D.tzmax) return -1;
-  const int ey = 2 * D.nk1 + 1, ez = 2 * D.nk2 + 1;
-  const size_t idx = ((((size_t)(x + D.nk0) * ey + (y + D.nk1)) * ez + (z + D.nk2)) * 2 + (s > 0)) * 2 + (t > 0);
-  return D.orbit_of[idx];
-}
-
 // The 18 gather-contractions of a pair run in the contraction type W: the engine's
 // scalar S (FP64), or its FP32 counterpart (float, or cplxf for complex engines) on
 // FP32 copies of T, V_hppp and V_hhhp.  GB300's FP64 pipe retires 2 FMA per clock per SM
@@ -96,15 +88,12 @@ __device__ __forceinline__ float flip(float x, unsigned s) { return __int_as_flo
 __device__ __forceinline__ cplx flip(cplx x, unsigned s) { return cplx(flip(x.re, s), flip(x.im, s)); }
 __device__ __forceinline__ cplxf flip(cplxf x, unsigned s) { return cplxf{flip(x.re, s), flip(x.im, s)}; }
 
-// T(ab, ij) with the antisymmetry signs of both pair slots, and the extra sign m
+// T(ab, ij) from the two pair slots, with the extra sign m
 template <typename W>
-__device__ inline W t2_at(const DevLayout &L, const W *T, int a, int b, int i, int j, unsigned m) {
-  const int2 sab = L.pp_slot[(int64_t)(a - L.A) * L.NP + (b - L.A)];
-  const int2 sij = L.hh_slot[i * L.A + j];
+__device__ __forceinline__ W t2_slots(const DevLayout &L, const W *T, int2 sab, int2 sij, unsigned m) {
   if (sab.y == 0 || sij.y == 0) return wzero<W>();
-  const int ch = sab.x;
   if ((sab.y < 0) != (sij.y < 0)) m ^= 1u;
-  return flip(T[L.t_off[ch] + sidx(sab.y) + (int64_t)L.P[ch] * sidx(sij.y)], m);
+  return flip(T[L.t_off[sab.x] + sidx(sab.y) + (int64_t)L.P[sab.x] * sidx(sij.y)], m);
 }
 __device__ __forceinline__ double madd_conj(double v, double t, double acc) { return fma(v, t, acc); }
 __device__ __forceinline__ cplx madd_conj(cplx v, cplx t, cplx acc) { return acc + conj_(v) * t; }
@@ -118,42 +107,51 @@ __device__ __forceinline__ double wnorm2(float w) { return (double)w * (double)w
 __device__ __forceinline__ double wnorm2(cplx w) { return w.re * w.re + w.im * w.im; }
 __device__ __forceinline__ double wnorm2(cplxf w) { return (double)w.re * (double)w.re + (double)w.im * (double)w.im; }
 
-// acc + sign * sum_d conj(<cb|V|kd>) T(ad, ij), the sign as a bit.  Not inlined: the 18
-// calls of a pair would otherwise unroll into a body larger than the instruction cache,
-// and the warps stall on fetches.
+// acc + sign * sum_d conj(<cb|V|kd>) T(ad, ij), the sign as a bit
 template <typename W>
-__device__ __noinline__ W one_particle(const TriplesDev &D, const DevLayout &L, const W *T, const W *V5, int a, int b,
+__device__ __forceinline__ W one_particle(const TriplesDev &D, const DevLayout &L, const W *T, const W *V5, int a, int b,
                                        int c, int i, int j, int k, unsigned m, W acc) {
   const int64_t ob = t_orbit_base(D, qsum(D.qn[i], D.qn[j], D.qn[a]));  // d = i + j - a
   if (ob < 0) return acc;
   const int2 cl = D.pp5_slot[(int64_t)(c - D.A) * D.NP + (b - D.A)];
   if (cl.x < 0) return acc;
+  const int2 sij = L.hh_slot[i * L.A + j];  // the same for both spins of d
+  if (sij.y == 0) return acc;
   for (int sd = 0; sd < 4; sd += 2) {
     const int d = D.orbit_of[ob + sd];
     if (d < D.A) continue;
     const int2 r = D.hp5_slot[(int64_t)k * D.NP + (d - D.A)];
     if (r.x < 0) continue;
-    const W t = t2_at<W>(L, T, a, d, i, j, m);
+    const W t = t2_slots<W>(L, T, L.pp_slot[(int64_t)(a - L.A) * L.NP + (d - L.A)], sij, m);
     acc = madd_conj(V5[D.v5_off[r.x] + r.y + (int64_t)D.n5[r.x] * cl.y], t, acc);
   }
   return acc;
 }
 
-// acc + sign * sum_l conj(<jk|V|lc>) T(ab, il) (not inlined, as one_particle)
+// acc + sign * sum_l conj(<jk|V|lc>) T(ab, il)
 template <typename W>
-__device__ __noinline__ W one_hole(const TriplesDev &D, const DevLayout &L, const W *T, const W *V2, int a, int b,
+__device__ __forceinline__ W one_hole(const TriplesDev &D, const DevLayout &L, const W *T, const W *V2, int a, int b,
                                    int c, int i, int j, int k, unsigned m, W acc) {
   const int64_t ob = t_orbit_base(D, qsum(D.qn[k], D.qn[j], D.qn[c]));  // l = k + j - c
   if (ob < 0) return acc;
   const int2 r = D.hh2_slot[j * D.A + k];
   if (r.x < 0) return acc;
+  // the same for both spins of l: the particle pair, its T column base and the V row
+  const int2 sab = L.pp_slot[(int64_t)(a - L.A) * L.NP + (b - L.A)];
+  if (sab.y == 0) return acc;
+  const W *Tc = T + L.t_off[sab.x] + sidx(sab.y);
+  const int64_t Pc = L.P[sab.x];
+  const W *Vr = V2 + D.v2_off[r.x] + r.y;
+  const int64_t nr = D.n2[r.x];
   for (int sl = 0; sl < 4; sl += 2) {
     const int l = D.orbit_of[ob + sl];
     if (l < 0 || l >= D.A) continue;
     const int2 cl = D.hp2_slot[(int64_t)l * D.NP + (c - D.A)];
     if (cl.x < 0) continue;
-    const W t = t2_at<W>(L, T, a, b, i, l, m);
-    acc = madd_conj(V2[D.v2_off[r.x] + r.y + (int64_t)D.n2[r.x] * cl.y], t, acc);
+    const int2 sil = L.hh_slot[i * L.A + l];
+    if (sil.y == 0) continue;
+    const W t = flip(Tc[Pc * sidx(sil.y)], m ^ (unsigned)((sab.y < 0) != (sil.y < 0)));
+    acc = madd_conj(Vr[nr * cl.y], t, acc);
   }
   return acc;
 }
@@ -193,6 +191,10 @@ __global__ void k_triple_fock(const int3 *__restrict__ t, int64_t n, const S *__
   }
 }
 
+// (permutation of the particles, permutation of the holes) of the nine terms of each
+// kind, 2 + 2 bits per term: (0,0) (1,0) (2,0) (0,1) (0,2) (2,2) (2,1) (1,2) (1,1)
+constexpr unsigned long long kTermOrder = 0x596A84210ull;
+
 template <typename S, typename W>
 __global__ void __launch_bounds__(256) k_triples(TriplesDev D, DevLayout L, const W *__restrict__ T,
                                                  const W *__restrict__ V5, const W *__restrict__ V2,
@@ -210,27 +212,27 @@ __global__ void __launch_bounds__(256) k_triples(TriplesDev D, DevLayout L, cons
     const int a = abc.x, b = abc.y, c = abc.z, i = ijk.x, j = ijk.y, k = ijk.z;
     const S spen = eh[D.hhh_off[ch] + bra] - ep[D.ppp_off[ch] + ket];
     // W = the 9 particle terms minus the 9 hole terms, accumulated in one sum with the
-    // permutation signs applied as sign-bit flips
-    constexpr unsigned P = 0, N = 1;
+    // permutation signs applied as sign-bit flips.  Each term is one permutation of
+    // (a, b, c) and one of (i, j, k), taken in pert_triples2's order (kTermOrder: 2 bits
+    // each); the orbitals of a term are picked by selects, so one copy of each term body
+    // serves all nine (eighteen inlined bodies outgrow the instruction cache).
     W tc = wzero<W>();
-    tc = one_particle<W>(D, L, T, V5, a, b, c, i, j, k, P, tc);
-    tc = one_particle<W>(D, L, T, V5, b, a, c, i, j, k, N, tc);
-    tc = one_particle<W>(D, L, T, V5, c, b, a, i, j, k, N, tc);
-    tc = one_particle<W>(D, L, T, V5, a, b, c, k, j, i, N, tc);
-    tc = one_particle<W>(D, L, T, V5, a, b, c, i, k, j, N, tc);
-    tc = one_particle<W>(D, L, T, V5, c, b, a, i, k, j, P, tc);
-    tc = one_particle<W>(D, L, T, V5, c, b, a, k, j, i, P, tc);
-    tc = one_particle<W>(D, L, T, V5, b, a, c, i, k, j, P, tc);
-    tc = one_particle<W>(D, L, T, V5, b, a, c, k, j, i, P, tc);
-    tc = one_hole<W>(D, L, T, V2, a, b, c, i, j, k, N, tc);
-    tc = one_hole<W>(D, L, T, V2, a, c, b, i, j, k, P, tc);
-    tc = one_hole<W>(D, L, T, V2, c, b, a, i, j, k, P, tc);
-    tc = one_hole<W>(D, L, T, V2, a, b, c, k, j, i, P, tc);
-    tc = one_hole<W>(D, L, T, V2, a, b, c, j, i, k, P, tc);
-    tc = one_hole<W>(D, L, T, V2, c, b, a, j, i, k, N, tc);
-    tc = one_hole<W>(D, L, T, V2, c, b, a, k, j, i, N, tc);
-    tc = one_hole<W>(D, L, T, V2, a, c, b, j, i, k, N, tc);
-    tc = one_hole<W>(D, L, T, V2, a, c, b, k, j, i, N, tc);
+#pragma unroll 1
+    for (int t = 0; t < 9; ++t) {
+      const int pp = (int)(kTermOrder >> (4 * t)) & 3, hp = (int)(kTermOrder >> (4 * t + 2)) & 3;
+      // particle term: (a, b, c) as is, (b, a, c) or (c, b, a); (i, j, k) as is, (k, j, i) or (i, k, j)
+      const int A1 = pp == 1 ? b : pp == 2 ? c : a, B1 = pp == 1 ? a : b, C1 = pp == 2 ? a : c;
+      const int I1 = hp == 1 ? k : i, J1 = hp == 2 ? k : j, K1 = hp == 1 ? i : hp == 2 ? j : k;
+      tc = one_particle<W>(D, L, T, V5, A1, B1, C1, I1, J1, K1, (unsigned)((pp != 0) != (hp != 0)), tc);
+    }
+#pragma unroll 1
+    for (int t = 0; t < 9; ++t) {
+      const int pp = (int)(kTermOrder >> (4 * t)) & 3, hp = (int)(kTermOrder >> (4 * t + 2)) & 3;
+      // hole term: (a, b, c) as is, (a, c, b) or (c, b, a); (i, j, k) as is, (k, j, i) or (j, i, k)
+      const int A1 = pp == 2 ? c : a, B1 = pp == 1 ? c : b, C1 = pp == 1 ? b : pp == 2 ? a : c;
+      const int I1 = hp == 1 ? k : hp == 2 ? j : i, J1 = hp == 2 ? i : j, K1 = hp == 1 ? i : k;
+      tc = one_hole<W>(D, L, T, V2, A1, B1, C1, I1, J1, K1, (unsigned)((pp != 0) == (hp != 0)), tc);
+    }
     const S term = S(wnorm2(tc)) / spen;
     acc[0] += real_(term);
     acc[1] += imag_(term);
