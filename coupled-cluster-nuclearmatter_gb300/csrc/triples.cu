@@ -217,7 +217,7 @@ __global__ void __launch_bounds__(256) k_triples(TriplesDev D, DevLayout L, cons
     // each); the orbitals of a term are picked by selects, so one copy of each term body
     // serves all nine (eighteen inlined bodies outgrow the instruction cache).
     W tc = wzero<W>();
-#pragma unroll 1
+#pragma unroll 3
     for (int t = 0; t < 9; ++t) {
       const int pp = (int)(kTermOrder >> (4 * t)) & 3, hp = (int)(kTermOrder >> (4 * t + 2)) & 3;
       // particle term: (a, b, c) as is, (b, a, c) or (c, b, a); (i, j, k) as is, (k, j, i) or (i, k, j)
@@ -225,7 +225,7 @@ __global__ void __launch_bounds__(256) k_triples(TriplesDev D, DevLayout L, cons
       const int I1 = hp == 1 ? k : i, J1 = hp == 2 ? k : j, K1 = hp == 1 ? i : hp == 2 ? j : k;
       tc = one_particle<W>(D, L, T, V5, A1, B1, C1, I1, J1, K1, (unsigned)((pp != 0) != (hp != 0)), tc);
     }
-#pragma unroll 1
+#pragma unroll 3
     for (int t = 0; t < 9; ++t) {
       const int pp = (int)(kTermOrder >> (4 * t)) & 3, hp = (int)(kTermOrder >> (4 * t + 2)) & 3;
       // hole term: (a, b, c) as is, (a, c, b) or (c, b, a); (i, j, k) as is, (k, j, i) or (j, i, k)
