@@ -103,9 +103,7 @@ __device__ __forceinline__ cplxf madd_conj(cplxf v, cplxf t, cplxf acc) {
 }
 // |W|^2 in FP64 as the engine's scalar
 __device__ __forceinline__ double wnorm2(double w) { return w * w; }
-__device__ __forceinline__ double wnorm2(float w) { return (double)w * (double)w; }
 __device__ __forceinline__ double wnorm2(cplx w) { return w.re * w.re + w.im * w.im; }
-__device__ __forceinline__ double wnorm2(cplxf w) { return (double)w.re * (double)w.re + (double)w.im * (double)w.im; }
 
 // acc + sign * sum_d conj(<cb|V|kd>) T(ad, ij), the sign as a bit
 template <typename W>
@@ -154,6 +152,27 @@ __device__ __forceinline__ W one_hole(const TriplesDev &D, const DevLayout &L, c
     acc = madd_conj(Vr[nr * cl.y], t, acc);
   }
   return acc;
+}
+
+// acc += |W|^2 / D.  With FP64 contractions in FP64; with FP32 contractions the ratio is
+// formed in FP32 as well (its rounding, 6e-8 of the term, is far below the FP32
+// contractions' own) and only the sum is FP64: this GPU's FP64 pipe is 64 times
+// narrower, and a complex FP64 division per pair kept it a third busy.
+__device__ __forceinline__ void add_term(double w, double d, double (&acc)[2]) { acc[0] += wnorm2(w) / d; }
+__device__ __forceinline__ void add_term(cplx w, cplx d, double (&acc)[2]) {
+  const cplx t = cplx(wnorm2(w), 0.0) / d;
+  acc[0] += t.re;
+  acc[1] += t.im;
+}
+__device__ __forceinline__ void add_term(float w, double d, double (&acc)[2]) {
+  acc[0] += (double)((w * w) / (float)d);
+}
+__device__ __forceinline__ void add_term(cplxf w, cplx d, double (&acc)[2]) {
+  const float n = w.re * w.re + w.im * w.im;  // |W|^2
+  const float dr = (float)d.re, di = (float)d.im;
+  const float s = n / (dr * dr + di * di);     // |W|^2 / D = |W|^2 conj(D) / |D|^2
+  acc[0] += (double)(s * dr);
+  acc[1] += (double)(-s * di);
 }
 
 // FP32 copy of an FP64 array
@@ -233,9 +252,7 @@ __global__ void __launch_bounds__(256) k_triples(TriplesDev D, DevLayout L, cons
       const int I1 = hp == 1 ? k : hp == 2 ? j : i, J1 = hp == 2 ? i : j, K1 = hp == 1 ? i : k;
       tc = one_hole<W>(D, L, T, V2, A1, B1, C1, I1, J1, K1, (unsigned)((pp != 0) == (hp != 0)), tc);
     }
-    const S term = S(wnorm2(tc)) / spen;
-    acc[0] += real_(term);
-    acc[1] += imag_(term);
+    add_term(tc, spen, acc);
   }
   block_sum<2>(acc, partial);
 }
