@@ -308,6 +308,12 @@ def run_ours(args, wl):
     e.generate(potential=wl["potential"])
     e.setup_t_amplitudes()
     tuned_shapes, _ = e.autotune()  # FP64 GEMM tile shape per column-count bucket
+    tc_form = None
+    if prec:  # launch form of each tensor-core correction product
+        tc_merged, tc_ms = e.autotune_tc(prec)
+        tc_form = {name: {"form": "one launch" if mg else "one launch per column bucket",
+                          "ms_per_bucket_launches": t[0], "ms_one_launch": t[1]}
+                   for name, mg, t in zip(("pp_hh_ladders", "dI4_dX", "ring"), tc_merged, tc_ms)}
     stream = torch.cuda.ExternalStream(e.stream(), device=local)
     P, H, ring = packed_sizes(L, ccx)
     flops = flop_model(P, H, ring, real=real)
@@ -423,7 +429,7 @@ def run_ours(args, wl):
                        "precision": args.precision if prec else "fp64",
                        "defect_period": args.defect_period or "adaptive",
                        "rebase": args.rebase if prec else None,
-                       "gemm_tile_shapes_by_N_bucket": tuned_shapes,
+                       "gemm_tile_shapes_by_N_bucket": tuned_shapes, "tensor_core_launch_form": tc_form,
                        "l2": "inputs larger than L2 (V_pppp packed, %.2f GB, read every iteration)"
                              % (sum(p * p for p in P) * e_bytes / 1e9),
                        "replicas": world},
@@ -557,6 +563,8 @@ def run_e2e(args, ccx, torch, L, e, local, real, solve):
         for _ in range(max(1, args.warmup // 2)):
             step()
         eb.autotune()  # once per engine, as a host would after handing over the interaction
+        if PRECISIONS[args.precision]:
+            eb.autotune_tc(PRECISIONS[args.precision])
         step()
         torch.cuda.synchronize()
         for k in phase:

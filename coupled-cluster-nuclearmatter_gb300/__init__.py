@@ -147,6 +147,7 @@ def lib():
         "ccx_set_vblocks": ([vp, i32, i32, vp, vp], C.c_int),
         "ccx_ccd_iter_batch": ([vp, i32, vp, vp, C.POINTER(C.c_double)], C.c_int),
         "ccx_engine_autotune": ([vp, vp, vp], C.c_int),
+        "ccx_engine_autotune_tc": ([vp, C.c_int32, vp, vp], C.c_int),
         "ccx_learner_create": ([i32, C.c_uint64, C.POINTER(vp)], C.c_int),
         "ccx_learner_destroy": ([vp], C.c_int),
         "ccx_learner_add_solution": ([vp, vp], C.c_int),
@@ -640,6 +641,14 @@ class Engine:
         ms = np.zeros(8)
         _check(lib().ccx_engine_autotune(self._h, _ptr(s), _ptr(ms)))
         return s.tolist(), ms.reshape(4, 2).tolist()
+
+    def autotune_tc(self, precision: int = 1):
+        """Pick each tensor-core correction product's launch form (one launch, or one per
+        column bucket) by timing; returns (merged flags of pp, I4, ring; ms per form)."""
+        m = np.zeros(3, np.int32)
+        ms = np.zeros(6)
+        _check(lib().ccx_engine_autotune_tc(self._h, int(precision), _ptr(m), _ptr(ms)))
+        return m.tolist(), ms.reshape(3, 2).tolist()
 
     def kernel_timers(self) -> dict:
         """{slot: (total ms, timed brackets)} of individual launches in the last ccd_iter."""

@@ -384,6 +384,14 @@ int ccx_engine_autotune(ccx_engine *e, int32_t shapes[4], double ms[8]) {
     for (int k = 0; k < 4; ++k) shapes[k] = s[k];
   });
 }
+int ccx_engine_autotune_tc(ccx_engine *e, int32_t precision, int32_t merged[3], double ms[6]) {
+  if (!merged || !ms) return fail(CCX_EINVAL, "null argument");
+  ENGINE_CALL(e, {
+    int m[3];
+    e->E->autotune_tc(precision, m, ms);
+    for (int k = 0; k < 3; ++k) merged[k] = m[k];
+  });
+}
 int ccx_ccd_iter_batch(ccx_engine *const *engines, int32_t n, const ccx_iter_opts *opt, ccx_iter_result *res,
                        double *seconds) {
   if (!engines || !opt || !res || n < 1) return fail(CCX_EINVAL, "bad batch arguments");

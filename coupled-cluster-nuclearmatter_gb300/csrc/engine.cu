@@ -1199,6 +1199,46 @@ class Engine final : public IEngine {
     oz_ready_ = false;
   }
 
+  // Launch form of each BF16x3 / TF32x3 correction product (pp + hh ladders, dI4 + dX,
+  // ring): one launch per bucket of the column count, or one launch over all its tiles,
+  // whichever runs the engine's own tiles faster (best of 3 each).  The products write
+  // only what the next residual writes again first (R', dI4, dX, dR_ph).
+  void autotune_tc(int precision, int merged[3], double ms[6]) override {
+    require_ready();
+    if (precision != 1 && precision != 2) throw EngineError(1, "tensor-core autotune needs a mixed precision");
+    prepare_mixed(precision == 2 ? kTcTF32 : kTcBF16);
+    cudaEvent_t a, b;
+    CK(cudaEventCreate(&a));
+    CK(cudaEventCreate(&b));
+    TcPlan *plans[3] = {&tcPP_, &tcI4_, &tcR1_};
+    for (int p = 0; p < 3; ++p) {
+      double t[2];
+      for (int v = 0; v < 2; ++v) {
+        plans[p]->merged[0] = plans[p]->merged[1] = v;
+        float best = 1e30f;
+        for (int rep = 0; rep < 3; ++rep) {
+          CK(cudaEventRecord(a, st_));
+          run_tc(*plans[p]);
+          CK(cudaEventRecord(b, st_));
+          CK(cudaEventSynchronize(b));
+          float x = 0.f;
+          CK(cudaEventElapsedTime(&x, a, b));
+          best = std::min(best, x);
+        }
+        t[v] = best;
+        ms[2 * p + v] = best;
+      }
+      const int pick = t[1] <= t[0] ? 1 : 0;
+      plans[p]->merged[0] = plans[p]->merged[1] = pick;
+      tc_choice_[p] = pick;
+      merged[p] = pick;
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    check_flag("tensor-core autotune");
+    ++plan_epoch_;  // the replayed residual graphs are captured again with the chosen launches
+  }
+
   // ================================================================== iteration
   void mark(int i) {
     if (timing_) CK(cudaEventRecord(ev_[i], st_));
@@ -1638,10 +1678,17 @@ class Engine final : public IEngine {
   // Tiles bucketed by padded N, so that small problems run with small shared-memory
   // stages (and more CTAs per SM) instead of the largest problem's footprint.
   static constexpr int kTcBuckets = 4;
+  // One product's tensor-core tiles, listed twice: per bucket of the column count (one
+  // launch each, with as many shared-memory stages as the bucket's widest tile leaves)
+  // and all together (one launch, stages for the widest tile of all).  merged picks the
+  // launch form per phase: by default one launch while it still has three stages; the
+  // tensor-core autotuner times both.
   struct TcPlan {
     DBuf probs;
-    DBuf tiles[2][kTcBuckets];
+    DBuf tiles[2][kTcBuckets], tiles_m[2];
     int ntiles[2][kTcBuckets] = {}, npad_max[2][kTcBuckets] = {}, max_nk[2][kTcBuckets] = {};
+    int ntiles_m[2] = {0, 0}, npad_m[2] = {16, 16}, nk_m[2] = {1, 1};
+    int merged[2] = {0, 0};
   };
   struct SplitPlan {
     DBuf jobs, chunks;
@@ -1657,9 +1704,9 @@ class Engine final : public IEngine {
     std::vector<int> phase;
     std::vector<TcTile> tiles;
   };
-  void finalize_tc(TcPlan &pl, const TcList &l) {
+  void finalize_tc(TcPlan &pl, const TcList &l, int choice = -1) {
     upload(pl.probs, l.probs, &bytes_);
-    std::vector<TcTile> b[2][kTcBuckets];
+    std::vector<TcTile> b[2][kTcBuckets], m[2];
     for (int ph = 0; ph < 2; ++ph)
       for (int k = 0; k < kTcBuckets; ++k) { pl.npad_max[ph][k] = 16; pl.max_nk[ph][k] = 1; }
     for (const TcTile &t : l.tiles) {
@@ -1667,24 +1714,11 @@ class Engine final : public IEngine {
       const int ph = l.phase[t.prob];
       const int k = p.npad <= 32 ? 0 : p.npad <= 64 ? 1 : p.npad <= 128 ? 2 : 3;
       b[ph][k].push_back(t);
+      m[ph].push_back(t);
       int nk = p.nk;
       for (int e = 0; e < p.next; ++e) nk += p.ext[e].nk;
       pl.npad_max[ph][k] = std::max(pl.npad_max[ph][k], p.npad);
       pl.max_nk[ph][k] = std::max(pl.max_nk[ph][k], nk);
-    }
-    // One launch per phase when the widest bucket still leaves the kernel 3 shared-memory
-    // stages (A tiles dominate a stage): the persistent grid then has no tail per bucket.
-    for (int ph = 0; ph < 2; ++ph) {
-      int np = 16, nk = 1;
-      for (int k = 0; k < kTcBuckets; ++k)
-        if (!b[ph][k].empty()) { np = std::max(np, pl.npad_max[ph][k]); nk = std::max(nk, pl.max_nk[ph][k]); }
-      if (tc_stages(np) < 3) continue;
-      for (int k = 1; k < kTcBuckets; ++k) {
-        b[ph][0].insert(b[ph][0].end(), b[ph][k].begin(), b[ph][k].end());
-        b[ph][k].clear();
-      }
-      pl.npad_max[ph][0] = np;
-      pl.max_nk[ph][0] = nk;
     }
     // longest tiles first: the persistent CTAs take tiles in strides of the grid
     auto work = [&](const TcTile &t) {
@@ -1693,13 +1727,24 @@ class Engine final : public IEngine {
       for (int e = 0; e < p.next; ++e) nk += p.ext[e].nk;
       return nk;
     };
-    for (int ph = 0; ph < 2; ++ph)
+    auto by_work = [&](const TcTile &x, const TcTile &y) { return work(x) > work(y); };
+    for (int ph = 0; ph < 2; ++ph) {
+      int np = 16, nk = 1;
       for (int k = 0; k < kTcBuckets; ++k) {
-        std::stable_sort(b[ph][k].begin(), b[ph][k].end(),
-                         [&](const TcTile &x, const TcTile &y) { return work(x) > work(y); });
+        std::stable_sort(b[ph][k].begin(), b[ph][k].end(), by_work);
         upload(pl.tiles[ph][k], b[ph][k], &bytes_);
         pl.ntiles[ph][k] = (int)b[ph][k].size();
+        if (!b[ph][k].empty()) { np = std::max(np, pl.npad_max[ph][k]); nk = std::max(nk, pl.max_nk[ph][k]); }
       }
+      std::stable_sort(m[ph].begin(), m[ph].end(), by_work);
+      upload(pl.tiles_m[ph], m[ph], &bytes_);
+      pl.ntiles_m[ph] = (int)m[ph].size();
+      pl.npad_m[ph] = np;
+      pl.nk_m[ph] = nk;
+      // one launch when the widest bucket still leaves the kernel 3 shared-memory stages
+      // (A tiles dominate a stage): the persistent grid then has no tail per bucket
+      pl.merged[ph] = choice >= 0 ? choice : (tc_stages(np) >= 3 ? 1 : 0);
+    }
   }
   void finalize_split(SplitPlan &pl, const std::vector<TcSplitJob> &jobs) {
     upload(pl.jobs, jobs, &bytes_);
@@ -1708,13 +1753,21 @@ class Engine final : public IEngine {
     pl.nchunks = (int)ch.size();
   }
   void run_tc(const TcPlan &pl) {
-    for (int ph = 0; ph < 2; ++ph)
+    for (int ph = 0; ph < 2; ++ph) {
+      if (pl.merged[ph]) {
+        if (!pl.ntiles_m[ph]) continue;
+        launch_tc_gemm(tc_kind_, (const TcProb *)pl.probs.p, (const TcTile *)pl.tiles_m[ph].p, pl.ntiles_m[ph],
+                       pl.npad_m[ph], pl.nk_m[ph], tcerr_.as<int>(), st_);
+        ++launches_;
+        continue;
+      }
       for (int k = 0; k < kTcBuckets; ++k) {
         if (!pl.ntiles[ph][k]) continue;
         launch_tc_gemm(tc_kind_, (const TcProb *)pl.probs.p, (const TcTile *)pl.tiles[ph][k].p, pl.ntiles[ph][k],
                        pl.npad_max[ph][k], pl.max_nk[ph][k], tcerr_.as<int>(), st_);
         ++launches_;
       }
+    }
   }
   void run_split(const SplitPlan &pl, cudaStream_t s = nullptr) {
     if (!pl.nchunks) return;
@@ -2261,9 +2314,9 @@ class Engine final : public IEngine {
     }
     finalize_split(spIter2_, js_it2);
     finalize_split(spIter3_, js_it3);
-    finalize_tc(tcPP_, pp);
-    finalize_tc(tcI4_, p4);
-    finalize_tc(tcR1_, pr1);
+    finalize_tc(tcPP_, pp, tc_choice_[0]);
+    finalize_tc(tcI4_, p4, tc_choice_[1]);
+    finalize_tc(tcR1_, pr1, tc_choice_[2]);
     // FP64 plans of the re-base: PP_b = V_pppp' T, and R' += T I9
     {
       PlanBuilder bp, bh;
@@ -2512,6 +2565,7 @@ class Engine final : public IEngine {
   int64_t oz_v_version_ = -1;
   TileBuf tVpp_, tD_, tVph_, tDphB_, tTphbA_, tDphA_, tdI4B_, tI4B_, tDA_, tI9B_, tTbA_, tdI9B_, tVhT_;
   TcPlan tcPP_, tcI4_, tcR1_;
+  int tc_choice_[3] = {-1, -1, -1};  // launch form of each correction product picked by the autotuner
   SplitPlan spStatic_, spTphb_, spIter2_, spIter3_;
   DBuf phl_, tphmap_, mD_, mDA_, mDphB_, mDphA_;  // packed split of dT' (hi/lo pairs), gather maps
   SplitPlan gplan_;                                     // gather jobs (TcGatherJob) and chunks

@@ -108,6 +108,8 @@ class IEngine {
   virtual void set_profiling(bool on) = 0;
   // FP64 GEMM tile-shape autotuner: chosen shape per N bucket, ms[2 k + shape]
   virtual void autotune(int shapes[4], double ms[8]) = 0;
+  // launch form of each tensor-core correction product: 1 one launch, 0 one per bucket
+  virtual void autotune_tc(int precision, int merged[3], double ms[6]) = 0;
   // device view for the learned warm start (real engines only; false for complex)
   virtual bool ml_view(MLView &v, bool need_t) = 0;
   virtual void mark_t_set() = 0;

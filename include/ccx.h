@@ -319,6 +319,16 @@ int ccx_ccd_iter_batch(ccx_engine *const *engines, int32_t n, const ccx_iter_opt
  * time of shape s on bucket k (ms, best of 3).  Needs the interaction and amplitudes;
  * call it between solves. */
 int ccx_engine_autotune(ccx_engine *e, int32_t shapes[4], double ms[8]);
+/* Launch-form autotuner of the tensor-core correction products of the mixed residual
+ * (precision CCX_PREC_MIXED or CCX_PREC_MIXED_TF32): for the pp + hh ladders, dI4 + dX
+ * and the ring in turn, it times the engine's own tiles launched once per bucket of the
+ * column count (<= 32, <= 64, <= 128, wider; each launch with as many shared-memory
+ * stages as its widest tile leaves) and launched all together (stages for the widest
+ * tile of all), keeps the faster form and prepares the mixed residual with it.
+ * merged[p]: 1 for one launch, 0 for one per bucket; ms[2 p + f]: the time of form f
+ * (0 per bucket, 1 one launch; ms, best of 3).  Needs the interaction; call it between
+ * solves.  Without it, one launch is used while the widest tile leaves three stages. */
+int ccx_engine_autotune_tc(ccx_engine *e, int32_t precision, int32_t merged[3], double ms[6]);
 
 /* ---- (T) -------------------------------------------------------------- */
 /* pert_triples2, ccm_triples.f90:528-735 (NN part): E(T) from the current T2 with

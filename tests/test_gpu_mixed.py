@@ -146,3 +146,22 @@ def test_mixed_ring_channels_wider_than_256(ccx):
     assert rm["mixed_iterations"] == 1 and rm["fp64_sweeps"] == 1
     assert abs(rm["e_ccd"] - r64["e_ccd"]) < 1e-4 * abs(r64["e_ccd"])
     assert abs(rm["res_norm"] - r64["res_norm"]) < 1e-3 * r64["res_norm"]
+
+
+def test_tensor_core_launch_form_autotune(ccx):
+    """The autotuner times each correction product's two launch forms and keeps the
+    faster; the mixed solve after it reaches the same energy."""
+    L = ccx.Layout.from_basis(2, 28, 0.16, snm=True)
+    e = ccx.Engine(L, real=False)
+    e.generate(potential=ccx.POT_CHIRAL_LIKE)
+    e.setup_t_amplitudes()
+    r0 = e.ccd_iter(mode=ccx.MODE_STANDARD, precision=ccx.PREC_MIXED, rebase=ccx.REBASE_DIGITS, tol=1e-10,
+                    max_iter=200)
+    merged, ms = e.autotune_tc(ccx.PREC_MIXED)
+    assert all(m in (0, 1) for m in merged) and len(merged) == 3
+    assert all(t[0] > 0 and t[1] > 0 and (t[1] <= t[0]) == bool(m) for t, m in zip(ms, merged))
+    e.setup_t_amplitudes()
+    r1 = e.ccd_iter(mode=ccx.MODE_STANDARD, precision=ccx.PREC_MIXED, rebase=ccx.REBASE_DIGITS, tol=1e-10,
+                    max_iter=200)
+    assert r0["converged"] and r1["converged"]
+    assert abs(r1["e_ccd"] - r0["e_ccd"]) < 1e-12 * abs(r0["e_ccd"])
