@@ -1681,8 +1681,7 @@ class Engine final : public IEngine {
   // One product's tensor-core tiles, listed twice: per bucket of the column count (one
   // launch each, with as many shared-memory stages as the bucket's widest tile leaves)
   // and all together (one launch, stages for the widest tile of all).  merged picks the
-  // launch form per phase: by default one launch while it still has three stages; the
-  // tensor-core autotuner times both.
+  // launch form per phase: one launch by default; the tensor-core autotuner times both.
   struct TcPlan {
     DBuf probs;
     DBuf tiles[2][kTcBuckets], tiles_m[2];
@@ -1741,9 +1740,10 @@ class Engine final : public IEngine {
       pl.ntiles_m[ph] = (int)m[ph].size();
       pl.npad_m[ph] = np;
       pl.nk_m[ph] = nk;
-      // one launch when the widest bucket still leaves the kernel 3 shared-memory stages
-      // (A tiles dominate a stage): the persistent grid then has no tail per bucket
-      pl.merged[ph] = choice >= 0 ? choice : (tc_stages(np) >= 3 ? 1 : 0);
+      // one launch unless the autotuner found the bucket launches faster: the persistent
+      // grid then has no tail per bucket, and on every lattice measured it won even where
+      // the widest tile leaves the kernel only two shared-memory stages
+      pl.merged[ph] = choice >= 0 ? choice : 1;
     }
   }
   void finalize_split(SplitPlan &pl, const std::vector<TcSplitJob> &jobs) {

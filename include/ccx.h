@@ -327,7 +327,7 @@ int ccx_engine_autotune(ccx_engine *e, int32_t shapes[4], double ms[8]);
  * tile of all), keeps the faster form and prepares the mixed residual with it.
  * merged[p]: 1 for one launch, 0 for one per bucket; ms[2 p + f]: the time of form f
  * (0 per bucket, 1 one launch; ms, best of 3).  Needs the interaction; call it between
- * solves.  Without it, one launch is used while the widest tile leaves three stages. */
+ * solves.  Without it, one launch is used. */
 int ccx_engine_autotune_tc(ccx_engine *e, int32_t precision, int32_t merged[3], double ms[6]);
 
 /* ---- (T) -------------------------------------------------------------- */
