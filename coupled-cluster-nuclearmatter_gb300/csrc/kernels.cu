@@ -996,17 +996,11 @@ template <typename S>
 struct CoefPack {
   double re[kMaxDots], im[kMaxDots];
 };
-// y = sum_i c_i x_i; the m loads of an element are issued together, then summed in order
 template <typename S>
 __global__ void k_combine(int64_t n, PtrPack<S> xs, CoefPack<S> c, int m, S *y) {
   for (int64_t x = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; x < n; x += (int64_t)gridDim.x * blockDim.x) {
-    S v[kMaxDots];
-#pragma unroll
-    for (int i = 0; i < kMaxDots; ++i) v[i] = i < m ? xs.p[i][x] : S(0.0);
     S acc = S(0.0);
-#pragma unroll
-    for (int i = 0; i < kMaxDots; ++i)
-      if (i < m) acc += make_scalar<S>(c.re[i], c.im[i]) * v[i];
+    for (int i = 0; i < m; ++i) acc += make_scalar<S>(c.re[i], c.im[i]) * xs.p[i][x];
     y[x] = acc;
   }
 }
