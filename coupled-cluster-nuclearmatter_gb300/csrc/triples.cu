@@ -27,9 +27,8 @@ void tck(cudaError_t e, const char *what) {
 }
 
 struct TriplesDev {
-  int ns, A, NP, nk0, nk1, nk2, tzmin, tzmax;
+  int ns, A, NP, nk0, nk1, nk2;
   const int *orbit_of;                 // (nx, ny, nz, spin, isospin) -> orbital or -1
-  const int *nx, *ny, *nz, *tz;
   // quantum numbers of each orbital one per byte, biased by kQBias: nx, ny, nz, tz.  A
   // momentum sum q_i + q_j - q_a stays bytewise (no carries, no borrows).
   const unsigned *qn;
@@ -331,10 +330,8 @@ class Triples final : public ITriples<S> {
     const int ns = B.ns, A = B.A, NP = ns - A;
     TD_.ns = ns; TD_.A = A; TD_.NP = NP;
     TD_.nk0 = B.nkmax[0]; TD_.nk1 = B.nkmax[1]; TD_.nk2 = B.nkmax[2];
-    TD_.tzmin = B.tzmin; TD_.tzmax = B.tzmax;
     orbit_of_.put(B.orbit_of);
     TD_.orbit_of = orbit_of_.as<int>();
-    TD_.nx = O.nx; TD_.ny = O.ny; TD_.nz = O.nz; TD_.tz = O.tz;
     {
       const int nkm = std::max(B.nkmax[0], std::max(B.nkmax[1], B.nkmax[2]));
       if (nkm > 21) throw EngineError(1, "(T): momentum range too large for packed quantum numbers");
