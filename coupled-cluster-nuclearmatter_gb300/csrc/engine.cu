@@ -71,6 +71,32 @@ struct DBuf {
   template <typename T> T *as() const { return (T *)p; }
 };
 
+// Two timing events, destroyed on every path out of the scope that made them.
+struct EventPair {
+  cudaEvent_t a = nullptr, b = nullptr;
+  EventPair() {
+    CK(cudaEventCreate(&a));
+    CK(cudaEventCreate(&b));
+  }
+  EventPair(const EventPair &) = delete;
+  EventPair &operator=(const EventPair &) = delete;
+  ~EventPair() {
+    if (a) cudaEventDestroy(a);
+    if (b) cudaEventDestroy(b);
+  }
+  // device time of f() on stream s, in ms
+  template <class F>
+  float time(cudaStream_t s, F &&f) {
+    CK(cudaEventRecord(a, s));
+    f();
+    CK(cudaEventRecord(b, s));
+    CK(cudaEventSynchronize(b));
+    float x = 0.f;
+    CK(cudaEventElapsedTime(&x, a, b));
+    return x;
+  }
+};
+
 template <typename T>
 void upload(DBuf &d, const std::vector<T> &h, int64_t *counter) {
   d.alloc(std::max<size_t>(h.size(), 1) * sizeof(T), counter);
@@ -1160,9 +1186,7 @@ class Engine final : public IEngine {
   // timed launches only write buffers that each residual evaluation rewrites.
   void autotune(int shapes[4], double ms[8]) override {
     require_ready();
-    cudaEvent_t a, b;
-    CK(cudaEventCreate(&a));
-    CK(cudaEventCreate(&b));
+    EventPair ev;
     const int64_t held = bytes_;  // the trial plans are freed again below
     for (int k = 0; k < 4; ++k) {
       double best = 1e300;
@@ -1174,15 +1198,7 @@ class Engine final : public IEngine {
         double t = 0.0;
         for (const Plan *p : {&pl, &p4, &pr}) {
           float tbest = 1e30f;
-          for (int rep = 0; rep < 3; ++rep) {
-            CK(cudaEventRecord(a, st_));
-            run_plan(*p);
-            CK(cudaEventRecord(b, st_));
-            CK(cudaEventSynchronize(b));
-            float x = 0.f;
-            CK(cudaEventElapsedTime(&x, a, b));
-            tbest = std::min(tbest, x);
-          }
+          for (int rep = 0; rep < 3; ++rep) tbest = std::min(tbest, ev.time(st_, [&] { run_plan(*p); }));
           t += tbest;
         }
         ms[2 * k + sh] = t;
@@ -1191,8 +1207,6 @@ class Engine final : public IEngine {
       gemm_shape_[k] = pick;
       shapes[k] = pick;
     }
-    cudaEventDestroy(a);
-    cudaEventDestroy(b);
     bytes_ = held;
     build_fp64_plans(planLadder_, planI4_, planRing_, -1, nullptr);
     mixed_ready_ = false;  // the mixed residual's FP64 plans are rebuilt with the new shapes
@@ -1207,24 +1221,14 @@ class Engine final : public IEngine {
     require_ready();
     if (precision != 1 && precision != 2) throw EngineError(1, "tensor-core autotune needs a mixed precision");
     prepare_mixed(precision == 2 ? kTcTF32 : kTcBF16);
-    cudaEvent_t a, b;
-    CK(cudaEventCreate(&a));
-    CK(cudaEventCreate(&b));
+    EventPair ev;
     TcPlan *plans[3] = {&tcPP_, &tcI4_, &tcR1_};
     for (int p = 0; p < 3; ++p) {
       double t[2];
       for (int v = 0; v < 2; ++v) {
         plans[p]->merged[0] = plans[p]->merged[1] = v;
         float best = 1e30f;
-        for (int rep = 0; rep < 3; ++rep) {
-          CK(cudaEventRecord(a, st_));
-          run_tc(*plans[p]);
-          CK(cudaEventRecord(b, st_));
-          CK(cudaEventSynchronize(b));
-          float x = 0.f;
-          CK(cudaEventElapsedTime(&x, a, b));
-          best = std::min(best, x);
-        }
+        for (int rep = 0; rep < 3; ++rep) best = std::min(best, ev.time(st_, [&] { run_tc(*plans[p]); }));
         t[v] = best;
         ms[2 * p + v] = best;
       }
@@ -1233,9 +1237,13 @@ class Engine final : public IEngine {
       tc_choice_[p] = pick;
       merged[p] = pick;
     }
-    cudaEventDestroy(a);
-    cudaEventDestroy(b);
-    check_flag("tensor-core autotune");
+    int err = 0;
+    CK(cudaMemcpyAsync(&err, tcerr_.p, sizeof(int), cudaMemcpyDeviceToHost, st_));
+    CK(cudaStreamSynchronize(st_));
+    if (err) {
+      CK(cudaMemsetAsync(tcerr_.p, 0, sizeof(int), st_));
+      throw EngineError(2, "tensor-core GEMM reported error code " + std::to_string(err) + " during the autotune");
+    }
     ++plan_epoch_;  // the replayed residual graphs are captured again with the chosen launches
   }
 
