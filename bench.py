@@ -255,8 +255,7 @@ def kernel_work(P, H, ring, precision, real=True):
     return {"x_fp64": ("flop", x, None), "i4_fp64": ("flop", i4, None), "ring_fp64": ("flop", rg, None),
             "ladder_fp64": ("flop", pp + hh, None), "pp_rebase_fp64": ("flop", pp, None), "hh_fp64": ("flop", hh, None),
             "pp_tc": ("byte", a_pp, r_pp), "i4_tc": ("byte", a_i4, r_i4), "ring_tc": ("byte", a_rg, r_rg),
-            "pp_rebase_digits": ("byte", a_oz + a_hh_oz, r_oz + r_hh_oz),
-            "i4_rebase_digits": ("byte", a_i4_oz + a_x_oz, r_i4_oz + r_x_oz),
+            "pp_rebase_digits": ("byte", a_oz, r_oz), "i4_rebase_digits": ("byte", a_i4_oz, r_i4_oz),
             "ring_rebase_digits": ("byte", a_rg_oz, r_rg_oz), "x_rebase_digits": ("byte", a_x_oz, r_x_oz),
             "hh_rebase_digits": ("byte", a_hh_oz, r_hh_oz)}
 
@@ -266,8 +265,8 @@ KERNEL_NAMES = {"x_fp64": "k_xdot X = V_hhpp'^T T' (FP64 column dots)", "i4_fp64
                 "pp_rebase_fp64": "k_gemm<double> pp-ladder at a re-base", "hh_fp64": "k_gemm<double> hh-ladder",
                 "pp_tc": "k_tc_gemm pp + hh ladder corrections (3 products, one accumulator)", "i4_tc": "k_tc_gemm dI4 and dX corrections",
                 "ring_tc": "k_tc_gemm ring corrections (2 products, one accumulator)", "split": "k_tc_split",
-                "pp_rebase_digits": "k_oz_gemm pp and hh ladders at a re-base (exact digit products, one launch)",
-                "i4_rebase_digits": "k_oz_gemm I4 and X at a re-base (exact digit products, one launch)",
+                "pp_rebase_digits": "k_oz_gemm pp-ladder at a re-base (exact digit products)",
+                "i4_rebase_digits": "k_oz_gemm I4 at a re-base (exact digit products)",
                 "ring_rebase_digits": "k_oz_gemm ring at a re-base (exact digit products)",
                 "i7_fp64": "k_i7dots I7 of a mixed residual (FP64 column dots)",
                 "x_rebase_digits": "k_oz_gemm X = V_hhpp'^T T' at a re-base (exact digit products)",
@@ -463,8 +462,7 @@ def run_ours(args, wl):
 # captures of `bench.py --steps 1 --warmup 1 --no-e2e --no-cpu-baseline` on the workload:
 # (workload, precision, kernel slot) -> bytes
 PROFILED_TRAFFIC = {
-    # profiles/k_oz_gemm_snm132n3.md: both phase launches of the pp re-base product (captured
-    # before the hh ladder joined that launch; its tiles' operands are a few percent more)
+    # profiles/k_oz_gemm_snm132n3.md: both phase launches of the pp re-base product
     ("snm132n3", "bf16x3", "pp_rebase_digits"): 4.09e9,
     # the same scaled to SNM 132 nmax=4 by the algorithmic bytes (12.0 GB / 1.51 GB)
     ("snm132n4", "bf16x3", "pp_rebase_digits"): 32.6e9,

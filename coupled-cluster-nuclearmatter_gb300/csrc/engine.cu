@@ -2087,8 +2087,7 @@ class Engine final : public IEngine {
       CK(cudaMemset(tcerr_.p, 0, sizeof(int)));
     }
     std::vector<OzSplitJob> jv, jb, jt, ji, j9;
-    // X shares a launch with I4, and HH_b (into HHb_) with PP_b: independent outputs
-    OzList lpp, l4, lr;
+    OzList lpp, l4, lr, lx, lhh;
     {
       int64_t qa = 0, qb = 0, xa = 0, xb = 0, voff = 0, hoff = 0;
       int64_t qx = 0, xx = 0, qta = 0, xta = 0, q9 = 0, x9 = 0;
@@ -2100,11 +2099,11 @@ class Engine final : public IEngine {
           add_oz(lpp, ozVpp_, qa, xa, ozTb_, qb, xb, pk.P, pk.H, pk.P, PPb_.as<S>() + pk.t_off, 1, pk.P, 1.0);
           // X(kl, ij) = sum_cd V_hhpp'(cd, kl) T'(cd, ij): A = V_hhpp'^T, B the T' digits above
           add_oz_split(jv, Vhp_.as<S>() + pk.t_off, pk.P, 1, pk.H, pk.P, 128, mpad(pk.H), ozVhpA_, qx, xx);
-          add_oz(l4, ozVhpA_, qx, xx, ozTb_, qb, xb, pk.H, pk.H, pk.P, X_.as<S>() + hoff, 1, pk.H, 1.0);
+          add_oz(lx, ozVhpA_, qx, xx, ozTb_, qb, xb, pk.H, pk.H, pk.P, X_.as<S>() + hoff, 1, pk.H, 1.0);
           // HH_b(ab, ij) = sum_kl T'(ab, kl) I9'(kl, ij)
           add_oz_split(jb, T_.as<S>() + pk.t_off, 1, pk.P, pk.P, pk.H, 128, mpad(pk.P), ozTA_, qta, xta);
           add_oz_split(j9, I9_.as<S>() + hoff, pk.H, 1, pk.H, pk.H, npadf(pk.H), npadf(pk.H), ozI9B_, q9, x9);
-          add_oz(lpp, ozTA_, qta, xta, ozI9B_, q9, x9, pk.P, pk.H, pk.H, HHb_.as<S>() + pk.t_off, 1, pk.P, 1.0);
+          add_oz(lhh, ozTA_, qta, xta, ozI9B_, q9, x9, pk.P, pk.H, pk.H, PPb_.as<S>() + pk.t_off, 1, pk.P, 1.0);
           qa += (int64_t)mpad(pk.P) * nkf(pk.P) * 64;
           qb += (int64_t)npadf(pk.H) * nkf(pk.P) * 64;
           xa += pk.P;
@@ -2147,6 +2146,8 @@ class Engine final : public IEngine {
     finalize_oz_split(ozsI4_, ji);
     finalize_oz_split(ozsI9_, j9);
     finalize_oz(ozPP_, lpp);
+    finalize_oz(ozX_, lx);
+    finalize_oz(ozHH_, lhh);
     finalize_oz(ozI4_, l4);
     finalize_oz(ozRing_, lr);
     run_oz_split(ozsV_);
@@ -2372,24 +2373,21 @@ class Engine final : public IEngine {
 
   // FP64 residual at T that also becomes the new base of the defect correction.  With
   // digits, every product of it on the FP64 pipe except the one-body dots moves to the
-  // exact digit-product GEMM, in three launches (two phases each for complex engines):
-  // X = V_hhpp'^T T' with I4, the ring, and PP_b = V_pppp' T' with HH_b = T' I9'.
+  // exact digit-product GEMM: X = V_hhpp'^T T', I4, the ring, PP_b = V_pppp' T' and
+  // HH_b = T' I9'.
   void residual_fp64_rebase(bool digits) {
     mark(0);
     launch_gather_tph<S>(D_, T_.as<S>(), Tph_.as<S>(), st_);
     mark(1);
     cudaStream_t xs;
     if (digits) {
-      // T' digits as the B operand (X, PP_b) and as the A operand (HH_b), T_ph digits
-      // (I4, ring); then X = V_hhpp'^T T' and I4 = W + 1/2 V_ph T_ph in one launch
+      // T' digits as the B operand (X, PP_b) and as the A operand (HH_b)
       kbegin(kKSplit);
       run_oz_split(ozsTb_);
-      run_oz_split(ozsTph_);
       kend();
       CK(cudaMemsetAsync(X_.p, 0, std::max<int64_t>(n_hh2_, 1) * sizeof(S), st_));
-      CK(cudaMemcpyAsync(I4_.p, W_.p, std::max<int64_t>(n_i4_, 1) * sizeof(S), cudaMemcpyDeviceToDevice, st_));
-      kbegin(kKI4Oz);
-      run_oz(ozI4_);
+      kbegin(kKXOz);
+      run_oz(ozX_);
       kend();
       xs = fork_side();
     } else {
@@ -2404,7 +2402,14 @@ class Engine final : public IEngine {
     launch_i6<S>(D_, (const int2 *)i6rows_.p, ni6rows_, i6dots_.as<S>(), T_.as<S>(), Vhp_.as<S>(), fdiag_.as<S>(),
                  f6_.as<S>(), d2ab_.as<S>(), i6off_.as<S>(), xs);
     mark(3);
-    if (digits) {  // R_ph = T_ph I4 as a digit product (I4 came with X)
+    if (digits) {  // I4 = W + 1/2 V_ph T_ph and R_ph = T_ph I4 as digit products
+      kbegin(kKSplit);
+      run_oz_split(ozsTph_);
+      kend();
+      CK(cudaMemcpyAsync(I4_.p, W_.p, std::max<int64_t>(n_i4_, 1) * sizeof(S), cudaMemcpyDeviceToDevice, st_));
+      kbegin(kKI4Oz);
+      run_oz(ozI4_);
+      kend();
       kbegin(kKSplit);
       run_oz_split(ozsI4_);
       kend();
@@ -2429,16 +2434,17 @@ class Engine final : public IEngine {
                     i7off_.as<S>(), nullptr, Rringb_.as<S>(), R_.as<S>(), st_);
     mark(6);
     if (digits) {
-      // PP_b = V_pppp' T' and HH_b = T' I9' in one launch, then PP_b += HH_b
+      // PP_b and then HH_b accumulate into PP_b (two launches in stream order)
       kbegin(kKSplit);
       run_oz_split(ozsI9_);
       kend();
       CK(cudaMemsetAsync(PPb_.p, 0, n_t_ * sizeof(S), st_));
-      CK(cudaMemsetAsync(HHb_.p, 0, n_t_ * sizeof(S), st_));
       kbegin(kKPPOz);
       run_oz(ozPP_);
       kend();
-      launch_axpy<S>(n_t_, HHb_.as<S>(), PPb_.as<S>(), st_);
+      kbegin(kKHHOz);
+      run_oz(ozHH_);
+      kend();
     } else {
       kbegin(kKPP64);
       run_plan(planPP_);
@@ -2562,7 +2568,7 @@ class Engine final : public IEngine {
   DBuf Tb_, PPb_, Tphb_, Rringb_, I4b_, dI4_, tcerr_, Xb_, dI9_, HHb_, xd7_;
   OzBuf ozVpp_, ozTb_, ozVph_, ozTphB_, ozTphA_, ozI4B_, ozVhpA_, ozTA_, ozI9B_;
   OzSplitPlan ozsV_, ozsTb_, ozsTph_, ozsI4_, ozsI9_;
-  OzPlan ozPP_, ozI4_, ozRing_;  // PP_b with HH_b; X with I4; the ring
+  OzPlan ozPP_, ozI4_, ozRing_, ozX_, ozHH_;
   bool oz_ready_ = false;
   int64_t oz_v_version_ = -1;
   TileBuf tVpp_, tD_, tVph_, tDphB_, tTphbA_, tDphA_, tdI4B_, tI4B_, tDA_, tI9B_, tTbA_, tdI9B_, tVhT_;

@@ -51,12 +51,12 @@ enum KernelSlot {
   kKTcI4 = 7,   // k_tc_gemm: dI4 = 1/2 V_ph dT_ph
   kKTcRing = 8, // k_tc_gemm: dR_ph = T_ph,b dI4 + dT_ph I4, one launch
   kKSplit = 9,  // k_tc_split: per-iteration operand splits
-  kKPPOz = 10,  // k_oz_gemm: V_pppp' T' and T' I9' at a re-base as exact digit products, one launch
-  kKI4Oz = 11,  // k_oz_gemm: I4 and X = V_hhpp'^T T' at a re-base as exact digit products, one launch
+  kKPPOz = 10,  // k_oz_gemm: V_pppp' T' at a re-base as exact digit products
+  kKI4Oz = 11,  // k_oz_gemm: I4 at a re-base as exact digit products
   kKRingOz = 12,  // k_oz_gemm: ring at a re-base as exact digit products
   kKI7 = 13,    // k_i7dots + k_i7sum: I7 of a mixed residual from the X entries it reads
-  kKXOz = 14,   // unused since X shares the I4 launch (kept so the slot numbers stay)
-  kKHHOz = 15,  // unused since HH_b shares the pp launch (kept so the slot numbers stay)
+  kKXOz = 14,   // k_oz_gemm: X = V_hhpp'^T T' at a re-base as exact digit products
+  kKHHOz = 15,  // k_oz_gemm: HH_b = T' I9' at a re-base as exact digit products
   kKernelSlots = 16
 };
 
