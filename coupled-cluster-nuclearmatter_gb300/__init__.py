@@ -81,6 +81,14 @@ class _IterResult(C.Structure):
                 ("fp64_sweeps", C.c_int32), ("mixed_iterations", C.c_int32)]
 
 
+class _IterRecord(C.Structure):
+    _fields_ = [("iteration", C.c_int32), ("kind", C.c_int32), ("energy", C.c_double * 2), ("de", C.c_double),
+                ("res_norm", C.c_double), ("ms", C.c_double), ("term_ms", C.c_double * 9)]
+
+
+ITER_KINDS = ("reference", "fp64", "mixed")  # ccx_iter_record.kind
+TERM_KEYS = ("tph_gather", "i9_i7", "i6", "i4", "ring", "r_init", "ladders", "update", "diis")
+
 _lib = None
 vp = C.c_void_p
 
@@ -130,6 +138,7 @@ def lib():
         "ccx_ccd_energy": ([vp, vp], C.c_int),
         "ccx_residual_norm": ([vp, C.POINTER(dbl)], C.c_int),
         "ccx_ccd_iter": ([vp, C.POINTER(_IterOpts), C.POINTER(_IterResult)], C.c_int),
+        "ccx_engine_iter_log": ([vp, i32, vp, C.POINTER(i32)], C.c_int),
         "ccx_pert_triples": ([vp, vp], C.c_int),
         "ccx_get_vblock": ([vp, i32, i32, vp], C.c_int),
         "ccx_get_fock": ([vp, vp], C.c_int),
@@ -340,6 +349,41 @@ class Learner:
         out = np.zeros(len(X), np.float32)
         _check(lib().ccx_learner_infer(self._h, _ptr(X), len(X), _ptr(out), int(tensor_cores)))
         return out
+
+
+def kfermi(density: float, snm: bool) -> float:
+    """Fermi momentum (fm^-1) of a density (fm^-3): rho = g kf^3 / (3 pi^2) with g = 2 for
+    symmetric matter, 1 for neutron matter (ccm_main.f90:930-945 converts the other way)."""
+    return (3.0 * np.pi ** 2 * density / (2.0 if snm else 1.0)) ** (1.0 / 3.0)
+
+
+def iteration_records(log, e0: float, A: int) -> list:
+    """The structured per-iteration lines of a solve: Engine.iter_log() records as
+    JSON-ready dicts with the energy per nucleon (E0 + E_CCD) / A beside the correlation
+    energy; term_ms is kept only where the solve was profiled."""
+    out = []
+    for r in log:
+        d = {"record": "iteration", "iteration": r["iteration"], "kind": r["kind"],
+             "e_ccd": [r["e_ccd"].real, r["e_ccd"].imag], "e_per_a": (e0 + r["e_ccd"].real) / A,
+             "de": r["de"], "res_norm": r["res_norm"], "ms": r["ms"]}
+        if any(r["term_ms"].values()):
+            d["term_ms"] = dict(r["term_ms"])
+        out.append(d)
+    return out
+
+
+def result_record(A: int, density: float, snm: bool, e0: float, e_mbpt2: float, e_ccd: float,
+                  e_triples=None, cE: float = 0.0, cD: float = 0.0, iterations=None) -> dict:
+    """The final record of a run, the values of the (8f12.5) line ccm_main.f90:338-339
+    writes: cE, cD, kf, density and, per nucleon, E0, MBPT2 = E0 + E_MP2, E_CCD = E0 +
+    E_CCD(corr) and E_CCD + E(T) (None where (T) was not computed).  Energies are the real
+    parts, in MeV; e_mbpt2, e_ccd and e_triples are correlation energies."""
+    d = {"record": "result", "cE": cE, "cD": cD, "kf": kfermi(density, snm), "density": density,
+         "e0_per_a": e0 / A, "mbpt2_per_a": (e0 + e_mbpt2) / A, "eccd_per_a": (e0 + e_ccd) / A,
+         "eccdt_per_a": None if e_triples is None else (e0 + e_ccd + e_triples) / A}
+    if iterations is not None:
+        d["iterations"] = iterations
+    return d
 
 
 def deck_parse(text: str) -> dict:
@@ -599,6 +643,19 @@ class Engine:
                 "e_mbpt2": complex(r.e_mbpt2[0], r.e_mbpt2[1]), "e_ccd": complex(r.e_ccd[0], r.e_ccd[1]),
                 "res_norm": r.res_norm, "seconds": r.seconds, "fp64_sweeps": r.fp64_sweeps,
                 "mixed_iterations": r.mixed_iterations}
+
+    def iter_log(self) -> list:
+        """One record per residual evaluation of the last ccd_iter (or batched solve):
+        iteration, kind ("reference", "fp64" or "mixed"), e_ccd after the update, de (the
+        change since the previous record), res_norm, ms (host wall-clock of the iteration)
+        and term_ms (device ms per residual term; zeros unless profiling is on)."""
+        n = C.c_int32()
+        _check(lib().ccx_engine_iter_log(self._h, 0, None, C.byref(n)))
+        recs = (_IterRecord * max(n.value, 1))()
+        _check(lib().ccx_engine_iter_log(self._h, n.value, recs, C.byref(n)))
+        return [{"iteration": r.iteration, "kind": ITER_KINDS[r.kind], "e_ccd": complex(r.energy[0], r.energy[1]),
+                 "de": r.de, "res_norm": r.res_norm, "ms": r.ms, "term_ms": dict(zip(TERM_KEYS, r.term_ms))}
+                for r in recs[:n.value]]
 
     def prepare(self, mode=MODE_STANDARD, precision=PREC_FP64, diis_dim=8, rebase=REBASE_FP64):
         """The one-time set-up of a solve with these options, without solving."""

@@ -1,5 +1,6 @@
 // extern "C" entry points of include/ccx.h.  Every entry point catches all C++
 // exceptions, stores the message for ccx_last_error() and returns a status code.
+#include <algorithm>
 #include <cctype>
 #include <cstdio>
 #include <cstdlib>
@@ -370,6 +371,26 @@ int ccx_engine_diis_fallbacks(const ccx_engine *e, int64_t *n) {
 int ccx_engine_launches(const ccx_engine *e, int64_t *n) {
   if (!n) return fail(CCX_EINVAL, "null argument");
   ENGINE_CALL(e, *n = e->E->launches());
+}
+int ccx_engine_iter_log(const ccx_engine *e, int32_t capacity, ccx_iter_record *records, int32_t *n) {
+  if (!n || capacity < 0 || (capacity > 0 && !records)) return fail(CCX_EINVAL, "null argument or negative capacity");
+  ENGINE_CALL(e, {
+    const std::vector<ccx::IterRecord> &log = e->E->iter_log();
+    *n = (int32_t)log.size();
+    const size_t m = std::min(log.size(), (size_t)capacity);
+    for (size_t i = 0; i < m; ++i) {
+      const ccx::IterRecord &s = log[i];
+      ccx_iter_record &d = records[i];
+      d.iteration = s.iteration;
+      d.kind = s.kind;
+      d.energy[0] = s.e[0];
+      d.energy[1] = s.e[1];
+      d.de = s.de;
+      d.res_norm = s.res_norm;
+      d.ms = s.ms;
+      for (int k = 0; k < 9; ++k) d.term_ms[k] = s.term_ms[k];
+    }
+  });
 }
 int ccx_engine_set_profiling(ccx_engine *e, int32_t on) { ENGINE_CALL(e, e->E->set_profiling(on != 0)); }
 int ccx_engine_timers(const ccx_engine *e, double ms[10]) {

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <complex>
 #include <cstdio>
@@ -235,6 +236,7 @@ class Engine final : public IEngine {
   void kernel_timers(double ms[kKernelSlots], int64_t n[kKernelSlots]) const override {
     for (int i = 0; i < kKernelSlots; ++i) { ms[i] = ktimers_[i]; n[i] = kcount_[i]; }
   }
+  const std::vector<IterRecord> &iter_log() const override { return ilog_; }
 
   // ---------------------------------------------------------------- interaction
   void set_fock(const double *fock, const double e0[2]) override {
@@ -1372,6 +1374,36 @@ class Engine final : public IEngine {
       timers_[i] += ms;
     }
   }
+  // the per-iteration log: one record per residual, its term times the differences of
+  // the running per-term timers since the previous record
+  void log_begin() {
+    ilog_.clear();
+    for (int i = 0; i < 9; ++i) ilog_prev_[i] = timers_[i];
+    ilog_t_ = std::chrono::steady_clock::now();
+  }
+  void log_record(int it, int kind, const double e[2], double de, double rn) {
+    IterRecord rec;
+    rec.iteration = it;
+    rec.kind = kind;
+    rec.e[0] = e[0];
+    rec.e[1] = e[1];
+    rec.de = de;
+    rec.res_norm = rn;
+    const auto t = std::chrono::steady_clock::now();
+    rec.ms = std::chrono::duration<double, std::milli>(t - ilog_t_).count();
+    ilog_t_ = t;
+    for (int i = 0; i < 9; ++i) {
+      rec.term_ms[i] = timers_[i] - ilog_prev_[i];
+      ilog_prev_[i] = timers_[i];
+    }
+    ilog_.push_back(rec);
+  }
+  // the standard loop's DIIS extrapolation runs after its iteration's record
+  void log_amend_diis() {
+    if (ilog_.empty()) return;
+    ilog_.back().term_ms[8] += timers_[8] - ilog_prev_[8];
+    ilog_prev_[8] = timers_[8];
+  }
   void fetch_res(int n) {
     CK(cudaMemcpyAsync(host_res_, res_.p, n * sizeof(double), cudaMemcpyDeviceToHost, st_));
     CK(cudaStreamSynchronize(st_));
@@ -1440,6 +1472,7 @@ class Engine final : public IEngine {
   }
 
   void iterate_reference(const IterOpts &o, IterResult &r) {
+    log_begin();
     diis_setup(6, 6);
     int count = 0;
     std::complex<double> e1(r.e_mbpt2[0], r.e_mbpt2[1]), e2(0.0, 0.0), de(4.0, 0.0);
@@ -1459,6 +1492,7 @@ class Engine final : public IEngine {
       de = e2 - e1;
       e1 = e2;
       r.iterations = it;
+      log_record(it, 0, e, de.real(), r.res_norm);
       if (o.verbose) std::printf("ccx it %3d dE %.3e E %.12f |R| %.3e\n", it, de.real(), e2.real(), r.res_norm);
     }
     r.converged = !(std::abs(de) > o.tol);
@@ -1518,6 +1552,7 @@ class Engine final : public IEngine {
     s.e[0] = r.e_mbpt2[0];
     s.e[1] = r.e_mbpt2[1];
     s.done = o.max_iter < 1;
+    log_begin();
   }
   // the one-time set-up a solve with these options needs (operand tiles, digit planes
   // of the interaction, DIIS history), without solving
@@ -1577,6 +1612,7 @@ class Engine final : public IEngine {
       throw EngineError(5, "non-finite energy: the iteration diverged or the input holds NaN/Inf");
     mark(8);
     if (timing_) accumulate_timers(7, 8);
+    const double de = host_res_[0] - s.e[0];
     s.e[0] = host_res_[0];
     s.e[1] = host_res_[1];
     const double rn = 2.0 * std::sqrt(host_res_[2]);
@@ -1590,6 +1626,7 @@ class Engine final : public IEngine {
     r.iterations = s.it - 1;
     r.e_ccd[0] = s.e[0];
     r.e_ccd[1] = s.e[1];
+    log_record(s.it, s.exact ? 1 : 2, s.e, de, rn);
     if (s.o.verbose) std::printf("ccx it %3d %s |R| %.3e E %.12f\n", s.it, s.exact ? "fp64 " : "mixed", rn, s.e[0]);
     if (s.exact && rn < s.o.tol) {
       r.converged = 1;
@@ -1657,6 +1694,7 @@ class Engine final : public IEngine {
     ++launches_;
     mark(9);
     if (timing_) accumulate_timers(8, 9);
+    log_amend_diis();
     s.r->iterations = s.it;
     if (s.it >= s.o.max_iter) s.done = true;
   }
@@ -2585,6 +2623,9 @@ class Engine final : public IEngine {
   DBuf stage2_, copyjobs_;
   double e0_[2] = {0, 0};
   double last_rn_ = 0.0;
+  std::vector<IterRecord> ilog_;
+  double ilog_prev_[9] = {};
+  std::chrono::steady_clock::time_point ilog_t_;
   bool have_fock_ = false, have_t_ = false, dirty_ = true, vph_ready_ = false, generated_ = false;
   // W built on the device by generate(); caller V block kinds since then (bit = kind)
   bool w_generated_ = false;

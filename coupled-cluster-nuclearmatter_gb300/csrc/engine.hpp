@@ -5,6 +5,7 @@
 #include <memory>
 #include <stdexcept>
 #include <string>
+#include <vector>
 
 #include "layout.hpp"
 #include "learner.hpp"
@@ -32,6 +33,17 @@ struct IterResult {
   int fp64_sweeps = 0, mixed_iterations = 0;
   double e_mbpt2[2] = {0, 0}, e_ccd[2] = {0, 0};
   double res_norm = 0.0, seconds = 0.0;
+};
+// One residual evaluation of the last ccd_iter (or batched solve): what the loop decided
+// on, for a structured per-iteration log.
+struct IterRecord {
+  int iteration = 0;
+  int kind = 0;            // 0 reference-loop step, 1 FP64 residual, 2 mixed-precision residual
+  double e[2] = {0, 0};    // correlation energy after the update
+  double de = 0.0;         // Re of the change since the previous record (the first: since MP2)
+  double res_norm = 0.0;   // ||R - D T|| of this residual
+  double ms = 0.0;         // host wall-clock since the previous record (the loop synchronises once an iteration)
+  double term_ms[9] = {};  // profiling on: device ms of this iteration per residual term; else 0
 };
 struct PotentialSpec {
   int kind = 0;
@@ -70,6 +82,7 @@ class IEngine {
   virtual void set_triples_precision(int p) = 0;  // 0 FP64 contractions, 1 FP32 contractions
   virtual void timers(double ms[10]) const = 0;
   virtual void kernel_timers(double ms[kKernelSlots], int64_t n[kKernelSlots]) const = 0;
+  virtual const std::vector<IterRecord> &iter_log() const = 0;
   virtual void set_fock(const double *fock, const double e0[2]) = 0;
   virtual void set_vblock(int kind, int ch, const double *v) = 0;
   virtual void set_vblocks(int kind, int n, const int *chs, const double *const *vs) = 0;

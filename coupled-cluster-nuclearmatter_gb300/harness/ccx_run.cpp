@@ -16,7 +16,9 @@
 // held in a host array in the reference's layout and passed with ccx_set_vblock (the
 // arrays are exported from a device-generated helper engine, since the synthetic
 // potentials are generated on the device).  "--loop solver" runs ccx_ccd_iter instead
-// of the reference loop.  Output is one "key value..." line per result.
+// of the reference loop.  Output is one "key value..." line per result; "--json" adds
+// one JSON line per iteration and a final result record (the values of the (8f12.5)
+// line ccm_main.f90:338-339 writes).
 #include <cerrno>
 #include <chrono>
 #include <cmath>
@@ -35,7 +37,7 @@ struct Args {
   std::string deck, load, save, blocks = "generated", loop, mode, precision, rebase = "digits", pot;
   int nmax = -1, A = -1, snm = -1, device = 0, max_iter = -1, diis = 8, scalar = -1;
   double density = -1.0, theta[3] = {0, 0, 0}, tol = -1.0;
-  bool triples = false, layout_only = false, has_theta = false, f64_literals = false;
+  bool triples = false, layout_only = false, has_theta = false, f64_literals = false, json = false;
 };
 
 [[noreturn]] void usage(const char *msg) {
@@ -45,7 +47,8 @@ struct Args {
                "               [--potential minnesota|chiral_like] [--real|--complex] [--blocks generated|host]\n"
                "               [--loop shim|solver] [--mode reference|standard] [--precision fp64|bf16x3|tf32x3]\n"
                "               [--rebase fp64|digits] [--tol T] [--max-iter N] [--diis N] [--triples]\n"
-               "               [--load FILE] [--save FILE] [--device D] [--layout-only] [--f64-literals]\n");
+               "               [--load FILE] [--save FILE] [--device D] [--layout-only] [--f64-literals]\n"
+               "               [--json]\n");
   std::exit(2);
 }
 
@@ -97,6 +100,7 @@ Args parse(int argc, char **argv) {
     else if (k == "--device") a.device = (int)num("--device");
     else if (k == "--layout-only") a.layout_only = true;
     else if (k == "--f64-literals") a.f64_literals = true;
+    else if (k == "--json") a.json = true;
     else if (k == "-h" || k == "--help") usage(nullptr);
     else usage(("unknown option " + k).c_str());
   }
@@ -116,6 +120,35 @@ std::string read_file(const std::string &path) {
   while ((n = std::fread(buf, 1, sizeof buf, f)) > 0) s.append(buf, n);
   std::fclose(f);
   return s;
+}
+
+// a JSON number: shortest round-trip form; NaN and Inf (which JSON lacks) as null
+std::string jnum(double v) {
+  if (!std::isfinite(v)) return "null";
+  char b[32];
+  std::snprintf(b, sizeof b, "%.17g", v);
+  return b;
+}
+
+const char *kIterKind[] = {"reference", "fp64", "mixed"};
+const char *kTermName[] = {"tph_gather", "i9_i7", "i6", "i4", "ring", "r_init", "ladders", "update", "diis"};
+
+// one iteration of the solve as a JSON line: the energy per nucleon, its change, the
+// residual norm (null where the loop has none) and the times
+void json_iteration(const ccx_iter_record &r, double e0, int A, bool has_norm) {
+  std::string s = "{\"record\": \"iteration\", \"iteration\": " + std::to_string(r.iteration) + ", \"kind\": \"" +
+                  kIterKind[r.kind] + "\", \"e_ccd\": [" + jnum(r.energy[0]) + ", " + jnum(r.energy[1]) +
+                  "], \"e_per_a\": " + jnum((e0 + r.energy[0]) / A) + ", \"de\": " + jnum(r.de) +
+                  ", \"res_norm\": " + (has_norm ? jnum(r.res_norm) : std::string("null")) +
+                  ", \"ms\": " + jnum(r.ms);
+  bool timed = false;
+  for (double t : r.term_ms) timed = timed || t != 0.0;
+  if (timed) {
+    s += ", \"term_ms\": {";
+    for (int k = 0; k < 9; ++k) s += std::string(k ? ", " : "") + "\"" + kTermName[k] + "\": " + jnum(r.term_ms[k]);
+    s += "}";
+  }
+  std::printf("%s}\n", s.c_str());
 }
 
 double now() {
@@ -249,6 +282,7 @@ int main(int argc, char **argv) {
   double ener1[2], ener2[2] = {0, 0};
   check(ccx_ccd_energy(E, ener1), "ccx_ccd_energy");
   std::printf("e_mbpt2 %.17g %.17g\n", ener1[0], ener1[1]);
+  const double e_mbpt2 = ener1[0];
   const double t0 = now();
   int iterations = 0;
   double e_ccd[2];
@@ -256,7 +290,7 @@ int main(int argc, char **argv) {
     // ccd_iter (ccm_iter.f90:20-96): subspace 6, DIIS every 6, stop on |dE| <= tol
     check(ccx_diis_setup(E, 6, 6), "ccx_diis_setup");
     int32_t count = 0;
-    double dener = 4.0;
+    double dener = 4.0, tprev = now();
     for (int it = 1; it <= max_iter && std::fabs(dener) > tol; ++it) {
       check(ccx_t2_intermediate(E), "ccx_t2_intermediate");
       ++count;
@@ -267,6 +301,18 @@ int main(int argc, char **argv) {
       ener1[1] = ener2[1];
       iterations = it;
       std::printf("iter %d e_ccd %.17g de %.3e\n", it, ener2[0], dener);
+      if (a.json) {
+        ccx_iter_record rec{};
+        rec.iteration = it;
+        rec.kind = CCX_ITER_REFERENCE;
+        rec.energy[0] = ener2[0];
+        rec.energy[1] = ener2[1];
+        rec.de = dener;
+        const double t = now();
+        rec.ms = 1e3 * (t - tprev);
+        tprev = t;
+        json_iteration(rec, e0[0], bp.A, false);
+      }
     }
     e_ccd[0] = ener1[0];
     e_ccd[1] = ener1[1];
@@ -289,16 +335,37 @@ int main(int argc, char **argv) {
     e_ccd[1] = r.e_ccd[1];
     std::printf("converged %d res_norm %.3e fp64_sweeps %d mixed_iterations %d\n", r.converged, r.res_norm,
                 r.fp64_sweeps, r.mixed_iterations);
+    if (a.json) {
+      int32_t n = 0;
+      check(ccx_engine_iter_log(E, 0, nullptr, &n), "ccx_engine_iter_log");
+      std::vector<ccx_iter_record> log((size_t)n);
+      if (n > 0) check(ccx_engine_iter_log(E, n, log.data(), &n), "ccx_engine_iter_log");
+      for (const ccx_iter_record &rec : log) json_iteration(rec, e0[0], bp.A, true);
+    }
   }
   const double secs = now() - t0;
   std::printf("e_ccd %.17g %.17g\n", e_ccd[0], e_ccd[1]);
   std::printf("e_per_a %.17g\n", (e0[0] + e_ccd[0]) / bp.A);
   std::printf("iterations %d seconds %.6f\n", iterations, secs);
   const bool triples = a.triples || (have_deck && std::strcmp(d.cc_approx, "CCD(T)") == 0);
+  double et[2] = {0, 0};
   if (triples) {
-    double et[2];
     check(ccx_pert_triples(E, et), "ccx_pert_triples");
     std::printf("e_triples %.17g %.17g\n", et[0], et[1]);
+  }
+  if (a.json) {
+    // ccm_main.f90:338-339: cE, cD, kf, density, and per nucleon E0, MBPT2 = E0 + the MP2
+    // correlation energy, E_CCD = E0 + the CCD correlation energy, and E_CCD + E(T)
+    // (null where (T) was not computed); kf from the density as ccm_main.f90:930-945
+    const double pi = 3.14159265358979323846;
+    const double kf = std::cbrt(3.0 * pi * pi * bp.density / (bp.snm ? 2.0 : 1.0));
+    const double A = bp.A;
+    std::printf("{\"record\": \"result\", \"cE\": %s, \"cD\": %s, \"kf\": %s, \"density\": %s, \"e0_per_a\": %s, "
+                "\"mbpt2_per_a\": %s, \"eccd_per_a\": %s, \"eccdt_per_a\": %s, \"iterations\": %d}\n",
+                jnum(have_deck ? d.cE : 0.0).c_str(), jnum(have_deck ? d.cD : 0.0).c_str(), jnum(kf).c_str(),
+                jnum(bp.density).c_str(), jnum(e0[0] / A).c_str(), jnum((e0[0] + e_mbpt2) / A).c_str(),
+                jnum((e0[0] + e_ccd[0]) / A).c_str(),
+                triples ? jnum((e0[0] + e_ccd[0] + et[0]) / A).c_str() : "null", iterations);
   }
   if (!a.save.empty()) {
     check(ccx_get_t2_all(E, t2.data()), "ccx_get_t2_all");

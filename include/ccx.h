@@ -297,6 +297,27 @@ typedef struct {
 
 /* ccd_iter loop, ccm_iter.f90:67-133 */
 int ccx_ccd_iter(ccx_engine *e, const ccx_iter_opts *opt, ccx_iter_result *res);
+
+/* One residual evaluation of the last ccx_ccd_iter (or ccx_ccd_iter_batch) on an engine:
+ * the structured form of the per-iteration energy lines the reference writes from
+ * ccd_iter (ccm_iter.f90:67-133). */
+typedef struct {
+  int32_t iteration;         /* 1-based */
+  int32_t kind;              /* CCX_ITER_* */
+  double energy[2];          /* correlation energy after this iteration's update */
+  double de;                 /* Re of the energy change since the previous record (the first: since MP2) */
+  double res_norm;           /* ||R - D T|| of this residual (mixed kind: of the mixed residual) */
+  double ms;                 /* host wall-clock milliseconds since the previous record; the loop
+                                synchronises once an iteration, so this is the iteration's time */
+  double term_ms[9];         /* profiling on: device ms of this iteration per residual term, in the
+                                slots [0]..[8] of ccx_engine_timers; profiling off: 0 */
+} ccx_iter_record;
+#define CCX_ITER_REFERENCE 0   /* a step of the reference loop (|dE| test) */
+#define CCX_ITER_FP64 1        /* an FP64 residual of the standard loop (or a mixed-precision re-base) */
+#define CCX_ITER_MIXED 2       /* a mixed-precision (tensor-core correction) residual */
+/* The records of the last solve: *n receives their count, and the first
+ * min(*n, capacity) are copied to records (which may be NULL when capacity is 0). */
+int ccx_engine_iter_log(const ccx_engine *e, int32_t capacity, ccx_iter_record *records, int32_t *n);
 /* The one-time device set-up that the first ccx_ccd_iter with these options would do
  * (tensor-core operand tiles, digit planes of the interaction, DIIS history), without
  * solving, so that a host can keep set-up out of a timed or latency-critical solve.
@@ -445,7 +466,8 @@ int ccx_engine_timers(const ccx_engine *e, double ms[10]);
  * cores), [8] ring corrections dR_ph, one launch (tensor cores),
  * [9] operand splits, [10] pp-ladder, [11] I4 and [12] ring at a re-base as digit products
  * (tensor cores), [13] I7 of a mixed residual from the X entries it reads (FP64 column
- * dots), [14] .. [15] unused */
+ * dots), [14] X = V_hhpp'^T T' and [15] the hh-ladder base term T' I9' at a re-base as
+ * digit products (tensor cores) */
 int ccx_engine_kernel_timers(const ccx_engine *e, double ms[16], int64_t launches[16]);
 
 #ifdef __cplusplus
