@@ -101,7 +101,7 @@ def test_pnm66_nmax4_sizes(ccx):
     npp = sorted(d[1] for d in dims)
     assert (nh[0], nh[-1]) == (4, 132)
     assert (npp[0], npp[-1]) == (1112, 2784)
-    assert c["amps"] == 8065536 or abs(c["amps"] - 8.07e6) / 8.07e6 < 0.01
+    assert c["amps"] == 8067968 == sum(h * p for h, p in dims)
     assert c["ph_phhp"] == 1816
 
 
