@@ -6,7 +6,7 @@
  * Each routine cites the reference lines it follows.  Parity status: UNPINNED
  * (no golden vectors exist in the reference and it cannot be built here).
  *
- * Build: see oracle/Makefile (gcc -O2 -fopenmp -ffp-contract=off).
+ * Build: see oracle/Makefile (gcc -O3 -fopenmp -ffp-contract=off).
  */
 #include "ccd_oracle.h"
 
@@ -1008,19 +1008,73 @@ void ocl_mp2(ocl_t *o) {
   }
 }
 
-/* column-major C(m x n) = beta*C + alpha*A(m x k) B(k x n), deterministic order */
-static void zgemm_nn(int m, int n, int k, zd alpha, const zd *A, int lda, const zd *B, int ldb,
-                     zd *C, int ldc) {
-#pragma omp parallel for schedule(static) if ((double)m * n * k > 1e6)
-  for (int j = 0; j < n; j++) {
-    zd *c = C + (size_t)ldc * j;
-    for (int l = 0; l < k; l++) {
-      zd t = alpha * B[l + (size_t)ldb * j];
+/* One column-major product C(m x n) += alpha A(m x k) B(k x n) of a batch (the
+ * per-channel ZGEMM calls of the reference).  The jobs of one batch write disjoint C. */
+typedef struct {
+  int m, n, k, lda, ldb, ldc;
+  zd alpha;
+  const zd *A, *B;
+  zd *C;
+} zjob;
+
+/* Tiles of ZT_MB rows x ZT_NB columns.  Every C element takes its k products in
+ * ascending l, one complex multiply-add each -- (tr ar - ti ai) + i (tr ai + ti ar)
+ * added to C, products with a zero B entry skipped -- so the result is the one of the
+ * plain loop over l and depends neither on the tiling nor on the number of threads.  The
+ * tile's C is held split into real and imaginary rows, which the compiler vectorises,
+ * and each A column segment is read once for ZT_NB columns. */
+#define ZT_MB 128
+#define ZT_NB 16
+static void ztile(const zjob *g, int i0, int j0) {
+  const int ni = g->m - i0 < ZT_MB ? g->m - i0 : ZT_MB, nj = g->n - j0 < ZT_NB ? g->n - j0 : ZT_NB;
+  double cr[ZT_NB][ZT_MB], ci[ZT_NB][ZT_MB], ar[ZT_MB], ai[ZT_MB];
+  for (int jj = 0; jj < nj; jj++) {
+    const zd *c = g->C + (size_t)g->ldc * (j0 + jj) + i0;
+    for (int i = 0; i < ni; i++) { cr[jj][i] = creal(c[i]); ci[jj][i] = cimag(c[i]); }
+  }
+  for (int l = 0; l < g->k; l++) {
+    const zd *a = g->A + (size_t)g->lda * l + i0;
+    for (int i = 0; i < ni; i++) { ar[i] = creal(a[i]); ai[i] = cimag(a[i]); }
+    for (int jj = 0; jj < nj; jj++) {
+      const zd t = g->alpha * g->B[l + (size_t)g->ldb * (j0 + jj)];
       if (t == 0.0) continue;
-      const zd *a = A + (size_t)lda * l;
-      for (int i = 0; i < m; i++) c[i] += t * a[i];
+      const double tr = creal(t), ti = cimag(t);
+      double *xr = cr[jj], *xi = ci[jj];
+      for (int i = 0; i < ni; i++) {
+        xr[i] += tr * ar[i] - ti * ai[i];
+        xi[i] += tr * ai[i] + ti * ar[i];
+      }
     }
   }
+  for (int jj = 0; jj < nj; jj++) {
+    zd *c = g->C + (size_t)g->ldc * (j0 + jj) + i0;
+    for (int i = 0; i < ni; i++) c[i] = CMPLX(cr[jj][i], ci[jj][i]);
+  }
+}
+
+/* the tiles of all jobs of a batch over the threads */
+static void zgemm_batch(const zjob *g, int njobs) {
+  long *first = (long *)xcalloc((size_t)njobs + 1, sizeof(long));
+  for (int j = 0; j < njobs; j++) {
+    long nt = 0;
+    if (g[j].m > 0 && g[j].n > 0 && g[j].k > 0)
+      nt = (long)((g[j].m + ZT_MB - 1) / ZT_MB) * ((g[j].n + ZT_NB - 1) / ZT_NB);
+    first[j + 1] = first[j] + nt;
+  }
+  const long total = first[njobs];
+#pragma omp parallel for schedule(dynamic, 1)
+  for (long t = 0; t < total; t++) {
+    int lo = 0, hi = njobs;  /* the job with first[j] <= t < first[j + 1] */
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) / 2;
+      if (first[mid] <= t) lo = mid;
+      else hi = mid;
+    }
+    const zjob *q = &g[lo];
+    const long u = t - first[lo], nbi = (q->m + ZT_MB - 1) / ZT_MB;
+    ztile(q, (int)(u % nbi) * ZT_MB, (int)(u / nbi) * ZT_NB);
+  }
+  free(first);
 }
 
 /* ------------------------------------------------------------------ */
@@ -1032,7 +1086,8 @@ static inline int pair_channel3(const ocl_t *o, int p, int q) {
 }
 
 static void gather_tph(ocl_t *o) {
-  /* ccm_t2_eqn.f90:37-62 */
+  /* ccm_t2_eqn.f90:37-62; each channel writes its own block */
+#pragma omp parallel for schedule(dynamic, 4)
   for (int ch = 0; ch < o->nchph[1]; ch++) {
     plist *B = &o->P1[1][ch], *K = &o->P2[1][ch];
     zd *Tp = o->Tph[ch];
@@ -1113,13 +1168,16 @@ void ocl_t2_intermediate(ocl_t *o) {
   for (int i = 0; i < A; i++) { o->d2ij[i] = I7(o, i, i); I7(o, i, i) = 0.0; }
   for (int a = A; a < ns; a++) { o->d2ab[a - A] = I6(o, a, a); I6(o, a, a) = 0.0; }
   /* R = conj(V^T), :106-138 */
+#pragma omp parallel for schedule(dynamic, 4)
   for (int ch = 0; ch < o->nch[3]; ch++) {
     plist *H = &o->L1[3][ch], *P = &o->L2[3][ch];
     for (int bra = 0; bra < P->n; bra++)
       for (int ket = 0; ket < H->n; ket++)
         o->R[ch][bra + (size_t)P->n * ket] = conj(o->V_hhpp[ch][ket + (size_t)H->n * bra]);
   }
-  /* I6 / I7 one-body terms, :144-211 */
+  /* I6 / I7 one-body terms, :144-211; each channel updates its own block, in the order of
+   * the serial loop */
+#pragma omp parallel for schedule(dynamic, 4)
   for (int ch = 0; ch < o->nch[3]; ch++) {
     plist *H = &o->L1[3][ch], *P = &o->L2[3][ch];
     zd *R = o->R[ch];
@@ -1160,30 +1218,39 @@ void ocl_t2_intermediate(ocl_t *o) {
     int n = o->L1[1][c1].n;
     I9[c1] = (zd *)xcalloc((size_t)n * n, sizeof(zd));
   }
+  /* one job per channel; hhpp and hhhh channels pair one to one, so the jobs write
+   * disjoint I9 blocks (and below, disjoint R blocks) */
+  zjob *jobs = (zjob *)xcalloc((size_t)o->nch[3] + (size_t)o->nchph[2] + 1, sizeof(zjob));
+  int nj = 0;
   for (int ch = 0; ch < o->nch[3]; ch++) {
     int *q = o->qn[3] + 4 * ch;
     int c1 = locate(o, 1, q[0], q[1], q[2], q[3]);
     if (!c1) continue;
     int nh = o->L1[3][ch].n, np = o->L2[3][ch].n;
-    zgemm_nn(nh, nh, np, 0.5, o->V_hhpp[ch], nh, o->T[ch], np, I9[c1 - 1], nh);
+    jobs[nj++] = (zjob){nh, nh, np, nh, np, nh, 0.5, o->V_hhpp[ch], o->T[ch], I9[c1 - 1]};
   }
+  zgemm_batch(jobs, nj);
   for (int c1 = 0; c1 < o->nch[1]; c1++) {
     size_t n = (size_t)o->L1[1][c1].n * o->L1[1][c1].n;
     for (size_t x = 0; x < n; x++) I9[c1][x] += o->V_hhhh[c1][x];
   }
   /* pp-ladder R += 1/2 V_pppp T, :568-606 */
+  nj = 0;
   for (int ch = 0; ch < o->nch[3]; ch++) {
     int nh = o->L1[3][ch].n, np = o->L2[3][ch].n;
-    zgemm_nn(np, nh, np, 0.5, o->V_pppp[ch], np, o->T[ch], np, o->R[ch], np);
+    jobs[nj++] = (zjob){np, nh, np, np, np, np, 0.5, o->V_pppp[ch], o->T[ch], o->R[ch]};
   }
+  zgemm_batch(jobs, nj);
   /* hh-ladder R += 1/2 T I9, :613-645 */
+  nj = 0;
   for (int ch = 0; ch < o->nch[3]; ch++) {
     int *q = o->qn[3] + 4 * ch;
     int c1 = locate(o, 1, q[0], q[1], q[2], q[3]);
     if (!c1) continue;
     int nh = o->L1[3][ch].n, np = o->L2[3][ch].n;
-    zgemm_nn(np, nh, nh, 0.5, o->T[ch], np, I9[c1 - 1], nh, o->R[ch], np);
+    jobs[nj++] = (zjob){np, nh, nh, np, nh, np, 0.5, o->T[ch], I9[c1 - 1], o->R[ch]};
   }
+  zgemm_batch(jobs, nj);
   for (int c1 = 0; c1 < o->nch[1]; c1++) free(I9[c1]);
   free(I9);
   /* I4_ph = 1/2 amat T_ph - V_hphp, :654-780 */
@@ -1193,6 +1260,9 @@ void ocl_t2_intermediate(ocl_t *o) {
     int n = o->P1[2][ch].n;
     I4[ch] = (zd *)xcalloc((size_t)n * n, sizeof(zd));
   }
+  /* the amat blocks, one per channel, then one job per channel writing its own I4 */
+  zd **amats = (zd **)xcalloc(nhp, sizeof(zd *));
+#pragma omp parallel for schedule(dynamic, 4)
   for (int ch = 0; ch < nhp; ch++) {
     int *q = o->qnph[2] + 4 * ch;
     int c1 = locate_ph(o, 1, q[0], q[1], q[2], q[3]);
@@ -1211,10 +1281,21 @@ void ocl_t2_intermediate(ocl_t *o) {
         amat[bra + (size_t)B->n * ket] = o->V_hhpp[c2 - 1][(bra2 - 1) + (size_t)o->L1[3][c2 - 1].n * (ket2 - 1)];
       }
     }
-    int n1 = B->n, n3 = K->n, n2 = o->P2[1][c1 - 1].n;
-    zgemm_nn(n1, n2, n3, 0.5, amat, n1, o->Tph[c1 - 1], n3, I4[ch], n1);
-    free(amat);
+    amats[ch] = amat;
   }
+  nj = 0;
+  for (int ch = 0; ch < nhp; ch++) {
+    if (!amats[ch]) continue;
+    int *q = o->qnph[2] + 4 * ch;
+    int c1 = locate_ph(o, 1, q[0], q[1], q[2], q[3]);
+    int c3 = locate_ph(o, 3, q[0], q[1], q[2], q[3]);
+    int n1 = o->P1[3][c3 - 1].n, n3 = o->P2[3][c3 - 1].n, n2 = o->P2[1][c1 - 1].n;
+    jobs[nj++] = (zjob){n1, n2, n3, n1, n3, n1, 0.5, amats[ch], o->Tph[c1 - 1], I4[ch]};
+  }
+  zgemm_batch(jobs, nj);
+  for (int ch = 0; ch < nhp; ch++) free(amats[ch]);
+  free(amats);
+#pragma omp parallel for schedule(dynamic, 4)
   for (int ch = 0; ch < nhp; ch++) {
     plist *L = &o->P1[2][ch];
     for (int ket = 0; ket < L->n; ket++) {
@@ -1230,14 +1311,17 @@ void ocl_t2_intermediate(ocl_t *o) {
       }
     }
   }
-  /* ph-ring R_ph += T_ph I4, :800-829 */
+  /* ph-ring R_ph += T_ph I4, :800-829; hp and ph channels pair one to one */
+  nj = 0;
   for (int ch = 0; ch < nhp; ch++) {
     int *q = o->qnph[2] + 4 * ch;
     int c2 = locate_ph(o, 1, q[0], q[1], q[2], q[3]);
     if (!c2) continue;
     int n1 = o->P1[1][c2 - 1].n, n3 = o->P2[1][c2 - 1].n, n2 = o->P1[2][ch].n;
-    zgemm_nn(n1, n2, n3, 1.0, o->Tph[c2 - 1], n1, I4[ch], n3, o->Rph[c2 - 1], n1);
+    jobs[nj++] = (zjob){n1, n2, n3, n1, n3, n1, 1.0, o->Tph[c2 - 1], I4[ch], o->Rph[c2 - 1]};
   }
+  zgemm_batch(jobs, nj);
+  free(jobs);
   for (int ch = 0; ch < nhp; ch++) free(I4[ch]);
   free(I4);
   /* antisymmetrizing scatter, :840-892 */
