@@ -1110,30 +1110,64 @@ static void setup_i6i7(ocl_t *o) {
   int ns = o->ns, A = o->A;
   memset(o->I6, 0, sizeof(zd) * (size_t)ns * ns);
   memset(o->I7, 0, sizeof(zd) * (size_t)A * A);
-  /* I7(k,i) = 1/2 sum V(kl,cd) T(cd,il), ccm_t2_eqn.f90:1352-1392 */
-  for (int ch = 0; ch < o->nch[3]; ch++) {
-    plist *H = &o->L1[3][ch], *P = &o->L2[3][ch];
-    const zd *V = o->V_hhpp[ch], *T = o->T[ch];
-    for (int ket = 0; ket < P->n; ket++) {
-      for (int bra = 0; bra < H->n; bra++) {
-        int i = H->p[bra], l = H->q[bra];
-        for (int szc = -1; szc <= 1; szc += 2) {
-          int k = orbitof(o, o->nx[i], o->ny[i], o->nz[i], szc, o->tz[i]);
-          if (k < 0 || k >= A) continue;
-          int bra2 = o->hh_hhpp[PIDX(o, k, l)];
-          if (bra2 == 0) continue;
-          zd gmat = V[(bra2 - 1) + (size_t)H->n * ket];
-          o->I7[k + (size_t)A * i] += 0.5 * gmat * T[ket + (size_t)P->n * bra];
+  /* I7(k,i) = 1/2 sum V(kl,cd) T(cd,il), ccm_t2_eqn.f90:1352-1392.  Column i of I7 only
+   * takes terms of the bras (i,l); each thread sums whole columns, visiting channels,
+   * kets, bras and spins in the order of the reference loop, so every entry sees the
+   * same additions in the same order. */
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int i = 0; i < A; i++) {
+    int *mine = (int *)xcalloc((size_t)A, sizeof(int));
+    for (int ch = 0; ch < o->nch[3]; ch++) {
+      plist *H = &o->L1[3][ch], *P = &o->L2[3][ch];
+      int nb = 0;
+      for (int bra = 0; bra < H->n; bra++)
+        if (H->p[bra] == i) mine[nb++] = bra;
+      if (!nb) continue;
+      const zd *V = o->V_hhpp[ch], *T = o->T[ch];
+      for (int ket = 0; ket < P->n; ket++) {
+        for (int x = 0; x < nb; x++) {
+          int bra = mine[x], l = H->q[bra];
+          for (int szc = -1; szc <= 1; szc += 2) {
+            int k = orbitof(o, o->nx[i], o->ny[i], o->nz[i], szc, o->tz[i]);
+            if (k < 0 || k >= A) continue;
+            int bra2 = o->hh_hhpp[PIDX(o, k, l)];
+            if (bra2 == 0) continue;
+            zd gmat = V[(bra2 - 1) + (size_t)H->n * ket];
+            o->I7[k + (size_t)A * i] += 0.5 * gmat * T[ket + (size_t)P->n * bra];
+          }
         }
       }
     }
+    free(mine);
   }
-  /* I6(a,c) = -1/2 sum V(kl,dc) T(da,kl), ccm_t2_eqn.f90:1399-1441 */
+  /* I6(a,c) = -1/2 sum V(kl,dc) T(da,kl), ccm_t2_eqn.f90:1399-1441.  Row a of I6 only
+   * takes terms of the bras (d,a): those are listed per a, in the reference loop's
+   * (channel, bra) order, and each thread sums whole rows in that order. */
+  const int np_all = ns - A;
+  int64_t *off = (int64_t *)xcalloc((size_t)np_all + 1, sizeof(int64_t));
   for (int ch = 0; ch < o->nch[3]; ch++) {
-    plist *H = &o->L1[3][ch], *P = &o->L2[3][ch];
-    const zd *V = o->V_hhpp[ch], *T = o->T[ch];
+    plist *P = &o->L2[3][ch];
+    for (int bra = 0; bra < P->n; bra++) off[P->q[bra] - A + 1]++;
+  }
+  for (int a = 0; a < np_all; a++) off[a + 1] += off[a];
+  int64_t *fill = (int64_t *)xcalloc((size_t)np_all, sizeof(int64_t));
+  int *lch = (int *)xcalloc((size_t)off[np_all], sizeof(int)), *lbra = (int *)xcalloc((size_t)off[np_all], sizeof(int));
+  for (int ch = 0; ch < o->nch[3]; ch++) {
+    plist *P = &o->L2[3][ch];
     for (int bra = 0; bra < P->n; bra++) {
-      int d = P->p[bra], a = P->q[bra];
+      int64_t x = off[P->q[bra] - A] + fill[P->q[bra] - A]++;
+      lch[x] = ch;
+      lbra[x] = bra;
+    }
+  }
+  free(fill);
+#pragma omp parallel for schedule(dynamic, 4)
+  for (int a = A; a < ns; a++) {
+    for (int64_t x = off[a - A]; x < off[a - A + 1]; x++) {
+      const int ch = lch[x], bra = lbra[x];
+      plist *H = &o->L1[3][ch], *P = &o->L2[3][ch];
+      const zd *V = o->V_hhpp[ch], *T = o->T[ch];
+      int d = P->p[bra];
       for (int ket = 0; ket < H->n; ket++) {
         zd t2 = T[bra + (size_t)P->n * ket];
         for (int szc = -1; szc <= 1; szc += 2) {
@@ -1147,6 +1181,9 @@ static void setup_i6i7(ocl_t *o) {
       }
     }
   }
+  free(off);
+  free(lch);
+  free(lbra);
   /* add the Fock blocks, ccm_t2_eqn.f90:1507-1510 */
   for (int i = 0; i < A; i++)
     for (int k = 0; k < A; k++) o->I7[k + (size_t)A * i] += FOCK(o, k, i);
@@ -1155,6 +1192,65 @@ static void setup_i6i7(ocl_t *o) {
 }
 #define I6(o, a, c) ((o)->I6[(size_t)(a) + (size_t)(o)->ns * (c)])
 #define I7(o, k, i) ((o)->I7[(size_t)(k) + (size_t)(o)->A * (i)])
+
+/* The antisymmetrizing scatter R(ab,ij) += Rph(ai,jb) - Rph(bi,ja) - Rph(aj,ib) +
+ * Rph(bj,ia), ccm_t2_eqn.f90:840-892.  The reference pushes every Rph element (loop
+ * over ph channels, kets (j,b), bras (a,i)) into its four R entries.  Here every R
+ * entry pulls its (up to) four Rph elements and adds them in the order that loop visits
+ * them, so each entry sees the same additions in the same order, and the hhpp
+ * channels run in parallel. */
+typedef struct {
+  int64_t key;  /* (ph channel, ket, bra): the push loop's visiting order */
+  zd v;
+  int sign;
+} rph_src;
+
+static inline void rph_pull(const ocl_t *o, int p, int h, int h2, int p2, int sign, rph_src *s, int *n) {
+  const int cb = locate_ph(o, 1, (o->tz[p] - o->tz[h]) / 2, o->nx[p] - o->nx[h], o->ny[p] - o->ny[h],
+                           o->nz[p] - o->nz[h]);
+  if (!cb) return;
+  const int ck = locate_ph(o, 1, (o->tz[h2] - o->tz[p2]) / 2, o->nx[h2] - o->nx[p2], o->ny[h2] - o->ny[p2],
+                           o->nz[h2] - o->nz[p2]);
+  if (ck != cb) return;
+  const int ib = o->ph_ph_phhp[PIDX(o, p, h)], ik = o->hp_ph_phhp[PIDX(o, h2, p2)];
+  if (!ib || !ik) return;
+  rph_src *x = &s[(*n)++];
+  x->key = ((int64_t)cb << 42) | ((int64_t)(ik - 1) << 21) | (int64_t)(ib - 1);
+  x->v = o->Rph[cb - 1][(ib - 1) + (size_t)o->P1[1][cb - 1].n * (ik - 1)];
+  x->sign = sign;
+}
+
+static void scatter_rph(ocl_t *o) {
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int c1 = 0; c1 < o->nch[3]; c1++) {
+    plist *H = &o->L1[3][c1], *P = &o->L2[3][c1];
+    zd *R = o->R[c1];
+    const size_t ld = P->n;
+    for (int ket = 0; ket < H->n; ket++) {
+      const int i = H->p[ket], j = H->q[ket];
+      for (int bra = 0; bra < P->n; bra++) {
+        const int a = P->p[bra], b = P->q[bra];
+        rph_src s[4];
+        int n = 0;
+        rph_pull(o, a, i, j, b, +1, s, &n);
+        rph_pull(o, b, i, j, a, -1, s, &n);
+        rph_pull(o, a, j, i, b, -1, s, &n);
+        rph_pull(o, b, j, i, a, +1, s, &n);
+        for (int x = 1; x < n; x++)
+          for (int y = x; y > 0 && s[y - 1].key > s[y].key; y--) {
+            rph_src t = s[y];
+            s[y] = s[y - 1];
+            s[y - 1] = t;
+          }
+        zd *r = &R[bra + ld * ket];
+        for (int x = 0; x < n; x++) {
+          if (s[x].sign > 0) *r += s[x].v;
+          else *r -= s[x].v;
+        }
+      }
+    }
+  }
+}
 
 void ocl_t2_intermediate(ocl_t *o) {
   int A = o->A, ns = o->ns;
@@ -1324,32 +1420,7 @@ void ocl_t2_intermediate(ocl_t *o) {
   free(jobs);
   for (int ch = 0; ch < nhp; ch++) free(I4[ch]);
   free(I4);
-  /* antisymmetrizing scatter, :840-892 */
-  for (int ch = 0; ch < nhp; ch++) {
-    int *q = o->qnph[2] + 4 * ch;
-    int c2 = locate_ph(o, 1, q[0], q[1], q[2], q[3]);
-    if (!c2) continue;
-    plist *B = &o->P1[1][c2 - 1], *K = &o->P2[1][c2 - 1];
-    for (int ket = 0; ket < K->n; ket++) {
-      int j = K->p[ket], b = K->q[ket];
-      for (int bra = 0; bra < B->n; bra++) {
-        int a = B->p[bra], i = B->q[bra];
-        int c1 = pair_channel3(o, i, j);
-        if (!c1) continue;
-        int ket2 = o->hh_hhpp[PIDX(o, i, j)], bra2 = o->pp_hhpp[PIDX(o, a, b)];
-        if (bra2 * ket2 == 0) continue;
-        zd s2 = o->Rph[c2 - 1][bra + (size_t)B->n * ket];
-        zd *R = o->R[c1 - 1];
-        size_t ld = o->L2[3][c1 - 1].n;
-        int bra3 = o->pp_hhpp[PIDX(o, b, a)];
-        int ket3 = o->hh_hhpp[PIDX(o, j, i)];
-        R[(bra2 - 1) + ld * (ket2 - 1)] += s2;
-        R[(bra3 - 1) + ld * (ket2 - 1)] -= s2;
-        R[(bra2 - 1) + ld * (ket3 - 1)] -= s2;
-        R[(bra3 - 1) + ld * (ket3 - 1)] += s2;
-      }
-    }
-  }
+  scatter_rph(o);
 }
 
 /* ccd_energy_save, ccm_energy.f90:4-71 */
