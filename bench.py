@@ -163,7 +163,7 @@ def oracle_sample(wl: dict, iters: int, warm: int):
 
 # Oracle iterations per timed step and warm-up of the reference arm are capped so that
 # the whole run stays within a few minutes on the larger lattices (one SNM 132 nmax=4
-# iteration takes about 20 s on 16 cores, after about 40 s of V set-up).
+# iteration takes about 8 s on 16 Grace cores, after about 40 s of V set-up).
 REFERENCE_ARM_CAP = {"snm132n4": (3, 1), "snm132n3": (5, 1)}
 
 
