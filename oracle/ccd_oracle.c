@@ -1441,16 +1441,24 @@ static inline zd denom_of(const ocl_t *o, int a, int b, int i, int j) {
 }
 
 double ocl_residual_norm(const ocl_t *o) {
-  double s = 0.0;
+  /* per-channel sums in parallel, added in channel order: the same value at any thread
+   * count */
+  double *part = (double *)xcalloc((size_t)o->nch[3] + 1, sizeof(double));
+#pragma omp parallel for schedule(dynamic, 4)
   for (int ch = 0; ch < o->nch[3]; ch++) {
     plist *H = &o->L1[3][ch], *P = &o->L2[3][ch];
+    double s = 0.0;
     for (int bra = 0; bra < P->n; bra++)
       for (int ket = 0; ket < H->n; ket++) {
         zd d = denom_of(o, P->p[bra], P->q[bra], H->p[ket], H->q[ket]);
         zd r = o->R[ch][bra + (size_t)P->n * ket] - d * o->T[ch][bra + (size_t)P->n * ket];
         s += creal(r) * creal(r) + cimag(r) * cimag(r);
       }
+    part[ch] = s;
   }
+  double s = 0.0;
+  for (int ch = 0; ch < o->nch[3]; ch++) s += part[ch];
+  free(part);
   return sqrt(s);
 }
 

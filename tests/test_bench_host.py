@@ -67,3 +67,20 @@ def test_replica_twists_are_distinct():
     th = [bench.replica_theta(r) for r in range(8)]
     assert th[0] == (0.0, 0.0, 0.0)
     assert len({tuple(t) for t in th}) == 8
+
+
+def test_reference_arm_times_a_whole_solve():
+    """The reference arm on the PNM 14 lattice: one whole reference-mode solve of the
+    oracle from MP2 (it fits the full-solve budget), reported with the contract's keys."""
+    import json
+    import subprocess
+    out = subprocess.run([sys.executable, os.path.join(os.path.dirname(bench.__file__), "bench.py"), "--impl",
+                          "reference", "--workload", "pnm14", "--steps", "1", "--warmup", "3"],
+                         capture_output=True, text=True, timeout=600, check=True).stdout
+    line = json.loads([x for x in out.splitlines() if x.startswith("{")][-1])
+    assert line["impl"] == "reference" and line["unit"] == "s" and line["higher_is_better"] is False
+    assert line["config"]["sample_unit"] == "one whole reference-mode solve"
+    assert line["config"]["iterations"] == bench.REFERENCE_ITERATIONS["pnm14"]
+    assert line["value"] > 0 and line["value"] == line["cpu_baseline"]["value"] == line["e2e"]["value"]
+    assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
