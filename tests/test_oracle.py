@@ -106,16 +106,24 @@ def test_mp2_closed_form_and_antisymmetry(O):
 
 
 def test_thread_count_invariance(O):
-    code = ("import sys; sys.path.insert(0, %r); import oracle as O; o = O.Oracle(O.Config(nmax=2, A=14, rho=0.08)); "
-            "o.mp2(); r = o.ccd_iter(mode=O.MODE_REFERENCE); print(repr(r['e_ccd'].real), o.triples().real)"
+    # the PNM 14 reference solve and (T), and every residual block of a complex SNM 28
+    # chiral-like lattice (MP2 amplitudes) hashed bit for bit
+    code = ("import sys, hashlib; sys.path.insert(0, %r); import oracle as O; import numpy as np; "
+            "o = O.Oracle(O.Config(nmax=2, A=14, rho=0.08)); "
+            "o.mp2(); r = o.ccd_iter(mode=O.MODE_REFERENCE); print(repr(r['e_ccd'].real), o.triples().real); "
+            "s = O.Oracle(O.Config(nmax=2, A=28, rho=0.16, snm=True, potential=O.POT_CHIRAL_LIKE)); "
+            "s.mp2(); s.t2_intermediate(); "
+            "print(hashlib.sha1(b''.join(np.ascontiguousarray(s.r2(c)).tobytes() "
+            "for c in range(s.n_channels(3)))).hexdigest())"
             % os.path.join(os.path.dirname(HERE), "oracle"))
     outs = []
     for nt in ("1", "4"):
         env = dict(os.environ, OMP_NUM_THREADS=nt)
         outs.append(subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True,
                                    check=True).stdout.split())
-    assert outs[0][0] == outs[1][0]  # the residual loops have a fixed order
+    assert outs[0][0] == outs[1][0]  # each output element takes its terms in a fixed order
     assert abs(float(outs[0][1]) - float(outs[1][1])) <= 1e-14 * abs(float(outs[0][1]))
+    assert outs[0][2] == outs[1][2]
 
 
 def test_golden_fixtures(O):
