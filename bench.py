@@ -979,8 +979,31 @@ def run_triples(args, wl):
             "rel_dE_T_fp32_contractions": abs(out["fp64"]["triples"]["fp32"]["E_T_MeV"] - ref) / abs(ref),
             "rel_dE_T_mixed_ccd_fp32_contractions": abs(out["mixed"]["triples"]["fp32"]["E_T_MeV"] - ref) / abs(ref),
             "triples_pairs_note": "E(T) is summed over every (abc, ijk) pair of the triple channels"}
+    if args.triples_cpu_s > 0:
+        line["cpu_baseline"] = triples_cpu_sample(wl, args.triples_cpu_s)
     print(json.dumps(line), flush=True)
     return 0
+
+
+def triples_cpu_sample(wl: dict, budget_s: float) -> dict:
+    """Seconds of the oracle's pert_triples2 (the reference algorithm, complex<double>) on
+    the whole lattice on all host cores, extrapolated by (abc, ijk) pairs from every k-th
+    triple channel, k chosen from a probe so that the sample takes about budget_s.  The
+    amplitudes are MP2's: the work of a pair does not depend on the values."""
+    O, o = oracle_build(wl)
+    n_ch, total = o.triples_channels(), o.triples_count()
+    probe = max(1, n_ch // 64)
+    t = time.perf_counter()
+    _, p = o.triples_sample(0, probe)
+    rate = p / max(time.perf_counter() - t, 1e-6)
+    stride = max(1, min(n_ch, int(total / max(rate * budget_s, 1.0))))
+    t = time.perf_counter()
+    _, pairs = o.triples_sample(stride // 2, stride)
+    secs = time.perf_counter() - t
+    value = secs * total / max(pairs, 1)
+    return {"value": value, "unit": "s", "cores": O.num_threads(), "kind": "port",
+            "sample": (f"(T) of the oracle over every {stride}-th of {n_ch} triple channels ({pairs} of {total} "
+                       f"(abc, ijk) pairs, {secs:.1f} s), extrapolated by pairs; MP2 amplitudes")}
 
 
 def main():
@@ -992,6 +1015,8 @@ def main():
     ap.add_argument("--workload", default="snm132n4", choices=sorted(WORKLOADS))
     ap.add_argument("--plain-steps", type=int, default=2, help="timed plain FP64 solves beside the headline form")
     ap.add_argument("--tol", type=float, default=1e-10)
+    ap.add_argument("--triples-cpu-s", type=float, default=20.0,
+                    help="--triples: seconds of oracle (T) sampled for the CPU baseline (0: none)")
     ap.add_argument("--precision", default="bf16x3", choices=sorted(PRECISIONS))
     ap.add_argument("--defect-period", type=int, default=0, help="FP64 re-base every k iterations (0: adaptive)")
     ap.add_argument("--twists", type=int, default=0,

@@ -1901,6 +1901,11 @@ static zd tb_onehole(const ocl_t *o, int a, int b, int c, int i, int j, int k) {
   return sum1;
 }
 
+int ocl_triples_channels(ocl_t *o) {
+  setup_triples(o);
+  return o->t3n;
+}
+
 int64_t ocl_triples_count(ocl_t *o) {
   setup_triples(o);
   int64_t n = 0;
@@ -1908,10 +1913,13 @@ int64_t ocl_triples_count(ocl_t *o) {
   return n;
 }
 
-void ocl_pert_triples(ocl_t *o, double *re_im) {
+/* E(T) summed over the triple channels ch0, ch0 + stride, ... (all of them: 0, 1) */
+static zd triples_channels(ocl_t *o, int ch0, int stride, int64_t *pairs) {
   setup_triples(o);
   zd et = 0.0;
-  for (int ch = 0; ch < o->t3n; ch++) {
+  int64_t np = 0;
+  for (int ch = ch0; ch < o->t3n; ch += stride) {
+    np += (int64_t)o->t3ppp_n[ch] * o->t3hhh_n[ch];
     int nk = o->t3ppp_n[ch], nb = o->t3hhh_n[ch];
     zd *part = (zd *)xcalloc(nk > 0 ? nk : 1, sizeof(zd));
 #pragma omp parallel for schedule(dynamic, 4)
@@ -1950,6 +1958,18 @@ void ocl_pert_triples(ocl_t *o, double *re_im) {
     for (int ket = 0; ket < nk; ket++) et += part[ket];
     free(part);
   }
+  if (pairs) *pairs = np;
+  return et;
+}
+
+void ocl_pert_triples(ocl_t *o, double *re_im) {
+  zd et = triples_channels(o, 0, 1, NULL);
+  re_im[0] = creal(et);
+  re_im[1] = cimag(et);
+}
+
+void ocl_pert_triples_sample(ocl_t *o, int ch0, int stride, double *re_im, int64_t *pairs) {
+  zd et = triples_channels(o, ch0 < 0 ? 0 : ch0, stride < 1 ? 1 : stride, pairs);
   re_im[0] = creal(et);
   re_im[1] = cimag(et);
 }

@@ -113,6 +113,9 @@ def lib():
         L.ocl_ccd_iter.argtypes = [vp, C.POINTER(_IterOpts), C.POINTER(_IterResult)]
         L.ocl_ccd_iter.restype = C.c_int
         L.ocl_pert_triples.argtypes = [vp, vp]
+        L.ocl_pert_triples_sample.argtypes = [vp, C.c_int, C.c_int, vp, C.POINTER(C.c_int64)]
+        L.ocl_triples_channels.argtypes = [vp]
+        L.ocl_triples_channels.restype = C.c_int
         L.ocl_triples_count.argtypes = [vp]
         L.ocl_triples_count.restype = C.c_int64
         L.ocl_num_threads.restype = C.c_int
@@ -336,6 +339,16 @@ class Oracle:
         z = np.zeros(2)
         self._L.ocl_pert_triples(self._h, _ptr(z))
         return complex(z[0], z[1])
+
+    def triples_sample(self, ch0: int, stride: int):
+        """(E(T) over the triple channels ch0, ch0 + stride, ..., their (abc, ijk) pairs)."""
+        z = np.zeros(2)
+        n = C.c_int64()
+        self._L.ocl_pert_triples_sample(self._h, int(ch0), int(stride), _ptr(z), C.byref(n))
+        return complex(z[0], z[1]), n.value
+
+    def triples_channels(self) -> int:
+        return self._L.ocl_triples_channels(self._h)
 
     def triples_count(self) -> int:
         return self._L.ocl_triples_count(self._h)

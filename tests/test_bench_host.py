@@ -84,3 +84,9 @@ def test_reference_arm_times_a_whole_solve():
     assert line["value"] > 0 and line["value"] == line["cpu_baseline"]["value"] == line["e2e"]["value"]
     assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
+
+
+def test_triples_cpu_sample():
+    s = bench.triples_cpu_sample(bench.WORKLOADS["pnm14"], 0.5)
+    assert s["unit"] == "s" and s["kind"] == "port" and s["value"] > 0 and s["cores"] >= 1
+    assert "extrapolated by pairs" in s["sample"]

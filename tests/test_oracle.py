@@ -146,3 +146,16 @@ def test_golden_fixtures(O):
             r = o.ccd_iter(mode=O.MODE_REFERENCE)
             assert r["iterations"] == case["iterations_reference"]
             assert abs(r["e_ccd"].real - case["e_ccd_reference"]) <= 1e-11 * abs(case["e_ccd_reference"])
+
+
+def test_triples_channel_samples_add_up(O):
+    """The channel-strided (T) samples the CPU baseline times: three interleaved samples
+    hold every (abc, ijk) pair once and add up to the whole E(T)."""
+    o = O.Oracle(O.Config(nmax=2, A=14, rho=0.08))
+    o.mp2()
+    o.ccd_iter(mode=O.MODE_REFERENCE)
+    full = o.triples()
+    parts = [o.triples_sample(k, 3) for k in range(3)]
+    assert sum(p for _, p in parts) == o.triples_count()
+    assert o.triples_channels() >= 3 and all(p > 0 for _, p in parts)
+    assert abs(sum(e for e, _ in parts) - full) <= 1e-12 * abs(full)
