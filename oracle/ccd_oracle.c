@@ -1913,17 +1913,18 @@ int64_t ocl_triples_count(ocl_t *o) {
   return n;
 }
 
-/* E(T) summed over the triple channels ch0, ch0 + stride, ... (all of them: 0, 1) */
-static zd triples_channels(ocl_t *o, int ch0, int stride, int64_t *pairs) {
+/* E(T) summed over the (abc) triples k0, k0 + stride, ... of every triple channel (all
+ * of them: 0, 1) */
+static zd triples_channels(ocl_t *o, int k0, int stride, int64_t *pairs) {
   setup_triples(o);
   zd et = 0.0;
   int64_t np = 0;
-  for (int ch = ch0; ch < o->t3n; ch += stride) {
-    np += (int64_t)o->t3ppp_n[ch] * o->t3hhh_n[ch];
+  for (int ch = 0; ch < o->t3n; ch++) {
     int nk = o->t3ppp_n[ch], nb = o->t3hhh_n[ch];
+    if (nk > k0) np += (int64_t)((nk - k0 + stride - 1) / stride) * nb;
     zd *part = (zd *)xcalloc(nk > 0 ? nk : 1, sizeof(zd));
 #pragma omp parallel for schedule(dynamic, 4)
-    for (int ket = 0; ket < nk; ket++) {
+    for (int ket = k0; ket < nk; ket += stride) {
       const int *abc = o->t3ppp[ch] + 3 * ket;
       int a = abc[0], b = abc[1], c = abc[2];
       zd acc = 0.0;
@@ -1968,8 +1969,8 @@ void ocl_pert_triples(ocl_t *o, double *re_im) {
   re_im[1] = cimag(et);
 }
 
-void ocl_pert_triples_sample(ocl_t *o, int ch0, int stride, double *re_im, int64_t *pairs) {
-  zd et = triples_channels(o, ch0 < 0 ? 0 : ch0, stride < 1 ? 1 : stride, pairs);
+void ocl_pert_triples_sample(ocl_t *o, int k0, int stride, double *re_im, int64_t *pairs) {
+  zd et = triples_channels(o, k0 < 0 ? 0 : k0, stride < 1 ? 1 : stride, pairs);
   re_im[0] = creal(et);
   re_im[1] = cimag(et);
 }

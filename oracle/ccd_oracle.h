@@ -121,9 +121,9 @@ int ocl_ccd_iter(ocl_t *o, const ocl_iter_opts *opt, ocl_iter_result *res);
 void ocl_pert_triples(ocl_t *o, double *re_im);  /* pert_triples2, NN only */
 int64_t ocl_triples_count(ocl_t *o);             /* number of (abc, ijk) pairs */
 int ocl_triples_channels(ocl_t *o);              /* number of triple channels */
-/* the (T) sum over the triple channels ch0, ch0 + stride, ... only, and the number of
- * (abc, ijk) pairs they hold: a bounded timing sample of pert_triples2 */
-void ocl_pert_triples_sample(ocl_t *o, int ch0, int stride, double *re_im, int64_t *pairs);
+/* the (T) sum over the (abc) triples k0, k0 + stride, ... of every triple channel only,
+ * and the number of (abc, ijk) pairs it covers: a bounded timing sample of pert_triples2 */
+void ocl_pert_triples_sample(ocl_t *o, int k0, int stride, double *re_im, int64_t *pairs);
 
 #ifdef __cplusplus
 }

@@ -340,11 +340,12 @@ class Oracle:
         self._L.ocl_pert_triples(self._h, _ptr(z))
         return complex(z[0], z[1])
 
-    def triples_sample(self, ch0: int, stride: int):
-        """(E(T) over the triple channels ch0, ch0 + stride, ..., their (abc, ijk) pairs)."""
+    def triples_sample(self, k0: int, stride: int):
+        """(E(T) over the (abc) triples k0, k0 + stride, ... of every triple channel, the
+        (abc, ijk) pairs that covers)."""
         z = np.zeros(2)
         n = C.c_int64()
-        self._L.ocl_pert_triples_sample(self._h, int(ch0), int(stride), _ptr(z), C.byref(n))
+        self._L.ocl_pert_triples_sample(self._h, int(k0), int(stride), _ptr(z), C.byref(n))
         return complex(z[0], z[1]), n.value
 
     def triples_channels(self) -> int:

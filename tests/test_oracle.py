@@ -148,9 +148,10 @@ def test_golden_fixtures(O):
             assert abs(r["e_ccd"].real - case["e_ccd_reference"]) <= 1e-11 * abs(case["e_ccd_reference"])
 
 
-def test_triples_channel_samples_add_up(O):
-    """The channel-strided (T) samples the CPU baseline times: three interleaved samples
-    hold every (abc, ijk) pair once and add up to the whole E(T)."""
+def test_triples_samples_add_up(O):
+    """The strided (T) samples the CPU baseline times (every third (abc) triple of every
+    channel): three interleaved samples hold every (abc, ijk) pair once and add up to the
+    whole E(T)."""
     o = O.Oracle(O.Config(nmax=2, A=14, rho=0.08))
     o.mp2()
     o.ccd_iter(mode=O.MODE_REFERENCE)
