@@ -197,7 +197,7 @@ def run_reference(args, wl):
     if statistics.mean(t_warm) * n_ref <= REFERENCE_FULL_SOLVE_S:
         o.mp2()
         t = time.perf_counter()
-        r = o.ccd_iter(mode=O.MODE_REFERENCE)
+        r = o.ccd_iter(mode=O.MODE_REFERENCE, max_iter=n_ref + 10)  # bounded if it stalls
         value = time.perf_counter() - t
         iters = r["iterations"]
         ms_per_step = value * 1e3
