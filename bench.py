@@ -988,21 +988,22 @@ def run_triples(args, wl):
 def triples_cpu_sample(wl: dict, budget_s: float) -> dict:
     """Seconds of the oracle's pert_triples2 (the reference algorithm, complex<double>) on
     the whole lattice on all host cores, extrapolated by (abc, ijk) pairs from every k-th
-    (abc) triple of every triple channel, k chosen from a probe so that the sample takes
-    about budget_s.  The amplitudes are MP2's: the work of a pair does not depend on the
-    values."""
+    (abc) triple of every triple channel, k refined from short samples until the sample
+    takes about budget_s.  The amplitudes are MP2's: the work of a pair does not depend
+    on the values."""
     O, o = oracle_build(wl)
     n_ch, total = o.triples_channels(), o.triples_count()
     # a short first sample; the per-channel overhead makes it look slower per pair, so the
     # stride is refined until the sample takes at least half the budget
-    stride = 4096
+    nxt = 4096
     for _ in range(4):
+        stride = nxt
         t = time.perf_counter()
         _, pairs = o.triples_sample(stride // 2, stride)
         secs = time.perf_counter() - t
         if secs >= 0.5 * budget_s or stride == 1:
             break
-        stride = max(1, int(stride * secs / budget_s))
+        nxt = max(1, int(stride * secs / budget_s))
     value = secs * total / max(pairs, 1)
     return {"value": value, "unit": "s", "cores": O.num_threads(), "kind": "port",
             "sample": (f"(T) of the oracle over every {stride}-th (abc) triple of all {n_ch} triple channels "
