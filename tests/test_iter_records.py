@@ -154,3 +154,17 @@ def test_run_json_records(ccx):
     its = [x for x in json_lines(out) if x["record"] == "iteration"]
     assert len(its) == int(fields(out)["iterations"][0])
     assert all(x["kind"] == "reference" and x["res_norm"] is None for x in its)
+
+
+def test_iter_log_argument_checks(ccx):
+    """No engine is needed to see the entry point refuse bad arguments."""
+    L = ccx.lib()
+    n = C.c_int32(-1)
+    einval = 1  # CCX_EINVAL
+    assert L.ccx_engine_iter_log(None, 0, None, C.byref(n)) == einval
+    assert "null engine" in L.ccx_last_error().decode()
+    fake = C.c_void_p(1)  # never dereferenced: the argument checks come first
+    assert L.ccx_engine_iter_log(fake, 0, None, None) == einval
+    assert L.ccx_engine_iter_log(fake, -1, None, C.byref(n)) == einval
+    assert L.ccx_engine_iter_log(fake, 4, None, C.byref(n)) == einval
+    assert "capacity" in L.ccx_last_error().decode() and n.value == -1
